@@ -1,0 +1,347 @@
+"""ORACLE — test infrastructure only; never imported by the product.
+
+ctypes front end for two CPU checkers:
+
+* ``Oracle``  — the plain-C restatement in ``oracle/zimg_oracle.c`` (built to
+  ``oracle/_build/liboracle.so``). It exists on every machine, including the GPU
+  box, because ``__graft_entry__.build()`` compiles it there.
+* ``Reference`` — zimg's own resize code compiled from the reference checkout by
+  ``oracle/Makefile`` into ``oracle/_ref/libzimgref.so`` (only where that
+  checkout exists). It pins the restatement.
+
+Also holds the graph-level parameter mapping (chroma siting, field parity,
+active region -> per-plane shift/subwidth), restated from
+src/zimg/graph/graphbuilder.cpp:65-188,331-366,769-776 and
+src/zimg/api/zimg.cpp:370-400.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+import subprocess
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "_build", "liboracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libzimgref.so")
+
+# zimg_resample_filter_e (zimg.h:374-382)
+FILTERS = {"point": 0, "bilinear": 1, "bicubic": 2, "spline16": 3, "spline36": 4, "lanczos": 5, "spline64": 6}
+T_U16, T_F32, T_F64 = 1, 3, 4
+
+
+def build(quiet: bool = True) -> None:
+    """Compile the oracle (and the reference, where its sources exist)."""
+    out = subprocess.run(["make", "-C", HERE, "-j8", "all"], capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + out.stdout[-4000:] + out.stderr[-4000:])
+    if not quiet:
+        print(out.stdout)
+
+
+def _f(kind):
+    return FILTERS[kind] if isinstance(kind, str) else int(kind)
+
+
+@dataclass
+class FilterContext:
+    width: int
+    rows: int
+    f32: np.ndarray   # [rows, width] float32
+    i16: np.ndarray   # [rows, width] int16
+    left: np.ndarray  # [rows] uint32
+    f64: np.ndarray | None = None  # [rows, width] float64 (unquantised), oracle only
+
+
+class Oracle:
+    def __init__(self, path: str = ORACLE_SO):
+        if not os.path.exists(path):
+            build()
+        self.lib = C.CDLL(path)
+        L = self.lib
+        L.orc_compute_filter.argtypes = [C.c_int, C.c_double, C.c_double, C.c_uint, C.c_uint, C.c_double, C.c_double,
+                                         C.POINTER(C.c_uint), C.POINTER(C.c_uint), C.c_void_p, C.c_void_p, C.c_void_p,
+                                         C.c_void_p]
+        L.orc_resize_plane.argtypes = [C.c_int, C.c_uint, C.c_int, C.c_double, C.c_double, C.c_uint, C.c_uint,
+                                       C.c_uint, C.c_uint, C.c_double, C.c_double, C.c_double, C.c_double,
+                                       C.c_int, C.c_int, C.c_void_p, C.c_ssize_t, C.c_void_p, C.c_ssize_t]
+        L.orc_resize_pass.argtypes = [C.c_int, C.c_uint, C.c_int, C.c_int, C.c_double, C.c_double, C.c_uint,
+                                      C.c_uint, C.c_uint, C.c_double, C.c_double, C.c_int, C.c_int, C.c_void_p,
+                                      C.c_ssize_t, C.c_void_p, C.c_ssize_t]
+        L.orc_plan_order.argtypes = [C.c_uint, C.c_uint, C.c_uint, C.c_uint, C.c_double, C.c_double, C.c_double,
+                                     C.c_double, C.POINTER(C.c_int)]
+
+    def compute_filter(self, kind, src_dim, dst_dim, shift=0.0, width=None, a=math.nan, b=math.nan) -> FilterContext:
+        width = float(src_dim if width is None else width)
+        fw, rows = C.c_uint(), C.c_uint()
+        rc = self.lib.orc_compute_filter(_f(kind), a, b, src_dim, dst_dim, shift, width, C.byref(fw), C.byref(rows),
+                                         None, None, None, None)
+        if rc:
+            raise ValueError(f"compute_filter failed ({rc})")
+        f32 = np.zeros((rows.value, fw.value), np.float32)
+        i16 = np.zeros((rows.value, fw.value), np.int16)
+        f64 = np.zeros((rows.value, fw.value), np.float64)
+        left = np.zeros(rows.value, np.uint32)
+        rc = self.lib.orc_compute_filter(_f(kind), a, b, src_dim, dst_dim, shift, width, C.byref(fw), C.byref(rows),
+                                         f32.ctypes.data, i16.ctypes.data, left.ctypes.data, f64.ctypes.data)
+        if rc:
+            raise ValueError(f"compute_filter failed ({rc})")
+        return FilterContext(fw.value, rows.value, f32, i16, left, f64)
+
+    def plan_order(self, src_w, src_h, dst_w, dst_h, shift_w=0.0, shift_h=0.0, subwidth=None, subheight=None):
+        order = (C.c_int * 2)()
+        n = self.lib.orc_plan_order(src_w, src_h, dst_w, dst_h, shift_w, shift_h,
+                                    float(src_w if subwidth is None else subwidth),
+                                    float(src_h if subheight is None else subheight), order)
+        return ["h" if order[i] else "v" for i in range(n)]
+
+    def resize_plane(self, src: np.ndarray, dst_w: int, dst_h: int, kind, a=math.nan, b=math.nan, depth=None,
+                     shift_w=0.0, shift_h=0.0, subwidth=None, subheight=None, mode="c", nthreads=1) -> np.ndarray:
+        """mode: 'c' (zimg C path: u16 exact / f32 sequential without FMA),
+        'fma' (f32 sequential with fused multiply-add), 'f64' (FP64 oracle)."""
+        src = np.ascontiguousarray(src)
+        h, w = src.shape
+        if mode == "f64":
+            t, src = T_F64, src.astype(np.float64)
+            out = np.zeros((dst_h, dst_w), np.float64)
+        elif src.dtype == np.uint16:
+            t, out = T_U16, np.zeros((dst_h, dst_w), np.uint16)
+        elif src.dtype == np.float32:
+            t, out = T_F32, np.zeros((dst_h, dst_w), np.float32)
+        else:
+            raise TypeError(src.dtype)
+        depth = (16 if t == T_U16 else 32) if depth is None else depth
+        rc = self.lib.orc_resize_plane(t, depth, _f(kind), a, b, w, h, dst_w, dst_h, shift_w, shift_h,
+                                       float(w if subwidth is None else subwidth),
+                                       float(h if subheight is None else subheight),
+                                       1 if mode == "fma" else 0, nthreads, src.ctypes.data, w, out.ctypes.data, dst_w)
+        if rc:
+            raise ValueError(f"resize failed ({rc})")
+        return out
+
+    def resize_pass(self, src: np.ndarray, horizontal: bool, dst_dim: int, kind, a=math.nan, b=math.nan, depth=None,
+                    shift=0.0, subwidth=None, mode="c", nthreads=1) -> np.ndarray:
+        src = np.ascontiguousarray(src)
+        h, w = src.shape
+        ow, oh = (dst_dim, h) if horizontal else (w, dst_dim)
+        if mode == "f64":
+            t, src = T_F64, src.astype(np.float64)
+            out = np.zeros((oh, ow), np.float64)
+        elif src.dtype == np.uint16:
+            t, out = T_U16, np.zeros((oh, ow), np.uint16)
+        else:
+            t, out = T_F32, np.zeros((oh, ow), np.float32)
+        depth = (16 if t == T_U16 else 32) if depth is None else depth
+        sub = float((w if horizontal else h) if subwidth is None else subwidth)
+        rc = self.lib.orc_resize_pass(t, depth, int(horizontal), _f(kind), a, b, w, h, dst_dim, shift, sub,
+                                      1 if mode == "fma" else 0, nthreads, src.ctypes.data, w, out.ctypes.data, ow)
+        if rc:
+            raise ValueError(f"resize failed ({rc})")
+        return out
+
+
+class Reference:
+    """zimg's own code, compiled from the reference checkout (oracle/_ref)."""
+
+    def __init__(self, path: str = REF_SO):
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        self.lib = C.CDLL(path)
+        L = self.lib
+        self.err = C.create_string_buffer(512)
+        L.ref_filter_eval.argtypes = [C.c_int, C.c_double, C.c_double, C.c_void_p, C.c_void_p, C.c_size_t,
+                                      C.POINTER(C.c_uint), C.c_char_p, C.c_size_t]
+        L.ref_compute_filter.argtypes = [C.c_int, C.c_double, C.c_double, C.c_uint, C.c_uint, C.c_double,
+                                         C.c_double, C.POINTER(C.c_uint), C.POINTER(C.c_uint), C.POINTER(C.c_uint),
+                                         C.c_void_p, C.c_void_p, C.c_void_p, C.c_char_p, C.c_size_t]
+        L.ref_plan_create.restype = C.c_void_p
+        L.ref_plan_create.argtypes = [C.c_int, C.c_uint, C.c_int, C.c_double, C.c_double, C.c_uint, C.c_uint,
+                                      C.c_uint, C.c_uint, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int,
+                                      C.c_char_p, C.c_size_t]
+        L.ref_pass_create.restype = C.c_void_p
+        L.ref_pass_create.argtypes = [C.c_int, C.c_uint, C.c_uint, C.c_int, C.c_uint, C.c_uint, C.c_int, C.c_double,
+                                      C.c_double, C.c_double, C.c_double, C.c_int, C.c_char_p, C.c_size_t]
+        L.ref_plan_free.argtypes = [C.c_void_p]
+        L.ref_plan_num_passes.argtypes = [C.c_void_p]
+        L.ref_plan_run.argtypes = [C.c_void_p, C.c_void_p, C.c_ssize_t, C.c_void_p, C.c_ssize_t, C.c_char_p,
+                                   C.c_size_t]
+
+    def _raise(self, what):
+        raise ValueError(f"{what}: {self.err.value.decode(errors='replace')}")
+
+    def filter_eval(self, kind, x, a=math.nan, b=math.nan):
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.zeros_like(x)
+        sup = C.c_uint()
+        if self.lib.ref_filter_eval(_f(kind), a, b, x.ctypes.data, y.ctypes.data, x.size, C.byref(sup), self.err, 512):
+            self._raise("filter")
+        return y, sup.value
+
+    def compute_filter(self, kind, src_dim, dst_dim, shift=0.0, width=None, a=math.nan, b=math.nan) -> FilterContext:
+        width = float(src_dim if width is None else width)
+        fw, rows, iw = C.c_uint(), C.c_uint(), C.c_uint()
+        args = (_f(kind), a, b, src_dim, dst_dim, shift, width, C.byref(fw), C.byref(rows), C.byref(iw))
+        if self.lib.ref_compute_filter(*args, None, None, None, self.err, 512):
+            self._raise("compute_filter")
+        f32 = np.zeros((rows.value, fw.value), np.float32)
+        i16 = np.zeros((rows.value, fw.value), np.int16)
+        left = np.zeros(rows.value, np.uint32)
+        if self.lib.ref_compute_filter(*args, f32.ctypes.data, i16.ctypes.data, left.ctypes.data, self.err, 512):
+            self._raise("compute_filter")
+        return FilterContext(fw.value, rows.value, f32, i16, left)
+
+    def plan(self, pixel_type, depth, kind, src_w, src_h, dst_w, dst_h, a=math.nan, b=math.nan, shift_w=0.0,
+             shift_h=0.0, subwidth=None, subheight=None, cpu=0):
+        p = self.lib.ref_plan_create(pixel_type, depth, _f(kind), a, b, src_w, src_h, dst_w, dst_h, shift_w,
+                                     shift_h, float(src_w if subwidth is None else subwidth),
+                                     float(src_h if subheight is None else subheight), cpu, self.err, 512)
+        if not p:
+            self._raise("plan")
+        return p
+
+    def run(self, plan, src: np.ndarray, out: np.ndarray):
+        """Run on whole planes. The SIMD filters want 64-byte aligned lines
+        (align.h:11-20, filtergraph.cpp:188-216), so both planes are staged in
+        aligned, padded buffers."""
+        s = aligned_plane(*src.shape, src.dtype)
+        s[...] = src
+        d = aligned_plane(*out.shape, out.dtype)
+        if self.lib.ref_plan_run(plan, s.ctypes.data, s.strides[0], d.ctypes.data, d.strides[0], self.err, 512):
+            self._raise("run")
+        out[...] = d
+
+    def free(self, plan):
+        self.lib.ref_plan_free(plan)
+
+    def resize_plane(self, src: np.ndarray, dst_w, dst_h, kind, a=math.nan, b=math.nan, depth=None, shift_w=0.0,
+                     shift_h=0.0, subwidth=None, subheight=None, cpu=0) -> np.ndarray:
+        src = np.ascontiguousarray(src)
+        h, w = src.shape
+        t = 1 if src.dtype == np.uint16 else 3
+        depth = (16 if t == 1 else 32) if depth is None else depth
+        p = self.plan(t, depth, kind, w, h, dst_w, dst_h, a, b, shift_w, shift_h, subwidth, subheight, cpu)
+        try:
+            out = np.zeros((dst_h, dst_w), src.dtype)
+            self.run(p, src, out)
+        finally:
+            self.free(p)
+        return out
+
+    def resize_pass(self, src: np.ndarray, horizontal, dst_dim, kind, a=math.nan, b=math.nan, depth=None,
+                    shift=0.0, subwidth=None, cpu=0) -> np.ndarray:
+        src = np.ascontiguousarray(src)
+        h, w = src.shape
+        t = 1 if src.dtype == np.uint16 else 3
+        depth = (16 if t == 1 else 32) if depth is None else depth
+        sub = float((w if horizontal else h) if subwidth is None else subwidth)
+        p = self.lib.ref_pass_create(int(horizontal), w, h, t, depth, dst_dim, _f(kind), a, b, shift, sub, cpu,
+                                     self.err, 512)
+        if not p:
+            self._raise("pass")
+        try:
+            ow, oh = (dst_dim, h) if horizontal else (w, dst_dim)
+            out = np.zeros((oh, ow), src.dtype)
+            self.run(p, src, out)
+        finally:
+            self.free(p)
+        return out
+
+
+def aligned_plane(h: int, w: int, dtype) -> np.ndarray:
+    """[h, w] view with a 64-byte aligned base, 64-byte multiple stride and a
+    spare line plus 256 bytes of tail padding."""
+    dtype = np.dtype(dtype)
+    stride = (w * dtype.itemsize + 63) // 64 * 64
+    raw = np.zeros(stride * (h + 1) + 64 + 256, np.uint8)
+    off = (-raw.ctypes.data) % 64
+    base = raw[off:off + stride * (h + 1)]
+    return np.lib.stride_tricks.as_strided(base.view(dtype), shape=(h, w), strides=(stride, dtype.itemsize))
+
+
+def reference_available() -> bool:
+    return os.path.exists(REF_SO)
+
+
+# ---------------------------------------------------------------------------
+# Graph-level parameter mapping (graphbuilder.cpp), restated for the checker.
+# ---------------------------------------------------------------------------
+
+def chroma_offset_w(loc_left: bool, subsampling: float) -> float:
+    """graphbuilder.cpp:65-88"""
+    return -0.5 + 0.5 * subsampling if loc_left else 0.0
+
+
+def chroma_offset_h(loc: str, subsampling: float) -> float:
+    """graphbuilder.cpp:90-110; loc in {'top','center','bottom'}"""
+    if loc == "top":
+        return -0.5 + 0.5 * subsampling
+    if loc == "bottom":
+        return 0.5 - 0.5 * subsampling
+    return 0.0
+
+
+def chroma_parity_adjustment(parity: str, offset: float) -> float:
+    """graphbuilder.cpp:112-165"""
+    if parity == "top":
+        return -0.25 + offset / 2
+    if parity == "bottom":
+        return 0.25 + offset / 2
+    return offset
+
+
+def luma_parity_offset(parity: str) -> float:
+    """graphbuilder.cpp:167-188"""
+    return -0.25 if parity == "top" else (0.25 if parity == "bottom" else 0.0)
+
+
+# zimg_chroma_location_e -> (w is LEFT, h location) (zimg.cpp:214-236)
+CHROMA_LOC = {0: (True, "center"), 1: (False, "center"), 2: (True, "top"), 3: (False, "top"),
+              4: (True, "bottom"), 5: (False, "bottom")}
+PARITY = {0: "progressive", 1: "top", 2: "bottom"}
+
+
+def plane_geometry(fmt: dict) -> list[dict]:
+    """Per-plane (width, height, active_left/top/width/height) after siting,
+    for a format dict with keys width, height, subsample_w, subsample_h, color
+    ('grey'|'yuv'|'rgb'), chroma_location, field_parity, active_region (4 floats
+    or NaN). Follows zimg.cpp:388-397 and graphbuilder.cpp:331-366."""
+    w, h = fmt["width"], fmt["height"]
+    ar = fmt.get("active_region", (math.nan,) * 4)
+    al = 0.0 if math.isnan(ar[0]) else ar[0]
+    at = 0.0 if math.isnan(ar[1]) else ar[1]
+    aw = float(w) if math.isnan(ar[2]) else ar[2]
+    ah = float(h) if math.isnan(ar[3]) else ar[3]
+    planes = [dict(width=w, height=h, left=al, top=at, aw=aw, ah=ah)]
+    color = fmt.get("color", "grey")
+    if color != "grey":
+        sw, sh = fmt.get("subsample_w", 0), fmt.get("subsample_h", 0)
+        ssw, ssh = 1.0 / (1 << sw), 1.0 / (1 << sh)
+        u = dict(width=w >> sw, height=h >> sh, left=al * ssw, top=at * ssh, aw=aw * ssw, ah=ah * ssh)
+        planes += [dict(u), dict(u)]
+    parity = PARITY[fmt.get("field_parity", 0)]
+    planes[0]["top"] -= luma_parity_offset(parity)
+    if color != "grey":
+        loc_left, loc_h = CHROMA_LOC[fmt.get("chroma_location", 0)]
+        subscale_w = planes[1]["width"] / planes[0]["width"]
+        subscale_h = planes[1]["height"] / planes[0]["height"]
+        off_w = chroma_offset_w(loc_left, subscale_w)
+        off_h = chroma_parity_adjustment(parity, chroma_offset_h(loc_h, subscale_h))
+        for p in (1, 2):
+            planes[p]["left"] -= off_w
+            planes[p]["top"] -= off_h
+    return planes
+
+
+def resize_params(src_plane: dict, dst_plane: dict) -> dict:
+    """graphbuilder.cpp:769-776"""
+    scale_w = dst_plane["aw"] / src_plane["aw"]
+    scale_h = dst_plane["ah"] / src_plane["ah"]
+    return dict(src_w=src_plane["width"], src_h=src_plane["height"], dst_w=dst_plane["width"],
+                dst_h=dst_plane["height"],
+                shift_w=src_plane["left"] - dst_plane["left"] / scale_w,
+                shift_h=src_plane["top"] - dst_plane["top"] / scale_h,
+                subwidth=src_plane["aw"] * (dst_plane["width"] / dst_plane["aw"]),
+                subheight=src_plane["ah"] * (dst_plane["height"] / dst_plane["ah"]))

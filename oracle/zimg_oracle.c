@@ -1,0 +1,634 @@
+/*
+ * ORACLE — test infrastructure only. Not part of the shipped library.
+ *
+ * A plain-C restatement of zimg's separable polyphase resize, used by the
+ * tests (as the checker), by smoke() and by bench.py's CPU-baseline leg. The
+ * product never links, imports or calls this file.
+ *
+ * What it restates (paths relative to the zimg source tree):
+ *   - filter kernels                 src/zimg/resize/filter.cpp:132-246
+ *   - round_halfup                   src/zimg/resize/filter.cpp:32-40
+ *   - compute_filter                 src/zimg/resize/filter.cpp:249-306
+ *   - RowMatrix write semantics      src/zimg/common/matrix.cpp:14-21,93-149
+ *   - matrix_to_filter (f32 + i16)   src/zimg/resize/filter.cpp:43-127
+ *   - C line kernels u16/f32 H/V     src/zimg/resize/resize_impl.cpp:31-114
+ *   - pass order / skip rules        src/zimg/resize/resize.cpp:12-18,38-104
+ * plus an FP64 reference (unquantised taps, FP64 accumulation, FP64
+ * intermediate) that the reference does not expose.
+ *
+ * Build with -ffp-contract=off (oracle/Makefile) so that the taps do not depend
+ * on multiply-add fusion.
+ */
+#include <float.h>
+#include <limits.h>
+#include <math.h>
+#include <pthread.h>
+#include <stddef.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define ORC_PI 3.14159265358979323846
+
+enum { K_POINT = 0, K_BILINEAR = 1, K_BICUBIC = 2, K_SPLINE16 = 3, K_SPLINE36 = 4, K_LANCZOS = 5, K_SPLINE64 = 6 };
+
+typedef struct {
+	int kind;
+	unsigned support;
+	unsigned taps;
+	double p0, p2, p3, q0, q1, q2, q3;
+} orc_filter;
+
+/* filter.cpp:21-30 */
+static double orc_sinc(double x)
+{
+	return x == 0.0 ? 1.0 : sin(x * ORC_PI) / (x * ORC_PI);
+}
+
+static double orc_poly3(double x, double c0, double c1, double c2, double c3)
+{
+	return c0 + x * (c1 + x * (c2 + x * c3));
+}
+
+/* filter.cpp:32-40 */
+static double orc_round_halfup(double x)
+{
+	return x < 0 ? floor(x + 0.5) : floor(x + 0.49999999999999994);
+}
+
+/* Filter construction with the API's NaN defaults (zimg.cpp:320-350). Returns 0 or -1 (illegal). */
+int orc_filter_init(orc_filter *f, int kind, double a, double b)
+{
+	memset(f, 0, sizeof(*f));
+	f->kind = kind;
+	switch (kind) {
+	case K_POINT: f->support = 0; return 0;
+	case K_BILINEAR: f->support = 1; return 0;
+	case K_BICUBIC: {
+		/* filter.cpp:147-155 */
+		double bb = isnan(a) ? 0.0 : a;
+		double cc = isnan(b) ? 0.5 : b;
+		f->p0 = (6.0 - 2.0 * bb) / 6.0;
+		f->p2 = (-18.0 + 12.0 * bb + 6.0 * cc) / 6.0;
+		f->p3 = (12.0 - 9.0 * bb - 6.0 * cc) / 6.0;
+		f->q0 = (8.0 * bb + 24.0 * cc) / 6.0;
+		f->q1 = (-12.0 * bb - 48.0 * cc) / 6.0;
+		f->q2 = (6.0 * bb + 30.0 * cc) / 6.0;
+		f->q3 = (-bb - 6.0 * cc) / 6.0;
+		f->support = 2;
+		return 0;
+	}
+	case K_SPLINE16: f->support = 2; return 0;
+	case K_SPLINE36: f->support = 3; return 0;
+	case K_SPLINE64: f->support = 4; return 0;
+	case K_LANCZOS: {
+		/* zimg.cpp:343-345 and filter.cpp:232-238 */
+		double t = isnan(a) ? 3.0 : (a < 1.0 ? 1.0 : (a > 4294967295.0 ? 4294967295.0 : a));
+		unsigned taps = (unsigned)t;
+		if (taps >= 16)
+			return -1;
+		f->taps = taps;
+		f->support = taps;
+		return 0;
+	}
+	default:
+		return -2;
+	}
+}
+
+double orc_filter_eval(const orc_filter *f, double x)
+{
+	switch (f->kind) {
+	case K_POINT:
+		return 1.0;
+	case K_BILINEAR: {
+		double v = 1.0 - fabs(x);
+		return v > 0.0 ? v : 0.0;
+	}
+	case K_BICUBIC:
+		x = fabs(x);
+		if (x < 1.0)
+			return orc_poly3(x, f->p0, 0.0, f->p2, f->p3);
+		else if (x < 2.0)
+			return orc_poly3(x, f->q0, f->q1, f->q2, f->q3);
+		return 0.0;
+	case K_SPLINE16:
+		x = fabs(x);
+		if (x < 1.0)
+			return orc_poly3(x, 1.0, -1.0 / 5.0, -9.0 / 5.0, 1.0);
+		if (x < 2.0) {
+			x -= 1.0;
+			return orc_poly3(x, 0.0, -7.0 / 15.0, 4.0 / 5.0, -1.0 / 3.0);
+		}
+		return 0.0;
+	case K_SPLINE36:
+		x = fabs(x);
+		if (x < 1.0)
+			return orc_poly3(x, 1.0, -3.0 / 209.0, -453.0 / 209.0, 13.0 / 11.0);
+		if (x < 2.0) {
+			x -= 1.0;
+			return orc_poly3(x, 0.0, -156.0 / 209.0, 270.0 / 209.0, -6.0 / 11.0);
+		}
+		if (x < 3.0) {
+			x -= 2.0;
+			return orc_poly3(x, 0.0, 26.0 / 209.0, -45.0 / 209.0, 1.0 / 11.0);
+		}
+		return 0.0;
+	case K_SPLINE64:
+		x = fabs(x);
+		if (x < 1.0)
+			return orc_poly3(x, 1.0, -3.0 / 2911.0, -6387.0 / 2911.0, 49.0 / 41.0);
+		if (x < 2.0) {
+			x -= 1.0;
+			return orc_poly3(x, 0.0, -2328.0 / 2911.0, 4032.0 / 2911.0, -24.0 / 41.0);
+		}
+		if (x < 3.0) {
+			x -= 2.0;
+			return orc_poly3(x, 0.0, 582.0 / 2911.0, -1008.0 / 2911.0, 6.0 / 41.0);
+		}
+		if (x < 4.0) {
+			x -= 3.0;
+			return orc_poly3(x, 0.0, -97.0 / 2911.0, 168.0 / 2911.0, -1.0 / 41.0);
+		}
+		return 0.0;
+	case K_LANCZOS:
+		x = fabs(x);
+		return x < f->taps ? orc_sinc(x) * orc_sinc(x / f->taps) : 0.0;
+	default:
+		return 0.0;
+	}
+}
+
+/*
+ * One dense row of the sparse matrix with RowMatrix's storage rule: a write
+ * that does not change the stored value does not grow the row
+ * (matrix.cpp:14-21); growing fills with zeros (matrix.cpp:103-129).
+ */
+typedef struct {
+	double *buf; /* dense, indexed by column; zero outside [lo, hi) */
+	size_t lo, hi;
+	int empty;
+} orc_row;
+
+static double row_val(const orc_row *r, size_t j)
+{
+	return (r->empty || j < r->lo || j >= r->hi) ? 0.0 : r->buf[j];
+}
+
+static void row_assign(orc_row *r, size_t j, double v)
+{
+	if (row_val(r, j) == v)
+		return;
+	if (r->empty) {
+		r->lo = j;
+		r->hi = j + 1;
+		r->empty = 0;
+	} else if (j < r->lo) {
+		r->lo = j;
+	} else if (j >= r->hi) {
+		r->hi = j + 1;
+	}
+	r->buf[j] = v;
+}
+
+/*
+ * compute_filter + matrix_to_filter. Outputs rows*width taps packed densely.
+ * Call with out_f32 == NULL to learn the shape. f64 (optional) receives the
+ * unquantised matrix entries under the same window. Returns 0, or
+ *   -1 illegal filter, -2 filter too wide, -3 out of memory.
+ */
+int orc_compute_filter(int kind, double a, double b, unsigned src_dim, unsigned dst_dim, double shift, double width,
+                       unsigned *out_width, unsigned *out_rows,
+                       float *out_f32, int16_t *out_i16, unsigned *out_left, double *out_f64)
+{
+	orc_filter f;
+	if (orc_filter_init(&f, kind, a, b))
+		return -1;
+
+	double scale = (double)dst_dim / width;
+	double step = scale < 1.0 ? scale : 1.0;
+	double support = (double)f.support / step;
+	unsigned filter_size = (unsigned)ceil(support) * 2U;
+	if (filter_size < 1U)
+		filter_size = 1U;
+	if (support > (double)(unsigned)(UINT_MAX / 2))
+		return -2;
+
+	size_t rows = dst_dim;
+	double *dense = calloc(src_dim ? src_dim : 1, sizeof(double));
+	double **rowdata = calloc(rows ? rows : 1, sizeof(double *));
+	size_t *lo = calloc(rows ? rows : 1, sizeof(size_t));
+	size_t *hi = calloc(rows ? rows : 1, sizeof(size_t));
+	int rc = 0;
+	if (!dense || !rowdata || !lo || !hi) {
+		rc = -3;
+		goto done;
+	}
+
+	double src_hi = nextafter((double)src_dim, -INFINITY);
+	for (unsigned i = 0; i < dst_dim; ++i) {
+		orc_row r = { dense, 0, 0, 1 };
+		/* filter.cpp:262-300 */
+		double pos = (i + 0.5) / scale + shift;
+		double begin_pos = orc_round_halfup(pos - filter_size / 2.0) + 0.5;
+
+		double total = 0.0;
+		for (unsigned j = 0; j < filter_size; ++j) {
+			double xpos = begin_pos + j;
+			total += orc_filter_eval(&f, (xpos - pos) * step);
+		}
+
+		size_t left = SIZE_MAX;
+		for (unsigned j = 0; j < filter_size; ++j) {
+			double xpos = begin_pos + j;
+			double real_pos;
+			if (xpos < 0.0)
+				real_pos = -xpos;
+			else if (xpos >= src_dim)
+				real_pos = 2.0 * src_dim - xpos;
+			else
+				real_pos = xpos;
+			if (real_pos < 0.0)
+				real_pos = 0.0;
+			if (real_pos > src_hi)
+				real_pos = src_hi;
+
+			size_t idx = (size_t)floor(real_pos);
+			row_assign(&r, idx, row_val(&r, idx) + orc_filter_eval(&f, (xpos - pos) * step) / total);
+			if (idx < left)
+				left = idx;
+		}
+		if (row_val(&r, left) == 0.0) {
+			row_assign(&r, left, DBL_EPSILON);
+			row_assign(&r, left, 0.0);
+		}
+
+		lo[i] = r.lo;
+		hi[i] = r.hi;
+		rowdata[i] = malloc((r.hi - r.lo) * sizeof(double));
+		if (!rowdata[i]) {
+			rc = -3;
+			goto done;
+		}
+		memcpy(rowdata[i], dense + r.lo, (r.hi - r.lo) * sizeof(double));
+		memset(dense + r.lo, 0, (r.hi - r.lo) * sizeof(double));
+	}
+
+	/* matrix_to_filter (filter.cpp:43-127) */
+	size_t fw = 0;
+	for (size_t i = 0; i < rows; ++i)
+		if (hi[i] - lo[i] > fw)
+			fw = hi[i] - lo[i];
+	*out_width = (unsigned)fw;
+	*out_rows = (unsigned)rows;
+	if (!out_f32)
+		goto done;
+
+	for (size_t i = 0; i < rows; ++i) {
+		size_t left = lo[i] < (size_t)src_dim - fw ? lo[i] : (size_t)src_dim - fw;
+		double f32_err = 0.0;
+		double i16_err = 0.0;
+		int16_t i16_sum = 0;
+		int16_t i16_greatest = 0;
+		size_t i16_greatest_idx = 0;
+
+		for (size_t j = 0; j < fw; ++j) {
+			size_t col = left + j;
+			double coeff = (col < lo[i] || col >= hi[i]) ? 0.0 : rowdata[i][col - lo[i]];
+			double expected_f32 = coeff - f32_err;
+			double expected_i16 = coeff * (1 << 14) - i16_err;
+			float c32 = (float)expected_f32;
+			int16_t c16 = (int16_t)lrint(expected_i16);
+			f32_err = (double)c32 - expected_f32;
+			i16_err = (double)c16 - expected_i16;
+			if (abs(c16) > abs(i16_greatest)) {
+				i16_greatest = c16;
+				i16_greatest_idx = j;
+			}
+			i16_sum = (int16_t)(i16_sum + c16);
+			out_f32[i * fw + j] = c32;
+			out_i16[i * fw + j] = c16;
+			if (out_f64)
+				out_f64[i * fw + j] = coeff;
+		}
+		out_i16[i * fw + i16_greatest_idx] = (int16_t)(out_i16[i * fw + i16_greatest_idx] + ((1 << 14) - i16_sum));
+		out_left[i] = (unsigned)left;
+	}
+
+done:
+	if (rowdata)
+		for (size_t i = 0; i < rows; ++i)
+			free(rowdata[i]);
+	free(rowdata);
+	free(lo);
+	free(hi);
+	free(dense);
+	return rc;
+}
+
+/* ------------------------------------------------------------------ passes -- */
+
+typedef struct {
+	unsigned width, rows;
+	float *f32;
+	int16_t *i16;
+	double *f64;
+	unsigned *left;
+} orc_ctx;
+
+static void ctx_free(orc_ctx *c)
+{
+	free(c->f32);
+	free(c->i16);
+	free(c->f64);
+	free(c->left);
+	memset(c, 0, sizeof(*c));
+}
+
+static int ctx_make(orc_ctx *c, int kind, double a, double b, unsigned src_dim, unsigned dst_dim, double shift, double width)
+{
+	memset(c, 0, sizeof(*c));
+	int rc = orc_compute_filter(kind, a, b, src_dim, dst_dim, shift, width, &c->width, &c->rows, NULL, NULL, NULL, NULL);
+	if (rc)
+		return rc;
+	size_t n = (size_t)c->width * c->rows;
+	c->f32 = malloc(n * sizeof(float) + 1);
+	c->i16 = malloc(n * sizeof(int16_t) + 1);
+	c->f64 = malloc(n * sizeof(double) + 1);
+	c->left = malloc(c->rows * sizeof(unsigned) + 1);
+	if (!c->f32 || !c->i16 || !c->f64 || !c->left) {
+		ctx_free(c);
+		return -3;
+	}
+	return orc_compute_filter(kind, a, b, src_dim, dst_dim, shift, width, &c->width, &c->rows, c->f32, c->i16, c->left, c->f64);
+}
+
+/* resize_impl.cpp:31-42. Arithmetic in uint32 mirrors int32 wraparound. */
+static uint16_t pack_u16(uint32_t acc, int32_t pixel_max)
+{
+	int32_t x = (int32_t)(acc + (1u << 13));
+	x = (x >> 14) + 32768;
+	if (x > pixel_max)
+		x = pixel_max;
+	if (x < 0)
+		x = 0;
+	return (uint16_t)x;
+}
+
+enum { T_U16 = 1, T_F32 = 3, T_F64 = 4 };
+
+typedef struct {
+	const orc_ctx *ctx;
+	int horizontal;
+	int type;      /* T_U16, T_F32, T_F64 (T_F64: double in/out, f64 taps) */
+	int use_fma;   /* f32 only */
+	int32_t pixel_max;
+	const void *src;
+	ptrdiff_t src_stride; /* elements */
+	void *dst;
+	ptrdiff_t dst_stride; /* elements */
+	unsigned out_w, out_h;
+	unsigned row_begin, row_end;
+} orc_job;
+
+/* resize_line_{h,v}_{u16,f32}_c (resize_impl.cpp:44-114), one output row. */
+static void run_row(const orc_job *job, unsigned i)
+{
+	const orc_ctx *c = job->ctx;
+	unsigned fw = c->width;
+	if (job->horizontal) {
+		for (unsigned j = 0; j < job->out_w; ++j) {
+			unsigned l = c->left[j];
+			if (job->type == T_U16) {
+				const uint16_t *s = (const uint16_t *)job->src + (ptrdiff_t)i * job->src_stride;
+				uint32_t acc = 0;
+				for (unsigned k = 0; k < fw; ++k)
+					acc += (uint32_t)((int32_t)c->i16[(size_t)j * fw + k] * ((int32_t)s[l + k] - 32768));
+				((uint16_t *)job->dst)[(ptrdiff_t)i * job->dst_stride + j] = pack_u16(acc, job->pixel_max);
+			} else if (job->type == T_F32) {
+				const float *s = (const float *)job->src + (ptrdiff_t)i * job->src_stride;
+				float acc = 0;
+				for (unsigned k = 0; k < fw; ++k)
+					acc = job->use_fma ? fmaf(c->f32[(size_t)j * fw + k], s[l + k], acc) : acc + c->f32[(size_t)j * fw + k] * s[l + k];
+				((float *)job->dst)[(ptrdiff_t)i * job->dst_stride + j] = acc;
+			} else {
+				const double *s = (const double *)job->src + (ptrdiff_t)i * job->src_stride;
+				double acc = 0;
+				for (unsigned k = 0; k < fw; ++k)
+					acc += c->f64[(size_t)j * fw + k] * s[l + k];
+				((double *)job->dst)[(ptrdiff_t)i * job->dst_stride + j] = acc;
+			}
+		}
+	} else {
+		unsigned top = c->left[i];
+		if (job->type == T_U16) {
+			const int16_t *co = c->i16 + (size_t)i * fw;
+			for (unsigned j = 0; j < job->out_w; ++j) {
+				uint32_t acc = 0;
+				for (unsigned k = 0; k < fw; ++k) {
+					const uint16_t *s = (const uint16_t *)job->src + (ptrdiff_t)(top + k) * job->src_stride;
+					acc += (uint32_t)((int32_t)co[k] * ((int32_t)s[j] - 32768));
+				}
+				((uint16_t *)job->dst)[(ptrdiff_t)i * job->dst_stride + j] = pack_u16(acc, job->pixel_max);
+			}
+		} else if (job->type == T_F32) {
+			const float *co = c->f32 + (size_t)i * fw;
+			for (unsigned j = 0; j < job->out_w; ++j) {
+				float acc = 0;
+				for (unsigned k = 0; k < fw; ++k) {
+					const float *s = (const float *)job->src + (ptrdiff_t)(top + k) * job->src_stride;
+					acc = job->use_fma ? fmaf(co[k], s[j], acc) : acc + co[k] * s[j];
+				}
+				((float *)job->dst)[(ptrdiff_t)i * job->dst_stride + j] = acc;
+			}
+		} else {
+			const double *co = c->f64 + (size_t)i * fw;
+			for (unsigned j = 0; j < job->out_w; ++j) {
+				double acc = 0;
+				for (unsigned k = 0; k < fw; ++k) {
+					const double *s = (const double *)job->src + (ptrdiff_t)(top + k) * job->src_stride;
+					acc += co[k] * s[j];
+				}
+				((double *)job->dst)[(ptrdiff_t)i * job->dst_stride + j] = acc;
+			}
+		}
+	}
+}
+
+static void *run_rows(void *arg)
+{
+	const orc_job *job = arg;
+	for (unsigned i = job->row_begin; i < job->row_end; ++i)
+		run_row(job, i);
+	return NULL;
+}
+
+static int run_pass(const orc_job *proto, int nthreads)
+{
+	if (nthreads < 1)
+		nthreads = 1;
+	if (nthreads > 256)
+		nthreads = 256;
+	if ((unsigned)nthreads > proto->out_h)
+		nthreads = proto->out_h ? (int)proto->out_h : 1;
+	orc_job jobs[256];
+	pthread_t th[256];
+	int joined[256] = { 0 };
+	unsigned per = (proto->out_h + nthreads - 1) / nthreads;
+	for (int t = 0; t < nthreads; ++t) {
+		jobs[t] = *proto;
+		jobs[t].row_begin = t * per < proto->out_h ? t * per : proto->out_h;
+		jobs[t].row_end = (t + 1) * per < proto->out_h ? (t + 1) * per : proto->out_h;
+		if (t == 0)
+			continue;
+		if (pthread_create(&th[t], NULL, run_rows, &jobs[t]) == 0)
+			joined[t] = 1;
+		else
+			run_rows(&jobs[t]);
+	}
+	run_rows(&jobs[0]);
+	for (int t = 1; t < nthreads; ++t)
+		if (joined[t])
+			pthread_join(th[t], NULL);
+	return 0;
+}
+
+/* resize.cpp:12-18 */
+int orc_resize_h_first(double xscale, double yscale)
+{
+	double h_first_cost = (xscale > 1.0 ? xscale : 1.0) * 2.0 + xscale * (yscale > 1.0 ? yscale : 1.0);
+	double v_first_cost = (yscale > 1.0 ? yscale : 1.0) + yscale * (xscale > 1.0 ? xscale : 1.0) * 2.0;
+	return h_first_cost < v_first_cost;
+}
+
+/*
+ * Pass list of ResizeConversion::create (resize.cpp:38-104):
+ * returns the number of passes (0, 1, 2) and writes 1 for horizontal, 0 for
+ * vertical into order[0..n).
+ */
+int orc_plan_order(unsigned src_w, unsigned src_h, unsigned dst_w, unsigned dst_h,
+                   double shift_w, double shift_h, double subwidth, double subheight, int *order)
+{
+	int skip_h = (src_w == dst_w && shift_w == 0 && subwidth == src_w);
+	int skip_v = (src_h == dst_h && shift_h == 0 && subheight == src_h);
+	if (skip_h && skip_v)
+		return 0;
+	if (skip_h) {
+		order[0] = 0;
+		return 1;
+	}
+	if (skip_v) {
+		order[0] = 1;
+		return 1;
+	}
+	int h_first = orc_resize_h_first((double)dst_w / subwidth, (double)dst_h / subheight);
+	order[0] = h_first ? 1 : 0;
+	order[1] = h_first ? 0 : 1;
+	return 2;
+}
+
+static size_t type_size(int type)
+{
+	return type == T_U16 ? 2 : (type == T_F32 ? 4 : 8);
+}
+
+/*
+ * Whole-plane resize. type: 1 = u16 (C path, exact), 3 = f32 (sequential,
+ * optionally fused multiply-add), 4 = FP64 oracle (double in/out).
+ * Strides are in elements. Returns 0 or a negative error.
+ */
+int orc_resize_plane(int type, unsigned depth, int kind, double a, double b,
+                     unsigned src_w, unsigned src_h, unsigned dst_w, unsigned dst_h,
+                     double shift_w, double shift_h, double subwidth, double subheight,
+                     int use_fma, int nthreads,
+                     const void *src, ptrdiff_t src_stride, void *dst, ptrdiff_t dst_stride)
+{
+	int order[2];
+	int n = orc_plan_order(src_w, src_h, dst_w, dst_h, shift_w, shift_h, subwidth, subheight, order);
+	size_t ts = type_size(type);
+	if (n == 0) {
+		for (unsigned i = 0; i < dst_h; ++i)
+			memcpy((char *)dst + (size_t)i * dst_stride * ts, (const char *)src + (size_t)i * src_stride * ts, (size_t)dst_w * ts);
+		return 0;
+	}
+
+	unsigned cur_w = src_w, cur_h = src_h;
+	const void *cur = src;
+	ptrdiff_t cur_stride = src_stride;
+	void *tmp = NULL;
+	int rc = 0;
+	for (int p = 0; p < n; ++p) {
+		int h = order[p];
+		orc_ctx ctx;
+		rc = h ? ctx_make(&ctx, kind, a, b, cur_w, dst_w, shift_w, subwidth)
+		       : ctx_make(&ctx, kind, a, b, cur_h, dst_h, shift_h, subheight);
+		if (rc)
+			break;
+		unsigned out_w = h ? dst_w : cur_w;
+		unsigned out_h = h ? cur_h : dst_h;
+		void *out;
+		ptrdiff_t out_stride;
+		if (p == n - 1) {
+			out = dst;
+			out_stride = dst_stride;
+		} else {
+			tmp = malloc((size_t)out_w * out_h * ts + 64);
+			if (!tmp) {
+				ctx_free(&ctx);
+				rc = -3;
+				break;
+			}
+			out = tmp;
+			out_stride = out_w;
+		}
+		orc_job job;
+		memset(&job, 0, sizeof(job));
+		job.ctx = &ctx;
+		job.horizontal = h;
+		job.type = type;
+		job.use_fma = use_fma;
+		job.pixel_max = (int32_t)((1UL << depth) - 1);
+		job.src = cur;
+		job.src_stride = cur_stride;
+		job.dst = out;
+		job.dst_stride = out_stride;
+		job.out_w = out_w;
+		job.out_h = out_h;
+		run_pass(&job, nthreads);
+		ctx_free(&ctx);
+		cur = out;
+		cur_stride = out_stride;
+		cur_w = out_w;
+		cur_h = out_h;
+	}
+	free(tmp);
+	return rc;
+}
+
+/* One pass (ResizeImplBuilder, resize_impl.cpp:245-267) on a whole plane. */
+int orc_resize_pass(int type, unsigned depth, int horizontal, int kind, double a, double b,
+                    unsigned src_w, unsigned src_h, unsigned dst_dim, double shift, double subwidth,
+                    int use_fma, int nthreads,
+                    const void *src, ptrdiff_t src_stride, void *dst, ptrdiff_t dst_stride)
+{
+	orc_ctx ctx;
+	int rc = ctx_make(&ctx, kind, a, b, horizontal ? src_w : src_h, dst_dim, shift, subwidth);
+	if (rc)
+		return rc;
+	orc_job job;
+	memset(&job, 0, sizeof(job));
+	job.ctx = &ctx;
+	job.horizontal = horizontal;
+	job.type = type;
+	job.use_fma = use_fma;
+	job.pixel_max = (int32_t)((1UL << depth) - 1);
+	job.src = src;
+	job.src_stride = src_stride;
+	job.dst = dst;
+	job.dst_stride = dst_stride;
+	job.out_w = horizontal ? dst_dim : src_w;
+	job.out_h = horizontal ? src_h : dst_dim;
+	run_pass(&job, nthreads);
+	ctx_free(&ctx);
+	return 0;
+}
