@@ -1,0 +1,419 @@
+"""Benchmark of the resize path on GB300 (one JSON line on rank 0).
+
+Default workload (the FP32 headline case): FP32 bicubic (b=0, c=0.5)
+downscale of 3 planes 4:4:4 1920x1080 -> 1280x720, a batch of frames per step.
+Other workloads (--workload):
+  fhd_uhd_u16     1 plane 1920x1080 u16 10-bit Lanczos-3 -> 3840x2160 (bit-exact path)
+  bicubic_f32     the default
+  wide_f32        8 planes 7680x4320 f32 Lanczos-4 16x down -> 480x270
+  yuv420_batch    64 YUV 4:2:0 u16 frames of mixed sizes, Spline36 -> 1920x1080
+  extreme_f32     32 images 64x64 -> 6400x6400 and 6400x6400 -> 64x64 f32 Lanczos-3, plus 32 interlaced
+                  1920x1080 frames as fields -> 1280x720
+
+A step is one pass of the resize path over one batch of synthetic frames that
+are already resident in HBM (inputs larger than L2 across the batch). `value`
+is output Mpixel/s (output samples summed over planes, as zimg's ns/sample,
+resizeapp.cpp:119-123). `e2e` is the same metric with each step's input copied
+from pinned host memory and its output copied back inside the timed region.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+L2_BYTES = 129 * 1024 * 1024
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ------------------------------------------------------------------ workloads --
+
+def _job(sw, sh, dw, dh, ptype, depth, kind, a=math.nan, b=math.nan, shift_w=0.0, shift_h=0.0, engine="auto"):
+    return dict(sw=sw, sh=sh, dw=dw, dh=dh, ptype=ptype, depth=depth, kind=kind, a=a, b=b, shift_w=shift_w,
+                shift_h=shift_h, engine=engine)
+
+
+def workload(name: str, frames: int | None, seed: int):
+    """List of jobs for one step (one batch), plus config metadata."""
+    rng = np.random.default_rng(seed)
+    if name == "bicubic_f32":
+        n = frames or 128
+        jobs = [_job(1920, 1080, 1280, 720, "float", 32, "bicubic", 0.0, 0.5) for _ in range(3 * n)]
+        cfg = {"workload": "bicubic_f32: 3 planes 4:4:4 1920x1080 f32 -> 1280x720, bicubic b=0 c=0.5",
+               "frames_per_step": n, "planes_per_step": 3 * n}
+    elif name == "fhd_uhd_u16":
+        n = frames or 64
+        jobs = [_job(1920, 1080, 3840, 2160, "word", 10, "lanczos", 3) for _ in range(n)]
+        cfg = {"workload": "fhd_uhd_u16: 1 plane 1920x1080 u16 10-bit -> 3840x2160, Lanczos a=3, H then V",
+               "frames_per_step": n, "planes_per_step": n}
+    elif name == "wide_f32":
+        n = frames or 8
+        jobs = [_job(7680, 4320, 480, 270, "float", 32, "lanczos", 4) for _ in range(n)]
+        cfg = {"workload": "wide_f32: 8 planes 7680x4320 f32 -> 480x270, Lanczos a=4 (128 taps)",
+               "frames_per_step": 1, "planes_per_step": n}
+    elif name == "yuv420_batch":
+        n = frames or 64
+        sizes = [(720, 480), (1280, 720), (1920, 1080), (3840, 2160)]
+        jobs = []
+        for _ in range(n):
+            sw, sh = sizes[int(rng.integers(0, 4))]
+            jobs.append(_job(sw, sh, 1920, 1080, "word", 10, "spline36", shift_w=0.0))
+            # chroma 4:2:0 with MPEG-2 (left) siting on both sides: shift = 0.25 - 0.25 / scale
+            shw = 0.25 - 0.25 / (960 / (sw // 2))
+            for _c in range(2):
+                jobs.append(_job(sw // 2, sh // 2, 960, 540, "word", 10, "spline36", shift_w=shw))
+        cfg = {"workload": "yuv420_batch: 64 YUV 4:2:0 u16 10-bit frames, sizes drawn from 720x480..3840x2160, "
+                           "Spline36 -> 1920x1080 (+2x960x540), MPEG-2 siting",
+               "frames_per_step": n, "planes_per_step": 3 * n}
+    elif name == "extreme_f32":
+        n = frames or 32
+        jobs = [_job(64, 64, 6400, 6400, "float", 32, "lanczos", 3) for _ in range(n)]
+        jobs += [_job(6400, 6400, 64, 64, "float", 32, "lanczos", 3) for _ in range(n)]
+        for _ in range(n):
+            jobs.append(_job(1920, 540, 1280, 360, "float", 32, "lanczos", 3, shift_h=-0.125))
+            jobs.append(_job(1920, 540, 1280, 360, "float", 32, "lanczos", 3, shift_h=0.125))
+        cfg = {"workload": "extreme_f32: 32x(64^2->6400^2) + 32x(6400^2->64^2) + 32 interlaced 1080 frames "
+                           "as fields -> 720, Lanczos a=3", "frames_per_step": n, "planes_per_step": len(jobs)}
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    return jobs, cfg
+
+
+def job_bytes(j):
+    bpe = 2 if j["ptype"] == "word" else 4
+    return (j["sw"] * j["sh"] + j["dw"] * j["dh"]) * bpe
+
+
+def fill(rng, j):
+    if j["ptype"] == "word":
+        return rng.integers(0, 1 << j["depth"], size=(j["sh"], j["sw"]), dtype=np.uint16)
+    return rng.random((j["sh"], j["sw"]), dtype=np.float32)
+
+
+# ------------------------------------------------------------------- clocks --
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples while the GPU is busy."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 8:
+                self.rows.append((time.time(), parts))
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=5)
+
+    def summary(self, t0: float, t1: float):
+        rows = [r for t, r in self.rows if t0 - 0.15 <= t <= t1 + 0.15] or [r for _, r in self.rows]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(r[0]) for r in rows if num(r[0]) is not None]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for name, v in zip(names, r[4:8]):
+                if v.strip().lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": num(rows[0][1]),
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+# ------------------------------------------------------------------- our arm --
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+    import zimg_gb300 as zg
+    from zimg_gb300 import build as zbuild
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    zbuild.build()
+    zg.load()
+
+    jobs, cfg = workload(args.workload, args.frames, seed=0x5EED0000 + rank)
+    rng = np.random.default_rng(1234 + rank)
+    # Distinct source planes per job (the batch is the working set), generated on the device from a few seeded
+    # host planes so set-up stays quick.
+    host_proto = {}
+    srcs, dsts, convs = [], [], []
+    for j in jobs:
+        key = (j["sw"], j["sh"], j["ptype"])
+        if key not in host_proto:
+            host_proto[key] = [fill(rng, j) for _ in range(2)]
+        proto = host_proto[key][len(srcs) % 2]
+        t = torch.from_numpy(proto.view(np.int16) if proto.dtype == np.uint16 else proto).cuda()
+        srcs.append(t.clone())
+        tdt = torch.int16 if j["ptype"] == "word" else torch.float32
+        dsts.append(torch.empty((j["dh"], j["dw"]), dtype=tdt, device="cuda"))
+        convs.append(zg.ResizeConversion(j["sw"], j["sh"], j["ptype"]).set_depth(j["depth"])
+                     .set_filter(j["kind"], j["a"], j["b"]).set_dst_width(j["dw"]).set_dst_height(j["dh"])
+                     .set_shift_w(j["shift_w"]).set_shift_h(j["shift_h"]).set_engine(j["engine"]))
+    batch = zg.Batch(convs)
+    batch.set_io(srcs, dsts)
+    tmp = torch.empty(max(batch.tmp_size, 1), dtype=torch.uint8, device="cuda")
+    launches_per_step = batch.launch_count
+    stream = torch.cuda.current_stream()
+
+    out_px = sum(j["dw"] * j["dh"] for j in jobs)
+    alg_bytes = sum(job_bytes(j) for j in jobs)
+    in_bytes = sum(j["sw"] * j["sh"] * (2 if j["ptype"] == "word" else 4) for j in jobs)
+    out_bytes = alg_bytes - in_bytes
+
+    step = (lambda: batch.process_graph(tmp)) if args.graph else (lambda: batch.process(tmp))
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    # spin up the clocks before the timed region
+    for _ in range(max(args.warmup, 3)):
+        step()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0 = time.time()
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    t1 = time.time()
+    sampler.stop()
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    value = out_px * world * args.steps / (ms / 1e3) / 1e6
+
+    # ---- end to end through the public API with host buffers ----
+    e2e = None
+    if not args.no_e2e:
+        n_e2e = min(len(jobs), args.e2e_planes)
+        hsrc = [srcs[i].cpu().pin_memory() for i in range(n_e2e)]
+        hdst = [torch.empty(dsts[i].shape, dtype=dsts[i].dtype).pin_memory() for i in range(n_e2e)]
+        sub = zg.Batch(convs[:n_e2e])
+        sub.set_io(srcs[:n_e2e], dsts[:n_e2e])
+        stmp = torch.empty(max(sub.tmp_size, 1), dtype=torch.uint8, device="cuda")
+
+        def e2e_step():
+            for i in range(n_e2e):
+                srcs[i].copy_(hsrc[i], non_blocking=True)
+            sub.process(stmp)
+            for i in range(n_e2e):
+                hdst[i].copy_(dsts[i], non_blocking=True)
+        for _ in range(3):
+            e2e_step()
+        torch.cuda.synchronize()
+        k = max(3, args.steps // 4)
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record(stream)
+        for _ in range(k):
+            e2e_step()
+        a1.record(stream)
+        a1.synchronize()
+        e_ms = a0.elapsed_time(a1) / k
+        e_px = sum(jobs[i]["dw"] * jobs[i]["dh"] for i in range(n_e2e))
+        h2d = sum(jobs[i]["sw"] * jobs[i]["sh"] * (2 if jobs[i]["ptype"] == "word" else 4) for i in range(n_e2e))
+        d2h = sum(jobs[i]["dw"] * jobs[i]["dh"] * (2 if jobs[i]["ptype"] == "word" else 4) for i in range(n_e2e))
+        if world > 1:
+            t = torch.tensor([e_ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e_ms = float(t.item())
+        e2e = {"value": round(e_px * world / (e_ms / 1e3) / 1e6, 3), "unit": "Mpixel/s",
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "planes_per_step": n_e2e}
+
+    peak, peak_kind = load_peaks()
+    achieved = alg_bytes / (ms_step / 1e3) / 1e9
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "peak_source": f"{peak_kind} hbm_gbs",
+                "traffic": read_traffic(args.workload), "algorithmic_bytes_per_step": alg_bytes,
+                "kernel_launches_per_step": launches_per_step}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(jobs, seconds=args.cpu_seconds)
+
+    if rank == 0:
+        line = {"metric": "out Mpixel/s on 1 GB300 + % HBM roofline", "value": round(value, 3), "unit": "Mpixel/s",
+                "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 5),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "u16" if jobs[0]["ptype"] == "word" else "f32", "data": "synthetic (seeded)",
+                "config": dict(cfg, l2="inputs larger than L2 (batch working set %.2f GB)" % (alg_bytes / 1e9),
+                               parallelism=f"replicas x{world}", graph=bool(args.graph)),
+                "impl": "ours", "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
+                "clocks": sampler.summary(t0, t1), "gpu_launches": launches_per_step * args.steps}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def read_traffic(workload_name):
+    """DRAM bytes per launch from the committed ncu summary, if one exists."""
+    p = os.path.join(ROOT, "profiles", f"traffic_{workload_name}.txt")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("dram_bytes_per_step:"):
+            return int(float(line.split(":", 1)[1]))
+    return None
+
+
+# ---------------------------------------------------------------- CPU side --
+
+def cpu_baseline(jobs, seconds=10.0, impl_label=None):
+    """The oracle's C restatement of zimg's C path on the host cores (all
+    threads, row-parallel per plane), on a bounded sample of the workload."""
+    from oracle.oracle import Oracle, build
+    build()
+    o = Oracle()
+    cores = os.cpu_count() or 1
+    rng = np.random.default_rng(99)
+    sample = []
+    for j in jobs[: min(len(jobs), 6)]:
+        sample.append((j, fill(rng, j)))
+    px = 0
+    t0 = time.perf_counter()
+    n_planes = 0
+    while True:
+        for j, x in sample:
+            o.resize_plane(x, j["dw"], j["dh"], j["kind"], j["a"], j["b"], depth=j["depth"], shift_w=j["shift_w"],
+                           shift_h=j["shift_h"], mode="c", nthreads=cores)
+            px += j["dw"] * j["dh"]
+            n_planes += 1
+            if time.perf_counter() - t0 > seconds:
+                break
+        if time.perf_counter() - t0 > seconds:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": round(px / dt / 1e6, 3), "unit": "Mpixel/s", "cores": cores, "kind": "port",
+            "sample": f"{n_planes} planes of the workload's first {len(sample)} jobs in {dt:.1f} s, zimg C-path "
+                      f"restatement (oracle/zimg_oracle.c), {cores} threads row-parallel"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    jobs, cfg = workload(args.workload, args.frames, seed=0x5EED0000)
+    from oracle.oracle import Oracle, build
+    build()
+    o = Oracle()
+    cores = os.cpu_count() or 1
+    rng = np.random.default_rng(99)
+    j = jobs[0]
+    planes_per_step = 1
+    x = fill(rng, j)
+
+    def step():
+        o.resize_plane(x, j["dw"], j["dh"], j["kind"], j["a"], j["b"], depth=j["depth"], shift_w=j["shift_w"],
+                       shift_h=j["shift_h"], mode="c", nthreads=cores)
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = time.perf_counter() - t0
+    value = j["dw"] * j["dh"] * planes_per_step * args.steps / dt / 1e6
+    line = {"metric": "out Mpixel/s on 1 GB300 + % HBM roofline", "value": round(value, 3), "unit": "Mpixel/s",
+            "n_gpus": int(os.environ.get("WORLD_SIZE", "1")), "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(dt / args.steps * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u16" if j["ptype"] == "word" else "f32", "data": "synthetic (seeded)",
+            "config": cfg, "impl": "reference",
+            "cpu_baseline": {"value": round(value, 3), "unit": "Mpixel/s", "cores": cores, "kind": "port",
+                             "sample": f"one plane of the workload per step ({j['sw']}x{j['sh']} -> "
+                                       f"{j['dw']}x{j['dh']}), zimg C-path restatement, {cores} threads"},
+            "e2e": {"value": round(value, 3), "unit": "Mpixel/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--workload", default="bicubic_f32")
+    ap.add_argument("--frames", type=int, default=None)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--graph", action="store_true", help="replay the batch from a CUDA graph")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--e2e-planes", type=int, default=48)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

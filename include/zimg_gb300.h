@@ -1,0 +1,301 @@
+/*
+ * zimg_gb300 — zimg's separable polyphase resize (ResizeImplH / ResizeImplV)
+ * on one GB300 GPU, behind a plain C ABI.
+ *
+ * Every pointer passed to a *_process call is a DEVICE pointer on the GPU that
+ * was current when the object was created; every size is in elements or bytes
+ * as stated. Objects are immutable after creation, so several host threads may
+ * share one object, each with its own stream (as zimg's graphs are shared,
+ * graphapp.cpp:355-377). No call allocates device memory while processing; the
+ * caller provides the scratch buffer whose size *_get_tmp_size reports, as
+ * zimg_filter_graph_process does (zimg.h:494-507).
+ *
+ * Each declaration names the zimg interface it replaces (paths relative to the
+ * zimg source tree).
+ */
+#ifndef ZIMG_GB300_H_
+#define ZIMG_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define ZG_API __declspec(dllexport)
+#else
+#define ZG_API __attribute__((visibility("default")))
+#endif
+
+#define ZG_API_VERSION_MAJOR 1
+#define ZG_API_VERSION_MINOR 0
+
+/* Same layout as cudaStream_t; 0 is the legacy default stream. */
+typedef struct CUstream_st *zg_stream;
+
+/* Error codes: the values of zimg_error_code_e (zimg.h:79-121). */
+typedef enum zg_error_code {
+	ZG_ERROR_UNKNOWN = -1,
+	ZG_ERROR_SUCCESS = 0,
+	ZG_ERROR_OUT_OF_MEMORY = 1,
+	ZG_ERROR_USER_CALLBACK_FAILED = 2,
+	ZG_ERROR_LOGIC = (1 << 10),
+	ZG_ERROR_GREYSCALE_SUBSAMPLING = ZG_ERROR_LOGIC + 1,
+	ZG_ERROR_COLOR_FAMILY_MISMATCH = ZG_ERROR_LOGIC + 2,
+	ZG_ERROR_IMAGE_NOT_DIVISIBLE = ZG_ERROR_LOGIC + 3,
+	ZG_ERROR_BIT_DEPTH_OVERFLOW = ZG_ERROR_LOGIC + 4,
+	ZG_ERROR_ILLEGAL_ARGUMENT = (2 << 10),
+	ZG_ERROR_ENUM_OUT_OF_RANGE = ZG_ERROR_ILLEGAL_ARGUMENT + 1,
+	ZG_ERROR_INVALID_IMAGE_SIZE = ZG_ERROR_ILLEGAL_ARGUMENT + 2,
+	ZG_ERROR_UNSUPPORTED_OPERATION = (3 << 10),
+	ZG_ERROR_UNSUPPORTED_SUBSAMPLING = ZG_ERROR_UNSUPPORTED_OPERATION + 1,
+	ZG_ERROR_NO_COLORSPACE_CONVERSION = ZG_ERROR_UNSUPPORTED_OPERATION + 2,
+	ZG_ERROR_NO_FIELD_PARITY_CONVERSION = ZG_ERROR_UNSUPPORTED_OPERATION + 3,
+	ZG_ERROR_RESAMPLING_NOT_AVAILABLE = ZG_ERROR_UNSUPPORTED_OPERATION + 4
+} zg_error_code;
+
+/* Pixel types: the values of zimg_pixel_type_e (zimg.h:191-196). WORD and FLOAT resize. */
+typedef enum zg_pixel_type {
+	ZG_PIXEL_BYTE = 0,
+	ZG_PIXEL_WORD = 1,
+	ZG_PIXEL_HALF = 2,
+	ZG_PIXEL_FLOAT = 3
+} zg_pixel_type;
+
+/* Resampling filters: the values of zimg_resample_filter_e (zimg.h:374-382). */
+typedef enum zg_resample_filter {
+	ZG_RESIZE_POINT = 0,
+	ZG_RESIZE_BILINEAR = 1,
+	ZG_RESIZE_BICUBIC = 2,
+	ZG_RESIZE_SPLINE16 = 3,
+	ZG_RESIZE_SPLINE36 = 4,
+	ZG_RESIZE_SPLINE64 = 6,
+	ZG_RESIZE_LANCZOS = 5
+} zg_resample_filter;
+
+/* Arithmetic the planner may pick for a pass (see zg_resize_params.engine). */
+typedef enum zg_engine {
+	ZG_ENGINE_AUTO = 0,    /* autotuner's choice */
+	ZG_ENGINE_CUDA = 1,    /* CUDA-core kernels only */
+	ZG_ENGINE_TENSOR = 2   /* banded GEMM on the tensor cores where the pass allows it (FLOAT only) */
+} zg_engine;
+
+/* ------------------------------------------------------------------ errors --
+ * Replaces zimg_get_last_error / zimg_clear_last_error (zimg.h:120-151,
+ * zimg.cpp:531-538): the code and message of the last failure on this thread.
+ */
+ZG_API zg_error_code zg_get_last_error(char *err_msg, size_t n);
+ZG_API void zg_clear_last_error(void);
+
+/* Version of this library. Replaces zimg_get_version_info (zimg.h:54). */
+ZG_API void zg_get_version_info(unsigned *major, unsigned *minor, unsigned *micro);
+
+/* --------------------------------------------------------- filter context --
+ * Replaces compute_filter (src/zimg/resize/filter.h:178, filter.cpp:249-306):
+ * the FP64 filter matrix, quantised to float and to signed 1.14 int16 taps
+ * with zimg's error diffusion and row-sum fix-up (filter.cpp:43-127). Host
+ * only; no GPU is touched. Call with f32 == NULL to learn *filter_width and
+ * *filter_rows; then pass f32[rows*width], i16[rows*width], left[rows] (rows
+ * packed without zimg's stride padding). width <= 0 means "src_dim".
+ */
+ZG_API zg_error_code zg_compute_filter(zg_resample_filter filter, double param_a, double param_b,
+                                unsigned src_dim, unsigned dst_dim, double shift, double width,
+                                unsigned *filter_width, unsigned *filter_rows,
+                                float *f32, int16_t *i16, unsigned *left);
+
+/* -------------------------------------------------------------- one pass --
+ * Replaces ResizeImplBuilder{src_w, src_h, type}.set_horizontal()
+ * .set_dst_dim().set_depth().set_filter().set_shift().set_subwidth().create()
+ * (src/zimg/resize/resize_impl.h:45-63, resize_impl.cpp:245-267) and the
+ * resulting filter's process() over every line (resize_impl.cpp:130-160).
+ */
+typedef struct zg_resize_pass zg_resize_pass;
+
+typedef struct zg_pass_params {
+	unsigned src_width;
+	unsigned src_height;
+	zg_pixel_type pixel_type;   /* WORD or FLOAT */
+	unsigned depth;             /* bits per sample for WORD (1..16); ignored for FLOAT */
+	int horizontal;             /* non-zero: ResizeImplH, else ResizeImplV */
+	unsigned dst_dim;           /* output width (H) or height (V) */
+	zg_resample_filter filter;
+	double filter_param_a;      /* NaN: library default (zimg.cpp:320-350) */
+	double filter_param_b;
+	double shift;               /* in source pixels */
+	double subwidth;            /* active source extent; <= 0 or NaN means src dim */
+	zg_engine engine;
+} zg_pass_params;
+
+ZG_API zg_error_code zg_resize_pass_create(const zg_pass_params *params, zg_resize_pass **out);
+ZG_API void zg_resize_pass_free(zg_resize_pass *pass);
+/* Output plane size of the pass. */
+ZG_API zg_error_code zg_resize_pass_get_output(const zg_resize_pass *pass, unsigned *width, unsigned *height);
+/* Whole-plane process. Strides in bytes; src and dst must not overlap. */
+ZG_API zg_error_code zg_resize_pass_process(const zg_resize_pass *pass, const void *src, ptrdiff_t src_stride,
+                                     void *dst, ptrdiff_t dst_stride, zg_stream stream);
+
+/* ----------------------------------------------------------- conversion --
+ * Replaces ResizeConversion{w, h, type}.set_depth/filter/dst_width/dst_height/
+ * shift_w/shift_h/subwidth/subheight/cpu().create() (src/zimg/resize/resize.h:
+ * 22-44, resize.cpp:38-104): zero, one or two passes in zimg's order. The
+ * planner fuses both passes into one kernel when the tile fits on chip, so
+ * the intermediate plane never reaches HBM; otherwise the intermediate lives
+ * in the caller's tmp buffer.
+ */
+typedef struct zg_resize zg_resize;
+
+typedef struct zg_resize_params {
+	unsigned src_width;
+	unsigned src_height;
+	zg_pixel_type pixel_type;
+	unsigned depth;
+	unsigned dst_width;
+	unsigned dst_height;
+	zg_resample_filter filter;
+	double filter_param_a;
+	double filter_param_b;
+	double shift_w;
+	double shift_h;
+	double subwidth;            /* <= 0 or NaN: src_width */
+	double subheight;           /* <= 0 or NaN: src_height */
+	zg_engine engine;
+	int allow_fusion;           /* 0: always two passes through tmp (testing) */
+} zg_resize_params;
+
+ZG_API void zg_resize_params_default(zg_resize_params *p);
+ZG_API zg_error_code zg_resize_create(const zg_resize_params *params, zg_resize **out);
+ZG_API void zg_resize_free(zg_resize *r);
+/* Device scratch bytes that zg_resize_process needs (0 when fused or single pass). */
+ZG_API zg_error_code zg_resize_get_tmp_size(const zg_resize *r, size_t *out);
+/* Number of passes (0 = plain copy, 1, 2), whether the first is horizontal, and
+ * whether the passes run fused in one kernel. */
+ZG_API zg_error_code zg_resize_get_info(const zg_resize *r, int *num_passes, int *first_horizontal, int *fused);
+ZG_API zg_error_code zg_resize_process(const zg_resize *r, const void *src, ptrdiff_t src_stride,
+                                void *dst, ptrdiff_t dst_stride, void *tmp, zg_stream stream);
+
+/* ---------------------------------------------------------------- batch --
+ * Many planes of uneven sizes (luma plus subsampled chroma, mixed
+ * resolutions) in one persistent launch. Replaces running one zimg graph per
+ * frame on a thread pool (graphapp.cpp:355-425). Each job is a conversion as
+ * in zg_resize_params. The caller fills a table of per-job device pointers
+ * (zg_batch_io) once; zg_batch_process launches over the whole table, and
+ * zg_batch_process_graph replays the same launch from a CUDA graph that the
+ * batch captures on its first call on that stream.
+ */
+typedef struct zg_batch zg_batch;
+
+typedef struct zg_batch_io {
+	const void *src;
+	ptrdiff_t src_stride;  /* bytes */
+	void *dst;
+	ptrdiff_t dst_stride;  /* bytes */
+} zg_batch_io;
+
+ZG_API zg_error_code zg_batch_create(const zg_resize_params *jobs, unsigned num_jobs, zg_batch **out);
+ZG_API void zg_batch_free(zg_batch *b);
+ZG_API zg_error_code zg_batch_get_tmp_size(const zg_batch *b, size_t *out);
+/* Copy a host table of num_jobs entries into the batch's device table (async on stream). */
+ZG_API zg_error_code zg_batch_set_io(zg_batch *b, const zg_batch_io *io, zg_stream stream);
+ZG_API zg_error_code zg_batch_process(const zg_batch *b, void *tmp, zg_stream stream);
+ZG_API zg_error_code zg_batch_process_graph(zg_batch *b, void *tmp, zg_stream stream);
+/* Number of kernel launches one zg_batch_process issues. */
+ZG_API zg_error_code zg_batch_get_launch_count(const zg_batch *b, unsigned *out);
+
+/* ---------------------------------------------------------------- graph --
+ * Resize-only subset of zimg_filter_graph_build / _get_tmp_size / _process
+ * (zimg.h:507,550-552,679; zimg.cpp:662-690). The format structs have the same
+ * layout and meaning as zimg_image_format and zimg_graph_builder_params
+ * (zimg.h:558-647), so a zimg caller's structs can be passed through after a
+ * pointer cast. Supported: GREY/YUV/RGB with alpha, WORD or FLOAT, equal pixel
+ * type, depth and colorspace on both sides; chroma siting, field parity and
+ * active regions are honoured as zimg's graph builder does
+ * (graphbuilder.cpp:65-188,331-366,753-824). Anything needing a colorspace,
+ * depth or field-parity conversion returns ZG_ERROR_UNSUPPORTED_OPERATION.
+ */
+typedef struct zg_image_format {
+	unsigned version;
+	unsigned width;
+	unsigned height;
+	int pixel_type;               /* zg_pixel_type */
+	unsigned subsample_w;
+	unsigned subsample_h;
+	int color_family;             /* 0 GREY, 1 RGB, 2 YUV */
+	int matrix_coefficients;
+	int transfer_characteristics;
+	int color_primaries;
+	unsigned depth;
+	int pixel_range;
+	int field_parity;             /* 0 progressive, 1 top, 2 bottom */
+	int chroma_location;          /* zimg_chroma_location_e values */
+	struct {
+		double left;
+		double top;
+		double width;
+		double height;
+	} active_region;
+	int alpha;                    /* 0 none, 1 straight, 2 premultiplied */
+} zg_image_format;
+
+typedef struct zg_graph_builder_params {
+	unsigned version;
+	int resample_filter;          /* luma / RGB / alpha planes */
+	double filter_param_a;
+	double filter_param_b;
+	int resample_filter_uv;       /* chroma planes */
+	double filter_param_a_uv;
+	double filter_param_b_uv;
+	int dither_type;
+	int cpu_type;
+	double nominal_peak_luminance;
+	char allow_approximate_gamma;
+	char scene_referred;
+	char chromatic_adaptation;
+} zg_graph_builder_params;
+
+/* Buffer descriptors as zimg_image_buffer(_const) (zimg.h:387-433); only whole
+ * planes (mask == ZG_BUFFER_MAX) are accepted. */
+#define ZG_BUFFER_MAX (~0U)
+typedef struct zg_image_buffer_const {
+	unsigned version;
+	struct {
+		const void *data;
+		ptrdiff_t stride;
+		unsigned mask;
+	} plane[4];
+} zg_image_buffer_const;
+
+typedef struct zg_image_buffer {
+	unsigned version;
+	struct {
+		void *data;
+		ptrdiff_t stride;
+		unsigned mask;
+	} plane[4];
+} zg_image_buffer;
+
+typedef struct zg_graph zg_graph;
+
+/* API version numbers as ZIMG_MAKE_API_VERSION (zimg.h:30-38). */
+#define ZG_MAKE_API_VERSION(x, y) (((x) << 8) | (y))
+#define ZG_ZIMG_API_VERSION ZG_MAKE_API_VERSION(2, 4)
+
+ZG_API void zg_image_format_default(zg_image_format *ptr, unsigned version);
+ZG_API void zg_graph_builder_params_default(zg_graph_builder_params *ptr, unsigned version);
+ZG_API zg_graph *zg_graph_build(const zg_image_format *src_format, const zg_image_format *dst_format,
+                         const zg_graph_builder_params *params);
+ZG_API void zg_graph_free(zg_graph *g);
+ZG_API zg_error_code zg_graph_get_tmp_size(const zg_graph *g, size_t *out);
+ZG_API zg_error_code zg_graph_process(const zg_graph *g, const zg_image_buffer_const *src, const zg_image_buffer *dst,
+                               void *tmp, zg_stream stream);
+/* Per-plane resize parameters the builder chose (as zimg's FilterObserver
+ * reports them, graphbuilder.h:45-64); returns 0 passes for a plane copied
+ * unchanged. plane in 0..3. */
+ZG_API zg_error_code zg_graph_get_plane_params(const zg_graph *g, int plane, zg_resize_params *out, int *present);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* ZIMG_GB300_H_ */

@@ -1,0 +1,104 @@
+"""CPU checks of the C ABI: the library loads, exports every declared symbol,
+and its host-only entry points (planning, errors) behave like zimg's."""
+import ctypes as C
+import math
+import os
+import re
+import threading
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "zimg_gb300.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"^ZG_API\s+[\w\s\*]*?\b(zg_\w+)\s*\(", text, flags=re.M)))
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    for must in ("zg_compute_filter", "zg_resize_pass_create", "zg_resize_pass_process", "zg_resize_create",
+                 "zg_resize_process", "zg_batch_create", "zg_batch_process", "zg_graph_build", "zg_graph_process",
+                 "zg_get_last_error"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    for name in declared_functions():
+        assert hasattr(lib, name), name
+
+
+def test_ctypes_binding_covers_header(lib):
+    from zimg_gb300 import capi
+    bound = {n for n, _, _ in capi.SIGNATURES}
+    assert bound == set(declared_functions())
+
+
+def test_struct_layouts_match_header(lib):
+    """The ctypes mirrors have the C layout (compiled check against the header)."""
+    import subprocess
+    import tempfile
+    from zimg_gb300 import capi
+    src = r'''
+#include <stdio.h>
+#include <stddef.h>
+#include "zimg_gb300.h"
+int main(void) {
+  printf("%zu %zu %zu %zu %zu %zu %zu\n", sizeof(zg_pass_params), sizeof(zg_resize_params), sizeof(zg_batch_io),
+         sizeof(zg_image_format), sizeof(zg_graph_builder_params), sizeof(zg_image_buffer),
+         offsetof(zg_image_format, active_region));
+  return 0;
+}
+'''
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "t.c")
+        open(c, "w").write(src)
+        exe = os.path.join(d, "t")
+        subprocess.check_call(["gcc", "-std=c11", "-I", os.path.join(ROOT, "include"), c, "-o", exe])
+        got = [int(x) for x in subprocess.check_output([exe]).split()]
+    want = [C.sizeof(capi.PassParams), C.sizeof(capi.ResizeParams), C.sizeof(capi.BatchIO),
+            C.sizeof(capi.ImageFormat), C.sizeof(capi.GraphBuilderParams), C.sizeof(capi.ImageBuffer),
+            capi.ImageFormat.active_region.offset]
+    assert got == want
+
+
+def test_errors_match_zimg_codes(lib):
+    import zimg_gb300 as zg
+    with pytest.raises(zg.ZimgError) as e:
+        zg.compute_filter("lanczos", 100, 50, a=16)  # filter.cpp:232-238
+    assert e.value.code == 2048  # ILLEGAL_ARGUMENT
+    with pytest.raises(zg.ZimgError) as e:
+        zg.compute_filter(99, 100, 50)
+    assert e.value.code == 2049  # ENUM_OUT_OF_RANGE
+    with pytest.raises(zg.ZimgError) as e:
+        zg.compute_filter("bilinear", 0, 50)
+    assert e.value.code == 2050  # INVALID_IMAGE_SIZE
+
+
+def test_last_error_is_thread_local(lib):
+    import zimg_gb300 as zg
+    from zimg_gb300 import capi
+    lib.zg_clear_last_error()
+    with pytest.raises(zg.ZimgError):
+        zg.compute_filter("lanczos", 100, 50, a=16)
+    seen = {}
+
+    def other():
+        seen["code"] = capi.last_error()[0]
+
+    t = threading.Thread(target=other)
+    t.start()
+    t.join()
+    assert seen["code"] == 0
+    assert capi.last_error()[0] == 2048
+    lib.zg_clear_last_error()
+    assert capi.last_error() == (0, "")
+
+
+def test_version(lib):
+    a, b, c = C.c_uint(), C.c_uint(), C.c_uint()
+    lib.zg_get_version_info(C.byref(a), C.byref(b), C.byref(c))
+    assert (a.value, b.value) == (1, 0)

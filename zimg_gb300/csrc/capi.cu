@@ -1,0 +1,367 @@
+// C ABI: errors, filter tables, single passes and two-pass conversions.
+#include "capi_common.h"
+
+#include <algorithm>
+#include <climits>
+
+namespace {
+
+thread_local int g_last_code = ZG_ERROR_SUCCESS;
+thread_local std::string g_last_msg;
+
+} // namespace
+
+namespace zg {
+
+void set_last_error(int code, const std::string &msg)
+{
+	g_last_code = code;
+	g_last_msg = msg;
+}
+
+Sample sample_of(int pixel_type)
+{
+	if (pixel_type == ZG_PIXEL_WORD)
+		return Sample::U16;
+	if (pixel_type == ZG_PIXEL_FLOAT)
+		return Sample::F32;
+	if (pixel_type == ZG_PIXEL_BYTE || pixel_type == ZG_PIXEL_HALF)
+		throw Error(kErrUnsupported, "pixel type not supported by the resize path (WORD or FLOAT)");
+	throw Error(kErrEnumOutOfRange, "unrecognized pixel type");
+}
+
+unsigned bytes_of(Sample s)
+{
+	return s == Sample::U16 ? 2 : 4;
+}
+
+int current_device()
+{
+	int d = 0;
+	cuda_check(cudaGetDevice(&d), "cudaGetDevice");
+	return d;
+}
+
+void DevicePass::upload()
+{
+	const FilterTable &t = table;
+	const size_t n = static_cast<size_t>(t.width) * t.rows;
+	auto up = [](size_t x) { return (x + 255) & ~static_cast<size_t>(255); };
+	const size_t off_f32 = up(t.rows * sizeof(unsigned));
+	const size_t off_i16 = off_f32 + up(n * sizeof(float));
+	const size_t off_bias = off_i16 + up(n * sizeof(int16_t));
+	const size_t total = off_bias + up(t.rows * sizeof(int32_t));
+
+	std::vector<int32_t> bias(t.rows);
+	for (unsigned i = 0; i < t.rows; ++i) {
+		int64_t sum = 0;
+		for (unsigned k = 0; k < t.width; ++k)
+			sum += t.i16[static_cast<size_t>(i) * t.width + k];
+		bias[i] = static_cast<int32_t>(static_cast<uint32_t>(static_cast<uint64_t>(-32768 * sum)));
+	}
+
+	std::vector<unsigned char> host(total, 0);
+	std::memcpy(host.data(), t.left.data(), t.rows * sizeof(unsigned));
+	std::memcpy(host.data() + off_f32, t.f32.data(), n * sizeof(float));
+	std::memcpy(host.data() + off_i16, t.i16.data(), n * sizeof(int16_t));
+	std::memcpy(host.data() + off_bias, bias.data(), t.rows * sizeof(int32_t));
+
+	storage.reset(total);
+	cuda_check(cudaMemcpy(storage.get(), host.data(), total, cudaMemcpyHostToDevice), "upload taps");
+
+	unsigned char *base = static_cast<unsigned char *>(storage.get());
+	tables.left = reinterpret_cast<const unsigned *>(base);
+	tables.f32 = reinterpret_cast<const float *>(base + off_f32);
+	tables.i16 = reinterpret_cast<const int16_t *>(base + off_i16);
+	tables.bias = reinterpret_cast<const int32_t *>(base + off_bias);
+	tables.width = t.width;
+	tables.rows = t.rows;
+	tables.input_width = t.input_width;
+}
+
+std::unique_ptr<DevicePass> make_device_pass(const PassSpec &s)
+{
+	if (!s.src_w || !s.src_h || !s.dst_dim)
+		throw Error(kErrInvalidImageSize, "image dimensions must be non-zero");
+	if (s.sample == Sample::U16 && (s.depth < 1 || s.depth > 16))
+		throw Error(kErrBitDepthOverflow, "bit depth exceeds limits of type");
+
+	Kernel k(s.filter, s.a, s.b);
+	auto p = std::make_unique<DevicePass>();
+	const unsigned src_dim = s.horizontal ? s.src_w : s.src_h;
+	p->table = compute_filter(k, src_dim, s.dst_dim, s.shift, default_extent(s.subwidth, src_dim));
+	p->horizontal = s.horizontal;
+	p->sample = s.sample;
+	p->pixel_max = s.sample == Sample::U16 ? static_cast<int32_t>((1UL << s.depth) - 1) : 0;
+	p->src_w = s.src_w;
+	p->src_h = s.src_h;
+	p->dst_w = s.horizontal ? s.dst_dim : s.src_w;
+	p->dst_h = s.horizontal ? s.src_h : s.dst_dim;
+	p->upload();
+	return p;
+}
+
+} // namespace zg
+
+using namespace zg;
+
+struct zg_resize_pass {
+	int device;
+	std::unique_ptr<DevicePass> pass;
+};
+
+namespace {
+
+void check_device(int device)
+{
+	if (current_device() != device)
+		throw Error(kErrLogic, "object used on a different device than the one it was created on");
+}
+
+void run_pass(const DevicePass &p, const void *src, ptrdiff_t ss, void *dst, ptrdiff_t ds, cudaStream_t stream)
+{
+	PassLaunch l{};
+	l.t = p.tables;
+	l.horizontal = p.horizontal;
+	l.sample = p.sample;
+	l.pixel_max = p.pixel_max;
+	l.lines = p.horizontal ? p.src_h : p.src_w;
+	l.src = src;
+	l.src_stride = ss;
+	l.dst = dst;
+	l.dst_stride = ds;
+	cuda_check(launch_pass(l, stream), "resize pass launch");
+}
+
+void check_plane(const void *p, ptrdiff_t stride, unsigned w, Sample s, const char *what)
+{
+	if (!p)
+		throw Error(kErrIllegalArgument, std::string(what) + " is null");
+	if (stride < static_cast<ptrdiff_t>(w) * static_cast<ptrdiff_t>(bytes_of(s)))
+		throw Error(kErrIllegalArgument, std::string(what) + " stride smaller than a line");
+	if (reinterpret_cast<uintptr_t>(p) % bytes_of(s) || stride % bytes_of(s))
+		throw Error(kErrIllegalArgument, std::string(what) + " not aligned to the sample size");
+}
+
+} // namespace
+
+struct zg_resize {
+	int device;
+	zg_resize_params params;
+	int num_passes = 0;
+	bool first_horizontal = false;
+	bool fused = false;
+	std::unique_ptr<DevicePass> pass[2];
+	ptrdiff_t tmp_stride = 0;
+	size_t tmp_size = 0;
+	Sample sample = Sample::F32;
+};
+
+extern "C" {
+
+zg_error_code zg_get_last_error(char *err_msg, size_t n)
+{
+	if (err_msg && n) {
+		std::strncpy(err_msg, g_last_msg.c_str(), n - 1);
+		err_msg[n - 1] = '\0';
+	}
+	return static_cast<zg_error_code>(g_last_code);
+}
+
+void zg_clear_last_error(void)
+{
+	g_last_code = ZG_ERROR_SUCCESS;
+	g_last_msg.clear();
+}
+
+void zg_get_version_info(unsigned *major, unsigned *minor, unsigned *micro)
+{
+	if (major) *major = ZG_API_VERSION_MAJOR;
+	if (minor) *minor = ZG_API_VERSION_MINOR;
+	if (micro) *micro = 0;
+}
+
+zg_error_code zg_compute_filter(zg_resample_filter filter, double param_a, double param_b, unsigned src_dim,
+                                unsigned dst_dim, double shift, double width, unsigned *filter_width,
+                                unsigned *filter_rows, float *f32, int16_t *i16, unsigned *left)
+{
+	return guarded([&] {
+		if (!filter_width || !filter_rows)
+			throw Error(kErrIllegalArgument, "null output pointer");
+		Kernel k(filter, param_a, param_b);
+		FilterTable t = compute_filter(k, src_dim, dst_dim, shift, default_extent(width, src_dim));
+		*filter_width = t.width;
+		*filter_rows = t.rows;
+		if (f32) {
+			if (!i16 || !left)
+				throw Error(kErrIllegalArgument, "null output pointer");
+			std::memcpy(f32, t.f32.data(), t.f32.size() * sizeof(float));
+			std::memcpy(i16, t.i16.data(), t.i16.size() * sizeof(int16_t));
+			std::memcpy(left, t.left.data(), t.left.size() * sizeof(unsigned));
+		}
+	});
+}
+
+zg_error_code zg_resize_pass_create(const zg_pass_params *params, zg_resize_pass **out)
+{
+	return guarded([&] {
+		if (!params || !out)
+			throw Error(kErrIllegalArgument, "null pointer");
+		*out = nullptr;
+		PassSpec s{ params->src_width, params->src_height, sample_of(params->pixel_type), params->depth,
+		            params->horizontal != 0, params->dst_dim, params->filter, params->filter_param_a,
+		            params->filter_param_b, params->shift, params->subwidth };
+		auto r = std::make_unique<zg_resize_pass>();
+		r->device = current_device();
+		r->pass = make_device_pass(s);
+		*out = r.release();
+	});
+}
+
+void zg_resize_pass_free(zg_resize_pass *pass)
+{
+	delete pass;
+}
+
+zg_error_code zg_resize_pass_get_output(const zg_resize_pass *pass, unsigned *width, unsigned *height)
+{
+	return guarded([&] {
+		if (!pass)
+			throw Error(kErrIllegalArgument, "null pointer");
+		if (width) *width = pass->pass->dst_w;
+		if (height) *height = pass->pass->dst_h;
+	});
+}
+
+zg_error_code zg_resize_pass_process(const zg_resize_pass *pass, const void *src, ptrdiff_t src_stride, void *dst,
+                                     ptrdiff_t dst_stride, zg_stream stream)
+{
+	return guarded([&] {
+		if (!pass)
+			throw Error(kErrIllegalArgument, "null pointer");
+		check_device(pass->device);
+		const DevicePass &p = *pass->pass;
+		check_plane(src, src_stride, p.src_w, p.sample, "src");
+		check_plane(dst, dst_stride, p.dst_w, p.sample, "dst");
+		run_pass(p, src, src_stride, dst, dst_stride, reinterpret_cast<cudaStream_t>(stream));
+	});
+}
+
+void zg_resize_params_default(zg_resize_params *p)
+{
+	if (!p)
+		return;
+	std::memset(p, 0, sizeof(*p));
+	p->pixel_type = ZG_PIXEL_FLOAT;
+	p->depth = 32;
+	p->filter = ZG_RESIZE_BICUBIC;
+	p->filter_param_a = NAN;
+	p->filter_param_b = NAN;
+	p->subwidth = NAN;
+	p->subheight = NAN;
+	p->engine = ZG_ENGINE_AUTO;
+	p->allow_fusion = 1;
+}
+
+zg_error_code zg_resize_create(const zg_resize_params *params, zg_resize **out)
+{
+	return guarded([&] {
+		if (!params || !out)
+			throw Error(kErrIllegalArgument, "null pointer");
+		*out = nullptr;
+		const zg_resize_params &q = *params;
+		if (!q.src_width || !q.src_height || !q.dst_width || !q.dst_height)
+			throw Error(kErrInvalidImageSize, "image dimensions must be non-zero");
+		auto r = std::make_unique<zg_resize>();
+		r->device = current_device();
+		r->params = q;
+		r->sample = sample_of(q.pixel_type);
+		const double subw = default_extent(q.subwidth, q.src_width);
+		const double subh = default_extent(q.subheight, q.src_height);
+		r->params.subwidth = subw;
+		r->params.subheight = subh;
+		if (r->sample == Sample::U16 && (q.depth < 1 || q.depth > 16))
+			throw Error(kErrBitDepthOverflow, "bit depth exceeds limits of type");
+		// Kernel construction validates the filter even when no pass is needed.
+		Kernel probe(q.filter, q.filter_param_a, q.filter_param_b);
+		(void)probe;
+
+		bool order[2] = { false, false };
+		r->num_passes = plan_pass_order(q.src_width, q.src_height, q.dst_width, q.dst_height, q.shift_w, q.shift_h,
+		                                subw, subh, order);
+		r->first_horizontal = r->num_passes ? order[0] : false;
+
+		unsigned cur_w = q.src_width, cur_h = q.src_height;
+		for (int p = 0; p < r->num_passes; ++p) {
+			const bool h = order[p];
+			PassSpec s{ cur_w, cur_h, r->sample, q.depth, h, h ? q.dst_width : q.dst_height, q.filter,
+			            q.filter_param_a, q.filter_param_b, h ? q.shift_w : q.shift_h, h ? subw : subh };
+			r->pass[p] = make_device_pass(s);
+			cur_w = r->pass[p]->dst_w;
+			cur_h = r->pass[p]->dst_h;
+		}
+		if (r->num_passes == 2) {
+			const DevicePass &p0 = *r->pass[0];
+			r->tmp_stride = static_cast<ptrdiff_t>((static_cast<size_t>(p0.dst_w) * bytes_of(r->sample) + 255) & ~static_cast<size_t>(255));
+			r->tmp_size = static_cast<size_t>(r->tmp_stride) * p0.dst_h;
+		}
+		*out = r.release();
+	});
+}
+
+void zg_resize_free(zg_resize *r)
+{
+	delete r;
+}
+
+zg_error_code zg_resize_get_tmp_size(const zg_resize *r, size_t *out)
+{
+	return guarded([&] {
+		if (!r || !out)
+			throw Error(kErrIllegalArgument, "null pointer");
+		*out = r->tmp_size;
+	});
+}
+
+zg_error_code zg_resize_get_info(const zg_resize *r, int *num_passes, int *first_horizontal, int *fused)
+{
+	return guarded([&] {
+		if (!r)
+			throw Error(kErrIllegalArgument, "null pointer");
+		if (num_passes) *num_passes = r->num_passes;
+		if (first_horizontal) *first_horizontal = r->first_horizontal;
+		if (fused) *fused = r->fused;
+	});
+}
+
+zg_error_code zg_resize_process(const zg_resize *r, const void *src, ptrdiff_t src_stride, void *dst,
+                                ptrdiff_t dst_stride, void *tmp, zg_stream stream)
+{
+	return guarded([&] {
+		if (!r)
+			throw Error(kErrIllegalArgument, "null pointer");
+		check_device(r->device);
+		cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+		const zg_resize_params &q = r->params;
+		check_plane(src, src_stride, q.src_width, r->sample, "src");
+		check_plane(dst, dst_stride, q.dst_width, r->sample, "dst");
+		if (r->num_passes == 0) {
+			cuda_check(cudaMemcpy2DAsync(dst, dst_stride, src, src_stride,
+			                             static_cast<size_t>(q.dst_width) * bytes_of(r->sample), q.dst_height,
+			                             cudaMemcpyDeviceToDevice, st), "plane copy");
+			return;
+		}
+		if (r->num_passes == 1) {
+			run_pass(*r->pass[0], src, src_stride, dst, dst_stride, st);
+			return;
+		}
+		if (!tmp)
+			throw Error(kErrIllegalArgument, "tmp buffer required (zg_resize_get_tmp_size)");
+		if (reinterpret_cast<uintptr_t>(tmp) % 256)
+			throw Error(kErrIllegalArgument, "tmp buffer must be 256-byte aligned");
+		run_pass(*r->pass[0], src, src_stride, tmp, r->tmp_stride, st);
+		run_pass(*r->pass[1], tmp, r->tmp_stride, dst, dst_stride, st);
+	});
+}
+
+} // extern "C"

@@ -1,0 +1,118 @@
+// Shared host-side pieces of the C ABI: error capture, device buffers and the
+// device copy of a pass's tap tables.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "filter_plan.h"
+#include "kernels.h"
+#include "zimg_gb300.h"
+
+namespace zg {
+
+// Record the last error on this thread (zimg.cpp:33-34,61-105).
+void set_last_error(int code, const std::string &msg);
+
+// Run f; map exceptions to zg_error_code and the thread-local message.
+template <class F>
+zg_error_code guarded(F &&f) noexcept
+{
+	try {
+		f();
+		return ZG_ERROR_SUCCESS;
+	} catch (const Error &e) {
+		set_last_error(e.code, e.what());
+		return static_cast<zg_error_code>(e.code);
+	} catch (const std::bad_alloc &) {
+		set_last_error(ZG_ERROR_OUT_OF_MEMORY, "out of memory");
+		return ZG_ERROR_OUT_OF_MEMORY;
+	} catch (const std::exception &e) {
+		set_last_error(ZG_ERROR_UNKNOWN, e.what());
+		return ZG_ERROR_UNKNOWN;
+	} catch (...) {
+		set_last_error(ZG_ERROR_UNKNOWN, "unknown error");
+		return ZG_ERROR_UNKNOWN;
+	}
+}
+
+inline void cuda_check(cudaError_t e, const char *what)
+{
+	if (e == cudaErrorMemoryAllocation)
+		throw Error(kErrOutOfMemory, std::string(what) + ": " + cudaGetErrorString(e));
+	if (e != cudaSuccess)
+		throw Error(kErrUnknown, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// Owned device allocation made at plan-creation time.
+class DeviceBuffer {
+public:
+	DeviceBuffer() = default;
+	explicit DeviceBuffer(size_t bytes) { reset(bytes); }
+	~DeviceBuffer() { release(); }
+	DeviceBuffer(const DeviceBuffer &) = delete;
+	DeviceBuffer &operator=(const DeviceBuffer &) = delete;
+
+	void reset(size_t bytes)
+	{
+		release();
+		if (bytes)
+			cuda_check(cudaMalloc(&ptr_, bytes), "cudaMalloc");
+		size_ = bytes;
+	}
+	void release()
+	{
+		if (ptr_)
+			cudaFree(ptr_);
+		ptr_ = nullptr;
+		size_ = 0;
+	}
+	void *get() const { return ptr_; }
+	size_t size() const { return size_; }
+
+private:
+	void *ptr_ = nullptr;
+	size_t size_ = 0;
+};
+
+// Device copy of one FilterTable plus its geometry.
+struct DevicePass {
+	FilterTable table;        // host copy (kept for introspection)
+	DeviceBuffer storage;     // left | f32 | i16 | bias
+	PassTables tables{};
+	bool horizontal = false;
+	Sample sample = Sample::F32;
+	int32_t pixel_max = 0;
+	unsigned src_w = 0, src_h = 0, dst_w = 0, dst_h = 0;
+
+	void upload();
+};
+
+struct PassSpec {
+	unsigned src_w, src_h;
+	Sample sample;
+	unsigned depth;
+	bool horizontal;
+	unsigned dst_dim;
+	int filter;
+	double a, b;
+	double shift, subwidth;
+};
+
+std::unique_ptr<DevicePass> make_device_pass(const PassSpec &s);
+
+inline double default_extent(double v, unsigned dim)
+{
+	return (std::isnan(v) || v <= 0.0) ? static_cast<double>(dim) : v;
+}
+
+Sample sample_of(int pixel_type);
+unsigned bytes_of(Sample s);
+int current_device();
+
+} // namespace zg

@@ -1,0 +1,425 @@
+// C ABI: the resize-only subset of zimg's format-level graph.
+//
+// The per-plane geometry follows zimg's graph builder: chroma planes from luma
+// (graphbuilder.cpp:331-346), siting and field-parity offsets
+// (graphbuilder.cpp:65-188,348-366), active-region defaults (zimg.cpp:388-397),
+// subrectangle copies (graphbuilder.cpp:540-573) and the shift / subwidth
+// mapping of resize_plane (graphbuilder.cpp:769-776).
+#include "capi_common.h"
+
+#include <cfloat>
+#include <cmath>
+
+using namespace zg;
+
+namespace {
+
+enum { PLANE_Y = 0, PLANE_U = 1, PLANE_V = 2, PLANE_A = 3 };
+enum { COLOR_GREY = 0, COLOR_RGB = 1, COLOR_YUV = 2 };
+enum { PARITY_PROGRESSIVE = 0, PARITY_TOP = 1, PARITY_BOTTOM = 2 };
+
+struct PlaneGeom {
+	unsigned width = 0, height = 0;
+	double left = 0, top = 0, aw = 0, ah = 0;
+
+	bool operator==(const PlaneGeom &o) const
+	{
+		return width == o.width && height == o.height && left == o.left && top == o.top && aw == o.aw && ah == o.ah;
+	}
+};
+
+struct FormatState {
+	unsigned width, height;
+	int pixel_type;
+	unsigned depth;
+	unsigned subsample_w, subsample_h;
+	int color;
+	int matrix, transfer, primaries;
+	int range;
+	int parity;
+	int chroma_location;
+	int alpha;
+	PlaneGeom planes[4];
+};
+
+const unsigned kApi20 = ZG_MAKE_API_VERSION(2, 0);
+const unsigned kApi21 = ZG_MAKE_API_VERSION(2, 1);
+const unsigned kApi24 = ZG_MAKE_API_VERSION(2, 4);
+const unsigned kImageDimensionMax = 1U << 30;  // 64-bit hosts (graphbuilder.cpp:23-27)
+
+unsigned pixel_depth_max(int type)
+{
+	switch (type) {
+	case ZG_PIXEL_BYTE: return 8;
+	case ZG_PIXEL_WORD: return 16;
+	case ZG_PIXEL_HALF: return 16;
+	case ZG_PIXEL_FLOAT: return 32;
+	default: throw Error(kErrEnumOutOfRange, "unrecognized pixel type");
+	}
+}
+
+// Chroma offset from a centred sample, in chroma pixels (graphbuilder.cpp:65-110).
+double offset_w(bool left_sited, double subsampling)
+{
+	return left_sited ? -0.5 + 0.5 * subsampling : 0.0;
+}
+
+double offset_h(int loc_h, double subsampling)
+{
+	if (loc_h == 1)  // top
+		return -0.5 + 0.5 * subsampling;
+	if (loc_h == 2)  // bottom
+		return 0.5 - 0.5 * subsampling;
+	return 0.0;
+}
+
+// Field offsets relative to a progressive frame of field size
+// (graphbuilder.cpp:112-188).
+double parity_adjust(int parity, double offset)
+{
+	if (parity == PARITY_TOP)
+		return -0.25 + offset / 2;
+	if (parity == PARITY_BOTTOM)
+		return 0.25 + offset / 2;
+	return offset;
+}
+
+double luma_parity(int parity)
+{
+	return parity == PARITY_TOP ? -0.25 : (parity == PARITY_BOTTOM ? 0.25 : 0.0);
+}
+
+// zimg_chroma_location_e -> (left-sited?, vertical: 0 centre, 1 top, 2 bottom)
+// (zimg.cpp:214-236).
+void chroma_location(int loc, bool *left, int *vert)
+{
+	switch (loc) {
+	case 0: *left = true; *vert = 0; return;   // LEFT (MPEG-2)
+	case 1: *left = false; *vert = 0; return;  // CENTER
+	case 2: *left = true; *vert = 1; return;   // TOP_LEFT
+	case 3: *left = false; *vert = 1; return;  // TOP
+	case 4: *left = true; *vert = 2; return;   // BOTTOM_LEFT
+	case 5: *left = false; *vert = 2; return;  // BOTTOM
+	default: throw Error(kErrEnumOutOfRange, "unrecognized chroma location");
+	}
+}
+
+FormatState import_format(const zg_image_format &f)
+{
+	if (f.version < kApi20)
+		throw Error(kErrIllegalArgument, "API version invalid");
+	FormatState s{};
+	s.width = f.width;
+	s.height = f.height;
+	s.pixel_type = f.pixel_type;
+	s.depth = f.depth ? f.depth : pixel_depth_max(f.pixel_type);
+	s.subsample_w = f.subsample_w;
+	s.subsample_h = f.subsample_h;
+	s.color = f.color_family;
+	if (s.color < COLOR_GREY || s.color > COLOR_YUV)
+		throw Error(kErrEnumOutOfRange, "unrecognized color family");
+	s.matrix = f.matrix_coefficients;
+	s.transfer = f.transfer_characteristics;
+	s.primaries = f.color_primaries;
+	s.range = f.pixel_range;
+	if (s.range != 0 && s.range != 1)
+		throw Error(kErrEnumOutOfRange, "unrecognized pixel range");
+	s.parity = f.field_parity;
+	if (s.parity < PARITY_PROGRESSIVE || s.parity > PARITY_BOTTOM)
+		throw Error(kErrEnumOutOfRange, "unrecognized field parity");
+	s.chroma_location = f.chroma_location;
+	s.alpha = f.version >= kApi24 ? f.alpha : 0;
+	if (s.alpha < 0 || s.alpha > 2)
+		throw Error(kErrEnumOutOfRange, "unrecognized alpha type");
+
+	double al = 0.0, at = 0.0, aw = s.width, ah = s.height;
+	if (f.version >= kApi21) {
+		al = std::isnan(f.active_region.left) ? 0.0 : f.active_region.left;
+		at = std::isnan(f.active_region.top) ? 0.0 : f.active_region.top;
+		aw = std::isnan(f.active_region.width) ? static_cast<double>(s.width) : f.active_region.width;
+		ah = std::isnan(f.active_region.height) ? static_cast<double>(s.height) : f.active_region.height;
+	}
+
+	// validate_state (graphbuilder.cpp:190-235)
+	if (!s.width || !s.height)
+		throw Error(kErrInvalidImageSize, "image dimensions must be non-zero");
+	if (s.width > kImageDimensionMax || s.height > kImageDimensionMax)
+		throw Error(kErrInvalidImageSize, "image dimensions exceed implementation limit");
+	if (s.color == COLOR_GREY && (s.subsample_w || s.subsample_h))
+		throw Error(kErrGreyscaleSubsampling, "cannot subsample greyscale image");
+	if (s.color == COLOR_RGB && (s.subsample_w || s.subsample_h))
+		throw Error(kErrUnsupportedSubsampling, "subsampled RGB image not supported");
+	if (s.subsample_h > 1 && s.parity != PARITY_PROGRESSIVE)
+		throw Error(kErrUnsupportedSubsampling, "interlaced vertical subsampling greater than 2x is not supported");
+	if (s.subsample_w > 2 || s.subsample_h > 2)
+		throw Error(kErrUnsupportedSubsampling, "subsampling greater than 4x is not supported");
+	if (s.width % (1u << s.subsample_w) || s.height % (1u << s.subsample_h))
+		throw Error(kErrImageNotDivisible, "image dimensions must be divisible by subsampling factor");
+	if (s.depth > pixel_depth_max(s.pixel_type))
+		throw Error(kErrBitDepthOverflow, "bit depth exceeds limits of type");
+	if (s.pixel_type != ZG_PIXEL_FLOAT && s.pixel_type != ZG_PIXEL_HALF && s.range == 0 && s.depth < 8)
+		throw Error(kErrBitDepthOverflow, "bit depth must be at least 8 for limited range");
+	if (!std::isfinite(al) || !std::isfinite(at) || !std::isfinite(aw) || !std::isfinite(ah))
+		throw Error(kErrInvalidImageSize, "active window must be finite");
+	if (aw <= 0 || ah <= 0)
+		throw Error(kErrInvalidImageSize, "active window must be positive");
+
+	// Planes (graphbuilder.cpp:331-366).
+	PlaneGeom y{ s.width, s.height, al, at, aw, ah };
+	s.planes[PLANE_Y] = y;
+	if (s.color != COLOR_GREY) {
+		const double sw = 1.0 / (1UL << s.subsample_w);
+		const double sh = 1.0 / (1UL << s.subsample_h);
+		PlaneGeom u{ s.width >> s.subsample_w, s.height >> s.subsample_h, al * sw, at * sh, aw * sw, ah * sh };
+		s.planes[PLANE_U] = u;
+		s.planes[PLANE_V] = u;
+	}
+	if (s.alpha)
+		s.planes[PLANE_A] = s.planes[PLANE_Y];
+
+	s.planes[PLANE_Y].top -= luma_parity(s.parity);
+	if (s.color != COLOR_GREY) {
+		bool left_sited = false;
+		int vert = 0;
+		chroma_location(s.chroma_location, &left_sited, &vert);
+		const double subscale_w = static_cast<double>(s.planes[PLANE_U].width) / s.planes[PLANE_Y].width;
+		const double subscale_h = static_cast<double>(s.planes[PLANE_U].height) / s.planes[PLANE_Y].height;
+		const double ow = offset_w(left_sited, subscale_w);
+		const double oh = parity_adjust(s.parity, offset_h(vert, subscale_h));
+		for (int p : { PLANE_U, PLANE_V }) {
+			s.planes[p].left -= ow;
+			s.planes[p].top -= oh;
+		}
+	}
+	if (s.alpha)
+		s.planes[PLANE_A].top -= luma_parity(s.parity);
+	return s;
+}
+
+} // namespace
+
+struct zg_graph {
+	int device;
+	int sample_bytes;
+	struct Plane {
+		bool present = false;
+		int mode = 0;  // 0 copy, 1 copy subrectangle, 2 resize
+		unsigned w = 0, h = 0;      // output size
+		unsigned off_x = 0, off_y = 0;
+		zg_resize_params params{};
+		zg_resize *resize = nullptr;
+		size_t tmp = 0;
+	} planes[4];
+	size_t tmp_size = 0;
+
+	~zg_graph()
+	{
+		for (auto &p : planes)
+			zg_resize_free(p.resize);
+	}
+};
+
+extern "C" {
+
+void zg_image_format_default(zg_image_format *ptr, unsigned version)
+{
+	// zimg_image_format_default (zimg.cpp:595-630)
+	if (!ptr)
+		return;
+	std::memset(ptr, 0, sizeof(*ptr));
+	ptr->version = version;
+	ptr->pixel_type = -1;
+	ptr->color_family = COLOR_GREY;
+	ptr->matrix_coefficients = 2;
+	ptr->transfer_characteristics = 2;
+	ptr->color_primaries = 2;
+	ptr->pixel_range = 0;
+	ptr->field_parity = PARITY_PROGRESSIVE;
+	ptr->chroma_location = 0;
+	ptr->active_region.left = NAN;
+	ptr->active_region.top = NAN;
+	ptr->active_region.width = NAN;
+	ptr->active_region.height = NAN;
+	ptr->alpha = 0;
+}
+
+void zg_graph_builder_params_default(zg_graph_builder_params *ptr, unsigned version)
+{
+	// zimg_graph_builder_params_default (zimg.cpp:632-660)
+	if (!ptr)
+		return;
+	std::memset(ptr, 0, sizeof(*ptr));
+	ptr->version = version;
+	ptr->resample_filter = ZG_RESIZE_BICUBIC;
+	ptr->filter_param_a = NAN;
+	ptr->filter_param_b = NAN;
+	ptr->resample_filter_uv = ZG_RESIZE_BILINEAR;
+	ptr->filter_param_a_uv = NAN;
+	ptr->filter_param_b_uv = NAN;
+	ptr->dither_type = 0;
+	ptr->cpu_type = 1;
+	ptr->nominal_peak_luminance = NAN;
+}
+
+zg_graph *zg_graph_build(const zg_image_format *src_format, const zg_image_format *dst_format,
+                         const zg_graph_builder_params *params)
+{
+	zg_graph *result = nullptr;
+	guarded([&] {
+		if (!src_format || !dst_format)
+			throw Error(kErrIllegalArgument, "null pointer");
+		if (src_format->version != dst_format->version)
+			throw Error(kErrIllegalArgument, "image format versions do not match");
+		FormatState s = import_format(*src_format);
+		FormatState d = import_format(*dst_format);
+
+		zg_graph_builder_params defaults;
+		zg_graph_builder_params_default(&defaults, src_format->version);
+		const zg_graph_builder_params &gp = params ? *params : defaults;
+
+		if (s.pixel_type != d.pixel_type || s.depth != d.depth || (s.pixel_type != ZG_PIXEL_FLOAT && s.range != d.range))
+			throw Error(kErrUnsupported, "pixel format conversion is outside the resize path");
+		if (s.color != d.color || s.matrix != d.matrix || s.transfer != d.transfer || s.primaries != d.primaries)
+			throw Error(kErrNoColorspaceConversion, "colorspace conversion is outside the resize path");
+		if (s.alpha != d.alpha)
+			throw Error(kErrUnsupported, "alpha conversion is outside the resize path");
+		const Sample sample = sample_of(s.pixel_type);
+
+		auto g = std::make_unique<zg_graph>();
+		g->device = current_device();
+		g->sample_bytes = static_cast<int>(bytes_of(sample));
+
+		for (int p = 0; p < 4; ++p) {
+			const bool chroma = p == PLANE_U || p == PLANE_V;
+			if (chroma && s.color == COLOR_GREY)
+				continue;
+			if (p == PLANE_A && !s.alpha)
+				continue;
+			auto &gpl = g->planes[p];
+			gpl.present = true;
+			// RGB planes share the luma plane's conversion (graphbuilder.cpp:892-905).
+			const int q = (s.color == COLOR_RGB && chroma) ? PLANE_Y : p;
+			const PlaneGeom &sp = s.planes[q];
+			const PlaneGeom &dp = d.planes[q];
+			gpl.w = dp.width;
+			gpl.h = dp.height;
+
+			if (sp == dp) {
+				gpl.mode = 0;
+				continue;
+			}
+			// Pixel-aligned subrectangle equal to the output: plain copy
+			// (can_copy_tile, graphbuilder.cpp:540-573).
+			{
+				auto is_int = [](double x) { return std::trunc(x) == x; };
+				bool tile = !(sp.aw == sp.width || sp.ah == sp.height) &&
+				            dp.aw == dp.width && dp.ah == dp.height &&
+				            sp.aw == dp.width && sp.ah == dp.height;
+				double sl = sp.left - dp.left, st = sp.top - dp.top;
+				tile = tile && is_int(sl) && is_int(st) && sl >= 0 && st >= 0 &&
+				       sl + sp.aw <= sp.width && st + sp.ah <= sp.height;
+				if (tile) {
+					gpl.mode = 1;
+					gpl.off_x = static_cast<unsigned>(sl);
+					gpl.off_y = static_cast<unsigned>(st);
+					continue;
+				}
+			}
+			gpl.mode = 2;
+			const double scale_w = dp.aw / sp.aw;
+			const double scale_h = dp.ah / sp.ah;
+			zg_resize_params rp;
+			zg_resize_params_default(&rp);
+			rp.src_width = sp.width;
+			rp.src_height = sp.height;
+			rp.pixel_type = static_cast<zg_pixel_type>(s.pixel_type);
+			rp.depth = s.depth;
+			rp.dst_width = dp.width;
+			rp.dst_height = dp.height;
+			rp.filter = static_cast<zg_resample_filter>(chroma && s.color == COLOR_YUV ? gp.resample_filter_uv : gp.resample_filter);
+			rp.filter_param_a = chroma && s.color == COLOR_YUV ? gp.filter_param_a_uv : gp.filter_param_a;
+			rp.filter_param_b = chroma && s.color == COLOR_YUV ? gp.filter_param_b_uv : gp.filter_param_b;
+			rp.shift_w = sp.left - dp.left / scale_w;
+			rp.shift_h = sp.top - dp.top / scale_h;
+			rp.subwidth = sp.aw * (dp.width / dp.aw);
+			rp.subheight = sp.ah * (dp.height / dp.ah);
+			gpl.params = rp;
+			zg_error_code rc = zg_resize_create(&rp, &gpl.resize);
+			if (rc != ZG_ERROR_SUCCESS) {
+				char msg[256];
+				zg_get_last_error(msg, sizeof(msg));
+				throw Error(rc, msg);
+			}
+			zg_resize_get_tmp_size(gpl.resize, &gpl.tmp);
+			g->tmp_size = std::max(g->tmp_size, gpl.tmp);
+		}
+		result = g.release();
+	});
+	return result;
+}
+
+void zg_graph_free(zg_graph *g)
+{
+	delete g;
+}
+
+zg_error_code zg_graph_get_tmp_size(const zg_graph *g, size_t *out)
+{
+	return guarded([&] {
+		if (!g || !out)
+			throw Error(kErrIllegalArgument, "null pointer");
+		*out = g->tmp_size;
+	});
+}
+
+zg_error_code zg_graph_get_plane_params(const zg_graph *g, int plane, zg_resize_params *out, int *present)
+{
+	return guarded([&] {
+		if (!g || plane < 0 || plane > 3)
+			throw Error(kErrIllegalArgument, "bad plane");
+		const auto &p = g->planes[plane];
+		if (present)
+			*present = p.present ? (p.mode == 2 ? 2 : 1) : 0;
+		if (out && p.mode == 2)
+			*out = p.params;
+	});
+}
+
+zg_error_code zg_graph_process(const zg_graph *g, const zg_image_buffer_const *src, const zg_image_buffer *dst,
+                               void *tmp, zg_stream stream)
+{
+	return guarded([&] {
+		if (!g || !src || !dst)
+			throw Error(kErrIllegalArgument, "null pointer");
+		if (current_device() != g->device)
+			throw Error(kErrLogic, "graph used on a different device than the one it was created on");
+		cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+		for (int p = 0; p < 4; ++p) {
+			const auto &pl = g->planes[p];
+			if (!pl.present)
+				continue;
+			if (src->plane[p].mask != ZG_BUFFER_MAX || dst->plane[p].mask != ZG_BUFFER_MAX)
+				throw Error(kErrUnsupported, "only whole-plane buffers (mask ZG_BUFFER_MAX) are supported");
+			const char *sp = static_cast<const char *>(src->plane[p].data);
+			char *dp = static_cast<char *>(dst->plane[p].data);
+			if (!sp || !dp)
+				throw Error(kErrIllegalArgument, "null plane pointer");
+			if (pl.mode == 0 || pl.mode == 1) {
+				const char *from = sp + static_cast<ptrdiff_t>(pl.off_y) * src->plane[p].stride +
+				                   static_cast<ptrdiff_t>(pl.off_x) * g->sample_bytes;
+				cuda_check(cudaMemcpy2DAsync(dp, dst->plane[p].stride, from, src->plane[p].stride,
+				                             static_cast<size_t>(pl.w) * g->sample_bytes, pl.h,
+				                             cudaMemcpyDeviceToDevice, st), "plane copy");
+				continue;
+			}
+			zg_error_code rc = zg_resize_process(pl.resize, sp, src->plane[p].stride, dp, dst->plane[p].stride, tmp, stream);
+			if (rc != ZG_ERROR_SUCCESS) {
+				char msg[256];
+				zg_get_last_error(msg, sizeof(msg));
+				throw Error(rc, msg);
+			}
+		}
+	});
+}
+
+} // extern "C"

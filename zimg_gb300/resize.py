@@ -1,0 +1,363 @@
+"""Python mirror of zimg's resize interfaces, over the C ABI.
+
+Names and argument meaning follow the reference:
+
+* ``ResizeImplBuilder`` — src/zimg/resize/resize_impl.h:45-63 (one pass)
+* ``ResizeConversion`` — src/zimg/resize/resize.h:22-44 (zero to two passes)
+* ``compute_filter``   — src/zimg/resize/filter.h:178 (host-side tap tables)
+* ``Batch``            — many conversions in one persistent launch
+* ``Graph``            — resize-only zimg_filter_graph_build/process
+
+Device buffers are PyTorch CUDA tensors (plumbing only: memory and streams);
+every computation runs in the native library. WORD planes may be passed as
+int16 or uint16 tensors (the bytes are what matters).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import capi
+from .capi import ZimgError, check, load
+
+__all__ = ["ZimgError", "compute_filter", "FilterContext", "ResizeImplBuilder", "ResizePass", "ResizeConversion",
+           "Resize", "Batch", "Graph", "filter_id"]
+
+
+def filter_id(kind) -> int:
+    if isinstance(kind, str):
+        if kind not in capi.FILTER:
+            raise ZimgError(2049, f"unrecognized resampling filter {kind!r}")
+        return capi.FILTER[kind]
+    return int(kind)
+
+
+def _pixel_id(t) -> int:
+    if isinstance(t, str):
+        return capi.PIXEL[t]
+    return int(t)
+
+
+def _stream_handle(stream) -> int | None:
+    if stream is None:
+        import torch
+        return torch.cuda.current_stream().cuda_stream
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream
+
+
+def _plane(t):
+    """(device pointer, byte stride, width, height) of a 2-D CUDA tensor."""
+    if t.dim() != 2:
+        raise ValueError("planes are 2-D tensors [height, width]")
+    if t.stride(1) != 1:
+        raise ValueError("plane rows must be contiguous")
+    if not t.is_cuda:
+        raise ValueError("planes must be CUDA tensors")
+    return t.data_ptr(), t.stride(0) * t.element_size(), t.shape[1], t.shape[0]
+
+
+@dataclass
+class FilterContext:
+    """zimg's FilterContext (filter.h:133-165) with rows packed densely."""
+    filter_width: int
+    filter_rows: int
+    data: np.ndarray       # float32 [rows, width]
+    data_i16: np.ndarray   # int16   [rows, width]
+    left: np.ndarray       # uint32  [rows]
+
+
+def compute_filter(kind, src_dim: int, dst_dim: int, shift: float = 0.0, width: float | None = None,
+                   a: float = math.nan, b: float = math.nan) -> FilterContext:
+    lib = load()
+    w = float(src_dim if width is None else width)
+    fw, rows = C.c_uint(), C.c_uint()
+    check(lib.zg_compute_filter(filter_id(kind), a, b, src_dim, dst_dim, shift, w, C.byref(fw), C.byref(rows),
+                                None, None, None))
+    f32 = np.zeros((rows.value, fw.value), np.float32)
+    i16 = np.zeros((rows.value, fw.value), np.int16)
+    left = np.zeros(rows.value, np.uint32)
+    check(lib.zg_compute_filter(filter_id(kind), a, b, src_dim, dst_dim, shift, w, C.byref(fw), C.byref(rows),
+                                f32.ctypes.data, i16.ctypes.data, left.ctypes.data))
+    return FilterContext(fw.value, rows.value, f32, i16, left)
+
+
+class _Builder:
+    def _set(self, name, value):
+        setattr(self, name, value)
+        return self
+
+
+class ResizePass:
+    """One ResizeImplH / ResizeImplV equivalent on the GPU."""
+
+    def __init__(self, handle):
+        self._h = handle
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            load().zg_resize_pass_free(self._h)
+            self._h = None
+
+    @property
+    def output_size(self) -> tuple[int, int]:
+        w, h = C.c_uint(), C.c_uint()
+        check(load().zg_resize_pass_get_output(self._h, C.byref(w), C.byref(h)))
+        return w.value, h.value
+
+    def process(self, src, dst, stream=None) -> None:
+        sp, ss, _, _ = _plane(src)
+        dp, ds, _, _ = _plane(dst)
+        check(load().zg_resize_pass_process(self._h, sp, ss, dp, ds, _stream_handle(stream)))
+
+
+class ResizeImplBuilder(_Builder):
+    """ResizeImplBuilder{src_width, src_height, type} (resize_impl.h:45-63)."""
+
+    def __init__(self, src_width: int, src_height: int, pixel_type="float"):
+        self.src_width, self.src_height, self.type = src_width, src_height, _pixel_id(pixel_type)
+        self.horizontal, self.dst_dim, self.depth = False, 0, 16 if self.type == 1 else 32
+        self.filter, self.param_a, self.param_b = 2, math.nan, math.nan
+        self.shift, self.subwidth, self.engine = 0.0, math.nan, "auto"
+
+    def set_horizontal(self, v: bool): return self._set("horizontal", bool(v))
+    def set_dst_dim(self, v: int): return self._set("dst_dim", int(v))
+    def set_depth(self, v: int): return self._set("depth", int(v))
+    def set_shift(self, v: float): return self._set("shift", float(v))
+    def set_subwidth(self, v: float): return self._set("subwidth", float(v))
+    def set_engine(self, v: str): return self._set("engine", v)
+
+    def set_filter(self, kind, a: float = math.nan, b: float = math.nan):
+        self.filter, self.param_a, self.param_b = filter_id(kind), float(a), float(b)
+        return self
+
+    def create(self) -> ResizePass:
+        p = capi.PassParams(self.src_width, self.src_height, self.type, self.depth, int(self.horizontal),
+                            self.dst_dim, self.filter, self.param_a, self.param_b, self.shift, self.subwidth,
+                            capi.ENGINE[self.engine])
+        h = C.c_void_p()
+        check(load().zg_resize_pass_create(C.byref(p), C.byref(h)))
+        return ResizePass(h.value)
+
+
+class Resize:
+    """The created conversion (what ResizeConversion::create returns)."""
+
+    def __init__(self, handle, params: capi.ResizeParams):
+        self._h = handle
+        self.params = params
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            load().zg_resize_free(self._h)
+            self._h = None
+
+    @property
+    def handle(self) -> int:
+        return self._h
+
+    @property
+    def tmp_size(self) -> int:
+        n = C.c_size_t()
+        check(load().zg_resize_get_tmp_size(self._h, C.byref(n)))
+        return n.value
+
+    @property
+    def info(self) -> dict:
+        n, f, fu = C.c_int(), C.c_int(), C.c_int()
+        check(load().zg_resize_get_info(self._h, C.byref(n), C.byref(f), C.byref(fu)))
+        return {"num_passes": n.value, "first_horizontal": bool(f.value), "fused": bool(fu.value)}
+
+    def alloc_tmp(self, device=None):
+        import torch
+        n = self.tmp_size
+        return torch.empty(max(n, 1), dtype=torch.uint8, device=device or "cuda") if n else None
+
+    def process(self, src, dst, tmp=None, stream=None) -> None:
+        sp, ss, _, _ = _plane(src)
+        dp, ds, _, _ = _plane(dst)
+        if tmp is None and self.tmp_size:
+            tmp = self.alloc_tmp(src.device)
+        tp = tmp.data_ptr() if tmp is not None else None
+        check(load().zg_resize_process(self._h, sp, ss, dp, ds, tp, _stream_handle(stream)))
+
+
+def _resize_params(src_width, src_height, pixel_type, depth, dst_width, dst_height, kind, a, b, shift_w, shift_h,
+                   subwidth, subheight, engine="auto", allow_fusion=True) -> capi.ResizeParams:
+    p = capi.ResizeParams()
+    load().zg_resize_params_default(C.byref(p))
+    p.src_width, p.src_height, p.pixel_type = src_width, src_height, _pixel_id(pixel_type)
+    p.depth = depth if depth is not None else (16 if p.pixel_type == 1 else 32)
+    p.dst_width, p.dst_height = dst_width, dst_height
+    p.filter, p.filter_param_a, p.filter_param_b = filter_id(kind), a, b
+    p.shift_w, p.shift_h = shift_w, shift_h
+    p.subwidth = math.nan if subwidth is None else subwidth
+    p.subheight = math.nan if subheight is None else subheight
+    p.engine = capi.ENGINE[engine]
+    p.allow_fusion = int(bool(allow_fusion))
+    return p
+
+
+class ResizeConversion(_Builder):
+    """ResizeConversion{src_width, src_height, type} (resize.h:22-44)."""
+
+    def __init__(self, src_width: int, src_height: int, pixel_type="float"):
+        self.src_width, self.src_height, self.type = src_width, src_height, _pixel_id(pixel_type)
+        self.depth = 16 if self.type == 1 else 32
+        self.filter, self.param_a, self.param_b = 2, math.nan, math.nan
+        self.dst_width, self.dst_height = src_width, src_height
+        self.shift_w = self.shift_h = 0.0
+        self.subwidth = self.subheight = None
+        self.engine, self.fusion = "auto", True
+
+    def set_depth(self, v: int): return self._set("depth", int(v))
+    def set_dst_width(self, v: int): return self._set("dst_width", int(v))
+    def set_dst_height(self, v: int): return self._set("dst_height", int(v))
+    def set_shift_w(self, v: float): return self._set("shift_w", float(v))
+    def set_shift_h(self, v: float): return self._set("shift_h", float(v))
+    def set_subwidth(self, v: float): return self._set("subwidth", float(v))
+    def set_subheight(self, v: float): return self._set("subheight", float(v))
+    def set_engine(self, v: str): return self._set("engine", v)
+    def set_fusion(self, v: bool): return self._set("fusion", bool(v))
+
+    def set_filter(self, kind, a: float = math.nan, b: float = math.nan):
+        self.filter, self.param_a, self.param_b = filter_id(kind), float(a), float(b)
+        return self
+
+    def params(self) -> capi.ResizeParams:
+        return _resize_params(self.src_width, self.src_height, self.type, self.depth, self.dst_width,
+                              self.dst_height, self.filter, self.param_a, self.param_b, self.shift_w, self.shift_h,
+                              self.subwidth, self.subheight, self.engine, self.fusion)
+
+    def create(self) -> Resize:
+        p = self.params()
+        h = C.c_void_p()
+        check(load().zg_resize_create(C.byref(p), C.byref(h)))
+        return Resize(h.value, p)
+
+
+class Batch:
+    """Many conversions of uneven sizes, launched together."""
+
+    def __init__(self, conversions: list[ResizeConversion]):
+        arr = (capi.ResizeParams * len(conversions))(*[c.params() for c in conversions])
+        h = C.c_void_p()
+        check(load().zg_batch_create(arr, len(conversions), C.byref(h)))
+        self._h = h.value
+        self.n = len(conversions)
+        self._tmp = None
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            load().zg_batch_free(self._h)
+            self._h = None
+
+    @property
+    def tmp_size(self) -> int:
+        n = C.c_size_t()
+        check(load().zg_batch_get_tmp_size(self._h, C.byref(n)))
+        return n.value
+
+    @property
+    def launch_count(self) -> int:
+        n = C.c_uint()
+        check(load().zg_batch_get_launch_count(self._h, C.byref(n)))
+        return n.value
+
+    def set_io(self, srcs, dsts, stream=None) -> None:
+        if len(srcs) != self.n or len(dsts) != self.n:
+            raise ValueError("one src and one dst per job")
+        io = (capi.BatchIO * self.n)()
+        for i, (s, d) in enumerate(zip(srcs, dsts)):
+            sp, ss, _, _ = _plane(s)
+            dp, ds, _, _ = _plane(d)
+            io[i] = capi.BatchIO(sp, ss, dp, ds)
+        check(load().zg_batch_set_io(self._h, io, _stream_handle(stream)))
+
+    def _tmp_ptr(self, tmp):
+        if tmp is None and self.tmp_size:
+            if self._tmp is None:
+                import torch
+                self._tmp = torch.empty(self.tmp_size, dtype=torch.uint8, device="cuda")
+            tmp = self._tmp
+        return tmp.data_ptr() if tmp is not None else None
+
+    def process(self, tmp=None, stream=None) -> None:
+        check(load().zg_batch_process(self._h, self._tmp_ptr(tmp), _stream_handle(stream)))
+
+    def process_graph(self, tmp=None, stream=None) -> None:
+        check(load().zg_batch_process_graph(self._h, self._tmp_ptr(tmp), _stream_handle(stream)))
+
+
+def image_format(width, height, pixel_type="float", **kw) -> capi.ImageFormat:
+    """zimg_image_format with zimg's defaults (zimg.cpp:595-630), then kw."""
+    f = capi.ImageFormat()
+    load().zg_image_format_default(C.byref(f), capi.API_VERSION_2_4)
+    f.width, f.height, f.pixel_type = width, height, _pixel_id(pixel_type)
+    for k, v in kw.items():
+        if k == "active_region":
+            f.active_region = capi.ActiveRegion(*v)
+        else:
+            setattr(f, k, v)
+    return f
+
+
+def graph_params(**kw) -> capi.GraphBuilderParams:
+    p = capi.GraphBuilderParams()
+    load().zg_graph_builder_params_default(C.byref(p), capi.API_VERSION_2_4)
+    for k, v in kw.items():
+        if k in ("resample_filter", "resample_filter_uv"):
+            v = filter_id(v)
+        setattr(p, k, v)
+    return p
+
+
+class Graph:
+    """Resize-only zimg_filter_graph (zimg.h:507,550-552,679)."""
+
+    def __init__(self, src_format: capi.ImageFormat, dst_format: capi.ImageFormat,
+                 params: capi.GraphBuilderParams | None = None):
+        lib = load()
+        h = lib.zg_graph_build(C.byref(src_format), C.byref(dst_format), C.byref(params) if params else None)
+        if not h:
+            code, msg = capi.last_error()
+            raise ZimgError(code, msg)
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            load().zg_graph_free(self._h)
+            self._h = None
+
+    @property
+    def tmp_size(self) -> int:
+        n = C.c_size_t()
+        check(load().zg_graph_get_tmp_size(self._h, C.byref(n)))
+        return n.value
+
+    def plane_params(self, plane: int):
+        p = capi.ResizeParams()
+        present = C.c_int()
+        check(load().zg_graph_get_plane_params(self._h, plane, C.byref(p), C.byref(present)))
+        return present.value, p
+
+    def process(self, src_planes, dst_planes, tmp=None, stream=None) -> None:
+        def buf(planes):
+            b = capi.ImageBuffer()
+            b.version = capi.API_VERSION_2_4
+            for i, t in enumerate(planes):
+                if t is None:
+                    continue
+                ptr, stride, _, _ = _plane(t)
+                b.plane[i] = capi._PlaneC(ptr, stride, capi.BUFFER_MAX)
+            return b
+        s, d = buf(src_planes), buf(dst_planes)
+        if tmp is None and self.tmp_size:
+            import torch
+            tmp = torch.empty(self.tmp_size, dtype=torch.uint8, device="cuda")
+        check(load().zg_graph_process(self._h, C.byref(s), C.byref(d), tmp.data_ptr() if tmp is not None else None,
+                                      _stream_handle(stream)))
