@@ -175,6 +175,26 @@ ZG_API zg_error_code zg_resize_get_info(const zg_resize *r, int *num_passes, int
 ZG_API zg_error_code zg_resize_process(const zg_resize *r, const void *src, ptrdiff_t src_stride,
                                 void *dst, ptrdiff_t dst_stride, void *tmp, zg_stream stream);
 
+/*
+ * No counterpart in zimg: zg_resize_process without a tmp argument, for
+ * callers that cannot allocate device memory when they process a frame (a
+ * plugin host that only hands out frame buffers from its own pool, a
+ * real-time loop that must avoid cudaMalloc/cudaFree and their implicit
+ * device-wide synchronisation). It allocates nothing: two-pass conversions
+ * keep their intermediate plane in a scratch array compiled into the library,
+ * ZG_NO_ALLOC_TMP_BYTES (32 MiB) per GPU, held from the first call on a device
+ * until the process exits. A conversion whose zg_resize_get_tmp_size exceeds
+ * that is rejected with ZG_ERROR_OUT_OF_MEMORY and nothing is launched.
+ * The first call on each device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture. All calls on a device share the one array, so
+ * calls that overlap on the GPU (other streams, other threads) race; order
+ * them on one stream or use zg_resize_process with separate tmp buffers.
+ */
+#define ZG_NO_ALLOC_TMP_BYTES ((size_t)32 << 20)
+ZG_API zg_error_code zg_resize_process_no_alloc(const zg_resize *r, const void *src, ptrdiff_t src_stride,
+                                                void *dst, ptrdiff_t dst_stride, zg_stream stream);
+
 /* ---------------------------------------------------------------- batch --
  * Many planes of uneven sizes (luma plus subsampled chroma, mixed
  * resolutions) in one persistent launch. Replaces running one zimg graph per

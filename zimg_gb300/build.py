@@ -20,7 +20,8 @@ OUT_DIR = os.path.join(PKG, "_lib")
 OBJ_DIR = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT_DIR, "libzimg_gb300.so")
 
-SOURCES = ["filter_plan.cpp", "capi.cu", "capi_graph.cu", "capi_batch.cu", "pass_kernels.cu"]
+SOURCES = ["filter_plan.cpp", "capi.cu", "capi_graph.cu", "capi_batch.cu", "capi_static_tmp.cu",
+           "pass_kernels.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -103,6 +103,7 @@ SIGNATURES = [
     ("zg_resize_get_tmp_size", C.c_int, [_P, C.POINTER(C.c_size_t)]),
     ("zg_resize_get_info", C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     ("zg_resize_process", C.c_int, [_P, _P, C.c_ssize_t, _P, C.c_ssize_t, _P, _P]),
+    ("zg_resize_process_no_alloc", C.c_int, [_P, _P, C.c_ssize_t, _P, C.c_ssize_t, _P]),
     ("zg_batch_create", C.c_int, [C.POINTER(ResizeParams), C.c_uint, C.POINTER(_P)]),
     ("zg_batch_free", None, [_P]),
     ("zg_batch_get_tmp_size", C.c_int, [_P, C.POINTER(C.c_size_t)]),
