@@ -145,17 +145,6 @@ void check_plane(const void *p, ptrdiff_t stride, unsigned w, Sample s, const ch
 
 } // namespace
 
-struct zg_resize {
-	int device;
-	zg_resize_params params;
-	int num_passes = 0;
-	bool first_horizontal = false;
-	bool fused = false;
-	std::unique_ptr<DevicePass> pass[2];
-	ptrdiff_t tmp_stride = 0;
-	size_t tmp_size = 0;
-	Sample sample = Sample::F32;
-};
 
 extern "C" {
 
@@ -304,6 +293,17 @@ zg_error_code zg_resize_create(const zg_resize_params *params, zg_resize **out)
 			const DevicePass &p0 = *r->pass[0];
 			r->tmp_stride = static_cast<ptrdiff_t>((static_cast<size_t>(p0.dst_w) * bytes_of(r->sample) + 255) & ~static_cast<size_t>(255));
 			r->tmp_size = static_cast<size_t>(r->tmp_stride) * p0.dst_h;
+			if (q.allow_fusion && q.engine != ZG_ENGINE_TENSOR &&
+			    plan_fused(r->pass[0]->table, r->pass[1]->table, r->first_horizontal, r->sample == Sample::U16,
+			               q.depth, q.src_width, q.src_height, q.dst_width, q.dst_height, &r->fplan)) {
+				r->fblob.reset(r->fplan.blob.size());
+				cuda_check(cudaMemcpy(r->fblob.get(), r->fplan.blob.data(), r->fplan.blob.size(),
+				                      cudaMemcpyHostToDevice), "upload fused tables");
+				fused_bind(r->fplan, r->fblob.get());
+				r->fgrid = fused_grid_size(r->fplan.variant, r->fplan.smem_bytes);
+				r->fused = true;
+				r->tmp_size = 0;
+			}
 		}
 		*out = r.release();
 	});
@@ -353,6 +353,14 @@ zg_error_code zg_resize_process(const zg_resize *r, const void *src, ptrdiff_t s
 		}
 		if (r->num_passes == 1) {
 			run_pass(*r->pass[0], src, src_stride, dst, dst_stride, st);
+			return;
+		}
+		if (r->fused) {
+			FusedJob j = r->fplan.job;
+			fused_set_io(j, src, src_stride, dst, dst_stride);
+			j.tile_begin = 0;
+			cuda_check(launch_fused(r->fplan.variant, nullptr, 1, j.tiles_x * j.tiles_y, r->fplan.smem_bytes, r->fgrid,
+			                        j, st), "fused resize launch");
 			return;
 		}
 		if (!tmp)

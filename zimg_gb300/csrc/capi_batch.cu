@@ -1,16 +1,35 @@
 // C ABI: batches of conversions over planes of uneven sizes.
+//
+// Fused jobs are grouped by kernel variant; each group runs as ONE persistent
+// launch over the concatenated tile lists of its jobs (a device table of
+// FusedJob entries, one per plane). Jobs that cannot be fused (wide filters,
+// single passes, plain copies) run through their own conversion.
 #include "capi_common.h"
 
 #include <algorithm>
+#include <map>
 
 using namespace zg;
 
 struct zg_batch {
+	struct Group {
+		int variant;
+		size_t smem;
+		int grid;
+		int first;  // first entry in the device job table
+		int count;
+		int tiles;
+	};
+
 	int device;
 	std::vector<zg_resize *> jobs;
+	std::vector<int> table_index;  // per job: entry in the fused table, or -1
 	std::vector<size_t> tmp_offset;
 	size_t tmp_size = 0;
 	std::vector<zg_batch_io> io;
+	std::vector<Group> groups;
+	std::vector<FusedJob> table_host;
+	DeviceBuffer table_dev;
 	cudaGraphExec_t graph = nullptr;
 	cudaStream_t graph_stream = nullptr;
 	void *graph_tmp = nullptr;
@@ -37,7 +56,15 @@ void batch_launch(const zg_batch *b, void *tmp, cudaStream_t st)
 {
 	if (b->io.size() != b->jobs.size())
 		throw Error(kErrLogic, "zg_batch_set_io was not called");
+	const FusedJob *table = static_cast<const FusedJob *>(b->table_dev.get());
+	for (const auto &g : b->groups) {
+		FusedJob unused{};
+		cuda_check(launch_fused(g.variant, table + g.first, g.count, g.tiles, g.smem, g.grid, unused, st),
+		           "fused batch launch");
+	}
 	for (size_t i = 0; i < b->jobs.size(); ++i) {
+		if (b->table_index[i] >= 0)
+			continue;
 		const zg_batch_io &io = b->io[i];
 		void *t = b->tmp_size ? static_cast<char *>(tmp) + b->tmp_offset[i] : nullptr;
 		zg_error_code rc = zg_resize_process(b->jobs[i], io.src, io.src_stride, io.dst, io.dst_stride, t,
@@ -65,11 +92,33 @@ zg_error_code zg_batch_create(const zg_resize_params *jobs, unsigned num_jobs, z
 			if (rc != ZG_ERROR_SUCCESS)
 				rethrow_last(rc);
 			b->jobs.push_back(r);
-			size_t t = 0;
-			zg_resize_get_tmp_size(r, &t);
 			b->tmp_offset.push_back(b->tmp_size);
-			b->tmp_size += (t + 255) & ~static_cast<size_t>(255);
+			if (!r->fused)
+				b->tmp_size += (r->tmp_size + 255) & ~static_cast<size_t>(255);
 		}
+
+		// group fused jobs by variant, in job order within a group
+		std::map<int, std::vector<unsigned>> by_variant;
+		for (unsigned i = 0; i < num_jobs; ++i)
+			if (b->jobs[i]->fused)
+				by_variant[b->jobs[i]->fplan.variant].push_back(i);
+		b->table_index.assign(num_jobs, -1);
+		for (auto &kv : by_variant) {
+			zg_batch::Group g{ kv.first, 0, 0, static_cast<int>(b->table_host.size()), 0, 0 };
+			for (unsigned i : kv.second) {
+				FusedJob j = b->jobs[i]->fplan.job;
+				j.tile_begin = g.tiles;
+				g.tiles += j.tiles_x * j.tiles_y;
+				g.smem = std::max(g.smem, b->jobs[i]->fplan.smem_bytes);
+				b->table_index[i] = static_cast<int>(b->table_host.size());
+				b->table_host.push_back(j);
+				++g.count;
+			}
+			g.grid = fused_grid_size(g.variant, g.smem);
+			b->groups.push_back(g);
+		}
+		if (!b->table_host.empty())
+			b->table_dev.reset(b->table_host.size() * sizeof(FusedJob));
 		*out = b.release();
 	});
 }
@@ -93,8 +142,32 @@ zg_error_code zg_batch_set_io(zg_batch *b, const zg_batch_io *io, zg_stream stre
 	return guarded([&] {
 		if (!b || !io)
 			throw Error(kErrIllegalArgument, "null pointer");
-		(void)stream;
+		if (current_device() != b->device)
+			throw Error(kErrLogic, "batch used on a different device than the one it was created on");
+		for (size_t i = 0; i < b->jobs.size(); ++i) {
+			const zg_resize_params &q = b->jobs[i]->params;
+			const unsigned bpe = bytes_of(b->jobs[i]->sample);
+			if (!io[i].src || !io[i].dst)
+				throw Error(kErrIllegalArgument, "null plane pointer in batch io");
+			if (io[i].src_stride < static_cast<ptrdiff_t>(q.src_width * bpe) ||
+			    io[i].dst_stride < static_cast<ptrdiff_t>(q.dst_width * bpe))
+				throw Error(kErrIllegalArgument, "stride smaller than a line in batch io");
+			if (reinterpret_cast<uintptr_t>(io[i].src) % bpe || reinterpret_cast<uintptr_t>(io[i].dst) % bpe ||
+			    io[i].src_stride % bpe || io[i].dst_stride % bpe)
+				throw Error(kErrIllegalArgument, "batch io not aligned to the sample size");
+			if (b->table_index[i] >= 0)
+				fused_set_io(b->table_host[b->table_index[i]], io[i].src, io[i].src_stride, io[i].dst,
+				             io[i].dst_stride);
+		}
 		b->io.assign(io, io + b->jobs.size());
+		if (!b->table_host.empty()) {
+			// Ordered with earlier work on this stream; the host copy stays
+			// valid until the next set_io, which waits for this copy first.
+			cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+			cuda_check(cudaMemcpyAsync(b->table_dev.get(), b->table_host.data(), b->table_host.size() * sizeof(FusedJob),
+			                           cudaMemcpyHostToDevice, st), "batch io upload");
+			cuda_check(cudaStreamSynchronize(st), "batch io upload");
+		}
 		if (b->graph) {
 			cudaGraphExecDestroy(b->graph);
 			b->graph = nullptr;
@@ -156,11 +229,11 @@ zg_error_code zg_batch_get_launch_count(const zg_batch *b, unsigned *out)
 	return guarded([&] {
 		if (!b || !out)
 			throw Error(kErrIllegalArgument, "null pointer");
-		unsigned n = 0;
-		for (auto *j : b->jobs) {
-			int passes = 0, first = 0, fused = 0;
-			zg_resize_get_info(j, &passes, &first, &fused);
-			n += fused ? 1 : static_cast<unsigned>(passes);
+		unsigned n = static_cast<unsigned>(b->groups.size());
+		for (size_t i = 0; i < b->jobs.size(); ++i) {
+			if (b->table_index[i] >= 0)
+				continue;
+			n += static_cast<unsigned>(b->jobs[i]->num_passes);
 		}
 		*out = n;
 	});

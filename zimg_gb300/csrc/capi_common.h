@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "filter_plan.h"
+#include "fused.h"
 #include "kernels.h"
 #include "zimg_gb300.h"
 
@@ -116,3 +117,19 @@ unsigned bytes_of(Sample s);
 int current_device();
 
 } // namespace zg
+
+// A conversion: zero, one or two passes, optionally fused into one kernel.
+struct zg_resize {
+	int device;
+	zg_resize_params params;
+	int num_passes = 0;
+	bool first_horizontal = false;
+	bool fused = false;
+	std::unique_ptr<zg::DevicePass> pass[2];
+	ptrdiff_t tmp_stride = 0;
+	size_t tmp_size = 0;
+	zg::Sample sample = zg::Sample::F32;
+	zg::FusedPlan fplan;
+	zg::DeviceBuffer fblob;
+	int fgrid = 0;
+};
