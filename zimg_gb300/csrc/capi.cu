@@ -300,7 +300,9 @@ zg_error_code zg_resize_create(const zg_resize_params *params, zg_resize **out)
 				cuda_check(cudaMemcpy(r->fblob.get(), r->fplan.blob.data(), r->fplan.blob.size(),
 				                      cudaMemcpyHostToDevice), "upload fused tables");
 				fused_bind(r->fplan, r->fblob.get());
-				r->fgrid = fused_grid_size(r->fplan.variant, r->fplan.smem_bytes);
+				const FusedPlan *pp = &r->fplan;
+				r->flayout = fused_layout(&pp, 1);
+				r->fgrid = fused_grid_size(r->fplan.variant, static_cast<size_t>(r->flayout.total_bytes));
 				r->fused = true;
 				r->tmp_size = 0;
 			}
@@ -359,7 +361,7 @@ zg_error_code zg_resize_process(const zg_resize *r, const void *src, ptrdiff_t s
 			FusedJob j = r->fplan.job;
 			fused_set_io(j, src, src_stride, dst, dst_stride);
 			j.tile_begin = 0;
-			cuda_check(launch_fused(r->fplan.variant, nullptr, 1, j.tiles_x * j.tiles_y, r->fplan.smem_bytes, r->fgrid,
+			cuda_check(launch_fused(r->fplan.variant, nullptr, 1, j.tiles_x * j.tiles_y, r->flayout, r->fgrid,
 			                        j, st), "fused resize launch");
 			return;
 		}

@@ -14,7 +14,7 @@ using namespace zg;
 struct zg_batch {
 	struct Group {
 		int variant;
-		size_t smem;
+		SmemLayout layout;
 		int grid;
 		int first;  // first entry in the device job table
 		int count;
@@ -59,7 +59,7 @@ void batch_launch(const zg_batch *b, void *tmp, cudaStream_t st)
 	const FusedJob *table = static_cast<const FusedJob *>(b->table_dev.get());
 	for (const auto &g : b->groups) {
 		FusedJob unused{};
-		cuda_check(launch_fused(g.variant, table + g.first, g.count, g.tiles, g.smem, g.grid, unused, st),
+		cuda_check(launch_fused(g.variant, table + g.first, g.count, g.tiles, g.layout, g.grid, unused, st),
 		           "fused batch launch");
 	}
 	for (size_t i = 0; i < b->jobs.size(); ++i) {
@@ -104,17 +104,19 @@ zg_error_code zg_batch_create(const zg_resize_params *jobs, unsigned num_jobs, z
 				by_variant[b->jobs[i]->fplan.variant].push_back(i);
 		b->table_index.assign(num_jobs, -1);
 		for (auto &kv : by_variant) {
-			zg_batch::Group g{ kv.first, 0, 0, static_cast<int>(b->table_host.size()), 0, 0 };
+			zg_batch::Group g{ kv.first, SmemLayout{}, 0, static_cast<int>(b->table_host.size()), 0, 0 };
+			std::vector<const FusedPlan *> plans;
 			for (unsigned i : kv.second) {
 				FusedJob j = b->jobs[i]->fplan.job;
 				j.tile_begin = g.tiles;
 				g.tiles += j.tiles_x * j.tiles_y;
-				g.smem = std::max(g.smem, b->jobs[i]->fplan.smem_bytes);
+				plans.push_back(&b->jobs[i]->fplan);
 				b->table_index[i] = static_cast<int>(b->table_host.size());
 				b->table_host.push_back(j);
 				++g.count;
 			}
-			g.grid = fused_grid_size(g.variant, g.smem);
+			g.layout = fused_layout(plans.data(), static_cast<int>(plans.size()));
+			g.grid = fused_grid_size(g.variant, static_cast<size_t>(g.layout.total_bytes));
 			b->groups.push_back(g);
 		}
 		if (!b->table_host.empty())

@@ -131,5 +131,6 @@ struct zg_resize {
 	zg::Sample sample = zg::Sample::F32;
 	zg::FusedPlan fplan;
 	zg::DeviceBuffer fblob;
+	zg::SmemLayout flayout{};
 	int fgrid = 0;
 };

@@ -9,10 +9,10 @@
 namespace zg {
 
 // per-(H_FIRST, U16) instantiation units (fused_inst_*.cu)
-cudaError_t launch_fused_v_f32(int hw, int vs, const FusedJob *, int, int, size_t, int, const FusedJob &, cudaStream_t);
-cudaError_t launch_fused_v_u16(int hw, int vs, const FusedJob *, int, int, size_t, int, const FusedJob &, cudaStream_t);
-cudaError_t launch_fused_h_f32(int hw, int vs, const FusedJob *, int, int, size_t, int, const FusedJob &, cudaStream_t);
-cudaError_t launch_fused_h_u16(int hw, int vs, const FusedJob *, int, int, size_t, int, const FusedJob &, cudaStream_t);
+cudaError_t launch_fused_v_f32(int, int, const FusedJob *, int, int, const SmemLayout &, int, const FusedJob &, cudaStream_t);
+cudaError_t launch_fused_v_u16(int, int, const FusedJob *, int, int, const SmemLayout &, int, const FusedJob &, cudaStream_t);
+cudaError_t launch_fused_h_f32(int, int, const FusedJob *, int, int, const SmemLayout &, int, const FusedJob &, cudaStream_t);
+cudaError_t launch_fused_h_u16(int, int, const FusedJob *, int, int, const SmemLayout &, int, const FusedJob &, cudaStream_t);
 const void *fused_kernel_ptr_v_f32(int hw, int vs);
 const void *fused_kernel_ptr_v_u16(int hw, int vs);
 const void *fused_kernel_ptr_h_f32(int hw, int vs);
@@ -23,7 +23,7 @@ namespace {
 constexpr int kTileW = 128;
 constexpr int kHwBuckets[] = { 8, 16 };
 constexpr int kVsBuckets[] = { 8, 12, 16, 24 };
-constexpr size_t kSmemBudget = 110 * 1024;  // two CTAs per SM at least
+constexpr size_t kSmemBudget = 100 * 1024;  // two CTAs per SM at least
 
 int bucket_index(const int *b, int n, int v)
 {
@@ -121,18 +121,19 @@ bool plan_fused(const FilterTable &first, const FilterTable &second, bool h_firs
 		max_px = std::max(max_px, hi - lo);
 	}
 	const int pxa = (max_px + 7) & ~7;
-	const int p_pitch = pxa + 4;
 
-	// tile height: as tall as the shared-memory budget allows
+	// tile height: as tall as the shared-memory budget allows (a multiple of
+	// 16 rows, so each tile's group tables are whole 16-byte chunks)
 	int tile_h = h_first ? 64 : 32;
 	std::vector<int> win_row;
 	size_t smem = 0;
+	int max_py = 0;
 	for (;; tile_h /= 2) {
-		if (tile_h < kGroup)
+		if (tile_h < 16)
 			return false;
 		const unsigned tiles_y = (dst_h + tile_h - 1) / tile_h;
 		win_row.assign(2 * tiles_y, 0);
-		int max_py = 0;
+		max_py = 0;
 		for (unsigned ty = 0; ty < tiles_y; ++ty) {
 			int lo = INT_MAX, hi = INT_MIN;
 			const unsigned g_first = ty * tile_h / kGroup;
@@ -145,9 +146,16 @@ bool plan_fused(const FilterTable &first, const FilterTable &second, bool h_firs
 			win_row[2 * ty + 1] = hi;
 			max_py = std::max(max_py, hi - lo);
 		}
-		const size_t p_floats = static_cast<size_t>(max_py) * p_pitch;
-		const size_t i_floats = h_first ? static_cast<size_t>(max_py) * kTileW : static_cast<size_t>(tile_h) * p_pitch;
-		smem = (p_floats + i_floats) * sizeof(float);
+		FusedPlan probe;
+		probe.job.h_first = h_first ? 1 : 0;
+		probe.job.kind = static_cast<int>(u16 ? FusedKind::U16_EXACT : FusedKind::F32);
+		probe.job.tile_h = tile_h;
+		probe.job.hw = HW;
+		probe.job.vs = VS;
+		probe.max_py = max_py;
+		probe.max_pitch = pxa + 8;
+		const FusedPlan *pp = &probe;
+		smem = static_cast<size_t>(fused_layout(&pp, 1).total_bytes);
 		if (smem <= kSmemBudget)
 			break;
 	}
@@ -213,6 +221,8 @@ bool plan_fused(const FilterTable &first, const FilterTable &second, bool h_firs
 	J.magic = 12582912.0f + offset;
 	J.pixel_max = u16 ? static_cast<float>((1UL << depth) - 1) : 0.0f;
 	p.smem_bytes = smem;
+	p.max_py = max_py;
+	p.max_pitch = pxa + 8;
 	p.variant = ((J.h_first * 2 + (u16 ? 1 : 0)) * 2 + hw_i) * 4 + vs_i;
 	return true;
 }
@@ -249,6 +259,37 @@ const void *kernel_ptr(int variant)
 
 } // namespace
 
+SmemLayout fused_layout(const FusedPlan *const *plans, int n)
+{
+	int max_py = 0, max_pitch = 0, max_th = 0, hw = 0, vs = 0;
+	bool u16 = false, h_first = false;
+	for (int i = 0; i < n; ++i) {
+		const FusedPlan &p = *plans[i];
+		max_py = std::max(max_py, p.max_py);
+		max_pitch = std::max(max_pitch, p.max_pitch);
+		max_th = std::max(max_th, p.job.tile_h);
+		hw = std::max(hw, p.job.hw);
+		vs = std::max(vs, p.job.vs);
+		u16 = p.job.kind == static_cast<int>(FusedKind::U16_EXACT);
+		h_first = p.job.h_first != 0;
+	}
+	auto a16 = [](size_t x) { return static_cast<int>((x + 15) / 16 * 16); };
+	const int e = u16 ? 2 : 4;
+	SmemLayout L{};
+	const int patch = a16(static_cast<size_t>(max_py) * max_pitch * e);
+	L.vcoef_off = patch;
+	L.htaps_off = L.vcoef_off + a16(static_cast<size_t>(max_th / kGroup) * vs * 16);
+	L.hleft_off = L.htaps_off + a16(static_cast<size_t>(kTileW) * hw * 4);
+	L.vbase_off = L.hleft_off + a16(kTileW * 4);
+	L.buf_bytes = L.vbase_off + a16(static_cast<size_t>(max_th / kGroup) * 4);
+	L.pf_off = 2 * L.buf_bytes;
+	const int pf = u16 ? a16(static_cast<size_t>(max_py) * max_pitch * 4) : 0;
+	L.i_off = L.pf_off + pf;
+	const size_t ib = h_first ? static_cast<size_t>(max_py) * kTileW * 4 : static_cast<size_t>(max_th) * max_pitch * 4;
+	L.total_bytes = L.i_off + a16(ib);
+	return L;
+}
+
 size_t fused_max_smem()
 {
 	return kSmemBudget;
@@ -266,7 +307,7 @@ int fused_grid_size(int variant, size_t smem_bytes)
 	return std::max(1, sms) * per_sm;
 }
 
-cudaError_t launch_fused(int variant, const FusedJob *jobs, int num_jobs, int total_tiles, size_t smem_bytes,
+cudaError_t launch_fused(int variant, const FusedJob *jobs, int num_jobs, int total_tiles, const SmemLayout &smem_bytes,
                          int grid, const FusedJob &single, cudaStream_t stream)
 {
 	int hf, u16, hw, vs;

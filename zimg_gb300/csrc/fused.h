@@ -65,6 +65,17 @@ struct FusedJob {
 	int vec_ok;             // planes and strides 16-byte aligned: vector loads and stores
 };
 
+// Shared-memory layout of one launch (the maximum over its jobs): two
+// prefetch buffers, each holding a patch and the tile's tap tables, then the
+// converted-float patch (u16 only) and the intermediate.
+struct SmemLayout {
+	int buf_bytes;
+	int vcoef_off, htaps_off, hleft_off, vbase_off;  // within a buffer
+	int pf_off;                                      // from the start
+	int i_off;
+	int total_bytes;
+};
+
 // Fill the plane pointers of a job and its alignment flag.
 void fused_set_io(FusedJob &j, const void *src, ptrdiff_t src_stride, void *dst, ptrdiff_t dst_stride);
 
@@ -73,6 +84,7 @@ void fused_set_io(FusedJob &j, const void *src, ptrdiff_t src_stride, void *dst,
 struct FusedPlan {
 	FusedJob job{};
 	size_t smem_bytes = 0;   // dynamic shared memory this job needs
+	int max_py = 0, max_pitch = 0;  // largest patch (rows, elements per row)
 	int variant = 0;         // kernel instantiation index
 	std::vector<unsigned char> blob;  // host copy of the tables, uploaded by the owner
 	size_t off_h_taps = 0, off_h_left = 0, off_v_dense = 0, off_v_base = 0, off_win_row = 0, off_win_col = 0;
@@ -91,8 +103,11 @@ void fused_bind(FusedPlan &p, const void *device_blob);
 // Launch all tiles of `jobs` (a device array of num_jobs FusedJob, all of the
 // same variant) as one persistent grid; with jobs == nullptr, run `single`
 // (passed by value as a kernel parameter).
-cudaError_t launch_fused(int variant, const FusedJob *jobs, int num_jobs, int total_tiles, size_t smem_bytes,
+cudaError_t launch_fused(int variant, const FusedJob *jobs, int num_jobs, int total_tiles, const SmemLayout &L,
                          int grid, const FusedJob &single, cudaStream_t stream);
+
+// Shared-memory layout that covers every plan in `plans` (all one variant).
+SmemLayout fused_layout(const FusedPlan *const *plans, int n);
 
 // Largest dynamic shared memory any variant may use, and the CTA count per SM
 // the launcher targets.

@@ -29,7 +29,7 @@ const void *fused_kernel_ptr_h_f32(int hw, int vs)
 	return hw == 0 ? ptr_vs<8>(vs) : ptr_vs<16>(vs);
 }
 
-cudaError_t launch_fused_h_f32(int hw, int vs, const FusedJob *jobs, int num_jobs, int total_tiles, size_t smem,
+cudaError_t launch_fused_h_f32(int hw, int vs, const FusedJob *jobs, int num_jobs, int total_tiles, const SmemLayout &L,
                             int grid, const FusedJob &single, cudaStream_t stream)
 {
 	const void *k = fused_kernel_ptr_h_f32(hw, vs);
@@ -37,8 +37,9 @@ cudaError_t launch_fused_h_f32(int hw, int vs, const FusedJob *jobs, int num_job
 	if (e != cudaSuccess)
 		return e;
 	FusedJob one = single;
-	void *args[] = { &jobs, &num_jobs, &total_tiles, &one };
-	return cudaLaunchKernel(k, dim3(grid), dim3(kTileThreads), args, smem, stream);
+	SmemLayout layout = L;
+	void *args[] = { &jobs, &num_jobs, &total_tiles, &one, &layout };
+	return cudaLaunchKernel(k, dim3(grid), dim3(kTileThreads), args, static_cast<size_t>(L.total_bytes), stream);
 }
 
 } // namespace zg
