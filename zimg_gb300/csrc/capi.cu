@@ -300,6 +300,8 @@ zg_error_code zg_resize_create(const zg_resize_params *params, zg_resize **out)
 				cuda_check(cudaMemcpy(r->fblob.get(), r->fplan.blob.data(), r->fplan.blob.size(),
 				                      cudaMemcpyHostToDevice), "upload fused tables");
 				fused_bind(r->fplan, r->fblob.get());
+				FusedPlan *mp = &r->fplan;
+				fused_segment(&mp, 1, fused_wave_items());
 				const FusedPlan *pp = &r->fplan;
 				r->flayout = fused_layout(&pp, 1);
 				r->fgrid = fused_grid_size(r->fplan.variant, static_cast<size_t>(r->flayout.total_bytes));
@@ -360,8 +362,8 @@ zg_error_code zg_resize_process(const zg_resize *r, const void *src, ptrdiff_t s
 		if (r->fused) {
 			FusedJob j = r->fplan.job;
 			fused_set_io(j, src, src_stride, dst, dst_stride);
-			j.tile_begin = 0;
-			cuda_check(launch_fused(r->fplan.variant, nullptr, 1, j.tiles_x * j.tiles_y, r->flayout, r->fgrid,
+			j.item_begin = 0;
+			cuda_check(launch_fused(r->fplan.variant, nullptr, 1, fused_items(j), r->flayout, r->fgrid,
 			                        j, st), "fused resize launch");
 			return;
 		}

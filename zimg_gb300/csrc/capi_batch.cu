@@ -97,6 +97,15 @@ zg_error_code zg_batch_create(const zg_resize_params *jobs, unsigned num_jobs, z
 				b->tmp_size += (r->tmp_size + 255) & ~static_cast<size_t>(255);
 		}
 
+		// one wave of work items across the whole batch: split strips into row
+		// segments only as far as needed to fill the GPU
+		std::vector<FusedPlan *> all;
+		for (unsigned i = 0; i < num_jobs; ++i)
+			if (b->jobs[i]->fused)
+				all.push_back(&b->jobs[i]->fplan);
+		if (!all.empty())
+			fused_segment(all.data(), static_cast<int>(all.size()), fused_wave_items());
+
 		// group fused jobs by variant, in job order within a group
 		std::map<int, std::vector<unsigned>> by_variant;
 		for (unsigned i = 0; i < num_jobs; ++i)
@@ -108,8 +117,8 @@ zg_error_code zg_batch_create(const zg_resize_params *jobs, unsigned num_jobs, z
 			std::vector<const FusedPlan *> plans;
 			for (unsigned i : kv.second) {
 				FusedJob j = b->jobs[i]->fplan.job;
-				j.tile_begin = g.tiles;
-				g.tiles += j.tiles_x * j.tiles_y;
+				j.item_begin = g.tiles;
+				g.tiles += fused_items(j);
 				plans.push_back(&b->jobs[i]->fplan);
 				b->table_index[i] = static_cast<int>(b->table_host.size());
 				b->table_host.push_back(j);

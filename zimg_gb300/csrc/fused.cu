@@ -20,10 +20,10 @@ const void *fused_kernel_ptr_h_u16(int hw, int vs);
 
 namespace {
 
-constexpr int kTileW = 128;
 constexpr int kHwBuckets[] = { 8, 16 };
 constexpr int kVsBuckets[] = { 8, 12, 16, 24 };
-constexpr size_t kSmemBudget = 100 * 1024;  // two CTAs per SM at least
+constexpr size_t kSmemBudget = 56 * 1024;   // preferred: four CTAs of 128 threads per SM
+constexpr size_t kSmemMax = 110 * 1024;     // hard limit: two CTAs per SM
 
 int bucket_index(const int *b, int n, int v)
 {
@@ -82,14 +82,14 @@ bool plan_fused(const FilterTable &first, const FilterTable &second, bool h_firs
 		return false;
 	const int HW = kHwBuckets[hw_i];
 
-	// dense vertical groups
-	const unsigned groups = (dst_h + kGroup - 1) / kGroup;
+	// dense vertical groups; streaming needs non-decreasing group bases
+	const int groups = static_cast<int>((dst_h + kGroup - 1) / kGroup);
 	int max_span = 0;
 	std::vector<int> gbase(groups);
-	for (unsigned g = 0; g < groups; ++g) {
+	for (int g = 0; g < groups; ++g) {
 		int lo = INT_MAX, hi = INT_MIN;
-		for (unsigned j = 0; j < kGroup; ++j) {
-			const unsigned i = g * kGroup + j;
+		for (int j = 0; j < kGroup; ++j) {
+			const unsigned i = static_cast<unsigned>(g * kGroup + j);
 			if (i >= dst_h)
 				break;
 			lo = std::min(lo, static_cast<int>(V.left[i]));
@@ -97,84 +97,88 @@ bool plan_fused(const FilterTable &first, const FilterTable &second, bool h_firs
 		}
 		gbase[g] = lo;
 		max_span = std::max(max_span, hi - lo);
+		if (g && gbase[g] < gbase[g - 1])
+			return false;
 	}
 	const int vs_i = bucket_index(kVsBuckets, 4, max_span);
 	if (vs_i < 0)
 		return false;
 	const int VS = kVsBuckets[vs_i];
 
+	// source-column window of each strip
 	const int col_align = u16 ? 8 : 4;
-	const unsigned tiles_x = (dst_w + kTileW - 1) / kTileW;
-
-	// column windows (shared by all tile heights)
-	std::vector<int> win_col(2 * tiles_x);
-	int max_px = 0;
-	for (unsigned tx = 0; tx < tiles_x; ++tx) {
+	const int strips = static_cast<int>((dst_w + kStripW - 1) / kStripW);
+	std::vector<int> win_col(2 * strips);
+	int max_pxa = 0;
+	for (int s = 0; s < strips; ++s) {
 		int lo = INT_MAX, hi = INT_MIN;
-		for (unsigned c = tx * kTileW; c < std::min<unsigned>(dst_w, (tx + 1) * kTileW); ++c) {
+		for (unsigned c = s * kStripW; c < std::min<unsigned>(dst_w, (s + 1) * kStripW); ++c) {
 			lo = std::min(lo, static_cast<int>(H.left[c]));
 			hi = std::max(hi, static_cast<int>(H.left[c]) + HW);
 		}
 		lo = lo / col_align * col_align;
-		win_col[2 * tx] = lo;
-		win_col[2 * tx + 1] = hi;
-		max_px = std::max(max_px, hi - lo);
+		win_col[2 * s] = lo;
+		win_col[2 * s + 1] = hi;
+		max_pxa = std::max(max_pxa, (hi - lo + 7) & ~7);
 	}
-	const int pxa = (max_px + 7) & ~7;
 
-	// tile height: as tall as the shared-memory budget allows (a multiple of
-	// 16 rows, so each tile's group tables are whole 16-byte chunks)
-	int tile_h = h_first ? 64 : 32;
-	std::vector<int> win_row;
-	size_t smem = 0;
-	int max_py = 0;
-	for (;; tile_h /= 2) {
-		if (tile_h < 16)
-			return false;
-		const unsigned tiles_y = (dst_h + tile_h - 1) / tile_h;
-		win_row.assign(2 * tiles_y, 0);
-		max_py = 0;
-		for (unsigned ty = 0; ty < tiles_y; ++ty) {
-			int lo = INT_MAX, hi = INT_MIN;
-			const unsigned g_first = ty * tile_h / kGroup;
-			const unsigned g_last = std::min<unsigned>(groups, (ty + 1) * tile_h / kGroup);
-			for (unsigned g = g_first; g < g_last; ++g) {
-				lo = std::min(lo, gbase[g]);
-				hi = std::max(hi, gbase[g] + VS);
-			}
-			win_row[2 * ty] = lo;
-			win_row[2 * ty + 1] = hi;
-			max_py = std::max(max_py, hi - lo);
-		}
-		FusedPlan probe;
-		probe.job.h_first = h_first ? 1 : 0;
-		probe.job.kind = static_cast<int>(u16 ? FusedKind::U16_EXACT : FusedKind::F32);
-		probe.job.tile_h = tile_h;
-		probe.job.hw = HW;
-		probe.job.vs = VS;
-		probe.max_py = max_py;
-		probe.max_pitch = pxa + 8;
-		const FusedPlan *pp = &probe;
-		smem = static_cast<size_t>(fused_layout(&pp, 1).total_bytes);
-		if (smem <= kSmemBudget)
-			break;
-	}
-	const unsigned tiles_y = (dst_h + tile_h - 1) / tile_h;
-	// The last tile row may hold groups past the plane's last row: they get the
-	// last real group's base and zero taps, so every group a tile walks exists.
-	const unsigned real_groups = groups;
-	const unsigned padded_groups = tiles_y * static_cast<unsigned>(tile_h) / kGroup;
-	gbase.resize(padded_groups, gbase[real_groups - 1]);
-
-	// host blob: h_taps | h_left | v_dense | v_base | win_row | win_col
+	// steps and rings: try the preferred step, then smaller ones
 	FusedPlan &p = *out;
 	p = FusedPlan{};
+	bool fits = false;
+	for (int attempt = 0; attempt < 2 && !fits; ++attempt)
+	for (int step_groups = h_first ? 4 : 2; step_groups >= 1 && !fits; step_groups /= 2) {
+		const size_t budget = attempt == 0 ? kSmemBudget : kSmemMax;
+		const int nsteps = (groups + step_groups - 1) / step_groups;
+		auto hi_of = [&](int k) { return gbase[std::min(groups, (k + 1) * step_groups) - 1] + VS; };
+		int ring_need = 1, stage_need = 1, in_need = 1;
+		for (int k = 0; k < nsteps; ++k) {
+			const int win_lo = gbase[k * step_groups];
+			const int hi = hi_of(k);
+			const int hi_next = k + 1 < nsteps ? hi_of(k + 1) : hi;
+			// any step may start a segment, when its new lines are its whole window
+			if (h_first) {
+				ring_need = std::max(ring_need, hi - win_lo);
+				if (u16) {
+					in_need = std::max(in_need, hi - win_lo);
+					stage_need = std::max(stage_need, hi_next - win_lo);
+				} else {
+					in_need = std::max(in_need, hi_next - win_lo);
+				}
+			} else {
+				ring_need = std::max(ring_need, u16 ? hi - win_lo : hi_next - win_lo);
+				if (u16)
+					stage_need = std::max(stage_need, hi_next - win_lo);
+			}
+		}
+		auto pow2 = [](int x) { int r = 1; while (r < x) r <<= 1; return r; };
+		FusedJob &J = p.job;
+		J.h_first = h_first ? 1 : 0;
+		J.kind = static_cast<int>(u16 ? FusedKind::U16_EXACT : FusedKind::F32);
+		J.hw = HW;
+		J.vs = VS;
+		J.step_groups = step_groups;
+		J.groups = groups;
+		J.seg_groups = groups;
+		J.segments = 1;
+		J.ring_rows = pow2(ring_need);
+		J.in_rows = h_first ? pow2(in_need) : 1;
+		p.max_pxa = max_pxa;
+		// staging ring for u16 lives in the layout's stage_rows (recorded below)
+		p.stage_rows = u16 ? pow2(stage_need) : 1;
+		const FusedPlan *pp = &p;
+		if (static_cast<size_t>(fused_layout(&pp, 1).total_bytes) <= budget)
+			fits = true;
+	}
+	if (!fits)
+		return false;
+
+	// host blob: h_taps | h_left | v_dense | v_base | win_col
 	size_t off = 0;
 	p.off_h_taps = off;  off = align_up(off + static_cast<size_t>(dst_w) * HW * sizeof(float), 256);
 	p.off_h_left = off;  off = align_up(off + static_cast<size_t>(dst_w) * sizeof(int), 256);
-	p.off_v_dense = off; off = align_up(off + static_cast<size_t>(padded_groups) * VS * kGroup * sizeof(float), 256);
-	p.off_v_base = off;  off = align_up(off + static_cast<size_t>(padded_groups) * sizeof(int), 256);
-	p.off_win_row = off; off = align_up(off + win_row.size() * sizeof(int), 256);
+	p.off_v_dense = off; off = align_up(off + static_cast<size_t>(groups) * VS * kGroup * sizeof(float), 256);
+	p.off_v_base = off;  off = align_up(off + static_cast<size_t>(groups) * sizeof(int), 256);
 	p.off_win_col = off; off = align_up(off + win_col.size() * sizeof(int), 256);
 	p.blob.assign(off, 0);
 
@@ -187,12 +191,10 @@ bool plan_fused(const FilterTable &first, const FilterTable &second, bool h_firs
 	}
 	float *v_dense = reinterpret_cast<float *>(p.blob.data() + p.off_v_dense);
 	int *v_base = reinterpret_cast<int *>(p.blob.data() + p.off_v_base);
-	for (unsigned g = 0; g < padded_groups; ++g) {
+	for (int g = 0; g < groups; ++g) {
 		v_base[g] = gbase[g];
-		if (g >= real_groups)
-			continue;
-		for (unsigned j = 0; j < kGroup; ++j) {
-			const unsigned i = g * kGroup + j;
+		for (int j = 0; j < kGroup; ++j) {
+			const unsigned i = static_cast<unsigned>(g * kGroup + j);
 			if (i >= dst_h)
 				break;
 			const int d = static_cast<int>(V.left[i]) - gbase[g];
@@ -200,31 +202,49 @@ bool plan_fused(const FilterTable &first, const FilterTable &second, bool h_firs
 				v_dense[(static_cast<size_t>(g) * VS + d + k) * kGroup + j] = tap_value(V, u16, i, k);
 		}
 	}
-	std::memcpy(p.blob.data() + p.off_win_row, win_row.data(), win_row.size() * sizeof(int));
 	std::memcpy(p.blob.data() + p.off_win_col, win_col.data(), win_col.size() * sizeof(int));
 
 	FusedJob &J = p.job;
-	J.h_first = h_first ? 1 : 0;
-	J.kind = static_cast<int>(u16 ? FusedKind::U16_EXACT : FusedKind::F32);
 	J.src_w = static_cast<int>(src_w);
 	J.src_h = static_cast<int>(src_h);
 	J.dst_w = static_cast<int>(dst_w);
 	J.dst_h = static_cast<int>(dst_h);
-	J.tile_h = tile_h;
-	J.tile_w = kTileW;
-	J.tiles_x = static_cast<int>(tiles_x);
-	J.tiles_y = static_cast<int>(tiles_y);
-	J.hw = HW;
-	J.vs = VS;
+	J.strips = strips;
 	const float offset = u16 ? static_cast<float>(std::ldexp(1.0, static_cast<int>(depth) - 1)) : 0.0f;
 	J.offset = offset;
 	J.magic = 12582912.0f + offset;
 	J.pixel_max = u16 ? static_cast<float>((1UL << depth) - 1) : 0.0f;
-	p.smem_bytes = smem;
-	p.max_py = max_py;
-	p.max_pitch = pxa + 8;
 	p.variant = ((J.h_first * 2 + (u16 ? 1 : 0)) * 2 + hw_i) * 4 + vs_i;
 	return true;
+}
+
+void fused_segment(FusedPlan *const *plans, int n, int num_items_target)
+{
+	long strips = 0;
+	for (int i = 0; i < n; ++i)
+		strips += plans[i]->job.strips;
+	const int want = static_cast<int>(std::max<long>(1, (num_items_target + strips - 1) / std::max<long>(1, strips)));
+	for (int i = 0; i < n; ++i) {
+		FusedJob &J = plans[i]->job;
+		const int steps = (J.groups + J.step_groups - 1) / J.step_groups;
+		const int segs = std::max(1, std::min(want, steps));
+		const int steps_per_seg = (steps + segs - 1) / segs;
+		J.seg_groups = steps_per_seg * J.step_groups;
+		J.segments = (J.groups + J.seg_groups - 1) / J.seg_groups;
+	}
+}
+
+int fused_items(const FusedJob &j)
+{
+	return j.strips * j.segments;
+}
+
+int fused_wave_items()
+{
+	int dev = 0, sms = 0;
+	cudaGetDevice(&dev);
+	cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+	return std::max(1, sms) * 4;
 }
 
 void fused_bind(FusedPlan &p, const void *device_blob)
@@ -234,7 +254,6 @@ void fused_bind(FusedPlan &p, const void *device_blob)
 	p.job.h_left = reinterpret_cast<const int *>(b + p.off_h_left);
 	p.job.v_dense = reinterpret_cast<const float *>(b + p.off_v_dense);
 	p.job.v_base = reinterpret_cast<const int *>(b + p.off_v_base);
-	p.job.win_row = reinterpret_cast<const int *>(b + p.off_win_row);
 	p.job.win_col = reinterpret_cast<const int *>(b + p.off_win_col);
 }
 
@@ -261,38 +280,53 @@ const void *kernel_ptr(int variant)
 
 SmemLayout fused_layout(const FusedPlan *const *plans, int n)
 {
-	int max_py = 0, max_pitch = 0, max_th = 0, hw = 0, vs = 0;
+	int max_pxa = 0, hw = 0, vs = 0, ring = 1, in = 1, stage = 1, seg_groups = 1, step_groups = 1;
 	bool u16 = false, h_first = false;
 	for (int i = 0; i < n; ++i) {
 		const FusedPlan &p = *plans[i];
-		max_py = std::max(max_py, p.max_py);
-		max_pitch = std::max(max_pitch, p.max_pitch);
-		max_th = std::max(max_th, p.job.tile_h);
+		max_pxa = std::max(max_pxa, p.max_pxa);
 		hw = std::max(hw, p.job.hw);
 		vs = std::max(vs, p.job.vs);
+		ring = std::max(ring, p.job.ring_rows);
+		in = std::max(in, p.job.in_rows);
+		stage = std::max(stage, p.stage_rows);
+		seg_groups = std::max(seg_groups, p.job.seg_groups);
+		step_groups = std::max(step_groups, p.job.step_groups);
 		u16 = p.job.kind == static_cast<int>(FusedKind::U16_EXACT);
 		h_first = p.job.h_first != 0;
 	}
 	auto a16 = [](size_t x) { return static_cast<int>((x + 15) / 16 * 16); };
-	const int e = u16 ? 2 : 4;
 	SmemLayout L{};
-	const int patch = a16(static_cast<size_t>(max_py) * max_pitch * e);
-	L.vcoef_off = patch;
-	L.htaps_off = L.vcoef_off + a16(static_cast<size_t>(max_th / kGroup) * vs * 16);
-	L.hleft_off = L.htaps_off + a16(static_cast<size_t>(kTileW) * hw * 4);
-	L.vbase_off = L.hleft_off + a16(kTileW * 4);
-	L.buf_bytes = L.vbase_off + a16(static_cast<size_t>(max_th / kGroup) * 4);
-	L.pf_off = 2 * L.buf_bytes;
-	const int pf = u16 ? a16(static_cast<size_t>(max_py) * max_pitch * 4) : 0;
-	L.i_off = L.pf_off + pf;
-	const size_t ib = h_first ? static_cast<size_t>(max_py) * kTileW * 4 : static_cast<size_t>(max_th) * max_pitch * 4;
-	L.total_bytes = L.i_off + a16(ib);
+	L.pitch = max_pxa + 8;
+	L.ring_rows = ring;
+	L.in_rows = h_first ? in : 1;
+	L.stage_rows = u16 ? stage : 1;
+	L.seg_groups = seg_groups;
+	L.step_groups = step_groups;
+	int off = 0;
+	L.ring_off = off;
+	off += a16(static_cast<size_t>(ring) * (h_first ? kStripW : L.pitch) * 4);
+	L.stage_off = off;
+	off += u16 ? a16(static_cast<size_t>(L.stage_rows) * L.pitch * 2) : 0;
+	L.in_off = off;
+	off += h_first ? a16(static_cast<size_t>(L.in_rows) * L.pitch * 4) : 0;
+	L.i_off = off;
+	off += h_first ? 0 : a16(static_cast<size_t>(step_groups) * kGroup * L.pitch * 4);
+	L.htaps_off = off;
+	off += a16(static_cast<size_t>(kStripW) * hw * 4);
+	L.hleft_off = off;
+	off += a16(kStripW * 4);
+	L.vcoef_off = off;
+	off += 2 * a16(static_cast<size_t>(step_groups) * vs * 16);
+	L.vbase_off = off;
+	off += a16(static_cast<size_t>(seg_groups) * 4);
+	L.total_bytes = off;
 	return L;
 }
 
 size_t fused_max_smem()
 {
-	return kSmemBudget;
+	return kSmemMax;
 }
 
 int fused_grid_size(int variant, size_t smem_bytes)
@@ -301,8 +335,8 @@ int fused_grid_size(int variant, size_t smem_bytes)
 	cudaGetDevice(&dev);
 	cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
 	const void *k = kernel_ptr(variant);
-	cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kSmemBudget));
-	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kTileThreads, smem_bytes) != cudaSuccess || per_sm < 1)
+	cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kSmemMax));
+	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kStreamThreads, smem_bytes) != cudaSuccess || per_sm < 1)
 		per_sm = 1;
 	return std::max(1, sms) * per_sm;
 }
@@ -313,6 +347,8 @@ cudaError_t launch_fused(int variant, const FusedJob *jobs, int num_jobs, int to
 	int hf, u16, hw, vs;
 	split_variant(variant, &hf, &u16, &hw, &vs);
 	grid = std::max(1, std::min(grid, total_tiles));
+	if (smem_bytes.total_bytes > static_cast<int>(kSmemMax))
+		return cudaErrorInvalidValue;
 	if (hf)
 		return u16 ? launch_fused_h_u16(hw, vs, jobs, num_jobs, total_tiles, smem_bytes, grid, single, stream)
 		           : launch_fused_h_f32(hw, vs, jobs, num_jobs, total_tiles, smem_bytes, grid, single, stream);

@@ -39,7 +39,7 @@ cudaError_t launch_fused_v_u16(int hw, int vs, const FusedJob *jobs, int num_job
 	FusedJob one = single;
 	SmemLayout layout = L;
 	void *args[] = { &jobs, &num_jobs, &total_tiles, &one, &layout };
-	return cudaLaunchKernel(k, dim3(grid), dim3(kTileThreads), args, static_cast<size_t>(L.total_bytes), stream);
+	return cudaLaunchKernel(k, dim3(grid), dim3(kStreamThreads), args, static_cast<size_t>(L.total_bytes), stream);
 }
 
 } // namespace zg

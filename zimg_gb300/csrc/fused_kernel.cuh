@@ -1,16 +1,19 @@
-// The fused two-pass tile kernel (template). Instantiated per variant in
+// The fused two-pass streaming kernel (template). Instantiated per variant in
 // fused_inst_*.cu.
 //
-// Per output tile (tile_h x kTileW):
-//   1. the tile's source patch src[win_row] x src[win_col], its vertical tap
-//      groups, horizontal taps and window tables arrive in shared memory by
-//      cp.async, issued while the CTA was still computing the previous tile
-//      (two buffers);
-//   2. u16 samples are re-centred to exact floats;
-//   3. first pass  (H for H-first, V for V-first) into a shared intermediate;
-//   4. second pass from the intermediate straight to the destination plane.
-// The intermediate never touches HBM. The grid is persistent: each CTA walks
-// the launch's global tile list with a stride of gridDim.x.
+// A work item is one strip of 128 output columns over one segment of output
+// rows. The CTA walks the segment in steps of step_groups * 4 output rows.
+// Source lines enter a ring of lines in shared memory by cp.async one step
+// ahead of use, as zimg's graph keeps a ring of lines per filter
+// (zimg.h:387-396), so each source line is read from HBM once per strip.
+//
+//   V-first step:  ring (source lines) --V--> I (intermediate lines of the
+//                  step) --H--> destination rows
+//   H-first step:  new source lines --H--> ring (intermediate lines)
+//                  ring --V--> destination rows
+//
+// u16 samples are staged raw and converted once to exact centred floats. The
+// grid is persistent: CTA b takes items b, b + gridDim.x, ...
 #pragma once
 
 #include "fused.h"
@@ -18,24 +21,9 @@
 namespace zg {
 namespace fused_detail {
 
-constexpr int kTileW = 128;  // output columns per tile
-constexpr int kThreads = kTileThreads;
+constexpr int kThreads = kStreamThreads;
 constexpr int kWarps = kThreads / 32;
 
-__device__ __forceinline__ int find_job(const FusedJob *__restrict__ jobs, int num_jobs, int t)
-{
-	int lo = 0, hi = num_jobs - 1;
-	while (lo < hi) {
-		const int mid = (lo + hi + 1) >> 1;
-		if (__ldg(&jobs[mid].tile_begin) <= t)
-			lo = mid;
-		else
-			hi = mid - 1;
-	}
-	return lo;
-}
-
-// ------------------------------------------------------------ async copies --
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem, int src_bytes)
 {
 	const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
@@ -69,135 +57,150 @@ __device__ __forceinline__ float u16_round(float acc, float magic, float pixel_m
 	return fminf(fmaxf(y, 12582912.0f), 12582912.0f + pixel_max);
 }
 
-// Everything one tile needs, resolved from the job table.
-struct Tile {
-	int job;
-	int r0, c0, ty, tx;
-	int rows_valid, cols_valid;
-	int ylo, py, xlo, pxa, pitch;
-	int tile_h, vec_ok;
+__device__ __forceinline__ int find_job(const FusedJob *__restrict__ jobs, int num_jobs, int t)
+{
+	int lo = 0, hi = num_jobs - 1;
+	while (lo < hi) {
+		const int mid = (lo + hi + 1) >> 1;
+		if (__ldg(&jobs[mid].item_begin) <= t)
+			lo = mid;
+		else
+			hi = mid - 1;
+	}
+	return lo;
+}
+
+// Registers-resident description of one work item.
+struct Item {
+	const char *src;
+	ptrdiff_t src_stride;
 	char *dst;
 	ptrdiff_t dst_stride;
+	const char *v_dense;
+	const int *v_base;
+	int src_w, src_h, dst_h, vec_ok;
+	int c0, cols_valid, xlo, pxa;
+	int g_begin, g_end, step_groups;
 	float magic, pixel_max, offset;
 };
 
-__device__ __forceinline__ Tile make_tile(const FusedJob &J, int job, int t)
+template <int HW>
+__device__ __forceinline__ Item make_item(const FusedJob &J, int t, char *smem, const SmemLayout &L)
 {
-	Tile T;
-	T.job = job;
-	const int local = t - J.tile_begin;
-	T.ty = local / J.tiles_x;
-	T.tx = local - T.ty * J.tiles_x;
-	T.r0 = T.ty * J.tile_h;
-	T.c0 = T.tx * kTileW;
-	T.rows_valid = min(J.tile_h, J.dst_h - T.r0);
-	T.cols_valid = min(kTileW, J.dst_w - T.c0);
-	T.ylo = __ldg(J.win_row + 2 * T.ty);
-	T.py = __ldg(J.win_row + 2 * T.ty + 1) - T.ylo;
-	T.xlo = __ldg(J.win_col + 2 * T.tx);
-	T.pxa = (__ldg(J.win_col + 2 * T.tx + 1) - T.xlo + 7) & ~7;
-	T.pitch = T.pxa + 8;
-	T.tile_h = J.tile_h;
-	T.vec_ok = J.vec_ok;
-	T.dst = static_cast<char *>(J.dst);
-	T.dst_stride = J.dst_stride;
-	T.magic = J.magic;
-	T.pixel_max = J.pixel_max;
-	T.offset = J.offset;
-	return T;
+	Item it;
+	const int local = t - J.item_begin;
+	const int seg = local / J.strips;
+	const int strip = local - seg * J.strips;
+	it.src = static_cast<const char *>(J.src);
+	it.src_stride = J.src_stride;
+	it.dst = static_cast<char *>(J.dst);
+	it.dst_stride = J.dst_stride;
+	it.v_dense = reinterpret_cast<const char *>(J.v_dense);
+	it.v_base = J.v_base;
+	it.src_w = J.src_w;
+	it.src_h = J.src_h;
+	it.dst_h = J.dst_h;
+	it.vec_ok = J.vec_ok;
+	it.c0 = strip * kStripW;
+	it.cols_valid = min(kStripW, J.dst_w - it.c0);
+	it.xlo = __ldg(J.win_col + 2 * strip);
+	it.pxa = (__ldg(J.win_col + 2 * strip + 1) - it.xlo + 7) & ~7;
+	it.g_begin = seg * J.seg_groups;
+	it.g_end = min(J.groups, it.g_begin + J.seg_groups);
+	it.step_groups = J.step_groups;
+	it.magic = J.magic;
+	it.pixel_max = J.pixel_max;
+	it.offset = J.offset;
+
+	// per-item tables: h taps and left offsets of the strip, group bases
+	const char *ht = reinterpret_cast<const char *>(J.h_taps) + static_cast<size_t>(it.c0) * HW * 4;
+	for (int i = threadIdx.x; i < kStripW * HW / 4; i += kThreads) {
+		const bool ok = (i * 4) / HW < it.cols_valid;
+		cp_async16(smem + L.htaps_off + i * 16, ok ? ht + i * 16 : ht, ok ? 16 : 0);
+	}
+	for (int i = threadIdx.x; i < kStripW / 4; i += kThreads) {
+		const int n = max(0, min(4, it.cols_valid - 4 * i));
+		cp_async16(smem + L.hleft_off + i * 16, n ? J.h_left + it.c0 + 4 * i : J.h_left, n * 4);
+	}
+	int *vb = reinterpret_cast<int *>(smem + L.vbase_off);
+	for (int g = it.g_begin + threadIdx.x; g < it.g_end; g += kThreads)
+		vb[g - it.g_begin] = __ldg(J.v_base + g);
+	return it;
 }
 
-// Issue the async copies of one tile into buffer `buf`:
-//   patch (source samples, zero outside the plane), v-group taps, h taps,
-//   h left offsets, v group bases.
-template <bool U16, int HW, int VS>
-__device__ __forceinline__ void prefetch_tile(const FusedJob &J, const Tile &T, char *buf, const SmemLayout &L)
+// Lines [a, b) of the source strip into ring slots (line & mask) of `ring`
+// (pitch elements of E bytes per line), zero outside the plane. Warp w takes
+// lines a + w, a + w + 4, ...
+template <bool U16>
+__device__ __forceinline__ void load_lines(const Item &it, int a, int b, char *ring, int mask, int pitch)
 {
+	constexpr int E = U16 ? 2 : 4;
+	constexpr int PER = 16 / E;
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-	constexpr int E = U16 ? 2 : 4;          // bytes per sample
-	constexpr int PER = 16 / E;             // samples per 16-byte chunk
-	const char *src = static_cast<const char *>(J.src);
-	char *patch = buf;
-	const int chunks = T.pxa / PER;
-	const int row_bytes = T.pitch * E;
-	for (int r = warp; r < T.py; r += kWarps) {
-		const int gy = T.ylo + r;
-		const bool row_ok = gy < J.src_h;
-		const char *row = src + static_cast<ptrdiff_t>(row_ok ? gy : 0) * J.src_stride;
-		char *srow = patch + r * row_bytes;
-		if (J.vec_ok) {
+	const int chunks = it.pxa / PER;
+	for (int y = a + warp; y < b; y += kWarps) {
+		const bool row_ok = y < it.src_h;
+		const char *row = it.src + static_cast<ptrdiff_t>(row_ok ? y : 0) * it.src_stride;
+		char *srow = ring + (y & mask) * pitch * E;
+		if (it.vec_ok) {
 			for (int q = lane; q < chunks; q += 32) {
-				const int gx = T.xlo + q * PER;
-				int n = row_ok ? min(PER, J.src_w - gx) : 0;
-				n = max(n, 0);
-				cp_async16(srow + q * 16, n ? row + static_cast<ptrdiff_t>(gx) * E : src, n * E);
+				const int gx = it.xlo + q * PER;
+				const int n = row_ok ? max(0, min(PER, it.src_w - gx)) : 0;
+				cp_async16(srow + q * 16, n ? row + static_cast<ptrdiff_t>(gx) * E : it.src, n * E);
 			}
 		} else if (!U16) {
-			for (int x = lane; x < T.pxa; x += 32) {
-				const int gx = T.xlo + x;
-				const bool ok = row_ok && gx < J.src_w;
-				cp_async4(srow + x * 4, ok ? row + static_cast<ptrdiff_t>(gx) * 4 : src, ok ? 4 : 0);
+			for (int x = lane; x < it.pxa; x += 32) {
+				const int gx = it.xlo + x;
+				const bool ok = row_ok && gx < it.src_w;
+				cp_async4(srow + x * 4, ok ? row + static_cast<ptrdiff_t>(gx) * 4 : it.src, ok ? 4 : 0);
 			}
 		} else {
-			// 2-byte samples at 2-byte alignment: plain loads
-			for (int x = lane; x < T.pxa; x += 32) {
-				const int gx = T.xlo + x;
-				const bool ok = row_ok && gx < J.src_w;
-				reinterpret_cast<uint16_t *>(srow)[x] = ok ? __ldg(reinterpret_cast<const uint16_t *>(row) + gx) : 0;
+			for (int x = lane; x < it.pxa; x += 32) {
+				const int gx = it.xlo + x;
+				const bool ok = row_ok && gx < it.src_w;
+				reinterpret_cast<uint16_t *>(srow)[x] =
+					ok ? __ldg(reinterpret_cast<const uint16_t *>(row) + gx) : static_cast<uint16_t>(0);
 			}
 		}
 	}
-	// v-group taps: groups [r0/4, r0/4 + tile_h/4), VS float4 each
-	const int groups = J.tile_h / kGroup;
-	const char *vd = reinterpret_cast<const char *>(J.v_dense) + static_cast<size_t>(T.r0 / kGroup) * VS * 16;
-	for (int i = threadIdx.x; i < groups * VS; i += kThreads)
-		cp_async16(buf + L.vcoef_off + i * 16, vd + i * 16, 16);
-	// h taps of the tile's columns (zero past the plane)
-	const char *ht = reinterpret_cast<const char *>(J.h_taps) + static_cast<size_t>(T.c0) * HW * 4;
-	for (int i = threadIdx.x; i < kTileW * HW / 4; i += kThreads) {
-		const int col = (i * 4) / HW;
-		cp_async16(buf + L.htaps_off + i * 16, col < T.cols_valid ? ht + i * 16 : ht, col < T.cols_valid ? 16 : 0);
-	}
-	for (int i = threadIdx.x; i < kTileW / 4; i += kThreads) {
-		const int n = max(0, min(4, T.cols_valid - 4 * i));
-		cp_async16(buf + L.hleft_off + i * 16, n ? J.h_left + T.c0 + 4 * i : J.h_left, n * 4);
-	}
-	for (int i = threadIdx.x; i < groups / 4; i += kThreads)
-		cp_async16(buf + L.vbase_off + i * 16, J.v_base + T.r0 / kGroup + 4 * i, 16);
 }
 
-// u16 patch (raw samples in buf) -> centred floats in Pf.
-__device__ __forceinline__ void convert_u16(const Tile &T, const char *buf, float *Pf, float offset)
+// Convert the u16 lines this thread loaded with load_lines(a, b) from the
+// raw staging ring to centred floats in `ring`.
+__device__ __forceinline__ void convert_lines(const Item &it, int a, int b, const char *stage, int smask,
+                                              float *ring, int rmask, int pitch)
 {
-	const float bias = 8388608.0f + offset;
-	const int chunks = T.pxa / 8;
-	for (int i = threadIdx.x; i < T.py * chunks; i += kThreads) {
-		const int r = i / chunks, q = i - r * chunks;
-		const uint4 u = *reinterpret_cast<const uint4 *>(buf + r * T.pitch * 2 + q * 16);
-		const uint32_t w[4] = { u.x, u.y, u.z, u.w };
-		float f[8];
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	const float bias = 8388608.0f + it.offset;
+	const int chunks = it.pxa / 8;
+	for (int y = a + warp; y < b; y += kWarps) {
+		const char *srow = stage + (y & smask) * pitch * 2;
+		float *drow = ring + (y & rmask) * pitch;
+		for (int q = lane; q < chunks; q += 32) {
+			const uint4 u = *reinterpret_cast<const uint4 *>(srow + q * 16);
+			const uint32_t w[4] = { u.x, u.y, u.z, u.w };
+			float f[8];
 #pragma unroll
-		for (int k = 0; k < 8; ++k) {
-			const uint32_t v = (w[k >> 1] >> (16 * (k & 1))) & 0xFFFFu;
-			f[k] = __int_as_float(0x4B000000 | v) - bias;
+			for (int k = 0; k < 8; ++k)
+				f[k] = __int_as_float(0x4B000000 | ((w[k >> 1] >> (16 * (k & 1))) & 0xFFFFu)) - bias;
+			*reinterpret_cast<float4 *>(drow + q * 8) = make_float4(f[0], f[1], f[2], f[3]);
+			*reinterpret_cast<float4 *>(drow + q * 8 + 4) = make_float4(f[4], f[5], f[6], f[7]);
 		}
-		float *d = Pf + r * T.pitch + q * 8;
-		*reinterpret_cast<float4 *>(d) = make_float4(f[0], f[1], f[2], f[3]);
-		*reinterpret_cast<float4 *>(d + 4) = make_float4(f[4], f[5], f[6], f[7]);
 	}
 }
 
-// Horizontal pass: out[y][c] = sum_k taps[c][k] * in[y][left[c] - xlo + k].
-// One thread per output column (taps in registers), rows strided by the CTA.
+// Horizontal pass over lines [a, b): out[y][c] = sum_k taps[c][k] * in[y][left[c] - xlo + k].
+// Thread = output column; two lines per iteration for independent chains.
+// FINAL: write destination rows (row index = r0 + (y - a)); else write ring
+// slots (y & omask) of `out`.
 template <bool U16, bool FINAL, int HW>
-__device__ __forceinline__ void h_pass(const Tile &T, const char *buf, const SmemLayout &L,
-                                       const float *__restrict__ in, int in_pitch, int rows, float *__restrict__ I,
-                                       int i_pitch)
+__device__ __forceinline__ void h_pass(const Item &it, const char *smem, const SmemLayout &L, const float *in,
+                                       int imask, int a, int b, float *out, int omask, int r0)
 {
-	const int c = threadIdx.x % kTileW;
-	const bool col_ok = c < T.cols_valid;
+	const int c = threadIdx.x;
+	const bool col_ok = c < it.cols_valid;
 	float taps[HW];
-	const float4 *tp = reinterpret_cast<const float4 *>(buf + L.htaps_off) + c * (HW / 4);
+	const float4 *tp = reinterpret_cast<const float4 *>(smem + L.htaps_off) + c * (HW / 4);
 #pragma unroll
 	for (int k = 0; k < HW / 4; ++k) {
 		const float4 t4 = tp[k];
@@ -206,60 +209,81 @@ __device__ __forceinline__ void h_pass(const Tile &T, const char *buf, const Sme
 		taps[4 * k + 2] = t4.z;
 		taps[4 * k + 3] = t4.w;
 	}
-	const int l = col_ok ? reinterpret_cast<const int *>(buf + L.hleft_off)[c] - T.xlo : 0;
+	const int l = col_ok ? reinterpret_cast<const int *>(smem + L.hleft_off)[c] - it.xlo : 0;
 	const float init = U16 ? 8192.0f : 0.0f;
-	for (int y = threadIdx.x / kTileW; y < rows; y += kThreads / kTileW) {
-		const float *row = in + y * in_pitch + l;
-		float acc = init;
+	const int pitch = L.pitch;
+	for (int y = a; y < b; y += 2) {
+		const bool two = y + 1 < b;
+		const float *r0p = in + (y & imask) * pitch + l;
+		const float *r1p = in + ((y + 1) & imask) * pitch + l;
+		float acc0 = init, acc1 = init;
 #pragma unroll
-		for (int k = 0; k < HW; ++k)
-			acc = __fmaf_rn(taps[k], row[k], acc);
+		for (int k = 0; k < HW; ++k) {
+			acc0 = __fmaf_rn(taps[k], r0p[k], acc0);
+			acc1 = __fmaf_rn(taps[k], r1p[k], acc1);
+		}
 		if (!FINAL) {
-			float v = acc;
-			if (U16)
-				v = u16_round(acc, T.magic, T.pixel_max) - T.magic;
-			I[y * i_pitch + c] = v;
-		} else if (col_ok && y < T.rows_valid) {
-			char *drow = T.dst + static_cast<ptrdiff_t>(T.r0 + y) * T.dst_stride;
+			float v0 = acc0, v1 = acc1;
 			if (U16) {
-				const float q = u16_round(acc, T.magic, T.pixel_max);
-				reinterpret_cast<uint16_t *>(drow)[T.c0 + c] = static_cast<uint16_t>(__float_as_uint(q) & 0xFFFFu);
+				v0 = u16_round(acc0, it.magic, it.pixel_max) - it.magic;
+				v1 = u16_round(acc1, it.magic, it.pixel_max) - it.magic;
+			}
+			out[(y & omask) * kStripW + c] = v0;
+			if (two)
+				out[((y + 1) & omask) * kStripW + c] = v1;
+		} else if (col_ok) {
+			const int oy = r0 + (y - a);
+			char *d0 = it.dst + static_cast<ptrdiff_t>(oy) * it.dst_stride;
+			if (U16) {
+				const uint32_t q0 = __float_as_uint(u16_round(acc0, it.magic, it.pixel_max)) & 0xFFFFu;
+				const uint32_t q1 = __float_as_uint(u16_round(acc1, it.magic, it.pixel_max)) & 0xFFFFu;
+				if (oy < it.dst_h)
+					reinterpret_cast<uint16_t *>(d0)[it.c0 + c] = static_cast<uint16_t>(q0);
+				if (two && oy + 1 < it.dst_h)
+					reinterpret_cast<uint16_t *>(d0 + it.dst_stride)[it.c0 + c] = static_cast<uint16_t>(q1);
 			} else {
-				reinterpret_cast<float *>(drow)[T.c0 + c] = acc;
+				if (oy < it.dst_h)
+					reinterpret_cast<float *>(d0)[it.c0 + c] = acc0;
+				if (two && oy + 1 < it.dst_h)
+					reinterpret_cast<float *>(d0 + it.dst_stride)[it.c0 + c] = acc1;
 			}
 		}
 	}
 }
 
-// Vertical pass with dense groups of kGroup output rows:
-// out[g*4 + j][x] = sum_s dense[g][s][j] * in[base[g] - ylo + s][x], four
-// adjacent columns per thread (16-byte shared loads, broadcast tap loads).
+// Vertical pass for groups [g0, g1): out line (g - g0)*4 + j, columns 4q..4q+3:
+//   sum_s dense[g][s][j] * in[(base[g] + s) & imask][4q + e]
+// FINAL: destination rows g*4 + j (columns c0 + 4q ...); else lines of I.
 template <bool U16, bool FINAL, int VS>
-__device__ __forceinline__ void v_pass(const Tile &T, const char *buf, const SmemLayout &L,
-                                       const float *__restrict__ in, int in_pitch, int quads, float *__restrict__ I,
-                                       int i_pitch)
+__device__ __forceinline__ void v_pass(const Item &it, const char *smem, const SmemLayout &L, const float *in,
+                                       int imask, int in_pitch, int g0, int g1, const float4 *coef, int quads,
+                                       float *I, int i_pitch)
 {
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	const float init = U16 ? 8192.0f : 0.0f;
-	const int groups = T.tile_h / kGroup;
-	const float4 *dense_all = reinterpret_cast<const float4 *>(buf + L.vcoef_off);
-	const int *vbase = reinterpret_cast<const int *>(buf + L.vbase_off);
-	for (int g = warp; g < groups; g += kWarps) {
-		const int base = vbase[g] - T.ylo;
-		const float4 *dense = dense_all + g * VS;
-		for (int qx = lane; qx < quads; qx += 32) {
+	const int ng = g1 - g0;
+	const int wpg = ng >= kWarps ? 1 : kWarps / ng;  // warps per group
+	const int *vb = reinterpret_cast<const int *>(smem + L.vbase_off);
+	for (int gi = warp / wpg; gi < ng; gi += kWarps / wpg) {
+		const int g = g0 + gi;
+		const int base = vb[g - it.g_begin];
+		const float4 *cf = coef + gi * VS;
+		int off[VS];
+#pragma unroll
+		for (int s = 0; s < VS; ++s)
+			off[s] = ((base + s) & imask) * in_pitch;
+		for (int q = (warp % wpg) * 32 + lane; q < quads; q += wpg * 32) {
 			float acc[kGroup][4];
 #pragma unroll
 			for (int j = 0; j < kGroup; ++j)
 #pragma unroll
 				for (int e = 0; e < 4; ++e)
 					acc[j][e] = init;
-			const float *col = in + base * in_pitch + 4 * qx;
 #pragma unroll
 			for (int s = 0; s < VS; ++s) {
-				const float4 x = *reinterpret_cast<const float4 *>(col + s * in_pitch);
-				const float4 cf = dense[s];
-				const float cj[4] = { cf.x, cf.y, cf.z, cf.w };
+				const float4 x = *reinterpret_cast<const float4 *>(in + off[s] + 4 * q);
+				const float4 c4 = cf[s];
+				const float cj[4] = { c4.x, c4.y, c4.z, c4.w };
 #pragma unroll
 				for (int j = 0; j < kGroup; ++j) {
 					acc[j][0] = __fmaf_rn(cj[j], x.x, acc[j][0]);
@@ -270,43 +294,45 @@ __device__ __forceinline__ void v_pass(const Tile &T, const char *buf, const Sme
 			}
 #pragma unroll
 			for (int j = 0; j < kGroup; ++j) {
-				const int r = g * kGroup + j;
 				if (!FINAL) {
 					float4 v;
 					if (U16) {
-						v.x = u16_round(acc[j][0], T.magic, T.pixel_max) - T.magic;
-						v.y = u16_round(acc[j][1], T.magic, T.pixel_max) - T.magic;
-						v.z = u16_round(acc[j][2], T.magic, T.pixel_max) - T.magic;
-						v.w = u16_round(acc[j][3], T.magic, T.pixel_max) - T.magic;
+						v.x = u16_round(acc[j][0], it.magic, it.pixel_max) - it.magic;
+						v.y = u16_round(acc[j][1], it.magic, it.pixel_max) - it.magic;
+						v.z = u16_round(acc[j][2], it.magic, it.pixel_max) - it.magic;
+						v.w = u16_round(acc[j][3], it.magic, it.pixel_max) - it.magic;
 					} else {
 						v = make_float4(acc[j][0], acc[j][1], acc[j][2], acc[j][3]);
 					}
-					*reinterpret_cast<float4 *>(I + r * i_pitch + 4 * qx) = v;
-				} else if (r < T.rows_valid) {
-					const int x0 = 4 * qx;
-					char *drow = T.dst + static_cast<ptrdiff_t>(T.r0 + r) * T.dst_stride;
+					*reinterpret_cast<float4 *>(I + (gi * kGroup + j) * i_pitch + 4 * q) = v;
+				} else {
+					const int r = g * kGroup + j;
+					if (r >= it.dst_h)
+						continue;
+					const int x0 = 4 * q;
+					char *drow = it.dst + static_cast<ptrdiff_t>(r) * it.dst_stride;
 					if (U16) {
-						uint32_t q[4];
+						uint32_t u[4];
 #pragma unroll
 						for (int e = 0; e < 4; ++e)
-							q[e] = __float_as_uint(u16_round(acc[j][e], T.magic, T.pixel_max)) & 0xFFFFu;
-						uint16_t *d = reinterpret_cast<uint16_t *>(drow) + T.c0 + x0;
-						if (T.vec_ok && x0 + 3 < T.cols_valid) {
-							*reinterpret_cast<uint2 *>(d) = make_uint2(q[0] | (q[1] << 16), q[2] | (q[3] << 16));
+							u[e] = __float_as_uint(u16_round(acc[j][e], it.magic, it.pixel_max)) & 0xFFFFu;
+						uint16_t *d = reinterpret_cast<uint16_t *>(drow) + it.c0 + x0;
+						if (it.vec_ok && x0 + 3 < it.cols_valid) {
+							*reinterpret_cast<uint2 *>(d) = make_uint2(u[0] | (u[1] << 16), u[2] | (u[3] << 16));
 						} else {
 #pragma unroll
 							for (int e = 0; e < 4; ++e)
-								if (x0 + e < T.cols_valid)
-									d[e] = static_cast<uint16_t>(q[e]);
+								if (x0 + e < it.cols_valid)
+									d[e] = static_cast<uint16_t>(u[e]);
 						}
 					} else {
-						float *d = reinterpret_cast<float *>(drow) + T.c0 + x0;
-						if (T.vec_ok && x0 + 3 < T.cols_valid) {
+						float *d = reinterpret_cast<float *>(drow) + it.c0 + x0;
+						if (it.vec_ok && x0 + 3 < it.cols_valid) {
 							*reinterpret_cast<float4 *>(d) = make_float4(acc[j][0], acc[j][1], acc[j][2], acc[j][3]);
 						} else {
 #pragma unroll
 							for (int e = 0; e < 4; ++e)
-								if (x0 + e < T.cols_valid)
+								if (x0 + e < it.cols_valid)
 									d[e] = acc[j][e];
 						}
 					}
@@ -316,60 +342,110 @@ __device__ __forceinline__ void v_pass(const Tile &T, const char *buf, const Sme
 	}
 }
 
+// Source-line range a step needs: groups [g0, g1) read lines
+// [base[g0], base[g1 - 1] + VS) (bases are non-decreasing).
+template <int VS>
+__device__ __forceinline__ int step_end(const Item &it, const char *smem, const SmemLayout &L, int g1)
+{
+	return reinterpret_cast<const int *>(smem + L.vbase_off)[g1 - 1 - it.g_begin] + VS;
+}
+
+template <int VS>
+__device__ __forceinline__ void load_coef(const Item &it, int g0, int g1, char *dst)
+{
+	const char *src = it.v_dense + static_cast<size_t>(g0) * VS * 16;
+	for (int i = threadIdx.x; i < (g1 - g0) * VS; i += kThreads)
+		cp_async16(dst + i * 16, src + i * 16, 16);
+}
+
 template <bool H_FIRST, bool U16, int HW, int VS>
-__global__ void __launch_bounds__(kThreads, 2)
-fused_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_tiles, const __grid_constant__ FusedJob single,
+__global__ void __launch_bounds__(kThreads, 4)
+fused_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, const __grid_constant__ FusedJob single,
              const __grid_constant__ SmemLayout L)
 {
 	extern __shared__ float4 smem4[];
 	char *smem = reinterpret_cast<char *>(smem4);
+	float *ring = reinterpret_cast<float *>(smem + L.ring_off);
+	char *stage = smem + L.stage_off;
+	float *in = reinterpret_cast<float *>(smem + L.in_off);
+	float *I = reinterpret_cast<float *>(smem + L.i_off);
+	const int rmask = L.ring_rows - 1;
+	const int smask = L.stage_rows - 1;
+	const int imask = L.in_rows - 1;
 
-	int t = blockIdx.x;
-	if (t >= total_tiles)
-		return;
-	const FusedJob *Jp = jobs ? &jobs[find_job(jobs, num_jobs, t)] : &single;
-	Tile T = make_tile(*Jp, 0, t);
-	prefetch_tile<U16, HW, VS>(*Jp, T, smem, L);
-	cp_async_commit();
+	// Lines a step reads but does not load keep finite values: clear the rings once.
+	for (int i = threadIdx.x; i < L.vcoef_off / 16; i += kThreads)
+		smem4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+	__syncthreads();
 
-	for (int it = 0; t < total_tiles; ++it, t += gridDim.x) {
-		char *buf = smem + (it & 1) * L.buf_bytes;
-		// prefetch the next tile of this CTA into the other buffer
-		const int tn = t + gridDim.x;
-		Tile Tn;
-		if (tn < total_tiles) {
-			const FusedJob *Jn = jobs ? &jobs[find_job(jobs, num_jobs, tn)] : &single;
-			Tn = make_tile(*Jn, 0, tn);
-			prefetch_tile<U16, HW, VS>(*Jn, Tn, smem + ((it + 1) & 1) * L.buf_bytes, L);
-		}
-		cp_async_commit();
-		cp_async_wait<1>();
-		__syncthreads();
+	for (int t = blockIdx.x; t < total_items; t += gridDim.x) {
+		const FusedJob *Jp = jobs ? &jobs[find_job(jobs, num_jobs, t)] : &single;
+		const Item it = make_item<HW>(*Jp, t, smem, L);
+		__syncthreads();  // group bases visible
 
-		const float *P;
-		if (U16) {
-			float *Pf = reinterpret_cast<float *>(smem + L.pf_off);
-			convert_u16(T, buf, Pf, T.offset);
-			__syncthreads();
-			P = Pf;
-		} else {
-			P = reinterpret_cast<const float *>(buf);
+		const int nsteps = (it.g_end - it.g_begin + it.step_groups - 1) / it.step_groups;
+		// step k covers groups [gk, gk1); its new source lines are [lo_k, hi_k)
+		int hi_prev = reinterpret_cast<const int *>(smem + L.vbase_off)[0];
+		auto step_groups_of = [&](int k, int *g0, int *g1) {
+			*g0 = it.g_begin + k * it.step_groups;
+			*g1 = min(it.g_end, *g0 + it.step_groups);
+		};
+		// prologue: step 0's lines and taps
+		{
+			int g0, g1;
+			step_groups_of(0, &g0, &g1);
+			const int hi = step_end<VS>(it, smem, L, g1);
+			if (U16)
+				load_lines<true>(it, hi_prev, hi, stage, smask, L.pitch);
+			else
+				load_lines<false>(it, hi_prev, hi, reinterpret_cast<char *>(H_FIRST ? in : ring),
+				                  H_FIRST ? imask : rmask, L.pitch);
+			load_coef<VS>(it, g0, g1, smem + L.vcoef_off);
+			cp_async_commit();
 		}
-		float *I = reinterpret_cast<float *>(smem + L.i_off);
-		if (H_FIRST) {
-			h_pass<U16, false, HW>(T, buf, L, P, T.pitch, T.py, I, kTileW);
+		__syncthreads();  // lines stored by plain loads (unaligned u16) are visible to every converter
+		int lo_cur = hi_prev;
+		int hi_cur = step_end<VS>(it, smem, L, min(it.g_end, it.g_begin + it.step_groups));
+
+		for (int k = 0; k < nsteps; ++k) {
+			int g0, g1;
+			step_groups_of(k, &g0, &g1);
+			// prefetch step k+1
+			int hi_next = hi_cur;
+			if (k + 1 < nsteps) {
+				int n0, n1;
+				step_groups_of(k + 1, &n0, &n1);
+				hi_next = step_end<VS>(it, smem, L, n1);
+				if (U16)
+					load_lines<true>(it, hi_cur, hi_next, stage, smask, L.pitch);
+				else
+					load_lines<false>(it, hi_cur, hi_next, reinterpret_cast<char *>(H_FIRST ? in : ring),
+					                  H_FIRST ? imask : rmask, L.pitch);
+				load_coef<VS>(it, n0, n1, smem + L.vcoef_off + ((k + 1) & 1) * (L.vbase_off - L.vcoef_off) / 2);
+			}
+			cp_async_commit();
+			cp_async_wait<1>();
+			if (U16)
+				convert_lines(it, lo_cur, hi_cur, stage, smask, H_FIRST ? in : ring, H_FIRST ? imask : rmask, L.pitch);
 			__syncthreads();
-			v_pass<U16, true, VS>(T, buf, L, I, kTileW, kTileW / 4, nullptr, 0);
-		} else {
-			v_pass<U16, false, VS>(T, buf, L, P, T.pitch, T.pxa / 4, I, T.pitch);
-			__syncthreads();
-			h_pass<U16, true, HW>(T, buf, L, I, T.pitch, T.tile_h, nullptr, 0);
+
+			const float4 *coef = reinterpret_cast<const float4 *>(smem + L.vcoef_off + (k & 1) * (L.vbase_off - L.vcoef_off) / 2);
+			if (H_FIRST) {
+				// new source lines -> intermediate ring
+				h_pass<U16, false, HW>(it, smem, L, in, imask, lo_cur, hi_cur, ring, rmask, 0);
+				__syncthreads();
+				v_pass<U16, true, VS>(it, smem, L, ring, rmask, kStripW, g0, g1, coef, kStripW / 4, nullptr, 0);
+			} else {
+				v_pass<U16, false, VS>(it, smem, L, ring, rmask, L.pitch, g0, g1, coef, it.pxa / 4, I, L.pitch);
+				__syncthreads();
+				h_pass<U16, true, HW>(it, smem, L, I, 0x7fffffff, 0, (g1 - g0) * kGroup, nullptr, 0, g0 * kGroup);
+			}
+			lo_cur = hi_cur;
+			hi_cur = hi_next;
 		}
-		__syncthreads();  // this buffer and I are free for the next iteration
-		if (tn < total_tiles)
-			T = Tn;
+		cp_async_wait<0>();
+		__syncthreads();  // the next item reuses every buffer
 	}
-	cp_async_wait<0>();
 }
 
 } // namespace fused_detail
