@@ -79,7 +79,7 @@ typedef enum zg_resample_filter {
 typedef enum zg_engine {
 	ZG_ENGINE_AUTO = 0,    /* autotuner's choice */
 	ZG_ENGINE_CUDA = 1,    /* CUDA-core kernels only */
-	ZG_ENGINE_TENSOR = 2   /* banded GEMM on the tensor cores where the pass allows it (FLOAT only) */
+	ZG_ENGINE_TENSOR = 2   /* banded matrix products on the tensor cores where the conversion allows it */
 } zg_engine;
 
 /* ------------------------------------------------------------------ errors --
@@ -170,7 +170,8 @@ ZG_API void zg_resize_free(zg_resize *r);
 /* Device scratch bytes that zg_resize_process needs (0 when fused or single pass). */
 ZG_API zg_error_code zg_resize_get_tmp_size(const zg_resize *r, size_t *out);
 /* Number of passes (0 = plain copy, 1, 2), whether the first is horizontal, and
- * whether the passes run fused in one kernel. */
+ * how the passes run: 0 separate kernels, 1 one fused CUDA-core kernel, 2 one
+ * fused tensor-core kernel. */
 ZG_API zg_error_code zg_resize_get_info(const zg_resize *r, int *num_passes, int *first_horizontal, int *fused);
 ZG_API zg_error_code zg_resize_process(const zg_resize *r, const void *src, ptrdiff_t src_stride,
                                 void *dst, ptrdiff_t dst_stride, void *tmp, zg_stream stream);

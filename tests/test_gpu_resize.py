@@ -107,12 +107,30 @@ def test_config1_fhd_to_uhd_u16_bitexact(cuda, oracle):
     np.testing.assert_array_equal(got, want)
 
 
-def test_config1_two_pass_equals_fused(cuda, oracle):
+def test_config1_engines_agree(cuda, oracle):
+    """Tensor-core fused, CUDA-core fused and separate passes give zimg's bytes."""
     rng = np.random.default_rng(7)
     src = make_u16(rng, 270, 480, 10)
-    a, _ = run_conversion(src, 960, 540, "lanczos", 3, depth=10, fusion=True)
-    b, _ = run_conversion(src, 960, 540, "lanczos", 3, depth=10, fusion=False)
-    np.testing.assert_array_equal(a, b)
+    want = oracle.resize_plane(src, 960, 540, "lanczos", 3, depth=10, mode="c")
+    for engine, fusion, expect in (("auto", True, "tensor"), ("cuda", True, "cuda"), ("cuda", False, "passes")):
+        got, r = run_conversion(src, 960, 540, "lanczos", 3, depth=10, fusion=fusion, engine=engine)
+        assert r.info["engine"] == expect
+        np.testing.assert_array_equal(got, want, err_msg=engine)
+
+
+@pytest.mark.parametrize("depth", [8, 10, 12])
+@pytest.mark.parametrize("shape", [(1920, 1080, 3840, 2160), (720, 480, 1920, 1080), (3840, 2160, 1920, 1080),
+                                   (333, 97, 1001, 500), (640, 480, 427, 320)])
+def test_tensor_core_u16_bitexact(cuda, oracle, depth, shape):
+    """The tensor-core path (exact integer arithmetic in fp16 x fp16 -> fp32)."""
+    sw, sh, dw, dh = shape
+    rng = np.random.default_rng(depth * 1000 + sw)
+    src = make_u16(rng, sh, sw, depth)
+    for kind, a in (("spline36", math.nan), ("lanczos", 3.0), ("bicubic", math.nan)):
+        got, r = run_conversion(src, dw, dh, kind, a, depth=depth, engine="tensor")
+        assert r.info["engine"] == "tensor", (shape, kind)
+        want = oracle.resize_plane(src, dw, dh, kind, a, depth=depth, mode="c", nthreads=16)
+        np.testing.assert_array_equal(got, want, err_msg=str((shape, kind, depth)))
 
 
 def _f32_check(oracle, src, got, dst_w, dst_h, kind, a=math.nan, b=math.nan, exact=True, **kw):

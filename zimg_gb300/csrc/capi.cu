@@ -293,9 +293,15 @@ zg_error_code zg_resize_create(const zg_resize_params *params, zg_resize **out)
 			const DevicePass &p0 = *r->pass[0];
 			r->tmp_stride = static_cast<ptrdiff_t>((static_cast<size_t>(p0.dst_w) * bytes_of(r->sample) + 255) & ~static_cast<size_t>(255));
 			r->tmp_size = static_cast<size_t>(r->tmp_stride) * p0.dst_h;
-			if (q.allow_fusion && q.engine != ZG_ENGINE_TENSOR &&
-			    plan_fused(r->pass[0]->table, r->pass[1]->table, r->first_horizontal, r->sample == Sample::U16,
-			               q.depth, q.src_width, q.src_height, q.dst_width, q.dst_height, &r->fplan)) {
+			const bool u16 = r->sample == Sample::U16;
+			bool planned = false;
+			if (q.allow_fusion && u16 && q.engine != ZG_ENGINE_CUDA)
+				planned = plan_mma(r->pass[0]->table, r->pass[1]->table, r->first_horizontal, q.depth, q.src_width,
+				                   q.src_height, q.dst_width, q.dst_height, &r->fplan);
+			if (!planned && q.allow_fusion && q.engine != ZG_ENGINE_TENSOR)
+				planned = plan_fused(r->pass[0]->table, r->pass[1]->table, r->first_horizontal, u16, q.depth,
+				                     q.src_width, q.src_height, q.dst_width, q.dst_height, &r->fplan);
+			if (planned) {
 				r->fblob.reset(r->fplan.blob.size());
 				cuda_check(cudaMemcpy(r->fblob.get(), r->fplan.blob.data(), r->fplan.blob.size(),
 				                      cudaMemcpyHostToDevice), "upload fused tables");
@@ -334,7 +340,7 @@ zg_error_code zg_resize_get_info(const zg_resize *r, int *num_passes, int *first
 			throw Error(kErrIllegalArgument, "null pointer");
 		if (num_passes) *num_passes = r->num_passes;
 		if (first_horizontal) *first_horizontal = r->first_horizontal;
-		if (fused) *fused = r->fused;
+		if (fused) *fused = r->fused ? (r->fplan.mma ? 2 : 1) : 0;
 	});
 }
 

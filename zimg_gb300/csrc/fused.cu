@@ -269,6 +269,8 @@ void split_variant(int variant, int *hf, int *u16, int *hw_i, int *vs_i)
 
 const void *kernel_ptr(int variant)
 {
+	if (variant >= 100)
+		return mma_kernel_ptr(variant);
 	int hf, u16, hw, vs;
 	split_variant(variant, &hf, &u16, &hw, &vs);
 	if (hf)
@@ -280,6 +282,8 @@ const void *kernel_ptr(int variant)
 
 SmemLayout fused_layout(const FusedPlan *const *plans, int n)
 {
+	if (n > 0 && plans[0]->mma)
+		return mma_layout(plans, n);
 	int max_pxa = 0, hw = 0, vs = 0, ring = 1, in = 1, stage = 1, seg_groups = 1, step_groups = 1;
 	bool u16 = false, h_first = false;
 	for (int i = 0; i < n; ++i) {
@@ -344,6 +348,8 @@ int fused_grid_size(int variant, size_t smem_bytes)
 cudaError_t launch_fused(int variant, const FusedJob *jobs, int num_jobs, int total_tiles, const SmemLayout &smem_bytes,
                          int grid, const FusedJob &single, cudaStream_t stream)
 {
+	if (variant >= 100)
+		return launch_mma(variant, jobs, num_jobs, total_tiles, smem_bytes, grid, single, stream);
 	int hf, u16, hw, vs;
 	split_variant(variant, &hf, &u16, &hw, &vs);
 	grid = std::max(1, std::min(grid, total_tiles));

@@ -93,6 +93,7 @@ struct FusedPlan {
 	int variant = 0;         // kernel instantiation index
 	int max_pxa = 0;         // widest strip patch (elements)
 	int stage_rows = 1;      // u16 raw staging lines
+	bool mma = false;        // tensor-core variant (mma_kernel.cuh)
 	std::vector<unsigned char> blob;  // host copy of the tables, uploaded by the owner
 	size_t off_h_taps = 0, off_h_left = 0, off_v_dense = 0, off_v_base = 0, off_win_col = 0;
 };
@@ -127,6 +128,16 @@ cudaError_t launch_fused(int variant, const FusedJob *jobs, int num_jobs, int to
 size_t fused_max_smem();
 int fused_grid_size(int variant, size_t smem_bytes);
 int fused_items(const FusedJob &j);
+
+// Tensor-core u16 variant (exact, depth <= 12): same job table and streaming
+// structure; tap tables are mma fragments (h_taps/v_dense) and column-group
+// bases (h_left). Variants are numbered from 100.
+bool plan_mma(const FilterTable &first, const FilterTable &second, bool h_first, unsigned depth, unsigned src_w,
+              unsigned src_h, unsigned dst_w, unsigned dst_h, FusedPlan *out);
+SmemLayout mma_layout(const FusedPlan *const *plans, int n);
+cudaError_t launch_mma(int variant, const FusedJob *jobs, int num_jobs, int total_items, const SmemLayout &L, int grid,
+                       const FusedJob &single, cudaStream_t stream);
+const void *mma_kernel_ptr(int variant);
 // Work items that fill the current device once (SMs x resident CTAs).
 int fused_wave_items();
 

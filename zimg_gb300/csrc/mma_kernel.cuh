@@ -1,0 +1,441 @@
+// Tensor-core variant of the fused streaming kernel for u16 samples (exact).
+//
+// Same streaming structure as fused_kernel.cuh (strips of 128 output columns,
+// source lines through rings in shared memory), but both passes run as small
+// banded matrix products on the tensor cores with mma.sync m16n8k16
+// (fp16 operands, fp32 accumulation):
+//
+//   * samples are re-centred, v' = v - 2^(depth-1), which is exact in fp16 for
+//     depth <= 12;
+//   * each int16 tap is split c = hi + lo, hi = c - (c & 31) (a multiple of 32
+//     with at most 11 significant bits), lo = c & 31, both exact in fp16;
+//   * both halves multiply the same samples into one fp32 accumulator that
+//     starts at 8192. The planner proved per output that
+//     8192 + sum(|hi| + |lo|) * 2^(depth-1) < 2^24, so every product and every
+//     partial sum is an integer representable in fp32: the accumulator holds
+//     8192 + sum(c * v') exactly, and the rounding below reproduces zimg's
+//     ((sum + 8192) >> 14) + 32768 with clamping (resize_impl.cpp:31-42).
+//
+// Fragment layouts follow the PTX ISA description of mma.m16n8k16 (.f16):
+// groupID = lane >> 2, tig = lane & 3.
+#pragma once
+
+#include <cuda_fp16.h>
+
+#include "fused.h"
+
+namespace zg {
+namespace mma_detail {
+
+constexpr int kThreads = kStreamThreads;  // 4 warps
+constexpr int kWarps = kThreads / 32;
+constexpr int kMidPitch = kStripW + 8;    // halfs per intermediate line (272 bytes)
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem, int src_bytes)
+{
+	const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+	asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(src_bytes) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit()
+{
+	asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+
+template <int N>
+__device__ __forceinline__ void cp_async_wait()
+{
+	asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+__device__ __forceinline__ void ldsm_x4(uint32_t &r0, uint32_t &r1, uint32_t &r2, uint32_t &r3, const void *p)
+{
+	const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(p));
+	asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0, %1, %2, %3}, [%4];\n"
+	             : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3) : "r"(s));
+}
+
+__device__ __forceinline__ void ldsm_x4_trans(uint32_t &r0, uint32_t &r1, uint32_t &r2, uint32_t &r3, const void *p)
+{
+	const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(p));
+	asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0, %1, %2, %3}, [%4];\n"
+	             : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3) : "r"(s));
+}
+
+// D += A * B, m16n8k16, f16 x f16 -> f32
+__device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1)
+{
+	asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+	             "{%0, %1, %2, %3};\n"
+	             : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+	             : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// acc (exact 8192 + sum c*v') -> two packed, clamped zimg samples (low/high half).
+__device__ __forceinline__ uint32_t pack_u16x2(float acc0, float acc1, float magic, uint32_t pmax2)
+{
+	const float y0 = __fmaf_rd(acc0, 6.103515625e-05f, magic);
+	const float y1 = __fmaf_rd(acc1, 6.103515625e-05f, magic);
+	// low 16 bits of y are the signed sample before clamping
+	uint32_t q = __byte_perm(__float_as_uint(y0), __float_as_uint(y1), 0x5410);
+	q = __vmaxs2(q, 0u);
+	q = __vmins2(q, pmax2);
+	return q;
+}
+
+// Two clamped samples (packed u16, each < 1024 when fast) -> centred fp16x2.
+__device__ __forceinline__ uint32_t u16x2_to_centred_h2(uint32_t q, uint32_t bias_h2, bool fast)
+{
+	if (fast) {
+		// fp16 with exponent 2^10 and mantissa q is exactly 1024 + q (q < 1024)
+		const uint32_t v = q | 0x64006400u;
+		const __half2 h = __hsub2(*reinterpret_cast<const __half2 *>(&v), *reinterpret_cast<const __half2 *>(&bias_h2));
+		return *reinterpret_cast<const uint32_t *>(&h);
+	}
+	const float f0 = static_cast<float>(q & 0xFFFFu) - __half2float(__low2half(*reinterpret_cast<const __half2 *>(&bias_h2)));
+	const float f1 = static_cast<float>(q >> 16) - __half2float(__low2half(*reinterpret_cast<const __half2 *>(&bias_h2)));
+	const __half2 h = __floats2half2_rn(f0, f1);
+	return *reinterpret_cast<const uint32_t *>(&h);
+}
+
+struct Item {
+	const char *src;
+	ptrdiff_t src_stride;
+	char *dst;
+	ptrdiff_t dst_stride;
+	const uint4 *vfrag;
+	const uint2 *hfrag;
+	int src_w, src_h, dst_h, vec_ok;
+	int c0, cols_valid, xlo, pxa, strip;
+	int g_begin, g_end, step_groups;
+	float magic;
+	uint32_t pmax2, bias_h2;
+	bool fast;
+};
+
+__device__ __forceinline__ int find_job(const FusedJob *__restrict__ jobs, int num_jobs, int t)
+{
+	int lo = 0, hi = num_jobs - 1;
+	while (lo < hi) {
+		const int mid = (lo + hi + 1) >> 1;
+		if (__ldg(&jobs[mid].item_begin) <= t)
+			lo = mid;
+		else
+			hi = mid - 1;
+	}
+	return lo;
+}
+
+__device__ __forceinline__ Item make_item(const FusedJob &J, int t)
+{
+	Item it;
+	const int local = t - J.item_begin;
+	const int seg = local / J.strips;
+	it.strip = local - seg * J.strips;
+	it.src = static_cast<const char *>(J.src);
+	it.src_stride = J.src_stride;
+	it.dst = static_cast<char *>(J.dst);
+	it.dst_stride = J.dst_stride;
+	it.vfrag = reinterpret_cast<const uint4 *>(J.v_dense);
+	it.hfrag = reinterpret_cast<const uint2 *>(J.h_taps);
+	it.src_w = J.src_w;
+	it.src_h = J.src_h;
+	it.dst_h = J.dst_h;
+	it.vec_ok = J.vec_ok;
+	it.c0 = it.strip * kStripW;
+	it.cols_valid = min(kStripW, J.dst_w - it.c0);
+	it.xlo = __ldg(J.win_col + 2 * it.strip);
+	it.pxa = (__ldg(J.win_col + 2 * it.strip + 1) - it.xlo + 7) & ~7;
+	it.g_begin = seg * J.seg_groups;
+	it.g_end = min(J.groups, it.g_begin + J.seg_groups);
+	it.step_groups = J.step_groups;
+	it.magic = J.magic;
+	const uint32_t pm = static_cast<uint32_t>(J.pixel_max);
+	it.pmax2 = pm | (pm << 16);
+	const __half2 b = __floats2half2_rn(1024.0f + J.offset, 1024.0f + J.offset);
+	it.fast = J.pixel_max < 1024.0f;
+	const __half2 bo = __floats2half2_rn(J.offset, J.offset);
+	it.bias_h2 = it.fast ? *reinterpret_cast<const uint32_t *>(&b) : *reinterpret_cast<const uint32_t *>(&bo);
+	return it;
+}
+
+// Source lines [a, b) of the strip (raw u16) into staging slots (line & mask).
+__device__ __forceinline__ void load_lines(const Item &it, int a, int b, char *stage, int mask, int pitch)
+{
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	const int chunks = it.pxa / 8;
+	for (int y = a + warp; y < b; y += kWarps) {
+		const bool row_ok = y < it.src_h;
+		const char *row = it.src + static_cast<ptrdiff_t>(row_ok ? y : 0) * it.src_stride;
+		char *srow = stage + (y & mask) * pitch * 2;
+		if (it.vec_ok) {
+			for (int q = lane; q < chunks; q += 32) {
+				const int gx = it.xlo + q * 8;
+				const int n = row_ok ? max(0, min(8, it.src_w - gx)) : 0;
+				cp_async16(srow + q * 16, n ? row + static_cast<ptrdiff_t>(gx) * 2 : it.src, n * 2);
+			}
+		} else {
+			for (int x = lane; x < it.pxa; x += 32) {
+				const int gx = it.xlo + x;
+				const bool ok = row_ok && gx < it.src_w;
+				reinterpret_cast<uint16_t *>(srow)[x] =
+					ok ? __ldg(reinterpret_cast<const uint16_t *>(row) + gx) : static_cast<uint16_t>(0);
+			}
+		}
+	}
+}
+
+// Raw staged lines this thread loaded -> centred fp16 lines.
+__device__ __forceinline__ void convert_lines(const Item &it, int a, int b, const char *stage, int smask, char *ring,
+                                              int rmask, int pitch)
+{
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	const int chunks = it.pxa / 8;
+	for (int y = a + warp; y < b; y += kWarps) {
+		const uint4 *s = reinterpret_cast<const uint4 *>(stage + (y & smask) * pitch * 2);
+		uint4 *d = reinterpret_cast<uint4 *>(ring + (y & rmask) * pitch * 2);
+		for (int q = lane; q < chunks; q += 32) {
+			uint4 u = s[q];
+			u.x = u16x2_to_centred_h2(u.x, it.bias_h2, it.fast);
+			u.y = u16x2_to_centred_h2(u.y, it.bias_h2, it.fast);
+			u.z = u16x2_to_centred_h2(u.z, it.bias_h2, it.fast);
+			u.w = u16x2_to_centred_h2(u.w, it.bias_h2, it.fast);
+			d[q] = u;
+		}
+	}
+}
+
+// Horizontal pass on 16-line blocks: for each column group cg (8 outputs),
+// D[16 lines][8] = sum over KH*16 columns starting at hbase[cg] - xlo.
+// A: lines from `in` (ldmatrix, row addresses per line), B: tap fragments.
+// FINAL: lines are destination rows r0 + (y - a); else store centred fp16 into
+// intermediate ring slots (y & omask), columns cg*8...
+template <int KH, bool FINAL>
+__device__ __forceinline__ void h_pass(const Item &it, const int *hbase, const char *in, int imask, int in_pitch,
+                                       int a, int b, char *out, int omask, int r0)
+{
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	const int gid = lane >> 2, tig = lane & 3;
+	const int ncg = (it.cols_valid + 7) / 8;
+	for (int cg = warp; cg < ncg; cg += kWarps) {
+		const int gcg = it.c0 / 8 + cg;
+		uint2 bf[KH][2];
+#pragma unroll
+		for (int ks = 0; ks < KH; ++ks)
+#pragma unroll
+			for (int h = 0; h < 2; ++h)
+				bf[ks][h] = __ldg(it.hfrag + ((static_cast<size_t>(gcg) * KH + ks) * 2 + h) * 32 + lane);
+		const int col0 = hbase[cg] - it.xlo;
+		for (int y0 = a; y0 < b; y0 += 16) {
+			// row address for this lane: line y0 + (lane & 15), column block (lane >> 4) * 8
+			const int ly = y0 + (lane & 15);
+			const char *rowp = in + (ly & imask) * in_pitch * 2 + (col0 + (lane >> 4) * 8) * 2;
+			float d[4] = { 8192.0f, 8192.0f, 8192.0f, 8192.0f };
+#pragma unroll
+			for (int ks = 0; ks < KH; ++ks) {
+				uint32_t af[4];
+				ldsm_x4(af[0], af[1], af[2], af[3], rowp + ks * 32);
+				// ldmatrix gives matrices (rows 0-7, cols 0-7), (rows 8-15, cols 0-7),
+				// (rows 0-7, cols 8-15), (rows 8-15, cols 8-15): a0..a3 order
+				mma16816(d, af, bf[ks][0].x, bf[ks][0].y);
+				mma16816(d, af, bf[ks][1].x, bf[ks][1].y);
+			}
+			const uint32_t q01 = pack_u16x2(d[0], d[1], it.magic, it.pmax2);  // line y0+gid, cols 2tig..
+			const uint32_t q23 = pack_u16x2(d[2], d[3], it.magic, it.pmax2);  // line y0+gid+8
+			const int ya = y0 + gid, yb = y0 + gid + 8;
+			const int col = cg * 8 + 2 * tig;
+			if (!FINAL) {
+				*reinterpret_cast<uint32_t *>(out + (ya & omask) * kMidPitch * 2 + col * 2) =
+					u16x2_to_centred_h2(q01, it.bias_h2, it.fast);
+				*reinterpret_cast<uint32_t *>(out + (yb & omask) * kMidPitch * 2 + col * 2) =
+					u16x2_to_centred_h2(q23, it.bias_h2, it.fast);
+			} else {
+				const int ra = r0 + (ya - a), rb = r0 + (yb - a);
+				if (col < it.cols_valid) {
+					uint16_t *pa = reinterpret_cast<uint16_t *>(it.dst + static_cast<ptrdiff_t>(ra) * it.dst_stride) + it.c0 + col;
+					uint16_t *pb = reinterpret_cast<uint16_t *>(it.dst + static_cast<ptrdiff_t>(rb) * it.dst_stride) + it.c0 + col;
+					const bool pair = col + 1 < it.cols_valid;
+					if (ya < b && ra < it.dst_h) {
+						if (pair && it.vec_ok)
+							*reinterpret_cast<uint32_t *>(pa) = q01;
+						else {
+							pa[0] = static_cast<uint16_t>(q01);
+							if (pair)
+								pa[1] = static_cast<uint16_t>(q01 >> 16);
+						}
+					}
+					if (yb < b && rb < it.dst_h) {
+						if (pair && it.vec_ok)
+							*reinterpret_cast<uint32_t *>(pb) = q23;
+						else {
+							pb[0] = static_cast<uint16_t>(q23);
+							if (pair)
+								pb[1] = static_cast<uint16_t>(q23 >> 16);
+						}
+					}
+				}
+			}
+		}
+	}
+}
+
+// Vertical pass for one 16-row group g: D[16 rows][8 cols] = sum over KV*16
+// lines from vbase[g] of taps * in[line][col]. A: tap fragments, B: lines
+// (ldmatrix.trans, row addresses per line). Columns [0, ncols) in steps of 16
+// per warp iteration. FINAL: destination rows g*16 + r; else I lines.
+template <int KV, bool FINAL>
+__device__ __forceinline__ void v_pass(const Item &it, int g, int vbase, const char *in, int imask, int in_pitch,
+                                       int ncols, int wfirst, int wcount, char *I, int i_pitch)
+{
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	const int gid = lane >> 2, tig = lane & 3;
+	uint4 af[KV][2];
+#pragma unroll
+	for (int ks = 0; ks < KV; ++ks)
+#pragma unroll
+		for (int h = 0; h < 2; ++h)
+			af[ks][h] = __ldg(it.vfrag + ((static_cast<size_t>(g) * KV + ks) * 2 + h) * 32 + lane);
+	const int wi = warp - wfirst;
+	if (wi < 0 || wi >= wcount)
+		return;
+	// lane's ldmatrix row: line vbase + ks*16 + (lane & 7) + ((lane >> 3) & 1) * 8, column +(lane >> 4) * 8
+	const int krow = (lane & 7) + ((lane >> 3) & 1) * 8;
+	const int coff = (lane >> 4) * 8;
+	for (int x0 = wi * 16; x0 < ncols; x0 += wcount * 16) {
+		float d0[4] = { 8192.0f, 8192.0f, 8192.0f, 8192.0f };
+		float d1[4] = { 8192.0f, 8192.0f, 8192.0f, 8192.0f };
+#pragma unroll
+		for (int ks = 0; ks < KV; ++ks) {
+			const int line = vbase + ks * 16 + krow;
+			const char *p = in + (line & imask) * in_pitch * 2 + (x0 + coff) * 2;
+			uint32_t b0, b1, b2, b3;
+			ldsm_x4_trans(b0, b1, b2, b3, p);
+			const uint32_t ahi[4] = { af[ks][0].x, af[ks][0].y, af[ks][0].z, af[ks][0].w };
+			const uint32_t alo[4] = { af[ks][1].x, af[ks][1].y, af[ks][1].z, af[ks][1].w };
+			mma16816(d0, ahi, b0, b1);
+			mma16816(d0, alo, b0, b1);
+			mma16816(d1, ahi, b2, b3);
+			mma16816(d1, alo, b2, b3);
+		}
+#pragma unroll
+		for (int nb = 0; nb < 2; ++nb) {
+			const float *d = nb ? d1 : d0;
+			const uint32_t q01 = pack_u16x2(d[0], d[1], it.magic, it.pmax2);  // row gid
+			const uint32_t q23 = pack_u16x2(d[2], d[3], it.magic, it.pmax2);  // row gid + 8
+			const int col = x0 + nb * 8 + 2 * tig;
+			if (!FINAL) {
+				*reinterpret_cast<uint32_t *>(I + gid * i_pitch * 2 + col * 2) = u16x2_to_centred_h2(q01, it.bias_h2, it.fast);
+				*reinterpret_cast<uint32_t *>(I + (gid + 8) * i_pitch * 2 + col * 2) =
+					u16x2_to_centred_h2(q23, it.bias_h2, it.fast);
+			} else if (col < it.cols_valid) {
+				const int ra = g * 16 + gid, rb = ra + 8;
+				const bool pair = col + 1 < it.cols_valid;
+				uint16_t *pa = reinterpret_cast<uint16_t *>(it.dst + static_cast<ptrdiff_t>(ra) * it.dst_stride) + it.c0 + col;
+				uint16_t *pb = reinterpret_cast<uint16_t *>(it.dst + static_cast<ptrdiff_t>(rb) * it.dst_stride) + it.c0 + col;
+				if (ra < it.dst_h) {
+					if (pair && it.vec_ok)
+						*reinterpret_cast<uint32_t *>(pa) = q01;
+					else {
+						pa[0] = static_cast<uint16_t>(q01);
+						if (pair)
+							pa[1] = static_cast<uint16_t>(q01 >> 16);
+					}
+				}
+				if (rb < it.dst_h) {
+					if (pair && it.vec_ok)
+						*reinterpret_cast<uint32_t *>(pb) = q23;
+					else {
+						pb[0] = static_cast<uint16_t>(q23);
+						if (pair)
+							pb[1] = static_cast<uint16_t>(q23 >> 16);
+					}
+				}
+			}
+		}
+	}
+}
+
+// Kernel. Shared memory (MmaLayout): stage (raw u16 lines), src ring (fp16
+// source lines), mid ring (fp16 intermediate lines, H-first) or I (16 fp16
+// intermediate lines, V-first), per-item group bases and strip column bases.
+template <bool H_FIRST, int KV, int KH>
+__global__ void __launch_bounds__(kThreads, 4)
+mma_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, const __grid_constant__ FusedJob single,
+           const __grid_constant__ SmemLayout L)
+{
+	extern __shared__ float4 smem4[];
+	char *smem = reinterpret_cast<char *>(smem4);
+	char *stage = smem + L.stage_off;
+	char *src_ring = smem + L.in_off;     // fp16 source lines
+	char *mid = smem + L.ring_off;        // H-first: fp16 intermediate lines
+	char *I = smem + L.i_off;             // V-first: 16 fp16 intermediate lines
+	int *vb = reinterpret_cast<int *>(smem + L.vbase_off);
+	int *hb = reinterpret_cast<int *>(smem + L.hleft_off);
+	const int smask = L.stage_rows - 1;
+	const int imask = L.in_rows - 1;
+	const int rmask = L.ring_rows - 1;
+
+	// Lines a pass reads past the last loaded one hold finite values.
+	for (int i = threadIdx.x; i < L.htaps_off / 16; i += kThreads)
+		smem4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+	__syncthreads();
+
+	for (int t = blockIdx.x; t < total_items; t += gridDim.x) {
+		const FusedJob *Jp = jobs ? &jobs[find_job(jobs, num_jobs, t)] : &single;
+		const Item it = make_item(*Jp, t);
+		for (int g = it.g_begin + threadIdx.x; g < it.g_end; g += kThreads)
+			vb[g - it.g_begin] = __ldg(Jp->v_base + g);
+		for (int i = threadIdx.x; i < kStripW / 8; i += kThreads)
+			hb[i] = __ldg(Jp->h_left + min(it.c0 / 8 + i, (Jp->dst_w + 7) / 8 - 1));
+		__syncthreads();
+
+		const int nsteps = (it.g_end - it.g_begin + it.step_groups - 1) / it.step_groups;
+		auto hi_of = [&](int k) {
+			const int g1 = min(it.g_end, it.g_begin + (k + 1) * it.step_groups);
+			return vb[g1 - 1 - it.g_begin] + KV * 16;
+		};
+		int lo_cur = vb[0];
+		int hi_cur = hi_of(0);
+		load_lines(it, lo_cur, hi_cur, stage, smask, L.pitch);
+		cp_async_commit();
+		__syncthreads();
+
+		for (int k = 0; k < nsteps; ++k) {
+			const int g0 = it.g_begin + k * it.step_groups;
+			const int g1 = min(it.g_end, g0 + it.step_groups);
+			int hi_next = hi_cur;
+			if (k + 1 < nsteps) {
+				hi_next = hi_of(k + 1);
+				load_lines(it, hi_cur, hi_next, stage, smask, L.pitch);
+			}
+			cp_async_commit();
+			cp_async_wait<1>();
+			convert_lines(it, lo_cur, hi_cur, stage, smask, src_ring, imask, L.pitch);
+			__syncthreads();
+			if (H_FIRST) {
+				h_pass<KH, false>(it, hb, src_ring, imask, L.pitch, lo_cur, hi_cur, mid, rmask, 0);
+				__syncthreads();
+				const int ng = g1 - g0;
+				const int wpg = ng >= kWarps ? 1 : kWarps / ng;
+				for (int gi = 0; gi < ng; ++gi) {
+					const int first = (gi * wpg) % kWarps;
+					v_pass<KV, true>(it, g0 + gi, vb[g0 + gi - it.g_begin], mid, rmask, kMidPitch,
+					                 (it.cols_valid + 15) & ~15, ng >= kWarps ? (gi % kWarps) : first,
+					                 ng >= kWarps ? 1 : wpg, nullptr, 0);
+				}
+			} else {
+				// one 16-row group per step: ring -> I (16 lines x pxa) -> destination
+				v_pass<KV, false>(it, g0, vb[g0 - it.g_begin], src_ring, imask, L.pitch, it.pxa, 0, kWarps, I, L.pitch);
+				__syncthreads();
+				h_pass<KH, true>(it, hb, I, 0x7fffffff, L.pitch, 0, 16, nullptr, 0, g0 * 16);
+			}
+			lo_cur = hi_cur;
+			hi_cur = hi_next;
+		}
+		cp_async_wait<0>();
+		__syncthreads();
+	}
+}
+
+} // namespace mma_detail
+} // namespace zg

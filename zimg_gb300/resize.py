@@ -170,7 +170,8 @@ class Resize:
     def info(self) -> dict:
         n, f, fu = C.c_int(), C.c_int(), C.c_int()
         check(load().zg_resize_get_info(self._h, C.byref(n), C.byref(f), C.byref(fu)))
-        return {"num_passes": n.value, "first_horizontal": bool(f.value), "fused": bool(fu.value)}
+        return {"num_passes": n.value, "first_horizontal": bool(f.value), "fused": bool(fu.value),
+                "engine": {0: "passes", 1: "cuda", 2: "tensor"}[fu.value]}
 
     def alloc_tmp(self, device=None):
         import torch
