@@ -128,7 +128,9 @@ def test_tensor_core_u16_bitexact(cuda, oracle, depth, shape):
     src = make_u16(rng, sh, sw, depth)
     for kind, a in (("spline36", math.nan), ("lanczos", 3.0), ("bicubic", math.nan)):
         got, r = run_conversion(src, dw, dh, kind, a, depth=depth, engine="tensor")
-        assert r.info["engine"] == "tensor", (shape, kind)
+        # depth 12: 8192 + sum|tap| * 2^11 reaches 2^24, so exactness cannot be
+        # certified and the planner keeps the separate integer passes
+        assert r.info["engine"] == ("tensor" if depth <= 10 else "passes"), (shape, kind)
         want = oracle.resize_plane(src, dw, dh, kind, a, depth=depth, mode="c", nthreads=16)
         np.testing.assert_array_equal(got, want, err_msg=str((shape, kind, depth)))
 

@@ -210,6 +210,7 @@ bool plan_fused(const FilterTable &first, const FilterTable &second, bool h_firs
 	J.dst_w = static_cast<int>(dst_w);
 	J.dst_h = static_cast<int>(dst_h);
 	J.strips = strips;
+	J.strip_w = kStripW;
 	const float offset = u16 ? static_cast<float>(std::ldexp(1.0, static_cast<int>(depth) - 1)) : 0.0f;
 	J.offset = offset;
 	J.magic = 12582912.0f + offset;

@@ -44,7 +44,8 @@ struct FusedJob {
 	int src_w, src_h, dst_w, dst_h;
 
 	// work items: strips x row segments
-	int strips;             // ceil(dst_w / kStripW)
+	int strips;             // ceil(dst_w / strip_w)
+	int strip_w;            // output columns per strip (kStripW for the CUDA-core kernel)
 	int segments;           // row segments per strip
 	int seg_groups;         // vertical groups per segment (last may be shorter)
 	int groups;             // vertical groups of the plane (ceil(dst_h / kGroup))
@@ -53,6 +54,7 @@ struct FusedJob {
 
 	// rings (lines), powers of two
 	int ring_rows;          // V-first: source lines; H-first: intermediate lines
+	int depth;              // steps of source lines in flight (tensor-core kernel)
 	int in_rows;            // H-first: source lines staged for the H pass
 
 	// H pass: taps padded to hw per output column, left[] per output column
@@ -85,6 +87,7 @@ struct SmemLayout {
 	int vbase_off;          // one segment's group bases
 	int total_bytes;
 	int ring_rows, in_rows, stage_rows, seg_groups, step_groups;
+	int depth;              // steps of lines in flight ahead of the computing step
 };
 
 // Host-side plan of one fused job: device tables plus a FusedJob template.
@@ -93,6 +96,7 @@ struct FusedPlan {
 	int variant = 0;         // kernel instantiation index
 	int max_pxa = 0;         // widest strip patch (elements)
 	int stage_rows = 1;      // u16 raw staging lines
+	int depth = 1;           // prefetch depth in steps
 	bool mma = false;        // tensor-core variant (mma_kernel.cuh)
 	std::vector<unsigned char> blob;  // host copy of the tables, uploaded by the owner
 	size_t off_h_taps = 0, off_h_left = 0, off_v_dense = 0, off_v_base = 0, off_win_col = 0;

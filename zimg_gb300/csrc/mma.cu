@@ -134,11 +134,16 @@ bool plan_mma(const FilterTable &first, const FilterTable &second, bool h_first,
 	if (KH < 1 || KH > 3)
 		return false;
 
-	const int strips = static_cast<int>((dst_w + kStripW - 1) / kStripW);
-	std::vector<int> win_col(2 * strips);
+	// strips: 128 output columns, or 64 when a 128-column strip's rings do not fit
+	FusedPlan &p = *out;
+	std::vector<int> win_col;
+	bool fits = false;
+	for (int sw = kStripW; sw >= 64 && !fits; sw /= 2) {
+	const int strips = static_cast<int>((dst_w + sw - 1) / sw);
+	win_col.assign(2 * strips, 0);
 	int max_pxa = 0;
 	for (int s = 0; s < strips; ++s) {
-		const int cg0 = s * (kStripW / 8), cg1 = std::min(cgroups, (s + 1) * (kStripW / 8));
+		const int cg0 = s * (sw / 8), cg1 = std::min(cgroups, (s + 1) * (sw / 8));
 		int lo = INT_MAX, hi = INT_MIN;
 		for (int cg = cg0; cg < cg1; ++cg) {
 			lo = std::min(lo, hbase[cg]);
@@ -148,45 +153,65 @@ bool plan_mma(const FilterTable &first, const FilterTable &second, bool h_first,
 		win_col[2 * s + 1] = hi;
 		max_pxa = std::max(max_pxa, (hi - lo + 7) & ~7);
 	}
+	if (h_first && sw != kStripW)
+		break;  // intermediate lines are kStripW wide
 
-	// steps and rings
-	FusedPlan &p = *out;
+	// steps, prefetch depth and rings (exact sizes; lines index rings modulo)
 	p = FusedPlan{};
 	const int step_groups = h_first ? 2 : 1;
 	const int nsteps = (groups + step_groups - 1) / step_groups;
 	auto hi_of = [&](int k) { return gbase[std::min(groups, (k + 1) * step_groups) - 1] + 16 * KV; };
-	int mid_need = 1, src_need = 1, stage_need = 1;
-	for (int k = 0; k < nsteps; ++k) {
-		const int win_lo = gbase[k * step_groups];
-		const int hi = hi_of(k);
-		const int hi_next = k + 1 < nsteps ? hi_of(k + 1) : hi;
-		// 16-line blocks may run up to 15 lines past the step's end
-		mid_need = std::max(mid_need, hi - win_lo + 16);
-		src_need = std::max(src_need, hi - win_lo + (h_first ? 16 : 0));
-		stage_need = std::max(stage_need, hi_next - win_lo);
-	}
+	// enough source bytes in flight per CTA to cover memory latency
+	int new_lines = 1;
+	for (int k = 1; k < nsteps; ++k)
+		new_lines = std::max(new_lines, hi_of(k) - hi_of(k - 1));
+	const int step_bytes = std::max(1, new_lines * max_pxa * 2);
+	int ahead = std::max(1, std::min(4, (12 * 1024 + step_bytes - 1) / step_bytes));
 	FusedJob &J = p.job;
-	J.h_first = h_first ? 1 : 0;
-	J.kind = static_cast<int>(FusedKind::U16_EXACT);
-	J.src_w = static_cast<int>(src_w);
-	J.src_h = static_cast<int>(src_h);
-	J.dst_w = static_cast<int>(dst_w);
-	J.dst_h = static_cast<int>(dst_h);
-	J.strips = strips;
-	J.groups = groups;
-	J.seg_groups = groups;
-	J.segments = 1;
-	J.step_groups = step_groups;
-	J.ring_rows = h_first ? pow2(mid_need) : 1;
-	J.in_rows = pow2(src_need);
-	J.hw = KH;
-	J.vs = KV;
-	p.stage_rows = pow2(stage_need);
-	p.max_pxa = max_pxa;
-	p.mma = true;
-	const FusedPlan *pp = &p;
-	if (static_cast<size_t>(mma_layout(&pp, 1).total_bytes) > kMmaSmemMax)
+	for (;; --ahead) {
+		int mid_need = 1, src_need = 1, stage_need = 1;
+		for (int k = 0; k < nsteps; ++k) {
+			const int win_lo = gbase[k * step_groups];
+			const int hi = hi_of(k);
+			const int hi_ahead = hi_of(std::min(nsteps - 1, k + ahead));
+			// 16-line blocks may run up to 15 lines past the step's end
+			mid_need = std::max(mid_need, hi - win_lo + 16);
+			src_need = std::max(src_need, hi - win_lo + (h_first ? 16 : 0));
+			stage_need = std::max(stage_need, hi_ahead - win_lo);
+		}
+		J.h_first = h_first ? 1 : 0;
+		J.kind = static_cast<int>(FusedKind::U16_EXACT);
+		J.src_w = static_cast<int>(src_w);
+		J.src_h = static_cast<int>(src_h);
+		J.dst_w = static_cast<int>(dst_w);
+		J.dst_h = static_cast<int>(dst_h);
+		J.strips = strips;
+		J.strip_w = sw;
+		J.groups = groups;
+		J.seg_groups = groups;
+		J.segments = 1;
+		J.step_groups = step_groups;
+		J.ring_rows = h_first ? mid_need : 1;
+		J.in_rows = src_need;
+		J.hw = KH;
+		J.vs = KV;
+		p.stage_rows = stage_need;
+		p.max_pxa = max_pxa;
+		p.depth = ahead;
+		J.depth = ahead;
+		p.mma = true;
+		const FusedPlan *pp = &p;
+		if (static_cast<size_t>(mma_layout(&pp, 1).total_bytes) <= kMmaSmemMax) {
+			fits = true;
+			break;
+		}
+		if (ahead == 1)
+			break;
+	}
+	}
+	if (!fits)
 		return false;
+	FusedJob &J = p.job;
 
 	// tables: hfrag | hbase | vfrag | v_base | win_col
 	size_t off = 0;
@@ -272,15 +297,19 @@ bool plan_mma(const FilterTable &first, const FilterTable &second, bool h_first,
 
 SmemLayout mma_layout(const FusedPlan *const *plans, int n)
 {
-	int max_pxa = 0, ring = 1, in = 1, stage = 1, seg_groups = 1;
+	int max_pxa = 0, ring = 1, in = 1, stage = 1, seg_groups = 1, depth = 1, kv = 1, kh = 1, max_sw = 8;
 	bool h_first = false;
 	for (int i = 0; i < n; ++i) {
 		const FusedPlan &p = *plans[i];
+		max_sw = std::max(max_sw, p.job.strip_w);
 		max_pxa = std::max(max_pxa, p.max_pxa);
 		ring = std::max(ring, p.job.ring_rows);
 		in = std::max(in, p.job.in_rows);
 		stage = std::max(stage, p.stage_rows);
 		seg_groups = std::max(seg_groups, p.job.seg_groups);
+		depth = std::max(depth, p.depth);
+		kv = std::max(kv, p.job.vs);
+		kh = std::max(kh, p.job.hw);
 		h_first = p.job.h_first != 0;
 	}
 	auto a16 = [](size_t x) { return static_cast<int>((x + 15) / 16 * 16); };
@@ -291,6 +320,7 @@ SmemLayout mma_layout(const FusedPlan *const *plans, int n)
 	L.stage_rows = stage;
 	L.seg_groups = seg_groups;
 	L.step_groups = h_first ? 2 : 1;
+	L.depth = depth;
 	int off = 0;
 	L.ring_off = off;
 	off += h_first ? a16(static_cast<size_t>(ring) * mma_detail::kMidPitch * 2) : 0;
@@ -300,10 +330,12 @@ SmemLayout mma_layout(const FusedPlan *const *plans, int n)
 	off += a16(static_cast<size_t>(in) * L.pitch * 2);
 	L.i_off = off;
 	off += h_first ? 0 : a16(static_cast<size_t>(16) * L.pitch * 2);
-	L.htaps_off = off;
-	L.hleft_off = off;          // strip column-group bases
-	off += a16(kStripW / 8 * 4);
-	L.vcoef_off = off;
+	L.htaps_off = off;                       // the strip's horizontal tap fragments
+	off += a16(static_cast<size_t>(max_sw / 8) * kh * 2 * 32 * 8);
+	L.vcoef_off = off;                       // depth + 1 slots of vertical tap fragments
+	off += a16(static_cast<size_t>(depth + 1) * L.step_groups * kv * 2 * 32 * 16);
+	L.hleft_off = off;                       // strip column-group bases
+	off += a16(static_cast<size_t>(max_sw / 8) * 4);
 	L.vbase_off = off;
 	off += a16(static_cast<size_t>(seg_groups) * 4);
 	L.total_bytes = off;

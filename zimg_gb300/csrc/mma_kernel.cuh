@@ -106,8 +106,8 @@ struct Item {
 	const uint4 *vfrag;
 	const uint2 *hfrag;
 	int src_w, src_h, dst_h, vec_ok;
-	int c0, cols_valid, xlo, pxa, strip;
-	int g_begin, g_end, step_groups;
+	int c0, cols_valid, xlo, pxa, strip, sw;
+	int g_begin, g_end, step_groups, depth;
 	float magic;
 	uint32_t pmax2, bias_h2;
 	bool fast;
@@ -142,13 +142,15 @@ __device__ __forceinline__ Item make_item(const FusedJob &J, int t)
 	it.src_h = J.src_h;
 	it.dst_h = J.dst_h;
 	it.vec_ok = J.vec_ok;
-	it.c0 = it.strip * kStripW;
-	it.cols_valid = min(kStripW, J.dst_w - it.c0);
+	it.sw = J.strip_w;
+	it.c0 = it.strip * it.sw;
+	it.cols_valid = min(it.sw, J.dst_w - it.c0);
 	it.xlo = __ldg(J.win_col + 2 * it.strip);
 	it.pxa = (__ldg(J.win_col + 2 * it.strip + 1) - it.xlo + 7) & ~7;
 	it.g_begin = seg * J.seg_groups;
 	it.g_end = min(J.groups, it.g_begin + J.seg_groups);
 	it.step_groups = J.step_groups;
+	it.depth = J.depth;
 	it.magic = J.magic;
 	const uint32_t pm = static_cast<uint32_t>(J.pixel_max);
 	it.pmax2 = pm | (pm << 16);
@@ -159,15 +161,15 @@ __device__ __forceinline__ Item make_item(const FusedJob &J, int t)
 	return it;
 }
 
-// Source lines [a, b) of the strip (raw u16) into staging slots (line & mask).
-__device__ __forceinline__ void load_lines(const Item &it, int a, int b, char *stage, int mask, int pitch)
+// Source lines [a, b) of the strip (raw u16) into staging slots (line % R).
+__device__ __forceinline__ void load_lines(const Item &it, int a, int b, char *stage, int R, int pitch)
 {
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	const int chunks = it.pxa / 8;
 	for (int y = a + warp; y < b; y += kWarps) {
 		const bool row_ok = y < it.src_h;
 		const char *row = it.src + static_cast<ptrdiff_t>(row_ok ? y : 0) * it.src_stride;
-		char *srow = stage + (y & mask) * pitch * 2;
+		char *srow = stage + (y % R) * pitch * 2;
 		if (it.vec_ok) {
 			for (int q = lane; q < chunks; q += 32) {
 				const int gx = it.xlo + q * 8;
@@ -186,14 +188,14 @@ __device__ __forceinline__ void load_lines(const Item &it, int a, int b, char *s
 }
 
 // Raw staged lines this thread loaded -> centred fp16 lines.
-__device__ __forceinline__ void convert_lines(const Item &it, int a, int b, const char *stage, int smask, char *ring,
-                                              int rmask, int pitch)
+__device__ __forceinline__ void convert_lines(const Item &it, int a, int b, const char *stage, int SR, char *ring,
+                                              int RR, int pitch)
 {
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	const int chunks = it.pxa / 8;
 	for (int y = a + warp; y < b; y += kWarps) {
-		const uint4 *s = reinterpret_cast<const uint4 *>(stage + (y & smask) * pitch * 2);
-		uint4 *d = reinterpret_cast<uint4 *>(ring + (y & rmask) * pitch * 2);
+		const uint4 *s = reinterpret_cast<const uint4 *>(stage + (y % SR) * pitch * 2);
+		uint4 *d = reinterpret_cast<uint4 *>(ring + (y % RR) * pitch * 2);
 		for (int q = lane; q < chunks; q += 32) {
 			uint4 u = s[q];
 			u.x = u16x2_to_centred_h2(u.x, it.bias_h2, it.fast);
@@ -205,38 +207,47 @@ __device__ __forceinline__ void convert_lines(const Item &it, int a, int b, cons
 	}
 }
 
+// Vertical tap fragments of groups [g0, g1) into a shared slot.
+template <int KV>
+__device__ __forceinline__ void load_vfrag(const Item &it, int g0, int g1, char *slot)
+{
+	const char *src = reinterpret_cast<const char *>(it.vfrag) + static_cast<size_t>(g0) * KV * 2 * 32 * 16;
+	const int n = (g1 - g0) * KV * 2 * 32;
+	for (int i = threadIdx.x; i < n; i += kThreads)
+		cp_async16(slot + i * 16, src + i * 16, 16);
+}
+
 // Horizontal pass on 16-line blocks: for each column group cg (8 outputs),
 // D[16 lines][8] = sum over KH*16 columns starting at hbase[cg] - xlo.
-// A: lines from `in` (ldmatrix, row addresses per line), B: tap fragments.
-// FINAL: lines are destination rows r0 + (y - a); else store centred fp16 into
-// intermediate ring slots (y & omask), columns cg*8...
+// A: lines from `in` (ldmatrix, row addresses per line), B: tap fragments
+// from shared memory. FINAL: lines are destination rows r0 + (y - a); else
+// store centred fp16 into intermediate ring slots (y % OR), columns cg*8...
 template <int KH, bool FINAL>
-__device__ __forceinline__ void h_pass(const Item &it, const int *hbase, const char *in, int imask, int in_pitch,
-                                       int a, int b, char *out, int omask, int r0)
+__device__ __forceinline__ void h_pass(const Item &it, const int *hbase, const uint2 *hfrag, const char *in, int IR,
+                                       int in_pitch, int a, int b, char *out, int OR, int r0)
 {
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	const int gid = lane >> 2, tig = lane & 3;
 	const int ncg = (it.cols_valid + 7) / 8;
 	for (int cg = warp; cg < ncg; cg += kWarps) {
-		const int gcg = it.c0 / 8 + cg;
 		uint2 bf[KH][2];
 #pragma unroll
 		for (int ks = 0; ks < KH; ++ks)
 #pragma unroll
 			for (int h = 0; h < 2; ++h)
-				bf[ks][h] = __ldg(it.hfrag + ((static_cast<size_t>(gcg) * KH + ks) * 2 + h) * 32 + lane);
+				bf[ks][h] = hfrag[((cg * KH + ks) * 2 + h) * 32 + lane];
 		const int col0 = hbase[cg] - it.xlo;
 		for (int y0 = a; y0 < b; y0 += 16) {
 			// row address for this lane: line y0 + (lane & 15), column block (lane >> 4) * 8
 			const int ly = y0 + (lane & 15);
-			const char *rowp = in + (ly & imask) * in_pitch * 2 + (col0 + (lane >> 4) * 8) * 2;
+			const char *rowp = in + (ly % IR) * in_pitch * 2 + (col0 + (lane >> 4) * 8) * 2;
 			float d[4] = { 8192.0f, 8192.0f, 8192.0f, 8192.0f };
 #pragma unroll
 			for (int ks = 0; ks < KH; ++ks) {
 				uint32_t af[4];
-				ldsm_x4(af[0], af[1], af[2], af[3], rowp + ks * 32);
 				// ldmatrix gives matrices (rows 0-7, cols 0-7), (rows 8-15, cols 0-7),
 				// (rows 0-7, cols 8-15), (rows 8-15, cols 8-15): a0..a3 order
+				ldsm_x4(af[0], af[1], af[2], af[3], rowp + ks * 32);
 				mma16816(d, af, bf[ks][0].x, bf[ks][0].y);
 				mma16816(d, af, bf[ks][1].x, bf[ks][1].y);
 			}
@@ -245,33 +256,31 @@ __device__ __forceinline__ void h_pass(const Item &it, const int *hbase, const c
 			const int ya = y0 + gid, yb = y0 + gid + 8;
 			const int col = cg * 8 + 2 * tig;
 			if (!FINAL) {
-				*reinterpret_cast<uint32_t *>(out + (ya & omask) * kMidPitch * 2 + col * 2) =
+				*reinterpret_cast<uint32_t *>(out + (ya % OR) * kMidPitch * 2 + col * 2) =
 					u16x2_to_centred_h2(q01, it.bias_h2, it.fast);
-				*reinterpret_cast<uint32_t *>(out + (yb & omask) * kMidPitch * 2 + col * 2) =
+				*reinterpret_cast<uint32_t *>(out + (yb % OR) * kMidPitch * 2 + col * 2) =
 					u16x2_to_centred_h2(q23, it.bias_h2, it.fast);
-			} else {
+			} else if (col < it.cols_valid) {
 				const int ra = r0 + (ya - a), rb = r0 + (yb - a);
-				if (col < it.cols_valid) {
-					uint16_t *pa = reinterpret_cast<uint16_t *>(it.dst + static_cast<ptrdiff_t>(ra) * it.dst_stride) + it.c0 + col;
-					uint16_t *pb = reinterpret_cast<uint16_t *>(it.dst + static_cast<ptrdiff_t>(rb) * it.dst_stride) + it.c0 + col;
-					const bool pair = col + 1 < it.cols_valid;
-					if (ya < b && ra < it.dst_h) {
-						if (pair && it.vec_ok)
-							*reinterpret_cast<uint32_t *>(pa) = q01;
-						else {
-							pa[0] = static_cast<uint16_t>(q01);
-							if (pair)
-								pa[1] = static_cast<uint16_t>(q01 >> 16);
-						}
+				uint16_t *pa = reinterpret_cast<uint16_t *>(it.dst + static_cast<ptrdiff_t>(ra) * it.dst_stride) + it.c0 + col;
+				uint16_t *pb = reinterpret_cast<uint16_t *>(it.dst + static_cast<ptrdiff_t>(rb) * it.dst_stride) + it.c0 + col;
+				const bool pair = col + 1 < it.cols_valid;
+				if (ya < b && ra < it.dst_h) {
+					if (pair && it.vec_ok)
+						*reinterpret_cast<uint32_t *>(pa) = q01;
+					else {
+						pa[0] = static_cast<uint16_t>(q01);
+						if (pair)
+							pa[1] = static_cast<uint16_t>(q01 >> 16);
 					}
-					if (yb < b && rb < it.dst_h) {
-						if (pair && it.vec_ok)
-							*reinterpret_cast<uint32_t *>(pb) = q23;
-						else {
-							pb[0] = static_cast<uint16_t>(q23);
-							if (pair)
-								pb[1] = static_cast<uint16_t>(q23 >> 16);
-						}
+				}
+				if (yb < b && rb < it.dst_h) {
+					if (pair && it.vec_ok)
+						*reinterpret_cast<uint32_t *>(pb) = q23;
+					else {
+						pb[0] = static_cast<uint16_t>(q23);
+						if (pair)
+							pb[1] = static_cast<uint16_t>(q23 >> 16);
 					}
 				}
 			}
@@ -280,36 +289,39 @@ __device__ __forceinline__ void h_pass(const Item &it, const int *hbase, const c
 }
 
 // Vertical pass for one 16-row group g: D[16 rows][8 cols] = sum over KV*16
-// lines from vbase[g] of taps * in[line][col]. A: tap fragments, B: lines
-// (ldmatrix.trans, row addresses per line). Columns [0, ncols) in steps of 16
-// per warp iteration. FINAL: destination rows g*16 + r; else I lines.
+// lines from vbase of taps * in[line][col]. A: tap fragments (shared slot),
+// B: lines (ldmatrix.trans, row addresses per line). Warps [wfirst,
+// wfirst + wcount) take columns [0, ncols) 16 at a time. FINAL: destination
+// rows g*16 + r; else I lines.
 template <int KV, bool FINAL>
-__device__ __forceinline__ void v_pass(const Item &it, int g, int vbase, const char *in, int imask, int in_pitch,
-                                       int ncols, int wfirst, int wcount, char *I, int i_pitch)
+__device__ __forceinline__ void v_pass(const Item &it, int g, int vbase, const uint4 *afrag, const char *in, int IR,
+                                       int in_pitch, int ncols, int wfirst, int wcount, char *I, int i_pitch)
 {
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	const int wi = warp - wfirst;
+	if (wi < 0 || wi >= wcount)
+		return;
 	const int gid = lane >> 2, tig = lane & 3;
 	uint4 af[KV][2];
 #pragma unroll
 	for (int ks = 0; ks < KV; ++ks)
 #pragma unroll
 		for (int h = 0; h < 2; ++h)
-			af[ks][h] = __ldg(it.vfrag + ((static_cast<size_t>(g) * KV + ks) * 2 + h) * 32 + lane);
-	const int wi = warp - wfirst;
-	if (wi < 0 || wi >= wcount)
-		return;
+			af[ks][h] = afrag[(ks * 2 + h) * 32 + lane];
 	// lane's ldmatrix row: line vbase + ks*16 + (lane & 7) + ((lane >> 3) & 1) * 8, column +(lane >> 4) * 8
 	const int krow = (lane & 7) + ((lane >> 3) & 1) * 8;
 	const int coff = (lane >> 4) * 8;
+	const char *rowp[KV];
+#pragma unroll
+	for (int ks = 0; ks < KV; ++ks)
+		rowp[ks] = in + ((vbase + ks * 16 + krow) % IR) * in_pitch * 2 + coff * 2;
 	for (int x0 = wi * 16; x0 < ncols; x0 += wcount * 16) {
 		float d0[4] = { 8192.0f, 8192.0f, 8192.0f, 8192.0f };
 		float d1[4] = { 8192.0f, 8192.0f, 8192.0f, 8192.0f };
 #pragma unroll
 		for (int ks = 0; ks < KV; ++ks) {
-			const int line = vbase + ks * 16 + krow;
-			const char *p = in + (line & imask) * in_pitch * 2 + (x0 + coff) * 2;
 			uint32_t b0, b1, b2, b3;
-			ldsm_x4_trans(b0, b1, b2, b3, p);
+			ldsm_x4_trans(b0, b1, b2, b3, rowp[ks] + x0 * 2);
 			const uint32_t ahi[4] = { af[ks][0].x, af[ks][0].y, af[ks][0].z, af[ks][0].w };
 			const uint32_t alo[4] = { af[ks][1].x, af[ks][1].y, af[ks][1].z, af[ks][1].w };
 			mma16816(d0, ahi, b0, b1);
@@ -355,9 +367,23 @@ __device__ __forceinline__ void v_pass(const Item &it, int g, int vbase, const c
 	}
 }
 
-// Kernel. Shared memory (MmaLayout): stage (raw u16 lines), src ring (fp16
-// source lines), mid ring (fp16 intermediate lines, H-first) or I (16 fp16
-// intermediate lines, V-first), per-item group bases and strip column bases.
+__device__ __forceinline__ void wait_groups(int pending)
+{
+	// cp.async.wait_group takes an immediate
+	switch (pending) {
+	case 0: cp_async_wait<0>(); break;
+	case 1: cp_async_wait<1>(); break;
+	case 2: cp_async_wait<2>(); break;
+	case 3: cp_async_wait<3>(); break;
+	default: cp_async_wait<4>(); break;
+	}
+}
+
+// Kernel. Shared memory (SmemLayout): staging ring of raw u16 lines, ring of
+// fp16 source lines, ring of fp16 intermediate lines (H-first) or 16 fp16
+// intermediate lines (V-first), the strip's horizontal tap fragments, depth+1
+// slots of vertical tap fragments, column-group bases and group bases.
+// Lines of step k + depth are in flight while step k computes.
 template <bool H_FIRST, int KV, int KH>
 __global__ void __launch_bounds__(kThreads, 4)
 mma_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, const __grid_constant__ FusedJob single,
@@ -369,11 +395,12 @@ mma_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, con
 	char *src_ring = smem + L.in_off;     // fp16 source lines
 	char *mid = smem + L.ring_off;        // H-first: fp16 intermediate lines
 	char *I = smem + L.i_off;             // V-first: 16 fp16 intermediate lines
+	const uint2 *hfrag = reinterpret_cast<const uint2 *>(smem + L.htaps_off);
+	char *vslots = smem + L.vcoef_off;
 	int *vb = reinterpret_cast<int *>(smem + L.vbase_off);
 	int *hb = reinterpret_cast<int *>(smem + L.hleft_off);
-	const int smask = L.stage_rows - 1;
-	const int imask = L.in_rows - 1;
-	const int rmask = L.ring_rows - 1;
+	const int SR = L.stage_rows, IR = L.in_rows, MR = L.ring_rows;
+	const int slot_bytes = L.step_groups * KV * 2 * 32 * 16;
 
 	// Lines a pass reads past the last loaded one hold finite values.
 	for (int i = threadIdx.x; i < L.htaps_off / 16; i += kThreads)
@@ -385,52 +412,80 @@ mma_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, con
 		const Item it = make_item(*Jp, t);
 		for (int g = it.g_begin + threadIdx.x; g < it.g_end; g += kThreads)
 			vb[g - it.g_begin] = __ldg(Jp->v_base + g);
-		for (int i = threadIdx.x; i < kStripW / 8; i += kThreads)
-			hb[i] = __ldg(Jp->h_left + min(it.c0 / 8 + i, (Jp->dst_w + 7) / 8 - 1));
+		const int cgroups = (Jp->dst_w + 7) / 8;
+		for (int i = threadIdx.x; i < it.sw / 8; i += kThreads)
+			hb[i] = __ldg(Jp->h_left + min(it.c0 / 8 + i, cgroups - 1));
+		{
+			// the strip's horizontal tap fragments (one per column group)
+			const int ncg = min(it.sw / 8, cgroups - it.c0 / 8);
+			const char *src = reinterpret_cast<const char *>(it.hfrag) + static_cast<size_t>(it.c0 / 8) * KH * 2 * 32 * 8;
+			for (int i = threadIdx.x; i < ncg * KH * 2 * 32 * 8 / 16; i += kThreads)
+				cp_async16(smem + L.htaps_off + i * 16, src + i * 16, 16);
+		}
 		__syncthreads();
 
 		const int nsteps = (it.g_end - it.g_begin + it.step_groups - 1) / it.step_groups;
+		const int D = it.depth;
+		auto groups_of = [&](int k, int *g0, int *g1) {
+			*g0 = it.g_begin + k * it.step_groups;
+			*g1 = min(it.g_end, *g0 + it.step_groups);
+		};
 		auto hi_of = [&](int k) {
-			const int g1 = min(it.g_end, it.g_begin + (k + 1) * it.step_groups);
+			int g0, g1;
+			groups_of(k, &g0, &g1);
 			return vb[g1 - 1 - it.g_begin] + KV * 16;
 		};
-		int lo_cur = vb[0];
-		int hi_cur = hi_of(0);
-		load_lines(it, lo_cur, hi_cur, stage, smask, L.pitch);
-		cp_async_commit();
-		__syncthreads();
-
-		for (int k = 0; k < nsteps; ++k) {
-			const int g0 = it.g_begin + k * it.step_groups;
-			const int g1 = min(it.g_end, g0 + it.step_groups);
-			int hi_next = hi_cur;
-			if (k + 1 < nsteps) {
-				hi_next = hi_of(k + 1);
-				load_lines(it, hi_cur, hi_next, stage, smask, L.pitch);
+		// prologue: steps 0 .. D-1 in flight, one commit group each
+		int issued_hi = vb[0];
+		for (int k = 0; k < D; ++k) {
+			if (k < nsteps) {
+				int g0, g1;
+				groups_of(k, &g0, &g1);
+				const int hi = hi_of(k);
+				load_lines(it, issued_hi, hi, stage, SR, L.pitch);
+				load_vfrag<KV>(it, g0, g1, vslots + (k % (D + 1)) * slot_bytes);
+				issued_hi = hi;
 			}
 			cp_async_commit();
-			cp_async_wait<1>();
-			convert_lines(it, lo_cur, hi_cur, stage, smask, src_ring, imask, L.pitch);
+		}
+		__syncthreads();  // lines stored by plain loads (unaligned planes) are visible to every converter
+
+		int lo_cur = vb[0];
+		for (int k = 0; k < nsteps; ++k) {
+			int g0, g1;
+			groups_of(k, &g0, &g1);
+			const int hi_cur = hi_of(k);
+			if (k + D < nsteps) {
+				int n0, n1;
+				groups_of(k + D, &n0, &n1);
+				const int hi = hi_of(k + D);
+				load_lines(it, issued_hi, hi, stage, SR, L.pitch);
+				load_vfrag<KV>(it, n0, n1, vslots + ((k + D) % (D + 1)) * slot_bytes);
+				issued_hi = hi;
+			}
+			cp_async_commit();
+			wait_groups(D);
+			convert_lines(it, lo_cur, hi_cur, stage, SR, src_ring, IR, L.pitch);
 			__syncthreads();
+			const uint4 *afrag = reinterpret_cast<const uint4 *>(vslots + (k % (D + 1)) * slot_bytes);
 			if (H_FIRST) {
-				h_pass<KH, false>(it, hb, src_ring, imask, L.pitch, lo_cur, hi_cur, mid, rmask, 0);
+				h_pass<KH, false>(it, hb, hfrag, src_ring, IR, L.pitch, lo_cur, hi_cur, mid, MR, 0);
 				__syncthreads();
 				const int ng = g1 - g0;
 				const int wpg = ng >= kWarps ? 1 : kWarps / ng;
-				for (int gi = 0; gi < ng; ++gi) {
-					const int first = (gi * wpg) % kWarps;
-					v_pass<KV, true>(it, g0 + gi, vb[g0 + gi - it.g_begin], mid, rmask, kMidPitch,
-					                 (it.cols_valid + 15) & ~15, ng >= kWarps ? (gi % kWarps) : first,
+				for (int gi = 0; gi < ng; ++gi)
+					v_pass<KV, true>(it, g0 + gi, vb[g0 + gi - it.g_begin], afrag + gi * KV * 2 * 32, mid, MR, kMidPitch,
+					                 (it.cols_valid + 15) & ~15, ng >= kWarps ? (gi % kWarps) : (gi * wpg) % kWarps,
 					                 ng >= kWarps ? 1 : wpg, nullptr, 0);
-				}
 			} else {
 				// one 16-row group per step: ring -> I (16 lines x pxa) -> destination
-				v_pass<KV, false>(it, g0, vb[g0 - it.g_begin], src_ring, imask, L.pitch, it.pxa, 0, kWarps, I, L.pitch);
+				v_pass<KV, false>(it, g0, vb[g0 - it.g_begin], afrag, src_ring, IR, L.pitch, it.pxa, 0, kWarps, I,
+				                  L.pitch);
 				__syncthreads();
-				h_pass<KH, true>(it, hb, I, 0x7fffffff, L.pitch, 0, 16, nullptr, 0, g0 * 16);
+				h_pass<KH, true>(it, hb, hfrag, I, 0x7fffffff, L.pitch, 0, 16, nullptr, 1, g0 * 16);
 			}
+			__syncthreads();  // slots of step k are reused by step k + D + 1
 			lo_cur = hi_cur;
-			hi_cur = hi_next;
 		}
 		cp_async_wait<0>();
 		__syncthreads();
