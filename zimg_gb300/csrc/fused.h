@@ -88,6 +88,7 @@ struct SmemLayout {
 	int total_bytes;
 	int ring_rows, in_rows, stage_rows, seg_groups, step_groups;
 	int depth;              // steps of lines in flight ahead of the computing step
+	int tile_off, tile_pitch;  // tensor-core kernel: staged output rows (packed u16)
 };
 
 // Host-side plan of one fused job: device tables plus a FusedJob template.

@@ -87,7 +87,7 @@ bool plan_mma(const FilterTable &first, const FilterTable &second, bool h_first,
 {
 	const FilterTable &H = h_first ? first : second;
 	const FilterTable &V = h_first ? second : first;
-	if (depth > 12 || H.rows != dst_w || V.rows != dst_h || H.input_width != src_w || V.input_width != src_h)
+	if (depth > 10 || H.rows != dst_w || V.rows != dst_h || H.input_width != src_w || V.input_width != src_h)
 		return false;
 	if (!split_exact(H, depth) || !split_exact(V, depth))
 		return false;
@@ -330,6 +330,9 @@ SmemLayout mma_layout(const FusedPlan *const *plans, int n)
 	off += a16(static_cast<size_t>(in) * L.pitch * 2);
 	L.i_off = off;
 	off += h_first ? 0 : a16(static_cast<size_t>(16) * L.pitch * 2);
+	L.tile_off = off;                        // staged output rows
+	L.tile_pitch = max_sw + 8;
+	off += a16(static_cast<size_t>(L.step_groups) * 16 * L.tile_pitch * 2);
 	L.htaps_off = off;                       // the strip's horizontal tap fragments
 	off += a16(static_cast<size_t>(max_sw / 8) * kh * 2 * 32 * 8);
 	L.vcoef_off = off;                       // depth + 1 slots of vertical tap fragments

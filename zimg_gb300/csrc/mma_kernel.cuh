@@ -5,8 +5,8 @@
 // banded matrix products on the tensor cores with mma.sync m16n8k16
 // (fp16 operands, fp32 accumulation):
 //
-//   * samples are re-centred, v' = v - 2^(depth-1), which is exact in fp16 for
-//     depth <= 12;
+//   * samples are re-centred, v' = v - 2^(depth-1), exact in fp16 (the planner
+//     only certifies depths up to 10, see below);
 //   * each int16 tap is split c = hi + lo, hi = c - (c & 31) (a multiple of 32
 //     with at most 11 significant bits), lo = c & 31, both exact in fp16;
 //   * both halves multiply the same samples into one fp32 accumulator that
@@ -83,19 +83,19 @@ __device__ __forceinline__ uint32_t pack_u16x2(float acc0, float acc1, float mag
 	return q;
 }
 
-// Two clamped samples (packed u16, each < 1024 when fast) -> centred fp16x2.
-__device__ __forceinline__ uint32_t u16x2_to_centred_h2(uint32_t q, uint32_t bias_h2, bool fast)
+// Two clamped samples (packed u16, each < 1024) -> centred fp16x2: the fp16
+// with exponent 2^10 and mantissa q is exactly 1024 + q.
+__device__ __forceinline__ uint32_t u16x2_to_centred_h2(uint32_t q, uint32_t bias_h2)
 {
-	if (fast) {
-		// fp16 with exponent 2^10 and mantissa q is exactly 1024 + q (q < 1024)
-		const uint32_t v = q | 0x64006400u;
-		const __half2 h = __hsub2(*reinterpret_cast<const __half2 *>(&v), *reinterpret_cast<const __half2 *>(&bias_h2));
-		return *reinterpret_cast<const uint32_t *>(&h);
-	}
-	const float f0 = static_cast<float>(q & 0xFFFFu) - __half2float(__low2half(*reinterpret_cast<const __half2 *>(&bias_h2)));
-	const float f1 = static_cast<float>(q >> 16) - __half2float(__low2half(*reinterpret_cast<const __half2 *>(&bias_h2)));
-	const __half2 h = __floats2half2_rn(f0, f1);
+	const uint32_t v = q | 0x64006400u;
+	const __half2 h = __hsub2(*reinterpret_cast<const __half2 *>(&v), *reinterpret_cast<const __half2 *>(&bias_h2));
 	return *reinterpret_cast<const uint32_t *>(&h);
+}
+
+__device__ __forceinline__ int wrap(int s, int R)
+{
+	s = s >= R ? s - R : s;
+	return s >= R ? s - R : s;
 }
 
 struct Item {
@@ -108,9 +108,11 @@ struct Item {
 	int src_w, src_h, dst_h, vec_ok;
 	int c0, cols_valid, xlo, pxa, strip, sw;
 	int g_begin, g_end, step_groups, depth;
+	// this thread's place in line copies: chunk q0 of line offset l0, then
+	// advance by (sl lines, sq chunks) per iteration
+	int chunks, q0, l0, sl, sq;
 	float magic;
 	uint32_t pmax2, bias_h2;
-	bool fast;
 };
 
 __device__ __forceinline__ int find_job(const FusedJob *__restrict__ jobs, int num_jobs, int t)
@@ -155,54 +157,62 @@ __device__ __forceinline__ Item make_item(const FusedJob &J, int t)
 	const uint32_t pm = static_cast<uint32_t>(J.pixel_max);
 	it.pmax2 = pm | (pm << 16);
 	const __half2 b = __floats2half2_rn(1024.0f + J.offset, 1024.0f + J.offset);
-	it.fast = J.pixel_max < 1024.0f;
-	const __half2 bo = __floats2half2_rn(J.offset, J.offset);
-	it.bias_h2 = it.fast ? *reinterpret_cast<const uint32_t *>(&b) : *reinterpret_cast<const uint32_t *>(&bo);
+	it.bias_h2 = *reinterpret_cast<const uint32_t *>(&b);
+	it.chunks = it.pxa / 8;
+	it.q0 = threadIdx.x % it.chunks;
+	it.l0 = threadIdx.x / it.chunks;
+	it.sl = kThreads / it.chunks;
+	it.sq = kThreads % it.chunks;
 	return it;
 }
 
-// Source lines [a, b) of the strip (raw u16) into staging slots (line % R).
-__device__ __forceinline__ void load_lines(const Item &it, int a, int b, char *stage, int R, int pitch)
+// Source lines [a, b) of the strip (raw u16) into staging slots; sa = a % SR.
+__device__ __forceinline__ void load_lines(const Item &it, int a, int b, char *stage, int SR, int sa, int pitch)
 {
-	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-	const int chunks = it.pxa / 8;
-	for (int y = a + warp; y < b; y += kWarps) {
+	int y = a + it.l0, q = it.q0;
+	for (; y < b; ) {
 		const bool row_ok = y < it.src_h;
 		const char *row = it.src + static_cast<ptrdiff_t>(row_ok ? y : 0) * it.src_stride;
-		char *srow = stage + (y % R) * pitch * 2;
+		char *srow = stage + wrap(sa + (y - a), SR) * pitch * 2;
+		const int gx = it.xlo + q * 8;
 		if (it.vec_ok) {
-			for (int q = lane; q < chunks; q += 32) {
-				const int gx = it.xlo + q * 8;
-				const int n = row_ok ? max(0, min(8, it.src_w - gx)) : 0;
-				cp_async16(srow + q * 16, n ? row + static_cast<ptrdiff_t>(gx) * 2 : it.src, n * 2);
-			}
+			const int n = row_ok ? max(0, min(8, it.src_w - gx)) : 0;
+			cp_async16(srow + q * 16, n ? row + static_cast<ptrdiff_t>(gx) * 2 : it.src, n * 2);
 		} else {
-			for (int x = lane; x < it.pxa; x += 32) {
-				const int gx = it.xlo + x;
-				const bool ok = row_ok && gx < it.src_w;
-				reinterpret_cast<uint16_t *>(srow)[x] =
-					ok ? __ldg(reinterpret_cast<const uint16_t *>(row) + gx) : static_cast<uint16_t>(0);
-			}
+			uint16_t *d = reinterpret_cast<uint16_t *>(srow + q * 16);
+#pragma unroll
+			for (int e = 0; e < 8; ++e)
+				d[e] = (row_ok && gx + e < it.src_w) ? __ldg(reinterpret_cast<const uint16_t *>(row) + gx + e)
+				                                      : static_cast<uint16_t>(0);
+		}
+		q += it.sq;
+		y += it.sl;
+		if (q >= it.chunks) {
+			q -= it.chunks;
+			++y;
 		}
 	}
 }
 
-// Raw staged lines this thread loaded -> centred fp16 lines.
-__device__ __forceinline__ void convert_lines(const Item &it, int a, int b, const char *stage, int SR, char *ring,
-                                              int RR, int pitch)
+// Raw staged lines this thread loaded -> centred fp16 lines (same mapping).
+__device__ __forceinline__ void convert_lines(const Item &it, int a, int b, const char *stage, int SR, int sa,
+                                              char *ring, int RR, int ra, int pitch)
 {
-	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-	const int chunks = it.pxa / 8;
-	for (int y = a + warp; y < b; y += kWarps) {
-		const uint4 *s = reinterpret_cast<const uint4 *>(stage + (y % SR) * pitch * 2);
-		uint4 *d = reinterpret_cast<uint4 *>(ring + (y % RR) * pitch * 2);
-		for (int q = lane; q < chunks; q += 32) {
-			uint4 u = s[q];
-			u.x = u16x2_to_centred_h2(u.x, it.bias_h2, it.fast);
-			u.y = u16x2_to_centred_h2(u.y, it.bias_h2, it.fast);
-			u.z = u16x2_to_centred_h2(u.z, it.bias_h2, it.fast);
-			u.w = u16x2_to_centred_h2(u.w, it.bias_h2, it.fast);
-			d[q] = u;
+	int y = a + it.l0, q = it.q0;
+	for (; y < b; ) {
+		const uint4 *s = reinterpret_cast<const uint4 *>(stage + wrap(sa + (y - a), SR) * pitch * 2);
+		uint4 *d = reinterpret_cast<uint4 *>(ring + wrap(ra + (y - a), RR) * pitch * 2);
+		uint4 u = s[q];
+		u.x = u16x2_to_centred_h2(u.x, it.bias_h2);
+		u.y = u16x2_to_centred_h2(u.y, it.bias_h2);
+		u.z = u16x2_to_centred_h2(u.z, it.bias_h2);
+		u.w = u16x2_to_centred_h2(u.w, it.bias_h2);
+		d[q] = u;
+		q += it.sq;
+		y += it.sl;
+		if (q >= it.chunks) {
+			q -= it.chunks;
+			++y;
 		}
 	}
 }
@@ -219,12 +229,13 @@ __device__ __forceinline__ void load_vfrag(const Item &it, int g0, int g1, char 
 
 // Horizontal pass on 16-line blocks: for each column group cg (8 outputs),
 // D[16 lines][8] = sum over KH*16 columns starting at hbase[cg] - xlo.
-// A: lines from `in` (ldmatrix, row addresses per line), B: tap fragments
-// from shared memory. FINAL: lines are destination rows r0 + (y - a); else
-// store centred fp16 into intermediate ring slots (y % OR), columns cg*8...
-template <int KH, bool FINAL>
+// A: lines of `in` (ring of IR lines, line a in slot ia; ldmatrix with a row
+// address per line), B: tap fragments from shared memory.
+// out: TO_RING: centred fp16 into ring slots (line a in slot oa of OR);
+//      else: packed u16 into the staged output tile (line a -> tile row 0).
+template <int KH, bool TO_RING>
 __device__ __forceinline__ void h_pass(const Item &it, const int *hbase, const uint2 *hfrag, const char *in, int IR,
-                                       int in_pitch, int a, int b, char *out, int OR, int r0)
+                                       int ia, int in_pitch, int a, int b, char *out, int OR, int oa, int out_pitch)
 {
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	const int gid = lane >> 2, tig = lane & 3;
@@ -239,8 +250,7 @@ __device__ __forceinline__ void h_pass(const Item &it, const int *hbase, const u
 		const int col0 = hbase[cg] - it.xlo;
 		for (int y0 = a; y0 < b; y0 += 16) {
 			// row address for this lane: line y0 + (lane & 15), column block (lane >> 4) * 8
-			const int ly = y0 + (lane & 15);
-			const char *rowp = in + (ly % IR) * in_pitch * 2 + (col0 + (lane >> 4) * 8) * 2;
+			const char *rowp = in + wrap(ia + (y0 - a) + (lane & 15), IR) * in_pitch * 2 + (col0 + (lane >> 4) * 8) * 2;
 			float d[4] = { 8192.0f, 8192.0f, 8192.0f, 8192.0f };
 #pragma unroll
 			for (int ks = 0; ks < KH; ++ks) {
@@ -253,49 +263,27 @@ __device__ __forceinline__ void h_pass(const Item &it, const int *hbase, const u
 			}
 			const uint32_t q01 = pack_u16x2(d[0], d[1], it.magic, it.pmax2);  // line y0+gid, cols 2tig..
 			const uint32_t q23 = pack_u16x2(d[2], d[3], it.magic, it.pmax2);  // line y0+gid+8
-			const int ya = y0 + gid, yb = y0 + gid + 8;
 			const int col = cg * 8 + 2 * tig;
-			if (!FINAL) {
-				*reinterpret_cast<uint32_t *>(out + (ya % OR) * kMidPitch * 2 + col * 2) =
-					u16x2_to_centred_h2(q01, it.bias_h2, it.fast);
-				*reinterpret_cast<uint32_t *>(out + (yb % OR) * kMidPitch * 2 + col * 2) =
-					u16x2_to_centred_h2(q23, it.bias_h2, it.fast);
-			} else if (col < it.cols_valid) {
-				const int ra = r0 + (ya - a), rb = r0 + (yb - a);
-				uint16_t *pa = reinterpret_cast<uint16_t *>(it.dst + static_cast<ptrdiff_t>(ra) * it.dst_stride) + it.c0 + col;
-				uint16_t *pb = reinterpret_cast<uint16_t *>(it.dst + static_cast<ptrdiff_t>(rb) * it.dst_stride) + it.c0 + col;
-				const bool pair = col + 1 < it.cols_valid;
-				if (ya < b && ra < it.dst_h) {
-					if (pair && it.vec_ok)
-						*reinterpret_cast<uint32_t *>(pa) = q01;
-					else {
-						pa[0] = static_cast<uint16_t>(q01);
-						if (pair)
-							pa[1] = static_cast<uint16_t>(q01 >> 16);
-					}
-				}
-				if (yb < b && rb < it.dst_h) {
-					if (pair && it.vec_ok)
-						*reinterpret_cast<uint32_t *>(pb) = q23;
-					else {
-						pb[0] = static_cast<uint16_t>(q23);
-						if (pair)
-							pb[1] = static_cast<uint16_t>(q23 >> 16);
-					}
-				}
+			if (TO_RING) {
+				const int sa = wrap(oa + (y0 - a) + gid, OR), sb = wrap(oa + (y0 - a) + gid + 8, OR);
+				*reinterpret_cast<uint32_t *>(out + sa * out_pitch * 2 + col * 2) = u16x2_to_centred_h2(q01, it.bias_h2);
+				*reinterpret_cast<uint32_t *>(out + sb * out_pitch * 2 + col * 2) = u16x2_to_centred_h2(q23, it.bias_h2);
+			} else {
+				*reinterpret_cast<uint32_t *>(out + (y0 - a + gid) * out_pitch * 2 + col * 2) = q01;
+				*reinterpret_cast<uint32_t *>(out + (y0 - a + gid + 8) * out_pitch * 2 + col * 2) = q23;
 			}
 		}
 	}
 }
 
-// Vertical pass for one 16-row group g: D[16 rows][8 cols] = sum over KV*16
+// Vertical pass for one 16-row group: D[16 rows][8 cols] = sum over KV*16
 // lines from vbase of taps * in[line][col]. A: tap fragments (shared slot),
-// B: lines (ldmatrix.trans, row addresses per line). Warps [wfirst,
-// wfirst + wcount) take columns [0, ncols) 16 at a time. FINAL: destination
-// rows g*16 + r; else I lines.
-template <int KV, bool FINAL>
-__device__ __forceinline__ void v_pass(const Item &it, int g, int vbase, const uint4 *afrag, const char *in, int IR,
-                                       int in_pitch, int ncols, int wfirst, int wcount, char *I, int i_pitch)
+// B: lines of `in` (ring of IR lines, line vbase in slot iv; ldmatrix.trans).
+// Warps [wfirst, wfirst + wcount) take columns [0, ncols) 16 at a time.
+// TO_CENTRED: centred fp16 rows (tile of 16 lines); else packed u16 rows.
+template <int KV, bool TO_CENTRED>
+__device__ __forceinline__ void v_pass(const Item &it, const uint4 *afrag, const char *in, int IR, int iv,
+                                       int in_pitch, int ncols, int wfirst, int wcount, char *out, int out_pitch)
 {
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	const int wi = warp - wfirst;
@@ -314,7 +302,7 @@ __device__ __forceinline__ void v_pass(const Item &it, int g, int vbase, const u
 	const char *rowp[KV];
 #pragma unroll
 	for (int ks = 0; ks < KV; ++ks)
-		rowp[ks] = in + ((vbase + ks * 16 + krow) % IR) * in_pitch * 2 + coff * 2;
+		rowp[ks] = in + wrap(iv + ks * 16 + krow, IR) * in_pitch * 2 + coff * 2;
 	for (int x0 = wi * 16; x0 < ncols; x0 += wcount * 16) {
 		float d0[4] = { 8192.0f, 8192.0f, 8192.0f, 8192.0f };
 		float d1[4] = { 8192.0f, 8192.0f, 8192.0f, 8192.0f };
@@ -332,37 +320,38 @@ __device__ __forceinline__ void v_pass(const Item &it, int g, int vbase, const u
 #pragma unroll
 		for (int nb = 0; nb < 2; ++nb) {
 			const float *d = nb ? d1 : d0;
-			const uint32_t q01 = pack_u16x2(d[0], d[1], it.magic, it.pmax2);  // row gid
-			const uint32_t q23 = pack_u16x2(d[2], d[3], it.magic, it.pmax2);  // row gid + 8
-			const int col = x0 + nb * 8 + 2 * tig;
-			if (!FINAL) {
-				*reinterpret_cast<uint32_t *>(I + gid * i_pitch * 2 + col * 2) = u16x2_to_centred_h2(q01, it.bias_h2, it.fast);
-				*reinterpret_cast<uint32_t *>(I + (gid + 8) * i_pitch * 2 + col * 2) =
-					u16x2_to_centred_h2(q23, it.bias_h2, it.fast);
-			} else if (col < it.cols_valid) {
-				const int ra = g * 16 + gid, rb = ra + 8;
-				const bool pair = col + 1 < it.cols_valid;
-				uint16_t *pa = reinterpret_cast<uint16_t *>(it.dst + static_cast<ptrdiff_t>(ra) * it.dst_stride) + it.c0 + col;
-				uint16_t *pb = reinterpret_cast<uint16_t *>(it.dst + static_cast<ptrdiff_t>(rb) * it.dst_stride) + it.c0 + col;
-				if (ra < it.dst_h) {
-					if (pair && it.vec_ok)
-						*reinterpret_cast<uint32_t *>(pa) = q01;
-					else {
-						pa[0] = static_cast<uint16_t>(q01);
-						if (pair)
-							pa[1] = static_cast<uint16_t>(q01 >> 16);
-					}
-				}
-				if (rb < it.dst_h) {
-					if (pair && it.vec_ok)
-						*reinterpret_cast<uint32_t *>(pb) = q23;
-					else {
-						pb[0] = static_cast<uint16_t>(q23);
-						if (pair)
-							pb[1] = static_cast<uint16_t>(q23 >> 16);
-					}
-				}
+			uint32_t q01 = pack_u16x2(d[0], d[1], it.magic, it.pmax2);  // row gid
+			uint32_t q23 = pack_u16x2(d[2], d[3], it.magic, it.pmax2);  // row gid + 8
+			if (TO_CENTRED) {
+				q01 = u16x2_to_centred_h2(q01, it.bias_h2);
+				q23 = u16x2_to_centred_h2(q23, it.bias_h2);
 			}
+			const int col = x0 + nb * 8 + 2 * tig;
+			*reinterpret_cast<uint32_t *>(out + gid * out_pitch * 2 + col * 2) = q01;
+			*reinterpret_cast<uint32_t *>(out + (gid + 8) * out_pitch * 2 + col * 2) = q23;
+		}
+	}
+}
+
+// Staged output tile (rows [0, nrows) of packed u16, out_pitch halfs) ->
+// destination rows r0.., strip columns, 16-byte stores where whole.
+__device__ __forceinline__ void store_tile(const Item &it, const char *tile, int out_pitch, int r0, int nrows)
+{
+	const int per_row = it.sw / 8;
+	const int rows = min(nrows, it.dst_h - r0);
+	for (int i = threadIdx.x; i < rows * per_row; i += kThreads) {
+		const int r = i / per_row, q = i - r * per_row;
+		const int col = q * 8;
+		if (col >= it.cols_valid)
+			continue;
+		const uint4 v = *reinterpret_cast<const uint4 *>(tile + r * out_pitch * 2 + col * 2);
+		uint16_t *d = reinterpret_cast<uint16_t *>(it.dst + static_cast<ptrdiff_t>(r0 + r) * it.dst_stride) + it.c0 + col;
+		if (it.vec_ok && col + 8 <= it.cols_valid) {
+			*reinterpret_cast<uint4 *>(d) = v;
+		} else {
+			const uint32_t w[4] = { v.x, v.y, v.z, v.w };
+			for (int e = 0; e < 8 && col + e < it.cols_valid; ++e)
+				d[e] = static_cast<uint16_t>(w[e >> 1] >> (16 * (e & 1)));
 		}
 	}
 }
@@ -381,9 +370,10 @@ __device__ __forceinline__ void wait_groups(int pending)
 
 // Kernel. Shared memory (SmemLayout): staging ring of raw u16 lines, ring of
 // fp16 source lines, ring of fp16 intermediate lines (H-first) or 16 fp16
-// intermediate lines (V-first), the strip's horizontal tap fragments, depth+1
-// slots of vertical tap fragments, column-group bases and group bases.
-// Lines of step k + depth are in flight while step k computes.
+// intermediate lines (V-first), the staged output tile, the strip's
+// horizontal tap fragments, depth+1 slots of vertical tap fragments,
+// column-group bases and group bases. Lines of step k + depth are in flight
+// while step k computes.
 template <bool H_FIRST, int KV, int KH>
 __global__ void __launch_bounds__(kThreads, 4)
 mma_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, const __grid_constant__ FusedJob single,
@@ -394,13 +384,15 @@ mma_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, con
 	char *stage = smem + L.stage_off;
 	char *src_ring = smem + L.in_off;     // fp16 source lines
 	char *mid = smem + L.ring_off;        // H-first: fp16 intermediate lines
-	char *I = smem + L.i_off;             // V-first: 16 fp16 intermediate lines
+	char *I = smem + L.i_off;             // V-first: 16 fp16 intermediate lines; then the output tile
+	char *tile = smem + L.tile_off;       // staged output rows (packed u16)
 	const uint2 *hfrag = reinterpret_cast<const uint2 *>(smem + L.htaps_off);
 	char *vslots = smem + L.vcoef_off;
 	int *vb = reinterpret_cast<int *>(smem + L.vbase_off);
 	int *hb = reinterpret_cast<int *>(smem + L.hleft_off);
 	const int SR = L.stage_rows, IR = L.in_rows, MR = L.ring_rows;
 	const int slot_bytes = L.step_groups * KV * 2 * 32 * 16;
+	const int tile_pitch = L.tile_pitch;
 
 	// Lines a pass reads past the last loaded one hold finite values.
 	for (int i = threadIdx.x; i < L.htaps_off / 16; i += kThreads)
@@ -442,7 +434,7 @@ mma_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, con
 				int g0, g1;
 				groups_of(k, &g0, &g1);
 				const int hi = hi_of(k);
-				load_lines(it, issued_hi, hi, stage, SR, L.pitch);
+				load_lines(it, issued_hi, hi, stage, SR, issued_hi % SR, L.pitch);
 				load_vfrag<KV>(it, g0, g1, vslots + (k % (D + 1)) * slot_bytes);
 				issued_hi = hi;
 			}
@@ -459,32 +451,40 @@ mma_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, con
 				int n0, n1;
 				groups_of(k + D, &n0, &n1);
 				const int hi = hi_of(k + D);
-				load_lines(it, issued_hi, hi, stage, SR, L.pitch);
+				load_lines(it, issued_hi, hi, stage, SR, issued_hi % SR, L.pitch);
 				load_vfrag<KV>(it, n0, n1, vslots + ((k + D) % (D + 1)) * slot_bytes);
 				issued_hi = hi;
 			}
 			cp_async_commit();
 			wait_groups(D);
-			convert_lines(it, lo_cur, hi_cur, stage, SR, src_ring, IR, L.pitch);
+			convert_lines(it, lo_cur, hi_cur, stage, SR, lo_cur % SR, src_ring, IR, lo_cur % IR, L.pitch);
 			__syncthreads();
 			const uint4 *afrag = reinterpret_cast<const uint4 *>(vslots + (k % (D + 1)) * slot_bytes);
 			if (H_FIRST) {
-				h_pass<KH, false>(it, hb, hfrag, src_ring, IR, L.pitch, lo_cur, hi_cur, mid, MR, 0);
+				h_pass<KH, true>(it, hb, hfrag, src_ring, IR, lo_cur % IR, L.pitch, lo_cur, hi_cur, mid, MR,
+				                 lo_cur % MR, kMidPitch);
 				__syncthreads();
 				const int ng = g1 - g0;
-				const int wpg = ng >= kWarps ? 1 : kWarps / ng;
-				for (int gi = 0; gi < ng; ++gi)
-					v_pass<KV, true>(it, g0 + gi, vb[g0 + gi - it.g_begin], afrag + gi * KV * 2 * 32, mid, MR, kMidPitch,
-					                 (it.cols_valid + 15) & ~15, ng >= kWarps ? (gi % kWarps) : (gi * wpg) % kWarps,
-					                 ng >= kWarps ? 1 : wpg, nullptr, 0);
-			} else {
-				// one 16-row group per step: ring -> I (16 lines x pxa) -> destination
-				v_pass<KV, false>(it, g0, vb[g0 - it.g_begin], afrag, src_ring, IR, L.pitch, it.pxa, 0, kWarps, I,
-				                  L.pitch);
+				const int wpg = kWarps / ng;  // ng <= step_groups <= kWarps / 2
+				const int gi = (threadIdx.x >> 5) / wpg;
+				if (gi < ng) {
+					const int vbase = vb[g0 + gi - it.g_begin];
+					v_pass<KV, false>(it, afrag + gi * KV * 2 * 32, mid, MR, vbase % MR, kMidPitch,
+					                  (it.cols_valid + 15) & ~15, gi * wpg, wpg, tile + gi * 16 * tile_pitch * 2,
+					                  tile_pitch);
+				}
 				__syncthreads();
-				h_pass<KH, true>(it, hb, hfrag, I, 0x7fffffff, L.pitch, 0, 16, nullptr, 1, g0 * 16);
+				store_tile(it, tile, tile_pitch, g0 * 16, ng * 16);
+			} else {
+				// one 16-row group per step: ring -> I (16 lines x pxa) -> tile -> destination
+				const int vbase = vb[g0 - it.g_begin];
+				v_pass<KV, true>(it, afrag, src_ring, IR, vbase % IR, L.pitch, it.pxa, 0, kWarps, I, L.pitch);
+				__syncthreads();
+				h_pass<KH, false>(it, hb, hfrag, I, 1 << 30, 0, L.pitch, 0, 16, tile, 1, 0, tile_pitch);
+				__syncthreads();
+				store_tile(it, tile, tile_pitch, g0 * 16, 16);
 			}
-			__syncthreads();  // slots of step k are reused by step k + D + 1
+			__syncthreads();  // slots of step k are reused by step k + D + 1; the tile by step k + 1
 			lo_cur = hi_cur;
 		}
 		cp_async_wait<0>();
