@@ -191,6 +191,10 @@ def run_ours(args):
     zg.load()
 
     jobs, cfg = workload(args.workload, args.frames, seed=0x5EED0000 + rank)
+    if args.engine:
+        for j in jobs:
+            j["engine"] = args.engine
+        cfg["engine"] = args.engine
     rng = np.random.default_rng(1234 + rank)
     # Distinct source planes per job (the batch is the working set), generated on the device from a few seeded
     # host planes so set-up stays quick.
@@ -210,6 +214,9 @@ def run_ours(args):
                      .set_shift_w(j["shift_w"]).set_shift_h(j["shift_h"]).set_engine(j["engine"]))
     batch = zg.Batch(convs)
     batch.set_io(srcs, dsts)
+    if not args.engine and not args.no_autotune:
+        # plan choice per job kind by timing on the bound planes (set-up, not timed)
+        cfg["autotune_jobs_changed"] = batch.autotune()
     tmp = torch.empty(max(batch.tmp_size, 1), dtype=torch.uint8, device="cuda")
     launches_per_step = batch.launch_count
     stream = torch.cuda.current_stream()
@@ -261,6 +268,8 @@ def run_ours(args):
         hdst = [torch.empty(dsts[i].shape, dtype=dsts[i].dtype).pin_memory() for i in range(n_e2e)]
         sub = zg.Batch(convs[:n_e2e])
         sub.set_io(srcs[:n_e2e], dsts[:n_e2e])
+        if not args.engine and not args.no_autotune:
+            sub.autotune()
         stmp = torch.empty(max(sub.tmp_size, 1), dtype=torch.uint8, device="cuda")
 
         def e2e_step():
@@ -407,6 +416,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--e2e-planes", type=int, default=48)
+    ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--engine", default=None, choices=["auto", "cuda", "tensor"],
+                    help="override every job's engine (cuda = the plain CUDA-core kernels)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":

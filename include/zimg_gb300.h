@@ -170,8 +170,9 @@ ZG_API void zg_resize_free(zg_resize *r);
 /* Device scratch bytes that zg_resize_process needs (0 when fused or single pass). */
 ZG_API zg_error_code zg_resize_get_tmp_size(const zg_resize *r, size_t *out);
 /* Number of passes (0 = plain copy, 1, 2), whether the first is horizontal, and
- * how the passes run: 0 separate kernels, 1 one fused CUDA-core kernel, 2 one
- * fused tensor-core kernel. */
+ * how the passes run: 0 separate CUDA-core kernels, 1 one fused CUDA-core
+ * kernel, 2 one fused tensor-core kernel, 3 separate kernels of which at least
+ * one runs on the tensor cores (FP32 wide filters). */
 ZG_API zg_error_code zg_resize_get_info(const zg_resize *r, int *num_passes, int *first_horizontal, int *fused);
 ZG_API zg_error_code zg_resize_process(const zg_resize *r, const void *src, ptrdiff_t src_stride,
                                 void *dst, ptrdiff_t dst_stride, void *tmp, zg_stream stream);
@@ -221,6 +222,18 @@ ZG_API zg_error_code zg_batch_get_tmp_size(const zg_batch *b, size_t *out);
 ZG_API zg_error_code zg_batch_set_io(zg_batch *b, const zg_batch_io *io, zg_stream stream);
 ZG_API zg_error_code zg_batch_process(const zg_batch *b, void *tmp, zg_stream stream);
 ZG_API zg_error_code zg_batch_process_graph(zg_batch *b, void *tmp, zg_stream stream);
+/*
+ * No counterpart in zimg (its CPU dispatch is fixed per build, cpuinfo.h):
+ * the autotuner. For every set of jobs with identical parameters and engine
+ * ZG_ENGINE_AUTO, times each distinct way the planner can run them (fused
+ * CUDA-core kernel, separate CUDA-core passes, tensor-core kernel or passes)
+ * on up to 8 of their bound planes (zg_batch_set_io first; their outputs are
+ * overwritten with valid results), keeps the fastest and rebuilds the launch
+ * groups. Allocates scratch for the trials and synchronises the stream. The
+ * batch's tmp size may change: query zg_batch_get_tmp_size again. *changed
+ * (optional) receives the number of jobs whose plan changed.
+ */
+ZG_API zg_error_code zg_batch_autotune(zg_batch *b, zg_stream stream, unsigned *changed);
 /* Number of kernel launches one zg_batch_process issues. */
 ZG_API zg_error_code zg_batch_get_launch_count(const zg_batch *b, unsigned *out);
 

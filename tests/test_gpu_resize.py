@@ -5,6 +5,8 @@ tests demand (test/resize/x86/resize_impl_avx2_test.cpp:70, SNR = infinity).
 f32 CUDA-core path: bit-exact against the oracle's sequential fused
 multiply-add order (mode "fma"); its error against the FP64 oracle must be no
 worse than 2x zimg's C path's own error plus 1e-6 (tolerance stated here).
+f32 tensor-core passes (3xTF32, summed in another order) are held to that
+error bound only.
 """
 import math
 
@@ -174,7 +176,12 @@ def test_config3_wide_filter_down16_f32(cuda, oracle):
     rng = np.random.default_rng(0x5EED0003)
     src = band_limited(rng, 1080, 1920)
     got, r = run_conversion(src, 120, 67, "lanczos", 4, engine="cuda")
+    assert r.info["engine"] == "passes"
     _f32_check(oracle, src, got, 120, 67, "lanczos", 4)
+    # 128 taps per output: the planner puts both passes on the tensor cores (3xTF32)
+    got, r = run_conversion(src, 120, 67, "lanczos", 4)
+    assert r.info["engine"] == "tensor-passes"
+    _f32_check(oracle, src, got, 120, 67, "lanczos", 4, exact=False)
 
 
 def test_config5_extreme_ratios_f32(cuda, oracle):
@@ -185,6 +192,27 @@ def test_config5_extreme_ratios_f32(cuda, oracle):
     big = band_limited(rng, 1600, 1600)
     got, _ = run_conversion(big, 16, 16, "lanczos", 3, engine="cuda")
     _f32_check(oracle, big, got, 16, 16, "lanczos", 3)
+    got, r = run_conversion(big, 16, 16, "lanczos", 3)  # 600 taps: tensor cores
+    assert r.info["engine"] == "tensor-passes"
+    _f32_check(oracle, big, got, 16, 16, "lanczos", 3, exact=False)
+
+
+@pytest.mark.parametrize("kind,a", [("lanczos", 4), ("lanczos", 3), ("bicubic", math.nan), ("spline64", math.nan)])
+def test_tensor_core_f32_error_bound(cuda, oracle, kind, a):
+    """3xTF32 passes against the FP64 oracle: no worse than twice the C path's
+    own error, over shapes that exercise partial output groups, partial
+    16-wide tiles, clamped band ends and unaligned planes."""
+    rng = np.random.default_rng(abs(hash((kind, a, "tc"))) % 2**32)
+    shapes = [((1080, 1920), (67, 120)), ((517, 333), (31, 29)), ((64, 64), (300, 200)), ((130, 7), (9, 3)),
+              ((1, 257), (1, 5)), ((257, 1), (5, 1))]
+    for (sh, sw), (dh, dw) in shapes:
+        src = band_limited(rng, sh, sw) if sh > 1 and sw > 1 else rng.random((sh, sw), dtype=np.float32)
+        kw = dict(shift_w=float(rng.normal(0, 2)), shift_h=float(rng.normal(0, 2)))
+        pad, off = int(rng.choice([0, 1, 3])), int(rng.choice([0, 1]))
+        got, r = run_conversion(src, dw, dh, kind, a, pad=pad, offset=off, engine="tensor", **kw)
+        if r.info["num_passes"]:
+            assert r.info["engine"] == "tensor-passes", r.info
+        _f32_check(oracle, src, got, dw, dh, kind, a, exact=False, **kw)
 
 
 def test_config5_interlaced_fields_f32(cuda, oracle):
@@ -303,6 +331,43 @@ def test_batch_matches_single(cuda, oracle):
         torch.cuda.synchronize()
         for d, w in zip(dsts, wants):
             np.testing.assert_array_equal(to_host(d, np.uint16), w, err_msg=mode)
+
+
+def test_batch_autotune_keeps_results(cuda, oracle):
+    """The autotuner may swap plans per job kind; u16 outputs stay bit-exact
+    and f32 outputs stay within the FP64 error bound, in plain and graph
+    launches."""
+    import torch
+    import zimg_gb300 as zg
+    rng = np.random.default_rng(5)
+    convs, srcs, dsts, checks = [], [], [], []
+    for _ in range(3):  # identical u16 jobs are tuned once
+        src = rng.integers(0, 1024, size=(135, 240), dtype=np.uint16)
+        convs.append(zg.ResizeConversion(240, 135, "word").set_depth(10).set_filter("lanczos", 3)
+                     .set_dst_width(480).set_dst_height(270))
+        srcs.append(to_dev(src))
+        dsts.append(empty(270, 480, np.uint16))
+        checks.append(("u16", src, oracle.resize_plane(src, 480, 270, "lanczos", 3, depth=10)))
+    for (sh, sw, dh, dw, kind, a) in ((540, 960, 34, 60, "lanczos", 4), (270, 480, 180, 320, "bicubic", math.nan)):
+        src = band_limited(rng, sh, sw)
+        convs.append(zg.ResizeConversion(sw, sh, "float").set_filter(kind, a).set_dst_width(dw).set_dst_height(dh))
+        srcs.append(to_dev(src))
+        dsts.append(empty(dh, dw, np.float32))
+        checks.append(("f32", src, (dw, dh, kind, a)))
+    b = zg.Batch(convs)
+    b.set_io(srcs, dsts)
+    b.autotune()
+    for mode in ("plain", "graph"):
+        for d in dsts:
+            d.zero_()
+        (b.process if mode == "plain" else b.process_graph)()
+        torch.cuda.synchronize()
+        for d, (kind, src, want) in zip(dsts, checks):
+            if kind == "u16":
+                np.testing.assert_array_equal(to_host(d, np.uint16), want, err_msg=mode)
+            else:
+                dw, dh, fk, fa = want
+                _f32_check(oracle, src, to_host(d, np.float32), dw, dh, fk, fa, exact=False)
 
 
 def test_graph_plane_params_known_answers(cuda):

@@ -79,6 +79,26 @@ void DevicePass::upload()
 	tables.input_width = t.input_width;
 }
 
+void DevicePass::set_tensor()
+{
+	if (sample != Sample::F32 || wide.frag)
+		return;
+	std::vector<uint4> frag;
+	std::vector<int> kbase;
+	int ksteps = 0;
+	build_wide_tables(table.f32.data(), table.left.data(), table.width, table.rows, &frag, &kbase, &ksteps);
+	const size_t fbytes = frag.size() * sizeof(uint4);
+	const size_t kbytes = kbase.size() * sizeof(int);
+	wide_storage.reset(fbytes + kbytes);
+	unsigned char *base = static_cast<unsigned char *>(wide_storage.get());
+	cuda_check(cudaMemcpy(base, frag.data(), fbytes, cudaMemcpyHostToDevice), "upload band fragments");
+	cuda_check(cudaMemcpy(base + fbytes, kbase.data(), kbytes, cudaMemcpyHostToDevice), "upload band fragments");
+	wide.frag = reinterpret_cast<const uint4 *>(base);
+	wide.kbase = reinterpret_cast<const int *>(base + fbytes);
+	wide.groups = static_cast<int>(kbase.size());
+	wide.ksteps = ksteps;
+}
+
 std::unique_ptr<DevicePass> make_device_pass(const PassSpec &s)
 {
 	if (!s.src_w || !s.src_h || !s.dst_dim)
@@ -130,6 +150,7 @@ void run_pass(const DevicePass &p, const void *src, ptrdiff_t ss, void *dst, ptr
 	l.src_stride = ss;
 	l.dst = dst;
 	l.dst_stride = ds;
+	l.wide = p.wide;
 	cuda_check(launch_pass(l, stream), "resize pass launch");
 }
 
@@ -315,6 +336,15 @@ zg_error_code zg_resize_create(const zg_resize_params *params, zg_resize **out)
 				r->tmp_size = 0;
 			}
 		}
+		if (!r->fused && r->sample == Sample::F32 && q.engine != ZG_ENGINE_CUDA) {
+			// unfused FP32 passes: wide filters (or an explicit request) on the tensor cores
+			for (int p = 0; p < r->num_passes; ++p) {
+				if (q.engine == ZG_ENGINE_TENSOR || r->pass[p]->table.width >= kWideTaps) {
+					r->pass[p]->set_tensor();
+					r->tensor_passes = true;
+				}
+			}
+		}
 		*out = r.release();
 	});
 }
@@ -340,7 +370,7 @@ zg_error_code zg_resize_get_info(const zg_resize *r, int *num_passes, int *first
 			throw Error(kErrIllegalArgument, "null pointer");
 		if (num_passes) *num_passes = r->num_passes;
 		if (first_horizontal) *first_horizontal = r->first_horizontal;
-		if (fused) *fused = r->fused ? (r->fplan.mma ? 2 : 1) : 0;
+		if (fused) *fused = r->fused ? (r->fplan.mma ? 2 : 1) : (r->tensor_passes ? 3 : 0);
 	});
 }
 

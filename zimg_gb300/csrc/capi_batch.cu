@@ -7,6 +7,7 @@
 #include "capi_common.h"
 
 #include <algorithm>
+#include <cstring>
 #include <map>
 
 using namespace zg;
@@ -74,6 +75,81 @@ void batch_launch(const zg_batch *b, void *tmp, cudaStream_t st)
 	}
 }
 
+// Tmp offsets, fused work segmentation and the persistent launch groups
+// (fused jobs grouped by kernel variant, in job order within a group).
+void regroup(zg_batch *b)
+{
+	const unsigned num_jobs = static_cast<unsigned>(b->jobs.size());
+	b->tmp_offset.clear();
+	b->tmp_size = 0;
+	for (unsigned i = 0; i < num_jobs; ++i) {
+		b->tmp_offset.push_back(b->tmp_size);
+		if (!b->jobs[i]->fused)
+			b->tmp_size += (b->jobs[i]->tmp_size + 255) & ~static_cast<size_t>(255);
+	}
+	b->groups.clear();
+	b->table_host.clear();
+	b->table_dev.release();
+	// one wave of work items across the whole batch: split strips into row
+	// segments only as far as needed to fill the GPU
+	std::vector<FusedPlan *> all;
+	for (unsigned i = 0; i < num_jobs; ++i)
+		if (b->jobs[i]->fused)
+			all.push_back(&b->jobs[i]->fplan);
+	if (!all.empty())
+		fused_segment(all.data(), static_cast<int>(all.size()), fused_wave_items());
+
+	// group fused jobs by variant, in job order within a group
+	std::map<int, std::vector<unsigned>> by_variant;
+	for (unsigned i = 0; i < num_jobs; ++i)
+		if (b->jobs[i]->fused)
+			by_variant[b->jobs[i]->fplan.variant].push_back(i);
+	b->table_index.assign(num_jobs, -1);
+	for (auto &kv : by_variant) {
+		zg_batch::Group g{ kv.first, SmemLayout{}, 0, static_cast<int>(b->table_host.size()), 0, 0 };
+		std::vector<const FusedPlan *> plans;
+		for (unsigned i : kv.second) {
+			FusedJob j = b->jobs[i]->fplan.job;
+			j.item_begin = g.tiles;
+			g.tiles += fused_items(j);
+			plans.push_back(&b->jobs[i]->fplan);
+			b->table_index[i] = static_cast<int>(b->table_host.size());
+			b->table_host.push_back(j);
+			++g.count;
+		}
+		g.layout = fused_layout(plans.data(), static_cast<int>(plans.size()));
+		g.grid = fused_grid_size(g.variant, static_cast<size_t>(g.layout.total_bytes));
+		b->groups.push_back(g);
+	}
+	if (!b->table_host.empty())
+		b->table_dev.reset(b->table_host.size() * sizeof(FusedJob));
+}
+
+// Plane pointers of the fused jobs into the device table (ordered on st; the
+// host copy stays valid until the next upload, which waits for this one).
+void upload_io(zg_batch *b, cudaStream_t st)
+{
+	for (size_t i = 0; i < b->jobs.size(); ++i) {
+		if (b->table_index[i] >= 0) {
+			const zg_batch_io &x = b->io[i];
+			fused_set_io(b->table_host[b->table_index[i]], x.src, x.src_stride, x.dst, x.dst_stride);
+		}
+	}
+	if (!b->table_host.empty()) {
+		cuda_check(cudaMemcpyAsync(b->table_dev.get(), b->table_host.data(), b->table_host.size() * sizeof(FusedJob),
+		                           cudaMemcpyHostToDevice, st), "batch io upload");
+		cuda_check(cudaStreamSynchronize(st), "batch io upload");
+	}
+}
+
+// How a conversion runs, for the autotuner's de-duplication of candidates.
+int plan_mode(const zg_resize *r)
+{
+	if (r->num_passes == 0)
+		return -1;
+	return r->fused ? (r->fplan.mma ? 2 : 1) : (r->tensor_passes ? 3 : 0);
+}
+
 } // namespace
 
 extern "C" {
@@ -92,44 +168,9 @@ zg_error_code zg_batch_create(const zg_resize_params *jobs, unsigned num_jobs, z
 			if (rc != ZG_ERROR_SUCCESS)
 				rethrow_last(rc);
 			b->jobs.push_back(r);
-			b->tmp_offset.push_back(b->tmp_size);
-			if (!r->fused)
-				b->tmp_size += (r->tmp_size + 255) & ~static_cast<size_t>(255);
 		}
 
-		// one wave of work items across the whole batch: split strips into row
-		// segments only as far as needed to fill the GPU
-		std::vector<FusedPlan *> all;
-		for (unsigned i = 0; i < num_jobs; ++i)
-			if (b->jobs[i]->fused)
-				all.push_back(&b->jobs[i]->fplan);
-		if (!all.empty())
-			fused_segment(all.data(), static_cast<int>(all.size()), fused_wave_items());
-
-		// group fused jobs by variant, in job order within a group
-		std::map<int, std::vector<unsigned>> by_variant;
-		for (unsigned i = 0; i < num_jobs; ++i)
-			if (b->jobs[i]->fused)
-				by_variant[b->jobs[i]->fplan.variant].push_back(i);
-		b->table_index.assign(num_jobs, -1);
-		for (auto &kv : by_variant) {
-			zg_batch::Group g{ kv.first, SmemLayout{}, 0, static_cast<int>(b->table_host.size()), 0, 0 };
-			std::vector<const FusedPlan *> plans;
-			for (unsigned i : kv.second) {
-				FusedJob j = b->jobs[i]->fplan.job;
-				j.item_begin = g.tiles;
-				g.tiles += fused_items(j);
-				plans.push_back(&b->jobs[i]->fplan);
-				b->table_index[i] = static_cast<int>(b->table_host.size());
-				b->table_host.push_back(j);
-				++g.count;
-			}
-			g.layout = fused_layout(plans.data(), static_cast<int>(plans.size()));
-			g.grid = fused_grid_size(g.variant, static_cast<size_t>(g.layout.total_bytes));
-			b->groups.push_back(g);
-		}
-		if (!b->table_host.empty())
-			b->table_dev.reset(b->table_host.size() * sizeof(FusedJob));
+		regroup(b.get());
 		*out = b.release();
 	});
 }
@@ -166,19 +207,9 @@ zg_error_code zg_batch_set_io(zg_batch *b, const zg_batch_io *io, zg_stream stre
 			if (reinterpret_cast<uintptr_t>(io[i].src) % bpe || reinterpret_cast<uintptr_t>(io[i].dst) % bpe ||
 			    io[i].src_stride % bpe || io[i].dst_stride % bpe)
 				throw Error(kErrIllegalArgument, "batch io not aligned to the sample size");
-			if (b->table_index[i] >= 0)
-				fused_set_io(b->table_host[b->table_index[i]], io[i].src, io[i].src_stride, io[i].dst,
-				             io[i].dst_stride);
 		}
 		b->io.assign(io, io + b->jobs.size());
-		if (!b->table_host.empty()) {
-			// Ordered with earlier work on this stream; the host copy stays
-			// valid until the next set_io, which waits for this copy first.
-			cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-			cuda_check(cudaMemcpyAsync(b->table_dev.get(), b->table_host.data(), b->table_host.size() * sizeof(FusedJob),
-			                           cudaMemcpyHostToDevice, st), "batch io upload");
-			cuda_check(cudaStreamSynchronize(st), "batch io upload");
-		}
+		upload_io(b, reinterpret_cast<cudaStream_t>(stream));
 		if (b->graph) {
 			cudaGraphExecDestroy(b->graph);
 			b->graph = nullptr;
@@ -232,6 +263,137 @@ zg_error_code zg_batch_process_graph(zg_batch *b, void *tmp, zg_stream stream)
 			b->graph_tmp = tmp;
 		}
 		cuda_check(cudaGraphLaunch(b->graph, st), "graph launch");
+	});
+}
+
+zg_error_code zg_batch_autotune(zg_batch *b, zg_stream stream, unsigned *changed)
+{
+	return guarded([&] {
+		if (!b)
+			throw Error(kErrIllegalArgument, "null pointer");
+		if (b->io.size() != b->jobs.size())
+			throw Error(kErrLogic, "zg_batch_set_io was not called");
+		if (current_device() != b->device)
+			throw Error(kErrLogic, "batch used on a different device than the one it was created on");
+		cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+		unsigned n_changed = 0;
+
+		// jobs with identical parameters are tuned once, on up to kSample of their planes
+		constexpr size_t kSample = 8;
+		constexpr int kReps = 3;
+		std::vector<bool> done(b->jobs.size(), false);
+		for (size_t i = 0; i < b->jobs.size(); ++i) {
+			if (done[i])
+				continue;
+			const zg_resize_params &q = b->jobs[i]->params;
+			std::vector<size_t> same;
+			for (size_t j = i; j < b->jobs.size(); ++j) {
+				if (!done[j] && std::memcmp(&b->jobs[j]->params, &q, sizeof(q)) == 0) {
+					same.push_back(j);
+					done[j] = true;
+				}
+			}
+			if (q.engine != ZG_ENGINE_AUTO || !q.allow_fusion || plan_mode(b->jobs[i]) < 0)
+				continue;
+
+			// candidates: every distinct way the planner can run this conversion
+			struct Cand {
+				zg_resize *r;
+				float ms;
+			};
+			std::vector<Cand> cands;
+			const zg_engine engines[3] = { ZG_ENGINE_CUDA, ZG_ENGINE_CUDA, ZG_ENGINE_TENSOR };
+			const int fusion[3] = { 1, 0, 1 };
+			for (int c = 0; c < 3; ++c) {
+				zg_resize_params p = q;
+				p.engine = engines[c];
+				p.allow_fusion = fusion[c];
+				zg_resize *r = nullptr;
+				if (zg_error_code rc = zg_resize_create(&p, &r))
+					rethrow_last(rc);
+				bool dup = false;
+				for (const Cand &x : cands)
+					dup = dup || plan_mode(x.r) == plan_mode(r);
+				if (dup)
+					zg_resize_free(r);
+				else
+					cands.push_back({ r, 0.0f });
+			}
+			auto free_cands = [&](zg_resize *keep) {
+				for (Cand &x : cands)
+					if (x.r != keep)
+						zg_resize_free(x.r);
+			};
+			if (cands.size() < 2) {
+				free_cands(nullptr);
+				continue;
+			}
+			try {
+				size_t tmp_bytes = 0;
+				for (const Cand &x : cands)
+					tmp_bytes = std::max(tmp_bytes, x.r->tmp_size);
+				DeviceBuffer tmp(tmp_bytes);
+				cudaEvent_t e0 = nullptr, e1 = nullptr;
+				cuda_check(cudaEventCreate(&e0), "event");
+				cuda_check(cudaEventCreate(&e1), "event");
+				const size_t n = std::min(same.size(), kSample);
+				for (Cand &x : cands) {
+					auto run = [&] {
+						for (size_t s = 0; s < n; ++s) {
+							const zg_batch_io &io = b->io[same[s]];
+							if (zg_error_code rc = zg_resize_process(x.r, io.src, io.src_stride, io.dst, io.dst_stride,
+							                                         tmp.get(), stream))
+								rethrow_last(rc);
+						}
+					};
+					run();  // warm-up
+					x.ms = 1e30f;
+					for (int rep = 0; rep < kReps; ++rep) {
+						cuda_check(cudaEventRecord(e0, st), "event");
+						run();
+						cuda_check(cudaEventRecord(e1, st), "event");
+						cuda_check(cudaEventSynchronize(e1), "event");
+						float ms = 0.0f;
+						cuda_check(cudaEventElapsedTime(&ms, e0, e1), "event");
+						x.ms = std::min(x.ms, ms);
+					}
+				}
+				cudaEventDestroy(e0);
+				cudaEventDestroy(e1);
+			} catch (...) {
+				free_cands(nullptr);
+				throw;
+			}
+			size_t best = 0;
+			for (size_t c = 1; c < cands.size(); ++c)
+				if (cands[c].ms < cands[best].ms)
+					best = c;
+			if (plan_mode(cands[best].r) == plan_mode(b->jobs[i])) {
+				free_cands(nullptr);
+				continue;
+			}
+			// the winner's parameters for every job of this kind
+			const zg_resize_params chosen = cands[best].r->params;
+			free_cands(nullptr);
+			for (size_t j : same) {
+				zg_resize *r = nullptr;
+				if (zg_error_code rc = zg_resize_create(&chosen, &r))
+					rethrow_last(rc);
+				zg_resize_free(b->jobs[j]);
+				b->jobs[j] = r;
+				++n_changed;
+			}
+		}
+		if (n_changed) {
+			regroup(b);
+			upload_io(b, st);
+			if (b->graph) {
+				cudaGraphExecDestroy(b->graph);
+				b->graph = nullptr;
+			}
+		}
+		if (changed)
+			*changed = n_changed;
 	});
 }
 

@@ -90,9 +90,17 @@ struct DevicePass {
 	Sample sample = Sample::F32;
 	int32_t pixel_max = 0;
 	unsigned src_w = 0, src_h = 0, dst_w = 0, dst_h = 0;
+	// FP32 only: band fragments for the tensor-core kernel (set_tensor)
+	DeviceBuffer wide_storage;
+	WideTables wide{};
 
 	void upload();
+	void set_tensor();
 };
+
+// FP32 passes with at least this many taps run on the tensor cores under
+// ZG_ENGINE_AUTO when they are not fused.
+constexpr unsigned kWideTaps = 32;
 
 struct PassSpec {
 	unsigned src_w, src_h;
@@ -125,6 +133,7 @@ struct zg_resize {
 	int num_passes = 0;
 	bool first_horizontal = false;
 	bool fused = false;
+	bool tensor_passes = false;  // separate passes, at least one on the tensor cores
 	std::unique_ptr<zg::DevicePass> pass[2];
 	ptrdiff_t tmp_stride = 0;
 	size_t tmp_size = 0;

@@ -143,6 +143,7 @@ SmemLayout mma_layout(const FusedPlan *const *plans, int n);
 cudaError_t launch_mma(int variant, const FusedJob *jobs, int num_jobs, int total_items, const SmemLayout &L, int grid,
                        const FusedJob &single, cudaStream_t stream);
 const void *mma_kernel_ptr(int variant);
+int mma_threads();
 // Work items that fill the current device once (SMs x resident CTAs).
 int fused_wave_items();
 

@@ -3,6 +3,8 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <vector>
+
 #include <cuda_runtime.h>
 
 namespace zg {
@@ -26,6 +28,22 @@ struct PassTables {
 
 enum class Sample { U16, F32 };
 
+// Band fragments of one FP32 pass for the tensor-core kernel (wide_kernel.cu).
+// Outputs are taken 8 at a time ("output groups"); group g covers outputs
+// 8g..8g+7 and the inputs [kbase[g], kbase[g] + 8 * ksteps), over which its
+// taps form a dense 8 x (8 * ksteps) block (zero outside each output's band).
+// frag[(g * ksteps + s) * 32 + lane] holds the mma.m16n8k8 B fragment of
+// k-step s for that lane, both tf32 halves of each f32 tap:
+//   {b0 high, b1 high, b0 low, b1 low},  b0 = tap(8g + lane/4, kbase + 8s + lane%4),
+//   b1 = the same 4 inputs further; high = tap rounded to tf32,
+//   low = (tap - high) rounded to tf32.
+struct WideTables {
+	const uint4 *frag;     // null: the pass runs on the CUDA cores
+	const int *kbase;
+	int groups;
+	int ksteps;
+};
+
 // One pass over a whole plane. For a horizontal pass the plane has
 // `lines` rows of input_width samples -> rows outputs each; for a vertical
 // pass it has `lines` columns, input_width rows -> rows rows.
@@ -39,7 +57,15 @@ struct PassLaunch {
 	ptrdiff_t src_stride;  // bytes
 	void *dst;
 	ptrdiff_t dst_stride;  // bytes
+	WideTables wide;       // FP32 passes on the tensor cores when wide.frag is set
 };
+
+// Host side of WideTables: fragments and group bases of a pass with `rows`
+// outputs of `width` taps (f32[i * width + k] applies to input left[i] + k).
+void build_wide_tables(const float *f32, const unsigned *left, unsigned width, unsigned rows,
+                       std::vector<uint4> *frag, std::vector<int> *kbase, int *ksteps);
+
+cudaError_t launch_wide(const PassLaunch &l, cudaStream_t stream);
 
 cudaError_t launch_pass(const PassLaunch &l, cudaStream_t stream);
 

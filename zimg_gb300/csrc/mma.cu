@@ -375,6 +375,11 @@ const void *mma_kernel_ptr(int variant)
 	return hf ? mma_ptr_kv<true>(kv, kh) : mma_ptr_kv<false>(kv, kh);
 }
 
+int mma_threads()
+{
+	return mma_detail::kThreads;
+}
+
 cudaError_t launch_mma(int variant, const FusedJob *jobs, int num_jobs, int total_items, const SmemLayout &L, int grid,
                        const FusedJob &single, cudaStream_t stream)
 {
@@ -388,7 +393,7 @@ cudaError_t launch_mma(int variant, const FusedJob *jobs, int num_jobs, int tota
 	SmemLayout layout = L;
 	void *args[] = { &jobs, &num_jobs, &total_items, &one, &layout };
 	grid = std::max(1, std::min(grid, total_items));
-	return cudaLaunchKernel(k, dim3(grid), dim3(kStreamThreads), args, static_cast<size_t>(L.total_bytes), stream);
+	return cudaLaunchKernel(k, dim3(grid), dim3(mma_detail::kThreads), args, static_cast<size_t>(L.total_bytes), stream);
 }
 
 } // namespace zg

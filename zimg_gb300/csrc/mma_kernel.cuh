@@ -27,7 +27,7 @@
 namespace zg {
 namespace mma_detail {
 
-constexpr int kThreads = kStreamThreads;  // 4 warps
+constexpr int kThreads = 256;             // 8 warps
 constexpr int kWarps = kThreads / 32;
 constexpr int kMidPitch = kStripW + 8;    // halfs per intermediate line (272 bytes)
 
@@ -78,8 +78,8 @@ __device__ __forceinline__ uint32_t pack_u16x2(float acc0, float acc1, float mag
 	const float y1 = __fmaf_rd(acc1, 6.103515625e-05f, magic);
 	// low 16 bits of y are the signed sample before clamping
 	uint32_t q = __byte_perm(__float_as_uint(y0), __float_as_uint(y1), 0x5410);
-	q = __vmaxs2(q, 0u);
-	q = __vmins2(q, pmax2);
+	asm("max.s16x2 %0, %0, %1;" : "+r"(q) : "r"(0u));
+	asm("min.s16x2 %0, %0, %1;" : "+r"(q) : "r"(pmax2));
 	return q;
 }
 
@@ -337,10 +337,10 @@ __device__ __forceinline__ void v_pass(const Item &it, const uint4 *afrag, const
 // destination rows r0.., strip columns, 16-byte stores where whole.
 __device__ __forceinline__ void store_tile(const Item &it, const char *tile, int out_pitch, int r0, int nrows)
 {
-	const int per_row = it.sw / 8;
+	const int shift = it.sw == 128 ? 4 : 3;  // chunks of 8 columns per row: 16 or 8
 	const int rows = min(nrows, it.dst_h - r0);
-	for (int i = threadIdx.x; i < rows * per_row; i += kThreads) {
-		const int r = i / per_row, q = i - r * per_row;
+	for (int i = threadIdx.x; i < (rows << shift); i += kThreads) {
+		const int r = i >> shift, q = i & ((1 << shift) - 1);
 		const int col = q * 8;
 		if (col >= it.cols_valid)
 			continue;
@@ -375,7 +375,7 @@ __device__ __forceinline__ void wait_groups(int pending)
 // column-group bases and group bases. Lines of step k + depth are in flight
 // while step k computes.
 template <bool H_FIRST, int KV, int KH>
-__global__ void __launch_bounds__(kThreads, 4)
+__global__ void __launch_bounds__(kThreads, 3)
 mma_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, const __grid_constant__ FusedJob single,
            const __grid_constant__ SmemLayout L)
 {

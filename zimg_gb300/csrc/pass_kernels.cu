@@ -185,6 +185,8 @@ bool aligned16(const void *p, ptrdiff_t stride)
 
 cudaError_t launch_pass(const PassLaunch &l, cudaStream_t stream)
 {
+	if (l.wide.frag && l.sample == Sample::F32)
+		return launch_wide(l, stream);
 	const uint8_t *src = static_cast<const uint8_t *>(l.src);
 	uint8_t *dst = static_cast<uint8_t *>(l.dst);
 	if (l.horizontal) {

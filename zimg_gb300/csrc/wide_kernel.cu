@@ -1,0 +1,225 @@
+// FP32 resize passes with wide filters (strong downscales: tens to hundreds
+// of taps per output) as banded matrix products on the tensor cores.
+//
+// One pass computes out[o][m] = sum_k tap(o, k) * in[k][m] for every output
+// o along the filtered axis and every m across it (m = column for a vertical
+// pass, row for a horizontal one). Outputs are taken 8 at a time; over the
+// inputs its 8 outputs touch, a group's taps form a dense 8 x K block, so the
+// pass is a sequence of small GEMMs D[16 m][8 o] += A[16 m][8 k] * B[8 k][8 o]
+// (mma.sync m16n8k8, tf32 operands, fp32 accumulation).
+//
+// Precision (3xTF32): every f32 operand x is split into x_hi = tf32(x) and
+// x_lo = tf32(x - x_hi); each product is a_hi*b_hi + a_hi*b_lo + a_lo*b_hi,
+// which keeps about 21 significant bits of every tap * sample product. The
+// taps are zimg's f32 taps (filter.cpp:43-127), so the kernel approximates
+// the same sums as the C path's resize_line_{h,v}_f32_c
+// (resize_impl.cpp:61-114), summed in a different order.
+//
+// Fragment layouts follow the PTX ISA description of mma.m16n8k8 (.tf32):
+// groupID = lane >> 2, tig = lane & 3;
+//   A: a0 (gid, tig), a1 (gid + 8, tig), a2 (gid, tig + 4), a3 (gid + 8, tig + 4)
+//   B: b0 (k = tig, n = gid), b1 (k = tig + 4, n = gid)
+//   D: d0 (gid, 2 tig), d1 (gid, 2 tig + 1), d2 (gid + 8, 2 tig), d3 (gid + 8, 2 tig + 1)
+//
+// Inputs of a group's block that lie outside an output's band get zero taps;
+// they are still read (clamped to the plane), so a non-finite sample within
+// a group's block reaches the group's other outputs as NaN.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "kernels.h"
+
+namespace zg {
+
+namespace {
+
+constexpr int kWideWarps = 4;
+
+__device__ __forceinline__ uint32_t tf32_rna(float x)
+{
+	uint32_t r;
+	asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+	return r;
+}
+
+__device__ __forceinline__ void mma_tf32(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                         uint32_t b0, uint32_t b1)
+{
+	asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, "
+	             "{%8, %9}, {%0, %1, %2, %3};\n"
+	             : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+	             : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+// One k-step: 4 samples of this lane -> split -> three products.
+__device__ __forceinline__ void step3(float (&d)[4], float x0, float x1, float x2, float x3, const uint4 &b)
+{
+	const uint32_t h0 = tf32_rna(x0), h1 = tf32_rna(x1), h2 = tf32_rna(x2), h3 = tf32_rna(x3);
+	const uint32_t l0 = tf32_rna(x0 - __uint_as_float(h0));
+	const uint32_t l1 = tf32_rna(x1 - __uint_as_float(h1));
+	const uint32_t l2 = tf32_rna(x2 - __uint_as_float(h2));
+	const uint32_t l3 = tf32_rna(x3 - __uint_as_float(h3));
+	mma_tf32(d, l0, l1, l2, l3, b.x, b.y);
+	mma_tf32(d, h0, h1, h2, h3, b.z, b.w);
+	mma_tf32(d, h0, h1, h2, h3, b.x, b.y);
+}
+
+// Element (m, k) of the input is at src + m * sm + k * sk (bytes); output
+// (o, m) at dst + m * dm + o * dko. A warp owns 16 consecutive m and walks
+// output groups [g0, g1).
+__global__ void __launch_bounds__(kWideWarps * 32)
+wide_tc_kernel(WideTables w, int m_extent, int src_dim, int dst_dim, const char *__restrict__ src, ptrdiff_t sm,
+               ptrdiff_t sk, char *__restrict__ dst, ptrdiff_t dm, ptrdiff_t dko, int groups_per_block)
+{
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	const int gid = lane >> 2, tig = lane & 3;
+	const int m0 = (blockIdx.x * kWideWarps + warp) * 16;
+	if (m0 >= m_extent)
+		return;
+	const int ma = min(m0 + gid, m_extent - 1), mb = min(m0 + gid + 8, m_extent - 1);
+	const int g0 = blockIdx.y * groups_per_block;
+	const int g1 = min(w.groups, g0 + groups_per_block);
+	const int KS = w.ksteps;
+	const char *base_a = src + ma * sm, *base_b = src + mb * sm;
+
+	for (int g = g0; g < g1; ++g) {
+		const int kb = __ldg(w.kbase + g);
+		const uint4 *bf = w.frag + static_cast<size_t>(g) * KS * 32 + lane;
+		float d[4] = { 0.f, 0.f, 0.f, 0.f };
+		if (kb + 8 * KS <= src_dim) {
+			const char *pa = base_a + (kb + tig) * sk, *pb = base_b + (kb + tig) * sk;
+			const ptrdiff_t s4 = 4 * sk, s8 = 8 * sk;
+			int s = 0;
+			for (; s + 4 <= KS; s += 4) {
+				float x[4][4];
+				uint4 b[4];
+#pragma unroll
+				for (int u = 0; u < 4; ++u) {
+					x[u][0] = __ldg(reinterpret_cast<const float *>(pa + u * s8));
+					x[u][1] = __ldg(reinterpret_cast<const float *>(pb + u * s8));
+					x[u][2] = __ldg(reinterpret_cast<const float *>(pa + u * s8 + s4));
+					x[u][3] = __ldg(reinterpret_cast<const float *>(pb + u * s8 + s4));
+					b[u] = __ldg(bf + (s + u) * 32);
+				}
+#pragma unroll
+				for (int u = 0; u < 4; ++u)
+					step3(d, x[u][0], x[u][1], x[u][2], x[u][3], b[u]);
+				pa += 4 * s8;
+				pb += 4 * s8;
+			}
+			for (; s < KS; ++s) {
+				const float x0 = __ldg(reinterpret_cast<const float *>(pa));
+				const float x1 = __ldg(reinterpret_cast<const float *>(pb));
+				const float x2 = __ldg(reinterpret_cast<const float *>(pa + s4));
+				const float x3 = __ldg(reinterpret_cast<const float *>(pb + s4));
+				step3(d, x0, x1, x2, x3, __ldg(bf + s * 32));
+				pa += s8;
+				pb += s8;
+			}
+		} else {
+			// the block reaches past the last input: clamp (those taps are zero)
+			const int kmax = src_dim - 1;
+			for (int s = 0; s < KS; ++s) {
+				const int k0 = min(kb + 8 * s + tig, kmax), k1 = min(kb + 8 * s + tig + 4, kmax);
+				const float x0 = __ldg(reinterpret_cast<const float *>(base_a + k0 * sk));
+				const float x1 = __ldg(reinterpret_cast<const float *>(base_b + k0 * sk));
+				const float x2 = __ldg(reinterpret_cast<const float *>(base_a + k1 * sk));
+				const float x3 = __ldg(reinterpret_cast<const float *>(base_b + k1 * sk));
+				step3(d, x0, x1, x2, x3, __ldg(bf + s * 32));
+			}
+		}
+		const int o = g * 8 + 2 * tig;
+		const int mA = m0 + gid, mB = m0 + gid + 8;
+		if (o < dst_dim) {
+			if (mA < m_extent) *reinterpret_cast<float *>(dst + mA * dm + o * dko) = d[0];
+			if (mB < m_extent) *reinterpret_cast<float *>(dst + mB * dm + o * dko) = d[2];
+		}
+		if (o + 1 < dst_dim) {
+			if (mA < m_extent) *reinterpret_cast<float *>(dst + mA * dm + (o + 1) * dko) = d[1];
+			if (mB < m_extent) *reinterpret_cast<float *>(dst + mB * dm + (o + 1) * dko) = d[3];
+		}
+	}
+}
+
+// Round an f32 to the nearest tf32 (ties away from zero), as cvt.rna.tf32.f32.
+float tf32_round(float x)
+{
+	uint32_t u;
+	std::memcpy(&u, &x, 4);
+	if ((u & 0x7F800000u) != 0x7F800000u) {
+		u += 0x1000u;
+		u &= ~0x1FFFu;
+	}
+	float r;
+	std::memcpy(&r, &u, 4);
+	return r;
+}
+
+uint32_t bits(float x)
+{
+	uint32_t u;
+	std::memcpy(&u, &x, 4);
+	return u;
+}
+
+} // namespace
+
+void build_wide_tables(const float *f32, const unsigned *left, unsigned width, unsigned rows,
+                       std::vector<uint4> *frag, std::vector<int> *kbase, int *ksteps)
+{
+	const int groups = static_cast<int>((rows + 7) / 8);
+	kbase->assign(groups, 0);
+	int ks = 1;
+	for (int g = 0; g < groups; ++g) {
+		unsigned lo = ~0u, hi = 0;
+		for (unsigned o = g * 8u; o < std::min(rows, g * 8u + 8); ++o) {
+			lo = std::min(lo, left[o]);
+			hi = std::max(hi, left[o] + width);
+		}
+		(*kbase)[g] = static_cast<int>(lo);
+		ks = std::max(ks, static_cast<int>((hi - lo + 7) / 8));
+	}
+	*ksteps = ks;
+	frag->assign(static_cast<size_t>(groups) * ks * 32, uint4{ 0, 0, 0, 0 });
+	auto tap = [&](unsigned o, long x) -> float {
+		if (o >= rows)
+			return 0.0f;
+		const long k = x - static_cast<long>(left[o]);
+		return (k >= 0 && k < static_cast<long>(width)) ? f32[static_cast<size_t>(o) * width + k] : 0.0f;
+	};
+	for (int g = 0; g < groups; ++g) {
+		for (int s = 0; s < ks; ++s) {
+			for (int lane = 0; lane < 32; ++lane) {
+				const unsigned o = g * 8u + (lane >> 2);
+				const long x = (*kbase)[g] + 8L * s + (lane & 3);
+				const float c0 = tap(o, x), c1 = tap(o, x + 4);
+				const float h0 = tf32_round(c0), h1 = tf32_round(c1);
+				const float l0 = tf32_round(c0 - h0), l1 = tf32_round(c1 - h1);
+				(*frag)[(static_cast<size_t>(g) * ks + s) * 32 + lane] = uint4{ bits(h0), bits(h1), bits(l0), bits(l1) };
+			}
+		}
+	}
+}
+
+cudaError_t launch_wide(const PassLaunch &l, cudaStream_t stream)
+{
+	const int m_extent = static_cast<int>(l.lines);
+	const int src_dim = static_cast<int>(l.t.input_width);
+	const int dst_dim = static_cast<int>(l.t.rows);
+	const ptrdiff_t sm = l.horizontal ? l.src_stride : 4, sk = l.horizontal ? 4 : l.src_stride;
+	const ptrdiff_t dm = l.horizontal ? l.dst_stride : 4, dko = l.horizontal ? 4 : l.dst_stride;
+	const int mtiles = (m_extent + 15) / 16;
+	const int bx = (mtiles + kWideWarps - 1) / kWideWarps;
+	// enough warps for several waves on every SM, then longer runs of groups
+	const long target = 152L * 64;
+	int gpb = static_cast<int>(std::max<long>(1, static_cast<long>(mtiles) * l.wide.groups / target));
+	gpb = std::max(std::min(gpb, 8), (l.wide.groups + 65534) / 65535);
+	const int by = (l.wide.groups + gpb - 1) / gpb;
+	wide_tc_kernel<<<dim3(bx, by), kWideWarps * 32, 0, stream>>>(l.wide, m_extent, src_dim, dst_dim,
+	                                                              static_cast<const char *>(l.src), sm, sk,
+	                                                              static_cast<char *>(l.dst), dm, dko, gpb);
+	return cudaGetLastError();
+}
+
+} // namespace zg

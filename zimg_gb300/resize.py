@@ -171,7 +171,7 @@ class Resize:
         n, f, fu = C.c_int(), C.c_int(), C.c_int()
         check(load().zg_resize_get_info(self._h, C.byref(n), C.byref(f), C.byref(fu)))
         return {"num_passes": n.value, "first_horizontal": bool(f.value), "fused": bool(fu.value),
-                "engine": {0: "passes", 1: "cuda", 2: "tensor"}[fu.value]}
+                "engine": {0: "passes", 1: "cuda", 2: "tensor", 3: "tensor-passes"}[fu.value]}
 
     def alloc_tmp(self, device=None):
         import torch
@@ -278,6 +278,15 @@ class Batch:
             dp, ds, _, _ = _plane(d)
             io[i] = capi.BatchIO(sp, ss, dp, ds)
         check(load().zg_batch_set_io(self._h, io, _stream_handle(stream)))
+
+    def autotune(self, stream=None) -> int:
+        """Time the planner's alternatives for every AUTO job on its bound
+        planes and keep the fastest (zg_batch_autotune). Returns the number of
+        jobs whose plan changed; the tmp size may change with them."""
+        n = C.c_uint()
+        check(load().zg_batch_autotune(self._h, _stream_handle(stream), C.byref(n)))
+        self._tmp = None
+        return n.value
 
     def _tmp_ptr(self, tmp):
         if tmp is None and self.tmp_size:
