@@ -317,6 +317,9 @@ zg_error_code zg_resize_create(const zg_resize_params *params, zg_resize **out)
 			const bool u16 = r->sample == Sample::U16;
 			bool planned = false;
 			if (q.allow_fusion && u16 && q.engine != ZG_ENGINE_CUDA)
+				planned = plan_chain(r->pass[0]->table, r->pass[1]->table, r->first_horizontal, q.depth, q.src_width,
+				                     q.src_height, q.dst_width, q.dst_height, &r->fplan);
+			if (!planned && q.allow_fusion && u16 && q.engine != ZG_ENGINE_CUDA)
 				planned = plan_mma(r->pass[0]->table, r->pass[1]->table, r->first_horizontal, q.depth, q.src_width,
 				                   q.src_height, q.dst_width, q.dst_height, &r->fplan);
 			if (!planned && q.allow_fusion && q.engine != ZG_ENGINE_TENSOR)

@@ -1,0 +1,377 @@
+// Tensor-core u16 kernel with the two passes chained in registers (exact).
+//
+// Arithmetic is that of mma_kernel.cuh (re-centred fp16 samples, int16 taps
+// split into two fp16 halves, fp32 accumulators that the planner proved hold
+// exact integers, zimg's rounding and clamping per pass,
+// resize_impl.cpp:31-42). The data flow differs: each warp owns 16 output
+// columns of a 128-column strip and, per group of 16 output rows, computes
+// both passes itself without shared memory in between:
+//
+//   H first:  Dh[16 out cols][8 lines]  = Ah[16 out cols][16 in cols] * src[in cols][lines]
+//             Dv[16 out rows][8 cols]   = Av[16 out rows][16 lines]   * Dh^T
+//   V first:  Dv[16 out rows][8 in cols] = Av * src[lines][in cols]
+//             Dh[16 out cols][8 rows]    = Ah * Dv^T
+//
+// The mma.m16n8k16 accumulator layout (row gid, columns 2tig, 2tig+1) is the
+// layout of the B operand of the next product (k = 2tig, 2tig+1, n = gid), so
+// the first product's rounded results, converted to centred fp16 pairs, are
+// the second product's B fragments as they stand. Source lines stream
+// through one ring of raw u16 lines per CTA (cp.async, prefetched `depth`
+// groups ahead, one barrier per group); results leave through a per-warp
+// staging tile (stmatrix) as 16-byte rows.
+#pragma once
+
+#include "mma_kernel.cuh"
+
+namespace zg {
+namespace chain_detail {
+
+using mma_detail::cp_async16;
+using mma_detail::cp_async_commit;
+using mma_detail::cp_async_wait;
+using mma_detail::find_job;
+using mma_detail::ldsm_x4_trans;
+using mma_detail::mma16816;
+using mma_detail::pack_u16x2;
+using mma_detail::u16x2_to_centred_h2;
+using mma_detail::wrap;
+
+constexpr int kWarps = 8;
+constexpr int kThreads = kWarps * 32;
+constexpr int kTileW = 16;                 // output columns per warp
+constexpr int kStageBytes = 48;            // staged row: 16 u16 + pad (stmatrix rows without bank conflicts)
+
+__device__ __forceinline__ void stsm_x4(void *p, uint32_t r0, uint32_t r1, uint32_t r2, uint32_t r3)
+{
+	const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(p));
+	asm volatile("stmatrix.sync.aligned.m8n8.x4.shared.b16 [%0], {%1, %2, %3, %4};\n" ::"r"(s), "r"(r0), "r"(r1),
+	             "r"(r2), "r"(r3)
+	             : "memory");
+}
+
+__device__ __forceinline__ void stsm_x4_trans(void *p, uint32_t r0, uint32_t r1, uint32_t r2, uint32_t r3)
+{
+	const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(p));
+	asm volatile("stmatrix.sync.aligned.m8n8.x4.trans.shared.b16 [%0], {%1, %2, %3, %4};\n" ::"r"(s), "r"(r0),
+	             "r"(r1), "r"(r2), "r"(r3)
+	             : "memory");
+}
+
+struct Item {
+	const char *src;
+	ptrdiff_t src_stride;
+	char *dst;
+	ptrdiff_t dst_stride;
+	int src_w, src_h, dst_w, dst_h, vec_ok;
+	int strip, c0, xlo;
+	int g_begin, g_end, depth;
+	// this thread's place in line copies: chunk q0 of line offset l0, then
+	// advance by (sl lines, sq chunks) per iteration
+	int chunks, q0, l0, sl, sq;
+	float magic;
+	uint32_t pmax2, bias_h2;
+};
+
+__device__ __forceinline__ Item make_item(const FusedJob &J, int t)
+{
+	Item it;
+	const int local = t - J.item_begin;
+	const int seg = local / J.strips;
+	it.strip = local - seg * J.strips;
+	it.src = static_cast<const char *>(J.src);
+	it.src_stride = J.src_stride;
+	it.dst = static_cast<char *>(J.dst);
+	it.dst_stride = J.dst_stride;
+	it.src_w = J.src_w;
+	it.src_h = J.src_h;
+	it.dst_w = J.dst_w;
+	it.dst_h = J.dst_h;
+	it.vec_ok = J.vec_ok;
+	it.c0 = it.strip * kWarps * kTileW;
+	it.xlo = __ldg(J.win_col + 2 * it.strip);
+	const int pxa = (__ldg(J.win_col + 2 * it.strip + 1) - it.xlo + 7) & ~7;
+	it.g_begin = seg * J.seg_groups;
+	it.g_end = min(J.groups, it.g_begin + J.seg_groups);
+	it.depth = J.depth;
+	it.magic = J.magic;
+	const uint32_t pm = static_cast<uint32_t>(J.pixel_max);
+	it.pmax2 = pm | (pm << 16);
+	const __half2 b = __floats2half2_rn(1024.0f + J.offset, 1024.0f + J.offset);
+	it.bias_h2 = *reinterpret_cast<const uint32_t *>(&b);
+	it.chunks = pxa / 8;
+	it.q0 = threadIdx.x % it.chunks;
+	it.l0 = threadIdx.x / it.chunks;
+	it.sl = kThreads / it.chunks;
+	it.sq = kThreads % it.chunks;
+	return it;
+}
+
+// Source lines [a, b) of the strip (raw u16, zeros outside the plane) into
+// ring slots; line a goes to slot sa.
+__device__ __forceinline__ void load_lines(const Item &it, int a, int b, char *ring, int R, int sa, int pitch_bytes)
+{
+	int y = a + it.l0, q = it.q0;
+	for (; y < b;) {
+		const bool row_ok = y < it.src_h;
+		const char *row = it.src + static_cast<ptrdiff_t>(row_ok ? y : 0) * it.src_stride;
+		char *srow = ring + wrap(sa + (y - a), R) * pitch_bytes;
+		const int gx = it.xlo + q * 8;
+		if (it.vec_ok) {
+			const int n = row_ok ? max(0, min(8, it.src_w - gx)) : 0;
+			cp_async16(srow + q * 16, n ? row + static_cast<ptrdiff_t>(gx) * 2 : it.src, n * 2);
+		} else {
+			uint16_t *d = reinterpret_cast<uint16_t *>(srow + q * 16);
+#pragma unroll
+			for (int e = 0; e < 8; ++e)
+				d[e] = (row_ok && gx + e < it.src_w) ? __ldg(reinterpret_cast<const uint16_t *>(row) + gx + e)
+				                                      : static_cast<uint16_t>(0);
+		}
+		q += it.sq;
+		y += it.sl;
+		if (q >= it.chunks) {
+			q -= it.chunks;
+			++y;
+		}
+	}
+}
+
+// Vertical tap fragments of group g into a shared slot.
+template <int KV>
+__device__ __forceinline__ void load_vfrag(const FusedJob &J, int g, char *slot)
+{
+	const char *src = reinterpret_cast<const char *>(J.v_dense) + static_cast<size_t>(g) * KV * 2 * 32 * 16;
+	for (int i = threadIdx.x; i < KV * 2 * 32; i += kThreads)
+		cp_async16(slot + i * 16, src + i * 16, 16);
+}
+
+__device__ __forceinline__ void wait_groups(int pending)
+{
+	// cp.async.wait_group takes an immediate
+	switch (pending) {
+	case 0: cp_async_wait<0>(); break;
+	case 1: cp_async_wait<1>(); break;
+	case 2: cp_async_wait<2>(); break;
+	case 3: cp_async_wait<3>(); break;
+	case 4: cp_async_wait<4>(); break;
+	case 5: cp_async_wait<5>(); break;
+	case 6: cp_async_wait<6>(); break;
+	case 7: cp_async_wait<7>(); break;
+	default: cp_async_wait<8>(); break;
+	}
+}
+
+__device__ __forceinline__ uint32_t centre(uint32_t q, uint32_t bias_h2)
+{
+	return u16x2_to_centred_h2(q, bias_h2);
+}
+
+__device__ __forceinline__ void mma_split(float (&d)[4], const uint4 &hi, const uint4 &lo, uint32_t b0, uint32_t b1)
+{
+	const uint32_t ah[4] = { hi.x, hi.y, hi.z, hi.w };
+	const uint32_t al[4] = { lo.x, lo.y, lo.z, lo.w };
+	mma16816(d, ah, b0, b1);
+	mma16816(d, al, b0, b1);
+}
+
+// Kernel. Shared memory (SmemLayout): ring of raw source lines (in_off,
+// in_rows x pitch), depth + 2 slots of vertical tap fragments (vcoef_off),
+// one 16-row staging tile per warp (tile_off), the segment's group bases
+// (vbase_off). A warp may still compute group k while others issue the loads
+// of group k + 1 + depth: the planner sizes the ring and the slots for that.
+template <bool H_FIRST, int KV, int KH>
+__global__ void __launch_bounds__(kThreads, 2)
+chain_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, const __grid_constant__ FusedJob single,
+             const __grid_constant__ SmemLayout L)
+{
+	extern __shared__ float4 smem4[];
+	char *smem = reinterpret_cast<char *>(smem4);
+	char *ring = smem + L.in_off;
+	char *vslots = smem + L.vcoef_off;
+	int *vb = reinterpret_cast<int *>(smem + L.vbase_off);
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	const int gid = lane >> 2, tig = lane & 3;
+	char *stage = smem + L.tile_off + warp * 16 * kStageBytes;
+	const int IR = L.in_rows;
+	const int P = L.pitch * 2;
+	constexpr int kSlotBytes = KV * 2 * 32 * 16;
+	// stmatrix / stage read addresses of this lane
+	char *st_addr = stage + (((lane >> 4) << 3) + (lane & 7)) * kStageBytes + ((lane >> 3) & 1) * 16;
+	const char *ld_addr = stage + (lane >> 1) * kStageBytes + (lane & 1) * 16;
+
+	// lines never written by a load still hold finite values
+	for (int i = threadIdx.x; i < L.in_rows * P / 16; i += kThreads)
+		reinterpret_cast<float4 *>(ring)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+	__syncthreads();
+
+	for (int t = blockIdx.x; t < total_items; t += gridDim.x) {
+		const FusedJob *Jp = jobs ? &jobs[find_job(jobs, num_jobs, t)] : &single;
+		const Item it = make_item(*Jp, t);
+		for (int g = it.g_begin + threadIdx.x; g < it.g_end; g += kThreads)
+			vb[g - it.g_begin] = __ldg(Jp->v_base + g);
+
+		// this warp's 16 output columns: horizontal tap fragments and window start
+		const int col0 = it.c0 + warp * kTileW;
+		const bool active = col0 < it.dst_w;
+		uint4 ah[KH][2];
+		int rel = 0;
+		{
+			const int tile = min(it.strip * kWarps + warp, (it.dst_w + kTileW - 1) / kTileW - 1);
+			const uint4 *hf = reinterpret_cast<const uint4 *>(Jp->h_taps) + static_cast<size_t>(tile) * KH * 2 * 32 + lane;
+#pragma unroll
+			for (int ks = 0; ks < KH; ++ks) {
+				ah[ks][0] = __ldg(hf + (ks * 2 + 0) * 32);
+				ah[ks][1] = __ldg(hf + (ks * 2 + 1) * 32);
+			}
+			rel = __ldg(Jp->h_left + tile) - it.xlo;
+		}
+		__syncthreads();
+
+		const int D = it.depth;
+		const int ngroups = it.g_end - it.g_begin;
+		const int nslots = D + 2;
+		// prologue: groups 0 .. D-1 in flight, one commit group each
+		int issued_hi = vb[0];
+		int issued_slot = wrap(vb[0] % IR, IR);
+		for (int k = 0; k < D; ++k) {
+			if (k < ngroups) {
+				const int hi = vb[k] + 16 * KV;
+				if (hi > issued_hi) {
+					load_lines(it, issued_hi, hi, ring, IR, issued_slot, P);
+					issued_slot = wrap(issued_slot + (hi - issued_hi), IR);
+					issued_hi = hi;
+				}
+				load_vfrag<KV>(*Jp, it.g_begin + k, vslots + k * kSlotBytes);
+			}
+			cp_async_commit();
+		}
+
+		int cur_vb = vb[0];
+		int cur_slot = wrap(cur_vb % IR, IR);
+		int fetch_slot = D % nslots, read_slot = 0;
+		for (int k = 0; k < ngroups; ++k) {
+			if (k + D < ngroups) {
+				const int hi = vb[k + D] + 16 * KV;
+				if (hi > issued_hi) {
+					load_lines(it, issued_hi, hi, ring, IR, issued_slot, P);
+					issued_slot = wrap(issued_slot + (hi - issued_hi), IR);
+					issued_hi = hi;
+				}
+				load_vfrag<KV>(*Jp, it.g_begin + k + D, vslots + fetch_slot * kSlotBytes);
+			}
+			cp_async_commit();
+			fetch_slot = fetch_slot + 1 == nslots ? 0 : fetch_slot + 1;
+			wait_groups(D);
+			__syncthreads();
+
+			const int vbk = vb[k];
+			cur_slot = wrap(cur_slot + (vbk - cur_vb), IR);
+			cur_vb = vbk;
+			if (active) {
+				const uint4 *avs = reinterpret_cast<const uint4 *>(vslots + read_slot * kSlotBytes) + lane;
+				uint4 av[KV][2];
+#pragma unroll
+				for (int kv = 0; kv < KV; ++kv) {
+					av[kv][0] = avs[(kv * 2 + 0) * 32];
+					av[kv][1] = avs[(kv * 2 + 1) * 32];
+				}
+				uint32_t m0, m1, m2, m3;
+				if (H_FIRST) {
+					// H over the group's KV*16 lines: B = src[line gid (+8)][in cols 2tig (+8)]
+					uint32_t bv[KV][2][2];
+#pragma unroll
+					for (int kv = 0; kv < KV; ++kv) {
+						float dh0[4] = { 8192.f, 8192.f, 8192.f, 8192.f };  // lines 0-7
+						float dh1[4] = { 8192.f, 8192.f, 8192.f, 8192.f };  // lines 8-15
+						const char *r0 = ring + wrap(cur_slot + 16 * kv + gid, IR) * P + (rel + 2 * tig) * 2;
+						const char *r1 = ring + wrap(cur_slot + 16 * kv + gid + 8, IR) * P + (rel + 2 * tig) * 2;
+#pragma unroll
+						for (int ks = 0; ks < KH; ++ks) {
+							const uint32_t b0 = centre(*reinterpret_cast<const uint32_t *>(r0 + ks * 32), it.bias_h2);
+							const uint32_t b1 = centre(*reinterpret_cast<const uint32_t *>(r0 + ks * 32 + 16), it.bias_h2);
+							const uint32_t b2 = centre(*reinterpret_cast<const uint32_t *>(r1 + ks * 32), it.bias_h2);
+							const uint32_t b3 = centre(*reinterpret_cast<const uint32_t *>(r1 + ks * 32 + 16), it.bias_h2);
+							mma_split(dh0, ah[ks][0], ah[ks][1], b0, b1);
+							mma_split(dh1, ah[ks][0], ah[ks][1], b2, b3);
+						}
+						// Dh (out col gid / gid+8, lines 2tig..) -> V operands (k = lines, n = out col)
+						bv[kv][0][0] = centre(pack_u16x2(dh0[0], dh0[1], it.magic, it.pmax2), it.bias_h2);
+						bv[kv][0][1] = centre(pack_u16x2(dh1[0], dh1[1], it.magic, it.pmax2), it.bias_h2);
+						bv[kv][1][0] = centre(pack_u16x2(dh0[2], dh0[3], it.magic, it.pmax2), it.bias_h2);
+						bv[kv][1][1] = centre(pack_u16x2(dh1[2], dh1[3], it.magic, it.pmax2), it.bias_h2);
+					}
+					float dv0[4] = { 8192.f, 8192.f, 8192.f, 8192.f };  // out cols 0-7
+					float dv1[4] = { 8192.f, 8192.f, 8192.f, 8192.f };  // out cols 8-15
+#pragma unroll
+					for (int kv = 0; kv < KV; ++kv) {
+						mma_split(dv0, av[kv][0], av[kv][1], bv[kv][0][0], bv[kv][0][1]);
+						mma_split(dv1, av[kv][0], av[kv][1], bv[kv][1][0], bv[kv][1][1]);
+					}
+					// (out row gid / gid+8, out cols 2tig..): row-major 8x8 blocks
+					m0 = pack_u16x2(dv0[0], dv0[1], it.magic, it.pmax2);
+					m1 = pack_u16x2(dv1[0], dv1[1], it.magic, it.pmax2);
+					m2 = pack_u16x2(dv0[2], dv0[3], it.magic, it.pmax2);
+					m3 = pack_u16x2(dv1[2], dv1[3], it.magic, it.pmax2);
+					stsm_x4(st_addr, m0, m1, m2, m3);
+				} else {
+					float dh0[4] = { 8192.f, 8192.f, 8192.f, 8192.f };  // out rows 0-7
+					float dh1[4] = { 8192.f, 8192.f, 8192.f, 8192.f };  // out rows 8-15
+					// ldmatrix.trans rows: line (lane & 7) + ((lane >> 3) & 1) * 8, column + (lane >> 4) * 8
+					const int krow = (lane & 7) + ((lane >> 3) & 1) * 8;
+					const int coff = (rel + (lane >> 4) * 8) * 2;
+#pragma unroll
+					for (int ks = 0; ks < KH; ++ks) {
+						float dv0[4] = { 8192.f, 8192.f, 8192.f, 8192.f };  // in cols 0-7 of this k-step
+						float dv1[4] = { 8192.f, 8192.f, 8192.f, 8192.f };  // in cols 8-15
+#pragma unroll
+						for (int kv = 0; kv < KV; ++kv) {
+							uint32_t b0, b1, b2, b3;
+							ldsm_x4_trans(b0, b1, b2, b3,
+							              ring + wrap(cur_slot + 16 * kv + krow, IR) * P + coff + ks * 32);
+							b0 = centre(b0, it.bias_h2);
+							b1 = centre(b1, it.bias_h2);
+							b2 = centre(b2, it.bias_h2);
+							b3 = centre(b3, it.bias_h2);
+							mma_split(dv0, av[kv][0], av[kv][1], b0, b1);
+							mma_split(dv1, av[kv][0], av[kv][1], b2, b3);
+						}
+						// Dv (out row gid / gid+8, in cols 2tig..) -> H operands (k = in cols, n = out row)
+						const uint32_t h00 = centre(pack_u16x2(dv0[0], dv0[1], it.magic, it.pmax2), it.bias_h2);
+						const uint32_t h01 = centre(pack_u16x2(dv1[0], dv1[1], it.magic, it.pmax2), it.bias_h2);
+						const uint32_t h10 = centre(pack_u16x2(dv0[2], dv0[3], it.magic, it.pmax2), it.bias_h2);
+						const uint32_t h11 = centre(pack_u16x2(dv1[2], dv1[3], it.magic, it.pmax2), it.bias_h2);
+						mma_split(dh0, ah[ks][0], ah[ks][1], h00, h01);
+						mma_split(dh1, ah[ks][0], ah[ks][1], h10, h11);
+					}
+					// (out col gid / gid+8, out rows 2tig..): transposed 8x8 blocks
+					m0 = pack_u16x2(dh0[0], dh0[1], it.magic, it.pmax2);
+					m1 = pack_u16x2(dh0[2], dh0[3], it.magic, it.pmax2);
+					m2 = pack_u16x2(dh1[0], dh1[1], it.magic, it.pmax2);
+					m3 = pack_u16x2(dh1[2], dh1[3], it.magic, it.pmax2);
+					stsm_x4_trans(st_addr, m0, m1, m2, m3);
+				}
+				__syncwarp();
+				// staged 16 x 16 tile -> destination, one 16-byte half row per lane
+				const int row = (it.g_begin + k) * 16 + (lane >> 1);
+				const int col = col0 + (lane & 1) * 8;
+				if (row < it.dst_h && col < it.dst_w) {
+					const uint4 v = *reinterpret_cast<const uint4 *>(ld_addr);
+					uint16_t *d = reinterpret_cast<uint16_t *>(it.dst + static_cast<ptrdiff_t>(row) * it.dst_stride) + col;
+					if (it.vec_ok && col + 8 <= it.dst_w) {
+						*reinterpret_cast<uint4 *>(d) = v;
+					} else {
+						const uint32_t w[4] = { v.x, v.y, v.z, v.w };
+						for (int e = 0; e < 8 && col + e < it.dst_w; ++e)
+							d[e] = static_cast<uint16_t>(w[e >> 1] >> (16 * (e & 1)));
+					}
+				}
+				__syncwarp();
+			}
+			read_slot = read_slot + 1 == nslots ? 0 : read_slot + 1;
+		}
+		cp_async_wait<0>();
+		__syncthreads();  // the next item rewrites the group bases and the ring
+	}
+}
+
+} // namespace chain_detail
+} // namespace zg

@@ -270,6 +270,8 @@ void split_variant(int variant, int *hf, int *u16, int *hw_i, int *vs_i)
 
 const void *kernel_ptr(int variant)
 {
+	if (variant >= 200)
+		return chain_kernel_ptr(variant);
 	if (variant >= 100)
 		return mma_kernel_ptr(variant);
 	int hf, u16, hw, vs;
@@ -283,6 +285,8 @@ const void *kernel_ptr(int variant)
 
 SmemLayout fused_layout(const FusedPlan *const *plans, int n)
 {
+	if (n > 0 && plans[0]->chain)
+		return chain_layout(plans, n);
 	if (n > 0 && plans[0]->mma)
 		return mma_layout(plans, n);
 	int max_pxa = 0, hw = 0, vs = 0, ring = 1, in = 1, stage = 1, seg_groups = 1, step_groups = 1;
@@ -341,7 +345,7 @@ int fused_grid_size(int variant, size_t smem_bytes)
 	cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
 	const void *k = kernel_ptr(variant);
 	cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kSmemMax));
-	const int threads = variant >= 100 ? mma_threads() : kStreamThreads;
+	const int threads = variant >= 200 ? chain_threads() : (variant >= 100 ? mma_threads() : kStreamThreads);
 	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, threads, smem_bytes) != cudaSuccess || per_sm < 1)
 		per_sm = 1;
 	return std::max(1, sms) * per_sm;
@@ -350,6 +354,8 @@ int fused_grid_size(int variant, size_t smem_bytes)
 cudaError_t launch_fused(int variant, const FusedJob *jobs, int num_jobs, int total_tiles, const SmemLayout &smem_bytes,
                          int grid, const FusedJob &single, cudaStream_t stream)
 {
+	if (variant >= 200)
+		return launch_chain(variant, jobs, num_jobs, total_tiles, smem_bytes, grid, single, stream);
 	if (variant >= 100)
 		return launch_mma(variant, jobs, num_jobs, total_tiles, smem_bytes, grid, single, stream);
 	int hf, u16, hw, vs;

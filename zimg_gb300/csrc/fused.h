@@ -98,7 +98,8 @@ struct FusedPlan {
 	int max_pxa = 0;         // widest strip patch (elements)
 	int stage_rows = 1;      // u16 raw staging lines
 	int depth = 1;           // prefetch depth in steps
-	bool mma = false;        // tensor-core variant (mma_kernel.cuh)
+	bool mma = false;        // tensor-core variant (mma_kernel.cuh or chain_kernel.cuh)
+	bool chain = false;      // tensor-core variant with the passes chained in registers (chain_kernel.cuh)
 	std::vector<unsigned char> blob;  // host copy of the tables, uploaded by the owner
 	size_t off_h_taps = 0, off_h_left = 0, off_v_dense = 0, off_v_base = 0, off_win_col = 0;
 };
@@ -144,6 +145,17 @@ cudaError_t launch_mma(int variant, const FusedJob *jobs, int num_jobs, int tota
                        const FusedJob &single, cudaStream_t stream);
 const void *mma_kernel_ptr(int variant);
 int mma_threads();
+
+// Chained tensor-core u16 kernel (chain_kernel.cuh): variants 200+. Same
+// exactness certificate as plan_mma; 16-column tiles per warp, windows of up
+// to 3 x 16 lines and 4 x 16 columns.
+bool plan_chain(const FilterTable &first, const FilterTable &second, bool h_first, unsigned depth, unsigned src_w,
+                unsigned src_h, unsigned dst_w, unsigned dst_h, FusedPlan *out);
+SmemLayout chain_layout(const FusedPlan *const *plans, int n);
+const void *chain_kernel_ptr(int variant);
+int chain_threads();
+cudaError_t launch_chain(int variant, const FusedJob *jobs, int num_jobs, int total_items, const SmemLayout &L, int grid,
+                         const FusedJob &single, cudaStream_t stream);
 // Work items that fill the current device once (SMs x resident CTAs).
 int fused_wave_items();
 
