@@ -144,13 +144,14 @@ bool plan_chain(const FilterTable &first, const FilterTable &second, bool h_firs
 	if (KH < 1 || KH > kChainKHMax)
 		return false;
 
-	// strips of 128 output columns (8 tiles); source columns [lo, hi) with lo a multiple of 8
-	const int strip_w = chain_detail::kWarps * chain_detail::kTileW;
+	// strips of 8 warps' tiles; source columns [lo, hi) with lo a multiple of 8
+	const int strip_tiles = chain_detail::kWarps * chain_detail::tiles_per_warp(KV, KH);
+	const int strip_w = strip_tiles * chain_detail::kTileW;
 	const int strips = static_cast<int>((dst_w + strip_w - 1) / strip_w);
 	std::vector<int> win_col(2 * strips);
 	int max_pxa = 0;
 	for (int s = 0; s < strips; ++s) {
-		const int t0 = s * chain_detail::kWarps, t1 = std::min(tiles, t0 + chain_detail::kWarps);
+		const int t0 = s * strip_tiles, t1 = std::min(tiles, t0 + strip_tiles);
 		int lo = INT_MAX, hi = INT_MIN;
 		for (int t = t0; t < t1; ++t) {
 			lo = std::min(lo, hstart[t]);

@@ -38,7 +38,14 @@ using mma_detail::wrap;
 
 constexpr int kWarps = 8;
 constexpr int kThreads = kWarps * 32;
-constexpr int kTileW = 16;                 // output columns per warp
+constexpr int kTileW = 16;                 // output columns of one tile (one m16 block)
+
+// Tiles per warp: two share the loop, the loads and the barriers, where the
+// tap fragments of two tiles fit in registers next to everything else.
+__host__ __device__ constexpr int tiles_per_warp(int kv, int kh)
+{
+	return (kv + kh <= 3 || kh == 1) ? 2 : 1;
+}
 constexpr int kStageBytes = 48;            // staged row: 16 u16 + pad (stmatrix rows without bank conflicts)
 
 __device__ __forceinline__ void stsm_x4(void *p, uint32_t r0, uint32_t r1, uint32_t r2, uint32_t r3)
@@ -72,7 +79,7 @@ struct Item {
 	uint32_t pmax2, bias_h2;
 };
 
-__device__ __forceinline__ Item make_item(const FusedJob &J, int t)
+__device__ __forceinline__ Item make_item(const FusedJob &J, int t, int strip_tiles)
 {
 	Item it;
 	const int local = t - J.item_begin;
@@ -87,7 +94,7 @@ __device__ __forceinline__ Item make_item(const FusedJob &J, int t)
 	it.dst_w = J.dst_w;
 	it.dst_h = J.dst_h;
 	it.vec_ok = J.vec_ok;
-	it.c0 = it.strip * kWarps * kTileW;
+	it.c0 = it.strip * strip_tiles * kTileW;
 	it.xlo = __ldg(J.win_col + 2 * it.strip);
 	const int pxa = (__ldg(J.win_col + 2 * it.strip + 1) - it.xlo + 7) & ~7;
 	it.g_begin = seg * J.seg_groups;
@@ -165,12 +172,149 @@ __device__ __forceinline__ uint32_t centre(uint32_t q, uint32_t bias_h2)
 	return u16x2_to_centred_h2(q, bias_h2);
 }
 
-__device__ __forceinline__ void mma_split(float (&d)[4], const uint4 &hi, const uint4 &lo, uint32_t b0, uint32_t b1)
+// Accumulators of one 16x8 product: the hi and lo tap halves in separate
+// registers (two independent mma chains); both hold exact integers, so their
+// sum is exact too.
+struct Acc {
+	float h[4];
+	float l[4];
+	__device__ __forceinline__ void init()
+	{
+#pragma unroll
+		for (int i = 0; i < 4; ++i) {
+			h[i] = 8192.0f;
+			l[i] = 0.0f;
+		}
+	}
+	__device__ __forceinline__ void mma(const uint4 &hi, const uint4 &lo, uint32_t b0, uint32_t b1)
+	{
+		const uint32_t ah[4] = { hi.x, hi.y, hi.z, hi.w };
+		const uint32_t al[4] = { lo.x, lo.y, lo.z, lo.w };
+		mma16816(h, ah, b0, b1);
+		mma16816(l, al, b0, b1);
+	}
+	__device__ __forceinline__ float operator[](int i) const { return h[i] + l[i]; }
+};
+
+// Two accumulators -> packed, clamped samples (low / high half).
+__device__ __forceinline__ uint32_t pack(const Acc &a, int i, const Item &it)
 {
-	const uint32_t ah[4] = { hi.x, hi.y, hi.z, hi.w };
-	const uint32_t al[4] = { lo.x, lo.y, lo.z, lo.w };
-	mma16816(d, ah, b0, b1);
-	mma16816(d, al, b0, b1);
+#ifdef ZG_CHAIN_FLOAT_CLAMP
+	const float lo = -(it.magic - 12582912.0f) * 16384.0f;
+	const float hi = (static_cast<float>(it.pmax2 & 0xFFFF) - (it.magic - 12582912.0f)) * 16384.0f;
+	const float a0 = fminf(fmaxf(a[i], lo), hi), a1 = fminf(fmaxf(a[i + 1], lo), hi);
+	const float y0 = __fmaf_rd(a0, 6.103515625e-05f, it.magic);
+	const float y1 = __fmaf_rd(a1, 6.103515625e-05f, it.magic);
+	return __byte_perm(__float_as_uint(y0), __float_as_uint(y1), 0x5410);
+#else
+	return pack_u16x2(a[i], a[i + 1], it.magic, it.pmax2);
+#endif
+}
+
+// One 16-column tile of one 16-row group: both passes, then the staged
+// result to the destination. ah: the tile's horizontal tap fragments, rel: its
+// window start in the strip's lines, av: the group's vertical fragments.
+template <bool H_FIRST, int KV, int KH>
+__device__ __forceinline__ void tile_pass(const Item &it, const char *ring, int IR, int P, int slot, int rel,
+                                          const uint4 (&ah)[KH][2], const uint4 (&av)[KV][2], char *st_addr,
+                                          const char *ld_addr, int row0, int col0)
+{
+	const int lane = threadIdx.x & 31;
+	const int gid = lane >> 2, tig = lane & 3;
+	uint32_t m0, m1, m2, m3;
+	if (H_FIRST) {
+		// H over the group's KV*16 lines: B = src[line gid (+8)][in cols 2tig (+8)]
+		uint32_t bv[KV][2][2];
+#pragma unroll
+		for (int kv = 0; kv < KV; ++kv) {
+			Acc dh0, dh1;  // lines 0-7, 8-15
+			dh0.init();
+			dh1.init();
+			const char *r0 = ring + wrap(slot + 16 * kv + gid, IR) * P + (rel + 2 * tig) * 2;
+			const char *r1 = ring + wrap(slot + 16 * kv + gid + 8, IR) * P + (rel + 2 * tig) * 2;
+#pragma unroll
+			for (int ks = 0; ks < KH; ++ks) {
+				const uint32_t b0 = centre(*reinterpret_cast<const uint32_t *>(r0 + ks * 32), it.bias_h2);
+				const uint32_t b1 = centre(*reinterpret_cast<const uint32_t *>(r0 + ks * 32 + 16), it.bias_h2);
+				const uint32_t b2 = centre(*reinterpret_cast<const uint32_t *>(r1 + ks * 32), it.bias_h2);
+				const uint32_t b3 = centre(*reinterpret_cast<const uint32_t *>(r1 + ks * 32 + 16), it.bias_h2);
+				dh0.mma(ah[ks][0], ah[ks][1], b0, b1);
+				dh1.mma(ah[ks][0], ah[ks][1], b2, b3);
+			}
+			// Dh (out col gid / gid+8, lines 2tig..) -> V operands (k = lines, n = out col)
+			bv[kv][0][0] = centre(pack(dh0, 0, it), it.bias_h2);
+			bv[kv][0][1] = centre(pack(dh1, 0, it), it.bias_h2);
+			bv[kv][1][0] = centre(pack(dh0, 2, it), it.bias_h2);
+			bv[kv][1][1] = centre(pack(dh1, 2, it), it.bias_h2);
+		}
+		Acc dv0, dv1;  // out cols 0-7, 8-15
+		dv0.init();
+		dv1.init();
+#pragma unroll
+		for (int kv = 0; kv < KV; ++kv) {
+			dv0.mma(av[kv][0], av[kv][1], bv[kv][0][0], bv[kv][0][1]);
+			dv1.mma(av[kv][0], av[kv][1], bv[kv][1][0], bv[kv][1][1]);
+		}
+		// (out row gid / gid+8, out cols 2tig..): row-major 8x8 blocks
+		m0 = pack(dv0, 0, it);
+		m1 = pack(dv1, 0, it);
+		m2 = pack(dv0, 2, it);
+		m3 = pack(dv1, 2, it);
+		stsm_x4(st_addr, m0, m1, m2, m3);
+	} else {
+		Acc dh0, dh1;  // out rows 0-7, 8-15
+		dh0.init();
+		dh1.init();
+		// ldmatrix.trans rows: line (lane & 7) + ((lane >> 3) & 1) * 8, column + (lane >> 4) * 8
+		const int krow = (lane & 7) + ((lane >> 3) & 1) * 8;
+		const int coff = (rel + (lane >> 4) * 8) * 2;
+#pragma unroll
+		for (int ks = 0; ks < KH; ++ks) {
+			Acc dv0, dv1;  // in cols 0-7, 8-15 of this k-step
+			dv0.init();
+			dv1.init();
+#pragma unroll
+			for (int kv = 0; kv < KV; ++kv) {
+				uint32_t b0, b1, b2, b3;
+				ldsm_x4_trans(b0, b1, b2, b3, ring + wrap(slot + 16 * kv + krow, IR) * P + coff + ks * 32);
+				b0 = centre(b0, it.bias_h2);
+				b1 = centre(b1, it.bias_h2);
+				b2 = centre(b2, it.bias_h2);
+				b3 = centre(b3, it.bias_h2);
+				dv0.mma(av[kv][0], av[kv][1], b0, b1);
+				dv1.mma(av[kv][0], av[kv][1], b2, b3);
+			}
+			// Dv (out row gid / gid+8, in cols 2tig..) -> H operands (k = in cols, n = out row)
+			const uint32_t h00 = centre(pack(dv0, 0, it), it.bias_h2);
+			const uint32_t h01 = centre(pack(dv1, 0, it), it.bias_h2);
+			const uint32_t h10 = centre(pack(dv0, 2, it), it.bias_h2);
+			const uint32_t h11 = centre(pack(dv1, 2, it), it.bias_h2);
+			dh0.mma(ah[ks][0], ah[ks][1], h00, h01);
+			dh1.mma(ah[ks][0], ah[ks][1], h10, h11);
+		}
+		// (out col gid / gid+8, out rows 2tig..): transposed 8x8 blocks
+		m0 = pack(dh0, 0, it);
+		m1 = pack(dh0, 2, it);
+		m2 = pack(dh1, 0, it);
+		m3 = pack(dh1, 2, it);
+		stsm_x4_trans(st_addr, m0, m1, m2, m3);
+	}
+	__syncwarp();
+	// staged 16 x 16 tile -> destination, one 16-byte half row per lane
+	const int row = row0 + (lane >> 1);
+	const int col = col0 + (lane & 1) * 8;
+	if (row < it.dst_h && col < it.dst_w) {
+		const uint4 v = *reinterpret_cast<const uint4 *>(ld_addr);
+		uint16_t *d = reinterpret_cast<uint16_t *>(it.dst + static_cast<ptrdiff_t>(row) * it.dst_stride) + col;
+		if (it.vec_ok && col + 8 <= it.dst_w) {
+			*reinterpret_cast<uint4 *>(d) = v;
+		} else {
+			const uint32_t w[4] = { v.x, v.y, v.z, v.w };
+			for (int e = 0; e < 8 && col + e < it.dst_w; ++e)
+				d[e] = static_cast<uint16_t>(w[e >> 1] >> (16 * (e & 1)));
+		}
+	}
+	__syncwarp();
 }
 
 // Kernel. Shared memory (SmemLayout): ring of raw source lines (in_off,
@@ -189,11 +333,12 @@ chain_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 	char *vslots = smem + L.vcoef_off;
 	int *vb = reinterpret_cast<int *>(smem + L.vbase_off);
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-	const int gid = lane >> 2, tig = lane & 3;
 	char *stage = smem + L.tile_off + warp * 16 * kStageBytes;
 	const int IR = L.in_rows;
 	const int P = L.pitch * 2;
 	constexpr int kSlotBytes = KV * 2 * 32 * 16;
+	constexpr int kTilesPerWarp = tiles_per_warp(KV, KH);
+	constexpr int kStripTiles = kWarps * kTilesPerWarp;
 	// stmatrix / stage read addresses of this lane
 	char *st_addr = stage + (((lane >> 4) << 3) + (lane & 7)) * kStageBytes + ((lane >> 3) & 1) * 16;
 	const char *ld_addr = stage + (lane >> 1) * kStageBytes + (lane & 1) * 16;
@@ -205,24 +350,25 @@ chain_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 
 	for (int t = blockIdx.x; t < total_items; t += gridDim.x) {
 		const FusedJob *Jp = jobs ? &jobs[find_job(jobs, num_jobs, t)] : &single;
-		const Item it = make_item(*Jp, t);
+		const Item it = make_item(*Jp, t, kStripTiles);
 		for (int g = it.g_begin + threadIdx.x; g < it.g_end; g += kThreads)
 			vb[g - it.g_begin] = __ldg(Jp->v_base + g);
 
-		// this warp's 16 output columns: horizontal tap fragments and window start
-		const int col0 = it.c0 + warp * kTileW;
-		const bool active = col0 < it.dst_w;
-		uint4 ah[KH][2];
-		int rel = 0;
-		{
-			const int tile = min(it.strip * kWarps + warp, (it.dst_w + kTileW - 1) / kTileW - 1);
+		// this warp's tiles of 16 output columns: horizontal tap fragments and window starts
+		const int ntiles = (it.dst_w + kTileW - 1) / kTileW;
+		const int tile0 = it.strip * kStripTiles + warp * kTilesPerWarp;
+		uint4 ah[kTilesPerWarp][KH][2];
+		int rel[kTilesPerWarp];
+#pragma unroll
+		for (int j = 0; j < kTilesPerWarp; ++j) {
+			const int tile = min(tile0 + j, ntiles - 1);
 			const uint4 *hf = reinterpret_cast<const uint4 *>(Jp->h_taps) + static_cast<size_t>(tile) * KH * 2 * 32 + lane;
 #pragma unroll
 			for (int ks = 0; ks < KH; ++ks) {
-				ah[ks][0] = __ldg(hf + (ks * 2 + 0) * 32);
-				ah[ks][1] = __ldg(hf + (ks * 2 + 1) * 32);
+				ah[j][ks][0] = __ldg(hf + (ks * 2 + 0) * 32);
+				ah[j][ks][1] = __ldg(hf + (ks * 2 + 1) * 32);
 			}
-			rel = __ldg(Jp->h_left + tile) - it.xlo;
+			rel[j] = __ldg(Jp->h_left + tile) - it.xlo;
 		}
 		__syncthreads();
 
@@ -266,7 +412,7 @@ chain_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 			const int vbk = vb[k];
 			cur_slot = wrap(cur_slot + (vbk - cur_vb), IR);
 			cur_vb = vbk;
-			if (active) {
+			if (tile0 * kTileW < it.dst_w) {
 				const uint4 *avs = reinterpret_cast<const uint4 *>(vslots + read_slot * kSlotBytes) + lane;
 				uint4 av[KV][2];
 #pragma unroll
@@ -274,97 +420,11 @@ chain_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 					av[kv][0] = avs[(kv * 2 + 0) * 32];
 					av[kv][1] = avs[(kv * 2 + 1) * 32];
 				}
-				uint32_t m0, m1, m2, m3;
-				if (H_FIRST) {
-					// H over the group's KV*16 lines: B = src[line gid (+8)][in cols 2tig (+8)]
-					uint32_t bv[KV][2][2];
 #pragma unroll
-					for (int kv = 0; kv < KV; ++kv) {
-						float dh0[4] = { 8192.f, 8192.f, 8192.f, 8192.f };  // lines 0-7
-						float dh1[4] = { 8192.f, 8192.f, 8192.f, 8192.f };  // lines 8-15
-						const char *r0 = ring + wrap(cur_slot + 16 * kv + gid, IR) * P + (rel + 2 * tig) * 2;
-						const char *r1 = ring + wrap(cur_slot + 16 * kv + gid + 8, IR) * P + (rel + 2 * tig) * 2;
-#pragma unroll
-						for (int ks = 0; ks < KH; ++ks) {
-							const uint32_t b0 = centre(*reinterpret_cast<const uint32_t *>(r0 + ks * 32), it.bias_h2);
-							const uint32_t b1 = centre(*reinterpret_cast<const uint32_t *>(r0 + ks * 32 + 16), it.bias_h2);
-							const uint32_t b2 = centre(*reinterpret_cast<const uint32_t *>(r1 + ks * 32), it.bias_h2);
-							const uint32_t b3 = centre(*reinterpret_cast<const uint32_t *>(r1 + ks * 32 + 16), it.bias_h2);
-							mma_split(dh0, ah[ks][0], ah[ks][1], b0, b1);
-							mma_split(dh1, ah[ks][0], ah[ks][1], b2, b3);
-						}
-						// Dh (out col gid / gid+8, lines 2tig..) -> V operands (k = lines, n = out col)
-						bv[kv][0][0] = centre(pack_u16x2(dh0[0], dh0[1], it.magic, it.pmax2), it.bias_h2);
-						bv[kv][0][1] = centre(pack_u16x2(dh1[0], dh1[1], it.magic, it.pmax2), it.bias_h2);
-						bv[kv][1][0] = centre(pack_u16x2(dh0[2], dh0[3], it.magic, it.pmax2), it.bias_h2);
-						bv[kv][1][1] = centre(pack_u16x2(dh1[2], dh1[3], it.magic, it.pmax2), it.bias_h2);
-					}
-					float dv0[4] = { 8192.f, 8192.f, 8192.f, 8192.f };  // out cols 0-7
-					float dv1[4] = { 8192.f, 8192.f, 8192.f, 8192.f };  // out cols 8-15
-#pragma unroll
-					for (int kv = 0; kv < KV; ++kv) {
-						mma_split(dv0, av[kv][0], av[kv][1], bv[kv][0][0], bv[kv][0][1]);
-						mma_split(dv1, av[kv][0], av[kv][1], bv[kv][1][0], bv[kv][1][1]);
-					}
-					// (out row gid / gid+8, out cols 2tig..): row-major 8x8 blocks
-					m0 = pack_u16x2(dv0[0], dv0[1], it.magic, it.pmax2);
-					m1 = pack_u16x2(dv1[0], dv1[1], it.magic, it.pmax2);
-					m2 = pack_u16x2(dv0[2], dv0[3], it.magic, it.pmax2);
-					m3 = pack_u16x2(dv1[2], dv1[3], it.magic, it.pmax2);
-					stsm_x4(st_addr, m0, m1, m2, m3);
-				} else {
-					float dh0[4] = { 8192.f, 8192.f, 8192.f, 8192.f };  // out rows 0-7
-					float dh1[4] = { 8192.f, 8192.f, 8192.f, 8192.f };  // out rows 8-15
-					// ldmatrix.trans rows: line (lane & 7) + ((lane >> 3) & 1) * 8, column + (lane >> 4) * 8
-					const int krow = (lane & 7) + ((lane >> 3) & 1) * 8;
-					const int coff = (rel + (lane >> 4) * 8) * 2;
-#pragma unroll
-					for (int ks = 0; ks < KH; ++ks) {
-						float dv0[4] = { 8192.f, 8192.f, 8192.f, 8192.f };  // in cols 0-7 of this k-step
-						float dv1[4] = { 8192.f, 8192.f, 8192.f, 8192.f };  // in cols 8-15
-#pragma unroll
-						for (int kv = 0; kv < KV; ++kv) {
-							uint32_t b0, b1, b2, b3;
-							ldsm_x4_trans(b0, b1, b2, b3,
-							              ring + wrap(cur_slot + 16 * kv + krow, IR) * P + coff + ks * 32);
-							b0 = centre(b0, it.bias_h2);
-							b1 = centre(b1, it.bias_h2);
-							b2 = centre(b2, it.bias_h2);
-							b3 = centre(b3, it.bias_h2);
-							mma_split(dv0, av[kv][0], av[kv][1], b0, b1);
-							mma_split(dv1, av[kv][0], av[kv][1], b2, b3);
-						}
-						// Dv (out row gid / gid+8, in cols 2tig..) -> H operands (k = in cols, n = out row)
-						const uint32_t h00 = centre(pack_u16x2(dv0[0], dv0[1], it.magic, it.pmax2), it.bias_h2);
-						const uint32_t h01 = centre(pack_u16x2(dv1[0], dv1[1], it.magic, it.pmax2), it.bias_h2);
-						const uint32_t h10 = centre(pack_u16x2(dv0[2], dv0[3], it.magic, it.pmax2), it.bias_h2);
-						const uint32_t h11 = centre(pack_u16x2(dv1[2], dv1[3], it.magic, it.pmax2), it.bias_h2);
-						mma_split(dh0, ah[ks][0], ah[ks][1], h00, h01);
-						mma_split(dh1, ah[ks][0], ah[ks][1], h10, h11);
-					}
-					// (out col gid / gid+8, out rows 2tig..): transposed 8x8 blocks
-					m0 = pack_u16x2(dh0[0], dh0[1], it.magic, it.pmax2);
-					m1 = pack_u16x2(dh0[2], dh0[3], it.magic, it.pmax2);
-					m2 = pack_u16x2(dh1[0], dh1[1], it.magic, it.pmax2);
-					m3 = pack_u16x2(dh1[2], dh1[3], it.magic, it.pmax2);
-					stsm_x4_trans(st_addr, m0, m1, m2, m3);
-				}
-				__syncwarp();
-				// staged 16 x 16 tile -> destination, one 16-byte half row per lane
-				const int row = (it.g_begin + k) * 16 + (lane >> 1);
-				const int col = col0 + (lane & 1) * 8;
-				if (row < it.dst_h && col < it.dst_w) {
-					const uint4 v = *reinterpret_cast<const uint4 *>(ld_addr);
-					uint16_t *d = reinterpret_cast<uint16_t *>(it.dst + static_cast<ptrdiff_t>(row) * it.dst_stride) + col;
-					if (it.vec_ok && col + 8 <= it.dst_w) {
-						*reinterpret_cast<uint4 *>(d) = v;
-					} else {
-						const uint32_t w[4] = { v.x, v.y, v.z, v.w };
-						for (int e = 0; e < 8 && col + e < it.dst_w; ++e)
-							d[e] = static_cast<uint16_t>(w[e >> 1] >> (16 * (e & 1)));
-					}
-				}
-				__syncwarp();
+				for (int j = 0; j < kTilesPerWarp; ++j)
+					if ((tile0 + j) * kTileW < it.dst_w)
+						tile_pass<H_FIRST, KV, KH>(it, ring, IR, P, cur_slot, rel[j], ah[j], av, st_addr, ld_addr,
+						                           (it.g_begin + k) * 16, (tile0 + j) * kTileW);
 			}
 			read_slot = read_slot + 1 == nslots ? 0 : read_slot + 1;
 		}
