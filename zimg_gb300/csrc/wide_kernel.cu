@@ -35,6 +35,7 @@ namespace zg {
 namespace {
 
 constexpr int kWideWarps = 4;
+constexpr int kUnroll = 8;  // k-steps whose loads are issued together (a multiple of 4)
 
 __device__ __forceinline__ uint32_t tf32_rna(float x)
 {
@@ -77,18 +78,100 @@ __device__ __forceinline__ void add4(float (&d)[4], const float (&c)[4])
 	d[3] += c[3];
 }
 
-// Element (m, k) of the input is at src + m * sm + k * sk (bytes); output
-// (o, m) at dst + m * dm + o * dko. A warp owns 16 consecutive m and walks
-// output groups [g0, g1).
+// k-steps [s0, s1) of output group g for this lane's rows/columns ma, mb:
+// d += sum of the 3xTF32 products. Element (m, k) of the input is at
+// src + m * sm + k * sk (bytes).
+__device__ __forceinline__ void band_sum(float (&d)[4], const WideTables &w, int g, int s0, int s1, int src_dim,
+                                         const char *base_a, const char *base_b, ptrdiff_t sk)
+{
+	const int lane = threadIdx.x & 31, tig = lane & 3;
+	const int kb = __ldg(w.kbase + g);
+	const uint4 *bf = w.frag + static_cast<size_t>(g) * w.ksteps * 32 + lane;
+	if (kb + 8 * s1 <= src_dim) {
+		const char *pa = base_a + (kb + 8 * s0 + tig) * sk, *pb = base_b + (kb + 8 * s0 + tig) * sk;
+		const ptrdiff_t s4 = 4 * sk, s8 = 8 * sk;
+		int s = s0;
+		for (; s + kUnroll <= s1; s += kUnroll) {
+			float x[kUnroll][4];
+			uint4 b[kUnroll];
+#pragma unroll
+			for (int u = 0; u < kUnroll; ++u) {
+				x[u][0] = __ldg(reinterpret_cast<const float *>(pa + u * s8));
+				x[u][1] = __ldg(reinterpret_cast<const float *>(pb + u * s8));
+				x[u][2] = __ldg(reinterpret_cast<const float *>(pa + u * s8 + s4));
+				x[u][3] = __ldg(reinterpret_cast<const float *>(pb + u * s8 + s4));
+				b[u] = __ldg(bf + (s + u) * 32);
+			}
+#pragma unroll
+			for (int c0 = 0; c0 < kUnroll; c0 += 4) {
+				float c[4] = { 0.f, 0.f, 0.f, 0.f };
+#pragma unroll
+				for (int u = c0; u < c0 + 4; ++u)
+					step3(c, x[u][0], x[u][1], x[u][2], x[u][3], b[u]);
+				add4(d, c);
+			}
+			pa += kUnroll * s8;
+			pb += kUnroll * s8;
+		}
+		for (; s < s1; ++s) {
+			const float x0 = __ldg(reinterpret_cast<const float *>(pa));
+			const float x1 = __ldg(reinterpret_cast<const float *>(pb));
+			const float x2 = __ldg(reinterpret_cast<const float *>(pa + s4));
+			const float x3 = __ldg(reinterpret_cast<const float *>(pb + s4));
+			float c[4] = { 0.f, 0.f, 0.f, 0.f };
+			step3(c, x0, x1, x2, x3, __ldg(bf + s * 32));
+			add4(d, c);
+			pa += s8;
+			pb += s8;
+		}
+	} else {
+		// the block reaches past the last input: clamp (those taps are zero)
+		const int kmax = src_dim - 1;
+		for (int s = s0; s < s1; ++s) {
+			const int k0 = min(kb + 8 * s + tig, kmax), k1 = min(kb + 8 * s + tig + 4, kmax);
+			const float x0 = __ldg(reinterpret_cast<const float *>(base_a + k0 * sk));
+			const float x1 = __ldg(reinterpret_cast<const float *>(base_b + k0 * sk));
+			const float x2 = __ldg(reinterpret_cast<const float *>(base_a + k1 * sk));
+			const float x3 = __ldg(reinterpret_cast<const float *>(base_b + k1 * sk));
+			float c[4] = { 0.f, 0.f, 0.f, 0.f };
+			step3(c, x0, x1, x2, x3, __ldg(bf + s * 32));
+			add4(d, c);
+		}
+	}
+}
+
+__device__ __forceinline__ void store_group(const float (&d)[4], int g, int m0, int m_extent, int dst_dim, char *dst,
+                                            ptrdiff_t dm, ptrdiff_t dko)
+{
+	const int lane = threadIdx.x & 31, gid = lane >> 2, tig = lane & 3;
+	const int o = g * 8 + 2 * tig;
+	const int mA = m0 + gid, mB = m0 + gid + 8;
+	if (o < dst_dim) {
+		if (mA < m_extent) *reinterpret_cast<float *>(dst + mA * dm + o * dko) = d[0];
+		if (mB < m_extent) *reinterpret_cast<float *>(dst + mB * dm + o * dko) = d[2];
+	}
+	if (o + 1 < dst_dim) {
+		if (mA < m_extent) *reinterpret_cast<float *>(dst + mA * dm + (o + 1) * dko) = d[1];
+		if (mB < m_extent) *reinterpret_cast<float *>(dst + mB * dm + (o + 1) * dko) = d[3];
+	}
+}
+
+// Output (o, m) is at dst + m * dm + o * dko. KSPLIT 1: a warp owns 16
+// consecutive m and walks output groups [g0, g1). KSPLIT = kWideWarps (passes
+// with few m, e.g. the horizontal pass after a strong vertical downscale): the
+// CTA's warps share one 16-m tile and split each group's k-steps; the
+// partial sums are added in warp order (deterministic) by warp 0.
+template <int KSPLIT>
 __global__ void __launch_bounds__(kWideWarps * 32)
 wide_tc_kernel(WideTables w, int m_extent, int src_dim, int dst_dim, const char *__restrict__ src, ptrdiff_t sm,
                ptrdiff_t sk, char *__restrict__ dst, ptrdiff_t dm, ptrdiff_t dko, int groups_per_block)
 {
+	__shared__ float4 red[KSPLIT > 1 ? KSPLIT * 32 : 1];
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-	const int gid = lane >> 2, tig = lane & 3;
-	const int m0 = (blockIdx.x * kWideWarps + warp) * 16;
+	const int gid = lane >> 2;
+	const int m0 = (KSPLIT > 1 ? blockIdx.x : blockIdx.x * kWideWarps + warp) * 16;
 	if (m0 >= m_extent)
-		return;
+		return;  // whole CTA when KSPLIT > 1
 	const int ma = min(m0 + gid, m_extent - 1), mb = min(m0 + gid + 8, m_extent - 1);
 	const int g0 = blockIdx.y * groups_per_block;
 	const int g1 = min(w.groups, g0 + groups_per_block);
@@ -96,66 +179,29 @@ wide_tc_kernel(WideTables w, int m_extent, int src_dim, int dst_dim, const char 
 	const char *base_a = src + ma * sm, *base_b = src + mb * sm;
 
 	for (int g = g0; g < g1; ++g) {
-		const int kb = __ldg(w.kbase + g);
-		const uint4 *bf = w.frag + static_cast<size_t>(g) * KS * 32 + lane;
 		float d[4] = { 0.f, 0.f, 0.f, 0.f };
-		if (kb + 8 * KS <= src_dim) {
-			const char *pa = base_a + (kb + tig) * sk, *pb = base_b + (kb + tig) * sk;
-			const ptrdiff_t s4 = 4 * sk, s8 = 8 * sk;
-			int s = 0;
-			for (; s + 4 <= KS; s += 4) {
-				float x[4][4];
-				uint4 b[4];
-#pragma unroll
-				for (int u = 0; u < 4; ++u) {
-					x[u][0] = __ldg(reinterpret_cast<const float *>(pa + u * s8));
-					x[u][1] = __ldg(reinterpret_cast<const float *>(pb + u * s8));
-					x[u][2] = __ldg(reinterpret_cast<const float *>(pa + u * s8 + s4));
-					x[u][3] = __ldg(reinterpret_cast<const float *>(pb + u * s8 + s4));
-					b[u] = __ldg(bf + (s + u) * 32);
-				}
-				float c[4] = { 0.f, 0.f, 0.f, 0.f };
-#pragma unroll
-				for (int u = 0; u < 4; ++u)
-					step3(c, x[u][0], x[u][1], x[u][2], x[u][3], b[u]);
-				add4(d, c);
-				pa += 4 * s8;
-				pb += 4 * s8;
-			}
-			for (; s < KS; ++s) {
-				const float x0 = __ldg(reinterpret_cast<const float *>(pa));
-				const float x1 = __ldg(reinterpret_cast<const float *>(pb));
-				const float x2 = __ldg(reinterpret_cast<const float *>(pa + s4));
-				const float x3 = __ldg(reinterpret_cast<const float *>(pb + s4));
-				float c[4] = { 0.f, 0.f, 0.f, 0.f };
-				step3(c, x0, x1, x2, x3, __ldg(bf + s * 32));
-				add4(d, c);
-				pa += s8;
-				pb += s8;
-			}
+		if (KSPLIT == 1) {
+			band_sum(d, w, g, 0, KS, src_dim, base_a, base_b, sk);
+			store_group(d, g, m0, m_extent, dst_dim, dst, dm, dko);
 		} else {
-			// the block reaches past the last input: clamp (those taps are zero)
-			const int kmax = src_dim - 1;
-			for (int s = 0; s < KS; ++s) {
-				const int k0 = min(kb + 8 * s + tig, kmax), k1 = min(kb + 8 * s + tig + 4, kmax);
-				const float x0 = __ldg(reinterpret_cast<const float *>(base_a + k0 * sk));
-				const float x1 = __ldg(reinterpret_cast<const float *>(base_b + k0 * sk));
-				const float x2 = __ldg(reinterpret_cast<const float *>(base_a + k1 * sk));
-				const float x3 = __ldg(reinterpret_cast<const float *>(base_b + k1 * sk));
-				float c[4] = { 0.f, 0.f, 0.f, 0.f };
-				step3(c, x0, x1, x2, x3, __ldg(bf + s * 32));
-				add4(d, c);
+			const int per = (KS + KSPLIT - 1) / KSPLIT;
+			const int s0 = min(KS, warp * per), s1 = min(KS, s0 + per);
+			band_sum(d, w, g, s0, s1, src_dim, base_a, base_b, sk);
+			red[warp * 32 + lane] = make_float4(d[0], d[1], d[2], d[3]);
+			__syncthreads();
+			if (warp == 0) {
+				float t[4] = { 0.f, 0.f, 0.f, 0.f };
+#pragma unroll
+				for (int i = 0; i < KSPLIT; ++i) {
+					const float4 v = red[i * 32 + lane];
+					t[0] += v.x;
+					t[1] += v.y;
+					t[2] += v.z;
+					t[3] += v.w;
+				}
+				store_group(t, g, m0, m_extent, dst_dim, dst, dm, dko);
 			}
-		}
-		const int o = g * 8 + 2 * tig;
-		const int mA = m0 + gid, mB = m0 + gid + 8;
-		if (o < dst_dim) {
-			if (mA < m_extent) *reinterpret_cast<float *>(dst + mA * dm + o * dko) = d[0];
-			if (mB < m_extent) *reinterpret_cast<float *>(dst + mB * dm + o * dko) = d[2];
-		}
-		if (o + 1 < dst_dim) {
-			if (mA < m_extent) *reinterpret_cast<float *>(dst + mA * dm + (o + 1) * dko) = d[1];
-			if (mB < m_extent) *reinterpret_cast<float *>(dst + mB * dm + (o + 1) * dko) = d[3];
+			__syncthreads();
 		}
 	}
 }
@@ -172,6 +218,21 @@ float tf32_round(float x)
 	float r;
 	std::memcpy(&r, &u, 4);
 	return r;
+}
+
+int sm_count()
+{
+	static int cached[64] = {};
+	int dev = 0;
+	cudaGetDevice(&dev);
+	if (dev < 0 || dev >= 64)
+		return 152;
+	if (!cached[dev]) {
+		int n = 0;
+		cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+		cached[dev] = n > 0 ? n : 152;
+	}
+	return cached[dev];
 }
 
 uint32_t bits(float x)
@@ -228,15 +289,24 @@ cudaError_t launch_wide(const PassLaunch &l, cudaStream_t stream)
 	const ptrdiff_t sm = l.horizontal ? l.src_stride : 4, sk = l.horizontal ? 4 : l.src_stride;
 	const ptrdiff_t dm = l.horizontal ? l.dst_stride : 4, dko = l.horizontal ? 4 : l.dst_stride;
 	const int mtiles = (m_extent + 15) / 16;
+	const long sms = sm_count();
+	const long target = sms * 64;  // enough warps for several waves on every SM
+	if (static_cast<long>(mtiles) * l.wide.groups < sms * 16 && l.wide.ksteps >= 2 * kWideWarps) {
+		// few output tiles: split each group's k-steps across the CTA's warps
+		int gpb = std::max(1, (l.wide.groups + 65534) / 65535);
+		const int by = (l.wide.groups + gpb - 1) / gpb;
+		wide_tc_kernel<kWideWarps><<<dim3(mtiles, by), kWideWarps * 32, 0, stream>>>(
+			l.wide, m_extent, src_dim, dst_dim, static_cast<const char *>(l.src), sm, sk, static_cast<char *>(l.dst), dm,
+			dko, gpb);
+		return cudaGetLastError();
+	}
 	const int bx = (mtiles + kWideWarps - 1) / kWideWarps;
-	// enough warps for several waves on every SM, then longer runs of groups
-	const long target = 152L * 64;
 	int gpb = static_cast<int>(std::max<long>(1, static_cast<long>(mtiles) * l.wide.groups / target));
 	gpb = std::max(std::min(gpb, 8), (l.wide.groups + 65534) / 65535);
 	const int by = (l.wide.groups + gpb - 1) / gpb;
-	wide_tc_kernel<<<dim3(bx, by), kWideWarps * 32, 0, stream>>>(l.wide, m_extent, src_dim, dst_dim,
-	                                                              static_cast<const char *>(l.src), sm, sk,
-	                                                              static_cast<char *>(l.dst), dm, dko, gpb);
+	wide_tc_kernel<1><<<dim3(bx, by), kWideWarps * 32, 0, stream>>>(l.wide, m_extent, src_dim, dst_dim,
+	                                                                 static_cast<const char *>(l.src), sm, sk,
+	                                                                 static_cast<char *>(l.dst), dm, dko, gpb);
 	return cudaGetLastError();
 }
 
