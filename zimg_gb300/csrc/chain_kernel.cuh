@@ -71,7 +71,7 @@ struct Item {
 	ptrdiff_t dst_stride;
 	int src_w, src_h, dst_w, dst_h, vec_ok;
 	int strip, c0, xlo;
-	int g_begin, g_end, depth;
+	int g_begin, g_end, depth, vstep8;
 	// this thread's place in line copies: chunk q0 of line offset l0, then
 	// advance by (sl lines, sq chunks) per iteration
 	int chunks, q0, l0, sl, sq;
@@ -100,6 +100,7 @@ __device__ __forceinline__ Item make_item(const FusedJob &J, int t, int strip_ti
 	it.g_begin = seg * J.seg_groups;
 	it.g_end = min(J.groups, it.g_begin + J.seg_groups);
 	it.depth = J.depth;
+	it.vstep8 = J.vstep8;
 	it.magic = J.magic;
 	const uint32_t pm = static_cast<uint32_t>(J.pixel_max);
 	it.pmax2 = pm | (pm << 16);
@@ -172,18 +173,22 @@ __device__ __forceinline__ uint32_t centre(uint32_t q, uint32_t bias_h2)
 	return u16x2_to_centred_h2(q, bias_h2);
 }
 
-// Accumulators of one 16x8 product: the hi and lo tap halves in separate
-// registers (two independent mma chains); both hold exact integers, so their
-// sum is exact too.
+// Accumulator of one 16x8 product: the hi and lo tap halves accumulate into
+// the same exact-integer fp32 registers (with ZG_CHAIN_SPLIT_ACC: separate
+// registers, two independent mma chains, added at the end; also exact).
 struct Acc {
 	float h[4];
+#ifdef ZG_CHAIN_SPLIT_ACC
 	float l[4];
+#endif
 	__device__ __forceinline__ void init()
 	{
 #pragma unroll
 		for (int i = 0; i < 4; ++i) {
 			h[i] = 8192.0f;
+#ifdef ZG_CHAIN_SPLIT_ACC
 			l[i] = 0.0f;
+#endif
 		}
 	}
 	__device__ __forceinline__ void mma(const uint4 &hi, const uint4 &lo, uint32_t b0, uint32_t b1)
@@ -191,12 +196,20 @@ struct Acc {
 		const uint32_t ah[4] = { hi.x, hi.y, hi.z, hi.w };
 		const uint32_t al[4] = { lo.x, lo.y, lo.z, lo.w };
 		mma16816(h, ah, b0, b1);
+#ifdef ZG_CHAIN_SPLIT_ACC
 		mma16816(l, al, b0, b1);
+#else
+		mma16816(h, al, b0, b1);
+#endif
 	}
+#ifdef ZG_CHAIN_SPLIT_ACC
 	__device__ __forceinline__ float operator[](int i) const { return h[i] + l[i]; }
+#else
+	__device__ __forceinline__ float operator[](int i) const { return h[i]; }
+#endif
 };
 
-// Two accumulators -> packed, clamped samples (low / high half).
+// Two accumulator values -> packed, clamped samples (low / high half).
 __device__ __forceinline__ uint32_t pack(const Acc &a, int i, const Item &it)
 {
 #ifdef ZG_CHAIN_FLOAT_CLAMP
@@ -214,10 +227,17 @@ __device__ __forceinline__ uint32_t pack(const Acc &a, int i, const Item &it)
 // One 16-column tile of one 16-row group: both passes, then the staged
 // result to the destination. ah: the tile's horizontal tap fragments, rel: its
 // window start in the strip's lines, av: the group's vertical fragments.
+// H first, one 16-line window per group: the H results of lines 8-15 (V
+// operands of output columns 0-7 and 8-15) carried to the next group when it
+// starts 8 lines later.
+struct Carry {
+	uint32_t b[2];
+};
+
 template <bool H_FIRST, int KV, int KH>
 __device__ __forceinline__ void tile_pass(const Item &it, const char *ring, int IR, int P, int slot, int rel,
                                           const uint4 (&ah)[KH][2], const uint4 (&av)[KV][2], char *st_addr,
-                                          const char *ld_addr, int row0, int col0)
+                                          const char *ld_addr, int row0, int col0, Carry &carry, bool reuse)
 {
 	const int lane = threadIdx.x & 31;
 	const int gid = lane >> 2, tig = lane & 3;
@@ -228,24 +248,37 @@ __device__ __forceinline__ void tile_pass(const Item &it, const char *ring, int 
 #pragma unroll
 		for (int kv = 0; kv < KV; ++kv) {
 			Acc dh0, dh1;  // lines 0-7, 8-15
-			dh0.init();
+			const bool top = !(KV == 1 && reuse);
+			if (top)
+				dh0.init();
 			dh1.init();
 			const char *r0 = ring + wrap(slot + 16 * kv + gid, IR) * P + (rel + 2 * tig) * 2;
 			const char *r1 = ring + wrap(slot + 16 * kv + gid + 8, IR) * P + (rel + 2 * tig) * 2;
 #pragma unroll
 			for (int ks = 0; ks < KH; ++ks) {
-				const uint32_t b0 = centre(*reinterpret_cast<const uint32_t *>(r0 + ks * 32), it.bias_h2);
-				const uint32_t b1 = centre(*reinterpret_cast<const uint32_t *>(r0 + ks * 32 + 16), it.bias_h2);
+				if (top) {
+					const uint32_t b0 = centre(*reinterpret_cast<const uint32_t *>(r0 + ks * 32), it.bias_h2);
+					const uint32_t b1 = centre(*reinterpret_cast<const uint32_t *>(r0 + ks * 32 + 16), it.bias_h2);
+					dh0.mma(ah[ks][0], ah[ks][1], b0, b1);
+				}
 				const uint32_t b2 = centre(*reinterpret_cast<const uint32_t *>(r1 + ks * 32), it.bias_h2);
 				const uint32_t b3 = centre(*reinterpret_cast<const uint32_t *>(r1 + ks * 32 + 16), it.bias_h2);
-				dh0.mma(ah[ks][0], ah[ks][1], b0, b1);
 				dh1.mma(ah[ks][0], ah[ks][1], b2, b3);
 			}
 			// Dh (out col gid / gid+8, lines 2tig..) -> V operands (k = lines, n = out col)
-			bv[kv][0][0] = centre(pack(dh0, 0, it), it.bias_h2);
+			if (top) {
+				bv[kv][0][0] = centre(pack(dh0, 0, it), it.bias_h2);
+				bv[kv][1][0] = centre(pack(dh0, 2, it), it.bias_h2);
+			} else {
+				bv[kv][0][0] = carry.b[0];
+				bv[kv][1][0] = carry.b[1];
+			}
 			bv[kv][0][1] = centre(pack(dh1, 0, it), it.bias_h2);
-			bv[kv][1][0] = centre(pack(dh0, 2, it), it.bias_h2);
 			bv[kv][1][1] = centre(pack(dh1, 2, it), it.bias_h2);
+		}
+		if (KV == 1) {
+			carry.b[0] = bv[0][0][1];
+			carry.b[1] = bv[0][1][1];
 		}
 		Acc dv0, dv1;  // out cols 0-7, 8-15
 		dv0.init();
@@ -359,6 +392,7 @@ chain_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 		const int tile0 = it.strip * kStripTiles + warp * kTilesPerWarp;
 		uint4 ah[kTilesPerWarp][KH][2];
 		int rel[kTilesPerWarp];
+		Carry carry[kTilesPerWarp];
 #pragma unroll
 		for (int j = 0; j < kTilesPerWarp; ++j) {
 			const int tile = min(tile0 + j, ntiles - 1);
@@ -424,7 +458,8 @@ chain_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 				for (int j = 0; j < kTilesPerWarp; ++j)
 					if ((tile0 + j) * kTileW < it.dst_w)
 						tile_pass<H_FIRST, KV, KH>(it, ring, IR, P, cur_slot, rel[j], ah[j], av, st_addr, ld_addr,
-						                           (it.g_begin + k) * 16, (tile0 + j) * kTileW);
+						                           (it.g_begin + k) * 16, (tile0 + j) * kTileW, carry[j],
+						                           it.vstep8 && k > 0);
 			}
 			read_slot = read_slot + 1 == nslots ? 0 : read_slot + 1;
 		}
