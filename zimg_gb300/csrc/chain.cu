@@ -261,9 +261,6 @@ bool plan_chain(const FilterTable &first, const FilterTable &second, bool h_firs
 	std::memcpy(p.blob.data() + p.off_v_base, gbase.data(), gbase.size() * 4);
 	std::memcpy(p.blob.data() + p.off_win_col, win_col.data(), win_col.size() * 4);
 
-	J.vstep8 = h_first && KV == 1 ? 1 : 0;
-	for (int g = 1; g < groups && J.vstep8; ++g)
-		J.vstep8 = gbase[g] - gbase[g - 1] == 8;
 	const float offset = static_cast<float>(std::ldexp(1.0, static_cast<int>(depth) - 1));
 	J.offset = offset;
 	J.magic = 12582912.0f + offset;

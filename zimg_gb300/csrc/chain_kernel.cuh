@@ -16,9 +16,9 @@
 // layout of the B operand of the next product (k = 2tig, 2tig+1, n = gid), so
 // the first product's rounded results, converted to centred fp16 pairs, are
 // the second product's B fragments as they stand. Source lines stream
-// through one ring of raw u16 lines per CTA (cp.async, prefetched `depth`
-// groups ahead, one barrier per group); results leave through a per-warp
-// staging tile (stmatrix) as 16-byte rows.
+// through one ring of lines per CTA (cp.async, prefetched `depth` groups
+// ahead, centred to fp16 in place once they land, one barrier per group);
+// results leave through a per-warp staging tile (stmatrix) as 16-byte rows.
 #pragma once
 
 #include "mma_kernel.cuh"
@@ -71,7 +71,7 @@ struct Item {
 	ptrdiff_t dst_stride;
 	int src_w, src_h, dst_w, dst_h, vec_ok;
 	int strip, c0, xlo;
-	int g_begin, g_end, depth, vstep8;
+	int g_begin, g_end, depth;
 	// this thread's place in line copies: chunk q0 of line offset l0, then
 	// advance by (sl lines, sq chunks) per iteration
 	int chunks, q0, l0, sl, sq;
@@ -100,7 +100,6 @@ __device__ __forceinline__ Item make_item(const FusedJob &J, int t, int strip_ti
 	it.g_begin = seg * J.seg_groups;
 	it.g_end = min(J.groups, it.g_begin + J.seg_groups);
 	it.depth = J.depth;
-	it.vstep8 = J.vstep8;
 	it.magic = J.magic;
 	const uint32_t pm = static_cast<uint32_t>(J.pixel_max);
 	it.pmax2 = pm | (pm << 16);
@@ -143,6 +142,34 @@ __device__ __forceinline__ void load_lines(const Item &it, int a, int b, char *r
 	}
 }
 
+__device__ __forceinline__ uint32_t centre(uint32_t q, uint32_t bias_h2)
+{
+	return u16x2_to_centred_h2(q, bias_h2);
+}
+
+// The same lines, once their copies have landed: raw u16 -> centred fp16 in
+// place. Each thread converts exactly the chunks it copied (same mapping as
+// load_lines), so its own completed copies are all it reads.
+__device__ __forceinline__ void convert_lines(const Item &it, int a, int b, char *ring, int R, int sa, int pitch_bytes)
+{
+	int y = a + it.l0, q = it.q0;
+	for (; y < b;) {
+		uint4 *p = reinterpret_cast<uint4 *>(ring + wrap(sa + (y - a), R) * pitch_bytes + q * 16);
+		uint4 u = *p;
+		u.x = centre(u.x, it.bias_h2);
+		u.y = centre(u.y, it.bias_h2);
+		u.z = centre(u.z, it.bias_h2);
+		u.w = centre(u.w, it.bias_h2);
+		*p = u;
+		q += it.sq;
+		y += it.sl;
+		if (q >= it.chunks) {
+			q -= it.chunks;
+			++y;
+		}
+	}
+}
+
 // Vertical tap fragments of group g into a shared slot.
 template <int KV>
 __device__ __forceinline__ void load_vfrag(const FusedJob &J, int g, char *slot)
@@ -166,11 +193,6 @@ __device__ __forceinline__ void wait_groups(int pending)
 	case 7: cp_async_wait<7>(); break;
 	default: cp_async_wait<8>(); break;
 	}
-}
-
-__device__ __forceinline__ uint32_t centre(uint32_t q, uint32_t bias_h2)
-{
-	return u16x2_to_centred_h2(q, bias_h2);
 }
 
 // Accumulator of one 16x8 product: the hi and lo tap halves accumulate into
@@ -257,12 +279,12 @@ __device__ __forceinline__ void tile_pass(const Item &it, const char *ring, int 
 #pragma unroll
 			for (int ks = 0; ks < KH; ++ks) {
 				if (top) {
-					const uint32_t b0 = centre(*reinterpret_cast<const uint32_t *>(r0 + ks * 32), it.bias_h2);
-					const uint32_t b1 = centre(*reinterpret_cast<const uint32_t *>(r0 + ks * 32 + 16), it.bias_h2);
+					const uint32_t b0 = *reinterpret_cast<const uint32_t *>(r0 + ks * 32);
+					const uint32_t b1 = *reinterpret_cast<const uint32_t *>(r0 + ks * 32 + 16);
 					dh0.mma(ah[ks][0], ah[ks][1], b0, b1);
 				}
-				const uint32_t b2 = centre(*reinterpret_cast<const uint32_t *>(r1 + ks * 32), it.bias_h2);
-				const uint32_t b3 = centre(*reinterpret_cast<const uint32_t *>(r1 + ks * 32 + 16), it.bias_h2);
+				const uint32_t b2 = *reinterpret_cast<const uint32_t *>(r1 + ks * 32);
+				const uint32_t b3 = *reinterpret_cast<const uint32_t *>(r1 + ks * 32 + 16);
 				dh1.mma(ah[ks][0], ah[ks][1], b2, b3);
 			}
 			// Dh (out col gid / gid+8, lines 2tig..) -> V operands (k = lines, n = out col)
@@ -310,10 +332,6 @@ __device__ __forceinline__ void tile_pass(const Item &it, const char *ring, int 
 			for (int kv = 0; kv < KV; ++kv) {
 				uint32_t b0, b1, b2, b3;
 				ldsm_x4_trans(b0, b1, b2, b3, ring + wrap(slot + 16 * kv + krow, IR) * P + coff + ks * 32);
-				b0 = centre(b0, it.bias_h2);
-				b1 = centre(b1, it.bias_h2);
-				b2 = centre(b2, it.bias_h2);
-				b3 = centre(b3, it.bias_h2);
 				dv0.mma(av[kv][0], av[kv][1], b0, b1);
 				dv1.mma(av[kv][0], av[kv][1], b2, b3);
 			}
@@ -427,6 +445,7 @@ chain_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 
 		int cur_vb = vb[0];
 		int cur_slot = wrap(cur_vb % IR, IR);
+		int conv_hi = vb[0], conv_slot = cur_slot;
 		int fetch_slot = D % nslots, read_slot = 0;
 		for (int k = 0; k < ngroups; ++k) {
 			if (k + D < ngroups) {
@@ -441,9 +460,18 @@ chain_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 			cp_async_commit();
 			fetch_slot = fetch_slot + 1 == nslots ? 0 : fetch_slot + 1;
 			wait_groups(D);
+			{
+				const int hi = vb[k] + 16 * KV;
+				if (hi > conv_hi) {
+					convert_lines(it, conv_hi, hi, ring, IR, conv_slot, P);
+					conv_slot = wrap(conv_slot + (hi - conv_hi), IR);
+					conv_hi = hi;
+				}
+			}
 			__syncthreads();
 
 			const int vbk = vb[k];
+			const bool reuse = H_FIRST && KV == 1 && k > 0 && vbk - cur_vb == 8;
 			cur_slot = wrap(cur_slot + (vbk - cur_vb), IR);
 			cur_vb = vbk;
 			if (tile0 * kTileW < it.dst_w) {
@@ -458,8 +486,7 @@ chain_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 				for (int j = 0; j < kTilesPerWarp; ++j)
 					if ((tile0 + j) * kTileW < it.dst_w)
 						tile_pass<H_FIRST, KV, KH>(it, ring, IR, P, cur_slot, rel[j], ah[j], av, st_addr, ld_addr,
-						                           (it.g_begin + k) * 16, (tile0 + j) * kTileW, carry[j],
-						                           it.vstep8 && k > 0);
+						                           (it.g_begin + k) * 16, (tile0 + j) * kTileW, carry[j], reuse);
 			}
 			read_slot = read_slot + 1 == nslots ? 0 : read_slot + 1;
 		}

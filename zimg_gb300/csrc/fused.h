@@ -73,8 +73,6 @@ struct FusedJob {
 	float pixel_max;
 	float offset;           // 2^(depth-1)
 	int vec_ok;             // planes and strides 16-byte aligned: vector loads and stores
-	int vstep8;             // chained kernel, H first, one 16-line window: every group starts 8 lines
-	                        // after the previous one (the lower half of its window is reused)
 };
 
 // Shared-memory layout of one launch (the maximum over its jobs).
