@@ -16,8 +16,9 @@
 // layout of the B operand of the next product (k = 2tig, 2tig+1, n = gid), so
 // the first product's rounded results, converted to centred fp16 pairs, are
 // the second product's B fragments as they stand. Source lines stream
-// through one ring of lines per CTA (cp.async, prefetched `depth` groups
-// ahead, centred to fp16 in place once they land, one barrier per group);
+// through one ring of raw u16 lines per CTA (bulk async copies completing on
+// mbarriers, or cp.async for unaligned planes; prefetched `depth` groups
+// ahead; one CTA barrier per group) and are centred to fp16 as they are read;
 // results leave through a per-warp staging tile (stmatrix) as 16-byte rows.
 #pragma once
 
@@ -70,7 +71,7 @@ struct Item {
 	char *dst;
 	ptrdiff_t dst_stride;
 	int src_w, src_h, dst_w, dst_h, vec_ok;
-	int strip, c0, xlo;
+	int strip, c0, xlo, pxa;
 	int g_begin, g_end, depth;
 	// this thread's place in line copies: chunk q0 of line offset l0, then
 	// advance by (sl lines, sq chunks) per iteration
@@ -97,6 +98,7 @@ __device__ __forceinline__ Item make_item(const FusedJob &J, int t, int strip_ti
 	it.c0 = it.strip * strip_tiles * kTileW;
 	it.xlo = __ldg(J.win_col + 2 * it.strip);
 	const int pxa = (__ldg(J.win_col + 2 * it.strip + 1) - it.xlo + 7) & ~7;
+	it.pxa = pxa;
 	it.g_begin = seg * J.seg_groups;
 	it.g_end = min(J.groups, it.g_begin + J.seg_groups);
 	it.depth = J.depth;
@@ -147,25 +149,85 @@ __device__ __forceinline__ uint32_t centre(uint32_t q, uint32_t bias_h2)
 	return u16x2_to_centred_h2(q, bias_h2);
 }
 
-// The same lines, once their copies have landed: raw u16 -> centred fp16 in
-// place. Each thread converts exactly the chunks it copied (same mapping as
-// load_lines), so its own completed copies are all it reads.
-__device__ __forceinline__ void convert_lines(const Item &it, int a, int b, char *ring, int R, int sa, int pitch_bytes)
+// ------------------------------------------------ bulk copies, mbarriers --
+// Aligned planes: each source line of a group is one cp.async.bulk copy
+// (issued by one lane of one warp), completing on the group's mbarrier; the
+// consumers wait on that barrier's phase. Every wait is bounded: after
+// kWaitLimit polls it counts a timeout in g_wait_timeouts and goes on (the
+// results of that launch are then garbage, but the kernel ends).
+
+__device__ unsigned int g_wait_timeouts;
+constexpr unsigned kWaitLimit = 1u << 22;
+
+__device__ __forceinline__ unsigned smem_u32(const void *p)
 {
-	int y = a + it.l0, q = it.q0;
-	for (; y < b;) {
-		uint4 *p = reinterpret_cast<uint4 *>(ring + wrap(sa + (y - a), R) * pitch_bytes + q * 16);
-		uint4 u = *p;
-		u.x = centre(u.x, it.bias_h2);
-		u.y = centre(u.y, it.bias_h2);
-		u.z = centre(u.z, it.bias_h2);
-		u.w = centre(u.w, it.bias_h2);
-		*p = u;
-		q += it.sq;
-		y += it.sl;
-		if (q >= it.chunks) {
-			q -= it.chunks;
-			++y;
+	return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *b, unsigned count)
+{
+	asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *b, unsigned bytes)
+{
+	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void bulk_copy(void *dst, const void *src, unsigned bytes, uint64_t *b)
+{
+	asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+	                 smem_u32(dst)),
+	             "l"(src), "r"(bytes), "r"(smem_u32(b))
+	             : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *b, unsigned parity)
+{
+	unsigned done;
+	asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n}\n"
+	             : "=r"(done)
+	             : "r"(smem_u32(b)), "r"(parity)
+	             : "memory");
+	return done != 0;
+}
+
+__device__ __forceinline__ void mbar_wait(uint64_t *b, unsigned parity)
+{
+	for (unsigned i = 0; !mbar_try_wait(b, parity); ++i) {
+		if (i == kWaitLimit) {
+			atomicAdd(&g_wait_timeouts, 1u);
+			break;
+		}
+	}
+}
+
+// One warp: the new lines [a, b) of a group (line a into ring slot sa) and
+// its vertical fragments, all completing on barrier bar. Lines below the
+// plane are not copied (their taps are zero; the ring keeps finite stale
+// samples there), nor are columns right of it; a tail that is not a whole
+// 16-byte chunk is copied with plain loads.
+__device__ __forceinline__ void issue_group(const Item &it, int a, int b, char *ring, int R, int sa, int P,
+                                            const void *vsrc, void *vslot, unsigned vbytes, uint64_t *bar,
+                                            int nbulk, int tail_hi)
+{
+	const int lane = threadIdx.x & 31;
+	const int nvalid = max(0, min(b, it.src_h) - a);
+	if (lane == 0) {
+		mbar_expect_tx(bar, static_cast<unsigned>(nvalid * nbulk * 2) + vbytes);
+		bulk_copy(vslot, vsrc, vbytes, bar);
+	}
+	for (int i = lane; i < nvalid; i += 32) {
+		const int y = a + i;
+		char *dst = ring + wrap(sa + i, R) * P;
+		const uint16_t *row = reinterpret_cast<const uint16_t *>(it.src + static_cast<ptrdiff_t>(y) * it.src_stride);
+		if (nbulk)
+			bulk_copy(dst, row + it.xlo, static_cast<unsigned>(nbulk * 2), bar);
+		if (it.xlo + nbulk < tail_hi) {
+			for (int x = it.xlo + nbulk; x < tail_hi; ++x)
+				reinterpret_cast<uint16_t *>(dst)[x - it.xlo] = __ldg(row + x);
+			// these generic writes precede later bulk copies into the same bytes
+			asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
 		}
 	}
 }
@@ -279,12 +341,12 @@ __device__ __forceinline__ void tile_pass(const Item &it, const char *ring, int 
 #pragma unroll
 			for (int ks = 0; ks < KH; ++ks) {
 				if (top) {
-					const uint32_t b0 = *reinterpret_cast<const uint32_t *>(r0 + ks * 32);
-					const uint32_t b1 = *reinterpret_cast<const uint32_t *>(r0 + ks * 32 + 16);
+					const uint32_t b0 = centre(*reinterpret_cast<const uint32_t *>(r0 + ks * 32), it.bias_h2);
+					const uint32_t b1 = centre(*reinterpret_cast<const uint32_t *>(r0 + ks * 32 + 16), it.bias_h2);
 					dh0.mma(ah[ks][0], ah[ks][1], b0, b1);
 				}
-				const uint32_t b2 = *reinterpret_cast<const uint32_t *>(r1 + ks * 32);
-				const uint32_t b3 = *reinterpret_cast<const uint32_t *>(r1 + ks * 32 + 16);
+				const uint32_t b2 = centre(*reinterpret_cast<const uint32_t *>(r1 + ks * 32), it.bias_h2);
+				const uint32_t b3 = centre(*reinterpret_cast<const uint32_t *>(r1 + ks * 32 + 16), it.bias_h2);
 				dh1.mma(ah[ks][0], ah[ks][1], b2, b3);
 			}
 			// Dh (out col gid / gid+8, lines 2tig..) -> V operands (k = lines, n = out col)
@@ -332,6 +394,10 @@ __device__ __forceinline__ void tile_pass(const Item &it, const char *ring, int 
 			for (int kv = 0; kv < KV; ++kv) {
 				uint32_t b0, b1, b2, b3;
 				ldsm_x4_trans(b0, b1, b2, b3, ring + wrap(slot + 16 * kv + krow, IR) * P + coff + ks * 32);
+				b0 = centre(b0, it.bias_h2);
+				b1 = centre(b1, it.bias_h2);
+				b2 = centre(b2, it.bias_h2);
+				b3 = centre(b3, it.bias_h2);
 				dv0.mma(av[kv][0], av[kv][1], b0, b1);
 				dv1.mma(av[kv][0], av[kv][1], b2, b3);
 			}
@@ -394,10 +460,21 @@ chain_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 	char *st_addr = stage + (((lane >> 4) << 3) + (lane & 7)) * kStageBytes + ((lane >> 3) & 1) * 16;
 	const char *ld_addr = stage + (lane >> 1) * kStageBytes + (lane & 1) * 16;
 
+	uint64_t *bars = reinterpret_cast<uint64_t *>(smem + L.bar_off);
+	const int S = L.depth + 2;  // barriers (and fragment slots) in rotation
+
 	// lines never written by a load still hold finite values
 	for (int i = threadIdx.x; i < L.in_rows * P / 16; i += kThreads)
 		reinterpret_cast<float4 *>(ring)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+	if (threadIdx.x == 0) {
+		for (int i = 0; i < S; ++i)
+			mbar_init(bars + i, 1);
+		asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+	}
+	asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
 	__syncthreads();
+	int issue_bar = 0, wait_bar = 0;          // next barrier to arm / to wait on
+	unsigned issue_par = 0, wait_par = 0;     // their phase parities
 
 	for (int t = blockIdx.x; t < total_items; t += gridDim.x) {
 		const FusedJob *Jp = jobs ? &jobs[find_job(jobs, num_jobs, t)] : &single;
@@ -426,47 +503,62 @@ chain_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 
 		const int D = it.depth;
 		const int ngroups = it.g_end - it.g_begin;
-		const int nslots = D + 2;
-		// prologue: groups 0 .. D-1 in flight, one commit group each
+		const bool bulk = it.vec_ok != 0;
+		// bulk copies: whole 16-byte chunks of [xlo, min(src_w, xlo + pxa)), the rest by plain loads
+		const int tail_hi = min(it.src_w, it.xlo + it.pxa);
+		const int nbulk = max(0, tail_hi - it.xlo) & ~7;
+		const char *vtab = reinterpret_cast<const char *>(Jp->v_dense);
 		int issued_hi = vb[0];
 		int issued_slot = wrap(vb[0] % IR, IR);
-		for (int k = 0; k < D; ++k) {
-			if (k < ngroups) {
-				const int hi = vb[k] + 16 * KV;
-				if (hi > issued_hi) {
-					load_lines(it, issued_hi, hi, ring, IR, issued_slot, P);
-					issued_slot = wrap(issued_slot + (hi - issued_hi), IR);
-					issued_hi = hi;
-				}
-				load_vfrag<KV>(*Jp, it.g_begin + k, vslots + k * kSlotBytes);
+		// group k: new lines up to vb[k] + 16 KV, fragments into slot k % S
+		auto issue = [&](int k) {
+			const int hi = vb[k] + 16 * KV;
+			const int a = issued_hi;
+			const int sa = issued_slot;
+			if (hi > issued_hi) {
+				issued_slot = wrap(issued_slot + (hi - issued_hi), IR);
+				issued_hi = hi;
 			}
-			cp_async_commit();
+			char *vslot = vslots + (k % S) * kSlotBytes;
+			const char *vsrc = vtab + static_cast<size_t>(it.g_begin + k) * kSlotBytes;
+			if (bulk) {
+				if (warp == (k & (kWarps - 1)))
+					issue_group(it, a, max(a, hi), ring, IR, sa, P, vsrc, vslot, kSlotBytes, bars + issue_bar, nbulk,
+					            tail_hi);
+				if (++issue_bar == S) {
+					issue_bar = 0;
+					issue_par ^= 1u;
+				}
+			} else {
+				if (hi > a)
+					load_lines(it, a, hi, ring, IR, sa, P);
+				for (int i = threadIdx.x; i < KV * 2 * 32; i += kThreads)
+					cp_async16(vslot + i * 16, vsrc + i * 16, 16);
+			}
+		};
+
+		// prologue: groups 0 .. D-1 in flight
+		for (int k = 0; k < D; ++k) {
+			if (k < ngroups)
+				issue(k);
+			if (!bulk)
+				cp_async_commit();
 		}
 
 		int cur_vb = vb[0];
 		int cur_slot = wrap(cur_vb % IR, IR);
-		int conv_hi = vb[0], conv_slot = cur_slot;
-		int fetch_slot = D % nslots, read_slot = 0;
 		for (int k = 0; k < ngroups; ++k) {
-			if (k + D < ngroups) {
-				const int hi = vb[k + D] + 16 * KV;
-				if (hi > issued_hi) {
-					load_lines(it, issued_hi, hi, ring, IR, issued_slot, P);
-					issued_slot = wrap(issued_slot + (hi - issued_hi), IR);
-					issued_hi = hi;
+			if (k + D < ngroups)
+				issue(k + D);
+			if (bulk) {
+				mbar_wait(bars + wait_bar, wait_par);
+				if (++wait_bar == S) {
+					wait_bar = 0;
+					wait_par ^= 1u;
 				}
-				load_vfrag<KV>(*Jp, it.g_begin + k + D, vslots + fetch_slot * kSlotBytes);
-			}
-			cp_async_commit();
-			fetch_slot = fetch_slot + 1 == nslots ? 0 : fetch_slot + 1;
-			wait_groups(D);
-			{
-				const int hi = vb[k] + 16 * KV;
-				if (hi > conv_hi) {
-					convert_lines(it, conv_hi, hi, ring, IR, conv_slot, P);
-					conv_slot = wrap(conv_slot + (hi - conv_hi), IR);
-					conv_hi = hi;
-				}
+			} else {
+				cp_async_commit();
+				wait_groups(D);
 			}
 			__syncthreads();
 
@@ -475,7 +567,7 @@ chain_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 			cur_slot = wrap(cur_slot + (vbk - cur_vb), IR);
 			cur_vb = vbk;
 			if (tile0 * kTileW < it.dst_w) {
-				const uint4 *avs = reinterpret_cast<const uint4 *>(vslots + read_slot * kSlotBytes) + lane;
+				const uint4 *avs = reinterpret_cast<const uint4 *>(vslots + (k % S) * kSlotBytes) + lane;
 				uint4 av[KV][2];
 #pragma unroll
 				for (int kv = 0; kv < KV; ++kv) {
@@ -488,7 +580,6 @@ chain_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 						tile_pass<H_FIRST, KV, KH>(it, ring, IR, P, cur_slot, rel[j], ah[j], av, st_addr, ld_addr,
 						                           (it.g_begin + k) * 16, (tile0 + j) * kTileW, carry[j], reuse);
 			}
-			read_slot = read_slot + 1 == nslots ? 0 : read_slot + 1;
 		}
 		cp_async_wait<0>();
 		__syncthreads();  // the next item rewrites the group bases and the ring
