@@ -163,7 +163,7 @@ bool plan_chain(const FilterTable &first, const FilterTable &second, bool h_firs
 		max_pxa = std::max(max_pxa, (hi - lo + 7) & ~7);
 	}
 
-	// prefetch depth: about 16 KB of source lines in flight per CTA
+	// prefetch depth: about 32 KB of source lines in flight per CTA
 	auto hi_of = [&](int g) { return gbase[std::min(g, groups - 1)] + 16 * KV; };
 	int new_lines = 1;
 	for (int g = 1; g < groups; ++g)
@@ -173,7 +173,7 @@ bool plan_chain(const FilterTable &first, const FilterTable &second, bool h_firs
 	p = FusedPlan{};
 	FusedJob &J = p.job;
 	bool fits = false;
-	for (int ahead = std::max(1, std::min(8, (16 * 1024 + group_bytes - 1) / group_bytes)); ahead >= 1; --ahead) {
+	for (int ahead = std::max(1, std::min(8, (32 * 1024 + group_bytes - 1) / group_bytes)); ahead >= 1; --ahead) {
 		// a warp may read group g while loads of group g + 1 + ahead land
 		int ring = 16 * KV;
 		for (int g = 0; g < groups; ++g)
@@ -296,7 +296,8 @@ SmemLayout chain_layout(const FusedPlan *const *plans, int n)
 	off += a16(static_cast<size_t>(depth + 2) * kv * 2 * 32 * 16);
 	L.tile_off = off;
 	L.tile_pitch = chain_detail::kStageBytes / 2;
-	off += a16(static_cast<size_t>(chain_detail::kWarps) * 16 * chain_detail::kStageBytes);
+	off += a16(static_cast<size_t>(chain_detail::kWarps) * chain_detail::kMaxTilesPerWarp * 16 *
+	           chain_detail::kStageBytes);
 	L.vbase_off = off;
 	off += a16(static_cast<size_t>(seg_groups) * 4);
 	L.bar_off = off;

@@ -48,6 +48,7 @@ __host__ __device__ constexpr int tiles_per_warp(int kv, int kh)
 	return (kv + kh <= 3 || kh == 1) ? 2 : 1;
 }
 constexpr int kStageBytes = 48;            // staged row: 16 u16 + pad (stmatrix rows without bank conflicts)
+constexpr int kMaxTilesPerWarp = 2;
 
 __device__ __forceinline__ void stsm_x4(void *p, uint32_t r0, uint32_t r1, uint32_t r2, uint32_t r3)
 {
@@ -318,14 +319,15 @@ struct Carry {
 	uint32_t b[2];
 };
 
+// Both passes of one 16-column tile of one 16-row group; m: the four packed
+// 8x8 blocks of the result (row-major for H first, transposed for V first).
 template <bool H_FIRST, int KV, int KH>
-__device__ __forceinline__ void tile_pass(const Item &it, const char *ring, int IR, int P, int slot, int rel,
-                                          const uint4 (&ah)[KH][2], const uint4 (&av)[KV][2], char *st_addr,
-                                          const char *ld_addr, int row0, int col0, Carry &carry, bool reuse)
+__device__ __forceinline__ void tile_compute(const Item &it, const char *ring, int IR, int P, int slot, int rel,
+                                             const uint4 (&ah)[KH][2], const uint4 (&av)[KV][2], Carry &carry,
+                                             bool reuse, uint32_t (&m)[4])
 {
 	const int lane = threadIdx.x & 31;
 	const int gid = lane >> 2, tig = lane & 3;
-	uint32_t m0, m1, m2, m3;
 	if (H_FIRST) {
 		// H over the group's KV*16 lines: B = src[line gid (+8)][in cols 2tig (+8)]
 		uint32_t bv[KV][2][2];
@@ -373,11 +375,10 @@ __device__ __forceinline__ void tile_pass(const Item &it, const char *ring, int 
 			dv1.mma(av[kv][0], av[kv][1], bv[kv][1][0], bv[kv][1][1]);
 		}
 		// (out row gid / gid+8, out cols 2tig..): row-major 8x8 blocks
-		m0 = pack(dv0, 0, it);
-		m1 = pack(dv1, 0, it);
-		m2 = pack(dv0, 2, it);
-		m3 = pack(dv1, 2, it);
-		stsm_x4(st_addr, m0, m1, m2, m3);
+		m[0] = pack(dv0, 0, it);
+		m[1] = pack(dv1, 0, it);
+		m[2] = pack(dv0, 2, it);
+		m[3] = pack(dv1, 2, it);
 	} else {
 		Acc dh0, dh1;  // out rows 0-7, 8-15
 		dh0.init();
@@ -410,14 +411,18 @@ __device__ __forceinline__ void tile_pass(const Item &it, const char *ring, int 
 			dh1.mma(ah[ks][0], ah[ks][1], h10, h11);
 		}
 		// (out col gid / gid+8, out rows 2tig..): transposed 8x8 blocks
-		m0 = pack(dh0, 0, it);
-		m1 = pack(dh0, 2, it);
-		m2 = pack(dh1, 0, it);
-		m3 = pack(dh1, 2, it);
-		stsm_x4_trans(st_addr, m0, m1, m2, m3);
+		m[0] = pack(dh0, 0, it);
+		m[1] = pack(dh0, 2, it);
+		m[2] = pack(dh1, 0, it);
+		m[3] = pack(dh1, 2, it);
 	}
-	__syncwarp();
-	// staged 16 x 16 tile -> destination, one 16-byte half row per lane
+}
+
+// A staged 16 x 16 tile -> destination rows row0.., columns col0..; one
+// 16-byte half row per lane.
+__device__ __forceinline__ void store_tile(const Item &it, const char *ld_addr, int row0, int col0)
+{
+	const int lane = threadIdx.x & 31;
 	const int row = row0 + (lane >> 1);
 	const int col = col0 + (lane & 1) * 8;
 	if (row < it.dst_h && col < it.dst_w) {
@@ -431,7 +436,6 @@ __device__ __forceinline__ void tile_pass(const Item &it, const char *ring, int 
 				d[e] = static_cast<uint16_t>(w[e >> 1] >> (16 * (e & 1)));
 		}
 	}
-	__syncwarp();
 }
 
 // Kernel. Shared memory (SmemLayout): ring of raw source lines (in_off,
@@ -450,7 +454,7 @@ chain_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 	char *vslots = smem + L.vcoef_off;
 	int *vb = reinterpret_cast<int *>(smem + L.vbase_off);
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-	char *stage = smem + L.tile_off + warp * 16 * kStageBytes;
+	char *stage = smem + L.tile_off + warp * kMaxTilesPerWarp * 16 * kStageBytes;
 	const int IR = L.in_rows;
 	const int P = L.pitch * 2;
 	constexpr int kSlotBytes = KV * 2 * 32 * 16;
@@ -574,11 +578,25 @@ chain_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 					av[kv][0] = avs[(kv * 2 + 0) * 32];
 					av[kv][1] = avs[(kv * 2 + 1) * 32];
 				}
+				// the tiles' products interleave; stores follow
+				uint32_t m[kTilesPerWarp][4];
+#pragma unroll
+				for (int j = 0; j < kTilesPerWarp; ++j)
+					tile_compute<H_FIRST, KV, KH>(it, ring, IR, P, cur_slot, rel[j], ah[j], av, carry[j], reuse, m[j]);
+#pragma unroll
+				for (int j = 0; j < kTilesPerWarp; ++j) {
+					char *sa = st_addr + j * 16 * kStageBytes;
+					if (H_FIRST)
+						stsm_x4(sa, m[j][0], m[j][1], m[j][2], m[j][3]);
+					else
+						stsm_x4_trans(sa, m[j][0], m[j][1], m[j][2], m[j][3]);
+				}
+				__syncwarp();
 #pragma unroll
 				for (int j = 0; j < kTilesPerWarp; ++j)
 					if ((tile0 + j) * kTileW < it.dst_w)
-						tile_pass<H_FIRST, KV, KH>(it, ring, IR, P, cur_slot, rel[j], ah[j], av, st_addr, ld_addr,
-						                           (it.g_begin + k) * 16, (tile0 + j) * kTileW, carry[j], reuse);
+						store_tile(it, ld_addr + j * 16 * kStageBytes, (it.g_begin + k) * 16, (tile0 + j) * kTileW);
+				__syncwarp();
 			}
 		}
 		cp_async_wait<0>();
