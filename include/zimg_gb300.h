@@ -234,13 +234,6 @@ ZG_API zg_error_code zg_batch_process_graph(zg_batch *b, void *tmp, zg_stream st
  * (optional) receives the number of jobs whose plan changed.
  */
 ZG_API zg_error_code zg_batch_autotune(zg_batch *b, zg_stream stream, unsigned *changed);
-/*
- * No counterpart in zimg: the number of bounded device-side waits that ran
- * out on the current device since the library was loaded. Kernels never spin
- * without a limit; a wait that runs out is counted here and the launch ends
- * with unspecified output instead of hanging. 0 in normal operation.
- */
-ZG_API zg_error_code zg_get_wait_timeouts(unsigned *count);
 /* Number of kernel launches one zg_batch_process issues. */
 ZG_API zg_error_code zg_batch_get_launch_count(const zg_batch *b, unsigned *out);
 

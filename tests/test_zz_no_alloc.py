@@ -86,11 +86,3 @@ def test_no_alloc_rejects_oversized_scratch(cuda):
     code, msg = capi.last_error()
     assert code == 1 and "static scratch" in msg
 
-
-def test_no_device_wait_ran_out(cuda):
-    """Collected last: no bounded device-side wait of any earlier GPU test ran out."""
-    import ctypes as C
-    from zimg_gb300 import capi
-    n = C.c_uint(123)
-    assert capi.load().zg_get_wait_timeouts(C.byref(n)) == 0
-    assert n.value == 0

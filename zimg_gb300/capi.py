@@ -112,7 +112,6 @@ SIGNATURES = [
     ("zg_batch_process_graph", C.c_int, [_P, _P, _P]),
     ("zg_batch_get_launch_count", C.c_int, [_P, C.POINTER(C.c_uint)]),
     ("zg_batch_autotune", C.c_int, [_P, _P, C.POINTER(C.c_uint)]),
-    ("zg_get_wait_timeouts", C.c_int, [C.POINTER(C.c_uint)]),
     ("zg_image_format_default", None, [C.POINTER(ImageFormat), C.c_uint]),
     ("zg_graph_builder_params_default", None, [C.POINTER(GraphBuilderParams), C.c_uint]),
     ("zg_graph_build", _P, [C.POINTER(ImageFormat), C.POINTER(ImageFormat), C.POINTER(GraphBuilderParams)]),

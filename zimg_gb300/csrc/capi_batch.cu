@@ -397,18 +397,6 @@ zg_error_code zg_batch_autotune(zg_batch *b, zg_stream stream, unsigned *changed
 	});
 }
 
-zg_error_code zg_get_wait_timeouts(unsigned *count)
-{
-	return guarded([&] {
-		if (!count)
-			throw Error(kErrIllegalArgument, "null pointer");
-		const unsigned n = chain_wait_timeouts();
-		if (n == ~0u)
-			throw Error(kErrUnknown, "cannot read the device wait counter");
-		*count = n;
-	});
-}
-
 zg_error_code zg_batch_get_launch_count(const zg_batch *b, unsigned *out)
 {
 	return guarded([&] {

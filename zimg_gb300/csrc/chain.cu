@@ -300,8 +300,6 @@ SmemLayout chain_layout(const FusedPlan *const *plans, int n)
 	           chain_detail::kStageBytes);
 	L.vbase_off = off;
 	off += a16(static_cast<size_t>(seg_groups) * 4);
-	L.bar_off = off;
-	off += a16(static_cast<size_t>(depth + 2) * 8);
 	L.ring_off = L.stage_off = L.i_off = L.htaps_off = L.hleft_off = off;
 	L.total_bytes = off;
 	return L;
@@ -346,14 +344,6 @@ const void *chain_kernel_ptr(int variant)
 int chain_threads()
 {
 	return chain_detail::kThreads;
-}
-
-unsigned chain_wait_timeouts()
-{
-	unsigned n = 0;
-	if (cudaMemcpyFromSymbol(&n, chain_detail::g_wait_timeouts, sizeof(n)) != cudaSuccess)
-		return ~0u;
-	return n;
 }
 
 cudaError_t launch_chain(int variant, const FusedJob *jobs, int num_jobs, int total_items, const SmemLayout &L, int grid,

@@ -16,10 +16,10 @@
 // layout of the B operand of the next product (k = 2tig, 2tig+1, n = gid), so
 // the first product's rounded results, converted to centred fp16 pairs, are
 // the second product's B fragments as they stand. Source lines stream
-// through one ring of raw u16 lines per CTA (bulk async copies completing on
-// mbarriers, or cp.async for unaligned planes; prefetched `depth` groups
-// ahead; one CTA barrier per group) and are centred to fp16 as they are read;
-// results leave through a per-warp staging tile (stmatrix) as 16-byte rows.
+// through one ring of raw u16 lines per CTA (cp.async, prefetched `depth`
+// groups ahead, one CTA barrier per group) and are centred to fp16 as they
+// are read; results leave through per-warp staging tiles (stmatrix) as
+// 16-byte rows.
 #pragma once
 
 #include "mma_kernel.cuh"
@@ -72,7 +72,7 @@ struct Item {
 	char *dst;
 	ptrdiff_t dst_stride;
 	int src_w, src_h, dst_w, dst_h, vec_ok;
-	int strip, c0, xlo, pxa;
+	int strip, c0, xlo;
 	int g_begin, g_end, depth;
 	// this thread's place in line copies: chunk q0 of line offset l0, then
 	// advance by (sl lines, sq chunks) per iteration
@@ -99,7 +99,6 @@ __device__ __forceinline__ Item make_item(const FusedJob &J, int t, int strip_ti
 	it.c0 = it.strip * strip_tiles * kTileW;
 	it.xlo = __ldg(J.win_col + 2 * it.strip);
 	const int pxa = (__ldg(J.win_col + 2 * it.strip + 1) - it.xlo + 7) & ~7;
-	it.pxa = pxa;
 	it.g_begin = seg * J.seg_groups;
 	it.g_end = min(J.groups, it.g_begin + J.seg_groups);
 	it.depth = J.depth;
@@ -148,89 +147,6 @@ __device__ __forceinline__ void load_lines(const Item &it, int a, int b, char *r
 __device__ __forceinline__ uint32_t centre(uint32_t q, uint32_t bias_h2)
 {
 	return u16x2_to_centred_h2(q, bias_h2);
-}
-
-// ------------------------------------------------ bulk copies, mbarriers --
-// Aligned planes: each source line of a group is one cp.async.bulk copy
-// (issued by one lane of one warp), completing on the group's mbarrier; the
-// consumers wait on that barrier's phase. Every wait is bounded: after
-// kWaitLimit polls it counts a timeout in g_wait_timeouts and goes on (the
-// results of that launch are then garbage, but the kernel ends).
-
-__device__ unsigned int g_wait_timeouts;
-constexpr unsigned kWaitLimit = 1u << 22;
-
-__device__ __forceinline__ unsigned smem_u32(const void *p)
-{
-	return static_cast<unsigned>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t *b, unsigned count)
-{
-	asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(b)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *b, unsigned bytes)
-{
-	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
-}
-
-__device__ __forceinline__ void bulk_copy(void *dst, const void *src, unsigned bytes, uint64_t *b)
-{
-	asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
-	                 smem_u32(dst)),
-	             "l"(src), "r"(bytes), "r"(smem_u32(b))
-	             : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *b, unsigned parity)
-{
-	unsigned done;
-	asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n}\n"
-	             : "=r"(done)
-	             : "r"(smem_u32(b)), "r"(parity)
-	             : "memory");
-	return done != 0;
-}
-
-__device__ __forceinline__ void mbar_wait(uint64_t *b, unsigned parity)
-{
-	for (unsigned i = 0; !mbar_try_wait(b, parity); ++i) {
-		if (i == kWaitLimit) {
-			atomicAdd(&g_wait_timeouts, 1u);
-			break;
-		}
-	}
-}
-
-// One warp: the new lines [a, b) of a group (line a into ring slot sa) and
-// its vertical fragments, all completing on barrier bar. Lines below the
-// plane are not copied (their taps are zero; the ring keeps finite stale
-// samples there), nor are columns right of it; a tail that is not a whole
-// 16-byte chunk is copied with plain loads.
-__device__ __forceinline__ void issue_group(const Item &it, int a, int b, char *ring, int R, int sa, int P,
-                                            const void *vsrc, void *vslot, unsigned vbytes, uint64_t *bar,
-                                            int nbulk, int tail_hi)
-{
-	const int lane = threadIdx.x & 31;
-	const int nvalid = max(0, min(b, it.src_h) - a);
-	if (lane == 0) {
-		mbar_expect_tx(bar, static_cast<unsigned>(nvalid * nbulk * 2) + vbytes);
-		bulk_copy(vslot, vsrc, vbytes, bar);
-	}
-	for (int i = lane; i < nvalid; i += 32) {
-		const int y = a + i;
-		char *dst = ring + wrap(sa + i, R) * P;
-		const uint16_t *row = reinterpret_cast<const uint16_t *>(it.src + static_cast<ptrdiff_t>(y) * it.src_stride);
-		if (nbulk)
-			bulk_copy(dst, row + it.xlo, static_cast<unsigned>(nbulk * 2), bar);
-		if (it.xlo + nbulk < tail_hi) {
-			for (int x = it.xlo + nbulk; x < tail_hi; ++x)
-				reinterpret_cast<uint16_t *>(dst)[x - it.xlo] = __ldg(row + x);
-			// these generic writes precede later bulk copies into the same bytes
-			asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-		}
-	}
 }
 
 // Vertical tap fragments of group g into a shared slot.
@@ -464,21 +380,12 @@ chain_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 	char *st_addr = stage + (((lane >> 4) << 3) + (lane & 7)) * kStageBytes + ((lane >> 3) & 1) * 16;
 	const char *ld_addr = stage + (lane >> 1) * kStageBytes + (lane & 1) * 16;
 
-	uint64_t *bars = reinterpret_cast<uint64_t *>(smem + L.bar_off);
-	const int S = L.depth + 2;  // barriers (and fragment slots) in rotation
+	const int S = L.depth + 2;  // fragment slots in rotation
 
 	// lines never written by a load still hold finite values
 	for (int i = threadIdx.x; i < L.in_rows * P / 16; i += kThreads)
 		reinterpret_cast<float4 *>(ring)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-	if (threadIdx.x == 0) {
-		for (int i = 0; i < S; ++i)
-			mbar_init(bars + i, 1);
-		asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-	}
-	asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
 	__syncthreads();
-	int issue_bar = 0, wait_bar = 0;          // next barrier to arm / to wait on
-	unsigned issue_par = 0, wait_par = 0;     // their phase parities
 
 	for (int t = blockIdx.x; t < total_items; t += gridDim.x) {
 		const FusedJob *Jp = jobs ? &jobs[find_job(jobs, num_jobs, t)] : &single;
@@ -507,46 +414,28 @@ chain_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 
 		const int D = it.depth;
 		const int ngroups = it.g_end - it.g_begin;
-		const bool bulk = it.vec_ok != 0;
-		// bulk copies: whole 16-byte chunks of [xlo, min(src_w, xlo + pxa)), the rest by plain loads
-		const int tail_hi = min(it.src_w, it.xlo + it.pxa);
-		const int nbulk = max(0, tail_hi - it.xlo) & ~7;
 		const char *vtab = reinterpret_cast<const char *>(Jp->v_dense);
 		int issued_hi = vb[0];
 		int issued_slot = wrap(vb[0] % IR, IR);
 		// group k: new lines up to vb[k] + 16 KV, fragments into slot k % S
 		auto issue = [&](int k) {
 			const int hi = vb[k] + 16 * KV;
-			const int a = issued_hi;
-			const int sa = issued_slot;
 			if (hi > issued_hi) {
+				load_lines(it, issued_hi, hi, ring, IR, issued_slot, P);
 				issued_slot = wrap(issued_slot + (hi - issued_hi), IR);
 				issued_hi = hi;
 			}
 			char *vslot = vslots + (k % S) * kSlotBytes;
 			const char *vsrc = vtab + static_cast<size_t>(it.g_begin + k) * kSlotBytes;
-			if (bulk) {
-				if (warp == (k & (kWarps - 1)))
-					issue_group(it, a, max(a, hi), ring, IR, sa, P, vsrc, vslot, kSlotBytes, bars + issue_bar, nbulk,
-					            tail_hi);
-				if (++issue_bar == S) {
-					issue_bar = 0;
-					issue_par ^= 1u;
-				}
-			} else {
-				if (hi > a)
-					load_lines(it, a, hi, ring, IR, sa, P);
-				for (int i = threadIdx.x; i < KV * 2 * 32; i += kThreads)
-					cp_async16(vslot + i * 16, vsrc + i * 16, 16);
-			}
+			for (int i = threadIdx.x; i < KV * 2 * 32; i += kThreads)
+				cp_async16(vslot + i * 16, vsrc + i * 16, 16);
 		};
 
-		// prologue: groups 0 .. D-1 in flight
+		// prologue: groups 0 .. D-1 in flight, one commit group each
 		for (int k = 0; k < D; ++k) {
 			if (k < ngroups)
 				issue(k);
-			if (!bulk)
-				cp_async_commit();
+			cp_async_commit();
 		}
 
 		int cur_vb = vb[0];
@@ -554,16 +443,8 @@ chain_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 		for (int k = 0; k < ngroups; ++k) {
 			if (k + D < ngroups)
 				issue(k + D);
-			if (bulk) {
-				mbar_wait(bars + wait_bar, wait_par);
-				if (++wait_bar == S) {
-					wait_bar = 0;
-					wait_par ^= 1u;
-				}
-			} else {
-				cp_async_commit();
-				wait_groups(D);
-			}
+			cp_async_commit();
+			wait_groups(D);
 			__syncthreads();
 
 			const int vbk = vb[k];

@@ -89,7 +89,6 @@ struct SmemLayout {
 	int ring_rows, in_rows, stage_rows, seg_groups, step_groups;
 	int depth;              // steps of lines in flight ahead of the computing step
 	int tile_off, tile_pitch;  // tensor-core kernel: staged output rows (packed u16)
-	int bar_off;            // chained kernel: depth + 2 mbarriers (bulk copies of source lines)
 };
 
 // Host-side plan of one fused job: device tables plus a FusedJob template.
@@ -155,10 +154,6 @@ bool plan_chain(const FilterTable &first, const FilterTable &second, bool h_firs
 SmemLayout chain_layout(const FusedPlan *const *plans, int n);
 const void *chain_kernel_ptr(int variant);
 int chain_threads();
-// Bounded waits of the chained kernel that ran out since the library was
-// loaded on the current device (each one is a kernel that produced garbage
-// instead of hanging); 0 in normal operation.
-unsigned chain_wait_timeouts();
 cudaError_t launch_chain(int variant, const FusedJob *jobs, int num_jobs, int total_items, const SmemLayout &L, int grid,
                          const FusedJob &single, cudaStream_t stream);
 // Work items that fill the current device once (SMs x resident CTAs).
