@@ -339,6 +339,44 @@ def test_batch_matches_single(cuda, oracle):
             np.testing.assert_array_equal(to_host(d, np.uint16), w, err_msg=mode)
 
 
+def test_batch_identity_planes_copied(cuda):
+    """Identity conversions in a batch (no pass, resize.cpp:43-47) go through
+    one batched copy launch: exact copies for aligned and unaligned planes,
+    u16 and f32, next to a real conversion."""
+    import torch
+    import zimg_gb300 as zg
+    rng = np.random.default_rng(6)
+    cases = [((48, 64), np.uint16, 0, 0), ((37, 53), np.uint16, 3, 1), ((40, 96), np.float32, 0, 0),
+             ((17, 33), np.float32, 1, 1)]
+    convs, srcs, dsts, wants = [], [], [], []
+    for (h, w), dt, pad, off in cases:
+        src = (rng.integers(0, 1024, size=(h, w), dtype=np.uint16) if dt == np.uint16
+               else rng.random((h, w), dtype=np.float32))
+        ptype = "word" if dt == np.uint16 else "float"
+        convs.append(zg.ResizeConversion(w, h, ptype).set_depth(10 if dt == np.uint16 else 32)
+                     .set_filter("spline36").set_dst_width(w).set_dst_height(h))
+        s = empty(h, w, dt, pad, off)
+        s.copy_(to_dev(src))
+        srcs.append(s)
+        dsts.append(empty(h, w, dt, pad, off))
+        wants.append(src)
+    src = rng.integers(0, 1024, size=(30, 40), dtype=np.uint16)
+    convs.append(zg.ResizeConversion(40, 30, "word").set_depth(10).set_filter("spline36").set_dst_width(80)
+                 .set_dst_height(60))
+    srcs.append(to_dev(src))
+    dsts.append(empty(60, 80, np.uint16))
+    b = zg.Batch(convs)
+    b.set_io(srcs, dsts)
+    assert b.launch_count == 2  # one copy launch for the four identity planes, one fused launch
+    for mode in ("plain", "graph"):
+        for d in dsts:
+            d.zero_()
+        (b.process if mode == "plain" else b.process_graph)()
+        torch.cuda.synchronize()
+        for d, w, (shape, dt, pad, off) in zip(dsts, wants, cases):
+            np.testing.assert_array_equal(to_host(d, dt), w, err_msg=(mode, shape, pad, off))
+
+
 def test_batch_autotune_keeps_results(cuda, oracle):
     """The autotuner may swap plans per job kind; u16 outputs stay bit-exact
     and f32 outputs stay within the FP64 error bound, in plain and graph

@@ -2,8 +2,9 @@
 //
 // Fused jobs are grouped by kernel variant; each group runs as ONE persistent
 // launch over the concatenated tile lists of its jobs (a device table of
-// FusedJob entries, one per plane). Jobs that cannot be fused (wide filters,
-// single passes, plain copies) run through their own conversion.
+// FusedJob entries, one per plane). Identity conversions are copied by one
+// batched copy launch. Jobs that cannot be fused (wide filters, single
+// passes) run through their own conversion.
 #include "capi_common.h"
 
 #include <algorithm>
@@ -31,6 +32,11 @@ struct zg_batch {
 	std::vector<Group> groups;
 	std::vector<FusedJob> table_host;
 	DeviceBuffer table_dev;
+	// identity conversions: one batched copy launch
+	std::vector<int> copy_jobs;
+	std::vector<PlaneCopy> copy_host;
+	DeviceBuffer copy_dev;
+	unsigned long long copy_chunks = 0;
 	cudaGraphExec_t graph = nullptr;
 	cudaStream_t graph_stream = nullptr;
 	void *graph_tmp = nullptr;
@@ -63,8 +69,12 @@ void batch_launch(const zg_batch *b, void *tmp, cudaStream_t st)
 		cuda_check(launch_fused(g.variant, table + g.first, g.count, g.tiles, g.layout, g.grid, unused, st),
 		           "fused batch launch");
 	}
+	if (!b->copy_jobs.empty())
+		cuda_check(launch_plane_copies(static_cast<const PlaneCopy *>(b->copy_dev.get()),
+		                               static_cast<int>(b->copy_jobs.size()), b->copy_chunks, st),
+		           "batch plane copies");
 	for (size_t i = 0; i < b->jobs.size(); ++i) {
-		if (b->table_index[i] >= 0)
+		if (b->table_index[i] >= 0 || b->jobs[i]->num_passes == 0)
 			continue;
 		const zg_batch_io &io = b->io[i];
 		void *t = b->tmp_size ? static_cast<char *>(tmp) + b->tmp_offset[i] : nullptr;
@@ -123,6 +133,14 @@ void regroup(zg_batch *b)
 	}
 	if (!b->table_host.empty())
 		b->table_dev.reset(b->table_host.size() * sizeof(FusedJob));
+	b->copy_jobs.clear();
+	for (unsigned i = 0; i < num_jobs; ++i)
+		if (b->jobs[i]->num_passes == 0)
+			b->copy_jobs.push_back(static_cast<int>(i));
+	b->copy_host.assign(b->copy_jobs.size(), PlaneCopy{});
+	b->copy_dev.release();
+	if (!b->copy_jobs.empty())
+		b->copy_dev.reset(b->copy_jobs.size() * sizeof(PlaneCopy));
 }
 
 // Plane pointers of the fused jobs into the device table (ordered on st; the
@@ -135,11 +153,35 @@ void upload_io(zg_batch *b, cudaStream_t st)
 			fused_set_io(b->table_host[b->table_index[i]], x.src, x.src_stride, x.dst, x.dst_stride);
 		}
 	}
-	if (!b->table_host.empty()) {
+	b->copy_chunks = 0;
+	for (size_t c = 0; c < b->copy_jobs.size(); ++c) {
+		const zg_resize *r = b->jobs[b->copy_jobs[c]];
+		const zg_batch_io &x = b->io[b->copy_jobs[c]];
+		PlaneCopy &p = b->copy_host[c];
+		p.src = x.src;
+		p.src_stride = x.src_stride;
+		p.dst = x.dst;
+		p.dst_stride = x.dst_stride;
+		p.row_bytes = r->params.dst_width * bytes_of(r->sample);
+		p.rows = r->params.dst_height;
+		auto al = [](const void *q, ptrdiff_t s, unsigned a) {
+			return reinterpret_cast<uintptr_t>(q) % a == 0 && s % a == 0;
+		};
+		const bool v16 = al(x.src, x.src_stride, 16) && al(x.dst, x.dst_stride, 16) && p.row_bytes % 16 == 0;
+		const bool v4 = al(x.src, x.src_stride, 4) && al(x.dst, x.dst_stride, 4) && p.row_bytes % 4 == 0;
+		p.unit = v16 ? 16 : (v4 ? 4 : 2);
+		p.chunks_per_row = p.row_bytes / p.unit;
+		p.chunk_begin = b->copy_chunks;
+		b->copy_chunks += static_cast<unsigned long long>(p.chunks_per_row) * p.rows;
+	}
+	if (!b->copy_host.empty())
+		cuda_check(cudaMemcpyAsync(b->copy_dev.get(), b->copy_host.data(), b->copy_host.size() * sizeof(PlaneCopy),
+		                           cudaMemcpyHostToDevice, st), "batch io upload");
+	if (!b->table_host.empty())
 		cuda_check(cudaMemcpyAsync(b->table_dev.get(), b->table_host.data(), b->table_host.size() * sizeof(FusedJob),
 		                           cudaMemcpyHostToDevice, st), "batch io upload");
+	if (!b->table_host.empty() || !b->copy_host.empty())
 		cuda_check(cudaStreamSynchronize(st), "batch io upload");
-	}
 }
 
 // How a conversion runs, for the autotuner's de-duplication of candidates.
@@ -402,7 +444,7 @@ zg_error_code zg_batch_get_launch_count(const zg_batch *b, unsigned *out)
 	return guarded([&] {
 		if (!b || !out)
 			throw Error(kErrIllegalArgument, "null pointer");
-		unsigned n = static_cast<unsigned>(b->groups.size());
+		unsigned n = static_cast<unsigned>(b->groups.size()) + (b->copy_jobs.empty() ? 0u : 1u);
 		for (size_t i = 0; i < b->jobs.size(); ++i) {
 			if (b->table_index[i] >= 0)
 				continue;

@@ -67,6 +67,24 @@ void build_wide_tables(const float *f32, const unsigned *left, unsigned width, u
 
 cudaError_t launch_wide(const PassLaunch &l, cudaStream_t stream);
 
+// Planes that a batch copies unchanged (conversions with no pass,
+// resize.cpp:43-47): one launch for all of them. Each plane is split into
+// `unit`-byte chunks (16 when both planes and strides allow it, else the
+// sample size); chunk_begin is the plane's first chunk in the launch.
+struct PlaneCopy {
+	const void *src;
+	ptrdiff_t src_stride;
+	void *dst;
+	ptrdiff_t dst_stride;
+	unsigned row_bytes;
+	unsigned rows;
+	unsigned unit;
+	unsigned chunks_per_row;
+	unsigned long long chunk_begin;
+};
+
+cudaError_t launch_plane_copies(const PlaneCopy *table, int n, unsigned long long total_chunks, cudaStream_t stream);
+
 cudaError_t launch_pass(const PassLaunch &l, cudaStream_t stream);
 
 } // namespace zg
