@@ -74,9 +74,11 @@ struct Item {
 	int src_w, src_h, dst_w, dst_h, vec_ok;
 	int strip, c0, xlo;
 	int g_begin, g_end, depth;
-	// this thread's place in line copies: chunk q0 of line offset l0, then
-	// advance by (sl lines, sq chunks) per iteration
-	int chunks, q0, l0, sl, sq;
+	// this thread's part of line copies: 16-byte chunk q0 of lines l0,
+	// l0 + lpp, ... (threads with l0 >= lpp copy nothing); src_col: that
+	// chunk's first sample in row 0, col_bytes of it inside the plane
+	int q0, l0, lpp, gx, col_bytes;
+	const char *src_col;
 	float magic;
 	uint32_t pmax2, bias_h2;
 };
@@ -107,39 +109,42 @@ __device__ __forceinline__ Item make_item(const FusedJob &J, int t, int strip_ti
 	it.pmax2 = pm | (pm << 16);
 	const __half2 b = __floats2half2_rn(1024.0f + J.offset, 1024.0f + J.offset);
 	it.bias_h2 = *reinterpret_cast<const uint32_t *>(&b);
-	it.chunks = pxa / 8;
-	it.q0 = threadIdx.x % it.chunks;
-	it.l0 = threadIdx.x / it.chunks;
-	it.sl = kThreads / it.chunks;
-	it.sq = kThreads % it.chunks;
+	const int chunks = pxa / 8;
+	it.q0 = threadIdx.x % chunks;
+	it.l0 = threadIdx.x / chunks;
+	it.lpp = kThreads / chunks;
+	it.gx = it.xlo + it.q0 * 8;
+	const int n = max(0, min(8, it.src_w - it.gx));
+	it.col_bytes = n * 2;
+	it.src_col = n ? it.src + static_cast<ptrdiff_t>(it.gx) * 2 : it.src;
 	return it;
 }
 
 // Source lines [a, b) of the strip (raw u16, zeros outside the plane) into
-// ring slots; line a goes to slot sa.
+// ring slots; line a goes to slot sa. b - a is less than the ring size R.
 __device__ __forceinline__ void load_lines(const Item &it, int a, int b, char *ring, int R, int sa, int pitch_bytes)
 {
-	int y = a + it.l0, q = it.q0;
-	for (; y < b;) {
-		const bool row_ok = y < it.src_h;
-		const char *row = it.src + static_cast<ptrdiff_t>(row_ok ? y : 0) * it.src_stride;
-		char *srow = ring + wrap(sa + (y - a), R) * pitch_bytes;
-		const int gx = it.xlo + q * 8;
-		if (it.vec_ok) {
-			const int n = row_ok ? max(0, min(8, it.src_w - gx)) : 0;
-			cp_async16(srow + q * 16, n ? row + static_cast<ptrdiff_t>(gx) * 2 : it.src, n * 2);
-		} else {
-			uint16_t *d = reinterpret_cast<uint16_t *>(srow + q * 16);
+	int y = a + it.l0;
+	if (it.l0 >= it.lpp || y >= b)
+		return;
+	int slot = wrap(sa + it.l0, R);
+	if (it.vec_ok) {
+		const char *src = it.src_col + static_cast<ptrdiff_t>(y) * it.src_stride;
+		const ptrdiff_t step = static_cast<ptrdiff_t>(it.lpp) * it.src_stride;
+		for (; y < b; y += it.lpp, src += step) {
+			const bool ok = y < it.src_h;
+			cp_async16(ring + slot * pitch_bytes + it.q0 * 16, ok ? src : it.src, ok ? it.col_bytes : 0);
+			slot = wrap(slot + it.lpp, R);
+		}
+	} else {
+		for (; y < b; y += it.lpp) {
+			const bool row_ok = y < it.src_h;
+			const uint16_t *row = reinterpret_cast<const uint16_t *>(it.src + static_cast<ptrdiff_t>(row_ok ? y : 0) * it.src_stride);
+			uint16_t *d = reinterpret_cast<uint16_t *>(ring + slot * pitch_bytes + it.q0 * 16);
 #pragma unroll
 			for (int e = 0; e < 8; ++e)
-				d[e] = (row_ok && gx + e < it.src_w) ? __ldg(reinterpret_cast<const uint16_t *>(row) + gx + e)
-				                                      : static_cast<uint16_t>(0);
-		}
-		q += it.sq;
-		y += it.sl;
-		if (q >= it.chunks) {
-			q -= it.chunks;
-			++y;
+				d[e] = (row_ok && it.gx + e < it.src_w) ? __ldg(row + it.gx + e) : static_cast<uint16_t>(0);
+			slot = wrap(slot + it.lpp, R);
 		}
 	}
 }
@@ -417,7 +422,8 @@ chain_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 		const char *vtab = reinterpret_cast<const char *>(Jp->v_dense);
 		int issued_hi = vb[0];
 		int issued_slot = wrap(vb[0] % IR, IR);
-		// group k: new lines up to vb[k] + 16 KV, fragments into slot k % S
+		// group k: new lines up to vb[k] + 16 KV, fragments into the next of S slots
+		int fetch_slot = 0, read_slot = 0;
 		auto issue = [&](int k) {
 			const int hi = vb[k] + 16 * KV;
 			if (hi > issued_hi) {
@@ -425,7 +431,8 @@ chain_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 				issued_slot = wrap(issued_slot + (hi - issued_hi), IR);
 				issued_hi = hi;
 			}
-			char *vslot = vslots + (k % S) * kSlotBytes;
+			char *vslot = vslots + fetch_slot * kSlotBytes;
+			fetch_slot = fetch_slot + 1 == S ? 0 : fetch_slot + 1;
 			const char *vsrc = vtab + static_cast<size_t>(it.g_begin + k) * kSlotBytes;
 			for (int i = threadIdx.x; i < KV * 2 * 32; i += kThreads)
 				cp_async16(vslot + i * 16, vsrc + i * 16, 16);
@@ -452,7 +459,7 @@ chain_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 			cur_slot = wrap(cur_slot + (vbk - cur_vb), IR);
 			cur_vb = vbk;
 			if (tile0 * kTileW < it.dst_w) {
-				const uint4 *avs = reinterpret_cast<const uint4 *>(vslots + (k % S) * kSlotBytes) + lane;
+				const uint4 *avs = reinterpret_cast<const uint4 *>(vslots + read_slot * kSlotBytes) + lane;
 				uint4 av[KV][2];
 #pragma unroll
 				for (int kv = 0; kv < KV; ++kv) {
@@ -479,6 +486,7 @@ chain_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 						store_tile(it, ld_addr + j * 16 * kStageBytes, (it.g_begin + k) * 16, (tile0 + j) * kTileW);
 				__syncwarp();
 			}
+			read_slot = read_slot + 1 == S ? 0 : read_slot + 1;
 		}
 		cp_async_wait<0>();
 		__syncthreads();  // the next item rewrites the group bases and the ring
