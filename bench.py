@@ -99,6 +99,36 @@ def workload(name: str, frames: int | None, seed: int):
     return jobs, cfg
 
 
+# ------------------------------------------------------------------ replicas --
+# Planes and frames are independent: N ranks are N replicas, each with its own
+# seeded batch; no data moves between ranks. Only the timing is reduced.
+
+def rank_workload(name: str, frames: int | None, rank: int):
+    """This rank's batch: the workload drawn with a per-rank seed."""
+    return workload(name, frames, seed=0x5EED0000 + rank)
+
+
+def _reduce(x: float, op) -> float:
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=op)
+    return float(t.item())
+
+
+def max_over_ranks(x: float) -> float:
+    import torch.distributed as dist
+    return _reduce(x, dist.ReduceOp.MAX)
+
+
+def sum_over_ranks(x: float) -> float:
+    import torch.distributed as dist
+    return _reduce(x, dist.ReduceOp.SUM)
+
+
 def job_bytes(j):
     bpe = 2 if j["ptype"] == "word" else 4
     return (j["sw"] * j["sh"] + j["dw"] * j["dh"]) * bpe
@@ -190,7 +220,7 @@ def run_ours(args):
     zbuild.build()
     zg.load()
 
-    jobs, cfg = workload(args.workload, args.frames, seed=0x5EED0000 + rank)
+    jobs, cfg = rank_workload(args.workload, args.frames, rank)
     if args.engine:
         for j in jobs:
             j["engine"] = args.engine
@@ -252,13 +282,10 @@ def run_ours(args):
         dist.barrier()
     t1 = time.time()
     sampler.stop()
-    ms = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(e0.elapsed_time(e1))
     ms_step = ms / args.steps
-    value = out_px * world * args.steps / (ms / 1e3) / 1e6
+    # whole-job throughput: every rank's output samples over the slowest rank's time
+    value = sum_over_ranks(out_px) * args.steps / (ms / 1e3) / 1e6
 
     # ---- end to end through the public API with host buffers ----
     e2e = None
@@ -292,11 +319,8 @@ def run_ours(args):
         e_px = sum(jobs[i]["dw"] * jobs[i]["dh"] for i in range(n_e2e))
         h2d = sum(jobs[i]["sw"] * jobs[i]["sh"] * (2 if jobs[i]["ptype"] == "word" else 4) for i in range(n_e2e))
         d2h = sum(jobs[i]["dw"] * jobs[i]["dh"] * (2 if jobs[i]["ptype"] == "word" else 4) for i in range(n_e2e))
-        if world > 1:
-            t = torch.tensor([e_ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e_ms = float(t.item())
-        e2e = {"value": round(e_px * world / (e_ms / 1e3) / 1e6, 3), "unit": "Mpixel/s",
+        e_ms = max_over_ranks(e_ms)
+        e2e = {"value": round(sum_over_ranks(e_px) / (e_ms / 1e3) / 1e6, 3), "unit": "Mpixel/s",
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "planes_per_step": n_e2e}
 
     peak, peak_kind = load_peaks()
