@@ -9,6 +9,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <functional>
 #include <map>
 
 using namespace zg;
@@ -40,11 +41,22 @@ struct zg_batch {
 	cudaGraphExec_t graph = nullptr;
 	cudaStream_t graph_stream = nullptr;
 	void *graph_tmp = nullptr;
+	// independent launches (variant groups, the copy launch, unfused jobs) run
+	// concurrently on side streams forked from and joined to the caller's
+	mutable std::vector<cudaStream_t> side;
+	mutable std::vector<cudaEvent_t> joins;
+	mutable cudaEvent_t fork = nullptr;
 
 	~zg_batch()
 	{
 		if (graph)
 			cudaGraphExecDestroy(graph);
+		for (cudaStream_t s : side)
+			cudaStreamDestroy(s);
+		for (cudaEvent_t e : joins)
+			cudaEventDestroy(e);
+		if (fork)
+			cudaEventDestroy(fork);
 		for (auto *j : jobs)
 			zg_resize_free(j);
 	}
@@ -59,29 +71,64 @@ void rethrow_last(zg_error_code rc)
 	throw Error(rc, msg);
 }
 
+constexpr size_t kSideStreams = 4;
+
 void batch_launch(const zg_batch *b, void *tmp, cudaStream_t st)
 {
 	if (b->io.size() != b->jobs.size())
 		throw Error(kErrLogic, "zg_batch_set_io was not called");
 	const FusedJob *table = static_cast<const FusedJob *>(b->table_dev.get());
+	std::vector<std::function<void(cudaStream_t)>> work;
 	for (const auto &g : b->groups) {
-		FusedJob unused{};
-		cuda_check(launch_fused(g.variant, table + g.first, g.count, g.tiles, g.layout, g.grid, unused, st),
-		           "fused batch launch");
+		work.push_back([&g, table](cudaStream_t s) {
+			FusedJob unused{};
+			cuda_check(launch_fused(g.variant, table + g.first, g.count, g.tiles, g.layout, g.grid, unused, s),
+			           "fused batch launch");
+		});
 	}
-	if (!b->copy_jobs.empty())
-		cuda_check(launch_plane_copies(static_cast<const PlaneCopy *>(b->copy_dev.get()),
-		                               static_cast<int>(b->copy_jobs.size()), b->copy_chunks, st),
-		           "batch plane copies");
+	if (!b->copy_jobs.empty()) {
+		work.push_back([b](cudaStream_t s) {
+			cuda_check(launch_plane_copies(static_cast<const PlaneCopy *>(b->copy_dev.get()),
+			                               static_cast<int>(b->copy_jobs.size()), b->copy_chunks, s),
+			           "batch plane copies");
+		});
+	}
 	for (size_t i = 0; i < b->jobs.size(); ++i) {
 		if (b->table_index[i] >= 0 || b->jobs[i]->num_passes == 0)
 			continue;
-		const zg_batch_io &io = b->io[i];
-		void *t = b->tmp_size ? static_cast<char *>(tmp) + b->tmp_offset[i] : nullptr;
-		zg_error_code rc = zg_resize_process(b->jobs[i], io.src, io.src_stride, io.dst, io.dst_stride, t,
-		                                     reinterpret_cast<zg_stream>(st));
-		if (rc != ZG_ERROR_SUCCESS)
-			rethrow_last(rc);
+		work.push_back([b, i, tmp](cudaStream_t s) {
+			const zg_batch_io &io = b->io[i];
+			void *t = b->tmp_size ? static_cast<char *>(tmp) + b->tmp_offset[i] : nullptr;
+			zg_error_code rc = zg_resize_process(b->jobs[i], io.src, io.src_stride, io.dst, io.dst_stride, t,
+			                                     reinterpret_cast<zg_stream>(s));
+			if (rc != ZG_ERROR_SUCCESS)
+				rethrow_last(rc);
+		});
+	}
+	if (work.size() <= 1) {
+		for (auto &w : work)
+			w(st);
+		return;
+	}
+	const size_t n = std::min(work.size(), kSideStreams);
+	while (b->side.size() < n) {
+		cudaStream_t s = nullptr;
+		cudaEvent_t e = nullptr;
+		cuda_check(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "side stream");
+		b->side.push_back(s);
+		cuda_check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
+		b->joins.push_back(e);
+	}
+	if (!b->fork)
+		cuda_check(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming), "event");
+	cuda_check(cudaEventRecord(b->fork, st), "fork");
+	for (size_t k = 0; k < n; ++k)
+		cuda_check(cudaStreamWaitEvent(b->side[k], b->fork, 0), "fork");
+	for (size_t i = 0; i < work.size(); ++i)
+		work[i](b->side[i % n]);
+	for (size_t k = 0; k < n; ++k) {
+		cuda_check(cudaEventRecord(b->joins[k], b->side[k]), "join");
+		cuda_check(cudaStreamWaitEvent(st, b->joins[k], 0), "join");
 	}
 }
 

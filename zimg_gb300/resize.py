@@ -303,6 +303,57 @@ class Batch:
         check(load().zg_batch_process_graph(self._h, self._tmp_ptr(tmp), _stream_handle(stream)))
 
 
+class HostPipeline:
+    """Conversions of planes that live in (pinned) host memory.
+
+    The planes are split into `chunks` sub-batches, each with its own device
+    staging planes and Batch. Per call, chunk i's host-to-device copies, its
+    batch launch and its device-to-host copies go to three streams ordered by
+    events, so the copies of one chunk overlap the work of its neighbours.
+    `run` returns once the results are in the host planes."""
+
+    def __init__(self, conversions: list[ResizeConversion], chunks: int = 4, autotune: bool = True):
+        import torch
+        n = len(conversions)
+        self.chunks = max(1, min(chunks, n))
+        bounds = [round(i * n / self.chunks) for i in range(self.chunks + 1)]
+        self.parts = []
+        for c in range(self.chunks):
+            convs = conversions[bounds[c]:bounds[c + 1]]
+            srcs, dsts = [], []
+            for conv in convs:
+                dt = torch.int16 if conv.type == _pixel_id("word") else torch.float32
+                srcs.append(torch.empty((conv.src_height, conv.src_width), dtype=dt, device="cuda"))
+                dsts.append(torch.empty((conv.dst_height, conv.dst_width), dtype=dt, device="cuda"))
+            b = Batch(convs)
+            b.set_io(srcs, dsts)
+            if autotune:
+                b.autotune()
+            tmp = torch.empty(max(b.tmp_size, 1), dtype=torch.uint8, device="cuda")
+            self.parts.append((bounds[c], b, srcs, dsts, tmp))
+        self.streams = [torch.cuda.Stream() for _ in range(3)]
+
+    def run(self, host_srcs, host_dsts) -> None:
+        import torch
+        h2d, work, d2h = self.streams
+        cur = torch.cuda.current_stream()
+        for s in self.streams:
+            s.wait_stream(cur)
+        for first, b, srcs, dsts, tmp in self.parts:
+            with torch.cuda.stream(h2d):
+                for k, d in enumerate(srcs):
+                    d.copy_(host_srcs[first + k], non_blocking=True)
+            work.wait_stream(h2d)
+            b.process(tmp, stream=work)
+            d2h.wait_stream(work)
+            with torch.cuda.stream(d2h):
+                for k, d in enumerate(dsts):
+                    host_dsts[first + k].copy_(d, non_blocking=True)
+        for s in self.streams:
+            cur.wait_stream(s)
+        cur.synchronize()
+
+
 def image_format(width, height, pixel_type="float", **kw) -> capi.ImageFormat:
     """zimg_image_format with zimg's defaults (zimg.cpp:595-630), then kw."""
     f = capi.ImageFormat()
