@@ -129,26 +129,51 @@ __device__ __forceinline__ Item make_item(const FusedJob &J, int t, char *smem, 
 }
 
 // Lines [a, b) of the source strip into ring slots (line & mask) of `ring`
-// (pitch elements of E bytes per line), zero outside the plane. Warp w takes
-// lines a + w, a + w + 4, ...
+// (pitch elements of E bytes per line), zero outside the plane. Aligned
+// planes: thread t copies 16-byte chunk t % chunks of lines a + t / chunks,
+// then every kThreads / chunks lines further (one address step per line).
+// Otherwise warp w takes lines a + w, a + w + 4, ... sample by sample.
 template <bool U16>
 __device__ __forceinline__ void load_lines(const Item &it, int a, int b, char *ring, int mask, int pitch)
 {
 	constexpr int E = U16 ? 2 : 4;
 	constexpr int PER = 16 / E;
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-	const int chunks = it.pxa / PER;
+	if (it.vec_ok) {
+		const int chunks = it.pxa / PER;
+		const int lpp = kThreads / chunks;
+		if (lpp == 0) {
+			// strips wider than kThreads chunks: warp per line
+			for (int y = a + warp; y < b; y += kWarps) {
+				const bool row_ok = y < it.src_h;
+				const char *row = it.src + static_cast<ptrdiff_t>(row_ok ? y : 0) * it.src_stride;
+				char *srow = ring + (y & mask) * pitch * E;
+				for (int q = lane; q < chunks; q += 32) {
+					const int gx = it.xlo + q * PER;
+					const int n = row_ok ? max(0, min(PER, it.src_w - gx)) : 0;
+					cp_async16(srow + q * 16, n ? row + static_cast<ptrdiff_t>(gx) * E : it.src, n * E);
+				}
+			}
+			return;
+		}
+		const int q = threadIdx.x % chunks, l0 = threadIdx.x / chunks;
+		if (l0 >= lpp)
+			return;
+		const int gx = it.xlo + q * PER;
+		const int nb = max(0, min(PER, it.src_w - gx)) * E;
+		const char *src = it.src + (nb ? static_cast<ptrdiff_t>(gx) * E : 0) + static_cast<ptrdiff_t>(a + l0) * it.src_stride;
+		const ptrdiff_t step = static_cast<ptrdiff_t>(lpp) * it.src_stride;
+		for (int y = a + l0; y < b; y += lpp, src += step) {
+			const bool ok = y < it.src_h && nb;
+			cp_async16(ring + ((y & mask) * pitch * E) + q * 16, ok ? src : it.src, ok ? nb : 0);
+		}
+		return;
+	}
 	for (int y = a + warp; y < b; y += kWarps) {
 		const bool row_ok = y < it.src_h;
 		const char *row = it.src + static_cast<ptrdiff_t>(row_ok ? y : 0) * it.src_stride;
 		char *srow = ring + (y & mask) * pitch * E;
-		if (it.vec_ok) {
-			for (int q = lane; q < chunks; q += 32) {
-				const int gx = it.xlo + q * PER;
-				const int n = row_ok ? max(0, min(PER, it.src_w - gx)) : 0;
-				cp_async16(srow + q * 16, n ? row + static_cast<ptrdiff_t>(gx) * E : it.src, n * E);
-			}
-		} else if (!U16) {
+		if (!U16) {
 			for (int x = lane; x < it.pxa; x += 32) {
 				const int gx = it.xlo + x;
 				const bool ok = row_ok && gx < it.src_w;
@@ -167,25 +192,42 @@ __device__ __forceinline__ void load_lines(const Item &it, int a, int b, char *r
 
 // Convert the u16 lines this thread loaded with load_lines(a, b) from the
 // raw staging ring to centred floats in `ring`.
+__device__ __forceinline__ void convert_chunk(const char *srow, float *drow, int q, float bias)
+{
+	const uint4 u = *reinterpret_cast<const uint4 *>(srow + q * 16);
+	const uint32_t w[4] = { u.x, u.y, u.z, u.w };
+	float f[8];
+#pragma unroll
+	for (int k = 0; k < 8; ++k)
+		f[k] = __int_as_float(0x4B000000 | ((w[k >> 1] >> (16 * (k & 1))) & 0xFFFFu)) - bias;
+	*reinterpret_cast<float4 *>(drow + q * 8) = make_float4(f[0], f[1], f[2], f[3]);
+	*reinterpret_cast<float4 *>(drow + q * 8 + 4) = make_float4(f[4], f[5], f[6], f[7]);
+}
+
+// Convert the u16 lines [a, b) from the raw staging ring to centred floats
+// in `ring`. With cp.async copies each thread converts exactly the chunks it
+// copied (the mapping of load_lines); plain loads were made visible by a
+// CTA barrier, so any mapping serves.
 __device__ __forceinline__ void convert_lines(const Item &it, int a, int b, const char *stage, int smask,
                                               float *ring, int rmask, int pitch)
 {
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	const float bias = 8388608.0f + it.offset;
 	const int chunks = it.pxa / 8;
+	const int lpp = kThreads / chunks;
+	if (it.vec_ok && lpp) {
+		const int q = threadIdx.x % chunks, l0 = threadIdx.x / chunks;
+		if (l0 >= lpp)
+			return;
+		for (int y = a + l0; y < b; y += lpp)
+			convert_chunk(stage + (y & smask) * pitch * 2, ring + (y & rmask) * pitch, q, bias);
+		return;
+	}
 	for (int y = a + warp; y < b; y += kWarps) {
 		const char *srow = stage + (y & smask) * pitch * 2;
 		float *drow = ring + (y & rmask) * pitch;
-		for (int q = lane; q < chunks; q += 32) {
-			const uint4 u = *reinterpret_cast<const uint4 *>(srow + q * 16);
-			const uint32_t w[4] = { u.x, u.y, u.z, u.w };
-			float f[8];
-#pragma unroll
-			for (int k = 0; k < 8; ++k)
-				f[k] = __int_as_float(0x4B000000 | ((w[k >> 1] >> (16 * (k & 1))) & 0xFFFFu)) - bias;
-			*reinterpret_cast<float4 *>(drow + q * 8) = make_float4(f[0], f[1], f[2], f[3]);
-			*reinterpret_cast<float4 *>(drow + q * 8 + 4) = make_float4(f[4], f[5], f[6], f[7]);
-		}
+		for (int q = lane; q < chunks; q += 32)
+			convert_chunk(srow, drow, q, bias);
 	}
 }
 
