@@ -20,7 +20,7 @@ const void *fused_kernel_ptr_h_u16(int hw, int vs);
 
 namespace {
 
-constexpr int kHwBuckets[] = { 8, 16 };
+constexpr int kHwBuckets[] = { 6, 8, 16 };
 constexpr int kVsBuckets[] = { 8, 12, 16, 24 };
 constexpr size_t kSmemBudget = 56 * 1024;   // preferred: four CTAs of 128 threads per SM
 constexpr size_t kSmemMax = 110 * 1024;     // hard limit: two CTAs per SM
@@ -77,7 +77,7 @@ bool plan_fused(const FilterTable &first, const FilterTable &second, bool h_firs
 	if (u16 && (!u16_exact_in_float(H, depth) || !u16_exact_in_float(V, depth)))
 		return false;
 
-	const int hw_i = bucket_index(kHwBuckets, 2, static_cast<int>(H.width));
+	const int hw_i = bucket_index(kHwBuckets, 3, static_cast<int>(H.width));
 	if (hw_i < 0)
 		return false;
 	const int HW = kHwBuckets[hw_i];
@@ -127,7 +127,7 @@ bool plan_fused(const FilterTable &first, const FilterTable &second, bool h_firs
 	p = FusedPlan{};
 	bool fits = false;
 	for (int attempt = 0; attempt < 2 && !fits; ++attempt)
-	for (int step_groups = h_first ? 4 : 2; step_groups >= 1 && !fits; step_groups /= 2) {
+	for (int step_groups = h_first ? 8 : 4; step_groups >= 1 && !fits; step_groups /= 2) {
 		const size_t budget = attempt == 0 ? kSmemBudget : kSmemMax;
 		const int nsteps = (groups + step_groups - 1) / step_groups;
 		auto hi_of = [&](int k) { return gbase[std::min(groups, (k + 1) * step_groups) - 1] + VS; };
@@ -215,7 +215,7 @@ bool plan_fused(const FilterTable &first, const FilterTable &second, bool h_firs
 	J.offset = offset;
 	J.magic = 12582912.0f + offset;
 	J.pixel_max = u16 ? static_cast<float>((1UL << depth) - 1) : 0.0f;
-	p.variant = ((J.h_first * 2 + (u16 ? 1 : 0)) * 2 + hw_i) * 4 + vs_i;
+	p.variant = ((J.h_first * 2 + (u16 ? 1 : 0)) * 3 + hw_i) * 4 + vs_i;
 	return true;
 }
 
@@ -263,9 +263,9 @@ namespace {
 void split_variant(int variant, int *hf, int *u16, int *hw_i, int *vs_i)
 {
 	*vs_i = variant % 4;
-	*hw_i = (variant / 4) % 2;
-	*u16 = (variant / 8) % 2;
-	*hf = (variant / 16) % 2;
+	*hw_i = (variant / 4) % 3;
+	*u16 = (variant / 12) % 2;
+	*hf = (variant / 24) % 2;
 }
 
 const void *kernel_ptr(int variant)
@@ -326,7 +326,7 @@ SmemLayout fused_layout(const FusedPlan *const *plans, int n)
 	L.hleft_off = off;
 	off += a16(kStripW * 4);
 	L.vcoef_off = off;
-	off += 2 * a16(static_cast<size_t>(step_groups) * vs * 16);
+	off += 2 * a16(static_cast<size_t>(step_groups) * vs * kGroup * 4);
 	L.vbase_off = off;
 	off += a16(static_cast<size_t>(seg_groups) * 4);
 	L.total_bytes = off;

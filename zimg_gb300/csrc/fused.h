@@ -26,8 +26,8 @@ enum class FusedKind : int { F32 = 0, U16_EXACT = 1 };
 
 // Vertical taps come in groups of kGroup output rows laid out densely over a
 // window of VS input lines (VS = 8, 12, 16 or 24); horizontal taps per output
-// column are padded with zeros to HW (8 or 16).
-constexpr int kGroup = 4;
+// column are padded with zeros to HW (6, 8 or 16).
+constexpr int kGroup = 2;
 constexpr int kStripW = 128;      // output columns per strip
 constexpr int kStreamThreads = 128;
 

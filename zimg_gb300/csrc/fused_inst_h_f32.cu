@@ -26,7 +26,7 @@ const void *ptr_vs(int vs)
 
 const void *fused_kernel_ptr_h_f32(int hw, int vs)
 {
-	return hw == 0 ? ptr_vs<8>(vs) : ptr_vs<16>(vs);
+	return hw == 0 ? ptr_vs<6>(vs) : (hw == 1 ? ptr_vs<8>(vs) : ptr_vs<16>(vs));
 }
 
 cudaError_t launch_fused_h_f32(int hw, int vs, const FusedJob *jobs, int num_jobs, int total_tiles, const SmemLayout &L,

@@ -114,9 +114,10 @@ __device__ __forceinline__ Item make_item(const FusedJob &J, int t, char *smem, 
 
 	// per-item tables: h taps and left offsets of the strip, group bases
 	const char *ht = reinterpret_cast<const char *>(J.h_taps) + static_cast<size_t>(it.c0) * HW * 4;
+	const int tap_bytes = it.cols_valid * HW * 4;
 	for (int i = threadIdx.x; i < kStripW * HW / 4; i += kThreads) {
-		const bool ok = (i * 4) / HW < it.cols_valid;
-		cp_async16(smem + L.htaps_off + i * 16, ok ? ht + i * 16 : ht, ok ? 16 : 0);
+		const int n = max(0, min(16, tap_bytes - i * 16));
+		cp_async16(smem + L.htaps_off + i * 16, n ? ht + i * 16 : ht, n);
 	}
 	for (int i = threadIdx.x; i < kStripW / 4; i += kThreads) {
 		const int n = max(0, min(4, it.cols_valid - 4 * i));
@@ -242,14 +243,12 @@ __device__ __forceinline__ void h_pass(const Item &it, const char *smem, const S
 	const int c = threadIdx.x;
 	const bool col_ok = c < it.cols_valid;
 	float taps[HW];
-	const float4 *tp = reinterpret_cast<const float4 *>(smem + L.htaps_off) + c * (HW / 4);
+	const float2 *tp = reinterpret_cast<const float2 *>(smem + L.htaps_off) + c * (HW / 2);
 #pragma unroll
-	for (int k = 0; k < HW / 4; ++k) {
-		const float4 t4 = tp[k];
-		taps[4 * k] = t4.x;
-		taps[4 * k + 1] = t4.y;
-		taps[4 * k + 2] = t4.z;
-		taps[4 * k + 3] = t4.w;
+	for (int k = 0; k < HW / 2; ++k) {
+		const float2 t2 = tp[k];
+		taps[2 * k] = t2.x;
+		taps[2 * k + 1] = t2.y;
 	}
 	const int l = col_ok ? reinterpret_cast<const int *>(smem + L.hleft_off)[c] - it.xlo : 0;
 	const float init = U16 ? 8192.0f : 0.0f;
@@ -298,7 +297,7 @@ __device__ __forceinline__ void h_pass(const Item &it, const char *smem, const S
 // FINAL: destination rows g*4 + j (columns c0 + 4q ...); else lines of I.
 template <bool U16, bool FINAL, int VS>
 __device__ __forceinline__ void v_pass(const Item &it, const char *smem, const SmemLayout &L, const float *in,
-                                       int imask, int in_pitch, int g0, int g1, const float4 *coef, int quads,
+                                       int imask, int in_pitch, int g0, int g1, const float2 *coef, int quads,
                                        float *I, int i_pitch)
 {
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -309,7 +308,7 @@ __device__ __forceinline__ void v_pass(const Item &it, const char *smem, const S
 	for (int gi = warp / wpg; gi < ng; gi += kWarps / wpg) {
 		const int g = g0 + gi;
 		const int base = vb[g - it.g_begin];
-		const float4 *cf = coef + gi * VS;
+		const float2 *cf = coef + gi * VS;  // [line][row] taps of the group's two rows
 		int off[VS];
 #pragma unroll
 		for (int s = 0; s < VS; ++s)
@@ -324,8 +323,8 @@ __device__ __forceinline__ void v_pass(const Item &it, const char *smem, const S
 #pragma unroll
 			for (int s = 0; s < VS; ++s) {
 				const float4 x = *reinterpret_cast<const float4 *>(in + off[s] + 4 * q);
-				const float4 c4 = cf[s];
-				const float cj[4] = { c4.x, c4.y, c4.z, c4.w };
+				const float2 c2 = cf[s];
+				const float cj[kGroup] = { c2.x, c2.y };
 #pragma unroll
 				for (int j = 0; j < kGroup; ++j) {
 					acc[j][0] = __fmaf_rn(cj[j], x.x, acc[j][0]);
@@ -395,8 +394,9 @@ __device__ __forceinline__ int step_end(const Item &it, const char *smem, const 
 template <int VS>
 __device__ __forceinline__ void load_coef(const Item &it, int g0, int g1, char *dst)
 {
-	const char *src = it.v_dense + static_cast<size_t>(g0) * VS * 16;
-	for (int i = threadIdx.x; i < (g1 - g0) * VS; i += kThreads)
+	// kGroup floats per line: (g1 - g0) * VS * kGroup * 4 bytes, a multiple of 16 (VS even)
+	const char *src = it.v_dense + static_cast<size_t>(g0) * VS * kGroup * 4;
+	for (int i = threadIdx.x; i < (g1 - g0) * VS * kGroup / 4; i += kThreads)
 		cp_async16(dst + i * 16, src + i * 16, 16);
 }
 
@@ -471,7 +471,7 @@ fused_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 				convert_lines(it, lo_cur, hi_cur, stage, smask, H_FIRST ? in : ring, H_FIRST ? imask : rmask, L.pitch);
 			__syncthreads();
 
-			const float4 *coef = reinterpret_cast<const float4 *>(smem + L.vcoef_off + (k & 1) * (L.vbase_off - L.vcoef_off) / 2);
+			const float2 *coef = reinterpret_cast<const float2 *>(smem + L.vcoef_off + (k & 1) * (L.vbase_off - L.vcoef_off) / 2);
 			if (H_FIRST) {
 				// new source lines -> intermediate ring
 				h_pass<U16, false, HW>(it, smem, L, in, imask, lo_cur, hi_cur, ring, rmask, 0);
