@@ -145,7 +145,7 @@ bool plan_chain(const FilterTable &first, const FilterTable &second, bool h_firs
 		return false;
 
 	// strips of 8 warps' tiles; source columns [lo, hi) with lo a multiple of 8
-	const int strip_tiles = chain_detail::kWarps * chain_detail::tiles_per_warp(KV, KH);
+	const int strip_tiles = chain_detail::warps_per_cta(h_first) * chain_detail::tiles_per_warp(KV, KH);
 	const int strip_w = strip_tiles * chain_detail::kTileW;
 	const int strips = static_cast<int>((dst_w + strip_w - 1) / strip_w);
 	std::vector<int> win_col(2 * strips);
@@ -296,7 +296,7 @@ SmemLayout chain_layout(const FusedPlan *const *plans, int n)
 	off += a16(static_cast<size_t>(depth + 2) * kv * 2 * 32 * 16);
 	L.tile_off = off;
 	L.tile_pitch = chain_detail::kStageBytes / 2;
-	off += a16(static_cast<size_t>(chain_detail::kWarps) * chain_detail::kMaxTilesPerWarp * 16 *
+	off += a16(static_cast<size_t>(chain_detail::kMaxWarps) * chain_detail::kMaxTilesPerWarp * 16 *
 	           chain_detail::kStageBytes);
 	L.vbase_off = off;
 	off += a16(static_cast<size_t>(seg_groups) * 4);
@@ -341,9 +341,10 @@ const void *chain_kernel_ptr(int variant)
 	return hf ? chain_ptr_kv<true>(kv, kh) : chain_ptr_kv<false>(kv, kh);
 }
 
-int chain_threads()
+int chain_threads(int variant)
 {
-	return chain_detail::kThreads;
+	const bool hf = variant - 200 >= kChainKVMax * kChainKHMax;
+	return chain_detail::warps_per_cta(hf) * 32;
 }
 
 cudaError_t launch_chain(int variant, const FusedJob *jobs, int num_jobs, int total_items, const SmemLayout &L, int grid,
@@ -359,7 +360,7 @@ cudaError_t launch_chain(int variant, const FusedJob *jobs, int num_jobs, int to
 	SmemLayout layout = L;
 	void *args[] = { &jobs, &num_jobs, &total_items, &one, &layout };
 	grid = std::max(1, std::min(grid, total_items));
-	return cudaLaunchKernel(k, dim3(grid), dim3(chain_detail::kThreads), args, static_cast<size_t>(L.total_bytes),
+	return cudaLaunchKernel(k, dim3(grid), dim3(chain_threads(variant)), args, static_cast<size_t>(L.total_bytes),
 	                        stream);
 }
 

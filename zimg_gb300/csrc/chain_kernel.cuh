@@ -37,8 +37,14 @@ using mma_detail::pack_u16x2;
 using mma_detail::u16x2_to_centred_h2;
 using mma_detail::wrap;
 
-constexpr int kWarps = 8;
-constexpr int kThreads = kWarps * 32;
+// CTA shape: H-first conversions (upscales) run 4-warp CTAs, four per SM;
+// V-first ones (downscales, wider windows and more registers) 8-warp CTAs,
+// two per SM.
+__host__ __device__ constexpr int warps_per_cta(bool h_first)
+{
+	return h_first ? 4 : 8;
+}
+constexpr int kMaxWarps = 8;
 constexpr int kTileW = 16;                 // output columns of one tile (one m16 block)
 
 // Tiles per warp: two share the loop, the loads and the barriers, where the
@@ -83,7 +89,7 @@ struct Item {
 	uint32_t pmax2, bias_h2;
 };
 
-__device__ __forceinline__ Item make_item(const FusedJob &J, int t, int strip_tiles)
+__device__ __forceinline__ Item make_item(const FusedJob &J, int t, int strip_tiles, int nthreads)
 {
 	Item it;
 	const int local = t - J.item_begin;
@@ -112,7 +118,7 @@ __device__ __forceinline__ Item make_item(const FusedJob &J, int t, int strip_ti
 	const int chunks = pxa / 8;
 	it.q0 = threadIdx.x % chunks;
 	it.l0 = threadIdx.x / chunks;
-	it.lpp = kThreads / chunks;
+	it.lpp = nthreads / chunks;
 	it.gx = it.xlo + it.q0 * 8;
 	const int n = max(0, min(8, it.src_w - it.gx));
 	it.col_bytes = n * 2;
@@ -159,7 +165,7 @@ template <int KV>
 __device__ __forceinline__ void load_vfrag(const FusedJob &J, int g, char *slot)
 {
 	const char *src = reinterpret_cast<const char *>(J.v_dense) + static_cast<size_t>(g) * KV * 2 * 32 * 16;
-	for (int i = threadIdx.x; i < KV * 2 * 32; i += kThreads)
+	for (int i = threadIdx.x; i < KV * 2 * 32; i += blockDim.x)
 		cp_async16(slot + i * 16, src + i * 16, 16);
 }
 
@@ -365,7 +371,7 @@ __device__ __forceinline__ void store_tile(const Item &it, const char *ld_addr, 
 // (vbase_off). A warp may still compute group k while others issue the loads
 // of group k + 1 + depth: the planner sizes the ring and the slots for that.
 template <bool H_FIRST, int KV, int KH>
-__global__ void __launch_bounds__(kThreads, 2)
+__global__ void __launch_bounds__(warps_per_cta(H_FIRST) * 32, H_FIRST ? 4 : 2)
 chain_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, const __grid_constant__ FusedJob single,
              const __grid_constant__ SmemLayout L)
 {
@@ -380,6 +386,8 @@ chain_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 	const int P = L.pitch * 2;
 	constexpr int kSlotBytes = KV * 2 * 32 * 16;
 	constexpr int kTilesPerWarp = tiles_per_warp(KV, KH);
+	constexpr int kWarps = warps_per_cta(H_FIRST);
+	constexpr int kThreads = kWarps * 32;
 	constexpr int kStripTiles = kWarps * kTilesPerWarp;
 	// stmatrix / stage read addresses of this lane
 	char *st_addr = stage + (((lane >> 4) << 3) + (lane & 7)) * kStageBytes + ((lane >> 3) & 1) * 16;
@@ -394,7 +402,7 @@ chain_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 
 	for (int t = blockIdx.x; t < total_items; t += gridDim.x) {
 		const FusedJob *Jp = jobs ? &jobs[find_job(jobs, num_jobs, t)] : &single;
-		const Item it = make_item(*Jp, t, kStripTiles);
+		const Item it = make_item(*Jp, t, kStripTiles, kThreads);
 		for (int g = it.g_begin + threadIdx.x; g < it.g_end; g += kThreads)
 			vb[g - it.g_begin] = __ldg(Jp->v_base + g);
 

@@ -345,7 +345,7 @@ int fused_grid_size(int variant, size_t smem_bytes)
 	cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
 	const void *k = kernel_ptr(variant);
 	cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kSmemMax));
-	const int threads = variant >= 200 ? chain_threads() : (variant >= 100 ? mma_threads() : kStreamThreads);
+	const int threads = variant >= 200 ? chain_threads(variant) : (variant >= 100 ? mma_threads() : kStreamThreads);
 	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, threads, smem_bytes) != cudaSuccess || per_sm < 1)
 		per_sm = 1;
 	return std::max(1, sms) * per_sm;

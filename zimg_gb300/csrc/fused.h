@@ -153,7 +153,7 @@ bool plan_chain(const FilterTable &first, const FilterTable &second, bool h_firs
                 unsigned src_h, unsigned dst_w, unsigned dst_h, FusedPlan *out);
 SmemLayout chain_layout(const FusedPlan *const *plans, int n);
 const void *chain_kernel_ptr(int variant);
-int chain_threads();
+int chain_threads(int variant);
 cudaError_t launch_chain(int variant, const FusedJob *jobs, int num_jobs, int total_items, const SmemLayout &L, int grid,
                          const FusedJob &single, cudaStream_t stream);
 // Work items that fill the current device once (SMs x resident CTAs).
