@@ -412,6 +412,19 @@ chain_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 		uint4 ah[kTilesPerWarp][KH][2];
 		int rel[kTilesPerWarp];
 		Carry carry[kTilesPerWarp];
+		// this lane's 16-byte half row of each tile in the item's first group,
+		// advanced by 16 rows per group; whole-tile stores where the tile is
+		// inside the plane
+		char *drow[kTilesPerWarp];
+		bool wide[kTilesPerWarp];
+#pragma unroll
+		for (int j = 0; j < kTilesPerWarp; ++j) {
+			const int col = (tile0 + j) * kTileW + (lane & 1) * 8;
+			wide[j] = it.vec_ok && col + 8 <= it.dst_w;
+			drow[j] = it.dst + static_cast<ptrdiff_t>(it.g_begin * 16 + (lane >> 1)) * it.dst_stride +
+			          static_cast<ptrdiff_t>(col) * 2;
+		}
+		const ptrdiff_t group_step = 16 * it.dst_stride;
 #pragma unroll
 		for (int j = 0; j < kTilesPerWarp; ++j) {
 			const int tile = min(tile0 + j, ntiles - 1);
@@ -488,13 +501,20 @@ chain_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 						stsm_x4_trans(sa, m[j][0], m[j][1], m[j][2], m[j][3]);
 				}
 				__syncwarp();
+				const bool rows_in = (it.g_begin + k + 1) * 16 <= it.dst_h;
 #pragma unroll
-				for (int j = 0; j < kTilesPerWarp; ++j)
-					if ((tile0 + j) * kTileW < it.dst_w)
+				for (int j = 0; j < kTilesPerWarp; ++j) {
+					if (wide[j] && rows_in)
+						*reinterpret_cast<uint4 *>(drow[j]) = *reinterpret_cast<const uint4 *>(ld_addr + j * 16 * kStageBytes);
+					else if ((tile0 + j) * kTileW < it.dst_w)
 						store_tile(it, ld_addr + j * 16 * kStageBytes, (it.g_begin + k) * 16, (tile0 + j) * kTileW);
+				}
 				__syncwarp();
 			}
 			read_slot = read_slot + 1 == S ? 0 : read_slot + 1;
+#pragma unroll
+			for (int j = 0; j < kTilesPerWarp; ++j)
+				drow[j] += group_step;
 		}
 		cp_async_wait<0>();
 		__syncthreads();  // the next item rewrites the group bases and the ring
