@@ -236,6 +236,28 @@ __device__ __forceinline__ uint32_t pack(const Acc &a, int i, const Item &it)
 #endif
 }
 
+// Two accumulator values -> the next product's centred fp16 pair. With
+// ZG_CHAIN_H16 the rounding lands directly on fp16 bit patterns: the magic
+// constant 1.5 * 2^23 + 0x6400 + offset leaves 0x6400 + u in the low 16 bits
+// of each rounded float, u = floor(acc / 2^14) + offset; |u| < 1024 (the
+// exactness certificate), so the pair is two positive fp16 values ordered as
+// u, clamped by fp16 min/max to [1024, 1024 + pixel_max] and re-centred.
+__device__ __forceinline__ uint32_t pack_centre(const Acc &a, int i, const Item &it)
+{
+#ifdef ZG_CHAIN_H16
+	const float y0 = __fmaf_rd(a[i], 6.103515625e-05f, it.magic + 25600.0f);
+	const float y1 = __fmaf_rd(a[i + 1], 6.103515625e-05f, it.magic + 25600.0f);
+	uint32_t q = __byte_perm(__float_as_uint(y0), __float_as_uint(y1), 0x5410);
+	__half2 h = *reinterpret_cast<const __half2 *>(&q);
+	const uint32_t lo_bits = 0x64006400u, hi_bits = 0x64006400u + it.pmax2;
+	h = __hmin2(__hmax2(h, *reinterpret_cast<const __half2 *>(&lo_bits)), *reinterpret_cast<const __half2 *>(&hi_bits));
+	h = __hsub2(h, *reinterpret_cast<const __half2 *>(&it.bias_h2));
+	return *reinterpret_cast<const uint32_t *>(&h);
+#else
+	return centre(pack(a, i, it), it.bias_h2);
+#endif
+}
+
 // One 16-column tile of one 16-row group: both passes, then the staged
 // result to the destination. ah: the tile's horizontal tap fragments, rel: its
 // window start in the strip's lines, av: the group's vertical fragments.
@@ -280,14 +302,14 @@ __device__ __forceinline__ void tile_compute(const Item &it, const char *ring, i
 			}
 			// Dh (out col gid / gid+8, lines 2tig..) -> V operands (k = lines, n = out col)
 			if (top) {
-				bv[kv][0][0] = centre(pack(dh0, 0, it), it.bias_h2);
-				bv[kv][1][0] = centre(pack(dh0, 2, it), it.bias_h2);
+				bv[kv][0][0] = pack_centre(dh0, 0, it);
+				bv[kv][1][0] = pack_centre(dh0, 2, it);
 			} else {
 				bv[kv][0][0] = carry.b[0];
 				bv[kv][1][0] = carry.b[1];
 			}
-			bv[kv][0][1] = centre(pack(dh1, 0, it), it.bias_h2);
-			bv[kv][1][1] = centre(pack(dh1, 2, it), it.bias_h2);
+			bv[kv][0][1] = pack_centre(dh1, 0, it);
+			bv[kv][1][1] = pack_centre(dh1, 2, it);
 		}
 		if (KV == 1) {
 			carry.b[0] = bv[0][0][1];
@@ -330,10 +352,10 @@ __device__ __forceinline__ void tile_compute(const Item &it, const char *ring, i
 				dv1.mma(av[kv][0], av[kv][1], b2, b3);
 			}
 			// Dv (out row gid / gid+8, in cols 2tig..) -> H operands (k = in cols, n = out row)
-			const uint32_t h00 = centre(pack(dv0, 0, it), it.bias_h2);
-			const uint32_t h01 = centre(pack(dv1, 0, it), it.bias_h2);
-			const uint32_t h10 = centre(pack(dv0, 2, it), it.bias_h2);
-			const uint32_t h11 = centre(pack(dv1, 2, it), it.bias_h2);
+			const uint32_t h00 = pack_centre(dv0, 0, it);
+			const uint32_t h01 = pack_centre(dv1, 0, it);
+			const uint32_t h10 = pack_centre(dv0, 2, it);
+			const uint32_t h11 = pack_centre(dv1, 2, it);
 			dh0.mma(ah[ks][0], ah[ks][1], h00, h01);
 			dh1.mma(ah[ks][0], ah[ks][1], h10, h11);
 		}
