@@ -236,26 +236,10 @@ __device__ __forceinline__ uint32_t pack(const Acc &a, int i, const Item &it)
 #endif
 }
 
-// Two accumulator values -> the next product's centred fp16 pair. With
-// ZG_CHAIN_H16 the rounding lands directly on fp16 bit patterns: the magic
-// constant 1.5 * 2^23 + 0x6400 + offset leaves 0x6400 + u in the low 16 bits
-// of each rounded float, u = floor(acc / 2^14) + offset; |u| < 1024 (the
-// exactness certificate), so the pair is two positive fp16 values ordered as
-// u, clamped by fp16 min/max to [1024, 1024 + pixel_max] and re-centred.
+// Two accumulator values -> the next product's centred fp16 pair.
 __device__ __forceinline__ uint32_t pack_centre(const Acc &a, int i, const Item &it)
 {
-#ifdef ZG_CHAIN_H16
-	const float y0 = __fmaf_rd(a[i], 6.103515625e-05f, it.magic + 25600.0f);
-	const float y1 = __fmaf_rd(a[i + 1], 6.103515625e-05f, it.magic + 25600.0f);
-	uint32_t q = __byte_perm(__float_as_uint(y0), __float_as_uint(y1), 0x5410);
-	__half2 h = *reinterpret_cast<const __half2 *>(&q);
-	const uint32_t lo_bits = 0x64006400u, hi_bits = 0x64006400u + it.pmax2;
-	h = __hmin2(__hmax2(h, *reinterpret_cast<const __half2 *>(&lo_bits)), *reinterpret_cast<const __half2 *>(&hi_bits));
-	h = __hsub2(h, *reinterpret_cast<const __half2 *>(&it.bias_h2));
-	return *reinterpret_cast<const uint32_t *>(&h);
-#else
 	return centre(pack(a, i, it), it.bias_h2);
-#endif
 }
 
 // One 16-column tile of one 16-row group: both passes, then the staged

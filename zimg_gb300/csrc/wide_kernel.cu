@@ -35,7 +35,6 @@ namespace zg {
 namespace {
 
 constexpr int kWideWarps = 4;
-constexpr int kUnroll = 8;  // k-steps whose loads are issued together (a multiple of 4)
 
 __device__ __forceinline__ uint32_t tf32_rna(float x)
 {
@@ -90,29 +89,50 @@ __device__ __forceinline__ void band_sum(float (&d)[4], const WideTables &w, int
 	if (kb + 8 * s1 <= src_dim) {
 		const char *pa = base_a + (kb + 8 * s0 + tig) * sk, *pb = base_b + (kb + 8 * s0 + tig) * sk;
 		const ptrdiff_t s4 = 4 * sk, s8 = 8 * sk;
-		int s = s0;
-		for (; s + kUnroll <= s1; s += kUnroll) {
-			float x[kUnroll][4];
-			uint4 b[kUnroll];
+		// chunks of 4 k-steps, double-buffered: the loads of the next chunk are
+		// in flight while the current one runs on the tensor cores
+		auto load4 = [&](float (&x)[4][4], uint4 (&b)[4], int s) {
+			const char *qa = pa + static_cast<ptrdiff_t>(s - s0) * s8, *qb = pb + static_cast<ptrdiff_t>(s - s0) * s8;
 #pragma unroll
-			for (int u = 0; u < kUnroll; ++u) {
-				x[u][0] = __ldg(reinterpret_cast<const float *>(pa + u * s8));
-				x[u][1] = __ldg(reinterpret_cast<const float *>(pb + u * s8));
-				x[u][2] = __ldg(reinterpret_cast<const float *>(pa + u * s8 + s4));
-				x[u][3] = __ldg(reinterpret_cast<const float *>(pb + u * s8 + s4));
+			for (int u = 0; u < 4; ++u) {
+				x[u][0] = __ldg(reinterpret_cast<const float *>(qa + u * s8));
+				x[u][1] = __ldg(reinterpret_cast<const float *>(qb + u * s8));
+				x[u][2] = __ldg(reinterpret_cast<const float *>(qa + u * s8 + s4));
+				x[u][3] = __ldg(reinterpret_cast<const float *>(qb + u * s8 + s4));
 				b[u] = __ldg(bf + (s + u) * 32);
 			}
+		};
+		auto run4 = [&](const float (&x)[4][4], const uint4 (&b)[4]) {
+			float c[4] = { 0.f, 0.f, 0.f, 0.f };
 #pragma unroll
-			for (int c0 = 0; c0 < kUnroll; c0 += 4) {
-				float c[4] = { 0.f, 0.f, 0.f, 0.f };
-#pragma unroll
-				for (int u = c0; u < c0 + 4; ++u)
-					step3(c, x[u][0], x[u][1], x[u][2], x[u][3], b[u]);
-				add4(d, c);
+			for (int u = 0; u < 4; ++u)
+				step3(c, x[u][0], x[u][1], x[u][2], x[u][3], b[u]);
+			add4(d, c);
+		};
+		int s = s0;
+		if (s + 4 <= s1) {
+			float xa[4][4], xb[4][4];
+			uint4 ba[4], bb[4];
+			load4(xa, ba, s);
+			for (;;) {
+				const bool has_b = s + 8 <= s1;
+				if (has_b)
+					load4(xb, bb, s + 4);
+				run4(xa, ba);
+				s += 4;
+				if (!has_b)
+					break;
+				const bool has_a = s + 8 <= s1;
+				if (has_a)
+					load4(xa, ba, s + 4);
+				run4(xb, bb);
+				s += 4;
+				if (!has_a)
+					break;
 			}
-			pa += kUnroll * s8;
-			pb += kUnroll * s8;
 		}
+		pa += static_cast<ptrdiff_t>(s - s0) * s8;
+		pb += static_cast<ptrdiff_t>(s - s0) * s8;
 		for (; s < s1; ++s) {
 			const float x0 = __ldg(reinterpret_cast<const float *>(pa));
 			const float x1 = __ldg(reinterpret_cast<const float *>(pb));
