@@ -252,72 +252,6 @@ struct Carry {
 	uint32_t b[2];
 };
 
-// H first, first product of one tile and group: the horizontal products over
-// the group's KV*16 lines, rounded and re-centred into the vertical product's
-// B operands bv[kv][output column half][line half].
-template <int KV, int KH>
-__device__ __forceinline__ void h_part(const Item &it, const char *ring, int IR, int P, int slot, int rel,
-                                       const uint4 (&ah)[KH][2], Carry &carry, bool reuse, uint32_t (&bv)[KV][2][2])
-{
-	const int lane = threadIdx.x & 31;
-	const int gid = lane >> 2, tig = lane & 3;
-#pragma unroll
-	for (int kv = 0; kv < KV; ++kv) {
-		Acc dh0, dh1;  // lines 0-7, 8-15
-		const bool top = !(KV == 1 && reuse);
-		if (top)
-			dh0.init();
-		dh1.init();
-		const char *r0 = ring + wrap(slot + 16 * kv + gid, IR) * P + (rel + 2 * tig) * 2;
-		const char *r1 = ring + wrap(slot + 16 * kv + gid + 8, IR) * P + (rel + 2 * tig) * 2;
-#pragma unroll
-		for (int ks = 0; ks < KH; ++ks) {
-			if (top) {
-				const uint32_t b0 = centre(*reinterpret_cast<const uint32_t *>(r0 + ks * 32), it.bias_h2);
-				const uint32_t b1 = centre(*reinterpret_cast<const uint32_t *>(r0 + ks * 32 + 16), it.bias_h2);
-				dh0.mma(ah[ks][0], ah[ks][1], b0, b1);
-			}
-			const uint32_t b2 = centre(*reinterpret_cast<const uint32_t *>(r1 + ks * 32), it.bias_h2);
-			const uint32_t b3 = centre(*reinterpret_cast<const uint32_t *>(r1 + ks * 32 + 16), it.bias_h2);
-			dh1.mma(ah[ks][0], ah[ks][1], b2, b3);
-		}
-		// Dh (out col gid / gid+8, lines 2tig..) -> V operands (k = lines, n = out col)
-		if (top) {
-			bv[kv][0][0] = pack_centre(dh0, 0, it);
-			bv[kv][1][0] = pack_centre(dh0, 2, it);
-		} else {
-			bv[kv][0][0] = carry.b[0];
-			bv[kv][1][0] = carry.b[1];
-		}
-		bv[kv][0][1] = pack_centre(dh1, 0, it);
-		bv[kv][1][1] = pack_centre(dh1, 2, it);
-	}
-	if (KV == 1) {
-		carry.b[0] = bv[0][0][1];
-		carry.b[1] = bv[0][1][1];
-	}
-}
-
-// H first, second product: m = the four packed row-major 8x8 blocks.
-template <int KV>
-__device__ __forceinline__ void v_part(const Item &it, const uint4 (&av)[KV][2], const uint32_t (&bv)[KV][2][2],
-                                       uint32_t (&m)[4])
-{
-	Acc dv0, dv1;  // out cols 0-7, 8-15
-	dv0.init();
-	dv1.init();
-#pragma unroll
-	for (int kv = 0; kv < KV; ++kv) {
-		dv0.mma(av[kv][0], av[kv][1], bv[kv][0][0], bv[kv][0][1]);
-		dv1.mma(av[kv][0], av[kv][1], bv[kv][1][0], bv[kv][1][1]);
-	}
-	// (out row gid / gid+8, out cols 2tig..)
-	m[0] = pack(dv0, 0, it);
-	m[1] = pack(dv1, 0, it);
-	m[2] = pack(dv0, 2, it);
-	m[3] = pack(dv1, 2, it);
-}
-
 // Both passes of one 16-column tile of one 16-row group; m: the four packed
 // 8x8 blocks of the result (row-major for H first, transposed for V first).
 template <bool H_FIRST, int KV, int KH>
@@ -328,9 +262,56 @@ __device__ __forceinline__ void tile_compute(const Item &it, const char *ring, i
 	const int lane = threadIdx.x & 31;
 	const int gid = lane >> 2, tig = lane & 3;
 	if (H_FIRST) {
+		// H over the group's KV*16 lines: B = src[line gid (+8)][in cols 2tig (+8)]
 		uint32_t bv[KV][2][2];
-		h_part<KV, KH>(it, ring, IR, P, slot, rel, ah, carry, reuse, bv);
-		v_part<KV>(it, av, bv, m);
+#pragma unroll
+		for (int kv = 0; kv < KV; ++kv) {
+			Acc dh0, dh1;  // lines 0-7, 8-15
+			const bool top = !(KV == 1 && reuse);
+			if (top)
+				dh0.init();
+			dh1.init();
+			const char *r0 = ring + wrap(slot + 16 * kv + gid, IR) * P + (rel + 2 * tig) * 2;
+			const char *r1 = ring + wrap(slot + 16 * kv + gid + 8, IR) * P + (rel + 2 * tig) * 2;
+#pragma unroll
+			for (int ks = 0; ks < KH; ++ks) {
+				if (top) {
+					const uint32_t b0 = centre(*reinterpret_cast<const uint32_t *>(r0 + ks * 32), it.bias_h2);
+					const uint32_t b1 = centre(*reinterpret_cast<const uint32_t *>(r0 + ks * 32 + 16), it.bias_h2);
+					dh0.mma(ah[ks][0], ah[ks][1], b0, b1);
+				}
+				const uint32_t b2 = centre(*reinterpret_cast<const uint32_t *>(r1 + ks * 32), it.bias_h2);
+				const uint32_t b3 = centre(*reinterpret_cast<const uint32_t *>(r1 + ks * 32 + 16), it.bias_h2);
+				dh1.mma(ah[ks][0], ah[ks][1], b2, b3);
+			}
+			// Dh (out col gid / gid+8, lines 2tig..) -> V operands (k = lines, n = out col)
+			if (top) {
+				bv[kv][0][0] = pack_centre(dh0, 0, it);
+				bv[kv][1][0] = pack_centre(dh0, 2, it);
+			} else {
+				bv[kv][0][0] = carry.b[0];
+				bv[kv][1][0] = carry.b[1];
+			}
+			bv[kv][0][1] = pack_centre(dh1, 0, it);
+			bv[kv][1][1] = pack_centre(dh1, 2, it);
+		}
+		if (KV == 1) {
+			carry.b[0] = bv[0][0][1];
+			carry.b[1] = bv[0][1][1];
+		}
+		Acc dv0, dv1;  // out cols 0-7, 8-15
+		dv0.init();
+		dv1.init();
+#pragma unroll
+		for (int kv = 0; kv < KV; ++kv) {
+			dv0.mma(av[kv][0], av[kv][1], bv[kv][0][0], bv[kv][0][1]);
+			dv1.mma(av[kv][0], av[kv][1], bv[kv][1][0], bv[kv][1][1]);
+		}
+		// (out row gid / gid+8, out cols 2tig..): row-major 8x8 blocks
+		m[0] = pack(dv0, 0, it);
+		m[1] = pack(dv1, 0, it);
+		m[2] = pack(dv0, 2, it);
+		m[3] = pack(dv1, 2, it);
 	} else {
 		Acc dh0, dh1;  // out rows 0-7, 8-15
 		dh0.init();
@@ -491,122 +472,55 @@ chain_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 			cp_async_commit();
 		}
 
-		const bool active = tile0 * kTileW < it.dst_w;
 		int cur_vb = vb[0];
 		int cur_slot = wrap(cur_vb % IR, IR);
-		// stage the four 8x8 blocks of every tile and store them
-		auto emit = [&](const uint32_t (&m)[kTilesPerWarp][4], int k) {
-#pragma unroll
-			for (int j = 0; j < kTilesPerWarp; ++j) {
-				char *sa = st_addr + j * 16 * kStageBytes;
-				if (H_FIRST)
-					stsm_x4(sa, m[j][0], m[j][1], m[j][2], m[j][3]);
-				else
-					stsm_x4_trans(sa, m[j][0], m[j][1], m[j][2], m[j][3]);
-			}
-			__syncwarp();
-			const bool rows_in = (it.g_begin + k + 1) * 16 <= it.dst_h;
-#pragma unroll
-			for (int j = 0; j < kTilesPerWarp; ++j) {
-				if (wide[j] && rows_in)
-					*reinterpret_cast<uint4 *>(drow[j]) = *reinterpret_cast<const uint4 *>(ld_addr + j * 16 * kStageBytes);
-				else if ((tile0 + j) * kTileW < it.dst_w)
-					store_tile(it, ld_addr + j * 16 * kStageBytes, (it.g_begin + k) * 16, (tile0 + j) * kTileW);
-			}
-			__syncwarp();
-		};
-		auto load_av = [&](uint4 (&av)[KV][2]) {
-			const uint4 *avs = reinterpret_cast<const uint4 *>(vslots + read_slot * kSlotBytes) + lane;
-#pragma unroll
-			for (int kv = 0; kv < KV; ++kv) {
-				av[kv][0] = avs[(kv * 2 + 0) * 32];
-				av[kv][1] = avs[(kv * 2 + 1) * 32];
-			}
-		};
-		if constexpr (H_FIRST) {
-			// Software pipeline over groups: iteration k runs the horizontal
-			// products of group k + 1 next to the vertical products of group k
-			// (two independent chains per tile), so groups up to k + 1 must
-			// have landed at iteration k.
-			wait_groups(D - 1);
+		for (int k = 0; k < ngroups; ++k) {
+			if (k + D < ngroups)
+				issue(k + D);
+			cp_async_commit();
+			wait_groups(D);
 			__syncthreads();
-			uint32_t bv[kTilesPerWarp][KV][2][2];
-			if (active) {
-#pragma unroll
-				for (int j = 0; j < kTilesPerWarp; ++j)
-					h_part<KV, KH>(it, ring, IR, P, cur_slot, rel[j], ah[j], carry[j], false, bv[j]);
-			}
-			for (int k = 0; k < ngroups; ++k) {
-				if (k + D < ngroups)
-					issue(k + D);
-				cp_async_commit();
-				wait_groups(D - 1);
-				__syncthreads();
 
-				const bool next = k + 1 < ngroups;
-				bool reuse = false;
-				if (next) {
-					const int vbn = vb[k + 1];
-					reuse = KV == 1 && vbn - cur_vb == 8;
-					cur_slot = wrap(cur_slot + (vbn - cur_vb), IR);
-					cur_vb = vbn;
+			const int vbk = vb[k];
+			const bool reuse = H_FIRST && KV == 1 && k > 0 && vbk - cur_vb == 8;
+			cur_slot = wrap(cur_slot + (vbk - cur_vb), IR);
+			cur_vb = vbk;
+			if (tile0 * kTileW < it.dst_w) {
+				const uint4 *avs = reinterpret_cast<const uint4 *>(vslots + read_slot * kSlotBytes) + lane;
+				uint4 av[KV][2];
+#pragma unroll
+				for (int kv = 0; kv < KV; ++kv) {
+					av[kv][0] = avs[(kv * 2 + 0) * 32];
+					av[kv][1] = avs[(kv * 2 + 1) * 32];
 				}
-				if (active) {
-					uint4 av[KV][2];
-					load_av(av);
-					uint32_t bn[kTilesPerWarp][KV][2][2];
-					if (next) {
-#pragma unroll
-						for (int j = 0; j < kTilesPerWarp; ++j)
-							h_part<KV, KH>(it, ring, IR, P, cur_slot, rel[j], ah[j], carry[j], reuse, bn[j]);
-					}
-					uint32_t m[kTilesPerWarp][4];
-#pragma unroll
-					for (int j = 0; j < kTilesPerWarp; ++j)
-						v_part<KV>(it, av, bv[j], m[j]);
-					emit(m, k);
-					if (next) {
-#pragma unroll
-						for (int j = 0; j < kTilesPerWarp; ++j)
-#pragma unroll
-							for (int kv = 0; kv < KV; ++kv)
-#pragma unroll
-								for (int h = 0; h < 2; ++h) {
-									bv[j][kv][h][0] = bn[j][kv][h][0];
-									bv[j][kv][h][1] = bn[j][kv][h][1];
-								}
-					}
-				}
-				read_slot = read_slot + 1 == S ? 0 : read_slot + 1;
+				// the tiles' products interleave; stores follow
+				uint32_t m[kTilesPerWarp][4];
 #pragma unroll
 				for (int j = 0; j < kTilesPerWarp; ++j)
-					drow[j] += group_step;
-			}
-		} else {
-			for (int k = 0; k < ngroups; ++k) {
-				if (k + D < ngroups)
-					issue(k + D);
-				cp_async_commit();
-				wait_groups(D);
-				__syncthreads();
-
-				const int vbk = vb[k];
-				cur_slot = wrap(cur_slot + (vbk - cur_vb), IR);
-				cur_vb = vbk;
-				if (active) {
-					uint4 av[KV][2];
-					load_av(av);
-					uint32_t m[kTilesPerWarp][4];
+					tile_compute<H_FIRST, KV, KH>(it, ring, IR, P, cur_slot, rel[j], ah[j], av, carry[j], reuse, m[j]);
 #pragma unroll
-					for (int j = 0; j < kTilesPerWarp; ++j)
-						tile_compute<H_FIRST, KV, KH>(it, ring, IR, P, cur_slot, rel[j], ah[j], av, carry[j], false, m[j]);
-					emit(m, k);
+				for (int j = 0; j < kTilesPerWarp; ++j) {
+					char *sa = st_addr + j * 16 * kStageBytes;
+					if (H_FIRST)
+						stsm_x4(sa, m[j][0], m[j][1], m[j][2], m[j][3]);
+					else
+						stsm_x4_trans(sa, m[j][0], m[j][1], m[j][2], m[j][3]);
 				}
-				read_slot = read_slot + 1 == S ? 0 : read_slot + 1;
+				__syncwarp();
+				const bool rows_in = (it.g_begin + k + 1) * 16 <= it.dst_h;
 #pragma unroll
-				for (int j = 0; j < kTilesPerWarp; ++j)
-					drow[j] += group_step;
+				for (int j = 0; j < kTilesPerWarp; ++j) {
+					if (wide[j] && rows_in)
+						*reinterpret_cast<uint4 *>(drow[j]) = *reinterpret_cast<const uint4 *>(ld_addr + j * 16 * kStageBytes);
+					else if ((tile0 + j) * kTileW < it.dst_w)
+						store_tile(it, ld_addr + j * 16 * kStageBytes, (it.g_begin + k) * 16, (tile0 + j) * kTileW);
+				}
+				__syncwarp();
 			}
+			read_slot = read_slot + 1 == S ? 0 : read_slot + 1;
+#pragma unroll
+			for (int j = 0; j < kTilesPerWarp; ++j)
+				drow[j] += group_step;
 		}
 		cp_async_wait<0>();
 		__syncthreads();  // the next item rewrites the group bases and the ring
