@@ -401,7 +401,7 @@ __device__ __forceinline__ void load_coef(const Item &it, int g0, int g1, char *
 }
 
 template <bool H_FIRST, bool U16, int HW, int VS>
-__global__ void __launch_bounds__(kThreads, 4)
+__global__ void __launch_bounds__(kThreads, H_FIRST ? 4 : 5)
 fused_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, const __grid_constant__ FusedJob single,
              const __grid_constant__ SmemLayout L)
 {
