@@ -294,7 +294,7 @@ def run_ours(args):
         hsrc = [srcs[i].cpu().pin_memory() for i in range(n_e2e)]
         hdst = [torch.empty(dsts[i].shape, dtype=dsts[i].dtype).pin_memory() for i in range(n_e2e)]
         # the public host-buffer API: chunked, copies overlapping the launches
-        pipe = zg.HostPipeline(convs[:n_e2e], chunks=4, autotune=not args.engine and not args.no_autotune)
+        pipe = zg.HostPipeline(convs[:n_e2e], chunks=8, autotune=not args.engine and not args.no_autotune)
         for _ in range(3):
             pipe.run(hsrc, hdst)
         torch.cuda.synchronize()

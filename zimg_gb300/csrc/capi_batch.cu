@@ -418,22 +418,27 @@ zg_error_code zg_batch_autotune(zg_batch *b, zg_stream stream, unsigned *changed
 				continue;
 			}
 			try {
-				size_t tmp_bytes = 0;
-				for (const Cand &x : cands)
-					tmp_bytes = std::max(tmp_bytes, x.r->tmp_size);
-				DeviceBuffer tmp(tmp_bytes);
+				// each candidate runs as a batch of these jobs (persistent launch,
+				// side streams), as it would inside this batch
 				cudaEvent_t e0 = nullptr, e1 = nullptr;
 				cuda_check(cudaEventCreate(&e0), "event");
 				cuda_check(cudaEventCreate(&e1), "event");
 				const size_t n = std::min(same.size(), kSample);
+				std::vector<zg_batch_io> sub_io;
+				for (size_t k = 0; k < n; ++k)
+					sub_io.push_back(b->io[same[k]]);
 				for (Cand &x : cands) {
+					std::vector<zg_resize_params> ps(n, x.r->params);
+					zg_batch *tb = nullptr;
+					if (zg_error_code rc = zg_batch_create(ps.data(), static_cast<unsigned>(n), &tb))
+						rethrow_last(rc);
+					std::unique_ptr<zg_batch, void (*)(zg_batch *)> hold(tb, zg_batch_free);
+					if (zg_error_code rc = zg_batch_set_io(tb, sub_io.data(), stream))
+						rethrow_last(rc);
+					DeviceBuffer tmp(tb->tmp_size);
 					auto run = [&] {
-						for (size_t s = 0; s < n; ++s) {
-							const zg_batch_io &io = b->io[same[s]];
-							if (zg_error_code rc = zg_resize_process(x.r, io.src, io.src_stride, io.dst, io.dst_stride,
-							                                         tmp.get(), stream))
-								rethrow_last(rc);
-						}
+						if (zg_error_code rc = zg_batch_process(tb, tmp.get(), stream))
+							rethrow_last(rc);
 					};
 					run();  // warm-up
 					x.ms = 1e30f;
