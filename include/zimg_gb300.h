@@ -227,8 +227,9 @@ ZG_API zg_error_code zg_batch_process_graph(zg_batch *b, void *tmp, zg_stream st
  * the autotuner. For every set of jobs with identical parameters and engine
  * ZG_ENGINE_AUTO, times each distinct way the planner can run them (fused
  * CUDA-core kernel, separate CUDA-core passes, tensor-core kernel or passes)
- * on up to 8 of their bound planes (zg_batch_set_io first; their outputs are
- * overwritten with valid results), keeps the fastest and rebuilds the launch
+ * as a batch of up to 64 of their bound planes (zg_batch_set_io first; their
+ * outputs are overwritten with valid results), switches to the fastest when it
+ * beats the planner's own choice by at least 5 %, and rebuilds the launch
  * groups. Allocates scratch for the trials and synchronises the stream. The
  * batch's tmp size may change: query zg_batch_get_tmp_size again. *changed
  * (optional) receives the number of jobs whose plan changed.

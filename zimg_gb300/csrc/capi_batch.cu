@@ -367,9 +367,11 @@ zg_error_code zg_batch_autotune(zg_batch *b, zg_stream stream, unsigned *changed
 		cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
 		unsigned n_changed = 0;
 
-		// jobs with identical parameters are tuned once, on up to kSample of their planes
-		constexpr size_t kSample = 8;
+		// jobs with identical parameters are tuned once, on up to kSample of their
+		// planes; a plan replaces the static one only when it is kMargin faster
+		constexpr size_t kSample = 64;
 		constexpr int kReps = 3;
+		constexpr float kMargin = 0.95f;
 		std::vector<bool> done(b->jobs.size(), false);
 		for (size_t i = 0; i < b->jobs.size(); ++i) {
 			if (done[i])
@@ -458,11 +460,14 @@ zg_error_code zg_batch_autotune(zg_batch *b, zg_stream stream, unsigned *changed
 				free_cands(nullptr);
 				throw;
 			}
-			size_t best = 0;
-			for (size_t c = 1; c < cands.size(); ++c)
+			size_t best = 0, current = 0;
+			for (size_t c = 0; c < cands.size(); ++c) {
 				if (cands[c].ms < cands[best].ms)
 					best = c;
-			if (plan_mode(cands[best].r) == plan_mode(b->jobs[i])) {
+				if (plan_mode(cands[c].r) == plan_mode(b->jobs[i]))
+					current = c;
+			}
+			if (plan_mode(cands[best].r) == plan_mode(b->jobs[i]) || cands[best].ms > kMargin * cands[current].ms) {
 				free_cands(nullptr);
 				continue;
 			}
