@@ -3,8 +3,8 @@
 ctypes front end for two CPU checkers:
 
 * ``Oracle``  — the plain-C restatement in ``oracle/zimg_oracle.c`` (built to
-  ``oracle/_build/liboracle.so``). It exists on every machine, including the GPU
-  box, because ``__graft_entry__.build()`` compiles it there.
+  ``oracle/_build/liboracle.so``). It exists on every machine that runs the
+  tests, because ``__graft_entry__.build()`` compiles it there.
 * ``Reference`` — zimg's own resize code compiled from the reference checkout by
   ``oracle/Makefile`` into ``oracle/_ref/libzimgref.so`` (only where that
   checkout exists). It pins the restatement.

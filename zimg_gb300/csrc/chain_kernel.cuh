@@ -186,54 +186,30 @@ __device__ __forceinline__ void wait_groups(int pending)
 }
 
 // Accumulator of one 16x8 product: the hi and lo tap halves accumulate into
-// the same exact-integer fp32 registers (with ZG_CHAIN_SPLIT_ACC: separate
-// registers, two independent mma chains, added at the end; also exact).
+// the same exact-integer fp32 registers. (Separate registers per half, two
+// independent mma chains, measured no faster.)
 struct Acc {
 	float h[4];
-#ifdef ZG_CHAIN_SPLIT_ACC
-	float l[4];
-#endif
 	__device__ __forceinline__ void init()
 	{
 #pragma unroll
-		for (int i = 0; i < 4; ++i) {
+		for (int i = 0; i < 4; ++i)
 			h[i] = 8192.0f;
-#ifdef ZG_CHAIN_SPLIT_ACC
-			l[i] = 0.0f;
-#endif
-		}
 	}
 	__device__ __forceinline__ void mma(const uint4 &hi, const uint4 &lo, uint32_t b0, uint32_t b1)
 	{
 		const uint32_t ah[4] = { hi.x, hi.y, hi.z, hi.w };
 		const uint32_t al[4] = { lo.x, lo.y, lo.z, lo.w };
 		mma16816(h, ah, b0, b1);
-#ifdef ZG_CHAIN_SPLIT_ACC
-		mma16816(l, al, b0, b1);
-#else
 		mma16816(h, al, b0, b1);
-#endif
 	}
-#ifdef ZG_CHAIN_SPLIT_ACC
-	__device__ __forceinline__ float operator[](int i) const { return h[i] + l[i]; }
-#else
 	__device__ __forceinline__ float operator[](int i) const { return h[i]; }
-#endif
 };
 
 // Two accumulator values -> packed, clamped samples (low / high half).
 __device__ __forceinline__ uint32_t pack(const Acc &a, int i, const Item &it)
 {
-#ifdef ZG_CHAIN_FLOAT_CLAMP
-	const float lo = -(it.magic - 12582912.0f) * 16384.0f;
-	const float hi = (static_cast<float>(it.pmax2 & 0xFFFF) - (it.magic - 12582912.0f)) * 16384.0f;
-	const float a0 = fminf(fmaxf(a[i], lo), hi), a1 = fminf(fmaxf(a[i + 1], lo), hi);
-	const float y0 = __fmaf_rd(a0, 6.103515625e-05f, it.magic);
-	const float y1 = __fmaf_rd(a1, 6.103515625e-05f, it.magic);
-	return __byte_perm(__float_as_uint(y0), __float_as_uint(y1), 0x5410);
-#else
 	return pack_u16x2(a[i], a[i + 1], it.magic, it.pmax2);
-#endif
 }
 
 // Two accumulator values -> the next product's centred fp16 pair.
