@@ -86,7 +86,8 @@ void DevicePass::set_tensor()
 	std::vector<uint4> frag;
 	std::vector<int> kbase;
 	int ksteps = 0;
-	build_wide_tables(table.f32.data(), table.left.data(), table.width, table.rows, &frag, &kbase, &ksteps);
+	build_wide_tables(table.f32.data(), table.left.data(), table.width, table.rows, horizontal, &frag, &kbase,
+	                  &ksteps);
 	const size_t fbytes = frag.size() * sizeof(uint4);
 	const size_t kbytes = kbase.size() * sizeof(int);
 	wide_storage.reset(fbytes + kbytes);

@@ -35,8 +35,9 @@ enum class Sample { U16, F32 };
 // frag[(g * ksteps + s) * 32 + lane] holds the mma.m16n8k8 B fragment of
 // k-step s for that lane, both tf32 halves of each f32 tap:
 //   {b0 high, b1 high, b0 low, b1 low},  b0 = tap(8g + lane/4, kbase + 8s + lane%4),
-//   b1 = the same 4 inputs further; high = tap rounded to tf32,
-//   low = (tap - high) rounded to tf32.
+//   b1 = the same 4 inputs further (horizontal passes: b0 at input
+//   kbase + 8s + 2 (lane%4), b1 the next input, kbase even); high = tap
+//   rounded to tf32, low = (tap - high) rounded to tf32.
 struct WideTables {
 	const uint4 *frag;     // null: the pass runs on the CUDA cores
 	const int *kbase;
@@ -62,7 +63,7 @@ struct PassLaunch {
 
 // Host side of WideTables: fragments and group bases of a pass with `rows`
 // outputs of `width` taps (f32[i * width + k] applies to input left[i] + k).
-void build_wide_tables(const float *f32, const unsigned *left, unsigned width, unsigned rows,
+void build_wide_tables(const float *f32, const unsigned *left, unsigned width, unsigned rows, bool perm_k,
                        std::vector<uint4> *frag, std::vector<int> *kbase, int *ksteps);
 
 cudaError_t launch_wide(const PassLaunch &l, cudaStream_t stream);

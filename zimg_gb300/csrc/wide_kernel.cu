@@ -80,25 +80,54 @@ __device__ __forceinline__ void add4(float (&d)[4], const float (&c)[4])
 // k-steps [s0, s1) of output group g for this lane's rows/columns ma, mb:
 // d += sum of the 3xTF32 products. Element (m, k) of the input is at
 // src + m * sm + k * sk (bytes).
+//
+// Fragment index maps (the B fragments are built to match, build_wide_tables):
+//   PERM_K (horizontal passes): k = tig reads input kb + 8s + 2 tig and
+//     k = tig + 4 reads the next sample, so each lane's pair is adjacent;
+//   otherwise k = tig and tig + 4 read inputs kb + 8s + tig and + tig + 4.
+// PAIR: the lane's two samples of a k-step lie 4 bytes apart (ma, mb adjacent
+// columns in a vertical pass, or the PERM_K pair) and the plane is 8-byte
+// aligned: one 8-byte load each.
+template <bool PERM_K, bool PAIR>
 __device__ __forceinline__ void band_sum(float (&d)[4], const WideTables &w, int g, int s0, int s1, int src_dim,
                                          const char *base_a, const char *base_b, ptrdiff_t sk)
 {
 	const int lane = threadIdx.x & 31, tig = lane & 3;
 	const int kb = __ldg(w.kbase + g);
 	const uint4 *bf = w.frag + static_cast<size_t>(g) * w.ksteps * 32 + lane;
+	const int koff = PERM_K ? 2 * tig : tig;        // this lane's k = tig input
+	const ptrdiff_t khi = PERM_K ? sk : 4 * sk;     // k = tig + 4 relative to k = tig
 	if (kb + 8 * s1 <= src_dim) {
-		const char *pa = base_a + (kb + 8 * s0 + tig) * sk, *pb = base_b + (kb + 8 * s0 + tig) * sk;
-		const ptrdiff_t s4 = 4 * sk, s8 = 8 * sk;
+		const char *pa = base_a + (kb + 8 * s0 + koff) * sk, *pb = base_b + (kb + 8 * s0 + koff) * sk;
+		const ptrdiff_t s8 = 8 * sk;
 		// chunks of 4 k-steps, double-buffered: the loads of the next chunk are
 		// in flight while the current one runs on the tensor cores
 		auto load4 = [&](float (&x)[4][4], uint4 (&b)[4], int s) {
 			const char *qa = pa + static_cast<ptrdiff_t>(s - s0) * s8, *qb = pb + static_cast<ptrdiff_t>(s - s0) * s8;
 #pragma unroll
 			for (int u = 0; u < 4; ++u) {
-				x[u][0] = __ldg(reinterpret_cast<const float *>(qa + u * s8));
-				x[u][1] = __ldg(reinterpret_cast<const float *>(qb + u * s8));
-				x[u][2] = __ldg(reinterpret_cast<const float *>(qa + u * s8 + s4));
-				x[u][3] = __ldg(reinterpret_cast<const float *>(qb + u * s8 + s4));
+				if (PAIR && PERM_K) {
+					// (k = tig, k = tig + 4) of rows ma and mb
+					const float2 va = __ldg(reinterpret_cast<const float2 *>(qa + u * s8));
+					const float2 vb = __ldg(reinterpret_cast<const float2 *>(qb + u * s8));
+					x[u][0] = va.x;
+					x[u][2] = va.y;
+					x[u][1] = vb.x;
+					x[u][3] = vb.y;
+				} else if (PAIR) {
+					// columns ma, mb = ma + 1 of lines k = tig and tig + 4
+					const float2 v0 = __ldg(reinterpret_cast<const float2 *>(qa + u * s8));
+					const float2 v1 = __ldg(reinterpret_cast<const float2 *>(qa + u * s8 + khi));
+					x[u][0] = v0.x;
+					x[u][1] = v0.y;
+					x[u][2] = v1.x;
+					x[u][3] = v1.y;
+				} else {
+					x[u][0] = __ldg(reinterpret_cast<const float *>(qa + u * s8));
+					x[u][1] = __ldg(reinterpret_cast<const float *>(qb + u * s8));
+					x[u][2] = __ldg(reinterpret_cast<const float *>(qa + u * s8 + khi));
+					x[u][3] = __ldg(reinterpret_cast<const float *>(qb + u * s8 + khi));
+				}
 				b[u] = __ldg(bf + (s + u) * 32);
 			}
 		};
@@ -136,8 +165,8 @@ __device__ __forceinline__ void band_sum(float (&d)[4], const WideTables &w, int
 		for (; s < s1; ++s) {
 			const float x0 = __ldg(reinterpret_cast<const float *>(pa));
 			const float x1 = __ldg(reinterpret_cast<const float *>(pb));
-			const float x2 = __ldg(reinterpret_cast<const float *>(pa + s4));
-			const float x3 = __ldg(reinterpret_cast<const float *>(pb + s4));
+			const float x2 = __ldg(reinterpret_cast<const float *>(pa + khi));
+			const float x3 = __ldg(reinterpret_cast<const float *>(pb + khi));
 			float c[4] = { 0.f, 0.f, 0.f, 0.f };
 			step3(c, x0, x1, x2, x3, __ldg(bf + s * 32));
 			add4(d, c);
@@ -147,8 +176,9 @@ __device__ __forceinline__ void band_sum(float (&d)[4], const WideTables &w, int
 	} else {
 		// the block reaches past the last input: clamp (those taps are zero)
 		const int kmax = src_dim - 1;
+		const int kinc = PERM_K ? 1 : 4;
 		for (int s = s0; s < s1; ++s) {
-			const int k0 = min(kb + 8 * s + tig, kmax), k1 = min(kb + 8 * s + tig + 4, kmax);
+			const int k0 = min(kb + 8 * s + koff, kmax), k1 = min(kb + 8 * s + koff + kinc, kmax);
 			const float x0 = __ldg(reinterpret_cast<const float *>(base_a + k0 * sk));
 			const float x1 = __ldg(reinterpret_cast<const float *>(base_b + k0 * sk));
 			const float x2 = __ldg(reinterpret_cast<const float *>(base_a + k1 * sk));
@@ -160,12 +190,13 @@ __device__ __forceinline__ void band_sum(float (&d)[4], const WideTables &w, int
 	}
 }
 
-__device__ __forceinline__ void store_group(const float (&d)[4], int g, int m0, int m_extent, int dst_dim, char *dst,
-                                            ptrdiff_t dm, ptrdiff_t dko)
+// D (m = gid / gid + 8, n = 2 tig, 2 tig + 1) -> outputs; mA, mB: the m that
+// fragment rows gid and gid + 8 stand for.
+__device__ __forceinline__ void store_group(const float (&d)[4], int g, int mA, int mB, int m_extent, int dst_dim,
+                                            char *dst, ptrdiff_t dm, ptrdiff_t dko)
 {
-	const int lane = threadIdx.x & 31, gid = lane >> 2, tig = lane & 3;
+	const int tig = threadIdx.x & 3;
 	const int o = g * 8 + 2 * tig;
-	const int mA = m0 + gid, mB = m0 + gid + 8;
 	if (o < dst_dim) {
 		if (mA < m_extent) *reinterpret_cast<float *>(dst + mA * dm + o * dko) = d[0];
 		if (mB < m_extent) *reinterpret_cast<float *>(dst + mB * dm + o * dko) = d[2];
@@ -181,18 +212,27 @@ __device__ __forceinline__ void store_group(const float (&d)[4], int g, int m0, 
 // with few m, e.g. the horizontal pass after a strong vertical downscale): the
 // CTA's warps share one 16-m tile and split each group's k-steps; the
 // partial sums are added in warp order (deterministic) by warp 0.
-template <int KSPLIT>
+// HORIZ: horizontal pass (m = rows, k = columns, B fragments with PERM_K).
+// PAIR: 8-byte operand loads; the source plane's base and stride are
+// multiples of 8 bytes, and in a vertical pass every tile of [tile_begin,
+// tile_end) is whole, fragment rows gid and gid + 8 standing for the adjacent
+// columns m0 + 2 gid and m0 + 2 gid + 1.
+template <int KSPLIT, bool HORIZ, bool PAIR>
 __global__ void __launch_bounds__(kWideWarps * 32)
 wide_tc_kernel(WideTables w, int m_extent, int src_dim, int dst_dim, const char *__restrict__ src, ptrdiff_t sm,
-               ptrdiff_t sk, char *__restrict__ dst, ptrdiff_t dm, ptrdiff_t dko, int groups_per_block)
+               ptrdiff_t sk, char *__restrict__ dst, ptrdiff_t dm, ptrdiff_t dko, int groups_per_block, int tile_begin,
+               int tile_end)
 {
 	__shared__ float4 red[KSPLIT > 1 ? KSPLIT * 32 : 1];
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	const int gid = lane >> 2;
-	const int m0 = (KSPLIT > 1 ? blockIdx.x : blockIdx.x * kWideWarps + warp) * 16;
-	if (m0 >= m_extent)
+	const int tile = tile_begin + (KSPLIT > 1 ? blockIdx.x : blockIdx.x * kWideWarps + warp);
+	if (tile >= tile_end)
 		return;  // whole CTA when KSPLIT > 1
-	const int ma = min(m0 + gid, m_extent - 1), mb = min(m0 + gid + 8, m_extent - 1);
+	const int m0 = tile * 16;
+	const int mA = (!HORIZ && PAIR) ? m0 + 2 * gid : m0 + gid;
+	const int mB = (!HORIZ && PAIR) ? m0 + 2 * gid + 1 : m0 + gid + 8;
+	const int ma = min(mA, m_extent - 1), mb = min(mB, m_extent - 1);
 	const int g0 = blockIdx.y * groups_per_block;
 	const int g1 = min(w.groups, g0 + groups_per_block);
 	const int KS = w.ksteps;
@@ -200,13 +240,12 @@ wide_tc_kernel(WideTables w, int m_extent, int src_dim, int dst_dim, const char 
 
 	for (int g = g0; g < g1; ++g) {
 		float d[4] = { 0.f, 0.f, 0.f, 0.f };
+		const int per = (KS + KSPLIT - 1) / KSPLIT;
+		const int s0 = KSPLIT == 1 ? 0 : min(KS, warp * per), s1 = KSPLIT == 1 ? KS : min(KS, s0 + per);
+		band_sum<HORIZ, PAIR>(d, w, g, s0, s1, src_dim, base_a, base_b, sk);
 		if (KSPLIT == 1) {
-			band_sum(d, w, g, 0, KS, src_dim, base_a, base_b, sk);
-			store_group(d, g, m0, m_extent, dst_dim, dst, dm, dko);
+			store_group(d, g, mA, mB, m_extent, dst_dim, dst, dm, dko);
 		} else {
-			const int per = (KS + KSPLIT - 1) / KSPLIT;
-			const int s0 = min(KS, warp * per), s1 = min(KS, s0 + per);
-			band_sum(d, w, g, s0, s1, src_dim, base_a, base_b, sk);
 			red[warp * 32 + lane] = make_float4(d[0], d[1], d[2], d[3]);
 			__syncthreads();
 			if (warp == 0) {
@@ -219,7 +258,7 @@ wide_tc_kernel(WideTables w, int m_extent, int src_dim, int dst_dim, const char 
 					t[2] += v.z;
 					t[3] += v.w;
 				}
-				store_group(t, g, m0, m_extent, dst_dim, dst, dm, dko);
+				store_group(t, g, mA, mB, m_extent, dst_dim, dst, dm, dko);
 			}
 			__syncthreads();
 		}
@@ -264,7 +303,7 @@ uint32_t bits(float x)
 
 } // namespace
 
-void build_wide_tables(const float *f32, const unsigned *left, unsigned width, unsigned rows,
+void build_wide_tables(const float *f32, const unsigned *left, unsigned width, unsigned rows, bool perm_k,
                        std::vector<uint4> *frag, std::vector<int> *kbase, int *ksteps)
 {
 	const int groups = static_cast<int>((rows + 7) / 8);
@@ -276,6 +315,8 @@ void build_wide_tables(const float *f32, const unsigned *left, unsigned width, u
 			lo = std::min(lo, left[o]);
 			hi = std::max(hi, left[o] + width);
 		}
+		if (perm_k)
+			lo &= ~1u;  // 8-byte aligned pairs of inputs
 		(*kbase)[g] = static_cast<int>(lo);
 		ks = std::max(ks, static_cast<int>((hi - lo + 7) / 8));
 	}
@@ -291,8 +332,11 @@ void build_wide_tables(const float *f32, const unsigned *left, unsigned width, u
 		for (int s = 0; s < ks; ++s) {
 			for (int lane = 0; lane < 32; ++lane) {
 				const unsigned o = g * 8u + (lane >> 2);
-				const long x = (*kbase)[g] + 8L * s + (lane & 3);
-				const float c0 = tap(o, x), c1 = tap(o, x + 4);
+				const int tig = lane & 3;
+				// inputs of fragment k = tig and k = tig + 4 (see band_sum)
+				const long x0 = (*kbase)[g] + 8L * s + (perm_k ? 2 * tig : tig);
+				const long x1 = x0 + (perm_k ? 1 : 4);
+				const float c0 = tap(o, x0), c1 = tap(o, x1);
 				const float h0 = tf32_round(c0), h1 = tf32_round(c1);
 				const float l0 = tf32_round(c0 - h0), l1 = tf32_round(c1 - h1);
 				(*frag)[(static_cast<size_t>(g) * ks + s) * 32 + lane] = uint4{ bits(h0), bits(h1), bits(l0), bits(l1) };
@@ -300,6 +344,42 @@ void build_wide_tables(const float *f32, const unsigned *left, unsigned width, u
 		}
 	}
 }
+
+namespace {
+
+template <int KSPLIT, bool HORIZ, bool PAIR>
+void launch_tiles(const PassLaunch &l, int m_extent, int src_dim, int dst_dim, ptrdiff_t sm, ptrdiff_t sk, ptrdiff_t dm,
+                  ptrdiff_t dko, int gpb, int t0, int t1, cudaStream_t stream)
+{
+	if (t1 <= t0)
+		return;
+	const int bx = KSPLIT > 1 ? t1 - t0 : (t1 - t0 + kWideWarps - 1) / kWideWarps;
+	const int by = (l.wide.groups + gpb - 1) / gpb;
+	wide_tc_kernel<KSPLIT, HORIZ, PAIR><<<dim3(bx, by), kWideWarps * 32, 0, stream>>>(
+		l.wide, m_extent, src_dim, dst_dim, static_cast<const char *>(l.src), sm, sk, static_cast<char *>(l.dst), dm, dko,
+		gpb, t0, t1);
+}
+
+// One pass: aligned planes take 8-byte loads (in a vertical pass the whole
+// 16-column tiles; a partial last tile runs in a second, 4-byte launch).
+template <int KSPLIT>
+void launch_pass_tiles(const PassLaunch &l, int m_extent, int src_dim, int dst_dim, ptrdiff_t sm, ptrdiff_t sk,
+                       ptrdiff_t dm, ptrdiff_t dko, int gpb, bool aligned8, cudaStream_t stream)
+{
+	const int mtiles = (m_extent + 15) / 16;
+	if (l.horizontal) {
+		if (aligned8)
+			launch_tiles<KSPLIT, true, true>(l, m_extent, src_dim, dst_dim, sm, sk, dm, dko, gpb, 0, mtiles, stream);
+		else
+			launch_tiles<KSPLIT, true, false>(l, m_extent, src_dim, dst_dim, sm, sk, dm, dko, gpb, 0, mtiles, stream);
+		return;
+	}
+	const int whole = aligned8 ? m_extent / 16 : 0;
+	launch_tiles<KSPLIT, false, true>(l, m_extent, src_dim, dst_dim, sm, sk, dm, dko, gpb, 0, whole, stream);
+	launch_tiles<KSPLIT, false, false>(l, m_extent, src_dim, dst_dim, sm, sk, dm, dko, gpb, whole, mtiles, stream);
+}
+
+} // namespace
 
 cudaError_t launch_wide(const PassLaunch &l, cudaStream_t stream)
 {
@@ -309,24 +389,18 @@ cudaError_t launch_wide(const PassLaunch &l, cudaStream_t stream)
 	const ptrdiff_t sm = l.horizontal ? l.src_stride : 4, sk = l.horizontal ? 4 : l.src_stride;
 	const ptrdiff_t dm = l.horizontal ? l.dst_stride : 4, dko = l.horizontal ? 4 : l.dst_stride;
 	const int mtiles = (m_extent + 15) / 16;
+	const bool aligned8 = reinterpret_cast<uintptr_t>(l.src) % 8 == 0 && l.src_stride % 8 == 0;
 	const long sms = sm_count();
-	const long target = sms * 64;  // enough warps for several waves on every SM
+	const int gmin = (l.wide.groups + 65534) / 65535;  // grid y limit
 	if (static_cast<long>(mtiles) * l.wide.groups < sms * 16 && l.wide.ksteps >= 2 * kWideWarps) {
 		// few output tiles: split each group's k-steps across the CTA's warps
-		int gpb = std::max(1, (l.wide.groups + 65534) / 65535);
-		const int by = (l.wide.groups + gpb - 1) / gpb;
-		wide_tc_kernel<kWideWarps><<<dim3(mtiles, by), kWideWarps * 32, 0, stream>>>(
-			l.wide, m_extent, src_dim, dst_dim, static_cast<const char *>(l.src), sm, sk, static_cast<char *>(l.dst), dm,
-			dko, gpb);
+		launch_pass_tiles<kWideWarps>(l, m_extent, src_dim, dst_dim, sm, sk, dm, dko, gmin, aligned8, stream);
 		return cudaGetLastError();
 	}
-	const int bx = (mtiles + kWideWarps - 1) / kWideWarps;
-	int gpb = static_cast<int>(std::max<long>(1, static_cast<long>(mtiles) * l.wide.groups / target));
-	gpb = std::max(std::min(gpb, 8), (l.wide.groups + 65534) / 65535);
-	const int by = (l.wide.groups + gpb - 1) / gpb;
-	wide_tc_kernel<1><<<dim3(bx, by), kWideWarps * 32, 0, stream>>>(l.wide, m_extent, src_dim, dst_dim,
-	                                                                 static_cast<const char *>(l.src), sm, sk,
-	                                                                 static_cast<char *>(l.dst), dm, dko, gpb);
+	// enough warps for several waves on every SM, then longer runs of groups
+	int gpb = static_cast<int>(std::max<long>(1, static_cast<long>(mtiles) * l.wide.groups / (sms * 64)));
+	gpb = std::max(std::min(gpb, 8), gmin);
+	launch_pass_tiles<1>(l, m_extent, src_dim, dst_dim, sm, sk, dm, dko, gpb, aligned8, stream);
 	return cudaGetLastError();
 }
 
