@@ -265,103 +265,6 @@ wide_tc_kernel(WideTables w, int m_extent, int src_dim, int dst_dim, const char 
 	}
 }
 
-// ------------------------------------------------------------------------
-// Vertical passes over 16-byte aligned planes: operands staged in shared
-// memory. A CTA of kWideWarps warps owns kStagedCols columns (one 16-column
-// tile per warp, PAIR fragment mapping) and a run of output groups. The
-// chunks of every group (32 lines = 4 k-steps, with their tap fragments) form
-// one stream through kStages buffers filled by cp.async kStages - 1 chunks
-// ahead, so loads stay in flight across group boundaries. Lines shared by
-// neighbouring groups are fetched again (from L2).
-constexpr int kStagedCols = kWideWarps * 16;
-constexpr int kStagedPitch = kStagedCols + 8;       // floats per staged line (conflict-free 8-byte reads)
-constexpr int kStages = 4;
-constexpr int kChunkLines = 32;                      // 4 k-steps
-constexpr int kStageFloats = kChunkLines * kStagedPitch;
-constexpr int kStageFrag = 4 * 32;                   // uint4 fragments of 4 k-steps
-
-__device__ __forceinline__ void cp_async16_zfill(void *smem, const void *gmem, int src_bytes)
-{
-	const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
-	asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(src_bytes) : "memory");
-}
-
-__global__ void __launch_bounds__(kWideWarps * 32)
-wide_v_staged_kernel(WideTables w, int m_extent, int src_dim, int dst_dim, const char *__restrict__ src,
-                     ptrdiff_t src_stride, char *__restrict__ dst, ptrdiff_t dst_stride, int groups_per_block)
-{
-	__shared__ __align__(16) float lines[kStages][kStageFloats];
-	__shared__ __align__(16) uint4 frags[kStages][kStageFrag];
-	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-	const int gid = lane >> 2, tig = lane & 3;
-	const int c0 = blockIdx.x * kStagedCols;           // first column of the CTA
-	const int g0 = blockIdx.y * groups_per_block;
-	const int g1 = min(w.groups, g0 + groups_per_block);
-	if (g0 >= g1)
-		return;
-	const int KS = w.ksteps;
-	const int nch = (KS + 3) / 4;                      // chunks per group
-	const int total = (g1 - g0) * nch;
-
-	// chunk t: group g0 + t / nch, k-steps 4 (t % nch) .. + 3
-	auto issue = [&](int t) {
-		const int g = g0 + t / nch, c = t - (t / nch) * nch;
-		const int kb = __ldg(w.kbase + g);
-		float *ls = lines[t % kStages];
-		uint4 *fs = frags[t % kStages];
-		// 32 lines x kStagedCols columns in 16-byte chunks
-		for (int i = threadIdx.x; i < kChunkLines * (kStagedCols / 4); i += kWideWarps * 32) {
-			const int r = i / (kStagedCols / 4), q = i - r * (kStagedCols / 4);
-			const int y = kb + 32 * c + r;
-			const int x = c0 + 4 * q;
-			const int n = (y < src_dim) ? max(0, min(4, m_extent - x)) : 0;
-			const char *g_ptr = n ? src + static_cast<ptrdiff_t>(y) * src_stride + static_cast<ptrdiff_t>(x) * 4 : src;
-			cp_async16_zfill(ls + r * kStagedPitch + 4 * q, g_ptr, n * 4);
-		}
-		// fragments of k-steps 4c .. 4c + 3 (zeros past the group's k-steps)
-		for (int i = threadIdx.x; i < kStageFrag; i += kWideWarps * 32) {
-			const int s = 4 * c + i / 32;
-			const bool ok = s < KS;
-			const uint4 *f = w.frag + (static_cast<size_t>(g) * KS + (ok ? s : 0)) * 32 + (i & 31);
-			cp_async16_zfill(fs + i, f, ok ? 16 : 0);
-		}
-	};
-
-	for (int t = 0; t < kStages - 1; ++t) {
-		if (t < total)
-			issue(t);
-		asm volatile("cp.async.commit_group;\n" ::: "memory");
-	}
-	float d[4] = { 0.f, 0.f, 0.f, 0.f };
-	const int colA = warp * 16 + 2 * gid;              // this lane's columns colA, colA + 1 (PAIR)
-	for (int t = 0; t < total; ++t) {
-		asm volatile("cp.async.wait_group %0;\n" ::"n"(kStages - 2) : "memory");
-		__syncthreads();                                // chunk t landed; chunk t - 1 fully consumed
-		if (t + kStages - 1 < total)
-			issue(t + kStages - 1);
-		asm volatile("cp.async.commit_group;\n" ::: "memory");
-
-		const float *ls = lines[t % kStages];
-		const uint4 *fs = frags[t % kStages];
-		float c[4] = { 0.f, 0.f, 0.f, 0.f };
-#pragma unroll
-		for (int u = 0; u < 4; ++u) {
-			const float2 v0 = *reinterpret_cast<const float2 *>(ls + (8 * u + tig) * kStagedPitch + colA);
-			const float2 v1 = *reinterpret_cast<const float2 *>(ls + (8 * u + tig + 4) * kStagedPitch + colA);
-			step3(c, v0.x, v0.y, v1.x, v1.y, fs[u * 32 + lane]);
-		}
-		add4(d, c);
-		const int ch = t % nch;
-		if (ch == nch - 1) {
-			const int g = g0 + t / nch;
-			const int mA = c0 + colA;
-			store_group(d, g, mA, mA + 1, m_extent, dst_dim, dst, 4, dst_stride);
-			d[0] = d[1] = d[2] = d[3] = 0.f;
-		}
-	}
-	asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-}
-
 // Round an f32 to the nearest tf32 (ties away from zero), as cvt.rna.tf32.f32.
 float tf32_round(float x)
 {
@@ -497,15 +400,6 @@ cudaError_t launch_wide(const PassLaunch &l, cudaStream_t stream)
 	// enough warps for several waves on every SM, then longer runs of groups
 	int gpb = static_cast<int>(std::max<long>(1, static_cast<long>(mtiles) * l.wide.groups / (sms * 64)));
 	gpb = std::max(std::min(gpb, 8), gmin);
-	const bool aligned16 = reinterpret_cast<uintptr_t>(l.src) % 16 == 0 && l.src_stride % 16 == 0;
-	if (!l.horizontal && aligned16) {
-		const int bx = (m_extent + kStagedCols - 1) / kStagedCols;
-		const int by = (l.wide.groups + gpb - 1) / gpb;
-		wide_v_staged_kernel<<<dim3(bx, by), kWideWarps * 32, 0, stream>>>(
-			l.wide, m_extent, src_dim, dst_dim, static_cast<const char *>(l.src), l.src_stride, static_cast<char *>(l.dst),
-			l.dst_stride, gpb);
-		return cudaGetLastError();
-	}
 	launch_pass_tiles<1>(l, m_extent, src_dim, dst_dim, sm, sk, dm, dko, gpb, aligned8, stream);
 	return cudaGetLastError();
 }
