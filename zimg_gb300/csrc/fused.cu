@@ -83,6 +83,7 @@ bool plan_fused(const FilterTable &first, const FilterTable &second, bool h_firs
 	const int HW = kHwBuckets[hw_i];
 
 	// dense vertical groups; streaming needs non-decreasing group bases
+	const int kGroup = group_rows(h_first);
 	const int groups = static_cast<int>((dst_h + kGroup - 1) / kGroup);
 	int max_span = 0;
 	std::vector<int> gbase(groups);
@@ -127,7 +128,7 @@ bool plan_fused(const FilterTable &first, const FilterTable &second, bool h_firs
 	p = FusedPlan{};
 	bool fits = false;
 	for (int attempt = 0; attempt < 2 && !fits; ++attempt)
-	for (int step_groups = h_first ? 8 : 4; step_groups >= 1 && !fits; step_groups /= 2) {
+	for (int step_groups = 4; step_groups >= 1 && !fits; step_groups /= 2) {
 		const size_t budget = attempt == 0 ? kSmemBudget : kSmemMax;
 		const int nsteps = (groups + step_groups - 1) / step_groups;
 		auto hi_of = [&](int k) { return gbase[std::min(groups, (k + 1) * step_groups) - 1] + VS; };
@@ -320,13 +321,13 @@ SmemLayout fused_layout(const FusedPlan *const *plans, int n)
 	L.in_off = off;
 	off += h_first ? a16(static_cast<size_t>(L.in_rows) * L.pitch * 4) : 0;
 	L.i_off = off;
-	off += h_first ? 0 : a16(static_cast<size_t>(step_groups) * kGroup * L.pitch * 4);
+	off += h_first ? 0 : a16(static_cast<size_t>(step_groups) * group_rows(false) * L.pitch * 4);
 	L.htaps_off = off;
 	off += a16(static_cast<size_t>(kStripW) * hw * 4);
 	L.hleft_off = off;
 	off += a16(kStripW * 4);
 	L.vcoef_off = off;
-	off += 2 * a16(static_cast<size_t>(step_groups) * vs * kGroup * 4);
+	off += 2 * a16(static_cast<size_t>(step_groups) * vs * group_rows(h_first) * 4);
 	L.vbase_off = off;
 	off += a16(static_cast<size_t>(seg_groups) * 4);
 	L.total_bytes = off;

@@ -24,10 +24,15 @@ namespace zg {
 //              arithmetic bit for bit (resize_impl.cpp:31-59,78-95).
 enum class FusedKind : int { F32 = 0, U16_EXACT = 1 };
 
-// Vertical taps come in groups of kGroup output rows laid out densely over a
+// Vertical taps come in groups of group_rows() output rows laid out densely over a
 // window of VS input lines (VS = 8, 12, 16 or 24); horizontal taps per output
 // column are padded with zeros to HW (6, 8 or 16).
-constexpr int kGroup = 2;
+// Rows per vertical group: 4 for H-first conversions (upscales: one line load
+// feeds 4 rows), 2 for V-first ones (downscales: narrower dense windows).
+__host__ __device__ constexpr int group_rows(bool h_first)
+{
+	return h_first ? 4 : 2;
+}
 constexpr int kStripW = 128;      // output columns per strip
 constexpr int kStreamThreads = 128;
 
@@ -48,7 +53,7 @@ struct FusedJob {
 	int strip_w;            // output columns per strip (kStripW for the CUDA-core kernel)
 	int segments;           // row segments per strip
 	int seg_groups;         // vertical groups per segment (last may be shorter)
-	int groups;             // vertical groups of the plane (ceil(dst_h / kGroup))
+	int groups;             // vertical groups of the plane (ceil(dst_h / group_rows))
 	int step_groups;        // vertical groups per streaming step
 	int item_begin;         // first global item index of this job
 
@@ -61,8 +66,8 @@ struct FusedJob {
 	const float *h_taps;    // [dst_w][hw]
 	const int *h_left;      // [dst_w]
 	int hw;
-	// V pass: dense groups of kGroup output rows over vs input lines
-	const float *v_dense;   // [groups][vs][kGroup]
+	// V pass: dense groups of group_rows output rows over vs input lines
+	const float *v_dense;   // [groups][vs][group_rows]
 	const int *v_base;      // [groups] first input line of each group (non-decreasing)
 	int vs;
 

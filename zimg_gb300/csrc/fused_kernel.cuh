@@ -295,9 +295,9 @@ __device__ __forceinline__ void h_pass(const Item &it, const char *smem, const S
 // Vertical pass for groups [g0, g1): out line (g - g0)*4 + j, columns 4q..4q+3:
 //   sum_s dense[g][s][j] * in[(base[g] + s) & imask][4q + e]
 // FINAL: destination rows g*4 + j (columns c0 + 4q ...); else lines of I.
-template <bool U16, bool FINAL, int VS>
+template <bool U16, bool FINAL, int VS, int kGroup>
 __device__ __forceinline__ void v_pass(const Item &it, const char *smem, const SmemLayout &L, const float *in,
-                                       int imask, int in_pitch, int g0, int g1, const float2 *coef, int quads,
+                                       int imask, int in_pitch, int g0, int g1, const float *coef, int quads,
                                        float *I, int i_pitch)
 {
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -308,7 +308,7 @@ __device__ __forceinline__ void v_pass(const Item &it, const char *smem, const S
 	for (int gi = warp / wpg; gi < ng; gi += kWarps / wpg) {
 		const int g = g0 + gi;
 		const int base = vb[g - it.g_begin];
-		const float2 *cf = coef + gi * VS;  // [line][row] taps of the group's two rows
+		const float *cf = coef + gi * VS * kGroup;  // [line][row] taps of the group's rows
 		int off[VS];
 #pragma unroll
 		for (int s = 0; s < VS; ++s)
@@ -323,8 +323,18 @@ __device__ __forceinline__ void v_pass(const Item &it, const char *smem, const S
 #pragma unroll
 			for (int s = 0; s < VS; ++s) {
 				const float4 x = *reinterpret_cast<const float4 *>(in + off[s] + 4 * q);
-				const float2 c2 = cf[s];
-				const float cj[kGroup] = { c2.x, c2.y };
+				float cj[kGroup];
+				if constexpr (kGroup == 4) {
+					const float4 c4 = reinterpret_cast<const float4 *>(cf)[s];
+					cj[0] = c4.x;
+					cj[1] = c4.y;
+					cj[2] = c4.z;
+					cj[3] = c4.w;
+				} else {
+					const float2 c2 = reinterpret_cast<const float2 *>(cf)[s];
+					cj[0] = c2.x;
+					cj[1] = c2.y;
+				}
 #pragma unroll
 				for (int j = 0; j < kGroup; ++j) {
 					acc[j][0] = __fmaf_rn(cj[j], x.x, acc[j][0]);
@@ -391,7 +401,7 @@ __device__ __forceinline__ int step_end(const Item &it, const char *smem, const 
 	return reinterpret_cast<const int *>(smem + L.vbase_off)[g1 - 1 - it.g_begin] + VS;
 }
 
-template <int VS>
+template <int VS, int kGroup>
 __device__ __forceinline__ void load_coef(const Item &it, int g0, int g1, char *dst)
 {
 	// kGroup floats per line: (g1 - g0) * VS * kGroup * 4 bytes, a multiple of 16 (VS even)
@@ -405,6 +415,7 @@ __global__ void __launch_bounds__(kThreads, H_FIRST ? 4 : 5)
 fused_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, const __grid_constant__ FusedJob single,
              const __grid_constant__ SmemLayout L)
 {
+	constexpr int kGroup = group_rows(H_FIRST);
 	extern __shared__ float4 smem4[];
 	char *smem = reinterpret_cast<char *>(smem4);
 	float *ring = reinterpret_cast<float *>(smem + L.ring_off);
@@ -442,7 +453,7 @@ fused_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 			else
 				load_lines<false>(it, hi_prev, hi, reinterpret_cast<char *>(H_FIRST ? in : ring),
 				                  H_FIRST ? imask : rmask, L.pitch);
-			load_coef<VS>(it, g0, g1, smem + L.vcoef_off);
+			load_coef<VS, kGroup>(it, g0, g1, smem + L.vcoef_off);
 			cp_async_commit();
 		}
 		__syncthreads();  // lines stored by plain loads (unaligned u16) are visible to every converter
@@ -463,7 +474,7 @@ fused_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 				else
 					load_lines<false>(it, hi_cur, hi_next, reinterpret_cast<char *>(H_FIRST ? in : ring),
 					                  H_FIRST ? imask : rmask, L.pitch);
-				load_coef<VS>(it, n0, n1, smem + L.vcoef_off + ((k + 1) & 1) * (L.vbase_off - L.vcoef_off) / 2);
+				load_coef<VS, kGroup>(it, n0, n1, smem + L.vcoef_off + ((k + 1) & 1) * (L.vbase_off - L.vcoef_off) / 2);
 			}
 			cp_async_commit();
 			cp_async_wait<1>();
@@ -471,14 +482,14 @@ fused_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 				convert_lines(it, lo_cur, hi_cur, stage, smask, H_FIRST ? in : ring, H_FIRST ? imask : rmask, L.pitch);
 			__syncthreads();
 
-			const float2 *coef = reinterpret_cast<const float2 *>(smem + L.vcoef_off + (k & 1) * (L.vbase_off - L.vcoef_off) / 2);
+			const float *coef = reinterpret_cast<const float *>(smem + L.vcoef_off + (k & 1) * (L.vbase_off - L.vcoef_off) / 2);
 			if (H_FIRST) {
 				// new source lines -> intermediate ring
 				h_pass<U16, false, HW>(it, smem, L, in, imask, lo_cur, hi_cur, ring, rmask, 0);
 				__syncthreads();
-				v_pass<U16, true, VS>(it, smem, L, ring, rmask, kStripW, g0, g1, coef, kStripW / 4, nullptr, 0);
+				v_pass<U16, true, VS, kGroup>(it, smem, L, ring, rmask, kStripW, g0, g1, coef, kStripW / 4, nullptr, 0);
 			} else {
-				v_pass<U16, false, VS>(it, smem, L, ring, rmask, L.pitch, g0, g1, coef, it.pxa / 4, I, L.pitch);
+				v_pass<U16, false, VS, kGroup>(it, smem, L, ring, rmask, L.pitch, g0, g1, coef, it.pxa / 4, I, L.pitch);
 				__syncthreads();
 				h_pass<U16, true, HW>(it, smem, L, I, 0x7fffffff, 0, (g1 - g0) * kGroup, nullptr, 0, g0 * kGroup);
 			}
