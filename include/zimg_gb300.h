@@ -227,7 +227,7 @@ ZG_API zg_error_code zg_batch_process_graph(zg_batch *b, void *tmp, zg_stream st
  * the autotuner. For every set of jobs with identical parameters and engine
  * ZG_ENGINE_AUTO, times each distinct way the planner can run them (fused
  * CUDA-core kernel, separate CUDA-core passes, tensor-core kernel or passes)
- * as a batch of up to 64 of their bound planes (zg_batch_set_io first; their
+ * as a batch of up to 16 of their bound planes (zg_batch_set_io first; their
  * outputs are overwritten with valid results), switches to the fastest when it
  * beats the planner's own choice by at least 5 %, and rebuilds the launch
  * groups. Allocates scratch for the trials and synchronises the stream. The

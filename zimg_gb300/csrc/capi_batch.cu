@@ -369,8 +369,8 @@ zg_error_code zg_batch_autotune(zg_batch *b, zg_stream stream, unsigned *changed
 
 		// jobs with identical parameters are tuned once, on up to kSample of their
 		// planes; a plan replaces the static one only when it is kMargin faster
-		constexpr size_t kSample = 64;
-		constexpr int kReps = 3;
+		constexpr size_t kSample = 16;
+		constexpr int kReps = 2;
 		constexpr float kMargin = 0.95f;
 		std::vector<bool> done(b->jobs.size(), false);
 		for (size_t i = 0; i < b->jobs.size(); ++i) {
