@@ -3,9 +3,9 @@
 // Arithmetic is that of mma_kernel.cuh (re-centred fp16 samples, int16 taps
 // split into two fp16 halves, fp32 accumulators that the planner proved hold
 // exact integers, zimg's rounding and clamping per pass,
-// resize_impl.cpp:31-42). The data flow differs: each warp owns 16 output
-// columns of a 128-column strip and, per group of 16 output rows, computes
-// both passes itself without shared memory in between:
+// resize_impl.cpp:31-42). The data flow differs: each warp owns one or two
+// 16-column tiles of the CTA's strip of output columns and, per group of 16
+// output rows, computes both passes itself without shared memory in between:
 //
 //   H first:  Dh[16 out cols][8 lines]  = Ah[16 out cols][16 in cols] * src[in cols][lines]
 //             Dv[16 out rows][8 cols]   = Av[16 out rows][16 lines]   * Dh^T
