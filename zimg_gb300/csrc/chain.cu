@@ -282,7 +282,10 @@ SmemLayout chain_layout(const FusedPlan *const *plans, int n)
 	}
 	auto a16 = [](size_t x) { return static_cast<int>((x + 15) / 16 * 16); };
 	SmemLayout L{};
-	L.pitch = (max_pxa + 63) / 64 * 64 + 8;  // lines at 16 mod 128 bytes: fragment loads without bank conflicts
+	// lines at 16 mod 32 bytes: the 8 rows of an ldmatrix phase fall in 8
+	// different 16-byte bank groups, and 4-byte fragment loads of 8 lines x 4
+	// pairs in 32 different banks
+	L.pitch = (max_pxa + 15) / 16 * 16 + 8;
 	L.in_rows = in;
 	L.ring_rows = 1;
 	L.stage_rows = 1;
