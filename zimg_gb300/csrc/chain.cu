@@ -299,8 +299,7 @@ SmemLayout chain_layout(const FusedPlan *const *plans, int n)
 	off += a16(static_cast<size_t>(depth + 2) * kv * 2 * 32 * 16);
 	L.tile_off = off;
 	L.tile_pitch = chain_detail::kStageBytes / 2;
-	off += a16(static_cast<size_t>(chain_detail::kMaxWarps) * chain_detail::kMaxTilesPerWarp * 16 *
-	           chain_detail::kStageBytes);
+	off += a16(static_cast<size_t>(chain_detail::kMaxWarps) * chain_detail::kWarpStage);
 	L.vbase_off = off;
 	off += a16(static_cast<size_t>(seg_groups) * 4);
 	L.ring_off = L.stage_off = L.i_off = L.htaps_off = L.hleft_off = off;

@@ -55,6 +55,8 @@ __host__ __device__ constexpr int tiles_per_warp(int kv, int kh)
 }
 constexpr int kStageBytes = 48;            // staged row: 16 u16 + pad (stmatrix rows without bank conflicts)
 constexpr int kMaxTilesPerWarp = 2;
+constexpr int kTileStage = 16 * kStageBytes + 32;       // a warp's staged tiles lie 32 mod 128 bytes apart
+constexpr int kWarpStage = kMaxTilesPerWarp * kTileStage;
 
 __device__ __forceinline__ void stsm_x4(void *p, uint32_t r0, uint32_t r1, uint32_t r2, uint32_t r3)
 {
@@ -327,13 +329,10 @@ __device__ __forceinline__ void tile_compute(const Item &it, const char *ring, i
 	}
 }
 
-// A staged 16 x 16 tile -> destination rows row0.., columns col0..; one
-// 16-byte half row per lane.
-__device__ __forceinline__ void store_tile(const Item &it, const char *ld_addr, int row0, int col0)
+// One lane's staged 8-sample chunk -> destination row `row`, columns col..,
+// clipped to the plane.
+__device__ __forceinline__ void store_chunk(const Item &it, const char *ld_addr, int row, int col)
 {
-	const int lane = threadIdx.x & 31;
-	const int row = row0 + (lane >> 1);
-	const int col = col0 + (lane & 1) * 8;
 	if (row < it.dst_h && col < it.dst_w) {
 		const uint4 v = *reinterpret_cast<const uint4 *>(ld_addr);
 		uint16_t *d = reinterpret_cast<uint16_t *>(it.dst + static_cast<ptrdiff_t>(row) * it.dst_stride) + col;
@@ -363,7 +362,7 @@ chain_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 	char *vslots = smem + L.vcoef_off;
 	int *vb = reinterpret_cast<int *>(smem + L.vbase_off);
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-	char *stage = smem + L.tile_off + warp * kMaxTilesPerWarp * 16 * kStageBytes;
+	char *stage = smem + L.tile_off + warp * kWarpStage;
 	const int IR = L.in_rows;
 	const int P = L.pitch * 2;
 	constexpr int kSlotBytes = KV * 2 * 32 * 16;
@@ -371,9 +370,19 @@ chain_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 	constexpr int kWarps = warps_per_cta(H_FIRST);
 	constexpr int kThreads = kWarps * 32;
 	constexpr int kStripTiles = kWarps * kTilesPerWarp;
-	// stmatrix / stage read addresses of this lane
+	// stmatrix address of this lane
 	char *st_addr = stage + (((lane >> 4) << 3) + (lane & 7)) * kStageBytes + ((lane >> 3) & 1) * 16;
-	const char *ld_addr = stage + (lane >> 1) * kStageBytes + (lane & 1) * 16;
+	// Stage reads and global stores, one 16-byte chunk per lane. Two tiles per
+	// warp: one store covers 8 rows x 64 bytes (chunk lane & 3 of rows q and
+	// q + 4, q = lane >> 3); one tile: 16 rows x 32 bytes (rows q', q' + 2,
+	// q' + 4, q' + 6 of phase q). Either way the 8 lanes of a phase read 8
+	// different 16-byte bank groups.
+	constexpr int kStoreRows = kTilesPerWarp == 2 ? 8 : 16;
+	constexpr int kStores = 16 / kStoreRows;
+	const int st_row = kTilesPerWarp == 2 ? (lane >> 3) + 4 * ((lane >> 2) & 1)
+	                                      : ((lane >> 3) & 1) + 8 * (lane >> 4) + 2 * ((lane >> 1) & 3);
+	const int st_tile = kTilesPerWarp == 2 ? (lane >> 1) & 1 : 0;
+	const char *ld_addr = stage + st_tile * kTileStage + st_row * kStageBytes + (lane & 1) * 16;
 
 	const int S = L.depth + 2;  // fragment slots in rotation
 
@@ -394,19 +403,14 @@ chain_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 		uint4 ah[kTilesPerWarp][KH][2];
 		int rel[kTilesPerWarp];
 		Carry carry[kTilesPerWarp];
-		// this lane's 16-byte half row of each tile in the item's first group,
-		// advanced by 16 rows per group; whole-tile stores where the tile is
-		// inside the plane
-		char *drow[kTilesPerWarp];
-		bool wide[kTilesPerWarp];
-#pragma unroll
-		for (int j = 0; j < kTilesPerWarp; ++j) {
-			const int col = (tile0 + j) * kTileW + (lane & 1) * 8;
-			wide[j] = it.vec_ok && col + 8 <= it.dst_w;
-			drow[j] = it.dst + static_cast<ptrdiff_t>(it.g_begin * 16 + (lane >> 1)) * it.dst_stride +
-			          static_cast<ptrdiff_t>(col) * 2;
-		}
+		// this lane's destination chunk in the item's first group, advanced by
+		// 16 rows per group; plain 16-byte stores where it is inside the plane
+		const int st_col = (tile0 + st_tile) * kTileW + (lane & 1) * 8;
+		const bool wide = it.vec_ok && st_col + 8 <= it.dst_w;
+		char *drow = it.dst + static_cast<ptrdiff_t>(it.g_begin * 16 + st_row) * it.dst_stride +
+		             static_cast<ptrdiff_t>(st_col) * 2;
 		const ptrdiff_t group_step = 16 * it.dst_stride;
+		const ptrdiff_t store_step = kStoreRows * it.dst_stride;
 #pragma unroll
 		for (int j = 0; j < kTilesPerWarp; ++j) {
 			const int tile = min(tile0 + j, ntiles - 1);
@@ -476,7 +480,7 @@ chain_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 					tile_compute<H_FIRST, KV, KH>(it, ring, IR, P, cur_slot, rel[j], ah[j], av, carry[j], reuse, m[j]);
 #pragma unroll
 				for (int j = 0; j < kTilesPerWarp; ++j) {
-					char *sa = st_addr + j * 16 * kStageBytes;
+					char *sa = st_addr + j * kTileStage;
 					if (H_FIRST)
 						stsm_x4(sa, m[j][0], m[j][1], m[j][2], m[j][3]);
 					else
@@ -484,19 +488,21 @@ chain_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 				}
 				__syncwarp();
 				const bool rows_in = (it.g_begin + k + 1) * 16 <= it.dst_h;
+				if (wide && rows_in) {
 #pragma unroll
-				for (int j = 0; j < kTilesPerWarp; ++j) {
-					if (wide[j] && rows_in)
-						*reinterpret_cast<uint4 *>(drow[j]) = *reinterpret_cast<const uint4 *>(ld_addr + j * 16 * kStageBytes);
-					else if ((tile0 + j) * kTileW < it.dst_w)
-						store_tile(it, ld_addr + j * 16 * kStageBytes, (it.g_begin + k) * 16, (tile0 + j) * kTileW);
+					for (int i = 0; i < kStores; ++i)
+						*reinterpret_cast<uint4 *>(drow + i * store_step) =
+							*reinterpret_cast<const uint4 *>(ld_addr + i * kStoreRows * kStageBytes);
+				} else {
+#pragma unroll
+					for (int i = 0; i < kStores; ++i)
+						store_chunk(it, ld_addr + i * kStoreRows * kStageBytes,
+						            (it.g_begin + k) * 16 + st_row + i * kStoreRows, st_col);
 				}
 				__syncwarp();
 			}
 			read_slot = read_slot + 1 == S ? 0 : read_slot + 1;
-#pragma unroll
-			for (int j = 0; j < kTilesPerWarp; ++j)
-				drow[j] += group_step;
+			drow += group_step;
 		}
 		cp_async_wait<0>();
 		__syncthreads();  // the next item rewrites the group bases and the ring
