@@ -188,8 +188,8 @@ bool plan_chain(const FilterTable &first, const FilterTable &second, bool h_firs
 		J.strips = strips;
 		J.strip_w = strip_w;
 		J.groups = groups;
-		J.seg_groups = groups;
-		J.segments = 1;
+		J.seg_groups = 1;  // work units: (strip, group) pairs, split evenly over the CTAs
+		J.segments = groups;
 		J.step_groups = 1;
 		J.in_rows = ring;
 		J.ring_rows = 1;
@@ -276,7 +276,7 @@ SmemLayout chain_layout(const FusedPlan *const *plans, int n)
 		const FusedPlan &p = *plans[i];
 		max_pxa = std::max(max_pxa, p.max_pxa);
 		in = std::max(in, p.job.in_rows);
-		seg_groups = std::max(seg_groups, p.job.seg_groups);
+		seg_groups = std::max(seg_groups, p.job.groups);  // an item spans up to a whole strip
 		depth = std::max(depth, p.depth);
 		kv = std::max(kv, p.job.vs);
 	}

@@ -91,12 +91,15 @@ struct Item {
 	uint32_t pmax2, bias_h2;
 };
 
-__device__ __forceinline__ Item make_item(const FusedJob &J, int t, int strip_tiles, int nthreads)
+// Units t .. t_end - 1 of job J that lie in the strip of unit t: a work item.
+// A job's units are its (strip, 16-row group) pairs, strip-major.
+__device__ __forceinline__ Item make_item(const FusedJob &J, int t, int t_end, int strip_tiles, int nthreads)
 {
 	Item it;
 	const int local = t - J.item_begin;
-	const int seg = local / J.strips;
-	it.strip = local - seg * J.strips;
+	it.strip = local / J.groups;
+	it.g_begin = local - it.strip * J.groups;
+	it.g_end = min(J.groups, it.g_begin + (t_end - t));
 	it.src = static_cast<const char *>(J.src);
 	it.src_stride = J.src_stride;
 	it.dst = static_cast<char *>(J.dst);
@@ -109,8 +112,6 @@ __device__ __forceinline__ Item make_item(const FusedJob &J, int t, int strip_ti
 	it.c0 = it.strip * strip_tiles * kTileW;
 	it.xlo = __ldg(J.win_col + 2 * it.strip);
 	const int pxa = (__ldg(J.win_col + 2 * it.strip + 1) - it.xlo + 7) & ~7;
-	it.g_begin = seg * J.seg_groups;
-	it.g_end = min(J.groups, it.g_begin + J.seg_groups);
 	it.depth = J.depth;
 	it.magic = J.magic;
 	const uint32_t pm = static_cast<uint32_t>(J.pixel_max);
@@ -391,9 +392,13 @@ chain_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 		reinterpret_cast<float4 *>(ring)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
 	__syncthreads();
 
-	for (int t = blockIdx.x; t < total_items; t += gridDim.x) {
+	// this CTA's equal share of the launch's units, in job / strip / group
+	// order: whole strips where they fit, split at most at its two ends
+	const int t_end = static_cast<int>(static_cast<long long>(blockIdx.x + 1) * total_items / gridDim.x);
+	for (int t = static_cast<int>(static_cast<long long>(blockIdx.x) * total_items / gridDim.x); t < t_end;) {
 		const FusedJob *Jp = jobs ? &jobs[find_job(jobs, num_jobs, t)] : &single;
-		const Item it = make_item(*Jp, t, kStripTiles, kThreads);
+		const Item it = make_item(*Jp, t, t_end, kStripTiles, kThreads);
+		t += it.g_end - it.g_begin;
 		for (int g = it.g_begin + threadIdx.x; g < it.g_end; g += kThreads)
 			vb[g - it.g_begin] = __ldg(Jp->v_base + g);
 

@@ -228,6 +228,13 @@ void fused_segment(FusedPlan *const *plans, int n, int num_items_target)
 	const int want = static_cast<int>(std::max<long>(1, (num_items_target + strips - 1) / std::max<long>(1, strips)));
 	for (int i = 0; i < n; ++i) {
 		FusedJob &J = plans[i]->job;
+		if (plans[i]->chain) {
+			// the chained kernel splits the (strip, group) units evenly over
+			// its CTAs: one unit per segment
+			J.seg_groups = 1;
+			J.segments = J.groups;
+			continue;
+		}
 		const int steps = (J.groups + J.step_groups - 1) / J.step_groups;
 		const int segs = std::max(1, std::min(want, steps));
 		const int steps_per_seg = (steps + segs - 1) / segs;

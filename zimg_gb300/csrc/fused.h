@@ -51,7 +51,7 @@ struct FusedJob {
 	// work items: strips x row segments
 	int strips;             // ceil(dst_w / strip_w)
 	int strip_w;            // output columns per strip (kStripW for the CUDA-core kernel)
-	int segments;           // row segments per strip
+	int segments;           // row segments per strip (chained kernel: one per group)
 	int seg_groups;         // vertical groups per segment (last may be shorter)
 	int groups;             // vertical groups of the plane (ceil(dst_h / group_rows))
 	int step_groups;        // vertical groups per streaming step
