@@ -24,6 +24,7 @@ constexpr int kHwBuckets[] = { 6, 8, 16 };
 constexpr int kVsBuckets[] = { 8, 12, 16, 24 };
 constexpr size_t kSmemBudget = 56 * 1024;   // preferred: four CTAs of 128 threads per SM
 constexpr size_t kSmemMax = 110 * 1024;     // hard limit: two CTAs per SM
+constexpr int kItemGroupsMax = 256;          // groups of one work item (a multiple of every step)
 
 int bucket_index(const int *b, int n, int v)
 {
@@ -160,8 +161,8 @@ bool plan_fused(const FilterTable &first, const FilterTable &second, bool h_firs
 		J.vs = VS;
 		J.step_groups = step_groups;
 		J.groups = groups;
-		J.seg_groups = groups;
-		J.segments = 1;
+		J.seg_groups = step_groups;  // work units: (strip, step) pairs, split evenly over the CTAs
+		J.segments = nsteps;
 		J.ring_rows = pow2(ring_need);
 		J.in_rows = h_first ? pow2(in_need) : 1;
 		p.max_pxa = max_pxa;
@@ -228,11 +229,11 @@ void fused_segment(FusedPlan *const *plans, int n, int num_items_target)
 	const int want = static_cast<int>(std::max<long>(1, (num_items_target + strips - 1) / std::max<long>(1, strips)));
 	for (int i = 0; i < n; ++i) {
 		FusedJob &J = plans[i]->job;
-		if (plans[i]->chain) {
-			// the chained kernel splits the (strip, group) units evenly over
-			// its CTAs: one unit per segment
-			J.seg_groups = 1;
-			J.segments = J.groups;
+		if (!plans[i]->mma || plans[i]->chain) {
+			// the CUDA-core and chained kernels split their (strip, step)
+			// units evenly over their CTAs: one unit per segment
+			J.seg_groups = J.step_groups;
+			J.segments = (J.groups + J.step_groups - 1) / J.step_groups;
 			continue;
 		}
 		const int steps = (J.groups + J.step_groups - 1) / J.step_groups;
@@ -307,7 +308,7 @@ SmemLayout fused_layout(const FusedPlan *const *plans, int n)
 		ring = std::max(ring, p.job.ring_rows);
 		in = std::max(in, p.job.in_rows);
 		stage = std::max(stage, p.stage_rows);
-		seg_groups = std::max(seg_groups, p.job.seg_groups);
+		seg_groups = std::max(seg_groups, std::min(p.job.groups, kItemGroupsMax));
 		step_groups = std::max(step_groups, p.job.step_groups);
 		u16 = p.job.kind == static_cast<int>(FusedKind::U16_EXACT);
 		h_first = p.job.h_first != 0;

@@ -80,17 +80,21 @@ struct Item {
 	const int *v_base;
 	int src_w, src_h, dst_h, vec_ok;
 	int c0, cols_valid, xlo, pxa;
-	int g_begin, g_end, step_groups;
+	int g_begin, g_end, step_groups, units;
 	float magic, pixel_max, offset;
 };
 
+// Units t .. t_end - 1 of job J that lie in the strip of unit t, at most
+// L.seg_groups groups of them: a work item. A job's units are its (strip,
+// streaming step) pairs, strip-major.
 template <int HW>
-__device__ __forceinline__ Item make_item(const FusedJob &J, int t, char *smem, const SmemLayout &L)
+__device__ __forceinline__ Item make_item(const FusedJob &J, int t, int t_end, char *smem, const SmemLayout &L)
 {
 	Item it;
 	const int local = t - J.item_begin;
-	const int seg = local / J.strips;
-	const int strip = local - seg * J.strips;
+	const int strip = local / J.segments;
+	const int step0 = local - strip * J.segments;
+	it.units = max(1, min(min(J.segments - step0, t_end - t), L.seg_groups / J.step_groups));
 	it.src = static_cast<const char *>(J.src);
 	it.src_stride = J.src_stride;
 	it.dst = static_cast<char *>(J.dst);
@@ -105,8 +109,8 @@ __device__ __forceinline__ Item make_item(const FusedJob &J, int t, char *smem, 
 	it.cols_valid = min(kStripW, J.dst_w - it.c0);
 	it.xlo = __ldg(J.win_col + 2 * strip);
 	it.pxa = (__ldg(J.win_col + 2 * strip + 1) - it.xlo + 7) & ~7;
-	it.g_begin = seg * J.seg_groups;
-	it.g_end = min(J.groups, it.g_begin + J.seg_groups);
+	it.g_begin = step0 * J.step_groups;
+	it.g_end = min(J.groups, (step0 + it.units) * J.step_groups);
 	it.step_groups = J.step_groups;
 	it.magic = J.magic;
 	it.pixel_max = J.pixel_max;
@@ -431,9 +435,12 @@ fused_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 		smem4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
 	__syncthreads();
 
-	for (int t = blockIdx.x; t < total_items; t += gridDim.x) {
+	// this CTA's equal share of the launch's units, in job / strip / step order
+	const int t_end = static_cast<int>(static_cast<long long>(blockIdx.x + 1) * total_items / gridDim.x);
+	for (int t = static_cast<int>(static_cast<long long>(blockIdx.x) * total_items / gridDim.x); t < t_end;) {
 		const FusedJob *Jp = jobs ? &jobs[find_job(jobs, num_jobs, t)] : &single;
-		const Item it = make_item<HW>(*Jp, t, smem, L);
+		const Item it = make_item<HW>(*Jp, t, t_end, smem, L);
+		t += it.units;
 		__syncthreads();  // group bases visible
 
 		const int nsteps = (it.g_end - it.g_begin + it.step_groups - 1) / it.step_groups;
