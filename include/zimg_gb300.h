@@ -89,6 +89,14 @@ typedef enum zg_engine {
 ZG_API zg_error_code zg_get_last_error(char *err_msg, size_t n);
 ZG_API void zg_clear_last_error(void);
 
+/* Health of the pipelined kernels on the current device: 0, or the cause of
+ * the first bounded wait that ran out inside one (1: a group's copies never
+ * landed, 2: a buffer was never released, 3: a ring too small for a group).
+ * Nonzero means a library fault, not a caller error; the outputs of the
+ * launches involved are not valid. With reset != 0 the word is cleared.
+ * No zimg counterpart (zimg has no asynchronous device work). */
+ZG_API int zg_pipeline_status(int reset);
+
 /* Version of this library. Replaces zimg_get_version_info (zimg.h:54). */
 ZG_API void zg_get_version_info(unsigned *major, unsigned *minor, unsigned *micro);
 

@@ -54,3 +54,15 @@ def cuda(lib):
         pytest.fail("GPU test selected but no CUDA device is visible")
     torch.cuda.init()
     return torch.device("cuda:0")
+
+
+@pytest.fixture(autouse=True)
+def pipeline_healthy(request):
+    """After every GPU test: no bounded wait inside a pipelined kernel ran out."""
+    yield
+    if request.node.get_closest_marker("gpu") is None or "cuda" not in request.fixturenames:
+        return
+    import torch
+    torch.cuda.synchronize()
+    lib = request.getfixturevalue("lib")
+    assert lib.zg_pipeline_status(1) == 0, "a pipelined kernel's bounded wait ran out"

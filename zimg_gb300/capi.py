@@ -89,6 +89,7 @@ BUFFER_MAX = 0xFFFFFFFF
 _P = C.c_void_p
 SIGNATURES = [
     ("zg_get_last_error", C.c_int, [C.c_char_p, C.c_size_t]),
+    ("zg_pipeline_status", C.c_int, [C.c_int]),
     ("zg_clear_last_error", None, []),
     ("zg_get_version_info", None, [C.POINTER(C.c_uint)] * 3),
     ("zg_compute_filter", C.c_int, [C.c_int, C.c_double, C.c_double, C.c_uint, C.c_uint, C.c_double, C.c_double,

@@ -170,6 +170,11 @@ void check_plane(const void *p, ptrdiff_t stride, unsigned w, Sample s, const ch
 
 extern "C" {
 
+int zg_pipeline_status(int reset)
+{
+	return chain_tma_pipeline_error(reset != 0);
+}
+
 zg_error_code zg_get_last_error(char *err_msg, size_t n)
 {
 	if (err_msg && n) {
@@ -336,6 +341,11 @@ zg_error_code zg_resize_create(const zg_resize_params *params, zg_resize **out)
 				const FusedPlan *pp = &r->fplan;
 				r->flayout = fused_layout(&pp, 1);
 				r->fgrid = fused_grid_size(r->fplan.variant, static_cast<size_t>(r->flayout.total_bytes));
+				if (r->fplan.chain && chain_tma_enabled()) {
+					r->tma = chain_tma_layout(&pp, 1, &r->tlayout);
+					if (r->tma)
+						r->tgrid = chain_tma_grid_size(r->fplan.variant, static_cast<size_t>(r->tlayout.total_bytes));
+				}
 				r->fused = true;
 				r->tmp_size = 0;
 			}
@@ -403,6 +413,13 @@ zg_error_code zg_resize_process(const zg_resize *r, const void *src, ptrdiff_t s
 			FusedJob j = r->fplan.job;
 			fused_set_io(j, src, src_stride, dst, dst_stride);
 			j.item_begin = 0;
+			CUtensorMap map;
+			if (r->tma && chain_tma_source_map(&map, j, r->tlayout)) {
+				cuda_check(launch_chain_tma(r->fplan.variant, nullptr, 1, fused_items(j), r->tlayout, r->tgrid, j, &map,
+				                            st),
+				           "fused resize launch");
+				return;
+			}
 			cuda_check(launch_fused(r->fplan.variant, nullptr, 1, fused_items(j), r->flayout, r->fgrid,
 			                        j, st), "fused resize launch");
 			return;

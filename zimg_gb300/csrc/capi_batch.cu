@@ -22,6 +22,12 @@ struct zg_batch {
 		int first;  // first entry in the device job table
 		int count;
 		int tiles;
+		// chained groups: the TMA-pipelined kernel, when every source plane
+		// of the group has a tensor map (decided at each io upload)
+		bool tma_plan = false;
+		bool tma_now = false;
+		SmemLayout tlayout{};
+		int tgrid = 0;
 	};
 
 	int device;
@@ -33,6 +39,8 @@ struct zg_batch {
 	std::vector<Group> groups;
 	std::vector<FusedJob> table_host;
 	DeviceBuffer table_dev;
+	std::vector<CUtensorMap> maps_host;  // per table entry (chained TMA groups)
+	DeviceBuffer maps_dev;
 	// identity conversions: one batched copy launch
 	std::vector<int> copy_jobs;
 	std::vector<PlaneCopy> copy_host;
@@ -82,8 +90,13 @@ void batch_launch(const zg_batch *b, void *tmp, cudaStream_t st)
 	for (const auto &g : b->groups) {
 		work.push_back([&g, table](cudaStream_t s) {
 			FusedJob unused{};
-			cuda_check(launch_fused(g.variant, table + g.first, g.count, g.tiles, g.layout, g.grid, unused, s),
-			           "fused batch launch");
+			if (g.tma_now)
+				cuda_check(launch_chain_tma(g.variant, table + g.first, g.count, g.tiles, g.tlayout, g.tgrid, unused,
+				                            nullptr, s),
+				           "fused batch launch");
+			else
+				cuda_check(launch_fused(g.variant, table + g.first, g.count, g.tiles, g.layout, g.grid, unused, s),
+				           "fused batch launch");
 		});
 	}
 	if (!b->copy_jobs.empty()) {
@@ -176,10 +189,18 @@ void regroup(zg_batch *b)
 		}
 		g.layout = fused_layout(plans.data(), static_cast<int>(plans.size()));
 		g.grid = fused_grid_size(g.variant, static_cast<size_t>(g.layout.total_bytes));
+		if (plans[0]->chain && chain_tma_enabled()) {
+			g.tma_plan = chain_tma_layout(plans.data(), static_cast<int>(plans.size()), &g.tlayout);
+			if (g.tma_plan)
+				g.tgrid = chain_tma_grid_size(g.variant, static_cast<size_t>(g.tlayout.total_bytes));
+		}
 		b->groups.push_back(g);
 	}
-	if (!b->table_host.empty())
+	if (!b->table_host.empty()) {
 		b->table_dev.reset(b->table_host.size() * sizeof(FusedJob));
+		b->maps_host.assign(b->table_host.size(), CUtensorMap{});
+		b->maps_dev.reset(b->table_host.size() * sizeof(CUtensorMap));
+	}
 	b->copy_jobs.clear();
 	for (unsigned i = 0; i < num_jobs; ++i)
 		if (b->jobs[i]->num_passes == 0)
@@ -221,6 +242,20 @@ void upload_io(zg_batch *b, cudaStream_t st)
 		p.chunk_begin = b->copy_chunks;
 		b->copy_chunks += static_cast<unsigned long long>(p.chunks_per_row) * p.rows;
 	}
+	// tensor maps of the chained groups' source planes
+	bool any_map = false;
+	for (auto &g : b->groups) {
+		g.tma_now = g.tma_plan;
+		for (int e = g.first; g.tma_now && e < g.first + g.count; ++e)
+			g.tma_now = chain_tma_source_map(&b->maps_host[e], b->table_host[e], g.tlayout);
+		for (int e = g.first; e < g.first + g.count; ++e)
+			b->table_host[e].tmap = g.tma_now ? static_cast<const CUtensorMap *>(b->maps_dev.get()) + e : nullptr;
+		any_map = any_map || g.tma_now;
+	}
+	if (any_map)
+		cuda_check(cudaMemcpyAsync(b->maps_dev.get(), b->maps_host.data(), b->maps_host.size() * sizeof(CUtensorMap),
+		                           cudaMemcpyHostToDevice, st),
+		           "batch io upload");
 	if (!b->copy_host.empty())
 		cuda_check(cudaMemcpyAsync(b->copy_dev.get(), b->copy_host.data(), b->copy_host.size() * sizeof(PlaneCopy),
 		                           cudaMemcpyHostToDevice, st), "batch io upload");

@@ -142,4 +142,9 @@ struct zg_resize {
 	zg::DeviceBuffer fblob;
 	zg::SmemLayout flayout{};
 	int fgrid = 0;
+	// chained plans: the TMA-pipelined kernel's layout, used when the source
+	// plane admits a tensor map
+	bool tma = false;
+	zg::SmemLayout tlayout{};
+	int tgrid = 0;
 };

@@ -1,0 +1,199 @@
+// Host side of the TMA-pipelined chained kernel (chain_tma_kernel.cuh):
+// shared-memory layout, source tensor maps, launch, instantiations.
+#include "chain_tma_kernel.cuh"
+#include "fused.h"
+
+#include <algorithm>
+#include <cstdint>
+#include <cstdlib>
+#include <mutex>
+
+namespace zg {
+
+namespace {
+
+constexpr size_t kTmaSmemMax = 110 * 1024;  // two CTAs per SM
+constexpr int kKVMax = 3;
+constexpr int kKHMax = 4;
+constexpr int kMaxBoxW = 256;               // tensor-copy box limit per dimension
+constexpr int kAlignSlack = 128;            // the kernel aligns its shared-memory base to 128 bytes
+
+using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                 const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// The driver's tensor-map encoder, looked up once through the runtime.
+EncodeTiled encoder()
+{
+	static EncodeTiled fn = nullptr;
+	static std::once_flag once;
+	std::call_once(once, [] {
+		void *p = nullptr;
+		cudaDriverEntryPointQueryResult q{};
+		if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) == cudaSuccess &&
+		    q == cudaDriverEntryPointSuccess)
+			fn = reinterpret_cast<EncodeTiled>(p);
+	});
+	return fn;
+}
+
+template <bool HF, int KV, int KH>
+const void *tma_ptr()
+{
+	return reinterpret_cast<const void *>(&chain_detail::chain_tma_kernel<HF, KV, KH>);
+}
+
+template <bool HF, int KV>
+const void *tma_ptr_kh(int kh)
+{
+	switch (kh) {
+	case 1: return tma_ptr<HF, KV, 1>();
+	case 2: return tma_ptr<HF, KV, 2>();
+	case 3: return tma_ptr<HF, KV, 3>();
+	default: return tma_ptr<HF, KV, 4>();
+	}
+}
+
+template <bool HF>
+const void *tma_ptr_kv(int kv, int kh)
+{
+	return kv == 1 ? tma_ptr_kh<HF, 1>(kh) : (kv == 2 ? tma_ptr_kh<HF, 2>(kh) : tma_ptr_kh<HF, 3>(kh));
+}
+
+int tma_threads(int variant)
+{
+	return chain_detail::tma_threads(variant - 200 >= kKVMax * kKHMax);
+}
+
+} // namespace
+
+const void *chain_tma_kernel_ptr(int variant)
+{
+	const int v = variant - 200;
+	const int per = kKVMax * kKHMax;
+	const bool hf = v >= per;
+	const int kv = (v % per) / kKHMax + 1, kh = v % kKHMax + 1;
+	return hf ? tma_ptr_kv<true>(kv, kh) : tma_ptr_kv<false>(kv, kh);
+}
+
+bool chain_tma_enabled()
+{
+	// opt-in: on GB300 it measured level with the cp.async form on FHD->UHD
+	// and a few per cent slower on mixed batches
+	static const bool on = [] {
+		const char *e = std::getenv("ZG_CHAIN_TMA");
+		return e && e[0] == '1';
+	}();
+	return on;
+}
+
+bool chain_tma_layout(const FusedPlan *const *plans, int n, SmemLayout *out)
+{
+	int max_pxa = 0, in = 1, groups = 1, depth = 1, kv = 1;
+	for (int i = 0; i < n; ++i) {
+		const FusedPlan &p = *plans[i];
+		if (!p.chain)
+			return false;
+		max_pxa = std::max(max_pxa, p.max_pxa);
+		in = std::max(in, p.job.in_rows);
+		groups = std::max(groups, p.job.groups);
+		depth = std::max(depth, p.depth);
+		kv = std::max(kv, p.job.vs);
+	}
+	auto a16 = [](size_t x) { return static_cast<int>((x + 15) / 16 * 16); };
+	SmemLayout L{};
+	// box rows of 16 mod 32 bytes, as the cp.async form's lines
+	L.pitch = (max_pxa + 15) / 16 * 16 + 8;
+	if (L.pitch > kMaxBoxW)
+		return false;
+	// blocks covering any window span of `in` lines, block-rounded at both ends
+	const int blocks = (in + 2 * (chain_detail::kBlockLines - 1)) / chain_detail::kBlockLines + 1;
+	L.in_rows = blocks * chain_detail::kBlockLines;
+	L.depth = depth;
+	L.ring_rows = depth + 2;  // pipeline stages
+	L.stage_rows = 1;
+	L.seg_groups = groups;
+	L.step_groups = 1;
+	int off = 0;
+	L.in_off = off;
+	off += a16(static_cast<size_t>(L.in_rows) * L.pitch * 2);
+	L.vcoef_off = off;
+	off += a16(static_cast<size_t>(L.ring_rows) * kv * 2 * 32 * 16);
+	L.tile_off = off;
+	L.tile_pitch = chain_detail::kStageBytes / 2;
+	off += a16(static_cast<size_t>(chain_detail::kMaxWarps) * chain_detail::kWarpStage);
+	L.vbase_off = off;
+	off += a16(static_cast<size_t>(groups) * 4);
+	L.stage_off = off;  // full and empty mbarriers
+	off += a16(static_cast<size_t>(L.ring_rows) * 2 * 8);
+	L.ring_off = L.i_off = L.htaps_off = L.hleft_off = off;
+	L.total_bytes = off + kAlignSlack;
+	*out = L;
+	return static_cast<size_t>(L.total_bytes) <= kTmaSmemMax;
+}
+
+bool chain_tma_source_map(CUtensorMap *map, const FusedJob &j, const SmemLayout &L)
+{
+	const uintptr_t a = reinterpret_cast<uintptr_t>(j.src);
+	if (!j.src || a % 16 || j.src_stride <= 0 || j.src_stride % 16 || j.src_w < 1 || j.src_h < 1)
+		return false;
+	if (L.pitch > kMaxBoxW || (L.pitch * 2) % 16)
+		return false;
+	EncodeTiled fn = encoder();
+	if (!fn)
+		return false;
+	const cuuint64_t dims[2] = { static_cast<cuuint64_t>(j.src_w), static_cast<cuuint64_t>(j.src_h) };
+	const cuuint64_t strides[1] = { static_cast<cuuint64_t>(j.src_stride) };
+	const cuuint32_t box[2] = { static_cast<cuuint32_t>(L.pitch), static_cast<cuuint32_t>(chain_detail::kBlockLines) };
+	const cuuint32_t estr[2] = { 1, 1 };
+	return fn(map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, const_cast<void *>(j.src), dims, strides, box, estr,
+	          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+	          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+int chain_tma_grid_size(int variant, size_t smem_bytes)
+{
+	int dev = 0, sms = 0, per_sm = 0;
+	cudaGetDevice(&dev);
+	cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+	const void *k = chain_tma_kernel_ptr(variant);
+	cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kTmaSmemMax));
+	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, tma_threads(variant), smem_bytes) != cudaSuccess ||
+	    per_sm < 1)
+		per_sm = 1;
+	return std::max(1, sms) * per_sm;
+}
+
+cudaError_t launch_chain_tma(int variant, const FusedJob *jobs, int num_jobs, int total_items, const SmemLayout &L,
+                             int grid, const FusedJob &single, const CUtensorMap *single_map, cudaStream_t stream)
+{
+	if (static_cast<size_t>(L.total_bytes) > kTmaSmemMax || (!jobs && !single_map))
+		return cudaErrorInvalidValue;
+	const void *k = chain_tma_kernel_ptr(variant);
+	cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kTmaSmemMax));
+	if (e != cudaSuccess)
+		return e;
+	FusedJob one = single;
+	SmemLayout layout = L;
+	CUtensorMap map{};
+	if (single_map)
+		map = *single_map;
+	void *args[] = { &jobs, &num_jobs, &total_items, &one, &layout, &map };
+	grid = std::max(1, std::min(grid, total_items));
+	return cudaLaunchKernel(k, dim3(grid), dim3(tma_threads(variant)), args, static_cast<size_t>(L.total_bytes),
+	                        stream);
+}
+
+int chain_tma_pipeline_error(bool reset)
+{
+	int v = 0;
+	if (cudaMemcpyFromSymbol(&v, chain_detail::g_chain_pipeline_error, sizeof(v)) != cudaSuccess)
+		return -1;
+	if (reset && v) {
+		const int zero = 0;
+		cudaMemcpyToSymbol(chain_detail::g_chain_pipeline_error, &zero, sizeof(zero));
+	}
+	return v;
+}
+
+} // namespace zg

@@ -8,6 +8,7 @@
 #include <cstdint>
 #include <vector>
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "filter_plan.h"
@@ -78,6 +79,7 @@ struct FusedJob {
 	float pixel_max;
 	float offset;           // 2^(depth-1)
 	int vec_ok;             // planes and strides 16-byte aligned: vector loads and stores
+	const void *tmap;       // TMA-pipelined chained kernel: the source plane's tensor map (device memory)
 };
 
 // Shared-memory layout of one launch (the maximum over its jobs).
@@ -161,6 +163,18 @@ const void *chain_kernel_ptr(int variant);
 int chain_threads(int variant);
 cudaError_t launch_chain(int variant, const FusedJob *jobs, int num_jobs, int total_items, const SmemLayout &L, int grid,
                          const FusedJob &single, cudaStream_t stream);
+// The same kernel with source lines and tap fragments brought in by tensor
+// copies on an mbarrier pipeline (chain_tma_kernel.cuh). Usable when the
+// layout fits (box width <= 256) and the source plane has a tensor map
+// (16-byte aligned base and stride).
+bool chain_tma_enabled();  // true when the environment sets ZG_CHAIN_TMA=1
+bool chain_tma_layout(const FusedPlan *const *plans, int n, SmemLayout *out);
+bool chain_tma_source_map(CUtensorMap *map, const FusedJob &j, const SmemLayout &L);
+int chain_tma_grid_size(int variant, size_t smem_bytes);
+cudaError_t launch_chain_tma(int variant, const FusedJob *jobs, int num_jobs, int total_items, const SmemLayout &L,
+                             int grid, const FusedJob &single, const CUtensorMap *single_map, cudaStream_t stream);
+// Nonzero when a pipeline wait of that kernel ran out (optionally reset).
+int chain_tma_pipeline_error(bool reset);
 // Work items that fill the current device once (SMs x resident CTAs).
 int fused_wave_items();
 
