@@ -9,6 +9,8 @@ Other workloads (--workload):
   yuv420_batch    64 YUV 4:2:0 u16 frames of mixed sizes, Spline36 -> 1920x1080
   extreme_f32     32 images 64x64 -> 6400x6400 and 6400x6400 -> 64x64 f32 Lanczos-3, plus 32 interlaced
                   1920x1080 frames as fields -> 1280x720
+  depth_f32_u8    depth conversion around resize (zimg's DepthConversion): 16 frames of 3 planes
+                  3840x2160 f32 -> u8 8-bit limited range, ordered dither
 
 A step is one pass of the resize path over one batch of synthetic frames that
 are already resident in HBM (inputs larger than L2 across the batch). `value`
@@ -381,9 +383,172 @@ def cpu_baseline(jobs, seconds=10.0, impl_label=None):
                       f"restatement (oracle/zimg_oracle.c), {cores} threads row-parallel"}
 
 
+# ------------------------------------------------------- depth conversion --
+# zimg's DepthConversion, the filter the graph puts around resize: a 4K
+# output stage, 3 planes 3840x2160 f32 (luma + 2 chroma) -> 8-bit limited
+# range with ordered dither. Algorithmic bytes: 4 read + 1 written per sample.
+
+def depth_workload(frames: int | None):
+    n = frames or 16
+    planes = [dict(w=3840, h=2160, plane=p, chroma=p > 0) for _ in range(n) for p in range(3)]
+    cfg = {"workload": "depth_f32_u8: 3 planes 3840x2160 f32 -> u8 8-bit limited range, ordered dither "
+                       "(zimg DepthConversion)", "frames_per_step": n, "planes_per_step": 3 * n}
+    return planes, cfg
+
+
+def depth_source(rng, pl):
+    x = rng.random((pl["h"], pl["w"]), dtype=np.float32)
+    return (x - 0.5).astype(np.float32) if pl["chroma"] else x
+
+
+def run_depth(args):
+    import torch
+    import zimg_gb300 as zg
+    from zimg_gb300 import build as zbuild
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    zbuild.build()
+    zg.load()
+    planes, cfg = depth_workload(args.frames)
+    rng = np.random.default_rng(4321 + rank)
+    proto = [depth_source(rng, dict(planes[p], chroma=p > 0)) for p in range(3)]
+    convs, srcs, dsts = [], [], []
+    for pl in planes:
+        convs.append(zg.DepthConversion(pl["w"], pl["h"]).set_pixel_in("float", 32, False, pl["chroma"])
+                     .set_pixel_out("byte", 8, False, pl["chroma"]).set_dither_type("ordered")
+                     .set_plane(pl["plane"]).create())
+        srcs.append(torch.from_numpy(proto[pl["plane"]]).cuda())
+        dsts.append(torch.empty((pl["h"], pl["w"]), dtype=torch.uint8, device="cuda"))
+    stream = torch.cuda.Stream()
+    torch.cuda.synchronize()
+
+    def step():
+        for c, s, d in zip(convs, srcs, dsts):
+            c.process(s, d, stream=stream)
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step()
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=stream):
+        step()
+    torch.cuda.synchronize()
+    out_px = sum(pl["w"] * pl["h"] for pl in planes)
+    alg_bytes = out_px * 5
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    # replay() launches on the current stream: make that the timed one
+    with torch.cuda.stream(stream):
+        for _ in range(max(args.warmup, 3)):
+            graph.replay()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.time()
+        e0.record(stream)
+        for _ in range(args.steps):
+            graph.replay()
+        e1.record(stream)
+        e1.synchronize()
+        torch.cuda.synchronize()
+        t1 = time.time()
+    sampler.stop()
+    ms = max_over_ranks(e0.elapsed_time(e1))
+    ms_step = ms / args.steps
+    value = sum_over_ranks(out_px) * args.steps / (ms / 1e3) / 1e6
+
+    e2e = None
+    if not args.no_e2e:
+        # the public API with host buffers: pinned planes in, the launch, planes out, per plane on one stream
+        n_e2e = min(len(planes), 12)
+        hsrc = [srcs[i].cpu().pin_memory() for i in range(n_e2e)]
+        hdst = [torch.empty(dsts[i].shape, dtype=torch.uint8).pin_memory() for i in range(n_e2e)]
+
+        def e2e_step():
+            with torch.cuda.stream(stream):
+                for i in range(n_e2e):
+                    srcs[i].copy_(hsrc[i], non_blocking=True)
+                    convs[i].process(srcs[i], dsts[i], stream=stream)
+                    hdst[i].copy_(dsts[i], non_blocking=True)
+        for _ in range(2):
+            e2e_step()
+        torch.cuda.synchronize()
+        k = max(3, args.steps // 4)
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record(stream)
+        for _ in range(k):
+            e2e_step()
+        a1.record(stream)
+        a1.synchronize()
+        e_ms = max_over_ranks(a0.elapsed_time(a1) / k)
+        e_px = sum(planes[i]["w"] * planes[i]["h"] for i in range(n_e2e))
+        e2e = {"value": round(sum_over_ranks(e_px) / (e_ms / 1e3) / 1e6, 3), "unit": "Mpixel/s",
+               "h2d_bytes_per_step": e_px * 4, "d2h_bytes_per_step": e_px, "planes_per_step": n_e2e}
+
+    peak, peak_kind = load_peaks()
+    achieved = alg_bytes / (ms_step / 1e3) / 1e9
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "peak_source": f"{peak_kind} hbm_gbs",
+                "traffic": read_traffic(args.workload), "algorithmic_bytes_per_step": alg_bytes,
+                "kernel_launches_per_step": len(planes)}
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = depth_cpu_baseline(planes, seconds=args.cpu_seconds)
+    if rank == 0:
+        line = {"metric": "out Mpixel/s on 1 GB300 + % HBM roofline", "value": round(value, 3), "unit": "Mpixel/s",
+                "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 5),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded)",
+                "config": dict(cfg, l2="inputs larger than L2 (step working set %.2f GB)" % (alg_bytes / 1e9),
+                               parallelism=f"replicas x{world}", graph=True),
+                "impl": "ours", "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
+                "clocks": sampler.summary(t0, t1), "gpu_launches": len(planes) * args.steps}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def depth_cpu_baseline(planes, seconds=10.0):
+    """The oracle's restatement of zimg's C path (one thread), on a bounded sample."""
+    from oracle.oracle import Oracle, PixelFormat, build
+    build()
+    o = Oracle()
+    rng = np.random.default_rng(98)
+    xs = [depth_source(rng, dict(planes[p], chroma=p > 0)) for p in range(3)]
+    px, n, t0 = 0, 0, time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        p = n % 3
+        o.depth_convert(xs[p], PixelFormat("float", None, False, p > 0), PixelFormat("byte", 8, False, p > 0),
+                        "ordered", p)
+        px += xs[p].size
+        n += 1
+    dt = time.perf_counter() - t0
+    return {"value": round(px / dt / 1e6, 3), "unit": "Mpixel/s", "cores": 1, "kind": "port",
+            "sample": f"{n} planes 3840x2160 in {dt:.1f} s, zimg C-path restatement (oracle/zimg_oracle.c), "
+                      f"one thread"}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
+        return
+    if args.workload.startswith("depth_"):
+        planes, cfg = depth_workload(args.frames)
+        cpu = depth_cpu_baseline(planes, seconds=max(1.0, 0.5 * args.steps))
+        line = {"metric": "out Mpixel/s on 1 GB300 + % HBM roofline", "value": cpu["value"], "unit": "Mpixel/s",
+                "n_gpus": int(os.environ.get("WORLD_SIZE", "1")), "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32", "data": "synthetic (seeded)", "config": cfg, "impl": "reference", "cpu_baseline": cpu,
+                "e2e": {"value": cpu["value"], "unit": "Mpixel/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
         return
     jobs, cfg = workload(args.workload, args.frames, seed=0x5EED0000)
     from oracle.oracle import Oracle, build
@@ -437,6 +602,8 @@ def main():
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload.startswith("depth_"):
+        run_depth(args)
     else:
         run_ours(args)
 

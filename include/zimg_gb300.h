@@ -89,6 +89,60 @@ typedef enum zg_engine {
 ZG_API zg_error_code zg_get_last_error(char *err_msg, size_t n);
 ZG_API void zg_clear_last_error(void);
 
+/* ------------------------------------------------------- depth conversion --
+ * Replaces zimg's DepthConversion (src/zimg/depth/depth.h:29-53,
+ * depth.cpp:43-66), the filter the graph inserts around resize when the
+ * pixel type, depth or range changes (src/zimg/graph/graphbuilder.cpp:943-950).
+ * One plane per object, device planes, whole planes per call, as the resize
+ * objects. The conversion is zimg's choice for the two formats:
+ *   mode 0: formats equal (zimg's PixelFormat ==, pixel.h:194-199): a copy;
+ *   mode 1: integer to integer, both limited range, same luma/chroma, depth
+ *           not reduced: left shift (depth_convert.cpp:14-21);
+ *   mode 2: to FLOAT: x * scale + offset (depth_convert.cpp:32-39);
+ *   mode 3: otherwise, to an integer type: x * scale + offset plus the dither
+ *           value, clamped, rounded to nearest even (dither.cpp:37-54).
+ * scale and offset are zimg's (quantize.h:19-45). Results equal zimg's C path
+ * (CPUClass::NONE) bit for bit. Dither NONE and ORDERED (zimg's 16x16
+ * matrix, variant chosen by `plane` mod 4, dither.cpp:137-210) are built;
+ * RANDOM and ERROR_DIFFUSION, and the HALF type, return
+ * ZG_ERROR_UNSUPPORTED_OPERATION. A limited-range format below 8 bits returns
+ * ZG_ERROR_BIT_DEPTH_OVERFLOW (depth.cpp:52-53), as does a depth beyond its
+ * type. */
+typedef enum zg_dither_type {
+	ZG_DITHER_NONE = 0,
+	ZG_DITHER_ORDERED = 1,
+	ZG_DITHER_RANDOM = 2,
+	ZG_DITHER_ERROR_DIFFUSION = 3
+} zg_dither_type;
+
+/* zimg's PixelFormat (src/zimg/common/pixel.h:135-181). depth 0 = the
+ * type's full depth. */
+typedef struct zg_pixel_format {
+	zg_pixel_type type;
+	unsigned depth;
+	int fullrange;
+	int chroma;
+	int ycgco;
+} zg_pixel_format;
+
+typedef struct zg_depth_params {
+	unsigned width, height;
+	zg_pixel_format pixel_in, pixel_out;
+	zg_dither_type dither_type;
+	unsigned plane;  /* 0-3: the plane's index in its image (selects the dither table variant) */
+} zg_depth_params;
+
+typedef struct zg_depth zg_depth;
+
+ZG_API zg_error_code zg_depth_create(const zg_depth_params *params, zg_depth **out);
+ZG_API void zg_depth_free(zg_depth *d);
+/* The conversion chosen (*mode as above). */
+ZG_API zg_error_code zg_depth_get_info(const zg_depth *d, int *mode);
+/* Convert one plane (device pointers; strides in bytes) on `stream`. Never
+ * allocates and never synchronises. */
+ZG_API zg_error_code zg_depth_process(const zg_depth *d, const void *src, ptrdiff_t src_stride, void *dst,
+                                      ptrdiff_t dst_stride, zg_stream stream);
+
 /* Health of the pipelined kernels on the current device: 0, or the cause of
  * the first bounded wait that ran out inside one (1: a group's copies never
  * landed, 2: a buffer was never released, 3: a ring too small for a group).

@@ -31,6 +31,40 @@ REF_SO = os.path.join(HERE, "_ref", "libzimgref.so")
 # zimg_resample_filter_e (zimg.h:374-382)
 FILTERS = {"point": 0, "bilinear": 1, "bicubic": 2, "spline16": 3, "spline36": 4, "lanczos": 5, "spline64": 6}
 T_U16, T_F32, T_F64 = 1, 3, 4
+# zimg_pixel_type_e (zimg.h:184-189) and zimg_dither_type_e (zimg.h:191-196)
+PIXEL_TYPES = {"byte": 0, "word": 1, "half": 2, "float": 3}
+DITHERS = {"none": 0, "ordered": 1, "random": 2, "error_diffusion": 3}
+NP_TYPES = {0: np.uint8, 1: np.uint16, 3: np.float32}
+
+
+@dataclass(frozen=True)
+class PixelFormat:
+    """zimg's PixelFormat (src/zimg/common/pixel.h:135-181)."""
+    type: str = "word"
+    depth: int | None = None
+    fullrange: bool = False
+    chroma: bool = False
+
+    @property
+    def code(self) -> int:
+        return PIXEL_TYPES[self.type]
+
+    @property
+    def bits(self) -> int:
+        return self.depth if self.depth is not None else {0: 8, 1: 16, 2: 16, 3: 32}[self.code]
+
+    @property
+    def dtype(self):
+        return NP_TYPES[self.code]
+
+
+class _PixFmt(C.Structure):
+    _fields_ = [("type", C.c_int), ("depth", C.c_uint), ("fullrange", C.c_int), ("chroma", C.c_int),
+                ("ycgco", C.c_int)]
+
+
+def _pixfmt(f: PixelFormat) -> _PixFmt:
+    return _PixFmt(f.code, f.bits, int(f.fullrange), int(f.chroma), 0)
 
 
 def build(quiet: bool = True) -> None:
@@ -73,6 +107,39 @@ class Oracle:
                                       C.c_ssize_t, C.c_void_p, C.c_ssize_t]
         L.orc_plan_order.argtypes = [C.c_uint, C.c_uint, C.c_uint, C.c_uint, C.c_double, C.c_double, C.c_double,
                                      C.c_double, C.POINTER(C.c_int)]
+        L.orc_depth_convert.argtypes = [C.POINTER(_PixFmt), C.POINTER(_PixFmt), C.c_int, C.c_uint, C.c_uint,
+                                        C.c_uint, C.c_void_p, C.c_ssize_t, C.c_void_p, C.c_ssize_t]
+        L.orc_depth_mode.argtypes = [C.POINTER(_PixFmt), C.POINTER(_PixFmt), C.c_int]
+        L.orc_depth_scale_offset.argtypes = [C.POINTER(_PixFmt), C.POINTER(_PixFmt), C.POINTER(C.c_float),
+                                             C.POINTER(C.c_float)]
+        L.orc_bayer16.argtypes = [C.c_uint, C.c_uint]
+        L.orc_bayer16.restype = C.c_uint
+        L.orc_dither_value.argtypes = [C.c_int, C.c_uint, C.c_uint, C.c_uint]
+        L.orc_dither_value.restype = C.c_float
+
+    def depth_mode(self, fin: PixelFormat, fout: PixelFormat, dither="none") -> int:
+        """0 copy, 1 left shift, 2 to float, 3 dither; negative: not converted."""
+        a, b = _pixfmt(fin), _pixfmt(fout)
+        return self.lib.orc_depth_mode(C.byref(a), C.byref(b), DITHERS[dither])
+
+    def depth_scale_offset(self, fin: PixelFormat, fout: PixelFormat):
+        a, b = _pixfmt(fin), _pixfmt(fout)
+        sc, of = C.c_float(), C.c_float()
+        self.lib.orc_depth_scale_offset(C.byref(a), C.byref(b), C.byref(sc), C.byref(of))
+        return sc.value, of.value
+
+    def depth_convert(self, src: np.ndarray, fin: PixelFormat, fout: PixelFormat, dither="none",
+                      plane=0) -> np.ndarray:
+        """zimg's depth conversion of one plane (C path)."""
+        src = np.ascontiguousarray(src, dtype=fin.dtype)
+        h, w = src.shape
+        out = np.zeros((h, w), fout.dtype)
+        a, b = _pixfmt(fin), _pixfmt(fout)
+        rc = self.lib.orc_depth_convert(C.byref(a), C.byref(b), DITHERS[dither], plane, w, h, src.ctypes.data,
+                                        src.strides[0], out.ctypes.data, out.strides[0])
+        if rc:
+            raise ValueError(f"depth conversion not available ({rc})")
+        return out
 
     def compute_filter(self, kind, src_dim, dst_dim, shift=0.0, width=None, a=math.nan, b=math.nan) -> FilterContext:
         width = float(src_dim if width is None else width)
@@ -165,6 +232,9 @@ class Reference:
         L.ref_pass_create.argtypes = [C.c_int, C.c_uint, C.c_uint, C.c_int, C.c_uint, C.c_uint, C.c_int, C.c_double,
                                       C.c_double, C.c_double, C.c_double, C.c_int, C.c_char_p, C.c_size_t]
         L.ref_plan_free.argtypes = [C.c_void_p]
+        L.ref_depth_convert.argtypes = [C.c_int, C.c_uint, C.c_int, C.c_int, C.c_int, C.c_uint, C.c_int, C.c_int,
+                                        C.c_int, C.c_uint, C.c_int, C.c_uint, C.c_uint, C.c_void_p, C.c_ssize_t,
+                                        C.c_void_p, C.c_ssize_t, C.c_char_p, C.c_size_t]
         L.ref_plan_num_passes.argtypes = [C.c_void_p]
         L.ref_plan_run.argtypes = [C.c_void_p, C.c_void_p, C.c_ssize_t, C.c_void_p, C.c_ssize_t, C.c_char_p,
                                    C.c_size_t]
@@ -248,6 +318,24 @@ class Reference:
         finally:
             self.free(p)
         return out
+
+
+def _ref_depth_convert(self, src: np.ndarray, fin: PixelFormat, fout: PixelFormat, dither="none", plane=0,
+                       cpu=0) -> np.ndarray:
+    """zimg's own DepthConversion (src/zimg/depth/depth.cpp:43-66) on one plane."""
+    src = np.ascontiguousarray(src, dtype=fin.dtype)
+    h, w = src.shape
+    s = aligned_plane(h, w, fin.dtype)
+    s[...] = src
+    d = aligned_plane(h, w, fout.dtype)
+    if self.lib.ref_depth_convert(fin.code, fin.bits, int(fin.fullrange), int(fin.chroma), fout.code, fout.bits,
+                                  int(fout.fullrange), int(fout.chroma), DITHERS[dither], plane, cpu, w, h,
+                                  s.ctypes.data, s.strides[0], d.ctypes.data, d.strides[0], self.err, 512):
+        self._raise("depth_convert")
+    return np.array(d)
+
+
+Reference.depth_convert = _ref_depth_convert
 
 
 def aligned_plane(h: int, w: int, dtype) -> np.ndarray:

@@ -10,6 +10,7 @@
  * them line by line (src/zimg/resize/resize_impl.cpp:130-160).
  */
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdint>
 #include <cstdlib>
@@ -23,6 +24,7 @@
 #include "common/except.h"
 #include "common/pixel.h"
 #include "graphengine/filter.h"
+#include "depth/depth.h"
 #include "resize/filter.h"
 #include "resize/resize.h"
 #include "resize/resize_impl.h"
@@ -272,6 +274,43 @@ int ref_plan_run(const void *p, const void *src, ptrdiff_t src_stride, void *dst
 		run_filter(*plan->first, src, src_stride, tmp, tmp_stride);
 		run_filter(*plan->second, tmp, tmp_stride, dst, dst_stride);
 		std::free(tmp);
+		return 0;
+	} catch (...) {
+		return catch_all(err, errlen);
+	}
+}
+
+/*
+ * zimg's depth conversion (DepthConversion, src/zimg/depth/depth.cpp:43-66) of
+ * one plane: pixel formats as zimg's PixelFormat (type 0 BYTE, 1 WORD, 2
+ * HALF, 3 FLOAT), dither as DitherType, `plane` the plane index (0-3) that
+ * selects the dither table's variant; cpu as ref_plan_create.
+ */
+int ref_depth_convert(int in_type, unsigned in_depth, int in_full, int in_chroma, int out_type, unsigned out_depth,
+                      int out_full, int out_chroma, int dither, unsigned plane, int cpu, unsigned w, unsigned h,
+                      const void *src, ptrdiff_t src_stride, void *dst, ptrdiff_t dst_stride, char *err, size_t errlen)
+{
+	try {
+		const zimg::PixelFormat fin(static_cast<PixelType>(in_type), in_depth, in_full != 0, in_chroma != 0);
+		const zimg::PixelFormat fout(static_cast<PixelType>(out_type), out_depth, out_full != 0, out_chroma != 0);
+		std::array<bool, 4> planes{};
+		planes[plane & 3] = true;
+		zimg::depth::DepthConversion conv(w, h);
+		conv.set_pixel_in(fin)
+			.set_pixel_out(fout)
+			.set_dither_type(static_cast<zimg::depth::DitherType>(dither))
+			.set_planes(planes)
+			.set_cpu(make_cpu(cpu));
+		zimg::depth::DepthConversion::result res = conv.create();
+		const graphengine::Filter *f = res.filter_refs[plane & 3];
+		if (!f) {
+			const size_t bytes = static_cast<size_t>(w) * zimg::pixel_size(fout.type);
+			for (unsigned i = 0; i < h; ++i)
+				std::memcpy(static_cast<char *>(dst) + i * dst_stride, static_cast<const char *>(src) + i * src_stride,
+				            bytes);
+			return 0;
+		}
+		run_filter(*f, src, src_stride, dst, dst_stride);
 		return 0;
 	} catch (...) {
 		return catch_all(err, errlen);

@@ -632,3 +632,166 @@ int orc_resize_pass(int type, unsigned depth, int horizontal, int kind, double a
 	ctx_free(&ctx);
 	return 0;
 }
+
+/* ------------------------------------------------------------------ depth --
+ * zimg's depth conversion around resize (src/zimg/depth/), its C path
+ * (CPUClass::NONE): DepthConversion::create (depth.cpp:52-66) picks a plain
+ * copy, a lossless left shift (depth_convert.cpp:14-21), a conversion to float
+ * (depth_convert.cpp:32-39) or a dither to integer (dither.cpp:37-54, types
+ * NONE and ORDERED; RANDOM and ERROR_DIFFUSION are not restated). Pixel types
+ * follow zimg.h (0 BYTE, 1 WORD, 3 FLOAT; HALF is not restated).
+ */
+typedef struct orc_pixfmt {
+	int type;
+	unsigned depth;
+	int fullrange, chroma, ycgco;
+} orc_pixfmt;
+
+static int pix_is_float(int t)
+{
+	return t == 2 || t == 3;
+}
+
+/* integer_offset / integer_range, quantize.h:19-32 */
+static double pix_offset(const orc_pixfmt *f)
+{
+	if (pix_is_float(f->type))
+		return 0.0;
+	if (f->chroma)
+		return (double)(1L << (f->depth - 1));
+	if (!f->fullrange)
+		return (double)(16L << (f->depth - 8));
+	return 0.0;
+}
+
+static double pix_range(const orc_pixfmt *f)
+{
+	if (pix_is_float(f->type))
+		return 1.0;
+	if (f->fullrange)
+		return (double)((1L << f->depth) - 1);
+	if (f->chroma && !f->ycgco)
+		return (double)(224L << (f->depth - 8));
+	return (double)(219L << (f->depth - 8));
+}
+
+/* get_scale_offset, quantize.h:34-45: FP64, then rounded to float */
+void orc_depth_scale_offset(const orc_pixfmt *in, const orc_pixfmt *out, float *scale, float *offset)
+{
+	double ri = pix_range(in), oi = pix_offset(in), ro = pix_range(out), oo = pix_offset(out);
+	*scale = (float)(ro / ri);
+	*offset = (float)(-oi * ro / ri + oo);
+}
+
+/* PixelFormat equality, common/pixel.h:194-199 */
+static int pix_equal(const orc_pixfmt *a, const orc_pixfmt *b)
+{
+	if (pix_is_float(a->type))
+		return a->type == b->type && a->chroma == b->chroma;
+	return a->type == b->type && a->depth == b->depth && a->fullrange == b->fullrange && a->chroma == b->chroma;
+}
+
+/* The ordered-dither matrix of dither.cpp:137-155: a 16x16 Bayer matrix,
+ * written here from its recursive definition rather than as a table: digit k
+ * (k = 0 the least significant bit of the row i and the column j) contributes
+ * B[bit_k(i)][bit_k(j)] * 4^(3-k), with B = {{0, 3}, {2, 1}}. */
+unsigned orc_bayer16(unsigned i, unsigned j)
+{
+	static const unsigned B[2][2] = { { 0, 3 }, { 2, 1 } };
+	unsigned v = 0;
+	for (unsigned k = 0; k < 4; ++k)
+		v += B[(i >> k) & 1][(j >> k) & 1] << (2 * (3 - k));
+	return v;
+}
+
+/* Dither offset of row i, column j for plane `seq` (dither.cpp:157-210):
+ * value (m + 1) / 257 - 1/2 in float, from the matrix as is (seq 0), mirrored
+ * left-right (1), top-bottom (2) or transposed (3). dither 0 = NONE. */
+float orc_dither_value(int dither, unsigned seq, unsigned i, unsigned j)
+{
+	if (dither == 0)
+		return 0.0f;
+	i &= 15;
+	j &= 15;
+	unsigned m;
+	switch (seq % 4) {
+	case 0: m = orc_bayer16(i, j); break;
+	case 1: m = orc_bayer16(i, 15 - j); break;
+	case 2: m = orc_bayer16(15 - i, j); break;
+	default: m = orc_bayer16(j, i); break;
+	}
+	return (float)(m + 1) / 257.0f - 0.5f;
+}
+
+static float load_sample(int type, const void *row, unsigned j)
+{
+	if (type == 0)
+		return (float)((const uint8_t *)row)[j];
+	if (type == 1)
+		return (float)((const uint16_t *)row)[j];
+	return ((const float *)row)[j];
+}
+
+/* Mode of a conversion (depth.cpp:52-66): 0 copy, 1 left shift, 2 to float,
+ * 3 dither; negative: zimg's error (-1 bit depth below 8 in limited range,
+ * -2 not restated here: HALF, or RANDOM / ERROR_DIFFUSION dither). */
+int orc_depth_mode(const orc_pixfmt *in, const orc_pixfmt *out, int dither)
+{
+	if (in->type == 2 || out->type == 2)
+		return -2;
+	if ((!in->fullrange && in->depth < 8) || (!out->fullrange && out->depth < 8))
+		return -1;
+	if (pix_equal(in, out))
+		return 0;
+	if (!pix_is_float(in->type) && !pix_is_float(out->type) && !in->fullrange && !out->fullrange &&
+	    in->chroma == out->chroma && out->depth >= in->depth)
+		return 1;
+	if (pix_is_float(out->type))
+		return pix_is_float(in->type) ? 0 : 2;
+	return (dither == 0 || dither == 1) ? 3 : -2;
+}
+
+int orc_depth_convert(const orc_pixfmt *in, const orc_pixfmt *out, int dither, unsigned seq, unsigned w, unsigned h,
+                      const void *src, ptrdiff_t src_stride, void *dst, ptrdiff_t dst_stride)
+{
+	const int mode = orc_depth_mode(in, out, dither);
+	if (mode < 0)
+		return mode;
+	float scale = 1.0f, offset = 0.0f;
+	orc_depth_scale_offset(in, out, &scale, &offset);
+	const unsigned shift = out->depth - in->depth;
+	const float vmax = (float)((1UL << out->depth) - 1);
+	for (unsigned i = 0; i < h; ++i) {
+		const char *s = (const char *)src + (ptrdiff_t)i * src_stride;
+		char *d = (char *)dst + (ptrdiff_t)i * dst_stride;
+		for (unsigned j = 0; j < w; ++j) {
+			if (mode == 0) {
+				const size_t n = type_size(out->type);
+				memcpy(d + j * n, s + j * n, n);
+			} else if (mode == 1) {
+				/* integer_to_integer, depth_convert.cpp:14-21 */
+				const unsigned x = in->type == 0 ? ((const uint8_t *)s)[j] : ((const uint16_t *)s)[j];
+				if (out->type == 0)
+					((uint8_t *)d)[j] = (uint8_t)(x << shift);
+				else
+					((uint16_t *)d)[j] = (uint16_t)(x << shift);
+			} else if (mode == 2) {
+				/* integer_to_float, depth_convert.cpp:32-39 (product, then sum) */
+				const float p = load_sample(in->type, s, j) * scale;
+				((float *)d)[j] = p + offset;
+			} else {
+				/* dither_ordered, dither.cpp:37-54 */
+				const float p = load_sample(in->type, s, j) * scale;
+				float x = p + offset;
+				x = x + orc_dither_value(dither, seq, i, j);
+				x = x < 0.0f ? 0.0f : (vmax < x ? vmax : x);
+				const long q = lrintf(x);
+				if (out->type == 0)
+					((uint8_t *)d)[j] = (uint8_t)q;
+				else
+					((uint16_t *)d)[j] = (uint16_t)q;
+			}
+		}
+	}
+	return 0;
+}

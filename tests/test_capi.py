@@ -102,3 +102,27 @@ def test_version(lib):
     a, b, c = C.c_uint(), C.c_uint(), C.c_uint()
     lib.zg_get_version_info(C.byref(a), C.byref(b), C.byref(c))
     assert (a.value, b.value) == (1, 0)
+
+
+def test_depth_create_errors(lib):
+    """zg_depth_create rejects what zimg's DepthConversion rejects, with zimg's
+    codes, before touching a device."""
+    import ctypes as C
+    from zimg_gb300 import capi
+
+    def create(tin, din, tout, dout, dither=0, fin=0, fout=0):
+        p = capi.DepthParams(64, 32, capi.PixelFormat(tin, din, fin, 0, 0), capi.PixelFormat(tout, dout, fout, 0, 0),
+                             dither, 0)
+        h = C.c_void_p()
+        return lib.zg_depth_create(C.byref(p), C.byref(h))
+
+    assert create(2, 16, 0, 8) == 3072            # HALF: UNSUPPORTED_OPERATION
+    assert create(3, 32, 0, 8, dither=2) == 3072  # RANDOM dither: not built
+    assert create(3, 32, 0, 8, dither=3) == 3072  # ERROR_DIFFUSION: not built
+    assert create(1, 7, 1, 10) == 1028            # limited range below 8 bits: BIT_DEPTH_OVERFLOW
+    assert create(0, 9, 1, 10) == 1028            # depth beyond the type
+    assert create(1, 10, 0, 8, dither=9) == 2049  # ENUM_OUT_OF_RANGE
+    assert create(5, 10, 0, 8) == 2049
+    p = capi.DepthParams(0, 32, capi.PixelFormat(1, 10, 0, 0, 0), capi.PixelFormat(0, 8, 0, 0, 0), 0, 0)
+    h = C.c_void_p()
+    assert lib.zg_depth_create(C.byref(p), C.byref(h)) == 2050  # INVALID_IMAGE_SIZE

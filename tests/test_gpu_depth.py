@@ -1,0 +1,104 @@
+"""GPU parity of the depth conversion (zimg's DepthConversion) through the C
+ABI: bit-exact against the oracle's restatement of zimg's C path (which
+tests/test_oracle_depth.py pins against zimg's own code), on aligned
+planes (vector path), odd widths and offset planes (scalar path), the golden
+planes, and a depth -> resize -> depth pipeline."""
+import os
+
+import numpy as np
+import pytest
+
+from test_oracle_depth import CASES, GOLDEN, make_src
+
+pytestmark = pytest.mark.gpu
+
+TORCH_DT = {"byte": "uint8", "word": "int16", "float": "float32"}
+
+
+def to_dev(a):
+    import torch
+    if a.dtype == np.uint16:
+        return torch.from_numpy(np.ascontiguousarray(a).view(np.int16)).cuda()
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def empty(h, w, ptype, offset=0):
+    import torch
+    dt = getattr(torch, TORCH_DT[ptype])
+    buf = torch.zeros(h * w + offset + 16, dtype=dt, device="cuda")
+    return buf[offset:offset + h * w].view(h, w)
+
+
+def to_host(t, np_dtype):
+    a = t.cpu().numpy()
+    return a.view(np.uint16) if np_dtype == np.uint16 else a
+
+
+def convert(src, fin, fout, dither, plane, offset=0):
+    import torch
+    import zimg_gb300 as zg
+    h, w = src.shape
+    c = zg.DepthConversion(w, h).set_pixel_in(fin.type, fin.bits, fin.fullrange, fin.chroma) \
+        .set_pixel_out(fout.type, fout.bits, fout.fullrange, fout.chroma).set_dither_type(dither) \
+        .set_plane(plane).create()
+    if offset:
+        s = empty(h, w, fin.type, offset)
+        s.copy_(to_dev(src))
+    else:
+        s = to_dev(src)
+    d = empty(h, w, fout.type, offset)
+    c.process(s, d)
+    torch.cuda.synchronize()
+    return to_host(d, fout.dtype), c.mode
+
+
+@pytest.mark.parametrize("case", range(len(CASES)))
+def test_depth_bitexact(cuda, oracle, case):
+    fin, fout, dither = CASES[case]
+    rng = np.random.default_rng(300 + case)
+    for (h, w), offset in (((64, 256), 0), ((41, 157), 0), ((33, 200), 3)):
+        src = make_src(rng, fin, h, w)
+        for plane in range(4):
+            got, mode = convert(src, fin, fout, dither, plane, offset)
+            want = oracle.depth_convert(src, fin, fout, dither, plane)
+            np.testing.assert_array_equal(got.view(np.uint8), want.view(np.uint8),
+                                          err_msg=f"{CASES[case]} {h}x{w}+{offset} plane {plane} ({mode})")
+        assert mode == {0: "copy", 1: "left_shift", 2: "to_float", 3: "dither"}[oracle.depth_mode(fin, fout, dither)]
+
+
+def test_depth_golden(cuda):
+    data = np.load(GOLDEN)
+    for k in range(int(data["n"])):
+        fin, fout, dither = CASES[int(data[f"case{k}"])]
+        got, _ = convert(data[f"src{k}"], fin, fout, dither, int(data[f"plane{k}"]))
+        np.testing.assert_array_equal(got.view(np.uint8), data[f"out{k}"].view(np.uint8), err_msg=f"golden {k}")
+
+
+def test_depth_resize_depth_pipeline(cuda, oracle):
+    """8-bit source -> 10-bit (left shift) -> Lanczos-3 2x on the tensor-core
+    path -> 8-bit with ordered dither, as zimg's graph chains them."""
+    import torch
+    import zimg_gb300 as zg
+    from oracle.oracle import PixelFormat as PF
+    rng = np.random.default_rng(9)
+    h, w = 135, 240
+    src = rng.integers(16, 236, size=(h, w)).astype(np.uint8)
+    f8, f10 = PF("byte", 8), PF("word", 10)
+    up = zg.DepthConversion(w, h).set_pixel_in("byte", 8).set_pixel_out("word", 10).create()
+    rs = zg.ResizeConversion(w, h, "word").set_depth(10).set_filter("lanczos", 3).set_dst_width(2 * w) \
+        .set_dst_height(2 * h).create()
+    down = zg.DepthConversion(2 * w, 2 * h).set_pixel_in("word", 10).set_pixel_out("byte", 8) \
+        .set_dither_type("ordered").create()
+    a = to_dev(src)
+    b = torch.empty((h, w), dtype=torch.int16, device="cuda")
+    c = torch.empty((2 * h, 2 * w), dtype=torch.int16, device="cuda")
+    d = torch.empty((2 * h, 2 * w), dtype=torch.uint8, device="cuda")
+    up.process(a, b)
+    rs.process(b, c)
+    down.process(c, d)
+    torch.cuda.synchronize()
+    w10 = oracle.depth_convert(src, f8, f10)
+    r10 = oracle.resize_plane(w10, 2 * w, 2 * h, "lanczos", 3, depth=10, mode="c")
+    want = oracle.depth_convert(r10, f10, f8, "ordered", 0)
+    np.testing.assert_array_equal(d.cpu().numpy(), want)
+    assert rs.info["engine"] == "tensor"

@@ -1,0 +1,85 @@
+"""Depth conversion (zimg's DepthConversion, src/zimg/depth/): the oracle's C
+restatement pinned against zimg's own code compiled from the reference
+checkout (C path, CPUClass::NONE), and against the committed golden planes
+made from it. No GPU."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle.oracle import Oracle, PixelFormat as PF
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = os.path.join(ROOT, "tests", "golden", "depth_golden.npz")
+
+# (pixel in, pixel out, dither): every conversion kind zimg picks
+CASES = [
+    (PF("byte", 8), PF("word", 10), "none"),               # left shift
+    (PF("byte", 8), PF("word", 16), "none"),
+    (PF("word", 10, False, True), PF("word", 16, False, True), "none"),
+    (PF("word", 10), PF("byte", 8), "none"),               # dither to integer
+    (PF("word", 10), PF("byte", 8), "ordered"),
+    (PF("word", 16), PF("word", 10), "ordered"),
+    (PF("word", 12, True, True), PF("byte", 8, False, True), "ordered"),
+    (PF("byte", 8, True), PF("byte", 8), "ordered"),       # full -> limited range
+    (PF("byte", 8), PF("byte", 8, True), "none"),
+    (PF("float"), PF("byte", 8), "ordered"),
+    (PF("float"), PF("word", 10), "none"),
+    (PF("float"), PF("word", 16, True), "ordered"),
+    (PF("float", None, False, True), PF("byte", 8, False, True), "ordered"),
+    (PF("byte", 8), PF("float"), "none"),                  # to float
+    (PF("word", 10, False, True), PF("float", None, False, True), "none"),
+    (PF("word", 16, True), PF("float"), "none"),
+    (PF("word", 10), PF("word", 10), "ordered"),           # equal formats: copy
+]
+
+
+def make_src(rng, f: PF, h, w):
+    if f.type == "float":
+        x = rng.random((h, w), dtype=np.float32) * 1.25 - 0.125  # out-of-range values exercise the clamp
+        return (x - 0.5).astype(np.float32) if f.chroma else x.astype(np.float32)
+    return rng.integers(0, 1 << f.bits, size=(h, w)).astype(f.dtype)
+
+
+def test_bayer_matrix_first_rows():
+    # zimg's matrix rows 0 and 15 (dither.cpp:138,153) from the recursive definition
+    o = Oracle()
+    assert [o.lib.orc_bayer16(0, j) for j in range(8)] == [0, 192, 48, 240, 12, 204, 60, 252]
+    assert [o.lib.orc_bayer16(15, j) for j in range(13, 16)] == [101, 149, 85]
+    vals = sorted(o.lib.orc_bayer16(i, j) for i in range(16) for j in range(16))
+    assert vals == list(range(256))
+
+
+def test_depth_modes():
+    o = Oracle()
+    assert o.depth_mode(PF("byte", 8), PF("word", 10)) == 1
+    assert o.depth_mode(PF("float"), PF("byte", 8), "ordered") == 3
+    assert o.depth_mode(PF("byte", 8), PF("float")) == 2
+    assert o.depth_mode(PF("word", 10), PF("word", 10)) == 0
+    assert o.depth_mode(PF("word", 7), PF("word", 10)) == -1          # limited range below 8 bits
+    assert o.depth_mode(PF("float"), PF("byte", 8), "random") == -2   # not restated
+
+
+@pytest.mark.parametrize("case", range(len(CASES)))
+def test_oracle_matches_zimg(reference, case):
+    fin, fout, dither = CASES[case]
+    o = Oracle()
+    rng = np.random.default_rng(100 + case)
+    src = make_src(rng, fin, 41, 157)
+    for plane in range(4):
+        want = reference.depth_convert(src, fin, fout, dither, plane, cpu=0)
+        got = o.depth_convert(src, fin, fout, dither, plane)
+        np.testing.assert_array_equal(got.view(np.uint8), want.view(np.uint8), err_msg=f"{CASES[case]} plane {plane}")
+
+
+def test_oracle_matches_golden():
+    if not os.path.exists(GOLDEN):
+        pytest.skip("depth golden planes not generated")
+    data = np.load(GOLDEN)
+    o = Oracle()
+    n = int(data["n"])
+    for k in range(n):
+        fin, fout, dither = CASES[int(data[f"case{k}"])]
+        plane = int(data[f"plane{k}"])
+        got = o.depth_convert(data[f"src{k}"], fin, fout, dither, plane)
+        np.testing.assert_array_equal(got.view(np.uint8), data[f"out{k}"].view(np.uint8), err_msg=f"golden {k}")

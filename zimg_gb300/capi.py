@@ -49,6 +49,19 @@ class ResizeParams(C.Structure):
                 ("allow_fusion", C.c_int)]
 
 
+class PixelFormat(C.Structure):
+    _fields_ = [("type", C.c_int), ("depth", C.c_uint), ("fullrange", C.c_int), ("chroma", C.c_int),
+                ("ycgco", C.c_int)]
+
+
+class DepthParams(C.Structure):
+    _fields_ = [("width", C.c_uint), ("height", C.c_uint), ("pixel_in", PixelFormat), ("pixel_out", PixelFormat),
+                ("dither_type", C.c_int), ("plane", C.c_uint)]
+
+
+DITHER = {"none": 0, "ordered": 1, "random": 2, "error_diffusion": 3}
+
+
 class BatchIO(C.Structure):
     _fields_ = [("src", C.c_void_p), ("src_stride", C.c_ssize_t), ("dst", C.c_void_p), ("dst_stride", C.c_ssize_t)]
 
@@ -90,6 +103,10 @@ _P = C.c_void_p
 SIGNATURES = [
     ("zg_get_last_error", C.c_int, [C.c_char_p, C.c_size_t]),
     ("zg_pipeline_status", C.c_int, [C.c_int]),
+    ("zg_depth_create", C.c_int, [C.POINTER(DepthParams), C.POINTER(C.c_void_p)]),
+    ("zg_depth_free", None, [C.c_void_p]),
+    ("zg_depth_get_info", C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    ("zg_depth_process", C.c_int, [C.c_void_p, C.c_void_p, C.c_ssize_t, C.c_void_p, C.c_ssize_t, C.c_void_p]),
     ("zg_clear_last_error", None, []),
     ("zg_get_version_info", None, [C.POINTER(C.c_uint)] * 3),
     ("zg_compute_filter", C.c_int, [C.c_int, C.c_double, C.c_double, C.c_uint, C.c_uint, C.c_double, C.c_double,

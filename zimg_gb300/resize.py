@@ -241,6 +241,66 @@ class ResizeConversion(_Builder):
         return Resize(h.value, p)
 
 
+class Depth:
+    """The created depth conversion (zimg's DepthConversion::create result for
+    one plane): process(src, dst) converts a whole device plane."""
+
+    MODES = {0: "copy", 1: "left_shift", 2: "to_float", 3: "dither"}
+
+    def __init__(self, handle, params: capi.DepthParams):
+        self._h = handle
+        self.params = params
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            load().zg_depth_free(self._h)
+            self._h = None
+
+    @property
+    def mode(self) -> str:
+        m = C.c_int()
+        check(load().zg_depth_get_info(self._h, C.byref(m)))
+        return self.MODES[m.value]
+
+    def process(self, src, dst, stream=None) -> None:
+        sp, ss, _, _ = _plane(src)
+        dp, ds, _, _ = _plane(dst)
+        check(load().zg_depth_process(self._h, sp, ss, dp, ds, _stream_handle(stream)))
+
+
+class DepthConversion(_Builder):
+    """DepthConversion{width, height} (src/zimg/depth/depth.h:29-53): pixel
+    formats as (type, depth, fullrange, chroma), dither type, plane index."""
+
+    def __init__(self, width: int, height: int):
+        self.width, self.height = width, height
+        self.pixel_in = ("word", 16, False, False)
+        self.pixel_out = ("word", 16, False, False)
+        self.dither, self.plane = "none", 0
+
+    def set_pixel_in(self, type, depth=0, fullrange=False, chroma=False):
+        return self._set("pixel_in", (type, int(depth), bool(fullrange), bool(chroma)))
+
+    def set_pixel_out(self, type, depth=0, fullrange=False, chroma=False):
+        return self._set("pixel_out", (type, int(depth), bool(fullrange), bool(chroma)))
+
+    def set_dither_type(self, v: str): return self._set("dither", v)
+    def set_plane(self, v: int): return self._set("plane", int(v))
+
+    def params(self) -> capi.DepthParams:
+        def fmt(f):
+            t, d, full, chroma = f
+            return capi.PixelFormat(_pixel_id(t), d, int(full), int(chroma), 0)
+        return capi.DepthParams(self.width, self.height, fmt(self.pixel_in), fmt(self.pixel_out),
+                                capi.DITHER[self.dither], self.plane)
+
+    def create(self) -> Depth:
+        p = self.params()
+        h = C.c_void_p()
+        check(load().zg_depth_create(C.byref(p), C.byref(h)))
+        return Depth(h.value, p)
+
+
 class Batch:
     """Many conversions of uneven sizes, launched together."""
 
