@@ -433,3 +433,42 @@ def resize_params(src_plane: dict, dst_plane: dict) -> dict:
                 shift_h=src_plane["top"] - dst_plane["top"] / scale_h,
                 subwidth=src_plane["aw"] * (dst_plane["width"] / dst_plane["aw"]),
                 subheight=src_plane["ah"] * (dst_plane["height"] / dst_plane["ah"]))
+
+
+def resize_format(fs: PixelFormat, fd: PixelFormat, src_pels: float, dst_pels: float) -> PixelFormat:
+    """The format zimg's graph resizes a plane in (choose_resize_format,
+    src/zimg/graph/graphbuilder.cpp:720-751), resize supporting WORD and FLOAT."""
+    sup = ("word", "float")
+    if fs.type in sup and fd.type in sup:
+        return fd if src_pels < dst_pels else fs
+    if fs.type in sup:
+        return fs
+    if fd.type in sup:
+        return fd
+    if fs.type == "byte" and not fs.fullrange:
+        return PixelFormat("word", 16, False, fs.chroma)
+    return PixelFormat("float")
+
+
+def graph_plane_chain(o: "Oracle", src: np.ndarray, fs: PixelFormat, fd: PixelFormat, rp: dict | None, kind,
+                      a=math.nan, b=math.nan, dither="none", plane=0) -> np.ndarray:
+    """One plane through zimg's graph (connect_plane, graphbuilder.cpp:892-953):
+    full-range BYTE kept at its depth reinterpreted as limited range, a depth
+    conversion into the resize format, the resize (rp: resize_params(); None
+    when the geometry is unchanged), a depth conversion to the output format.
+    FP32 resizes use the sequential fused multiply-add order (mode "fma") that
+    the GPU's CUDA-core kernels follow bit for bit; u16 ones zimg's C path."""
+    import dataclasses
+    if fs.type == "byte" and fs.fullrange and fd.fullrange and fs.bits == fd.bits:
+        fs = dataclasses.replace(fs, fullrange=False)
+        fd = dataclasses.replace(fd, fullrange=False)
+    if rp is None:
+        return o.depth_convert(src, fs, fd, dither, plane)
+    h, w = src.shape
+    fr = resize_format(fs, fd, float(w * h), float(rp["dst_w"] * rp["dst_h"]))
+    x = src if o.depth_mode(fs, fr, dither) == 0 else o.depth_convert(src, fs, fr, dither, plane)
+    y = o.resize_plane(x.astype(fr.dtype), rp["dst_w"], rp["dst_h"], kind, a, b,
+                       depth=fr.bits if fr.type == "word" else None, shift_w=rp["shift_w"], shift_h=rp["shift_h"],
+                       subwidth=rp["subwidth"], subheight=rp["subheight"],
+                       mode="c" if fr.type == "word" else "fma", nthreads=16)
+    return y if o.depth_mode(fr, fd, dither) == 0 else o.depth_convert(y, fr, fd, dither, plane)

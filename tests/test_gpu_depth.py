@@ -102,3 +102,56 @@ def test_depth_resize_depth_pipeline(cuda, oracle):
     want = oracle.depth_convert(r10, f10, f8, "ordered", 0)
     np.testing.assert_array_equal(d.cpu().numpy(), want)
     assert rs.info["engine"] == "tensor"
+
+
+GRAPH_CASES = [
+    # (src type, depth, range, dst type, depth, range, size in, size out, color, dither)
+    ("byte", 8, 0, "word", 10, 0, (1920, 1080), (1280, 720), 2, "none"),      # convert, then resize in WORD 10
+    ("float", 32, 0, "byte", 8, 0, (640, 360), (1280, 720), 2, "ordered"),   # resize in FLOAT, dither after
+    ("byte", 8, 1, "byte", 8, 1, (720, 480), (960, 540), 0, "ordered"),      # full range BYTE: WORD 16 chain
+    ("word", 10, 0, "byte", 8, 0, (1280, 720), (1280, 720), 2, "ordered"),   # depth only
+    ("word", 16, 1, "float", 32, 0, (400, 300), (800, 600), 1, "none"),      # RGB, to float after resize
+]
+
+
+@pytest.mark.parametrize("case", range(len(GRAPH_CASES)))
+def test_graph_depth_around_resize(cuda, oracle, case):
+    """zg_graph with pixel format changes: every plane equals the oracle's
+    restatement of zimg's graph chain (depth -> resize -> depth)."""
+    import torch
+    import zimg_gb300 as zg
+    from oracle import oracle as O
+    st, sd, sr, dt, dd, dr, (sw, sh), (dw, dh), color, dither = GRAPH_CASES[case]
+    sub = 1 if color == 2 else 0
+    sfmt = zg.image_format(sw, sh, st, depth=sd, pixel_range=sr, color_family=color, subsample_w=sub,
+                           subsample_h=sub, chroma_location=0)
+    dfmt = zg.image_format(dw, dh, dt, depth=dd, pixel_range=dr, color_family=color, subsample_w=sub,
+                           subsample_h=sub, chroma_location=0)
+    dmap = {"none": 0, "ordered": 1}
+    g = zg.Graph(sfmt, dfmt, zg.graph_params(resample_filter="lanczos", resample_filter_uv="bicubic",
+                                             dither_type=dmap[dither]))
+    rng = np.random.default_rng(600 + case)
+    nplanes = 1 if color == 0 else 3
+    sgeo = O.plane_geometry(dict(width=sw, height=sh, subsample_w=sub, subsample_h=sub,
+                                 color=["grey", "rgb", "yuv"][color], chroma_location=0))
+    dgeo = O.plane_geometry(dict(width=dw, height=dh, subsample_w=sub, subsample_h=sub,
+                                 color=["grey", "rgb", "yuv"][color], chroma_location=0))
+    srcs, dsts, wants = [], [], []
+    for p in range(nplanes):
+        uv = color == 2 and p > 0
+        fs = O.PixelFormat(st, sd, bool(sr), uv)
+        fd = O.PixelFormat(dt, dd, bool(dr), uv)
+        ph, pw = sgeo[p]["height"], sgeo[p]["width"]
+        src = make_src(rng, fs, ph, pw)
+        srcs.append(src)
+        dsts.append(empty(dgeo[p]["height"], dgeo[p]["width"], dt))
+        same = (sw, sh) == (dw, dh)
+        rp = None if same else O.resize_params(sgeo[p], dgeo[p])
+        kind = "bicubic" if uv else "lanczos"
+        wants.append(O.graph_plane_chain(oracle, src, fs, fd, rp, kind, dither=dither, plane=p))
+    g.process([to_dev(s) for s in srcs] + [None] * (4 - nplanes), dsts + [None] * (4 - nplanes))
+    torch.cuda.synchronize()
+    for p in range(nplanes):
+        got = to_host(dsts[p], O.PixelFormat(dt, dd).dtype)
+        np.testing.assert_array_equal(got.view(np.uint8), wants[p].view(np.uint8),
+                                      err_msg=f"{GRAPH_CASES[case]} plane {p}")

@@ -1,4 +1,5 @@
-// C ABI: the resize-only subset of zimg's format-level graph.
+// C ABI: the resize subset of zimg's format-level graph, with the depth
+// conversions the graph puts around resize.
 //
 // The per-plane geometry follows zimg's graph builder: chroma planes from luma
 // (graphbuilder.cpp:331-346), siting and field-parity offsets
@@ -198,24 +199,102 @@ FormatState import_format(const zg_image_format &f)
 
 } // namespace
 
+namespace {
+
+// A plane's pixel format (zimg's PixelFormat, common/pixel.h:135-181).
+struct PixFmt {
+	int type;
+	unsigned depth;
+	bool full, chroma;
+};
+
+bool fmt_equal(const PixFmt &a, const PixFmt &b)
+{
+	// common/pixel.h:194-199: floats compare by type and chroma only
+	if (a.type == ZG_PIXEL_FLOAT || a.type == ZG_PIXEL_HALF)
+		return a.type == b.type && a.chroma == b.chroma;
+	return a.type == b.type && a.depth == b.depth && a.full == b.full && a.chroma == b.chroma;
+}
+
+// The format resize runs in (choose_resize_format, graphbuilder.cpp:720-751),
+// resize supporting WORD and FLOAT.
+PixFmt choose_resize_format(const PixFmt &s, const PixFmt &d, double src_pels, double dst_pels)
+{
+	auto supported = [](int t) { return t == ZG_PIXEL_WORD || t == ZG_PIXEL_FLOAT; };
+	if (supported(s.type) && supported(d.type))
+		return src_pels < dst_pels ? d : s;
+	if (supported(s.type))
+		return s;
+	if (supported(d.type))
+		return d;
+	if (s.type == ZG_PIXEL_BYTE && !s.full)
+		return PixFmt{ ZG_PIXEL_WORD, 16, false, s.chroma };
+	return PixFmt{ ZG_PIXEL_FLOAT, 32, false, false };
+}
+
+size_t pitch_of(unsigned w, unsigned bytes)
+{
+	return (static_cast<size_t>(w) * bytes + 255) & ~static_cast<size_t>(255);
+}
+
+zg_depth *make_depth(unsigned w, unsigned h, const PixFmt &in, const PixFmt &out, int dither, int plane)
+{
+	zg_depth_params q{};
+	q.width = w;
+	q.height = h;
+	q.pixel_in = zg_pixel_format{ static_cast<zg_pixel_type>(in.type), in.depth, in.full, in.chroma, 0 };
+	q.pixel_out = zg_pixel_format{ static_cast<zg_pixel_type>(out.type), out.depth, out.full, out.chroma, 0 };
+	q.dither_type = static_cast<zg_dither_type>(dither);
+	q.plane = static_cast<unsigned>(plane);
+	zg_depth *d = nullptr;
+	zg_error_code rc = zg_depth_create(&q, &d);
+	if (rc != ZG_ERROR_SUCCESS) {
+		char msg[256];
+		zg_get_last_error(msg, sizeof(msg));
+		throw Error(rc, msg);
+	}
+	return d;
+}
+
+void run_depth(const zg_depth *d, const void *src, ptrdiff_t ss, void *dst, ptrdiff_t ds, zg_stream st)
+{
+	zg_error_code rc = zg_depth_process(d, src, ss, dst, ds, st);
+	if (rc != ZG_ERROR_SUCCESS) {
+		char msg[256];
+		zg_get_last_error(msg, sizeof(msg));
+		throw Error(rc, msg);
+	}
+}
+
+} // namespace
+
 struct zg_graph {
 	int device;
-	int sample_bytes;
 	struct Plane {
 		bool present = false;
-		int mode = 0;  // 0 copy, 1 copy subrectangle, 2 resize
+		int mode = 0;  // 0 copy, 1 copy subrectangle, 2 resize, 3 depth only, 4 depth of a subrectangle
 		unsigned w = 0, h = 0;      // output size
 		unsigned off_x = 0, off_y = 0;
+		unsigned in_bytes = 0, out_bytes = 0;
 		zg_resize_params params{};
 		zg_resize *resize = nullptr;
+		// depth conversions around resize (graphbuilder.cpp:943-950): into
+		// the resize format before, to the output format after; their
+		// planes live in tmp (pre at 0, mid next, resize scratch last)
+		zg_depth *pre = nullptr, *post = nullptr, *only = nullptr;
+		size_t pre_pitch = 0, mid_pitch = 0, off_mid = 0, off_tmp = 0;
 		size_t tmp = 0;
 	} planes[4];
 	size_t tmp_size = 0;
 
 	~zg_graph()
 	{
-		for (auto &p : planes)
+		for (auto &p : planes) {
 			zg_resize_free(p.resize);
+			zg_depth_free(p.pre);
+			zg_depth_free(p.post);
+			zg_depth_free(p.only);
+		}
 	}
 };
 
@@ -277,17 +356,20 @@ zg_graph *zg_graph_build(const zg_image_format *src_format, const zg_image_forma
 		zg_graph_builder_params_default(&defaults, src_format->version);
 		const zg_graph_builder_params &gp = params ? *params : defaults;
 
-		if (s.pixel_type != d.pixel_type || s.depth != d.depth || (s.pixel_type != ZG_PIXEL_FLOAT && s.range != d.range))
-			throw Error(kErrUnsupported, "pixel format conversion is outside the resize path");
+		if (s.pixel_type == ZG_PIXEL_HALF || d.pixel_type == ZG_PIXEL_HALF)
+			throw Error(kErrUnsupported, "HALF samples are not supported by this library");
+		const bool format_change =
+			s.pixel_type != d.pixel_type || s.depth != d.depth || (s.pixel_type != ZG_PIXEL_FLOAT && s.range != d.range);
 		if (s.color != d.color || s.matrix != d.matrix || s.transfer != d.transfer || s.primaries != d.primaries)
 			throw Error(kErrNoColorspaceConversion, "colorspace conversion is outside the resize path");
 		if (s.alpha != d.alpha)
 			throw Error(kErrUnsupported, "alpha conversion is outside the resize path");
-		const Sample sample = sample_of(s.pixel_type);
+		if (s.alpha && format_change)
+			throw Error(kErrUnsupported, "depth conversion of alpha planes is not supported by this library");
 
 		auto g = std::make_unique<zg_graph>();
 		g->device = current_device();
-		g->sample_bytes = static_cast<int>(bytes_of(sample));
+		auto bytes = [](int t) { return t == ZG_PIXEL_BYTE ? 1u : (t == ZG_PIXEL_WORD ? 2u : 4u); };
 
 		for (int p = 0; p < 4; ++p) {
 			const bool chroma = p == PLANE_U || p == PLANE_V;
@@ -303,9 +385,23 @@ zg_graph *zg_graph_build(const zg_image_format *src_format, const zg_image_forma
 			const PlaneGeom &dp = d.planes[q];
 			gpl.w = dp.width;
 			gpl.h = dp.height;
+			gpl.in_bytes = bytes(s.pixel_type);
+			gpl.out_bytes = bytes(d.pixel_type);
+			// plane formats; full-range BYTE kept at its depth is treated as
+			// limited range for the whole chain (graphbuilder.cpp:912-920)
+			const bool uv = chroma && s.color == COLOR_YUV;
+			PixFmt fs{ s.pixel_type, s.depth, s.range == 1, uv }, fd{ d.pixel_type, d.depth, d.range == 1, uv };
+			if (fs.type == ZG_PIXEL_BYTE && fs.full && fd.full && fs.depth == fd.depth)
+				fs.full = fd.full = false;
+			const int dither = static_cast<int>(gp.dither_type);
 
 			if (sp == dp) {
-				gpl.mode = 0;
+				if (fmt_equal(fs, fd)) {
+					gpl.mode = 0;
+				} else {
+					gpl.mode = 3;
+					gpl.only = make_depth(dp.width, dp.height, fs, fd, dither, p);
+				}
 				continue;
 			}
 			// Pixel-aligned subrectangle equal to the output: plain copy
@@ -319,21 +415,25 @@ zg_graph *zg_graph_build(const zg_image_format *src_format, const zg_image_forma
 				tile = tile && is_int(sl) && is_int(st) && sl >= 0 && st >= 0 &&
 				       sl + sp.aw <= sp.width && st + sp.ah <= sp.height;
 				if (tile) {
-					gpl.mode = 1;
+					gpl.mode = fmt_equal(fs, fd) ? 1 : 4;
 					gpl.off_x = static_cast<unsigned>(sl);
 					gpl.off_y = static_cast<unsigned>(st);
+					if (gpl.mode == 4)
+						gpl.only = make_depth(dp.width, dp.height, fs, fd, dither, p);
 					continue;
 				}
 			}
 			gpl.mode = 2;
 			const double scale_w = dp.aw / sp.aw;
 			const double scale_h = dp.ah / sp.ah;
+			const PixFmt fr = choose_resize_format(fs, fd, static_cast<double>(sp.width) * sp.height,
+			                                       static_cast<double>(dp.width) * dp.height);
 			zg_resize_params rp;
 			zg_resize_params_default(&rp);
 			rp.src_width = sp.width;
 			rp.src_height = sp.height;
-			rp.pixel_type = static_cast<zg_pixel_type>(s.pixel_type);
-			rp.depth = s.depth;
+			rp.pixel_type = static_cast<zg_pixel_type>(fr.type);
+			rp.depth = fr.type == ZG_PIXEL_FLOAT ? 32 : fr.depth;
 			rp.dst_width = dp.width;
 			rp.dst_height = dp.height;
 			rp.filter = static_cast<zg_resample_filter>(chroma && s.color == COLOR_YUV ? gp.resample_filter_uv : gp.resample_filter);
@@ -350,7 +450,22 @@ zg_graph *zg_graph_build(const zg_image_format *src_format, const zg_image_forma
 				zg_get_last_error(msg, sizeof(msg));
 				throw Error(rc, msg);
 			}
-			zg_resize_get_tmp_size(gpl.resize, &gpl.tmp);
+			size_t rtmp = 0;
+			zg_resize_get_tmp_size(gpl.resize, &rtmp);
+			size_t off = 0;
+			if (!fmt_equal(fs, fr)) {
+				gpl.pre = make_depth(sp.width, sp.height, fs, fr, dither, p);
+				gpl.pre_pitch = pitch_of(sp.width, bytes(fr.type));
+				off += gpl.pre_pitch * sp.height;
+			}
+			if (!fmt_equal(fr, fd)) {
+				gpl.post = make_depth(dp.width, dp.height, fr, fd, dither, p);
+				gpl.mid_pitch = pitch_of(dp.width, bytes(fr.type));
+				gpl.off_mid = off;
+				off += gpl.mid_pitch * dp.height;
+			}
+			gpl.off_tmp = off;
+			gpl.tmp = off + rtmp;
 			g->tmp_size = std::max(g->tmp_size, gpl.tmp);
 		}
 		result = g.release();
@@ -404,20 +519,38 @@ zg_error_code zg_graph_process(const zg_graph *g, const zg_image_buffer_const *s
 			char *dp = static_cast<char *>(dst->plane[p].data);
 			if (!sp || !dp)
 				throw Error(kErrIllegalArgument, "null plane pointer");
+			const char *from = sp + static_cast<ptrdiff_t>(pl.off_y) * src->plane[p].stride +
+			                   static_cast<ptrdiff_t>(pl.off_x) * pl.in_bytes;
 			if (pl.mode == 0 || pl.mode == 1) {
-				const char *from = sp + static_cast<ptrdiff_t>(pl.off_y) * src->plane[p].stride +
-				                   static_cast<ptrdiff_t>(pl.off_x) * g->sample_bytes;
 				cuda_check(cudaMemcpy2DAsync(dp, dst->plane[p].stride, from, src->plane[p].stride,
-				                             static_cast<size_t>(pl.w) * g->sample_bytes, pl.h,
+				                             static_cast<size_t>(pl.w) * pl.in_bytes, pl.h,
 				                             cudaMemcpyDeviceToDevice, st), "plane copy");
 				continue;
 			}
-			zg_error_code rc = zg_resize_process(pl.resize, sp, src->plane[p].stride, dp, dst->plane[p].stride, tmp, stream);
+			if (pl.mode == 3 || pl.mode == 4) {
+				run_depth(pl.only, from, src->plane[p].stride, dp, dst->plane[p].stride, stream);
+				continue;
+			}
+			if (pl.tmp && !tmp)
+				throw Error(kErrIllegalArgument, "tmp is null");
+			char *t = static_cast<char *>(tmp);
+			const void *rs = sp;
+			ptrdiff_t rss = src->plane[p].stride;
+			if (pl.pre) {
+				run_depth(pl.pre, sp, src->plane[p].stride, t, static_cast<ptrdiff_t>(pl.pre_pitch), stream);
+				rs = t;
+				rss = static_cast<ptrdiff_t>(pl.pre_pitch);
+			}
+			void *rd = pl.post ? static_cast<void *>(t + pl.off_mid) : static_cast<void *>(dp);
+			const ptrdiff_t rds = pl.post ? static_cast<ptrdiff_t>(pl.mid_pitch) : dst->plane[p].stride;
+			zg_error_code rc = zg_resize_process(pl.resize, rs, rss, rd, rds, t ? t + pl.off_tmp : nullptr, stream);
 			if (rc != ZG_ERROR_SUCCESS) {
 				char msg[256];
 				zg_get_last_error(msg, sizeof(msg));
 				throw Error(rc, msg);
 			}
+			if (pl.post)
+				run_depth(pl.post, rd, rds, dp, dst->plane[p].stride, stream);
 		}
 	});
 }

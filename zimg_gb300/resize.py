@@ -6,7 +6,9 @@ Names and argument meaning follow the reference:
 * ``ResizeConversion`` — src/zimg/resize/resize.h:22-44 (zero to two passes)
 * ``compute_filter``   — src/zimg/resize/filter.h:178 (host-side tap tables)
 * ``Batch``            — many conversions in one persistent launch
-* ``Graph``            — resize-only zimg_filter_graph_build/process
+* ``DepthConversion``  — src/zimg/depth/depth.h:29-53 (pixel type / depth / range)
+* ``Graph``            — zimg_filter_graph_build/process: resize, with the depth
+                         conversions zimg's graph puts around it
 
 Device buffers are PyTorch CUDA tensors (plumbing only: memory and streams);
 every computation runs in the native library. WORD planes may be passed as
@@ -24,7 +26,7 @@ from . import capi
 from .capi import ZimgError, check, load
 
 __all__ = ["ZimgError", "compute_filter", "FilterContext", "ResizeImplBuilder", "ResizePass", "ResizeConversion",
-           "Resize", "Batch", "Graph", "filter_id"]
+           "Resize", "Batch", "Graph", "DepthConversion", "Depth", "filter_id"]
 
 
 def filter_id(kind) -> int:
@@ -438,7 +440,8 @@ def graph_params(**kw) -> capi.GraphBuilderParams:
 
 
 class Graph:
-    """Resize-only zimg_filter_graph (zimg.h:507,550-552,679)."""
+    """zimg_filter_graph (zimg.h:507,550-552,679): resize, with the depth
+    conversions zimg's graph puts around it when the pixel format changes."""
 
     def __init__(self, src_format: capi.ImageFormat, dst_format: capi.ImageFormat,
                  params: capi.GraphBuilderParams | None = None):
