@@ -98,14 +98,15 @@ ZG_API void zg_clear_last_error(void);
  *   mode 0: formats equal (zimg's PixelFormat ==, pixel.h:194-199): a copy;
  *   mode 1: integer to integer, both limited range, same luma/chroma, depth
  *           not reduced: left shift (depth_convert.cpp:14-21);
- *   mode 2: to FLOAT: x * scale + offset (depth_convert.cpp:32-39);
+ *   mode 2: to FLOAT or HALF: x * scale + offset from integers, the value
+ *           itself between HALF and FLOAT (depth_convert.cpp:23-57; HALF is
+ *           IEEE binary16, rounded to nearest even);
  *   mode 3: otherwise, to an integer type: x * scale + offset plus the dither
  *           value, clamped, rounded to nearest even (dither.cpp:37-54).
  * scale and offset are zimg's (quantize.h:19-45). Results equal zimg's C path
  * (CPUClass::NONE) bit for bit. Dither NONE and ORDERED (zimg's 16x16
  * matrix, variant chosen by `plane` mod 4, dither.cpp:137-210) are built;
- * RANDOM and ERROR_DIFFUSION, and the HALF type, return
- * ZG_ERROR_UNSUPPORTED_OPERATION. A limited-range format below 8 bits returns
+ * RANDOM and ERROR_DIFFUSION return ZG_ERROR_UNSUPPORTED_OPERATION. A limited-range format below 8 bits returns
  * ZG_ERROR_BIT_DEPTH_OVERFLOW (depth.cpp:52-53), as does a depth beyond its
  * type. */
 typedef enum zg_dither_type {

@@ -34,7 +34,7 @@ T_U16, T_F32, T_F64 = 1, 3, 4
 # zimg_pixel_type_e (zimg.h:184-189) and zimg_dither_type_e (zimg.h:191-196)
 PIXEL_TYPES = {"byte": 0, "word": 1, "half": 2, "float": 3}
 DITHERS = {"none": 0, "ordered": 1, "random": 2, "error_diffusion": 3}
-NP_TYPES = {0: np.uint8, 1: np.uint16, 3: np.float32}
+NP_TYPES = {0: np.uint8, 1: np.uint16, 2: np.uint16, 3: np.float32}  # HALF planes hold binary16 bits
 
 
 @dataclass(frozen=True)

@@ -639,7 +639,7 @@ int orc_resize_pass(int type, unsigned depth, int horizontal, int kind, double a
  * copy, a lossless left shift (depth_convert.cpp:14-21), a conversion to float
  * (depth_convert.cpp:32-39) or a dither to integer (dither.cpp:37-54, types
  * NONE and ORDERED; RANDOM and ERROR_DIFFUSION are not restated). Pixel types
- * follow zimg.h (0 BYTE, 1 WORD, 3 FLOAT; HALF is not restated).
+ * follow zimg.h (0 BYTE, 1 WORD, 2 HALF, 3 FLOAT).
  */
 typedef struct orc_pixfmt {
 	int type;
@@ -650,6 +650,11 @@ typedef struct orc_pixfmt {
 static int pix_is_float(int t)
 {
 	return t == 2 || t == 3;
+}
+
+static size_t pix_size(int t)
+{
+	return t == 0 ? 1 : (t == 3 ? 4 : 2);
 }
 
 /* integer_offset / integer_range, quantize.h:19-32 */
@@ -723,22 +728,88 @@ float orc_dither_value(int dither, unsigned seq, unsigned i, unsigned j)
 	return (float)(m + 1) / 257.0f - 0.5f;
 }
 
+/* IEEE binary16 <-> binary32 (quantize.cpp:24-146 follows the same
+ * definitions): half to float is exact; float to half rounds to nearest
+ * even, overflows to infinity, and keeps NaNs quiet with the payload's top
+ * bits. Written here from the IEEE formats. */
+float orc_half_to_float(uint16_t h)
+{
+	const uint32_t sign = (uint32_t)(h >> 15) << 31;
+	const uint32_t e = (h >> 10) & 0x1F, m = h & 0x3FF;
+	uint32_t bits;
+	if (e == 0x1F) {
+		bits = sign | 0x7F800000u | (m ? ((m << 13) | 0x00400000u) : 0);
+	} else if (e == 0) {
+		if (m == 0) {
+			bits = sign;
+		} else {
+			/* subnormal: normalise the significand */
+			int k = 0;
+			uint32_t mm = m;
+			while (!(mm & 0x400)) {
+				mm <<= 1;
+				++k;
+			}
+			bits = sign | ((uint32_t)(127 - 15 - k + 1) << 23) | ((mm & 0x3FF) << 13);
+		}
+	} else {
+		bits = sign | ((e + 127 - 15) << 23) | (m << 13);
+	}
+	float f;
+	memcpy(&f, &bits, 4);
+	return f;
+}
+
+uint16_t orc_float_to_half(float f)
+{
+	uint32_t x;
+	memcpy(&x, &f, 4);
+	const uint32_t sign = (x >> 31) << 15;
+	const uint32_t e = (x >> 23) & 0xFF, m = x & 0x7FFFFF;
+	if (e == 0xFF)
+		return (uint16_t)(sign | 0x7C00u | (m ? ((m >> 13) | 0x200u) : 0));
+	/* the significand with its leading bit, and how far it must move right
+	 * for a half's 10 stored bits (more for results below the normal range) */
+	uint32_t sig = m, shift = 13, he;
+	if (e <= 112) {
+		shift = 13 + 112 - e + 1;
+		if (shift > 31)
+			shift = 31;
+		sig = m | 0x800000u;
+		he = 0;
+	} else {
+		he = e - 112;
+	}
+	/* round to nearest, ties to even */
+	const uint32_t rem = sig & ((1u << shift) - 1), halfway = 1u << (shift - 1);
+	uint32_t q = sig >> shift;
+	if (rem > halfway || (rem == halfway && (q & 1)))
+		++q;
+	if (q > 0x3FF) {
+		q &= 0x3FF;
+		++he;
+	}
+	if (he >= 0x1F)
+		return (uint16_t)(sign | 0x7C00u);
+	return (uint16_t)(sign | (he << 10) | q);
+}
+
 static float load_sample(int type, const void *row, unsigned j)
 {
 	if (type == 0)
 		return (float)((const uint8_t *)row)[j];
 	if (type == 1)
 		return (float)((const uint16_t *)row)[j];
+	if (type == 2)
+		return orc_half_to_float(((const uint16_t *)row)[j]);
 	return ((const float *)row)[j];
 }
 
-/* Mode of a conversion (depth.cpp:52-66): 0 copy, 1 left shift, 2 to float,
- * 3 dither; negative: zimg's error (-1 bit depth below 8 in limited range,
- * -2 not restated here: HALF, or RANDOM / ERROR_DIFFUSION dither). */
+/* Mode of a conversion (depth.cpp:52-66): 0 copy, 1 left shift, 2 to float
+ * or half, 3 dither; negative: zimg's error (-1 bit depth below 8 in limited
+ * range, -2 not restated here: RANDOM / ERROR_DIFFUSION dither). */
 int orc_depth_mode(const orc_pixfmt *in, const orc_pixfmt *out, int dither)
 {
-	if (in->type == 2 || out->type == 2)
-		return -2;
 	if ((!in->fullrange && in->depth < 8) || (!out->fullrange && out->depth < 8))
 		return -1;
 	if (pix_equal(in, out))
@@ -747,7 +818,7 @@ int orc_depth_mode(const orc_pixfmt *in, const orc_pixfmt *out, int dither)
 	    in->chroma == out->chroma && out->depth >= in->depth)
 		return 1;
 	if (pix_is_float(out->type))
-		return pix_is_float(in->type) ? 0 : 2;
+		return (pix_is_float(in->type) && in->type == out->type) ? 0 : 2;
 	return (dither == 0 || dither == 1) ? 3 : -2;
 }
 
@@ -766,7 +837,7 @@ int orc_depth_convert(const orc_pixfmt *in, const orc_pixfmt *out, int dither, u
 		char *d = (char *)dst + (ptrdiff_t)i * dst_stride;
 		for (unsigned j = 0; j < w; ++j) {
 			if (mode == 0) {
-				const size_t n = type_size(out->type);
+				const size_t n = pix_size(out->type);
 				memcpy(d + j * n, s + j * n, n);
 			} else if (mode == 1) {
 				/* integer_to_integer, depth_convert.cpp:14-21 */
@@ -776,9 +847,19 @@ int orc_depth_convert(const orc_pixfmt *in, const orc_pixfmt *out, int dither, u
 				else
 					((uint16_t *)d)[j] = (uint16_t)(x << shift);
 			} else if (mode == 2) {
-				/* integer_to_float, depth_convert.cpp:32-39 (product, then sum) */
-				const float p = load_sample(in->type, s, j) * scale;
-				((float *)d)[j] = p + offset;
+				/* integer_to_float / integer_to_half (product, then sum), or
+				 * half <-> float as is (depth_convert.cpp:23-57) */
+				float v;
+				if (pix_is_float(in->type)) {
+					v = load_sample(in->type, s, j);
+				} else {
+					const float p = load_sample(in->type, s, j) * scale;
+					v = p + offset;
+				}
+				if (out->type == 2)
+					((uint16_t *)d)[j] = orc_float_to_half(v);
+				else
+					((float *)d)[j] = v;
 			} else {
 				/* dither_ordered, dither.cpp:37-54 */
 				const float p = load_sample(in->type, s, j) * scale;

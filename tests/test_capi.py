@@ -116,7 +116,7 @@ def test_depth_create_errors(lib):
         h = C.c_void_p()
         return lib.zg_depth_create(C.byref(p), C.byref(h))
 
-    assert create(2, 16, 0, 8) == 3072            # HALF: UNSUPPORTED_OPERATION
+    assert create(2, 17, 0, 8) == 1028            # HALF deeper than 16 bits: BIT_DEPTH_OVERFLOW
     assert create(3, 32, 0, 8, dither=2) == 3072  # RANDOM dither: not built
     assert create(3, 32, 0, 8, dither=3) == 3072  # ERROR_DIFFUSION: not built
     assert create(1, 7, 1, 10) == 1028            # limited range below 8 bits: BIT_DEPTH_OVERFLOW

@@ -31,13 +31,27 @@ CASES = [
     (PF("word", 10, False, True), PF("float", None, False, True), "none"),
     (PF("word", 16, True), PF("float"), "none"),
     (PF("word", 10), PF("word", 10), "ordered"),           # equal formats: copy
+    (PF("half"), PF("float"), "none"),                     # HALF (IEEE binary16)
+    (PF("float"), PF("half"), "none"),
+    (PF("byte", 8), PF("half"), "none"),
+    (PF("word", 10, False, True), PF("half", None, False, True), "none"),
+    (PF("half"), PF("byte", 8), "ordered"),
+    (PF("half", None, False, True), PF("word", 10, False, True), "ordered"),
 ]
 
 
-def make_src(rng, f: PF, h, w):
-    if f.type == "float":
+def make_src(rng, f: PF, h, w, special=True):
+    if f.type in ("float", "half"):
         x = rng.random((h, w), dtype=np.float32) * 1.25 - 0.125  # out-of-range values exercise the clamp
-        return (x - 0.5).astype(np.float32) if f.chroma else x.astype(np.float32)
+        x = (x - 0.5).astype(np.float32) if f.chroma else x.astype(np.float32)
+        if special:
+            # signed zeros, infinities, binary16 subnormals and overflow
+            v = np.array([0.0, -0.0, np.inf, -np.inf, 3e-6, 6.1e-5, 70000.0, 65519.0], np.float32)
+            x.flat[: min(x.size, v.size)] = v[: min(x.size, v.size)]
+        if f.type == "half":
+            with np.errstate(over="ignore"):
+                return x.astype(np.float16).view(np.uint16)
+        return x
     return rng.integers(0, 1 << f.bits, size=(h, w)).astype(f.dtype)
 
 

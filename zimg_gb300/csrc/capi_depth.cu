@@ -105,8 +105,6 @@ zg_error_code zg_depth_create(const zg_depth_params *params, zg_depth **out)
 		if (!q.width || !q.height)
 			throw Error(kErrInvalidImageSize, "image dimensions must be non-zero");
 		const int ci = type_code(q.pixel_in.type), co = type_code(q.pixel_out.type);
-		if (ci == 2 || co == 2)
-			throw Error(kErrUnsupported, "HALF samples are not supported by this library");
 		if (q.dither_type < ZG_DITHER_NONE || q.dither_type > ZG_DITHER_ERROR_DIFFUSION)
 			throw Error(kErrEnumOutOfRange, "unrecognized dither type");
 		const zg_pixel_format fi = normalised(q.pixel_in, ci), fo = normalised(q.pixel_out, co);
@@ -124,7 +122,7 @@ zg_error_code zg_depth_create(const zg_depth_params *params, zg_depth **out)
 			d->mode = 1;
 			d->shift = fo.depth - fi.depth;
 		} else if (is_float(co)) {
-			d->mode = is_float(ci) ? 0 : 2;
+			d->mode = (is_float(ci) && ci == co) ? 0 : 2;
 		} else {
 			if (q.dither_type != ZG_DITHER_NONE && q.dither_type != ZG_DITHER_ORDERED)
 				throw Error(kErrUnsupported, "only NONE and ORDERED dithering are supported by this library");
@@ -195,7 +193,7 @@ zg_error_code zg_depth_process(const zg_depth *d, const void *src, ptrdiff_t src
 		L.shift = d->shift;
 		L.seq = q.plane;
 		L.ordered = q.dither_type == ZG_DITHER_ORDERED;
-		// 8 samples per vector: 8-byte loads of BYTE, 16-byte loads of WORD and FLOAT
+		// 8 samples per vector: 8-byte loads of BYTE, 16-byte loads of WORD, HALF and FLOAT
 		L.vec_in = aligned(src, src_stride, bi == 1 ? 8 : 16);
 		L.vec_out = aligned(dst, dst_stride, bo == 1 ? 8 : 16);
 		cuda_check(launch_depth(ci, co, d->mode, L, st), "depth conversion launch");

@@ -356,8 +356,6 @@ zg_graph *zg_graph_build(const zg_image_format *src_format, const zg_image_forma
 		zg_graph_builder_params_default(&defaults, src_format->version);
 		const zg_graph_builder_params &gp = params ? *params : defaults;
 
-		if (s.pixel_type == ZG_PIXEL_HALF || d.pixel_type == ZG_PIXEL_HALF)
-			throw Error(kErrUnsupported, "HALF samples are not supported by this library");
 		const bool format_change =
 			s.pixel_type != d.pixel_type || s.depth != d.depth || (s.pixel_type != ZG_PIXEL_FLOAT && s.range != d.range);
 		if (s.color != d.color || s.matrix != d.matrix || s.transfer != d.transfer || s.primaries != d.primaries)
@@ -369,7 +367,7 @@ zg_graph *zg_graph_build(const zg_image_format *src_format, const zg_image_forma
 
 		auto g = std::make_unique<zg_graph>();
 		g->device = current_device();
-		auto bytes = [](int t) { return t == ZG_PIXEL_BYTE ? 1u : (t == ZG_PIXEL_WORD ? 2u : 4u); };
+		auto bytes = [](int t) { return t == ZG_PIXEL_BYTE ? 1u : (t == ZG_PIXEL_FLOAT ? 4u : 2u); };
 
 		for (int p = 0; p < 4; ++p) {
 			const bool chroma = p == PLANE_U || p == PLANE_V;

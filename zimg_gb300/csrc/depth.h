@@ -22,8 +22,8 @@ struct DepthLaunch {
 	int vec_in, vec_out;  // planes aligned for 8-sample vector loads / stores
 };
 
-// in_type / out_type: 0 BYTE, 1 WORD, 3 FLOAT; mode 1 left shift, 2 to
-// float, 3 dither to integer.
+// in_type / out_type: 0 BYTE, 1 WORD, 2 HALF, 3 FLOAT; mode 1 left shift,
+// 2 to FLOAT or HALF, 3 dither to integer.
 cudaError_t launch_depth(int in_type, int out_type, int mode, const DepthLaunch &L, cudaStream_t stream);
 
 } // namespace zg

@@ -1,6 +1,6 @@
 // Depth conversion of one plane (zimg's DepthConversion, src/zimg/depth/):
-// left shift, integer to float, and dither (NONE / ORDERED) to an integer
-// type. One pass over the plane, HBM-bound: each thread converts runs of 8
+// left shift, integer to FLOAT or HALF, HALF <-> FLOAT, and dither (NONE /
+// ORDERED) to an integer type. One pass over the plane, HBM-bound: each thread converts runs of 8
 // samples of one line with vector loads and stores where the plane allows.
 //
 // Arithmetic is zimg's C path in IEEE single precision, step for step:
@@ -12,6 +12,7 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <type_traits>
 
 #include "depth.h"
 
@@ -37,10 +38,73 @@ __device__ __forceinline__ unsigned bayer16(unsigned i, unsigned j)
 	return v;
 }
 
+// HALF samples: IEEE binary16 bits, a type of its own so that templates do
+// not take them for WORD.
+struct Half {
+	uint16_t bits;
+};
+
+// binary16 -> binary32, exact; NaNs stay NaN with the quiet bit set.
+__device__ __forceinline__ float half_bits_to_float(uint32_t h)
+{
+	const uint32_t sign = (h & 0x8000u) << 16;
+	const uint32_t e = (h >> 10) & 0x1Fu, m = h & 0x3FFu;
+	if (e == 0x1Fu)
+		return __uint_as_float(sign | 0x7F800000u | (m ? ((m << 13) | 0x00400000u) : 0u));
+	if (e == 0) {
+		// zero or subnormal: m * 2^-24, exact in binary32
+		const float v = __fmul_rn(static_cast<float>(m), 5.9604644775390625e-8f);
+		return __uint_as_float(__float_as_uint(v) | sign);
+	}
+	return __uint_as_float(sign | ((e + 112u) << 23) | (m << 13));
+}
+
+// binary32 -> binary16 bits, rounded to nearest even; overflow to infinity;
+// NaNs keep the payload's top bits with the quiet bit set.
+__device__ __forceinline__ uint32_t float_to_half_bits(float f)
+{
+	const uint32_t x = __float_as_uint(f);
+	const uint32_t sign = (x >> 16) & 0x8000u;
+	const uint32_t e = (x >> 23) & 0xFFu, m = x & 0x7FFFFFu;
+	if (e == 0xFFu)
+		return sign | 0x7C00u | (m ? ((m >> 13) | 0x200u) : 0u);
+	uint32_t sig = m, shift = 13, he;
+	if (e <= 112u) {
+		shift = min(13u + 112u - e + 1u, 31u);
+		sig = m | 0x800000u;
+		he = 0;
+	} else {
+		he = e - 112u;
+	}
+	const uint32_t rem = sig & ((1u << shift) - 1u), halfway = 1u << (shift - 1u);
+	uint32_t q = sig >> shift;
+	if (rem > halfway || (rem == halfway && (q & 1u)))
+		++q;
+	if (q > 0x3FFu) {
+		q &= 0x3FFu;
+		++he;
+	}
+	if (he >= 0x1Fu)
+		return sign | 0x7C00u;
+	return sign | (he << 10) | q;
+}
+
 template <class T>
 __device__ __forceinline__ void load_run(const T *p, float (&x)[kRun], bool vec)
 {
-	if (vec) {
+	if constexpr (std::is_same_v<T, Half>) {
+		if (vec) {
+			const uint4 v = *reinterpret_cast<const uint4 *>(p);
+			const uint32_t w[4] = { v.x, v.y, v.z, v.w };
+#pragma unroll
+			for (int e = 0; e < kRun; ++e)
+				x[e] = half_bits_to_float((w[e >> 1] >> (16 * (e & 1))) & 0xffffu);
+		} else {
+#pragma unroll
+			for (int e = 0; e < kRun; ++e)
+				x[e] = half_bits_to_float(p[e].bits);
+		}
+	} else if (vec) {
 		if constexpr (sizeof(T) == 1) {
 			const uint2 v = *reinterpret_cast<const uint2 *>(p);
 			const uint32_t w[2] = { v.x, v.y };
@@ -64,6 +128,16 @@ __device__ __forceinline__ void load_run(const T *p, float (&x)[kRun], bool vec)
 		for (int e = 0; e < kRun; ++e)
 			x[e] = static_cast<float>(p[e]);
 	}
+}
+
+// one sample of a partial run
+template <class T>
+__device__ __forceinline__ float load_one(const T *p)
+{
+	if constexpr (std::is_same_v<T, Half>)
+		return half_bits_to_float(p->bits);
+	else
+		return static_cast<float>(*p);
 }
 
 // Round-to-nearest-even integers of 0 <= v < 2^22: v + 1.5 * 2^23 has an ulp
@@ -141,14 +215,29 @@ depth_kernel(DepthLaunch L)
 			} else {
 #pragma unroll
 				for (int e = 0; e < kRun; ++e)
-					x[e] = e < n ? static_cast<float>(s[e]) : 0.0f;
+					x[e] = e < n ? load_one<T>(s + e) : 0.0f;
 			}
 			if constexpr (MODE == 2) {
+				// integer in: x * scale + offset; HALF / FLOAT in: the value
+				// as it is (depth_convert.cpp:23-57)
+				constexpr bool kFloatIn = std::is_same_v<T, float> || std::is_same_v<T, Half>;
 				float y[kRun];
 #pragma unroll
 				for (int e = 0; e < kRun; ++e)
-					y[e] = __fadd_rn(__fmul_rn(x[e], L.scale), L.offset);
-				if (n == kRun && L.vec_out) {
+					y[e] = kFloatIn ? x[e] : __fadd_rn(__fmul_rn(x[e], L.scale), L.offset);
+				if constexpr (std::is_same_v<U, Half>) {
+					uint32_t h[kRun];
+#pragma unroll
+					for (int e = 0; e < kRun; ++e)
+						h[e] = float_to_half_bits(y[e]);
+					if (n == kRun && L.vec_out) {
+						*reinterpret_cast<uint4 *>(d) = make_uint4(h[0] | (h[1] << 16), h[2] | (h[3] << 16),
+						                                           h[4] | (h[5] << 16), h[6] | (h[7] << 16));
+					} else {
+						for (int e = 0; e < n; ++e)
+							d[e].bits = static_cast<uint16_t>(h[e]);
+					}
+				} else if (n == kRun && L.vec_out) {
 					reinterpret_cast<float4 *>(d)[0] = make_float4(y[0], y[1], y[2], y[3]);
 					reinterpret_cast<float4 *>(d)[1] = make_float4(y[4], y[5], y[6], y[7]);
 				} else {
@@ -186,24 +275,29 @@ depth_kernel(DepthLaunch L)
 	}
 }
 
+template <class T>
+constexpr bool is_int = std::is_same_v<T, uint8_t> || std::is_same_v<T, uint16_t>;
+template <class T>
+constexpr bool is_fp = std::is_same_v<T, float> || std::is_same_v<T, Half>;
+
 template <class T, class U>
 cudaError_t launch_tu(int mode, const DepthLaunch &L, int grid, cudaStream_t st)
 {
 	switch (mode) {
 	case 1:
-		if constexpr (sizeof(U) != 4 && sizeof(T) != 4) {
+		if constexpr (is_int<T> && is_int<U>) {
 			depth_kernel<T, U, 1><<<grid, kThreads, 0, st>>>(L);
 			return cudaGetLastError();
 		}
 		return cudaErrorInvalidValue;
 	case 2:
-		if constexpr (sizeof(U) == 4) {
-			depth_kernel<T, float, 2><<<grid, kThreads, 0, st>>>(L);
+		if constexpr (is_fp<U>) {
+			depth_kernel<T, U, 2><<<grid, kThreads, 0, st>>>(L);
 			return cudaGetLastError();
 		}
 		return cudaErrorInvalidValue;
 	case 3:
-		if constexpr (sizeof(U) != 4) {
+		if constexpr (is_int<U>) {
 			depth_kernel<T, U, 3><<<grid, kThreads, 0, st>>>(L);
 			return cudaGetLastError();
 		}
@@ -218,6 +312,7 @@ cudaError_t launch_t(int out_type, int mode, const DepthLaunch &L, int grid, cud
 	switch (out_type) {
 	case 0: return launch_tu<T, uint8_t>(mode, L, grid, st);
 	case 1: return launch_tu<T, uint16_t>(mode, L, grid, st);
+	case 2: return launch_tu<T, Half>(mode, L, grid, st);
 	case 3: return launch_tu<T, float>(mode, L, grid, st);
 	default: return cudaErrorInvalidValue;
 	}
@@ -242,6 +337,7 @@ cudaError_t launch_depth(int in_type, int out_type, int mode, const DepthLaunch 
 	switch (in_type) {
 	case 0: return launch_t<uint8_t>(out_type, mode, L, grid, stream);
 	case 1: return launch_t<uint16_t>(out_type, mode, L, grid, stream);
+	case 2: return launch_t<Half>(out_type, mode, L, grid, stream);
 	case 3: return launch_t<float>(out_type, mode, L, grid, stream);
 	default: return cudaErrorInvalidValue;
 	}
