@@ -10,6 +10,10 @@
  * caller provides the scratch buffer whose size *_get_tmp_size reports, as
  * zimg_filter_graph_process does (zimg.h:494-507).
  *
+ * Plane strides are in bytes and may be negative (bottom-up planes: line i at
+ * data + i * stride, as zimg_image_buffer allows, zimg.h:387-433); their
+ * magnitude must cover a line.
+ *
  * Each declaration names the zimg interface it replaces (paths relative to the
  * zimg source tree).
  */

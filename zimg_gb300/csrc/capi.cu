@@ -159,7 +159,7 @@ void check_plane(const void *p, ptrdiff_t stride, unsigned w, Sample s, const ch
 {
 	if (!p)
 		throw Error(kErrIllegalArgument, std::string(what) + " is null");
-	if (stride < static_cast<ptrdiff_t>(w) * static_cast<ptrdiff_t>(bytes_of(s)))
+	if (abs_stride(stride) < static_cast<ptrdiff_t>(w) * static_cast<ptrdiff_t>(bytes_of(s)))
 		throw Error(kErrIllegalArgument, std::string(what) + " stride smaller than a line");
 	if (reinterpret_cast<uintptr_t>(p) % bytes_of(s) || stride % bytes_of(s))
 		throw Error(kErrIllegalArgument, std::string(what) + " not aligned to the sample size");
@@ -400,9 +400,8 @@ zg_error_code zg_resize_process(const zg_resize *r, const void *src, ptrdiff_t s
 		check_plane(src, src_stride, q.src_width, r->sample, "src");
 		check_plane(dst, dst_stride, q.dst_width, r->sample, "dst");
 		if (r->num_passes == 0) {
-			cuda_check(cudaMemcpy2DAsync(dst, dst_stride, src, src_stride,
-			                             static_cast<size_t>(q.dst_width) * bytes_of(r->sample), q.dst_height,
-			                             cudaMemcpyDeviceToDevice, st), "plane copy");
+			copy_plane(dst, dst_stride, src, src_stride, static_cast<size_t>(q.dst_width) * bytes_of(r->sample),
+			           q.dst_height, st);
 			return;
 		}
 		if (r->num_passes == 1) {

@@ -325,8 +325,8 @@ zg_error_code zg_batch_set_io(zg_batch *b, const zg_batch_io *io, zg_stream stre
 			const unsigned bpe = bytes_of(b->jobs[i]->sample);
 			if (!io[i].src || !io[i].dst)
 				throw Error(kErrIllegalArgument, "null plane pointer in batch io");
-			if (io[i].src_stride < static_cast<ptrdiff_t>(q.src_width * bpe) ||
-			    io[i].dst_stride < static_cast<ptrdiff_t>(q.dst_width * bpe))
+			if (abs_stride(io[i].src_stride) < static_cast<ptrdiff_t>(q.src_width * bpe) ||
+			    abs_stride(io[i].dst_stride) < static_cast<ptrdiff_t>(q.dst_width * bpe))
 				throw Error(kErrIllegalArgument, "stride smaller than a line in batch io");
 			if (reinterpret_cast<uintptr_t>(io[i].src) % bpe || reinterpret_cast<uintptr_t>(io[i].dst) % bpe ||
 			    io[i].src_stride % bpe || io[i].dst_stride % bpe)

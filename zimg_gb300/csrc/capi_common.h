@@ -50,6 +50,37 @@ inline void cuda_check(cudaError_t e, const char *what)
 		throw Error(kErrUnknown, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+// A plane copy of `rows` lines of `row_bytes` on `st`; strides may be
+// negative (zimg_image_buffer allows them, zimg.h:387-433). Both negative:
+// the same rows walked from the last one with positive pitches; one negative:
+// line by line.
+inline void copy_plane(void *dst, ptrdiff_t ds, const void *src, ptrdiff_t ss, size_t row_bytes, unsigned rows,
+                       cudaStream_t st)
+{
+	if (!rows || !row_bytes)
+		return;
+	if (ds >= 0 && ss >= 0) {
+		cuda_check(cudaMemcpy2DAsync(dst, static_cast<size_t>(ds), src, static_cast<size_t>(ss), row_bytes, rows,
+		                             cudaMemcpyDeviceToDevice, st), "plane copy");
+	} else if (ds < 0 && ss < 0) {
+		char *d = static_cast<char *>(dst) + static_cast<ptrdiff_t>(rows - 1) * ds;
+		const char *s = static_cast<const char *>(src) + static_cast<ptrdiff_t>(rows - 1) * ss;
+		cuda_check(cudaMemcpy2DAsync(d, static_cast<size_t>(-ds), s, static_cast<size_t>(-ss), row_bytes, rows,
+		                             cudaMemcpyDeviceToDevice, st), "plane copy");
+	} else {
+		for (unsigned i = 0; i < rows; ++i)
+			cuda_check(cudaMemcpyAsync(static_cast<char *>(dst) + static_cast<ptrdiff_t>(i) * ds,
+			                           static_cast<const char *>(src) + static_cast<ptrdiff_t>(i) * ss, row_bytes,
+			                           cudaMemcpyDeviceToDevice, st),
+			           "plane copy");
+	}
+}
+
+inline ptrdiff_t abs_stride(ptrdiff_t s)
+{
+	return s < 0 ? -s : s;
+}
+
 // Owned device allocation made at plan-creation time.
 class DeviceBuffer {
 public:

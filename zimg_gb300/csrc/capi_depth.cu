@@ -166,7 +166,7 @@ zg_error_code zg_depth_process(const zg_depth *d, const void *src, ptrdiff_t src
 		auto check = [](const void *p, ptrdiff_t stride, unsigned w, unsigned b, const char *what) {
 			if (!p)
 				throw Error(kErrIllegalArgument, std::string(what) + " is null");
-			if (stride < static_cast<ptrdiff_t>(w) * static_cast<ptrdiff_t>(b))
+			if (abs_stride(stride) < static_cast<ptrdiff_t>(w) * static_cast<ptrdiff_t>(b))
 				throw Error(kErrIllegalArgument, std::string(what) + " stride smaller than a line");
 			if (reinterpret_cast<uintptr_t>(p) % b || stride % b)
 				throw Error(kErrIllegalArgument, std::string(what) + " not aligned to the sample size");
@@ -175,9 +175,7 @@ zg_error_code zg_depth_process(const zg_depth *d, const void *src, ptrdiff_t src
 		check(dst, dst_stride, q.width, bo, "dst");
 		cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
 		if (d->mode == 0) {
-			cuda_check(cudaMemcpy2DAsync(dst, dst_stride, src, src_stride, static_cast<size_t>(q.width) * bo, q.height,
-			                             cudaMemcpyDeviceToDevice, st),
-			           "plane copy");
+			copy_plane(dst, dst_stride, src, src_stride, static_cast<size_t>(q.width) * bo, q.height, st);
 			return;
 		}
 		DepthLaunch L{};

@@ -520,9 +520,8 @@ zg_error_code zg_graph_process(const zg_graph *g, const zg_image_buffer_const *s
 			const char *from = sp + static_cast<ptrdiff_t>(pl.off_y) * src->plane[p].stride +
 			                   static_cast<ptrdiff_t>(pl.off_x) * pl.in_bytes;
 			if (pl.mode == 0 || pl.mode == 1) {
-				cuda_check(cudaMemcpy2DAsync(dp, dst->plane[p].stride, from, src->plane[p].stride,
-				                             static_cast<size_t>(pl.w) * pl.in_bytes, pl.h,
-				                             cudaMemcpyDeviceToDevice, st), "plane copy");
+				copy_plane(dp, dst->plane[p].stride, from, src->plane[p].stride, static_cast<size_t>(pl.w) * pl.in_bytes,
+				           pl.h, st);
 				continue;
 			}
 			if (pl.mode == 3 || pl.mode == 4) {
