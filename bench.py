@@ -11,6 +11,8 @@ Other workloads (--workload):
                   1920x1080 frames as fields -> 1280x720
   depth_f32_u8    depth conversion around resize (zimg's DepthConversion): 16 frames of 3 planes
                   3840x2160 f32 -> u8 8-bit limited range, ordered dither
+  unresize_f32    zimg's UnresizeConversion (inverse bilinear): 8 frames of 3 planes 1920x1080 f32
+                  -> 1280x720
 
 A step is one pass of the resize path over one batch of synthetic frames that
 are already resident in HBM (inputs larger than L2 across the batch). `value`
@@ -516,6 +518,132 @@ def run_depth(args):
         dist.destroy_process_group()
 
 
+# ---------------------------------------------------------------- unresize --
+# zimg's UnresizeConversion (inverse bilinear, FP32): 8 frames of 3 planes
+# 1920x1080 -> 1280x720. Algorithmic bytes: the planes read and written once.
+
+def unresize_workload(frames: int | None):
+    n = frames or 8
+    planes = [dict(w=1920, h=1080, ow=1280, oh=720) for _ in range(3 * n)]
+    cfg = {"workload": "unresize_f32: 3 planes 1920x1080 f32 -> 1280x720, inverse bilinear "
+                       "(zimg UnresizeConversion)", "frames_per_step": n, "planes_per_step": 3 * n}
+    return planes, cfg
+
+
+def run_unresize(args):
+    import torch
+    import zimg_gb300 as zg
+    from zimg_gb300 import build as zbuild
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    rank = int(os.environ.get("RANK", "0"))
+    torch.cuda.set_device(local)
+    zbuild.build()
+    zg.load()
+    planes, cfg = unresize_workload(args.frames)
+    rng = np.random.default_rng(777 + rank)
+    protos = [rng.random((1080, 1920), dtype=np.float32) for _ in range(2)]
+    u = zg.UnresizeConversion(1920, 1080).set_orig_width(1280).set_orig_height(720).create()
+    srcs = [torch.from_numpy(protos[i % 2]).cuda() for i in range(len(planes))]
+    dsts = [torch.empty((720, 1280), dtype=torch.float32, device="cuda") for _ in planes]
+    # the planes are independent: four streams (each with its own scratch),
+    # forked from and joined to the timed one, run them side by side
+    side = [torch.cuda.Stream() for _ in range(4)]
+    tmps = [torch.empty(max(u.tmp_size, 1), dtype=torch.uint8, device="cuda") for _ in side]
+    tmp = tmps[0]
+    stream = torch.cuda.Stream()
+
+    def step():
+        cur = torch.cuda.current_stream()
+        for sd in side:
+            sd.wait_stream(cur)
+        for k, (s_, d_) in enumerate(zip(srcs, dsts)):
+            u.process(s_, d_, tmps[k % 4], stream=side[k % 4])
+        for sd in side:
+            cur.wait_stream(sd)
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step()
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=stream):
+        step()
+    torch.cuda.synchronize()
+    out_px = sum(pl["ow"] * pl["oh"] for pl in planes)
+    alg_bytes = sum((pl["w"] * pl["h"] + pl["ow"] * pl["oh"]) * 4 for pl in planes)
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    with torch.cuda.stream(stream):
+        for _ in range(max(args.warmup, 3)):
+            graph.replay()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.time()
+        e0.record(stream)
+        for _ in range(args.steps):
+            graph.replay()
+        e1.record(stream)
+        e1.synchronize()
+        t1 = time.time()
+    sampler.stop()
+    ms_step = max_over_ranks(e0.elapsed_time(e1)) / args.steps
+    value = sum_over_ranks(out_px) / (ms_step / 1e3) / 1e6
+    e2e = None
+    if not args.no_e2e:
+        n_e2e = min(len(planes), 6)
+        hsrc = [srcs[i].cpu().pin_memory() for i in range(n_e2e)]
+        hdst = [torch.empty((720, 1280), dtype=torch.float32).pin_memory() for _ in range(n_e2e)]
+
+        def e2e_step():
+            with torch.cuda.stream(stream):
+                for i in range(n_e2e):
+                    srcs[i].copy_(hsrc[i], non_blocking=True)
+                    u.process(srcs[i], dsts[i], tmp, stream=stream)
+                    hdst[i].copy_(dsts[i], non_blocking=True)
+        e2e_step()
+        torch.cuda.synchronize()
+        k = max(3, args.steps // 4)
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record(stream)
+        for _ in range(k):
+            e2e_step()
+        a1.record(stream)
+        a1.synchronize()
+        e_ms = max_over_ranks(a0.elapsed_time(a1) / k)
+        e2e = {"value": round(sum_over_ranks(1280 * 720 * n_e2e) / (e_ms / 1e3) / 1e6, 3), "unit": "Mpixel/s",
+               "h2d_bytes_per_step": 1920 * 1080 * 4 * n_e2e, "d2h_bytes_per_step": 1280 * 720 * 4 * n_e2e,
+               "planes_per_step": n_e2e}
+    peak, peak_kind = load_peaks()
+    achieved = alg_bytes / (ms_step / 1e3) / 1e9
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle.oracle import Oracle, build
+        build()
+        o = Oracle()
+        x = protos[0]
+        n, t_0 = 0, time.perf_counter()
+        while time.perf_counter() - t_0 < args.cpu_seconds:
+            o.unresize_plane(x, 1280, 720)
+            n += 1
+        dt = time.perf_counter() - t_0
+        cpu = {"value": round(n * 1280 * 720 / dt / 1e6, 3), "unit": "Mpixel/s", "cores": 1, "kind": "port",
+               "sample": f"{n} planes 1920x1080 -> 1280x720 in {dt:.1f} s, zimg C-path restatement, one thread"}
+    if rank == 0:
+        line = {"metric": "out Mpixel/s on 1 GB300 + % HBM roofline", "value": round(value, 3), "unit": "Mpixel/s",
+                "n_gpus": int(os.environ.get("WORLD_SIZE", "1")), "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": round(ms_step, 5), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32", "data": "synthetic (seeded)",
+                "config": dict(cfg, l2="inputs larger than L2 (step working set %.2f GB)" % (alg_bytes / 1e9),
+                               parallelism="replicas x1", graph=True),
+                "impl": "ours", "e2e": e2e,
+                "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                             "frac": round(achieved / peak, 4), "peak_source": f"{peak_kind} hbm_gbs",
+                             "traffic": read_traffic(args.workload), "algorithmic_bytes_per_step": alg_bytes,
+                             "kernel_launches_per_step": 2 * len(planes)},
+                "cpu_baseline": cpu, "clocks": sampler.summary(t0, t1), "gpu_launches": 2 * len(planes) * args.steps}
+        print(json.dumps(line), flush=True)
+
+
 def depth_cpu_baseline(planes, seconds=10.0):
     """The oracle's restatement of zimg's C path (one thread), on a bounded sample."""
     from oracle.oracle import Oracle, PixelFormat, build
@@ -539,6 +667,29 @@ def depth_cpu_baseline(planes, seconds=10.0):
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
+        return
+    if args.workload.startswith("unresize_"):
+        from oracle.oracle import Oracle, build
+        build()
+        o = Oracle()
+        planes, cfg = unresize_workload(args.frames)
+        x = np.random.default_rng(99).random((1080, 1920), dtype=np.float32)
+        for _ in range(args.warmup):
+            o.unresize_plane(x, 1280, 720)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            o.unresize_plane(x, 1280, 720)
+        dt = time.perf_counter() - t0
+        v = round(1280 * 720 * args.steps / dt / 1e6, 3)
+        line = {"metric": "out Mpixel/s on 1 GB300 + % HBM roofline", "value": v, "unit": "Mpixel/s",
+                "n_gpus": int(os.environ.get("WORLD_SIZE", "1")), "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": round(dt / args.steps * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)", "config": cfg,
+                "impl": "reference",
+                "cpu_baseline": {"value": v, "unit": "Mpixel/s", "cores": 1, "kind": "port",
+                                 "sample": "one plane 1920x1080 -> 1280x720 per step, zimg C-path restatement"},
+                "e2e": {"value": v, "unit": "Mpixel/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
         return
     if args.workload.startswith("depth_"):
         planes, cfg = depth_workload(args.frames)
@@ -604,6 +755,8 @@ def main():
         run_reference(args)
     elif args.workload.startswith("depth_"):
         run_depth(args)
+    elif args.workload.startswith("unresize_"):
+        run_unresize(args)
     else:
         run_ours(args)
 

@@ -148,6 +148,30 @@ ZG_API zg_error_code zg_depth_get_info(const zg_depth *d, int *mode);
 ZG_API zg_error_code zg_depth_process(const zg_depth *d, const void *src, ptrdiff_t src_stride, void *dst,
                                       ptrdiff_t dst_stride, zg_stream stream);
 
+/* ----------------------------------------------------------------- unresize --
+ * Replaces zimg's UnresizeConversion (src/zimg/unresize/unresize.h:96-114,
+ * unresize.cpp:34-91): the least-squares inverse of a bilinear upsampling of
+ * one FLOAT plane, up_width x up_height -> orig_width x orig_height (shifts
+ * as zimg's). Results equal zimg's C path (CPUClass::NONE) bit for bit. An
+ * axis with orig > up returns ZG_ERROR_RESAMPLING_NOT_AVAILABLE ("unresize can
+ * not upscale", bilinear.cpp:109-110); an axis that keeps its size and has
+ * no shift is skipped, as zimg does. */
+typedef struct zg_unresize_params {
+	unsigned up_width, up_height;
+	unsigned orig_width, orig_height;
+	double shift_w, shift_h;
+} zg_unresize_params;
+
+typedef struct zg_unresize zg_unresize;
+
+ZG_API zg_error_code zg_unresize_create(const zg_unresize_params *params, zg_unresize **out);
+ZG_API void zg_unresize_free(zg_unresize *u);
+ZG_API zg_error_code zg_unresize_get_tmp_size(const zg_unresize *u, size_t *out);
+/* Device planes of FLOAT samples; tmp as *_get_tmp_size asks (may be NULL
+ * when it is 0). */
+ZG_API zg_error_code zg_unresize_process(const zg_unresize *u, const void *src, ptrdiff_t src_stride, void *dst,
+                                         ptrdiff_t dst_stride, void *tmp, zg_stream stream);
+
 /* Health of the pipelined kernels on the current device: 0, or the cause of
  * the first bounded wait that ran out inside one (1: a group's copies never
  * landed, 2: a buffer was never released, 3: a ring too small for a group).

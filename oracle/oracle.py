@@ -116,6 +116,19 @@ class Oracle:
         L.orc_bayer16.restype = C.c_uint
         L.orc_dither_value.argtypes = [C.c_int, C.c_uint, C.c_uint, C.c_uint]
         L.orc_dither_value.restype = C.c_float
+        L.orc_unresize_plane.argtypes = [C.c_uint, C.c_uint, C.c_uint, C.c_uint, C.c_double, C.c_double,
+                                         C.c_void_p, C.c_ssize_t, C.c_void_p, C.c_ssize_t]
+
+    def unresize_plane(self, src: np.ndarray, orig_w: int, orig_h: int, shift_w=0.0, shift_h=0.0) -> np.ndarray:
+        """zimg's UnresizeConversion of one FLOAT plane (C path)."""
+        src = np.ascontiguousarray(src, dtype=np.float32)
+        h, w = src.shape
+        out = np.zeros((orig_h, orig_w), np.float32)
+        rc = self.lib.orc_unresize_plane(w, h, orig_w, orig_h, shift_w, shift_h, src.ctypes.data, src.strides[0],
+                                         out.ctypes.data, out.strides[0])
+        if rc:
+            raise ValueError(f"unresize not available ({rc})")
+        return out
 
     def depth_mode(self, fin: PixelFormat, fout: PixelFormat, dither="none") -> int:
         """0 copy, 1 left shift, 2 to float, 3 dither; negative: not converted."""
@@ -232,6 +245,8 @@ class Reference:
         L.ref_pass_create.argtypes = [C.c_int, C.c_uint, C.c_uint, C.c_int, C.c_uint, C.c_uint, C.c_int, C.c_double,
                                       C.c_double, C.c_double, C.c_double, C.c_int, C.c_char_p, C.c_size_t]
         L.ref_plan_free.argtypes = [C.c_void_p]
+        L.ref_unresize_plane.argtypes = [C.c_uint, C.c_uint, C.c_uint, C.c_uint, C.c_double, C.c_double, C.c_int,
+                                         C.c_void_p, C.c_ssize_t, C.c_void_p, C.c_ssize_t, C.c_char_p, C.c_size_t]
         L.ref_depth_convert.argtypes = [C.c_int, C.c_uint, C.c_int, C.c_int, C.c_int, C.c_uint, C.c_int, C.c_int,
                                         C.c_int, C.c_uint, C.c_int, C.c_uint, C.c_uint, C.c_void_p, C.c_ssize_t,
                                         C.c_void_p, C.c_ssize_t, C.c_char_p, C.c_size_t]
@@ -336,6 +351,23 @@ def _ref_depth_convert(self, src: np.ndarray, fin: PixelFormat, fout: PixelForma
 
 
 Reference.depth_convert = _ref_depth_convert
+
+
+def _ref_unresize_plane(self, src: np.ndarray, orig_w: int, orig_h: int, shift_w=0.0, shift_h=0.0,
+                        cpu=0) -> np.ndarray:
+    """zimg's own UnresizeConversion (src/zimg/unresize/unresize.cpp:34-91)."""
+    src = np.ascontiguousarray(src, dtype=np.float32)
+    h, w = src.shape
+    s = aligned_plane(h, w, np.float32)
+    s[...] = src
+    d = aligned_plane(orig_h, orig_w, np.float32)
+    if self.lib.ref_unresize_plane(w, h, orig_w, orig_h, shift_w, shift_h, cpu, s.ctypes.data, s.strides[0],
+                                   d.ctypes.data, d.strides[0], self.err, 512):
+        self._raise("unresize")
+    return np.array(d)
+
+
+Reference.unresize_plane = _ref_unresize_plane
 
 
 def aligned_plane(h: int, w: int, dtype) -> np.ndarray:

@@ -25,6 +25,7 @@
 #include "common/pixel.h"
 #include "graphengine/filter.h"
 #include "depth/depth.h"
+#include "unresize/unresize.h"
 #include "resize/filter.h"
 #include "resize/resize.h"
 #include "resize/resize_impl.h"
@@ -311,6 +312,43 @@ int ref_depth_convert(int in_type, unsigned in_depth, int in_full, int in_chroma
 			return 0;
 		}
 		run_filter(*f, src, src_stride, dst, dst_stride);
+		return 0;
+	} catch (...) {
+		return catch_all(err, errlen);
+	}
+}
+
+/*
+ * zimg's UnresizeConversion (src/zimg/unresize/unresize.h:96-114,
+ * unresize.cpp:34-91) on one FLOAT plane, its filters driven over the whole
+ * plane; the intermediate of two passes lives in an aligned buffer.
+ */
+int ref_unresize_plane(unsigned up_w, unsigned up_h, unsigned orig_w, unsigned orig_h, double shift_w, double shift_h,
+                       int cpu, const void *src, ptrdiff_t src_stride, void *dst, ptrdiff_t dst_stride, char *err,
+                       size_t errlen)
+{
+	try {
+		zimg::unresize::UnresizeConversion conv(up_w, up_h, PixelType::FLOAT);
+		conv.set_orig_width(orig_w).set_orig_height(orig_h).set_shift_w(shift_w).set_shift_h(shift_h).set_cpu(make_cpu(cpu));
+		auto pair = conv.create();
+		if (!pair.first) {
+			for (unsigned i = 0; i < up_h; ++i)
+				std::memcpy(static_cast<char *>(dst) + i * dst_stride, static_cast<const char *>(src) + i * src_stride,
+				            static_cast<size_t>(up_w) * 4);
+			return 0;
+		}
+		if (!pair.second) {
+			run_filter(*pair.first, src, src_stride, dst, dst_stride);
+			return 0;
+		}
+		const graphengine::FilterDescriptor &d = pair.first->descriptor();
+		ptrdiff_t tmp_stride = (static_cast<ptrdiff_t>(d.format.width) * 4 + 63) & ~static_cast<ptrdiff_t>(63);
+		void *tmp = aligned_buf(static_cast<size_t>(tmp_stride) * (d.format.height + 1));
+		if (!tmp)
+			throw std::bad_alloc{};
+		run_filter(*pair.first, src, src_stride, tmp, tmp_stride);
+		run_filter(*pair.second, tmp, tmp_stride, dst, dst_stride);
+		std::free(tmp);
 		return 0;
 	} catch (...) {
 		return catch_all(err, errlen);

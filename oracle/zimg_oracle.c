@@ -876,3 +876,271 @@ int orc_depth_convert(const orc_pixfmt *in, const orc_pixfmt *out, int dither, u
 	}
 	return 0;
 }
+
+/* ---------------------------------------------------------------- unresize --
+ * zimg's unresize (src/zimg/unresize/): the least-squares inverse of a
+ * bilinear upsampling, FP32 only, C path.
+ *
+ * Context (bilinear.cpp:60-170), all FP64: A (up x orig) holds the bilinear
+ * weights of each upsampled sample, written with RowMatrix's rule (a write
+ * that does not change the value does not grow the row); A' is its transpose
+ * under the same rule, then trimmed of zeros at both ends (matrix.cpp:164-200);
+ * of A'A (matrix.cpp:202-219: k ascending over A' row r's run, products then
+ * sums) only the band r-1..r+1 is used, by a tridiagonal LU with DBL_EPSILON
+ * guards (bilinear.cpp:20-57). The per-line data are A''s rows packed to a
+ * common width (their run starts clamped so the run fits) and the LU terms
+ * as float, 1/(l + eps) pre-inverted.
+ */
+typedef struct {
+	unsigned up, orig;      /* input (upsampled) and output (original) dimensions */
+	unsigned row_size;
+	float *coef;            /* [orig][row_size] */
+	unsigned *offset;       /* [orig] */
+	float *lu_c, *lu_l, *lu_u;
+} orc_unresize_ctx;
+
+void orc_unresize_ctx_free(orc_unresize_ctx *c)
+{
+	free(c->coef);
+	free(c->offset);
+	free(c->lu_c);
+	free(c->lu_l);
+	free(c->lu_u);
+	memset(c, 0, sizeof(*c));
+}
+
+/* A's row i: up to two (column, weight) entries (bilinear_weights,
+ * bilinear.cpp:60-104, with shift already mapped to the input grid). */
+static int bilinear_row(unsigned in, unsigned out, double shift, unsigned i, unsigned col[2], double w[2])
+{
+	const double leftmost = 0.5 + shift, rightmost = in - 0.5 + shift;
+	double lf = floor(leftmost), rf = floor(rightmost);
+	lf = lf < 0.0 ? 0.0 : (lf > in - 1.0 ? in - 1.0 : lf);
+	rf = rf < 0.0 ? 0.0 : (rf > in - 1.0 ? in - 1.0 : rf);
+	const double position = (i + 0.5) * in / out;
+	int n = 0;
+	if (position <= leftmost) {
+		col[n] = (unsigned)lf;
+		w[n++] = 1.0;
+	} else if (position >= rightmost) {
+		col[n] = (unsigned)rf;
+		w[n++] = 1.0;
+	} else {
+		const unsigned left = (unsigned)floor(position - leftmost);
+		const double distance = position - left - leftmost;
+		/* a zero weight leaves the row as it is */
+		if (1.0 - distance != 0.0) {
+			col[n] = left;
+			w[n++] = 1.0 - distance;
+		}
+		if (distance != 0.0) {
+			col[n] = left + 1;
+			w[n++] = distance;
+		}
+	}
+	return n;
+}
+
+int orc_unresize_context(unsigned orig, unsigned up, double shift, orc_unresize_ctx *ctx)
+{
+	memset(ctx, 0, sizeof(*ctx));
+	if (orig > up)
+		return -2; /* "unresize can not upscale" */
+	const unsigned N = orig, M = up;
+	const double s = -shift * N / M; /* output shift mapped to the input grid */
+	/* A as M rows of at most 2 entries */
+	unsigned *acol = malloc(sizeof(unsigned) * 2 * M);
+	double *aw = malloc(sizeof(double) * 2 * M);
+	int *an = malloc(sizeof(int) * M);
+	/* A' row r: run [lo, hi) over A's rows, lo the first row with a nonzero
+	 * entry in column r, hi one past the last */
+	size_t *lo = malloc(sizeof(size_t) * N), *hi = malloc(sizeof(size_t) * N);
+	if (!acol || !aw || !an || !lo || !hi) {
+		free(acol); free(aw); free(an); free(lo); free(hi);
+		return -3;
+	}
+	for (unsigned r = 0; r < N; ++r) {
+		lo[r] = 0;
+		hi[r] = 0;
+	}
+	for (unsigned i = 0; i < M; ++i) {
+		an[i] = bilinear_row(N, M, s, i, acol + 2 * i, aw + 2 * i);
+		for (int e = 0; e < an[i]; ++e) {
+			const unsigned r = acol[2 * i + e];
+			if (hi[r] == 0) {
+				lo[r] = i;
+				hi[r] = i + 1;
+			} else {
+				hi[r] = i + 1;
+			}
+		}
+	}
+	/* A[i][c] */
+#define A_AT(i, c) (an[i] > 0 && acol[2 * (i)] == (c) ? aw[2 * (i)] : (an[i] > 1 && acol[2 * (i) + 1] == (c) ? aw[2 * (i) + 1] : 0.0))
+	/* band of A'A: P[r][c] = sum over k in A' row r's run of A'[r][k] * A[k][c] */
+	double *pl = malloc(sizeof(double) * N), *pd = malloc(sizeof(double) * N), *pu = malloc(sizeof(double) * N);
+	unsigned row_size = 0;
+	for (unsigned r = 0; r < N; ++r) {
+		double acc[3] = { 0.0, 0.0, 0.0 };
+		for (int t = 0; t < 3; ++t) {
+			const long c = (long)r - 1 + t;
+			if (c < 0 || c >= (long)N)
+				continue;
+			double a = 0.0;
+			for (size_t k = lo[r]; k < hi[r]; ++k) {
+				const double p = A_AT(k, r) * A_AT(k, (unsigned)c);
+				a = a + p;
+			}
+			acc[t] = a;
+		}
+		pl[r] = acc[0];
+		pd[r] = acc[1];
+		pu[r] = acc[2];
+		if (hi[r] - lo[r] > row_size)
+			row_size = (unsigned)(hi[r] - lo[r]);
+	}
+	/* tridiagonal LU (bilinear.cpp:20-57) */
+	double *c = calloc(N, sizeof(double)), *l = calloc(N, sizeof(double)), *u = calloc(N, sizeof(double));
+	const double eps = DBL_EPSILON;
+	if (N == 1) {
+		l[0] = pd[0];
+	} else {
+		c[0] = 0.0;
+		l[0] = pd[0];
+		u[0] = pu[0] / (pd[0] + eps);
+		for (unsigned i = 1; i + 1 < N; ++i) {
+			c[i] = pl[i];
+			l[i] = pd[i] - c[i] * u[i - 1];
+			u[i] = pu[i] / (l[i] + eps);
+		}
+		c[N - 1] = pl[N - 1];
+		l[N - 1] = pd[N - 1] - c[N - 1] * u[N - 2];
+		u[N - 1] = 0.0;
+	}
+	ctx->up = M;
+	ctx->orig = N;
+	ctx->row_size = row_size;
+	ctx->coef = calloc((size_t)N * (row_size ? row_size : 1), sizeof(float));
+	ctx->offset = calloc(N, sizeof(unsigned));
+	ctx->lu_c = malloc(sizeof(float) * N);
+	ctx->lu_l = malloc(sizeof(float) * N);
+	ctx->lu_u = malloc(sizeof(float) * N);
+	for (unsigned r = 0; r < N; ++r) {
+		size_t left = lo[r] < (size_t)M - row_size ? lo[r] : (size_t)M - row_size;
+		if (hi[r] == 0)
+			left = 0;
+		for (size_t j = 0; hi[r] && left + j < hi[r]; ++j)
+			ctx->coef[(size_t)r * row_size + j] = (float)A_AT(left + j, r);
+		ctx->offset[r] = (unsigned)left;
+		ctx->lu_c[r] = (float)c[r];
+		ctx->lu_l[r] = (float)(1.0 / (l[r] + eps));
+		ctx->lu_u[r] = (float)u[r];
+	}
+#undef A_AT
+	free(acol); free(aw); free(an); free(lo); free(hi);
+	free(pl); free(pd); free(pu); free(c); free(l); free(u);
+	return 0;
+}
+
+/* One horizontal pass (unresize_line_h_f32_c, unresize_impl.cpp:27-58) over h
+ * lines, or one vertical pass (unresize_line_forward/back_v_f32_c,
+ * unresize_impl.cpp:60-97) over w columns. Products and sums are rounded
+ * one by one (no fused multiply-add). */
+static void unresize_pass(const orc_unresize_ctx *x, int horizontal, unsigned w, unsigned h, const float *src,
+                          ptrdiff_t ss, float *dst, ptrdiff_t ds)
+{
+	const ptrdiff_t sse = ss / 4, dse = ds / 4;
+	if (horizontal) {
+		for (unsigned i = 0; i < h; ++i) {
+			const float *s = src + i * sse;
+			float *d = dst + i * dse;
+			float z = 0.0f, wv = 0.0f;
+			for (unsigned j = 0; j < x->orig; ++j) {
+				float accum = 0.0f;
+				for (unsigned k = 0; k < x->row_size; ++k) {
+					const float p = x->coef[(size_t)j * x->row_size + k] * s[x->offset[j] + k];
+					accum = accum + p;
+				}
+				const float cz = x->lu_c[j] * z;
+				z = (accum - cz) * x->lu_l[j];
+				d[j] = z;
+			}
+			for (unsigned j = x->orig; j != 0; --j) {
+				const float uw = x->lu_u[j - 1] * wv;
+				wv = d[j - 1] - uw;
+				d[j - 1] = wv;
+			}
+		}
+	} else {
+		for (unsigned j = 0; j < w; ++j) {
+			float z = 0.0f;
+			for (unsigned i = 0; i < x->orig; ++i) {
+				float accum = 0.0f;
+				for (unsigned k = 0; k < x->row_size; ++k) {
+					const float p = x->coef[(size_t)i * x->row_size + k] * src[(x->offset[i] + k) * sse + j];
+					accum = accum + p;
+				}
+				const float cz = x->lu_c[i] * z;
+				z = (accum - cz) * x->lu_l[i];
+				dst[i * dse + j] = z;
+			}
+			float wv = 0.0f;
+			for (unsigned i = x->orig; i != 0; --i) {
+				const float uw = x->lu_u[i - 1] * wv;
+				wv = dst[(i - 1) * dse + j] - uw;
+				dst[(i - 1) * dse + j] = wv;
+			}
+		}
+	}
+}
+
+/* unresize_h_first (unresize.cpp:14-19) */
+int orc_unresize_h_first(double xscale, double yscale)
+{
+	const double h = (xscale > 1.0 ? xscale : 1.0) * 2.0 + xscale * (yscale > 1.0 ? yscale : 1.0);
+	const double v = (yscale > 1.0 ? yscale : 1.0) + yscale * (xscale > 1.0 ? xscale : 1.0) * 2.0;
+	return h < v;
+}
+
+/* UnresizeConversion on one FLOAT plane (unresize.cpp:34-91): zero, one or
+ * two passes; 0, or -2 for an upscale. */
+int orc_unresize_plane(unsigned up_w, unsigned up_h, unsigned orig_w, unsigned orig_h, double shift_w,
+                       double shift_h, const float *src, ptrdiff_t ss, float *dst, ptrdiff_t ds)
+{
+	const int skip_h = up_w == orig_w && shift_w == 0.0;
+	const int skip_v = up_h == orig_h && shift_h == 0.0;
+	if (orig_w > up_w || orig_h > up_h)
+		return -2;
+	if (skip_h && skip_v) {
+		for (unsigned i = 0; i < up_h; ++i)
+			memcpy((char *)dst + i * ds, (const char *)src + i * ss, (size_t)up_w * 4);
+		return 0;
+	}
+	orc_unresize_ctx cw, ch;
+	memset(&cw, 0, sizeof(cw));
+	memset(&ch, 0, sizeof(ch));
+	if (!skip_h && orc_unresize_context(orig_w, up_w, shift_w, &cw))
+		return -2;
+	if (!skip_v && orc_unresize_context(orig_h, up_h, shift_h, &ch)) {
+		orc_unresize_ctx_free(&cw);
+		return -2;
+	}
+	if (skip_h) {
+		unresize_pass(&ch, 0, up_w, up_h, src, ss, dst, ds);
+	} else if (skip_v) {
+		unresize_pass(&cw, 1, up_w, up_h, src, ss, dst, ds);
+	} else if (orc_unresize_h_first((double)orig_w / up_w, (double)orig_h / up_h)) {
+		float *t = malloc(sizeof(float) * (size_t)orig_w * up_h);
+		unresize_pass(&cw, 1, up_w, up_h, src, ss, t, (ptrdiff_t)orig_w * 4);
+		unresize_pass(&ch, 0, orig_w, up_h, t, (ptrdiff_t)orig_w * 4, dst, ds);
+		free(t);
+	} else {
+		float *t = malloc(sizeof(float) * (size_t)up_w * orig_h);
+		unresize_pass(&ch, 0, up_w, up_h, src, ss, t, (ptrdiff_t)up_w * 4);
+		unresize_pass(&cw, 1, up_w, orig_h, t, (ptrdiff_t)up_w * 4, dst, ds);
+		free(t);
+	}
+	orc_unresize_ctx_free(&cw);
+	orc_unresize_ctx_free(&ch);
+	return 0;
+}

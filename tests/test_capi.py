@@ -126,3 +126,15 @@ def test_depth_create_errors(lib):
     p = capi.DepthParams(0, 32, capi.PixelFormat(1, 10, 0, 0, 0), capi.PixelFormat(0, 8, 0, 0, 0), 0, 0)
     h = C.c_void_p()
     assert lib.zg_depth_create(C.byref(p), C.byref(h)) == 2050  # INVALID_IMAGE_SIZE
+
+
+def test_unresize_create_errors(lib):
+    """zg_unresize_create refuses an upscale, as zimg's context builder does
+    (bilinear.cpp:109-110), before touching a device."""
+    import ctypes as C
+    from zimg_gb300 import capi
+    h = C.c_void_p()
+    p = capi.UnresizeParams(64, 48, 96, 24, 0.0, 0.0)
+    assert lib.zg_unresize_create(C.byref(p), C.byref(h)) == 3076  # RESAMPLING_NOT_AVAILABLE
+    p = capi.UnresizeParams(64, 48, 0, 24, 0.0, 0.0)
+    assert lib.zg_unresize_create(C.byref(p), C.byref(h)) == 2050  # INVALID_IMAGE_SIZE

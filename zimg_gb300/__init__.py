@@ -6,7 +6,7 @@ include/zimg_gb300.h. This package is a thin Python mirror of that ABI.
 """
 from .capi import ZimgError, load  # noqa: F401
 from .resize import (Batch, Depth, DepthConversion, FilterContext, Graph, HostPipeline, Resize,  # noqa: F401
-                     ResizeConversion,
+                     ResizeConversion, Unresize, UnresizeConversion,
                      ResizeImplBuilder, ResizePass, compute_filter, filter_id, graph_params, image_format)
 
 __version__ = "0.1.0"

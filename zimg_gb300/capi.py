@@ -62,6 +62,11 @@ class DepthParams(C.Structure):
 DITHER = {"none": 0, "ordered": 1, "random": 2, "error_diffusion": 3}
 
 
+class UnresizeParams(C.Structure):
+    _fields_ = [("up_width", C.c_uint), ("up_height", C.c_uint), ("orig_width", C.c_uint),
+                ("orig_height", C.c_uint), ("shift_w", C.c_double), ("shift_h", C.c_double)]
+
+
 class BatchIO(C.Structure):
     _fields_ = [("src", C.c_void_p), ("src_stride", C.c_ssize_t), ("dst", C.c_void_p), ("dst_stride", C.c_ssize_t)]
 
@@ -103,6 +108,11 @@ _P = C.c_void_p
 SIGNATURES = [
     ("zg_get_last_error", C.c_int, [C.c_char_p, C.c_size_t]),
     ("zg_pipeline_status", C.c_int, [C.c_int]),
+    ("zg_unresize_create", C.c_int, [C.POINTER(UnresizeParams), C.POINTER(C.c_void_p)]),
+    ("zg_unresize_free", None, [C.c_void_p]),
+    ("zg_unresize_get_tmp_size", C.c_int, [C.c_void_p, C.POINTER(C.c_size_t)]),
+    ("zg_unresize_process", C.c_int, [C.c_void_p, C.c_void_p, C.c_ssize_t, C.c_void_p, C.c_ssize_t, C.c_void_p,
+                                      C.c_void_p]),
     ("zg_depth_create", C.c_int, [C.POINTER(DepthParams), C.POINTER(C.c_void_p)]),
     ("zg_depth_free", None, [C.c_void_p]),
     ("zg_depth_get_info", C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),

@@ -7,6 +7,7 @@ Names and argument meaning follow the reference:
 * ``compute_filter``   — src/zimg/resize/filter.h:178 (host-side tap tables)
 * ``Batch``            — many conversions in one persistent launch
 * ``DepthConversion``  — src/zimg/depth/depth.h:29-53 (pixel type / depth / range)
+* ``UnresizeConversion`` — src/zimg/unresize/unresize.h:96-114 (inverse bilinear)
 * ``Graph``            — zimg_filter_graph_build/process: resize, with the depth
                          conversions zimg's graph puts around it
 
@@ -26,7 +27,7 @@ from . import capi
 from .capi import ZimgError, check, load
 
 __all__ = ["ZimgError", "compute_filter", "FilterContext", "ResizeImplBuilder", "ResizePass", "ResizeConversion",
-           "Resize", "Batch", "Graph", "DepthConversion", "Depth", "filter_id"]
+           "Resize", "Batch", "Graph", "DepthConversion", "Depth", "UnresizeConversion", "Unresize", "filter_id"]
 
 
 def filter_id(kind) -> int:
@@ -301,6 +302,55 @@ class DepthConversion(_Builder):
         h = C.c_void_p()
         check(load().zg_depth_create(C.byref(p), C.byref(h)))
         return Depth(h.value, p)
+
+
+class Unresize:
+    """The created unresize (zimg's UnresizeConversion::create result)."""
+
+    def __init__(self, handle, params: capi.UnresizeParams):
+        self._h = handle
+        self.params = params
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            load().zg_unresize_free(self._h)
+            self._h = None
+
+    @property
+    def tmp_size(self) -> int:
+        n = C.c_size_t()
+        check(load().zg_unresize_get_tmp_size(self._h, C.byref(n)))
+        return n.value
+
+    def process(self, src, dst, tmp=None, stream=None) -> None:
+        sp, ss, _, _ = _plane(src)
+        dp, ds, _, _ = _plane(dst)
+        if tmp is None and self.tmp_size:
+            import torch
+            tmp = torch.empty(self.tmp_size, dtype=torch.uint8, device=src.device)
+        tp = tmp.data_ptr() if tmp is not None else None
+        check(load().zg_unresize_process(self._h, sp, ss, dp, ds, tp, _stream_handle(stream)))
+
+
+class UnresizeConversion(_Builder):
+    """UnresizeConversion{up_width, up_height, FLOAT} (src/zimg/unresize/unresize.h:96-114)."""
+
+    def __init__(self, up_width: int, up_height: int):
+        self.up_width, self.up_height = up_width, up_height
+        self.orig_width, self.orig_height = up_width, up_height
+        self.shift_w = self.shift_h = 0.0
+
+    def set_orig_width(self, v: int): return self._set("orig_width", int(v))
+    def set_orig_height(self, v: int): return self._set("orig_height", int(v))
+    def set_shift_w(self, v: float): return self._set("shift_w", float(v))
+    def set_shift_h(self, v: float): return self._set("shift_h", float(v))
+
+    def create(self) -> Unresize:
+        p = capi.UnresizeParams(self.up_width, self.up_height, self.orig_width, self.orig_height, self.shift_w,
+                                self.shift_h)
+        h = C.c_void_p()
+        check(load().zg_unresize_create(C.byref(p), C.byref(h)))
+        return Unresize(h.value, p)
 
 
 class Batch:
