@@ -76,7 +76,10 @@ typedef enum zg_resample_filter {
 	ZG_RESIZE_SPLINE16 = 3,
 	ZG_RESIZE_SPLINE36 = 4,
 	ZG_RESIZE_SPLINE64 = 6,
-	ZG_RESIZE_LANCZOS = 5
+	ZG_RESIZE_LANCZOS = 5,
+	/* zimg's internal value (zimg.cpp:21): the graph unresizes instead
+	 * (graphbuilder.cpp:753-800); only zg_graph_build accepts it */
+	ZG_RESIZE_UNRESIZE = -1
 } zg_resample_filter;
 
 /* Arithmetic the planner may pick for a pass (see zg_resize_params.engine). */

@@ -497,6 +497,11 @@ def graph_plane_chain(o: "Oracle", src: np.ndarray, fs: PixelFormat, fd: PixelFo
     if rp is None:
         return o.depth_convert(src, fs, fd, dither, plane)
     h, w = src.shape
+    if kind == "unresize":  # FLOAT working format (graphbuilder.cpp:722-723,780-790)
+        fr = PixelFormat("float")
+        x = src if o.depth_mode(fs, fr, dither) == 0 else o.depth_convert(src, fs, fr, dither, plane)
+        y = o.unresize_plane(x, rp["dst_w"], rp["dst_h"], rp["shift_w"], rp["shift_h"])
+        return y if o.depth_mode(fr, fd, dither) == 0 else o.depth_convert(y, fr, fd, dither, plane)
     fr = resize_format(fs, fd, float(w * h), float(rp["dst_w"] * rp["dst_h"]))
     x = src if o.depth_mode(fs, fr, dither) == 0 else o.depth_convert(src, fs, fr, dither, plane)
     y = o.resize_plane(x.astype(fr.dtype), rp["dst_w"], rp["dst_h"], kind, a, b,

@@ -158,3 +158,63 @@ def test_graph_depth_around_resize(cuda, oracle, case):
         got = to_host(dsts[p], O.PixelFormat(dt, dd).dtype)
         np.testing.assert_array_equal(got.view(np.uint8), wants[p].view(np.uint8),
                                       err_msg=f"{GRAPH_CASES[case]} plane {p}")
+
+
+UNRESIZE_GRAPH_CASES = [
+    # (src type, depth, range, dst type, depth, range, size in, size out, color, dither)
+    ("float", 32, 0, "float", 32, 0, (1280, 720), (960, 540), 0, "none"),   # FLOAT in and out
+    ("word", 10, 0, "word", 10, 0, (1920, 1080), (1280, 720), 2, "none"),   # to FLOAT, unresize, back to WORD
+    ("byte", 8, 0, "byte", 8, 0, (960, 540), (640, 360), 1, "ordered"),    # RGB BYTE, dithered back
+]
+
+
+@pytest.mark.parametrize("case", range(len(UNRESIZE_GRAPH_CASES)))
+def test_graph_unresize(cuda, oracle, case):
+    """zimg's graph with resample_filter ZIMG_RESIZE_UNRESIZE (zimg.cpp:21,450;
+    graphbuilder.cpp:761-790): every plane converted to FLOAT, unresized to
+    the output size, converted to the output format; equal to the oracle's
+    chain bit for bit."""
+    import torch
+    import zimg_gb300 as zg
+    from oracle import oracle as O
+    st, sd, sr, dt, dd, dr, (sw, sh), (dw, dh), color, dither = UNRESIZE_GRAPH_CASES[case]
+    sub = 1 if color == 2 else 0
+    sfmt = zg.image_format(sw, sh, st, depth=sd, pixel_range=sr, color_family=color, subsample_w=sub,
+                           subsample_h=sub, chroma_location=0)
+    dfmt = zg.image_format(dw, dh, dt, depth=dd, pixel_range=dr, color_family=color, subsample_w=sub,
+                           subsample_h=sub, chroma_location=0)
+    g = zg.Graph(sfmt, dfmt, zg.graph_params(resample_filter="unresize", dither_type={"none": 0, "ordered": 1}[dither]))
+    rng = np.random.default_rng(650 + case)
+    nplanes = 1 if color == 0 else 3
+    cname = ["grey", "rgb", "yuv"][color]
+    sgeo = O.plane_geometry(dict(width=sw, height=sh, subsample_w=sub, subsample_h=sub, color=cname, chroma_location=0))
+    dgeo = O.plane_geometry(dict(width=dw, height=dh, subsample_w=sub, subsample_h=sub, color=cname, chroma_location=0))
+    srcs, dsts, wants = [], [], []
+    for p in range(nplanes):
+        uv = color == 2 and p > 0
+        fs = O.PixelFormat(st, sd, bool(sr), uv)
+        fd = O.PixelFormat(dt, dd, bool(dr), uv)
+        src = make_src(rng, fs, sgeo[p]["height"], sgeo[p]["width"], special=False)
+        srcs.append(src)
+        dsts.append(empty(dgeo[p]["height"], dgeo[p]["width"], dt))
+        rp = O.resize_params(sgeo[p], dgeo[p])
+        wants.append(O.graph_plane_chain(oracle, src, fs, fd, rp, "unresize", dither=dither, plane=p))
+    g.process([to_dev(s) for s in srcs] + [None] * (4 - nplanes), dsts + [None] * (4 - nplanes))
+    torch.cuda.synchronize()
+    for p in range(nplanes):
+        got = to_host(dsts[p], O.PixelFormat(dt, dd).dtype)
+        np.testing.assert_array_equal(got.view(np.uint8), wants[p].view(np.uint8),
+                                      err_msg=f"{UNRESIZE_GRAPH_CASES[case]} plane {p}")
+
+
+def test_graph_unresize_refusals(cuda):
+    """A partial active region (graphbuilder.cpp:761-766) and a larger output
+    (bilinear.cpp:109-110) are RESAMPLING_NOT_AVAILABLE."""
+    import zimg_gb300 as zg
+    params = zg.graph_params(resample_filter="unresize")
+    cases = [(zg.image_format(640, 360, "float", active_region=(0.5, 0.0, 600.0, 360.0)), zg.image_format(320, 180, "float")),
+             (zg.image_format(640, 360, "float"), zg.image_format(960, 180, "float"))]
+    for s, d in cases:
+        with pytest.raises(zg.ZimgError) as e:
+            zg.Graph(s, d, params)
+        assert e.value.code == 3076

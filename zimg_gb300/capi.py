@@ -16,6 +16,7 @@ LIB_PATH = os.path.join(_PKG, "_lib", "libzimg_gb300.so")
 PIXEL = {"byte": 0, "word": 1, "half": 2, "float": 3}
 FILTER = {"point": 0, "bilinear": 1, "bicubic": 2, "spline16": 3, "spline36": 4, "lanczos": 5, "spline64": 6}
 ENGINE = {"auto": 0, "cuda": 1, "tensor": 2}
+RESIZE_UNRESIZE = -1  # graph only: unresize instead of resize (zimg.cpp:21)
 
 ERROR_NAMES = {
     -1: "UNKNOWN", 0: "SUCCESS", 1: "OUT_OF_MEMORY", 2: "USER_CALLBACK_FAILED", 1024: "LOGIC",

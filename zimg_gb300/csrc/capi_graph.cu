@@ -278,6 +278,7 @@ struct zg_graph {
 		unsigned in_bytes = 0, out_bytes = 0;
 		zg_resize_params params{};
 		zg_resize *resize = nullptr;
+		zg_unresize *unresize = nullptr;  // instead of resize when the filter is ZG_RESIZE_UNRESIZE
 		// depth conversions around resize (graphbuilder.cpp:943-950): into
 		// the resize format before, to the output format after; their
 		// planes live in tmp (pre at 0, mid next, resize scratch last)
@@ -291,6 +292,7 @@ struct zg_graph {
 	{
 		for (auto &p : planes) {
 			zg_resize_free(p.resize);
+			zg_unresize_free(p.unresize);
 			zg_depth_free(p.pre);
 			zg_depth_free(p.post);
 			zg_depth_free(p.only);
@@ -424,8 +426,13 @@ zg_graph *zg_graph_build(const zg_image_format *src_format, const zg_image_forma
 			gpl.mode = 2;
 			const double scale_w = dp.aw / sp.aw;
 			const double scale_h = dp.ah / sp.ah;
-			const PixFmt fr = choose_resize_format(fs, fd, static_cast<double>(sp.width) * sp.height,
-			                                       static_cast<double>(dp.width) * dp.height);
+			const bool unresize = gp.resample_filter == ZG_RESIZE_UNRESIZE;
+			if (unresize && (sp.aw != sp.width || sp.ah != sp.height || dp.aw != dp.width || dp.ah != dp.height))
+				throw Error(kErrResamplingNotAvailable, "unresize not supported for given subregion");
+			// unresize works in FLOAT (choose_resize_format, graphbuilder.cpp:722-723)
+			const PixFmt fr = unresize ? PixFmt{ ZG_PIXEL_FLOAT, 32, false, false }
+			                           : choose_resize_format(fs, fd, static_cast<double>(sp.width) * sp.height,
+			                                                  static_cast<double>(dp.width) * dp.height);
 			zg_resize_params rp;
 			zg_resize_params_default(&rp);
 			rp.src_width = sp.width;
@@ -442,14 +449,23 @@ zg_graph *zg_graph_build(const zg_image_format *src_format, const zg_image_forma
 			rp.subwidth = sp.aw * (dp.width / dp.aw);
 			rp.subheight = sp.ah * (dp.height / dp.ah);
 			gpl.params = rp;
-			zg_error_code rc = zg_resize_create(&rp, &gpl.resize);
+			size_t rtmp = 0;
+			zg_error_code rc;
+			if (unresize) {
+				const zg_unresize_params up{ sp.width, sp.height, dp.width, dp.height, rp.shift_w, rp.shift_h };
+				rc = zg_unresize_create(&up, &gpl.unresize);
+				if (rc == ZG_ERROR_SUCCESS)
+					zg_unresize_get_tmp_size(gpl.unresize, &rtmp);
+			} else {
+				rc = zg_resize_create(&rp, &gpl.resize);
+				if (rc == ZG_ERROR_SUCCESS)
+					zg_resize_get_tmp_size(gpl.resize, &rtmp);
+			}
 			if (rc != ZG_ERROR_SUCCESS) {
 				char msg[256];
 				zg_get_last_error(msg, sizeof(msg));
 				throw Error(rc, msg);
 			}
-			size_t rtmp = 0;
-			zg_resize_get_tmp_size(gpl.resize, &rtmp);
 			size_t off = 0;
 			if (!fmt_equal(fs, fr)) {
 				gpl.pre = make_depth(sp.width, sp.height, fs, fr, dither, p);
@@ -540,7 +556,9 @@ zg_error_code zg_graph_process(const zg_graph *g, const zg_image_buffer_const *s
 			}
 			void *rd = pl.post ? static_cast<void *>(t + pl.off_mid) : static_cast<void *>(dp);
 			const ptrdiff_t rds = pl.post ? static_cast<ptrdiff_t>(pl.mid_pitch) : dst->plane[p].stride;
-			zg_error_code rc = zg_resize_process(pl.resize, rs, rss, rd, rds, t ? t + pl.off_tmp : nullptr, stream);
+			zg_error_code rc = pl.unresize
+			                       ? zg_unresize_process(pl.unresize, rs, rss, rd, rds, t ? t + pl.off_tmp : nullptr, stream)
+			                       : zg_resize_process(pl.resize, rs, rss, rd, rds, t ? t + pl.off_tmp : nullptr, stream);
 			if (rc != ZG_ERROR_SUCCESS) {
 				char msg[256];
 				zg_get_last_error(msg, sizeof(msg));

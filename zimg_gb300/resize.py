@@ -483,7 +483,9 @@ def graph_params(**kw) -> capi.GraphBuilderParams:
     p = capi.GraphBuilderParams()
     load().zg_graph_builder_params_default(C.byref(p), capi.API_VERSION_2_4)
     for k, v in kw.items():
-        if k in ("resample_filter", "resample_filter_uv"):
+        if k == "resample_filter" and v == "unresize":
+            v = capi.RESIZE_UNRESIZE
+        elif k in ("resample_filter", "resample_filter_uv"):
             v = filter_id(v)
         setattr(p, k, v)
     return p
