@@ -88,16 +88,32 @@ void DevicePass::set_tensor()
 	int ksteps = 0;
 	build_wide_tables(table.f32.data(), table.left.data(), table.width, table.rows, horizontal, &frag, &kbase,
 	                  &ksteps);
+	std::vector<uint4> uchunk;
+	std::vector<int> ubegin, ukbase;
+	build_umma_tables(table.f32.data(), table.left.data(), table.width, table.rows, horizontal, &uchunk, &ubegin,
+	                  &ukbase);
 	const size_t fbytes = frag.size() * sizeof(uint4);
 	const size_t kbytes = kbase.size() * sizeof(int);
-	wide_storage.reset(fbytes + kbytes);
+	const size_t ubytes = uchunk.size() * sizeof(uint4);
+	const size_t bbytes = ubegin.size() * sizeof(int);
+	const size_t off_k = fbytes, off_u = (off_k + kbytes + 15) & ~size_t(15), off_b = off_u + ubytes,
+	             off_uk = off_b + bbytes;
+	wide_storage.reset(off_uk + ukbase.size() * sizeof(int));
 	unsigned char *base = static_cast<unsigned char *>(wide_storage.get());
 	cuda_check(cudaMemcpy(base, frag.data(), fbytes, cudaMemcpyHostToDevice), "upload band fragments");
-	cuda_check(cudaMemcpy(base + fbytes, kbase.data(), kbytes, cudaMemcpyHostToDevice), "upload band fragments");
+	cuda_check(cudaMemcpy(base + off_k, kbase.data(), kbytes, cudaMemcpyHostToDevice), "upload band fragments");
+	cuda_check(cudaMemcpy(base + off_u, uchunk.data(), ubytes, cudaMemcpyHostToDevice), "upload band chunks");
+	cuda_check(cudaMemcpy(base + off_b, ubegin.data(), bbytes, cudaMemcpyHostToDevice), "upload band chunks");
+	cuda_check(cudaMemcpy(base + off_uk, ukbase.data(), ukbase.size() * sizeof(int), cudaMemcpyHostToDevice),
+	           "upload band chunks");
 	wide.frag = reinterpret_cast<const uint4 *>(base);
-	wide.kbase = reinterpret_cast<const int *>(base + fbytes);
+	wide.kbase = reinterpret_cast<const int *>(base + off_k);
 	wide.groups = static_cast<int>(kbase.size());
 	wide.ksteps = ksteps;
+	wide.uchunk = reinterpret_cast<const uint4 *>(base + off_u);
+	wide.uchunk_begin = reinterpret_cast<const int *>(base + off_b);
+	wide.ukbase = reinterpret_cast<const int *>(base + off_uk);
+	wide.ugroups = static_cast<int>(ukbase.size());
 }
 
 std::unique_ptr<DevicePass> make_device_pass(const PassSpec &s)
@@ -172,7 +188,9 @@ extern "C" {
 
 int zg_pipeline_status(int reset)
 {
-	return chain_tma_pipeline_error(reset != 0);
+	const int chain = chain_tma_pipeline_error(reset != 0);
+	const int wide = wide_umma_pipeline_error(reset != 0);
+	return chain ? chain : wide;
 }
 
 zg_error_code zg_get_last_error(char *err_msg, size_t n)

@@ -132,6 +132,21 @@ bool chain_tma_layout(const FusedPlan *const *plans, int n, SmemLayout *out)
 	return static_cast<size_t>(L.total_bytes) <= kTmaSmemMax;
 }
 
+bool encode_tensor_map_2d(CUtensorMap *map, CUtensorMapDataType type, const void *base, uint64_t width,
+                          uint64_t height, uint64_t stride, uint32_t box_w, uint32_t box_h, bool swizzle128)
+{
+	EncodeTiled fn = encoder();
+	if (!fn || !base || reinterpret_cast<uintptr_t>(base) % 16 || stride % 16 || !width || !height)
+		return false;
+	const cuuint64_t dims[2] = { width, height };
+	const cuuint64_t strides[1] = { stride };
+	const cuuint32_t box[2] = { box_w, box_h };
+	const cuuint32_t estr[2] = { 1, 1 };
+	return fn(map, type, 2, const_cast<void *>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+	          swizzle128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+	          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 bool chain_tma_source_map(CUtensorMap *map, const FusedJob &j, const SmemLayout &L)
 {
 	const uintptr_t a = reinterpret_cast<uintptr_t>(j.src);

@@ -26,6 +26,7 @@
 // a group's block reaches the group's other outputs as NaN.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 
 #include "kernels.h"
@@ -36,13 +37,6 @@ namespace {
 
 constexpr int kWideWarps = 4;
 
-__device__ __forceinline__ uint32_t tf32_rna(float x)
-{
-	uint32_t r;
-	asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-	return r;
-}
-
 __device__ __forceinline__ void mma_tf32(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
                                          uint32_t b0, uint32_t b1)
 {
@@ -50,6 +44,13 @@ __device__ __forceinline__ void mma_tf32(float (&d)[4], uint32_t a0, uint32_t a1
 	             "{%8, %9}, {%0, %1, %2, %3};\n"
 	             : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
 	             : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ uint32_t tf32_rna(float x)
+{
+	uint32_t r;
+	asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+	return r;
 }
 
 // One k-step: 4 samples of this lane -> split -> three products.
@@ -345,7 +346,72 @@ void build_wide_tables(const float *f32, const unsigned *left, unsigned width, u
 	}
 }
 
+void build_umma_tables(const float *f32, const unsigned *left, unsigned width, unsigned rows, bool horizontal,
+                       std::vector<uint4> *chunks, std::vector<int> *chunk_begin, std::vector<int> *kbase)
+{
+	constexpr unsigned kN = 16, kKC = 32;
+	const unsigned groups = (rows + kN - 1) / kN;
+	chunk_begin->assign(groups + 1, 0);
+	kbase->assign(groups, 0);
+	int total = 0;
+	for (unsigned g = 0; g < groups; ++g) {
+		unsigned lo = ~0u, hi = 0;
+		for (unsigned o = g * kN; o < std::min(rows, (g + 1) * kN); ++o) {
+			lo = std::min(lo, left[o]);
+			hi = std::max(hi, left[o] + width);
+		}
+		if (horizontal)
+			lo &= ~3u;  // tensor copies start on 16-byte boundaries
+		(*kbase)[g] = static_cast<int>(lo);
+		(*chunk_begin)[g] = total;
+		total += static_cast<int>((hi - lo + kKC - 1) / kKC);
+	}
+	(*chunk_begin)[groups] = total;
+	// per chunk 1024 words: taps hi [16 outputs x 32 inputs] then lo, each in
+	// the K-major core-matrix layout (output / 8) * 128 + (input / 4) * 256 +
+	// (output % 8) * 16 + (input % 4) * 4 bytes
+	chunks->assign(static_cast<size_t>(total) * 256, uint4{ 0, 0, 0, 0 });
+	uint32_t *w32 = reinterpret_cast<uint32_t *>(chunks->data());
+	for (unsigned g = 0; g < groups; ++g) {
+		const int nc = (*chunk_begin)[g + 1] - (*chunk_begin)[g];
+		for (int c = 0; c < nc; ++c) {
+			uint32_t *blk = w32 + static_cast<size_t>((*chunk_begin)[g] + c) * 1024;
+			for (unsigned n = 0; n < kN; ++n) {
+				const unsigned o = g * kN + n;
+				if (o >= rows)
+					continue;
+				for (unsigned kk = 0; kk < kKC; ++kk) {
+					const long x = (*kbase)[g] + static_cast<long>(kKC) * c + kk;
+					const long k = x - static_cast<long>(left[o]);
+					if (k < 0 || k >= static_cast<long>(width))
+						continue;
+					const float t = f32[static_cast<size_t>(o) * width + k];
+					const float h = tf32_round(t);
+					const unsigned off = ((n >> 3) * 128 + (kk >> 2) * 256 + (n & 7) * 16 + (kk & 3) * 4) / 4;
+					blk[off] = bits(h);
+					blk[512 + off] = bits(tf32_round(t - h));
+				}
+			}
+		}
+	}
+}
+
 namespace {
+
+// ZG_WIDE_KERNEL=umma puts every eligible wide pass on the tcgen05 form
+// (wide_umma.cu); otherwise they run on the mma.sync form, which is faster
+// for these bands: a tcgen05.mma of M = 128, K = 8 (tf32) measured about 200
+// cycles whatever its N, and a band gives only ~10 useful outputs per
+// 8-input step, where the mma.sync form reached 0.5 m16n8k8 per clock.
+int wide_kernel_choice()
+{
+	const char *e = std::getenv("ZG_WIDE_KERNEL");
+	if (e && std::strcmp(e, "mma") == 0)
+		return 1;
+	if (e && std::strcmp(e, "umma") == 0)
+		return 2;
+	return 0;
+}
 
 template <int KSPLIT, bool HORIZ, bool PAIR>
 void launch_tiles(const PassLaunch &l, int m_extent, int src_dim, int dst_dim, ptrdiff_t sm, ptrdiff_t sk, ptrdiff_t dm,
@@ -383,6 +449,11 @@ void launch_pass_tiles(const PassLaunch &l, int m_extent, int src_dim, int dst_d
 
 cudaError_t launch_wide(const PassLaunch &l, cudaStream_t stream)
 {
+	if (l.wide.uchunk && wide_kernel_choice() == 2) {
+		const cudaError_t e = launch_wide_umma(l, stream);
+		if (e != cudaErrorNotSupported)
+			return e;
+	}
 	const int m_extent = static_cast<int>(l.lines);
 	const int src_dim = static_cast<int>(l.t.input_width);
 	const int dst_dim = static_cast<int>(l.t.rows);
