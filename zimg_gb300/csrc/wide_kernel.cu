@@ -78,6 +78,30 @@ __device__ __forceinline__ void add4(float (&d)[4], const float (&c)[4])
 	d[3] += c[3];
 }
 
+// Ask L2 for the source rows of k-steps [s, s + 4) of this warp's tile (pf:
+// the tile's first line; PERM_K: lines m0 + lane % 16 from input kb + 8 s,
+// both 64-byte halves of the 128 bytes; otherwise inputs kb + 8 s + lane,
+// the tile's 64 bytes of columns): one instruction per 4 k-steps.
+template <bool PERM_K>
+__device__ __forceinline__ void prefetch4(const char *pf, int kb, int s, int src_dim, int m_left, ptrdiff_t sm,
+                                          ptrdiff_t sk)
+{
+	const int lane = threadIdx.x & 31;
+	const char *a;
+	if (PERM_K) {
+		if ((lane & 15) >= m_left || kb + 8 * s + 16 * (lane >> 4) >= src_dim)
+			return;
+		a = pf + (lane & 15) * sm + static_cast<ptrdiff_t>(kb + 8 * s) * sk + (lane >> 4) * 64;
+	} else {
+		if (kb + 8 * s + lane >= src_dim)
+			return;
+		a = pf + static_cast<ptrdiff_t>(kb + 8 * s + lane) * sk;
+	}
+	asm volatile("prefetch.global.L2 [%0];\n" ::"l"(a));
+}
+
+constexpr int kPrefetchSteps = 16;  // k-steps between a prefetch and the loads it serves
+
 // k-steps [s0, s1) of output group g for this lane's rows/columns ma, mb:
 // d += sum of the 3xTF32 products. Element (m, k) of the input is at
 // src + m * sm + k * sk (bytes).
@@ -89,9 +113,12 @@ __device__ __forceinline__ void add4(float (&d)[4], const float (&c)[4])
 // PAIR: the lane's two samples of a k-step lie 4 bytes apart (ma, mb adjacent
 // columns in a vertical pass, or the PERM_K pair) and the plane is 8-byte
 // aligned: one 8-byte load each.
+// pf, m_left (lines from the tile's first to the plane's end), sm: the
+// prefetch of the rows kPrefetchSteps ahead (prefetch4).
 template <bool PERM_K, bool PAIR>
 __device__ __forceinline__ void band_sum(float (&d)[4], const WideTables &w, int g, int s0, int s1, int src_dim,
-                                         const char *base_a, const char *base_b, ptrdiff_t sk)
+                                         const char *base_a, const char *base_b, ptrdiff_t sk, const char *pf,
+                                         int m_left, ptrdiff_t sm)
 {
 	const int lane = threadIdx.x & 31, tig = lane & 3;
 	const int kb = __ldg(w.kbase + g);
@@ -146,6 +173,7 @@ __device__ __forceinline__ void band_sum(float (&d)[4], const WideTables &w, int
 			load4(xa, ba, s);
 			for (;;) {
 				const bool has_b = s + 8 <= s1;
+				prefetch4<PERM_K>(pf, kb, s + kPrefetchSteps, src_dim, m_left, sm, sk);
 				if (has_b)
 					load4(xb, bb, s + 4);
 				run4(xa, ba);
@@ -153,6 +181,7 @@ __device__ __forceinline__ void band_sum(float (&d)[4], const WideTables &w, int
 				if (!has_b)
 					break;
 				const bool has_a = s + 8 <= s1;
+				prefetch4<PERM_K>(pf, kb, s + kPrefetchSteps, src_dim, m_left, sm, sk);
 				if (has_a)
 					load4(xa, ba, s + 4);
 				run4(xb, bb);
@@ -243,7 +272,7 @@ wide_tc_kernel(WideTables w, int m_extent, int src_dim, int dst_dim, const char 
 		float d[4] = { 0.f, 0.f, 0.f, 0.f };
 		const int per = (KS + KSPLIT - 1) / KSPLIT;
 		const int s0 = KSPLIT == 1 ? 0 : min(KS, warp * per), s1 = KSPLIT == 1 ? KS : min(KS, s0 + per);
-		band_sum<HORIZ, PAIR>(d, w, g, s0, s1, src_dim, base_a, base_b, sk);
+		band_sum<HORIZ, PAIR>(d, w, g, s0, s1, src_dim, base_a, base_b, sk, src + m0 * sm, m_extent - m0, sm);
 		if (KSPLIT == 1) {
 			store_group(d, g, mA, mB, m_extent, dst_dim, dst, dm, dko);
 		} else {
