@@ -90,8 +90,8 @@ void DevicePass::set_tensor()
 	                  &ksteps);
 	std::vector<uint4> uchunk;
 	std::vector<int> ubegin, ukbase;
-	build_umma_tables(table.f32.data(), table.left.data(), table.width, table.rows, horizontal, &uchunk, &ubegin,
-	                  &ukbase);
+	if (!horizontal)
+		build_umma_tables(table.f32.data(), table.left.data(), table.width, table.rows, &uchunk, &ubegin, &ukbase);
 	const size_t fbytes = frag.size() * sizeof(uint4);
 	const size_t kbytes = kbase.size() * sizeof(int);
 	const size_t ubytes = uchunk.size() * sizeof(uint4);
@@ -102,18 +102,23 @@ void DevicePass::set_tensor()
 	unsigned char *base = static_cast<unsigned char *>(wide_storage.get());
 	cuda_check(cudaMemcpy(base, frag.data(), fbytes, cudaMemcpyHostToDevice), "upload band fragments");
 	cuda_check(cudaMemcpy(base + off_k, kbase.data(), kbytes, cudaMemcpyHostToDevice), "upload band fragments");
-	cuda_check(cudaMemcpy(base + off_u, uchunk.data(), ubytes, cudaMemcpyHostToDevice), "upload band chunks");
-	cuda_check(cudaMemcpy(base + off_b, ubegin.data(), bbytes, cudaMemcpyHostToDevice), "upload band chunks");
-	cuda_check(cudaMemcpy(base + off_uk, ukbase.data(), ukbase.size() * sizeof(int), cudaMemcpyHostToDevice),
-	           "upload band chunks");
+	if (!ukbase.empty()) {
+		cuda_check(cudaMemcpy(base + off_u, uchunk.data(), ubytes, cudaMemcpyHostToDevice), "upload band chunks");
+		cuda_check(cudaMemcpy(base + off_b, ubegin.data(), bbytes, cudaMemcpyHostToDevice), "upload band chunks");
+		cuda_check(cudaMemcpy(base + off_uk, ukbase.data(), ukbase.size() * sizeof(int), cudaMemcpyHostToDevice),
+		           "upload band chunks");
+	}
 	wide.frag = reinterpret_cast<const uint4 *>(base);
 	wide.kbase = reinterpret_cast<const int *>(base + off_k);
 	wide.groups = static_cast<int>(kbase.size());
 	wide.ksteps = ksteps;
-	wide.uchunk = reinterpret_cast<const uint4 *>(base + off_u);
-	wide.uchunk_begin = reinterpret_cast<const int *>(base + off_b);
-	wide.ukbase = reinterpret_cast<const int *>(base + off_uk);
-	wide.ugroups = static_cast<int>(ukbase.size());
+	if (!ukbase.empty()) {
+		wide.uchunk = reinterpret_cast<const uint4 *>(base + off_u);
+		wide.uchunk_begin = reinterpret_cast<const int *>(base + off_b);
+		wide.ukbase = reinterpret_cast<const int *>(base + off_uk);
+		wide.utiles = static_cast<int>(ukbase.size());
+		wide.umax_taps = static_cast<int>(table.width);
+	}
 }
 
 std::unique_ptr<DevicePass> make_device_pass(const PassSpec &s)

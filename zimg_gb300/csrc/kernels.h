@@ -43,12 +43,14 @@ struct WideTables {
 	const int *kbase;
 	int groups;
 	int ksteps;
-	// The tcgen05 form (wide_umma.cu): groups of 16 outputs, bands cut into
-	// chunks of 32 inputs. Null uchunk: only the mma.sync form exists.
-	const uint4 *uchunk;      // per chunk: taps hi [16 x 32] then lo, UMMA K-major layout (4 KB)
-	const int *uchunk_begin;  // per group: index of its first chunk; [ugroups] = number of chunks
-	const int *ukbase;        // per group: first input of its band
-	int ugroups;
+	// The tcgen05 form of vertical passes (wide_umma.cu): tiles of 64
+	// outputs, bands cut into chunks of 16 input rows. Null uchunk: only the
+	// mma.sync form exists (horizontal passes).
+	const uint4 *uchunk;      // per chunk: two 8-row blocks of [64 hi taps; 64 lo taps], UMMA K-major layout (8 KB)
+	const int *uchunk_begin;  // per tile: index of its first chunk; [utiles] = number of chunks
+	const int *ukbase;        // per tile: first input row of its band
+	int utiles;
+	int umax_taps;            // widest band of one output (taps)
 };
 
 // One pass over a whole plane. For a horizontal pass the plane has
@@ -74,12 +76,16 @@ void build_wide_tables(const float *f32, const unsigned *left, unsigned width, u
 
 cudaError_t launch_wide(const PassLaunch &l, cudaStream_t stream);
 
-// Host side of the tcgen05 form: per group of 16 outputs its band base (a
-// multiple of 4 inputs for horizontal passes) and its chunks' tap blocks.
-void build_umma_tables(const float *f32, const unsigned *left, unsigned width, unsigned rows, bool horizontal,
+// Host side of the tcgen05 form of a vertical pass: per tile of 64 outputs
+// its band base and its chunks' tap blocks.
+void build_umma_tables(const float *f32, const unsigned *left, unsigned width, unsigned rows,
                        std::vector<uint4> *chunks, std::vector<int> *chunk_begin, std::vector<int> *kbase);
-// The pass on the tcgen05 kernel when the plane allows it (16-byte aligned
-// source, positive stride): cudaErrorNotSupported otherwise, nothing launched.
+// Work items of a vertical pass on the tcgen05 form (tiles of 256 columns x
+// 64 outputs).
+int wide_umma_items(const PassLaunch &l);
+// The vertical pass on the tcgen05 kernel when the plane allows it (16-byte
+// aligned source, positive stride): cudaErrorNotSupported otherwise, nothing
+// launched.
 cudaError_t launch_wide_umma(const PassLaunch &l, cudaStream_t stream);
 // Nonzero when a pipeline wait of the tcgen05 kernel ran out (optionally reset).
 int wide_umma_pipeline_error(bool reset);

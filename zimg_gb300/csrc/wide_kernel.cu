@@ -375,50 +375,52 @@ void build_wide_tables(const float *f32, const unsigned *left, unsigned width, u
 	}
 }
 
-void build_umma_tables(const float *f32, const unsigned *left, unsigned width, unsigned rows, bool horizontal,
+void build_umma_tables(const float *f32, const unsigned *left, unsigned width, unsigned rows,
                        std::vector<uint4> *chunks, std::vector<int> *chunk_begin, std::vector<int> *kbase)
 {
-	constexpr unsigned kN = 16, kKC = 32;
-	const unsigned groups = (rows + kN - 1) / kN;
-	chunk_begin->assign(groups + 1, 0);
-	kbase->assign(groups, 0);
+	constexpr unsigned kOut = 64, kKC = 16;
+	const unsigned tiles = (rows + kOut - 1) / kOut;
+	chunk_begin->assign(tiles + 1, 0);
+	kbase->assign(tiles, 0);
 	int total = 0;
-	for (unsigned g = 0; g < groups; ++g) {
+	for (unsigned t = 0; t < tiles; ++t) {
 		unsigned lo = ~0u, hi = 0;
-		for (unsigned o = g * kN; o < std::min(rows, (g + 1) * kN); ++o) {
+		for (unsigned o = t * kOut; o < std::min(rows, (t + 1) * kOut); ++o) {
 			lo = std::min(lo, left[o]);
 			hi = std::max(hi, left[o] + width);
 		}
-		if (horizontal)
-			lo &= ~3u;  // tensor copies start on 16-byte boundaries
-		(*kbase)[g] = static_cast<int>(lo);
-		(*chunk_begin)[g] = total;
+		(*kbase)[t] = static_cast<int>(lo);
+		(*chunk_begin)[t] = total;
 		total += static_cast<int>((hi - lo + kKC - 1) / kKC);
 	}
-	(*chunk_begin)[groups] = total;
-	// per chunk 1024 words: taps hi [16 outputs x 32 inputs] then lo, each in
-	// the K-major core-matrix layout (output / 8) * 128 + (input / 4) * 256 +
-	// (output % 8) * 16 + (input % 4) * 4 bytes
-	chunks->assign(static_cast<size_t>(total) * 256, uint4{ 0, 0, 0, 0 });
+	(*chunk_begin)[tiles] = total;
+	// per chunk two 8-row blocks of 1024 words: row i < 64 holds the TF32
+	// high part of output 64 t + i's taps, row 64 + i its remainder; element
+	// (row, k) at (row / 8) * 128 + (k / 4) * 2048 + (row % 8) * 16 + (k % 4) * 4
+	// bytes (K-major core matrices)
+	chunks->assign(static_cast<size_t>(total) * 512, uint4{ 0, 0, 0, 0 });
 	uint32_t *w32 = reinterpret_cast<uint32_t *>(chunks->data());
-	for (unsigned g = 0; g < groups; ++g) {
-		const int nc = (*chunk_begin)[g + 1] - (*chunk_begin)[g];
+	for (unsigned t = 0; t < tiles; ++t) {
+		const int nc = (*chunk_begin)[t + 1] - (*chunk_begin)[t];
 		for (int c = 0; c < nc; ++c) {
-			uint32_t *blk = w32 + static_cast<size_t>((*chunk_begin)[g] + c) * 1024;
-			for (unsigned n = 0; n < kN; ++n) {
-				const unsigned o = g * kN + n;
+			uint32_t *blk = w32 + static_cast<size_t>((*chunk_begin)[t] + c) * 2048;
+			for (unsigned i = 0; i < kOut; ++i) {
+				const unsigned o = t * kOut + i;
 				if (o >= rows)
 					continue;
 				for (unsigned kk = 0; kk < kKC; ++kk) {
-					const long x = (*kbase)[g] + static_cast<long>(kKC) * c + kk;
+					const long x = (*kbase)[t] + static_cast<long>(kKC) * c + kk;
 					const long k = x - static_cast<long>(left[o]);
 					if (k < 0 || k >= static_cast<long>(width))
 						continue;
-					const float t = f32[static_cast<size_t>(o) * width + k];
-					const float h = tf32_round(t);
-					const unsigned off = ((n >> 3) * 128 + (kk >> 2) * 256 + (n & 7) * 16 + (kk & 3) * 4) / 4;
-					blk[off] = bits(h);
-					blk[512 + off] = bits(tf32_round(t - h));
+					const float v = f32[static_cast<size_t>(o) * width + k];
+					const float h = tf32_round(v);
+					const unsigned step = kk / 8, k8 = kk % 8;
+					auto at = [&](unsigned row) {
+						return step * 1024 + ((row >> 3) * 128 + (k8 >> 2) * 2048 + (row & 7) * 16 + (k8 & 3) * 4) / 4;
+					};
+					blk[at(i)] = bits(h);
+					blk[at(64 + i)] = bits(tf32_round(v - h));
 				}
 			}
 		}
@@ -427,11 +429,15 @@ void build_umma_tables(const float *f32, const unsigned *left, unsigned width, u
 
 namespace {
 
-// ZG_WIDE_KERNEL=umma puts every eligible wide pass on the tcgen05 form
-// (wide_umma.cu); otherwise they run on the mma.sync form, which is faster
-// for these bands: a tcgen05.mma of M = 128, K = 8 (tf32) measured about 200
-// cycles whatever its N, and a band gives only ~10 useful outputs per
-// 8-input step, where the mma.sync form reached 0.5 m16n8k8 per clock.
+// Which form runs a vertical wide pass. ZG_WIDE_KERNEL=mma: the mma.sync
+// form; =umma: the tcgen05 form wherever the plane and the band allow it;
+// unset: the tcgen05 form when its tiles fill at least three quarters of the
+// SMs (one tile is a long stream of products), else the mma.sync form. Bands
+// wider than kUmmaMaxTaps stay on the mma.sync form: the tcgen05 form
+// accumulates a whole band in tensor memory (2 products per 8 taps), and the
+// tensor core's accumulation is not round-to-nearest.
+constexpr int kUmmaMaxTaps = 160;
+
 int wide_kernel_choice()
 {
 	const char *e = std::getenv("ZG_WIDE_KERNEL");
@@ -478,7 +484,9 @@ void launch_pass_tiles(const PassLaunch &l, int m_extent, int src_dim, int dst_d
 
 cudaError_t launch_wide(const PassLaunch &l, cudaStream_t stream)
 {
-	if (l.wide.uchunk && wide_kernel_choice() == 2) {
+	const int choice = wide_kernel_choice();
+	if (l.wide.uchunk && !l.horizontal && choice != 1 && l.wide.umax_taps <= kUmmaMaxTaps &&
+	    (choice == 2 || 4L * wide_umma_items(l) >= 3L * sm_count())) {
 		const cudaError_t e = launch_wide_umma(l, stream);
 		if (e != cudaErrorNotSupported)
 			return e;

@@ -1,58 +1,50 @@
-// FP32 wide-filter passes (strong downscales, tens to hundreds of taps per
-// output) on the fifth-generation tensor cores: the banded product of
-// wide_kernel.cu with the split samples in tensor memory, the taps in shared
-// memory and the accumulators in tensor memory (tcgen05.mma with A from
-// TMEM), fed by tensor copies.
+// FP32 vertical wide-filter passes (strong downscales, tens to about 160 taps
+// per output) on the fifth-generation tensor cores (tcgen05.mma, operands in
+// shared memory, accumulators in tensor memory), fed by tensor copies.
 //
-// A pass computes out[o][m] = sum_k tap(o, k) * in[k][m] for every output o
-// along the filtered axis and every line m across it (m = column of a
-// vertical pass, row of a horizontal one). A work item is a tile of 128
-// lines times a group of 16 outputs; the group's band of inputs is cut into
-// chunks of 32. Per chunk:
+// A pass computes out[o][x] = sum_k tap(o, k) * in[k][x] for every output row
+// o and column x. The product is laid out for the tensor core's issue model:
+// a tcgen05.mma.kind::tf32 of M = 128, K = 8 costs about 200 cycles whatever
+// its N (measured, 16 <= N <= 256), so N carries 256 image columns and M the
+// taps of 64 outputs twice, their TF32 high parts in rows 0-63 and their TF32
+// remainders in rows 64-127. A work item is one tile of 256 columns x 64
+// outputs; its band of input rows is cut into chunks of 16 rows. Per chunk:
 //
-//  - a producer lane copies the 32 x 128 tile of input samples
+//  - a producer lane copies the 16 x 256 tile of samples
 //    (cp.async.bulk.tensor; zeros outside the plane) and the chunk's tap
-//    block (cp.async.bulk) into a stage of a ring;
-//  - 8 converter warps, two per TMEM lane quadrant, read their lines'
-//    samples, split each into a TF32 high part and a TF32 remainder
-//    (3xTF32) and store both into tensor memory (tcgen05.st; TMEM lane =
-//    line, column = input): the A operands of the chunk;
-//  - one MMA lane issues, per 8 inputs, the products lo*hi, hi*lo and hi*hi
-//    (tcgen05.mma.cta_group::1.kind::tf32, A from tensor memory, B from
-//    shared memory, M = 128 lines, N = 16 outputs, K = 8) into one of 8
-//    tensor-memory accumulators, from zero per chunk;
-//  - 4 epilogue warps read the chunk's accumulator (tcgen05.ld) and add it to
-//    their running sums in fp32, and store their line's 16 outputs when the
-//    band ends.
+//    blocks (cp.async.bulk, built on the host) into a stage of a ring;
+//  - 8 converter warps split each sample into a TF32 high part (truncation)
+//    and a TF32 remainder (rounded to nearest by integer arithmetic on its
+//    bits) and write both, with the tap blocks, into the K-major operand
+//    layout (core matrices of 8 rows x 4 inputs);
+//  - one MMA lane issues per 8 input rows D += A * X_hi and D += A * X_lo
+//    (M = 128, N = 256, K = 8), accumulating the whole band of the tile in
+//    one of two tensor-memory accumulators: row i < 64 of D is the sum of
+//    tap_hi * x over the band, row 64 + i the sum of tap_lo * x;
+//  - 4 epilogue warps read the accumulator (tcgen05.ld, TMEM lane = row),
+//    add row 64 + i to row i in fp32 through shared memory, and store output
+//    o0 + i of the tile's 256 columns.
 //
-// Shared memory carries each sample twice (the tensor copy's write, the
-// converter's read); the operands the tensor core re-reads for its three
-// products come from tensor memory.
+// Each output row sees nonzero taps only within its own band (at most
+// kUmmaMaxTaps inputs: 2 * ceil(taps / 8) + 2 accumulating products); rows
+// outside it add exact zeros. A non-finite sample gives a NaN remainder, so
+// its outputs are NaN.
 //
-// Split: hi = x with its 13 low mantissa bits cleared (truncation to TF32),
-// lo = x - hi (exact) rounded to nearest TF32 by integer arithmetic on its
-// bits; each product keeps about 21 significant bits. A non-finite sample
-// gives lo = NaN, so its outputs are NaN. Chunk sums are added with ordinary
-// fp32 adds, in chunk order: the tensor core's internal additions are not
-// round-to-nearest, and one accumulator carried through a whole 600-tap band
-// measured 7x the C path's error (resize_impl.cpp:61-114) against FP64,
-// where chunks of 32 inputs stay below it.
-//
-// Input tiles: a vertical pass copies 32 rows x 128 columns (raw[input][line],
-// 512-byte rows), a horizontal pass 128 rows x 32 columns with the 128-byte
-// swizzle (16-byte chunk c of line r at chunk c ^ (r % 8)), so that the 8
-// lines a quarter-warp reads fall in different shared-memory banks.
-//
-// Tap blocks (B, 16 outputs x 32 inputs, built on the host) use the K-major
-// no-swizzle layout of the tcgen05 shared memory descriptors: core matrices
-// of 8 outputs x 4 inputs (128 contiguous bytes), (output / 8) * 128 +
-// (input / 4) * 256; the descriptor's leading byte offset is the stride
-// between core matrices along K (256), its stride byte offset the stride
-// between groups of 8 outputs (128).
+// Operand layouts (PTX ISA, tcgen05 shared memory descriptors, K-major, no
+// swizzle): a core matrix is 8 rows x 16 bytes (4 TF32 values along K), 128
+// contiguous bytes; the descriptor's leading byte offset is the stride
+// between core matrices along K, its stride byte offset the stride between
+// groups of 8 rows (128 bytes in both operands). Taps (A, 128 rows x 8
+// inputs per 8-row block): core matrix (row / 8, input / 4) at (row / 8) *
+// 128 + (input / 4) * 2048. Samples (B, 256 columns x 16 inputs per chunk):
+// core matrix (column / 8, input / 4) at (column / 8) * 128 + (input / 4) *
+// kLboX, kLboX = 32 core matrices plus 16 bytes, so that the 4 core matrices
+// a converter lane writes fall in different banks.
 //
 // Every mbarrier wait is bounded (kWaitNs). A wait that runs out records its
 // cause in g_wide_pipeline_error, the CTA stops, the producer waits (bounded)
-// for the copies it has in flight, and tensor memory is freed.
+// for the copies it has in flight, the MMA lane for its products, and tensor
+// memory is freed.
 #include <cuda.h>
 
 #include <algorithm>
@@ -65,53 +57,53 @@ namespace zg {
 
 namespace {
 
-constexpr int kM = 128;                 // lines per tile: TMEM lanes
-constexpr int kN = 16;                  // outputs per group
-constexpr int kKC = 32;                 // inputs per chunk
-constexpr int kStages = 8;              // ring of input tiles
-constexpr int kRegions = 8;             // TMEM accumulators of kN columns
+constexpr int kCols = 256;              // image columns per tile: N
+constexpr int kOut = 64;                // outputs per tile; M = 2 * kOut
+constexpr int kKC = 16;                 // input rows per chunk
+constexpr int kStages = 5;              // ring of sample tiles
 constexpr int kConvWarps = 8;
 constexpr int kEpiWarps = 4;
 constexpr int kThreads = (2 + kEpiWarps + kConvWarps) * 32;  // producer, MMA, epilogue, converters
+constexpr uint32_t kTmemCols = 512;     // two accumulators of kCols columns
 
-// tensor memory columns: A operands of two chunks (hi 32 | lo 32 each), then
-// the accumulators
-constexpr uint32_t kColA = 0;
-constexpr uint32_t kColD = 2 * 2 * kKC;
-constexpr uint32_t kTmemCols = 256;
-static_assert(kColD + kRegions * kN <= kTmemCols, "tensor memory columns");
-
-constexpr unsigned kLboB = 256;
-constexpr unsigned kSboB = 128;
-constexpr unsigned kRawBytes = kKC * kM * 4;      // input tile
-constexpr unsigned kBBytes = 2 * kN * kKC * 4;    // tap block: hi | lo
-constexpr unsigned kStageBytes = kRawBytes + kBBytes;
-constexpr unsigned kOffBar = kStages * kStageBytes;
-constexpr unsigned kNumBars = 3 * kStages + 4 + 2 * kRegions + 1;
+constexpr unsigned kSbo = 128;
+constexpr unsigned kLboA = 2048;
+constexpr unsigned kLboX = (kCols / 8) * 128 + 16;
+constexpr unsigned kRawBytes = kKC * kCols * 4;            // sample tile, raw[row][column]
+constexpr unsigned kABytes = (kKC / 8) * 2 * kOut * 8 * 4; // tap blocks of a chunk
+constexpr unsigned kStageBytes = kRawBytes + kABytes;
+constexpr unsigned kXOp = (kKC / 4) * kLboX;               // one sample operand (hi or lo)
+constexpr unsigned kXBuf = 2 * kXOp + kABytes;             // hi | lo | tap blocks
+constexpr unsigned kXchStride = 36;                        // floats per exchanged row
+constexpr unsigned kXchBytes = 2 * 32 * kXchStride * 4;
+constexpr unsigned kOffX = kStages * kStageBytes;
+constexpr unsigned kOffXch = kOffX + 2 * kXBuf;
+constexpr unsigned kOffBar = kOffXch + kXchBytes;
+constexpr unsigned kNumBars = 2 * kStages + 4 + 4 + 1;
 constexpr unsigned kSmemBytes = kOffBar + kNumBars * 8 + 16 + 1024;  // + TMEM address slot, base alignment
 
 // kind::tf32 instruction descriptor: D f32 (bits 4-5 = 1), A and B TF32
 // (bits 7-9, 10-12 = 2), both K-major (bits 15, 16 = 0), N >> 3 at bit 17,
 // M >> 4 at bit 24.
-constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | (static_cast<uint32_t>(kN >> 3) << 17) |
-                            (static_cast<uint32_t>(kM >> 4) << 24);
+constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | (static_cast<uint32_t>(kCols >> 3) << 17) |
+                            (static_cast<uint32_t>((2 * kOut) >> 4) << 24);
 
-static_assert(kStageBytes % 1024 == 0, "swizzled tensor copies land on 1024-byte boundaries");
+static_assert(kStageBytes % 128 == 0 && kXBuf % 16 == 0 && kXOp % 16 == 0, "copy and operand alignment");
 static_assert(kSmemBytes <= 227 * 1024, "shared memory per CTA");
 
 __device__ int g_wide_pipeline_error;
 
 struct UmmaPass {
-	const uint4 *chunk;        // tap blocks, kBBytes each
-	const int *chunk_begin;    // per group; [groups] = number of chunks
-	const int *kbase;          // per group
-	int groups;
-	int items;                 // line tiles x groups
-	int m_extent;              // lines
-	int dst_dim;               // outputs
+	const uint4 *chunk;        // tap blocks, kABytes per chunk
+	const int *chunk_begin;    // per tile; [tiles] = number of chunks
+	const int *kbase;          // per tile
+	int tiles;                 // output tiles
+	int items;                 // column tiles x output tiles
+	int columns;               // plane width
+	int dst_dim;               // output rows
 	char *dst;
-	ptrdiff_t dm;              // bytes between lines of the destination
-	ptrdiff_t dko;             // bytes between outputs of the destination
+	ptrdiff_t dst_stride;
+	int dst_aligned;           // dst and dst_stride multiples of 16 bytes
 };
 
 // Shared memory descriptor (no swizzle, version 1 at bits 46-47).
@@ -121,15 +113,14 @@ __device__ __forceinline__ uint64_t umma_desc(unsigned saddr, unsigned lbo, unsi
 	       (static_cast<uint64_t>((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
 }
 
-// D (TMEM) (+)= A (TMEM) * B (shared memory).
-__device__ __forceinline__ void umma_tf32_ts(uint32_t d, uint32_t a, uint64_t b, uint32_t accumulate)
+__device__ __forceinline__ void umma_tf32(uint32_t d, uint64_t a, uint64_t b, uint32_t accumulate)
 {
 	asm volatile("{\n"
 	             "  .reg .pred p;\n"
 	             "  setp.ne.b32 p, %4, 0;\n"
-	             "  tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n"
+	             "  tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n"
 	             "}\n" ::"r"(d),
-	             "r"(a), "l"(b), "r"(kIdesc), "r"(accumulate)
+	             "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate)
 	             : "memory");
 }
 
@@ -150,38 +141,25 @@ __device__ __forceinline__ void tc_fence_after()
 	asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
 }
 
-// 16 consecutive columns of this warp's 32 TMEM lanes, one lane per thread;
+// 32 consecutive columns of this warp's 32 TMEM lanes, one lane per thread;
 // the load and its wait in one statement so that no use of the values is
 // scheduled before the wait.
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32])
 {
-	uint32_t r[16];
-	asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
-	             "%14, %15}, [%16];\n"
+	uint32_t r[32];
+	asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+	             "%14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];\n"
 	             "tcgen05.wait::ld.sync.aligned;\n"
 	             : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
 	               "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
-	               "=r"(r[15])
+	               "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+	               "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
+	               "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
 	             : "r"(taddr)
 	             : "memory");
 #pragma unroll
-	for (int i = 0; i < 16; ++i)
+	for (int i = 0; i < 32; ++i)
 		v[i] = __uint_as_float(r[i]);
-}
-
-// 16 consecutive columns of this warp's 32 TMEM lanes from registers.
-__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t (&r)[16])
-{
-	asm volatile("tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
-	             "%13, %14, %15, %16};\n" ::"r"(taddr),
-	             "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]),
-	             "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15])
-	             : "memory");
-}
-
-__device__ __forceinline__ void tmem_st_wait()
-{
-	asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory");
 }
 
 // x -> (TF32 high part by truncation, remainder rounded to nearest TF32).
@@ -197,44 +175,45 @@ __device__ __forceinline__ void record_failure(int cause, volatile int *abort_fl
 	*abort_flag = 1;
 }
 
-// HORIZ: horizontal pass (tile = 128 rows x 32 columns of the source,
-// swizzled); otherwise vertical (32 rows x 128 columns).
-template <bool HORIZ>
+__device__ __forceinline__ void epilogue_sync()
+{
+	asm volatile("bar.sync 1, %0;\n" ::"n"(kEpiWarps * 32) : "memory");
+}
+
 __global__ void __launch_bounds__(kThreads, 1)
 wide_umma_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ UmmaPass p)
 {
 	extern __shared__ unsigned char smem_dyn[];
-	__shared__ int abort_word;
+	__shared__ int abort_word, epi_fail_word;
 	volatile int *abort_flag = &abort_word;
+	volatile int *epi_fail = &epi_fail_word;  // set before an epilogue barrier, read after it
 	unsigned char *sm =
 		reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_dyn) + 1023) & ~static_cast<uintptr_t>(1023));
 	uint64_t *raw_full = reinterpret_cast<uint64_t *>(sm + kOffBar);
-	uint64_t *raw_empty = raw_full + kStages;   // the converters are done with the samples
-	uint64_t *b_empty = raw_empty + kStages;    // the MMAs are done with the taps
-	uint64_t *a_full = b_empty + kStages;
-	uint64_t *a_empty = a_full + 2;
-	uint64_t *t_full = a_empty + 2;
-	uint64_t *t_empty = t_full + kRegions;
-	uint64_t *done = t_empty + kRegions;
+	uint64_t *raw_empty = raw_full + kStages;
+	uint64_t *x_full = raw_empty + kStages;
+	uint64_t *x_empty = x_full + 2;
+	uint64_t *d_full = x_empty + 2;
+	uint64_t *d_empty = d_full + 2;
+	uint64_t *done = d_empty + 2;
 	uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
+	float *xch = reinterpret_cast<float *>(sm + kOffXch);
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
 	if (threadIdx.x == 0) {
 		for (int s = 0; s < kStages; ++s) {
 			mbar_init(&raw_full[s], 1);
 			mbar_init(&raw_empty[s], kConvWarps);
-			mbar_init(&b_empty[s], 1);
 		}
 		for (int b = 0; b < 2; ++b) {
-			mbar_init(&a_full[b], kConvWarps);
-			mbar_init(&a_empty[b], 1);
-		}
-		for (int r = 0; r < kRegions; ++r) {
-			mbar_init(&t_full[r], 1);
-			mbar_init(&t_empty[r], kEpiWarps);
+			mbar_init(&x_full[b], kConvWarps);
+			mbar_init(&x_empty[b], 1);
+			mbar_init(&d_full[b], 1);
+			mbar_init(&d_empty[b], kEpiWarps);
 		}
 		mbar_init(done, 1);
 		*abort_flag = 0;
+		*epi_fail = 0;
 		asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
 	}
 	if (warp == 1) {
@@ -248,6 +227,7 @@ wide_umma_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
 	tc_fence_after();
 	const uint32_t tmem = *tmem_slot;
 
+	// items: column tile major, output tile minor; each CTA a contiguous range
 	const long long i0 = static_cast<long long>(blockIdx.x) * p.items / gridDim.x;
 	const long long i1 = static_cast<long long>(blockIdx.x + 1) * p.items / gridDim.x;
 
@@ -258,12 +238,12 @@ wide_umma_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
 			unsigned seq = 0;
 			bool ok = true;
 			for (long long it = i0; ok && it < i1; ++it) {
-				const int g = static_cast<int>(it % p.groups), mt = static_cast<int>(it / p.groups);
-				const int c0 = __ldg(p.chunk_begin + g), nc = __ldg(p.chunk_begin + g + 1) - c0;
-				const int kb = __ldg(p.kbase + g);
+				const int t = static_cast<int>(it % p.tiles), ct = static_cast<int>(it / p.tiles);
+				const int c0 = __ldg(p.chunk_begin + t), nc = __ldg(p.chunk_begin + t + 1) - c0;
+				const int kb = __ldg(p.kbase + t);
 				for (int c = 0; c < nc; ++c, ++seq) {
 					const unsigned st = seq % kStages, ph = (seq / kStages) & 1;
-					if (*abort_flag || !mbar_wait(&raw_empty[st], ph ^ 1) || !mbar_wait(&b_empty[st], ph ^ 1)) {
+					if (*abort_flag || !mbar_wait(&raw_empty[st], ph ^ 1)) {
 						if (!*abort_flag)
 							record_failure(2, abort_flag);
 						ok = false;
@@ -271,11 +251,8 @@ wide_umma_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
 					}
 					unsigned char *stage = sm + st * kStageBytes;
 					mbar_arrive_expect_tx(&raw_full[st], kStageBytes);
-					if (HORIZ)
-						tma_load_2d(stage, &tmap, kb + kKC * c, mt * kM, &raw_full[st]);
-					else
-						tma_load_2d(stage, &tmap, mt * kM, kb + kKC * c, &raw_full[st]);
-					bulk_load(stage + kRawBytes, p.chunk + static_cast<size_t>(c0 + c) * (kBBytes / 16), kBBytes,
+					tma_load_2d(stage, &tmap, ct * kCols, kb + kKC * c, &raw_full[st]);
+					bulk_load(stage + kRawBytes, p.chunk + static_cast<size_t>(c0 + c) * (kABytes / 16), kABytes,
 					          &raw_full[st]);
 				}
 			}
@@ -288,39 +265,40 @@ wide_umma_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
 	} else if (warp == 1) {
 		if (lane == 0) {
 			// MMA issue
-			const unsigned sbase = smem_addr(sm);
-			unsigned seq = 0;
+			const unsigned xbase = smem_addr(sm + kOffX);
+			unsigned seq = 0, iseq = 0;
 			bool ok = true;
-			for (long long it = i0; ok && it < i1; ++it) {
-				const int g = static_cast<int>(it % p.groups);
-				const int nc = __ldg(p.chunk_begin + g + 1) - __ldg(p.chunk_begin + g);
+			for (long long it = i0; ok && it < i1; ++it, ++iseq) {
+				const int t = static_cast<int>(it % p.tiles);
+				const int nc = __ldg(p.chunk_begin + t + 1) - __ldg(p.chunk_begin + t);
+				const unsigned db = iseq & 1, dph = (iseq >> 1) & 1;
+				if (*abort_flag || !mbar_wait(&d_empty[db], dph ^ 1)) {
+					if (!*abort_flag)
+						record_failure(3, abort_flag);
+					break;
+				}
+				const uint32_t d = tmem + db * kCols;
 				for (int c = 0; c < nc; ++c, ++seq) {
-					const unsigned st = seq % kStages, ph = (seq / kStages) & 1;
-					const unsigned ab = seq & 1, aph = (seq >> 1) & 1;
-					const unsigned r = seq % kRegions, rph = (seq / kRegions) & 1;
-					if (*abort_flag || !mbar_wait(&a_full[ab], aph) || !mbar_wait(&raw_full[st], ph) ||
-					    !mbar_wait(&t_empty[r], rph ^ 1)) {
+					const unsigned xb = seq & 1, xph = (seq >> 1) & 1;
+					if (*abort_flag || !mbar_wait(&x_full[xb], xph)) {
 						if (!*abort_flag)
 							record_failure(3, abort_flag);
 						ok = false;
 						break;
 					}
 					tc_fence_after();
-					const uint32_t d = tmem + kColD + r * kN;
-					const uint32_t ahi = tmem + kColA + ab * 2 * kKC, alo = ahi + kKC;
-					const unsigned bhi = sbase + st * kStageBytes + kRawBytes, blo = bhi + kBBytes / 2;
+					const unsigned xhi = xbase + xb * kXBuf, xlo = xhi + kXOp, ab = xlo + kXOp;
 #pragma unroll
 					for (int s = 0; s < kKC / 8; ++s) {
-						const uint64_t db_hi = umma_desc(bhi + 2 * s * kLboB, kLboB, kSboB);
-						const uint64_t db_lo = umma_desc(blo + 2 * s * kLboB, kLboB, kSboB);
-						umma_tf32_ts(d, alo + 8 * s, db_hi, s > 0);
-						umma_tf32_ts(d, ahi + 8 * s, db_lo, 1);
-						umma_tf32_ts(d, ahi + 8 * s, db_hi, 1);
+						const uint64_t da = umma_desc(ab + s * (kABytes / 2), kLboA, kSbo);
+						umma_tf32(d, da, umma_desc(xhi + 2 * s * kLboX, kLboX, kSbo), c > 0 || s > 0);
+						umma_tf32(d, da, umma_desc(xlo + 2 * s * kLboX, kLboX, kSbo), 1);
 					}
-					umma_commit(&a_empty[ab]);
-					umma_commit(&b_empty[st]);
-					umma_commit(&t_full[r]);
+					umma_commit(&x_empty[xb]);
 				}
+				if (!ok)
+					break;
+				umma_commit(&d_full[db]);
 			}
 			// nothing of this CTA's may still read shared or tensor memory on return
 			umma_commit(done);
@@ -328,104 +306,119 @@ wide_umma_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
 				record_failure(3, abort_flag);
 		}
 	} else if (warp < 2 + kEpiWarps) {
-		// epilogue: TMEM lanes 32 q .. 32 q + 31 belong to warp q of a warpgroup
+		// epilogue: TMEM lanes 32 q .. 32 q + 31 belong to warp q of a warpgroup;
+		// quadrants 2 and 3 (remainder rows) hand their rows to quadrants 0 and 1
 		const int q = warp & 3;
 		const uint32_t tl = tmem + (static_cast<uint32_t>(32 * q) << 16);
-		const int ml = 32 * q + lane;
-		unsigned seq = 0;
-		bool ok = true;
-		for (long long it = i0; ok && it < i1; ++it) {
-			const int g = static_cast<int>(it % p.groups), mt = static_cast<int>(it / p.groups);
-			const int nc = __ldg(p.chunk_begin + g + 1) - __ldg(p.chunk_begin + g);
-			float sum[kN];
-#pragma unroll
-			for (int n = 0; n < kN; ++n)
-				sum[n] = 0.0f;
-			for (int c = 0; c < nc; ++c, ++seq) {
-				const unsigned r = seq % kRegions, rph = (seq / kRegions) & 1;
-				if (__any_sync(0xffffffffu, *abort_flag) || !__all_sync(0xffffffffu, mbar_wait(&t_full[r], rph))) {
-					if (lane == 0 && !*abort_flag)
-						record_failure(4, abort_flag);
-					ok = false;
-					break;
-				}
-				tc_fence_after();
-				float v[kN];
-				tmem_ld16(tl + kColD + r * kN, v);
-				tc_fence_before();
-				__syncwarp();
-				if (lane == 0)
-					mbar_arrive(&t_empty[r]);
-#pragma unroll
-				for (int n = 0; n < kN; ++n)
-					sum[n] += v[n];
+		float *xrow = xch + ((q & 1) * 32 + lane) * kXchStride;
+		unsigned iseq = 0;
+		for (long long it = i0; it < i1; ++it, ++iseq) {
+			const int t = static_cast<int>(it % p.tiles), ct = static_cast<int>(it / p.tiles);
+			const unsigned db = iseq & 1, dph = (iseq >> 1) & 1;
+			// the four warps leave together: each records its own outcome
+			// before the barrier and all read the common one after it
+			const bool got = __all_sync(0xffffffffu, mbar_wait(&d_full[db], dph)) && !*abort_flag;
+			if (!got && lane == 0) {
+				*epi_fail = 1;
+				record_failure(4, abort_flag);
 			}
-			if (!ok)
+			epilogue_sync();
+			if (*epi_fail)
 				break;
-			const int m = mt * kM + ml;
-			if (m < p.m_extent) {
-				const int o0 = g * kN;
-				char *d = p.dst + static_cast<ptrdiff_t>(m) * p.dm + static_cast<ptrdiff_t>(o0) * p.dko;
+			tc_fence_after();
+			const int o = t * kOut + 32 * (q & 1) + lane;
+			for (int piece = 0; piece < kCols / 32; ++piece) {
+				float v[32];
+				tmem_ld32(tl + db * kCols + piece * 32, v);
+				if (q >= 2) {
 #pragma unroll
-				for (int n = 0; n < kN; ++n)
-					if (o0 + n < p.dst_dim)
-						*reinterpret_cast<float *>(d + n * p.dko) = sum[n];
+					for (int j = 0; j < 32; j += 4)
+						*reinterpret_cast<float4 *>(xrow + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+				}
+				epilogue_sync();
+				if (q < 2) {
+					const int x0 = ct * kCols + piece * 32;
+					if (o < p.dst_dim) {
+						float *out = reinterpret_cast<float *>(p.dst + static_cast<ptrdiff_t>(o) * p.dst_stride) + x0;
+#pragma unroll
+						for (int j = 0; j < 32; j += 4) {
+							const float4 r = *reinterpret_cast<const float4 *>(xrow + j);
+							const float s0 = v[j] + r.x, s1 = v[j + 1] + r.y, s2 = v[j + 2] + r.z, s3 = v[j + 3] + r.w;
+							if (p.dst_aligned && x0 + j + 3 < p.columns) {
+								*reinterpret_cast<float4 *>(out + j) = make_float4(s0, s1, s2, s3);
+							} else if (x0 + j + 3 < p.columns) {
+								out[j] = s0;
+								out[j + 1] = s1;
+								out[j + 2] = s2;
+								out[j + 3] = s3;
+							} else {
+								if (x0 + j < p.columns)
+									out[j] = s0;
+								if (x0 + j + 1 < p.columns)
+									out[j + 1] = s1;
+								if (x0 + j + 2 < p.columns)
+									out[j + 2] = s2;
+							}
+						}
+					}
+				}
+				epilogue_sync();
 			}
+			tc_fence_before();
+			__syncwarp();
+			if (lane == 0)
+				mbar_arrive(&d_empty[db]);
 		}
 	} else {
-		// converters: warp (quadrant q, half h) splits inputs 16 h .. 16 h + 15
-		// of lines 32 q .. 32 q + 31
-		const int cw = warp - 2 - kEpiWarps;
-		const int q = warp & 3, h = cw >> 2;
-		const int m = 32 * q + lane;
-		const uint32_t tl = tmem + (static_cast<uint32_t>(32 * q) << 16) + kColA + 16 * h;
+		// converters: thread = column of the tile
+		const int n = (warp - 2 - kEpiWarps) * 32 + lane;
 		unsigned seq = 0;
 		bool ok = true;
 		for (long long it = i0; ok && it < i1; ++it) {
-			const int g = static_cast<int>(it % p.groups);
-			const int nc = __ldg(p.chunk_begin + g + 1) - __ldg(p.chunk_begin + g);
+			const int t = static_cast<int>(it % p.tiles);
+			const int nc = __ldg(p.chunk_begin + t + 1) - __ldg(p.chunk_begin + t);
 			for (int c = 0; c < nc; ++c, ++seq) {
 				const unsigned st = seq % kStages, ph = (seq / kStages) & 1;
-				const unsigned ab = seq & 1, aph = (seq >> 1) & 1;
+				const unsigned xb = seq & 1, xph = (seq >> 1) & 1;
 				if (__any_sync(0xffffffffu, *abort_flag) ||
-				    !__all_sync(0xffffffffu, mbar_wait(&raw_full[st], ph) && mbar_wait(&a_empty[ab], aph ^ 1))) {
+				    !__all_sync(0xffffffffu, mbar_wait(&raw_full[st], ph) && mbar_wait(&x_empty[xb], xph ^ 1))) {
 					if (lane == 0 && !*abort_flag)
 						record_failure(1, abort_flag);
 					ok = false;
 					break;
 				}
-				const unsigned char *raw = sm + st * kStageBytes;
-				float x[16];
-				if (HORIZ) {
-					// line m: 128 bytes, 16-byte chunk j at chunk j ^ (m % 8)
+				const unsigned char *stage = sm + st * kStageBytes;
+				const float *raw = reinterpret_cast<const float *>(stage);
+				unsigned char *xhi = sm + kOffX + xb * kXBuf, *xlo = xhi + kXOp;
+				// the chunk's tap blocks travel with the samples
+				const uint4 *asrc = reinterpret_cast<const uint4 *>(stage + kRawBytes);
+				uint4 *adst = reinterpret_cast<uint4 *>(xlo + kXOp);
+				const uint4 a0 = asrc[n], a1 = asrc[n + kCols];
+				float x[kKC];
 #pragma unroll
-					for (int i = 0; i < 4; ++i) {
-						const float4 v = *reinterpret_cast<const float4 *>(raw + m * 128 + (((4 * h + i) ^ (m & 7)) << 4));
-						x[4 * i] = v.x;
-						x[4 * i + 1] = v.y;
-						x[4 * i + 2] = v.z;
-						x[4 * i + 3] = v.w;
-					}
-				} else {
+				for (int k = 0; k < kKC; ++k)
+					x[k] = raw[k * kCols + n];
+				uint32_t hi[kKC], lo[kKC];
 #pragma unroll
-					for (int j = 0; j < 16; ++j)
-						x[j] = reinterpret_cast<const float *>(raw)[(16 * h + j) * kM + m];
-				}
-				uint32_t hi[16], lo[16];
-#pragma unroll
-				for (int j = 0; j < 16; ++j)
-					split(x[j], hi[j], lo[j]);
+				for (int k = 0; k < kKC; ++k)
+					split(x[k], hi[k], lo[k]);
 				__syncwarp();
 				if (lane == 0)
 					mbar_arrive(&raw_empty[st]);
-				tc_fence_after();
-				tmem_st16(tl + ab * 2 * kKC, hi);
-				tmem_st16(tl + ab * 2 * kKC + kKC, lo);
-				tmem_st_wait();
-				tc_fence_before();
+				adst[n] = a0;
+				adst[n + kCols] = a1;
+#pragma unroll
+				for (int kq = 0; kq < kKC / 4; ++kq) {
+					const unsigned off = (n >> 3) * kSbo + kq * kLboX + (n & 7) * 16;
+					*reinterpret_cast<uint4 *>(xhi + off) =
+						make_uint4(hi[4 * kq], hi[4 * kq + 1], hi[4 * kq + 2], hi[4 * kq + 3]);
+					*reinterpret_cast<uint4 *>(xlo + off) =
+						make_uint4(lo[4 * kq], lo[4 * kq + 1], lo[4 * kq + 2], lo[4 * kq + 3]);
+				}
+				asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
 				__syncwarp();
 				if (lane == 0)
-					mbar_arrive(&a_full[ab]);
+					mbar_arrive(&x_full[xb]);
 			}
 		}
 	}
@@ -447,50 +440,41 @@ int sm_count_umma()
 	return n > 0 ? n : 152;
 }
 
-template <bool HORIZ>
-cudaError_t set_smem_attr()
-{
-	return cudaFuncSetAttribute(wide_umma_kernel<HORIZ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-	                            static_cast<int>(kSmemBytes));
-}
-
 } // namespace
+
+int wide_umma_items(const PassLaunch &l)
+{
+	return static_cast<int>((l.lines + kCols - 1) / kCols) * l.wide.utiles;
+}
 
 cudaError_t launch_wide_umma(const PassLaunch &l, cudaStream_t stream)
 {
 	const WideTables &w = l.wide;
-	if (!w.uchunk || l.src_stride <= 0 || reinterpret_cast<uintptr_t>(l.src) % 16 || l.src_stride % 16)
+	if (!w.uchunk || l.horizontal || l.src_stride <= 0 || reinterpret_cast<uintptr_t>(l.src) % 16 || l.src_stride % 16)
 		return cudaErrorNotSupported;
-	const uint64_t src_dim = l.t.input_width, lines = l.lines;
 	CUtensorMap map;
-	const bool ok = l.horizontal
-	                    ? encode_tensor_map_2d(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, l.src, src_dim, lines,
-	                                           static_cast<uint64_t>(l.src_stride), kKC, kM, true)
-	                    : encode_tensor_map_2d(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, l.src, lines, src_dim,
-	                                           static_cast<uint64_t>(l.src_stride), kM, kKC, false);
-	if (!ok)
+	if (!encode_tensor_map_2d(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, l.src, l.lines, l.t.input_width,
+	                          static_cast<uint64_t>(l.src_stride), kCols, kKC, false))
 		return cudaErrorNotSupported;
 	UmmaPass p{};
 	p.chunk = w.uchunk;
 	p.chunk_begin = w.uchunk_begin;
 	p.kbase = w.ukbase;
-	p.groups = w.ugroups;
-	p.items = static_cast<int>((lines + kM - 1) / kM) * w.ugroups;
-	p.m_extent = static_cast<int>(lines);
+	p.tiles = w.utiles;
+	p.items = wide_umma_items(l);
+	p.columns = static_cast<int>(l.lines);
 	p.dst_dim = static_cast<int>(l.t.rows);
 	p.dst = static_cast<char *>(l.dst);
-	p.dm = l.horizontal ? l.dst_stride : 4;
-	p.dko = l.horizontal ? 4 : l.dst_stride;
+	p.dst_stride = l.dst_stride;
+	p.dst_aligned = reinterpret_cast<uintptr_t>(l.dst) % 16 == 0 && l.dst_stride % 16 == 0;
 	if (p.items <= 0)
 		return cudaSuccess;
 	const int grid = std::min(p.items, sm_count_umma());
-	cudaError_t e = l.horizontal ? set_smem_attr<true>() : set_smem_attr<false>();
+	const cudaError_t e = cudaFuncSetAttribute(wide_umma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+	                                           static_cast<int>(kSmemBytes));
 	if (e != cudaSuccess)
 		return e;
-	if (l.horizontal)
-		wide_umma_kernel<true><<<grid, kThreads, kSmemBytes, stream>>>(map, p);
-	else
-		wide_umma_kernel<false><<<grid, kThreads, kSmemBytes, stream>>>(map, p);
+	wide_umma_kernel<<<grid, kThreads, kSmemBytes, stream>>>(map, p);
 	return cudaGetLastError();
 }
 
