@@ -15,8 +15,9 @@
 //    blocks (cp.async.bulk, built on the host) into a stage of a ring;
 //  - 8 converter warps split each sample into a TF32 high part (truncation)
 //    and a TF32 remainder (rounded to nearest by integer arithmetic on its
-//    bits) and write both, with the tap blocks, into the K-major operand
-//    layout (core matrices of 8 rows x 4 inputs);
+//    bits) and write both into the K-major operand layout (core matrices of
+//    8 rows x 4 inputs); the MMAs read the tap blocks in the stage, which is
+//    refilled once both the converters and those MMAs are done with it;
 //  - one MMA lane issues per 8 input rows D += A * X_hi and D += A * X_lo
 //    (M = 128, N = 256, K = 8), accumulating the whole band of the tile in
 //    one of two tensor-memory accumulators: row i < 64 of D is the sum of
@@ -60,7 +61,7 @@ namespace {
 constexpr int kCols = 256;              // image columns per tile: N
 constexpr int kOut = 64;                // outputs per tile; M = 2 * kOut
 constexpr int kKC = 16;                 // input rows per chunk
-constexpr int kStages = 5;              // ring of sample tiles
+constexpr int kStages = 6;              // ring of sample tiles
 constexpr int kConvWarps = 8;
 constexpr int kEpiWarps = 4;
 constexpr int kThreads = (2 + kEpiWarps + kConvWarps) * 32;  // producer, MMA, epilogue, converters
@@ -73,7 +74,7 @@ constexpr unsigned kRawBytes = kKC * kCols * 4;            // sample tile, raw[r
 constexpr unsigned kABytes = (kKC / 8) * 2 * kOut * 8 * 4; // tap blocks of a chunk
 constexpr unsigned kStageBytes = kRawBytes + kABytes;
 constexpr unsigned kXOp = (kKC / 4) * kLboX;               // one sample operand (hi or lo)
-constexpr unsigned kXBuf = 2 * kXOp + kABytes;             // hi | lo | tap blocks
+constexpr unsigned kXBuf = 2 * kXOp;                       // hi | lo
 constexpr unsigned kXchStride = 36;                        // floats per exchanged row
 constexpr unsigned kXchBytes = 2 * 32 * kXchStride * 4;
 constexpr unsigned kOffX = kStages * kStageBytes;
@@ -203,7 +204,7 @@ wide_umma_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
 	if (threadIdx.x == 0) {
 		for (int s = 0; s < kStages; ++s) {
 			mbar_init(&raw_full[s], 1);
-			mbar_init(&raw_empty[s], kConvWarps);
+			mbar_init(&raw_empty[s], kConvWarps + 1);  // the converters, then the MMAs that read the tap blocks
 		}
 		for (int b = 0; b < 2; ++b) {
 			mbar_init(&x_full[b], kConvWarps);
@@ -265,7 +266,7 @@ wide_umma_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
 	} else if (warp == 1) {
 		if (lane == 0) {
 			// MMA issue
-			const unsigned xbase = smem_addr(sm + kOffX);
+			const unsigned xbase = smem_addr(sm + kOffX), sbase = smem_addr(sm);
 			unsigned seq = 0, iseq = 0;
 			bool ok = true;
 			for (long long it = i0; ok && it < i1; ++it, ++iseq) {
@@ -279,15 +280,16 @@ wide_umma_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
 				}
 				const uint32_t d = tmem + db * kCols;
 				for (int c = 0; c < nc; ++c, ++seq) {
+					const unsigned st = seq % kStages, ph = (seq / kStages) & 1;
 					const unsigned xb = seq & 1, xph = (seq >> 1) & 1;
-					if (*abort_flag || !mbar_wait(&x_full[xb], xph)) {
+					if (*abort_flag || !mbar_wait(&x_full[xb], xph) || !mbar_wait(&raw_full[st], ph)) {
 						if (!*abort_flag)
 							record_failure(3, abort_flag);
 						ok = false;
 						break;
 					}
 					tc_fence_after();
-					const unsigned xhi = xbase + xb * kXBuf, xlo = xhi + kXOp, ab = xlo + kXOp;
+					const unsigned xhi = xbase + xb * kXBuf, xlo = xhi + kXOp, ab = sbase + st * kStageBytes + kRawBytes;
 #pragma unroll
 					for (int s = 0; s < kKC / 8; ++s) {
 						const uint64_t da = umma_desc(ab + s * (kABytes / 2), kLboA, kSbo);
@@ -295,6 +297,7 @@ wide_umma_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
 						umma_tf32(d, da, umma_desc(xlo + 2 * s * kLboX, kLboX, kSbo), 1);
 					}
 					umma_commit(&x_empty[xb]);
+					umma_commit(&raw_empty[st]);
 				}
 				if (!ok)
 					break;
@@ -390,10 +393,6 @@ wide_umma_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
 				const unsigned char *stage = sm + st * kStageBytes;
 				const float *raw = reinterpret_cast<const float *>(stage);
 				unsigned char *xhi = sm + kOffX + xb * kXBuf, *xlo = xhi + kXOp;
-				// the chunk's tap blocks travel with the samples
-				const uint4 *asrc = reinterpret_cast<const uint4 *>(stage + kRawBytes);
-				uint4 *adst = reinterpret_cast<uint4 *>(xlo + kXOp);
-				const uint4 a0 = asrc[n], a1 = asrc[n + kCols];
 				float x[kKC];
 #pragma unroll
 				for (int k = 0; k < kKC; ++k)
@@ -405,8 +404,6 @@ wide_umma_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
 				__syncwarp();
 				if (lane == 0)
 					mbar_arrive(&raw_empty[st]);
-				adst[n] = a0;
-				adst[n + kCols] = a1;
 #pragma unroll
 				for (int kq = 0; kq < kKC / 4; ++kq) {
 					const unsigned off = (n >> 3) * kSbo + kq * kLboX + (n & 7) * 16;
