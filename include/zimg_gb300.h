@@ -183,6 +183,13 @@ ZG_API zg_error_code zg_unresize_process(const zg_unresize *u, const void *src, 
  * No zimg counterpart (zimg has no asynchronous device work). */
 ZG_API int zg_pipeline_status(int reset);
 
+/* The forms that ran the FP32 wide-filter passes enqueued by this host
+ * thread since the last reset: bit 0 the mma.sync form (3xTF32 fragments in
+ * registers), bit 1 the tcgen05 form (TMEM accumulators; vertical passes
+ * whose tiles fill the SMs). With reset != 0 the mask is cleared after it is
+ * read. A diagnostic for tests and tuning; no zimg counterpart. */
+ZG_API int zg_wide_forms_used(int reset);
+
 /* Version of this library. Replaces zimg_get_version_info (zimg.h:54). */
 ZG_API void zg_get_version_info(unsigned *major, unsigned *minor, unsigned *micro);
 

@@ -81,18 +81,42 @@ def test_umma_and_mma_forms_agree(cuda, monkeypatch):
     assert float(np.max(np.abs(outs[0].astype(np.float64) - outs[1]))) < 1e-5
 
 
-def test_umma_kernel_launches(cuda, monkeypatch):
-    """The tcgen05 kernel is what runs when selected (kernel names from the
-    CUDA activity trace)."""
+def test_default_choice_full_plane(cuda, oracle, lib, monkeypatch):
+    """Without ZG_WIDE_KERNEL the vertical pass of the 16x downscale of a
+    7680x4320 plane (150 tiles) takes the tcgen05 form and the horizontal pass
+    the mma.sync form; the result is within the FP64 bound."""
+    monkeypatch.delenv("ZG_WIDE_KERNEL", raising=False)
+    rng = np.random.default_rng(31)
+    src = rng.random((4320, 7680), dtype=np.float32)
+    lib.zg_wide_forms_used(1)
+    got, r = run(src, 480, 270, "lanczos", 4)
+    assert lib.zg_wide_forms_used(1) == 3  # both forms ran
+    bound_check(oracle, src, got, 480, 270, "lanczos", 4)
+
+
+def test_batch_wide_jobs_match_single(cuda, lib, monkeypatch):
+    """A batch of wide jobs (the bench's path, CUDA graph replay included)
+    gives the same bits as the same conversions run one by one."""
     import torch
-    from torch.profiler import ProfilerActivity, profile
-    monkeypatch.setenv("ZG_WIDE_KERNEL", "umma")
-    rng = np.random.default_rng(8)
-    src = band_limited(rng, 1080, 1920)
-    with profile(activities=[ProfilerActivity.CUDA]) as prof:
-        run(src, 120, 67, "lanczos", 4)
+    import zimg_gb300 as zg
+    monkeypatch.delenv("ZG_WIDE_KERNEL", raising=False)
+    rng = np.random.default_rng(32)
+    srcs = [rng.random((4320, 7680), dtype=np.float32) for _ in range(2)]
+    singles = [run(s, 480, 270, "lanczos", 4)[0] for s in srcs]
+    b = zg.Batch([zg.ResizeConversion(7680, 4320, "float").set_filter("lanczos", 4).set_dst_width(480)
+                  .set_dst_height(270) for _ in srcs])
+    dev_s = [to_dev(s) for s in srcs]
+    dev_d = [torch.empty((270, 480), device="cuda") for _ in srcs]
+    b.set_io(dev_s, dev_d)
+    lib.zg_wide_forms_used(1)
+    for graph in (False, True):
+        for d in dev_d:
+            d.zero_()
+        if graph:
+            b.process_graph()
+        else:
+            b.process()
         torch.cuda.synchronize()
-    names = [e.name for e in prof.events()]
-    if not names:
-        pytest.skip("the CUDA activity trace recorded no kernels on this machine")
-    assert any("wide_umma_kernel" in n for n in names), sorted(set(names))[:20]
+        for d, want in zip(dev_d, singles):
+            np.testing.assert_array_equal(d.cpu().numpy().view(np.uint32), want.view(np.uint32), err_msg=str(graph))
+    assert lib.zg_wide_forms_used(1) & 2

@@ -191,6 +191,11 @@ void check_plane(const void *p, ptrdiff_t stride, unsigned w, Sample s, const ch
 
 extern "C" {
 
+int zg_wide_forms_used(int reset)
+{
+	return wide_forms_used(reset != 0);
+}
+
 int zg_pipeline_status(int reset)
 {
 	const int chain = chain_tma_pipeline_error(reset != 0);

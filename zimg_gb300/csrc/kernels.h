@@ -87,6 +87,9 @@ int wide_umma_items(const PassLaunch &l);
 // aligned source, positive stride): cudaErrorNotSupported otherwise, nothing
 // launched.
 cudaError_t launch_wide_umma(const PassLaunch &l, cudaStream_t stream);
+// The forms of the wide passes enqueued by this host thread since the last
+// reset (bit 0 mma.sync, bit 1 tcgen05).
+int wide_forms_used(bool reset);
 // Nonzero when a pipeline wait of the tcgen05 kernel ran out (optionally reset).
 int wide_umma_pipeline_error(bool reset);
 

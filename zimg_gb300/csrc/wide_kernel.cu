@@ -482,15 +482,30 @@ void launch_pass_tiles(const PassLaunch &l, int m_extent, int src_dim, int dst_d
 
 } // namespace
 
+namespace {
+thread_local int g_wide_forms = 0;
+}
+
+int wide_forms_used(bool reset)
+{
+	const int v = g_wide_forms;
+	if (reset)
+		g_wide_forms = 0;
+	return v;
+}
+
 cudaError_t launch_wide(const PassLaunch &l, cudaStream_t stream)
 {
 	const int choice = wide_kernel_choice();
 	if (l.wide.uchunk && !l.horizontal && choice != 1 && l.wide.umax_taps <= kUmmaMaxTaps &&
 	    (choice == 2 || 4L * wide_umma_items(l) >= 3L * sm_count())) {
 		const cudaError_t e = launch_wide_umma(l, stream);
-		if (e != cudaErrorNotSupported)
+		if (e != cudaErrorNotSupported) {
+			g_wide_forms |= 2;
 			return e;
+		}
 	}
+	g_wide_forms |= 1;
 	const int m_extent = static_cast<int>(l.lines);
 	const int src_dim = static_cast<int>(l.t.input_width);
 	const int dst_dim = static_cast<int>(l.t.rows);
