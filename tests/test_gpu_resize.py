@@ -104,7 +104,7 @@ def test_golden_planes_on_gpu(cuda, golden, oracle):
             _f32_check(oracle, src, got, p["dst_w"], p["dst_h"], p["kind"], p["a"], p["b"], exact=False, **kw)
 
 
-# ------------------------------------------------------- BASELINE configs --
+# ------------------------------------------------- headline configurations --
 
 def test_config1_fhd_to_uhd_u16_bitexact(cuda, oracle):
     rng = np.random.default_rng(0x5EED0001)

@@ -179,7 +179,8 @@ int chain_tma_pipeline_error(bool reset);
 // height elements, `stride` bytes per line; swizzle128: boxes land in shared
 // memory with the 128-byte swizzle (16-byte chunk c of box line r at chunk
 // c ^ (r % 8); box lines of 128 bytes, destination 1024-byte aligned). False
-// when the driver's encoder refuses it or base / stride are not 16-byte aligned.
+// when the CUDA driver's tensor-map encoder refuses it or base / stride are
+// not 16-byte aligned.
 bool encode_tensor_map_2d(CUtensorMap *map, CUtensorMapDataType type, const void *base, uint64_t width,
                           uint64_t height, uint64_t stride, uint32_t box_w, uint32_t box_h, bool swizzle128 = false);
 // Work items that fill the current device once (SMs x resident CTAs).
