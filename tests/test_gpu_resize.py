@@ -106,7 +106,7 @@ def test_golden_planes_on_gpu(cuda, golden, oracle):
 
 # ------------------------------------------------- headline configurations --
 
-def test_config1_fhd_to_uhd_u16_bitexact(cuda, oracle):
+def test_fhd_to_uhd_u16_lanczos3_bitexact(cuda, oracle):
     rng = np.random.default_rng(0x5EED0001)
     src = make_u16(rng, 1080, 1920, 10)
     got, r = run_conversion(src, 3840, 2160, "lanczos", 3, depth=10)
@@ -115,7 +115,7 @@ def test_config1_fhd_to_uhd_u16_bitexact(cuda, oracle):
     np.testing.assert_array_equal(got, want)
 
 
-def test_config1_engines_agree(cuda, oracle):
+def test_fhd_to_uhd_engines_agree(cuda, oracle):
     """Tensor-core fused, CUDA-core fused and separate passes give zimg's bytes."""
     rng = np.random.default_rng(7)
     src = make_u16(rng, 270, 480, 10)
@@ -155,7 +155,7 @@ def _f32_check(oracle, src, got, dst_w, dst_h, kind, a=math.nan, b=math.nan, exa
     return err_gpu, err_c
 
 
-def test_config2_bicubic_downscale_f32(cuda, oracle):
+def test_bicubic_1080p_to_720p_f32(cuda, oracle):
     rng = np.random.default_rng(0x5EED0002)
     for plane in range(3):
         src = rng.random((1080, 1920), dtype=np.float32)
@@ -178,7 +178,7 @@ def band_limited(rng, h, w, cutoff=0.25):
     return y.astype(np.float32)
 
 
-def test_config3_wide_filter_down16_f32(cuda, oracle):
+def test_wide_filter_down16_f32(cuda, oracle):
     rng = np.random.default_rng(0x5EED0003)
     src = band_limited(rng, 1080, 1920)
     got, r = run_conversion(src, 120, 67, "lanczos", 4, engine="cuda")
@@ -190,7 +190,7 @@ def test_config3_wide_filter_down16_f32(cuda, oracle):
     _f32_check(oracle, src, got, 120, 67, "lanczos", 4, exact=False)
 
 
-def test_config5_extreme_ratios_f32(cuda, oracle):
+def test_extreme_ratios_f32(cuda, oracle):
     rng = np.random.default_rng(0x5EED0005)
     small = band_limited(rng, 64, 64)
     got, _ = run_conversion(small, 1600, 1600, "lanczos", 3, engine="cuda")
@@ -221,7 +221,7 @@ def test_tensor_core_f32_error_bound(cuda, oracle, kind, a):
         _f32_check(oracle, src, got, dw, dh, kind, a, exact=False, **kw)
 
 
-def test_config5_interlaced_fields_f32(cuda, oracle):
+def test_interlaced_fields_f32(cuda, oracle):
     rng = np.random.default_rng(0x5EED0055)
     frame = band_limited(rng, 1080, 1920)
     for parity, field in ((1, frame[0::2]), (2, frame[1::2])):
