@@ -66,7 +66,7 @@ def run_conversion(src, dst_w, dst_h, kind, a=math.nan, b=math.nan, depth=None, 
 
 
 def make_u16(rng, h, w, depth):
-    """Config-1 style content: 16x16 blocks of uniform noise or smooth waves."""
+    """FHD-to-UHD test content: 16x16 blocks of uniform noise or smooth waves."""
     out = np.empty((h, w), np.uint16)
     maxv = (1 << depth) - 1
     yy, xx = np.mgrid[0:h, 0:w]
