@@ -466,7 +466,7 @@ def test_graph_plane_params_known_answers(cuda):
 
 
 def test_graph_yuv420_mpeg2_spline36(cuda, oracle):
-    """Config-4 shape: YUV 4:2:0 u16, MPEG-2 (left) siting, Spline36 on all planes."""
+    """The mixed-batch shape: YUV 4:2:0 u16, MPEG-2 (left) siting, Spline36 on all planes."""
     import torch
     import zimg_gb300 as zg
     from oracle import oracle as O
