@@ -37,10 +37,13 @@ def bound_check(oracle, src, got, dw, dh, kind, a, **kw):
     return err_gpu, err_c
 
 
-# (src h, w) -> (dst h, w): both passes wide; tiles of 128 lines and groups of
-# 16 outputs partial, band ends clamped, a plane narrower than one tile
+# (src h, w) -> (dst h, w): both passes wide; column tiles of 256 and output
+# tiles of 64 partial, band ends clamped, bands too wide for the tcgen05 form
+# (> 160 taps: the mma.sync form runs)
 SHAPES = [((1080, 1920), (67, 120)), ((517, 333), (31, 29)), ((600, 100), (9, 6)), ((1600, 1600), (16, 16)),
-          ((130, 260), (9, 17))]
+          ((130, 260), (9, 17)),
+          ((517, 100), (31, 7)),     # 100 columns: one partial 256-column tile
+          ((1080, 300), (54, 15))]   # 20x Lanczos-4: 160 taps, the widest band the tcgen05 form takes
 
 
 @pytest.mark.parametrize("case", range(len(SHAPES)))
