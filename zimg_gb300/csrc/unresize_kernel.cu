@@ -119,12 +119,96 @@ __device__ __forceinline__ void substitute(const UnresizeTables &t, float *p, pt
 	}
 }
 
-__global__ void __launch_bounds__(kThreads)
+// Horizontal substitutions, one warp per 32 lines: a line's values are
+// contiguous, so a thread per line would read 32 rows per warp load. The warp
+// moves tiles of 32 lines x 32 values through shared memory instead (one
+// 128-byte row per load instruction, the next two tiles in flight in
+// registers), and each lane runs its own line's recurrence on the tile;
+// the arithmetic and its order are those of substitute().
+constexpr int kTile = 32;
+
+struct HTile {
+	float v[kTile];  // this lane's column of the tile: rows 0 .. 31
+};
+
+__device__ __forceinline__ void load_tile(HTile &r, const char *dst, ptrdiff_t ds, unsigned line0, unsigned lines,
+                                          unsigned col0, unsigned n)
+{
+	const unsigned lane = threadIdx.x & 31, c = col0 + lane;
+#pragma unroll
+	for (int i = 0; i < kTile; ++i)
+		r.v[i] = (line0 + i < lines && c < n)
+		             ? reinterpret_cast<const float *>(dst + static_cast<ptrdiff_t>(line0 + i) * ds)[c]
+		             : 0.0f;
+}
+
+__global__ void __launch_bounds__(32)
 unresize_subst_h(UnresizeTables t, unsigned lines, char *__restrict__ dst, ptrdiff_t ds)
 {
-	const unsigned line = blockIdx.x * kThreads + threadIdx.x;
-	if (line < lines)
-		substitute(t, reinterpret_cast<float *>(dst + static_cast<ptrdiff_t>(line) * ds), 1, t.orig);
+	__shared__ float tile[kTile][kTile + 1];
+	const unsigned lane = threadIdx.x & 31, line0 = blockIdx.x * kTile;
+	const unsigned n = t.orig, tiles = (n + kTile - 1) / kTile;
+	const bool mine = line0 + lane < lines;
+	// one pass over the tiles, forward (z) or backward (w); row `lane` of a
+	// tile is this lane's line
+	auto pass = [&](bool forward) {
+		HTile a, b;
+		float carry = 0.0f;
+		const unsigned first = forward ? 0 : tiles - 1;
+		load_tile(a, dst, ds, line0, lines, first * kTile, n);
+		if (tiles > 1)
+			load_tile(b, dst, ds, line0, lines, (forward ? first + 1 : first - 1) * kTile, n);
+		for (unsigned k = 0; k < tiles; ++k) {
+			const unsigned j = forward ? k : tiles - 1 - k;
+			const unsigned col0 = j * kTile, cnt = min(static_cast<unsigned>(kTile), n - col0);
+#pragma unroll
+			for (int i = 0; i < kTile; ++i)
+				tile[i][lane] = a.v[i];
+			a = b;
+			if (k + 2 < tiles)
+				load_tile(b, dst, ds, line0, lines, (forward ? j + 2 : j - 2) * kTile, n);
+			__syncwarp();
+			if (mine) {
+				// whole tiles unrolled, so that the coefficient loads run ahead of the chain
+				if (forward && cnt == kTile) {
+#pragma unroll
+					for (int c = 0; c < kTile; ++c) {
+						carry = __fmul_rn(__fsub_rn(tile[lane][c], __fmul_rn(__ldg(t.lu_c + col0 + c), carry)),
+						                  __ldg(t.lu_l + col0 + c));
+						tile[lane][c] = carry;
+					}
+				} else if (forward) {
+					for (unsigned c = 0; c < cnt; ++c) {
+						carry = __fmul_rn(__fsub_rn(tile[lane][c], __fmul_rn(__ldg(t.lu_c + col0 + c), carry)),
+						                  __ldg(t.lu_l + col0 + c));
+						tile[lane][c] = carry;
+					}
+				} else if (cnt == kTile) {
+#pragma unroll
+					for (int c = kTile - 1; c >= 0; --c) {
+						carry = __fsub_rn(tile[lane][c], __fmul_rn(__ldg(t.lu_u + col0 + c), carry));
+						tile[lane][c] = carry;
+					}
+				} else {
+					for (unsigned c = cnt; c-- > 0;) {
+						carry = __fsub_rn(tile[lane][c], __fmul_rn(__ldg(t.lu_u + col0 + c), carry));
+						tile[lane][c] = carry;
+					}
+				}
+			}
+			__syncwarp();
+			const unsigned cc = col0 + lane;
+			if (cc < n) {
+#pragma unroll
+				for (int i = 0; i < kTile; ++i)
+					if (line0 + i < lines)
+						reinterpret_cast<float *>(dst + static_cast<ptrdiff_t>(line0 + i) * ds)[cc] = tile[i][lane];
+			}
+			__syncwarp();
+		}
+	};
+	pass(true);
+	pass(false);
 }
 
 __global__ void __launch_bounds__(kThreads)
@@ -149,7 +233,7 @@ cudaError_t launch_unresize(const UnresizeTables &t, bool horizontal, unsigned l
 	if (horizontal) {
 		unresize_dot_h<<<dim3((t.orig + kThreads - 1) / kThreads, std::min(n, kGridY)), kThreads, 0, stream>>>(
 			t, n, s, src_stride, d, dst_stride);
-		unresize_subst_h<<<(n + kThreads - 1) / kThreads, kThreads, 0, stream>>>(t, n, d, dst_stride);
+		unresize_subst_h<<<(n + kTile - 1) / kTile, 32, 0, stream>>>(t, n, d, dst_stride);
 	} else {
 		unresize_dot_v<<<dim3((n + kThreads - 1) / kThreads, std::min(t.orig, kGridY)), kThreads, 0, stream>>>(
 			t, n, s, src_stride, d, dst_stride);
