@@ -7,8 +7,10 @@
 // so one thread per output sample computes them (k in zimg's order) into the
 // pass's output plane. The substitutions are recurrences along the line
 // (horizontal pass) or down the column (vertical pass): one thread each,
-// rewriting the plane in place, with the next group of inputs loaded before
-// the dependent steps so that memory latency overlaps the chain.
+// rewriting the plane in place, with the next inputs loaded before the
+// dependent steps so that memory latency overlaps the chain (down a column in
+// groups of kAhead values; along lines a warp moves tiles of 32 lines x 32
+// values through shared memory).
 #include "unresize.h"
 
 #include <algorithm>
