@@ -545,11 +545,12 @@ def run_unresize(args):
     u = zg.UnresizeConversion(1920, 1080).set_orig_width(1280).set_orig_height(720).create()
     srcs = [torch.from_numpy(protos[i % 2]).cuda() for i in range(len(planes))]
     dsts = [torch.empty((720, 1280), dtype=torch.float32, device="cuda") for _ in planes]
-    # the planes are independent: four streams (each with its own scratch),
-    # forked from and joined to the timed one, run them side by side
-    side = [torch.cuda.Stream() for _ in range(4)]
+    # the planes are independent: each plane is a chain of four launches whose
+    # substitutions occupy a few dozen SMs, so eight streams (each with its own
+    # scratch), forked from and joined to the timed one, run planes side by side
+    nside = 8
+    side = [torch.cuda.Stream() for _ in range(nside)]
     tmps = [torch.empty(max(u.tmp_size, 1), dtype=torch.uint8, device="cuda") for _ in side]
-    tmp = tmps[0]
     stream = torch.cuda.Stream()
 
     def step():
@@ -557,7 +558,7 @@ def run_unresize(args):
         for sd in side:
             sd.wait_stream(cur)
         for k, (s_, d_) in enumerate(zip(srcs, dsts)):
-            u.process(s_, d_, tmps[k % 4], stream=side[k % 4])
+            u.process(s_, d_, tmps[k % nside], stream=side[k % nside])
         for sd in side:
             cur.wait_stream(sd)
     with torch.cuda.stream(stream):
@@ -595,11 +596,18 @@ def run_unresize(args):
         hdst = [torch.empty((720, 1280), dtype=torch.float32).pin_memory() for _ in range(n_e2e)]
 
         def e2e_step():
-            with torch.cuda.stream(stream):
-                for i in range(n_e2e):
+            # each plane's upload, conversion and download on its own stream
+            cur = stream
+            for sd in side:
+                sd.wait_stream(cur)
+            for i in range(n_e2e):
+                sd = side[i % nside]
+                with torch.cuda.stream(sd):
                     srcs[i].copy_(hsrc[i], non_blocking=True)
-                    u.process(srcs[i], dsts[i], tmp, stream=stream)
+                    u.process(srcs[i], dsts[i], tmps[i % nside], stream=sd)
                     hdst[i].copy_(dsts[i], non_blocking=True)
+            for sd in side:
+                cur.wait_stream(sd)
         e2e_step()
         torch.cuda.synchronize()
         k = max(3, args.steps // 4)
