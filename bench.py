@@ -428,11 +428,20 @@ def run_depth(args):
         srcs.append(torch.from_numpy(proto[pl["plane"]]).cuda())
         dsts.append(torch.empty((pl["h"], pl["w"]), dtype=torch.uint8, device="cuda"))
     stream = torch.cuda.Stream()
+    # planes are independent: four streams forked from and joined to the timed
+    # one, so that one launch's last wave overlaps the next plane's first
+    nside = 4
+    side = [torch.cuda.Stream() for _ in range(nside)]
     torch.cuda.synchronize()
 
     def step():
-        for c, s, d in zip(convs, srcs, dsts):
-            c.process(s, d, stream=stream)
+        cur = torch.cuda.current_stream()
+        for sd in side:
+            sd.wait_stream(cur)
+        for k, (c, s, d) in enumerate(zip(convs, srcs, dsts)):
+            c.process(s, d, stream=side[k % nside])
+        for sd in side:
+            cur.wait_stream(sd)
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
             step()
@@ -468,17 +477,23 @@ def run_depth(args):
 
     e2e = None
     if not args.no_e2e:
-        # the public API with host buffers: pinned planes in, the launch, planes out, per plane on one stream
+        # the public API with host buffers: pinned planes in, the launch, planes out; each
+        # plane on one of the side streams, so that uploads and downloads overlap
         n_e2e = min(len(planes), 12)
         hsrc = [srcs[i].cpu().pin_memory() for i in range(n_e2e)]
         hdst = [torch.empty(dsts[i].shape, dtype=torch.uint8).pin_memory() for i in range(n_e2e)]
 
         def e2e_step():
-            with torch.cuda.stream(stream):
-                for i in range(n_e2e):
+            for sd in side:
+                sd.wait_stream(stream)
+            for i in range(n_e2e):
+                sd = side[i % nside]
+                with torch.cuda.stream(sd):
                     srcs[i].copy_(hsrc[i], non_blocking=True)
-                    convs[i].process(srcs[i], dsts[i], stream=stream)
+                    convs[i].process(srcs[i], dsts[i], stream=sd)
                     hdst[i].copy_(dsts[i], non_blocking=True)
+            for sd in side:
+                stream.wait_stream(sd)
         for _ in range(2):
             e2e_step()
         torch.cuda.synchronize()
