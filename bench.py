@@ -298,7 +298,8 @@ def run_ours(args):
         hsrc = [srcs[i].cpu().pin_memory() for i in range(n_e2e)]
         hdst = [torch.empty(dsts[i].shape, dtype=dsts[i].dtype).pin_memory() for i in range(n_e2e)]
         # the public host-buffer API: chunked, copies overlapping the launches
-        pipe = zg.HostPipeline(convs[:n_e2e], chunks=8, autotune=not args.engine and not args.no_autotune)
+        pipe = zg.HostPipeline(convs[:n_e2e], chunks=args.e2e_chunks,
+                               autotune=not args.engine and not args.no_autotune)
         for _ in range(3):
             pipe.run(hsrc, hdst)
         torch.cuda.synchronize()
@@ -769,6 +770,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--e2e-planes", type=int, default=48)
+    ap.add_argument("--e2e-chunks", type=int, default=8, help="sub-batches of the host pipeline")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--engine", default=None, choices=["auto", "cuda", "tensor"],
                     help="override every job's engine (cuda = the plain CUDA-core kernels)")
