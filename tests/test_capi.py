@@ -138,3 +138,14 @@ def test_unresize_create_errors(lib):
     assert lib.zg_unresize_create(C.byref(p), C.byref(h)) == 3076  # RESAMPLING_NOT_AVAILABLE
     p = capi.UnresizeParams(64, 48, 0, 24, 0.0, 0.0)
     assert lib.zg_unresize_create(C.byref(p), C.byref(h)) == 2050  # INVALID_IMAGE_SIZE
+
+
+def test_wide_forms_used_starts_empty(lib):
+    """zg_wide_forms_used is per host thread: a thread that enqueued no wide
+    pass reads 0, with or without reset."""
+    import threading
+    out = []
+    t = threading.Thread(target=lambda: out.extend([lib.zg_wide_forms_used(0), lib.zg_wide_forms_used(1)]))
+    t.start()
+    t.join()
+    assert out == [0, 0]
