@@ -175,13 +175,26 @@ ZG_API zg_error_code zg_unresize_get_tmp_size(const zg_unresize *u, size_t *out)
 ZG_API zg_error_code zg_unresize_process(const zg_unresize *u, const void *src, ptrdiff_t src_stride, void *dst,
                                          ptrdiff_t dst_stride, void *tmp, zg_stream stream);
 
-/* Health of the pipelined kernels on the current device: 0, or the cause of
- * the first bounded wait that ran out inside one (1: a group's copies never
- * landed, 2: a buffer was never released, 3: a ring too small for a group).
- * Nonzero means a library fault, not a caller error; the outputs of the
- * launches involved are not valid. With reset != 0 the word is cleared.
- * No zimg counterpart (zimg has no asynchronous device work). */
+/* Health of the pipelined kernels on the current device: 0, or which
+ * bounded wait ran out inside one. Bits 0-7: the chained u16 kernel's TMA
+ * form (1: a group's copies never landed, 2: a buffer was never released,
+ * 3: a ring too small for a group). Bits 8-15: the tcgen05 FP32 wide kernel,
+ * 16 + cause (17: converter warps, tile or operand buffer; 18: producer,
+ * stage never released; 19: MMA lane, operands, accumulator or completion;
+ * 20: epilogue, accumulator never complete). -1 when the device words cannot
+ * be read. Nonzero means a library fault, not a caller error; the outputs of
+ * the launches involved are not valid. With reset != 0 the words are
+ * cleared. No zimg counterpart (zimg has no asynchronous device work). */
 ZG_API int zg_pipeline_status(int reset);
+
+/* Test hook for the bounded waits of the chained u16 kernel's TMA form
+ * (current device): from the next launch on, CTA 0's producer skips group
+ * drop_group of its pipeline without arming that group's stage (-1: none),
+ * and every wait of that kernel gives up after wait_ns nanoseconds (0: the
+ * default 0.25 s). A consumer wait then runs out, the kernel returns and
+ * zg_pipeline_status reports cause 1. Returns 0, or -1 when the device
+ * words cannot be written. Not for production use; no zimg counterpart. */
+ZG_API int zg_debug_pipeline_fault(int drop_group, unsigned long long wait_ns);
 
 /* The forms that ran the FP32 wide-filter passes enqueued by this host
  * thread since the last reset: bit 0 the mma.sync form (3xTF32 fragments in

@@ -109,6 +109,7 @@ _P = C.c_void_p
 SIGNATURES = [
     ("zg_get_last_error", C.c_int, [C.c_char_p, C.c_size_t]),
     ("zg_pipeline_status", C.c_int, [C.c_int]),
+    ("zg_debug_pipeline_fault", C.c_int, [C.c_int, C.c_ulonglong]),
     ("zg_wide_forms_used", C.c_int, [C.c_int]),
     ("zg_unresize_create", C.c_int, [C.POINTER(UnresizeParams), C.POINTER(C.c_void_p)]),
     ("zg_unresize_free", None, [C.c_void_p]),

@@ -200,7 +200,14 @@ int zg_pipeline_status(int reset)
 {
 	const int chain = chain_tma_pipeline_error(reset != 0);
 	const int wide = wide_umma_pipeline_error(reset != 0);
-	return chain ? chain : wide;
+	if (chain < 0 || wide < 0)
+		return -1;
+	return (chain & 0xFF) | (wide ? (16 + wide) << 8 : 0);
+}
+
+int zg_debug_pipeline_fault(int drop_group, unsigned long long wait_ns)
+{
+	return chain_tma_set_fault(drop_group, wait_ns);
 }
 
 zg_error_code zg_get_last_error(char *err_msg, size_t n)

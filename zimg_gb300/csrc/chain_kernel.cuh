@@ -37,24 +37,26 @@ using mma_detail::pack_u16x2;
 using mma_detail::u16x2_to_centred_h2;
 using mma_detail::wrap;
 
-// CTA shape: H-first conversions (upscales) run 4-warp CTAs, four per SM;
-// V-first ones (downscales, wider windows and more registers) 8-warp CTAs,
-// two per SM.
-__host__ __device__ constexpr int warps_per_cta(bool h_first)
+// CTA shape: 7 computing warps, two CTAs per SM. The strip of a CTA (7 warps'
+// tiles) is also the strip of the warp-specialised TMA form
+// (chain_tma_kernel.cuh), whose CTAs add one producer warp: 8 warps at up to
+// 128 registers each, two CTAs per SM.
+__host__ __device__ constexpr int warps_per_cta(bool /*h_first*/)
 {
-	return h_first ? 4 : 8;
+	return 7;
 }
-constexpr int kMaxWarps = 8;
+constexpr int kMaxWarps = 7;
 constexpr int kTileW = 16;                 // output columns of one tile (one m16 block)
 
-// Tiles per warp: two share the loop, the loads and the barriers, where the
-// tap fragments of two tiles fit in registers next to everything else.
+// Tiles per warp: several share the loop, the loads and the barriers, as far
+// as their tap fragments fit in registers next to everything else: four for
+// 16-line, 16-column windows (the 2x upscales), two for other small windows.
 __host__ __device__ constexpr int tiles_per_warp(int kv, int kh)
 {
-	return (kv + kh <= 3 || kh == 1) ? 2 : 1;
+	return (kv == 1 && kh == 1) ? 4 : ((kv + kh <= 3 || kh == 1) ? 2 : 1);
 }
 constexpr int kStageBytes = 48;            // staged row: 16 u16 + pad (stmatrix rows without bank conflicts)
-constexpr int kMaxTilesPerWarp = 2;
+constexpr int kMaxTilesPerWarp = 4;
 constexpr int kTileStage = 16 * kStageBytes + 32;       // a warp's staged tiles lie 32 mod 128 bytes apart
 constexpr int kWarpStage = kMaxTilesPerWarp * kTileStage;
 
@@ -72,6 +74,28 @@ __device__ __forceinline__ void stsm_x4_trans(void *p, uint32_t r0, uint32_t r1,
 	asm volatile("stmatrix.sync.aligned.m8n8.x4.trans.shared.b16 [%0], {%1, %2, %3, %4};\n" ::"r"(s), "r"(r0),
 	             "r"(r1), "r"(r2), "r"(r3)
 	             : "memory");
+}
+
+// Stage reads and global stores of a warp's staged tiles, one 16-byte chunk
+// per lane and store: with four tiles a store covers 4 rows x 128 bytes (row
+// lane >> 3, tile (lane >> 1) & 3, half lane & 1); with two, 8 rows x 64
+// bytes (rows q and q + 4, q = lane >> 3, tile (lane >> 1) & 1); with one,
+// 16 rows x 32 bytes (rows q', q' + 2, q' + 4, q' + 6 of phase q). The staged
+// tiles lie 32 mod 128 bytes apart, so the 8 lanes of a phase always read 8
+// different 16-byte bank groups.
+__host__ __device__ constexpr int store_rows(int tiles)
+{
+	return tiles == 4 ? 4 : (tiles == 2 ? 8 : 16);
+}
+__device__ __forceinline__ int store_row(int tiles, int lane)
+{
+	return tiles == 4 ? (lane >> 3)
+	                  : (tiles == 2 ? (lane >> 3) + 4 * ((lane >> 2) & 1)
+	                                : ((lane >> 3) & 1) + 8 * (lane >> 4) + 2 * ((lane >> 1) & 3));
+}
+__device__ __forceinline__ int store_tile(int tiles, int lane)
+{
+	return tiles == 4 ? (lane >> 1) & 3 : (tiles == 2 ? (lane >> 1) & 1 : 0);
 }
 
 struct Item {
@@ -353,7 +377,7 @@ __device__ __forceinline__ void store_chunk(const Item &it, const char *ld_addr,
 // (vbase_off). A warp may still compute group k while others issue the loads
 // of group k + 1 + depth: the planner sizes the ring and the slots for that.
 template <bool H_FIRST, int KV, int KH>
-__global__ void __launch_bounds__(warps_per_cta(H_FIRST) * 32, H_FIRST ? 4 : 2)
+__global__ void __launch_bounds__(warps_per_cta(H_FIRST) * 32, 2)
 chain_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, const __grid_constant__ FusedJob single,
              const __grid_constant__ SmemLayout L)
 {
@@ -373,16 +397,11 @@ chain_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 	constexpr int kStripTiles = kWarps * kTilesPerWarp;
 	// stmatrix address of this lane
 	char *st_addr = stage + (((lane >> 4) << 3) + (lane & 7)) * kStageBytes + ((lane >> 3) & 1) * 16;
-	// Stage reads and global stores, one 16-byte chunk per lane. Two tiles per
-	// warp: one store covers 8 rows x 64 bytes (chunk lane & 3 of rows q and
-	// q + 4, q = lane >> 3); one tile: 16 rows x 32 bytes (rows q', q' + 2,
-	// q' + 4, q' + 6 of phase q). Either way the 8 lanes of a phase read 8
-	// different 16-byte bank groups.
-	constexpr int kStoreRows = kTilesPerWarp == 2 ? 8 : 16;
+	// Stage reads and global stores, one 16-byte chunk per lane (store_map).
+	constexpr int kStoreRows = store_rows(kTilesPerWarp);
 	constexpr int kStores = 16 / kStoreRows;
-	const int st_row = kTilesPerWarp == 2 ? (lane >> 3) + 4 * ((lane >> 2) & 1)
-	                                      : ((lane >> 3) & 1) + 8 * (lane >> 4) + 2 * ((lane >> 1) & 3);
-	const int st_tile = kTilesPerWarp == 2 ? (lane >> 1) & 1 : 0;
+	const int st_row = store_row(kTilesPerWarp, lane);
+	const int st_tile = store_tile(kTilesPerWarp, lane);
 	const char *ld_addr = stage + st_tile * kTileStage + st_row * kStageBytes + (lane & 1) * 16;
 
 	const int S = L.depth + 2;  // fragment slots in rotation

@@ -78,11 +78,11 @@ const void *chain_tma_kernel_ptr(int variant)
 
 bool chain_tma_enabled()
 {
-	// opt-in: on GB300 it measured level with the cp.async form on FHD->UHD
-	// and a few per cent slower on mixed batches
+	// the default where the source planes admit a tensor map; ZG_CHAIN_TMA=0
+	// keeps the cp.async form
 	static const bool on = [] {
 		const char *e = std::getenv("ZG_CHAIN_TMA");
-		return e && e[0] == '1';
+		return !(e && e[0] == '0');
 	}();
 	return on;
 }
@@ -102,13 +102,19 @@ bool chain_tma_layout(const FusedPlan *const *plans, int n, SmemLayout *out)
 	}
 	auto a16 = [](size_t x) { return static_cast<int>((x + 15) / 16 * 16); };
 	SmemLayout L{};
-	// box rows of 16 mod 32 bytes, as the cp.async form's lines
-	L.pitch = (max_pxa + 15) / 16 * 16 + 8;
+	// box rows of 16 mod 32 bytes (8 mod 16 samples) covering the widest
+	// window: 4-byte fragment loads of 8 lines x 4 pairs hit 32 different
+	// banks, the 8 rows of an ldmatrix phase 8 different 16-byte bank groups
+	L.pitch = std::max(8, (max_pxa - 8 + 15) / 16 * 16 + 8);
 	if (L.pitch > kMaxBoxW)
 		return false;
-	// blocks covering any window span of `in` lines, block-rounded at both ends
-	const int blocks = (in + 2 * (chain_detail::kBlockLines - 1)) / chain_detail::kBlockLines + 1;
-	L.in_rows = blocks * chain_detail::kBlockLines;
+	// blocks covering any window span of `in` lines, block-rounded at both
+	// ends, rounded up to a power of two (ring lines under a mask)
+	int blocks = (in + 2 * (chain_detail::kBlockLines - 1)) / chain_detail::kBlockLines + 1;
+	int nb = 1;
+	while (nb < blocks)
+		nb *= 2;
+	L.in_rows = nb * chain_detail::kBlockLines;
 	L.depth = depth;
 	L.ring_rows = depth + 2;  // pipeline stages
 	L.stage_rows = 1;
@@ -121,7 +127,7 @@ bool chain_tma_layout(const FusedPlan *const *plans, int n, SmemLayout *out)
 	off += a16(static_cast<size_t>(L.ring_rows) * kv * 2 * 32 * 16);
 	L.tile_off = off;
 	L.tile_pitch = chain_detail::kStageBytes / 2;
-	off += a16(static_cast<size_t>(chain_detail::kMaxWarps) * chain_detail::kWarpStage);
+	off += a16(static_cast<size_t>(chain_detail::kWsWarps) * chain_detail::kWarpStage);
 	L.vbase_off = off;
 	off += a16(static_cast<size_t>(groups) * 4);
 	L.stage_off = off;  // full and empty mbarriers
@@ -197,6 +203,14 @@ cudaError_t launch_chain_tma(int variant, const FusedJob *jobs, int num_jobs, in
 	grid = std::max(1, std::min(grid, total_items));
 	return cudaLaunchKernel(k, dim3(grid), dim3(tma_threads(variant)), args, static_cast<size_t>(L.total_bytes),
 	                        stream);
+}
+
+int chain_tma_set_fault(int drop_group, unsigned long long wait_ns)
+{
+	if (cudaMemcpyToSymbol(chain_detail::g_chain_drop_group, &drop_group, sizeof(drop_group)) != cudaSuccess ||
+	    cudaMemcpyToSymbol(chain_detail::g_chain_wait_ns, &wait_ns, sizeof(wait_ns)) != cudaSuccess)
+		return -1;
+	return 0;
 }
 
 int chain_tma_pipeline_error(bool reset)

@@ -1,27 +1,35 @@
-// Chained tensor-core u16 kernel, TMA pipeline form.
+// Chained tensor-core u16 kernel, warp-specialised TMA form.
 //
-// Arithmetic, tiles and stores are those of chain_kernel.cuh. What differs is
-// how source lines and tap fragments reach shared memory and how the warps
-// stay in step:
+// Arithmetic is that of chain_kernel.cuh (re-centred fp16 samples, int16
+// taps split into two exact fp16 halves, fp32 accumulators that the planner
+// proved hold exact integers, zimg's rounding and clamping per pass,
+// resize_impl.cpp:31-59,78-95), and so are the 16x16 output tiles, the tap
+// fragments and the strip plan. What differs is the feeding and the control
+// flow, cut to the few instructions a tile needs:
 //
-//  - Source lines arrive as 2-D tensor copies (cp.async.bulk.tensor) of
-//    16-line blocks of the strip's column window, the vertical tap fragments
-//    of a group as one bulk copy. Block b of the plane lands in ring block
-//    b mod NB, so line l sits in ring line l mod (16 NB) as in the cp.async
-//    form; every block starts on a 128-byte boundary (16 lines x a pitch of
-//    16 mod 32 bytes).
-//  - A producer warp (one lane) issues the copies; the consumer warps only
-//    compute. Group g of the CTA's pipeline uses stage s = g mod NS: a "full"
-//    mbarrier whose transaction count covers the group's copies, and an
-//    "empty" mbarrier on which each consumer warp arrives once it has read
-//    the group. No CTA-wide barrier runs per group: the producer runs ahead
-//    until a ring block or fragment slot it is about to overwrite is still
-//    being read, and consumer warps drift apart as far as that allows.
-//  - Source blocks wholly below the plane are not copied: the issuing thread
+//  - One producer warp (one lane) brings every group's data into shared
+//    memory: 16-line blocks of the strip's source columns as 2-D tensor
+//    copies (cp.async.bulk.tensor) into a ring of 2^n blocks, and the group's
+//    vertical tap fragments as one bulk copy into a stage. Group g of the
+//    CTA's pipeline uses stage g mod NS: a "full" mbarrier whose transaction
+//    count covers the group's copies, and an "empty" mbarrier on which every
+//    consumer warp arrives once it has read the group.
+//  - Seven consumer warps only compute and store: per group, one wait, the
+//    vertical fragments, the tiles of the warp (one or two of 16 columns),
+//    one arrive, the stores. Line addresses are ring offsets under a mask,
+//    computed once per group for all tiles; whether a group reuses the
+//    previous group's horizontal products (its window starts 8 lines lower)
+//    is a warp-uniform branch between two unrolled bodies.
+//  - Rounding is one paired fp32 multiply-add per two samples and one
+//    s16x2 minimum with relu (pack_u16x2).
+//  - Source blocks wholly below the plane are not copied: the producer
 //    writes them as zero lines before it arrives on the group's barrier.
-//  - Every mbarrier wait is bounded. A wait that runs out records its cause in
-//    g_chain_pipeline_error, the CTA stops, and the issuing thread first waits
-//    (again bounded) for the copies it still has in flight.
+//  - Every mbarrier wait is bounded (g_chain_wait_ns, default 0.25 s). A wait
+//    that runs out records its cause in g_chain_pipeline_error, the CTA
+//    stops, and the producer first waits (again bounded) for the copies it
+//    still has in flight. A test hook (g_chain_drop_group) makes CTA 0's
+//    producer skip one group without arming its stage, so that a test can
+//    see a consumer wait run out and the kernel return.
 #pragma once
 
 #include <cuda.h>
@@ -33,32 +41,236 @@ namespace zg {
 namespace chain_detail {
 
 constexpr int kBlockLines = 16;                     // source lines per tensor copy
+constexpr int kWsWarps = warps_per_cta(true);      // consumer warps per CTA
 
-// Nonzero after a pipeline wait ran out: 1 = group data never arrived, 2 = a
-// buffer was never released, 3 = ring too small for one group (planner error).
+// Nonzero after a pipeline wait ran out: 1 = a group's copies never landed,
+// 2 = a buffer was never released, 3 = ring too small for one group.
 __device__ int g_chain_pipeline_error;
+// Wait limit in ns (0: kWaitNs) and the test hook described above (-1: off).
+__device__ unsigned long long g_chain_wait_ns;
+__device__ int g_chain_drop_group = -1;
 
-// Kernel. Shared memory (SmemLayout, from a 128-byte aligned base): ring of
-// NB = in_rows / kBlockLines blocks of source lines (in_off), NS = ring_rows
-// slots of vertical tap fragments (vcoef_off), one staging tile pair per
-// consumer warp (tile_off), the item's group bases (vbase_off), NS full and
-// NS empty mbarriers (stage_off).
-// Threads of a CTA: the consumer warps of the cp.async form plus one
-// producer warp.
-__host__ __device__ constexpr int tma_threads(bool h_first)
+__host__ __device__ constexpr int tma_threads(bool /*h_first*/)
 {
-	return (warps_per_cta(h_first) + 1) * 32;
+	return (kWsWarps + 1) * 32;
 }
 
+__device__ __forceinline__ bool mbar_wait_for(uint64_t *bar, unsigned parity, unsigned long long limit)
+{
+	const unsigned a = smem_addr(bar);
+	unsigned long long t0 = 0;
+	for (unsigned i = 0;; ++i) {
+		unsigned done;
+		asm volatile("{\n"
+		             "  .reg .pred p;\n"
+		             "  mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+		             "  selp.u32 %0, 1, 0, p;\n"
+		             "}\n"
+		             : "=r"(done)
+		             : "r"(a), "r"(parity)
+		             : "memory");
+		if (done)
+			return true;
+		if ((i & 15) == 0) {
+			const unsigned long long t = global_ns();
+			if (i == 0)
+				t0 = t;
+			else if (t - t0 > limit)
+				return false;
+		}
+	}
+}
+
+__device__ __forceinline__ uint32_t lds32(const char *p)
+{
+	return *reinterpret_cast<const uint32_t *>(p);
+}
+
+// D = A * B + 8192 (all four accumulators), m16n8k16 f16 -> f32
+__device__ __forceinline__ void mma_init(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1, float c)
+{
+	asm("mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+	    "{%10, %10, %10, %10};\n"
+	             : "=f"(d[0]), "=f"(d[1]), "=f"(d[2]), "=f"(d[3])
+	             : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1), "f"(c));
+}
+
+// Accumulate both tap halves (hi, lo) of one 16x16 fragment pair; `first`
+// starts the accumulators at 8192.
+__device__ __forceinline__ void mma2(float (&d)[4], const uint4 &hi, const uint4 &lo, uint32_t b0, uint32_t b1,
+                                     bool first)
+{
+	const uint32_t ah[4] = { hi.x, hi.y, hi.z, hi.w };
+	const uint32_t al[4] = { lo.x, lo.y, lo.z, lo.w };
+	if (first)
+		mma_init(d, ah, b0, b1, 8192.0f);
+	else
+		mma16816(d, ah, b0, b1);
+	mma16816(d, al, b0, b1);
+}
+
+struct Epi {
+	float magic;
+	uint32_t pmax2, bias_h2;
+	__device__ __forceinline__ uint32_t pack(const float (&a)[4], int i) const
+	{
+		return pack_u16x2(a[i], a[i + 1], magic, pmax2);
+	}
+	__device__ __forceinline__ uint32_t pack_centre(const float (&a)[4], int i) const
+	{
+		return u16x2_to_centred_h2(pack(a, i), bias_h2);
+	}
+	__device__ __forceinline__ uint32_t centre(uint32_t q) const
+	{
+		return u16x2_to_centred_h2(q, bias_h2);
+	}
+};
+
+// H first, horizontal stage: the warp's T tiles of one group, up to the
+// vertical pass's operands bv. roff[kv][h]: byte offsets in the ring of lines
+// gid + 8h of window block kv; colb[j]: tile j's byte offset of its window's
+// input column 2tig in a line. REUSE (KV == 1 only): lines 0-7 of the window
+// are the previous group's lines 8-15, whose products sit in carry. Each step
+// runs over all tiles before the next, so that the tiles' dependency chains
+// overlap in issue order.
+template <int KV, int KH, int T, bool REUSE>
+__device__ __forceinline__ void hfirst_h(const char *ring, const uint32_t (&roff)[KV][2], const uint32_t (&colb)[T],
+                                         const uint4 (&ah)[T][KH][2], uint32_t (&carry)[T][2],
+                                         uint32_t (&bv)[T][KV][2][2], const Epi &e)
+{
+#pragma unroll
+	for (int kv = 0; kv < KV; ++kv) {
+		float dh0[T][4], dh1[T][4];  // window lines 0-7, 8-15 of block kv
+#pragma unroll
+		for (int ks = 0; ks < KH; ++ks) {
+			uint32_t b[T][4];
+#pragma unroll
+			for (int j = 0; j < T; ++j) {
+				const char *r0 = ring + roff[kv][0] + colb[j] + ks * 32;
+				const char *r1 = ring + roff[kv][1] + colb[j] + ks * 32;
+				if (!REUSE) {
+					b[j][0] = lds32(r0);
+					b[j][1] = lds32(r0 + 16);
+				}
+				b[j][2] = lds32(r1);
+				b[j][3] = lds32(r1 + 16);
+			}
+#pragma unroll
+			for (int j = 0; j < T; ++j) {
+				if (!REUSE)
+					mma2(dh0[j], ah[j][ks][0], ah[j][ks][1], e.centre(b[j][0]), e.centre(b[j][1]), ks == 0);
+				mma2(dh1[j], ah[j][ks][0], ah[j][ks][1], e.centre(b[j][2]), e.centre(b[j][3]), ks == 0);
+			}
+		}
+		// Dh (out col gid / gid+8, lines 2tig..) -> V operands (k = lines, n = out col)
+#pragma unroll
+		for (int j = 0; j < T; ++j) {
+			if (REUSE) {
+				bv[j][kv][0][0] = carry[j][0];
+				bv[j][kv][1][0] = carry[j][1];
+			} else {
+				bv[j][kv][0][0] = e.pack_centre(dh0[j], 0);
+				bv[j][kv][1][0] = e.pack_centre(dh0[j], 2);
+			}
+			bv[j][kv][0][1] = e.pack_centre(dh1[j], 0);
+			bv[j][kv][1][1] = e.pack_centre(dh1[j], 2);
+		}
+	}
+	if (KV == 1) {
+#pragma unroll
+		for (int j = 0; j < T; ++j) {
+			carry[j][0] = bv[j][0][0][1];
+			carry[j][1] = bv[j][0][1][1];
+		}
+	}
+}
+
+// H first, vertical stage: the vertical products of the warp's tiles, two
+// tiles at a time, each pair rounded and staged (row-major 8x8 blocks: out
+// row gid / gid+8, out cols 2tig..) before the next.
+template <int KV, int T>
+__device__ __forceinline__ void hfirst_v(const uint32_t (&bv)[T][KV][2][2], const uint4 (&av)[KV][2], char *st_addr,
+                                         const Epi &e)
+{
+	constexpr int P = T < 2 ? T : 2;
+#pragma unroll
+	for (int j0 = 0; j0 < T; j0 += P) {
+		float dv0[P][4], dv1[P][4];  // out cols 0-7, 8-15
+#pragma unroll
+		for (int kv = 0; kv < KV; ++kv) {
+#pragma unroll
+			for (int q = 0; q < P; ++q) {
+				mma2(dv0[q], av[kv][0], av[kv][1], bv[j0 + q][kv][0][0], bv[j0 + q][kv][0][1], kv == 0);
+				mma2(dv1[q], av[kv][0], av[kv][1], bv[j0 + q][kv][1][0], bv[j0 + q][kv][1][1], kv == 0);
+			}
+		}
+#pragma unroll
+		for (int q = 0; q < P; ++q)
+			stsm_x4(st_addr + (j0 + q) * kTileStage, e.pack(dv0[q], 0), e.pack(dv1[q], 0), e.pack(dv0[q], 2),
+			        e.pack(dv1[q], 2));
+	}
+}
+
+// V first: the warp's T tiles of one group, staged as they finish. roff[kv]:
+// byte offset in the ring of this lane's ldmatrix row (line (lane & 7) +
+// ((lane >> 3) & 1) * 8 of window block kv); colb[j]: tile j's byte offset of
+// its column (lane >> 4) * 8.
+template <int KV, int KH, int T>
+__device__ __forceinline__ void vfirst_tiles(const char *ring, const uint32_t (&roff)[KV], const uint32_t (&colb)[T],
+                                             const uint4 (&ah)[T][KH][2], const uint4 (&av)[KV][2], char *st_addr,
+                                             const Epi &e)
+{
+	float dh0[T][4], dh1[T][4];  // out rows 0-7, 8-15
+#pragma unroll
+	for (int ks = 0; ks < KH; ++ks) {
+		float dv0[T][4], dv1[T][4];  // in cols 0-7, 8-15 of this k-step
+#pragma unroll
+		for (int kv = 0; kv < KV; ++kv) {
+			uint32_t b[T][4];
+#pragma unroll
+			for (int j = 0; j < T; ++j)
+				mma_detail::ldsm_x4_trans(b[j][0], b[j][1], b[j][2], b[j][3], ring + roff[kv] + colb[j] + ks * 32);
+#pragma unroll
+			for (int j = 0; j < T; ++j) {
+				mma2(dv0[j], av[kv][0], av[kv][1], e.centre(b[j][0]), e.centre(b[j][1]), kv == 0);
+				mma2(dv1[j], av[kv][0], av[kv][1], e.centre(b[j][2]), e.centre(b[j][3]), kv == 0);
+			}
+		}
+		// Dv (out row gid / gid+8, in cols 2tig..) -> H operands (k = in cols, n = out row)
+#pragma unroll
+		for (int j = 0; j < T; ++j) {
+			const uint32_t h00 = e.pack_centre(dv0[j], 0);
+			const uint32_t h01 = e.pack_centre(dv1[j], 0);
+			const uint32_t h10 = e.pack_centre(dv0[j], 2);
+			const uint32_t h11 = e.pack_centre(dv1[j], 2);
+			mma2(dh0[j], ah[j][ks][0], ah[j][ks][1], h00, h01, ks == 0);
+			mma2(dh1[j], ah[j][ks][0], ah[j][ks][1], h10, h11, ks == 0);
+		}
+	}
+	// (out col gid / gid+8, out rows 2tig..): transposed 8x8 blocks
+#pragma unroll
+	for (int j = 0; j < T; ++j)
+		stsm_x4_trans(st_addr + j * kTileStage, e.pack(dh0[j], 0), e.pack(dh0[j], 2), e.pack(dh1[j], 0),
+		              e.pack(dh1[j], 2));
+}
+
+// Kernel. Shared memory (SmemLayout, from a 128-byte aligned base): ring of
+// NB = in_rows / kBlockLines blocks of source lines, NB a power of two
+// (in_off); NS = ring_rows stages of vertical tap fragments (vcoef_off); one
+// staging tile pair per consumer warp (tile_off); the item's group bases
+// (vbase_off); NS full and NS empty mbarriers (stage_off).
 template <bool H_FIRST, int KV, int KH>
-__global__ void __launch_bounds__(tma_threads(H_FIRST), H_FIRST ? 4 : 2)
+__global__ void __launch_bounds__(tma_threads(H_FIRST), 2)
 chain_tma_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, const __grid_constant__ FusedJob single,
                  const __grid_constant__ SmemLayout L, const __grid_constant__ CUtensorMap single_map)
 {
 	extern __shared__ float4 smem4[];
 	__shared__ int abort_item;
-	// tensor copies land on 128-byte boundaries: align the layout's base
-	char *smem = reinterpret_cast<char *>((reinterpret_cast<uintptr_t>(smem4) + 127) & ~static_cast<uintptr_t>(127));
+	// tensor copies land on 128-byte boundaries: align the layout's base (by
+	// an offset from the shared array, so that every access through these
+	// pointers stays a shared-memory access)
+	char *smem = reinterpret_cast<char *>(smem4);
+	smem += (128u - (smem_addr(smem) & 127u)) & 127u;
 	char *ring = smem + L.in_off;
 	char *vslots = smem + L.vcoef_off;
 	int *vb = reinterpret_cast<int *>(smem + L.vbase_off);
@@ -67,27 +279,20 @@ chain_tma_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_item
 	uint64_t *empty = full + NS;
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	constexpr int kSlotBytes = KV * 2 * 32 * 16;
-	constexpr int kTilesPerWarp = tiles_per_warp(KV, KH);
-	constexpr int kWarps = warps_per_cta(H_FIRST);  // consumer warps; warp kWarps issues the copies
+	constexpr int T = tiles_per_warp(KV, KH);
 	constexpr int kThreads = tma_threads(H_FIRST);
-	constexpr int kStripTiles = kWarps * kTilesPerWarp;
-	const bool producer = warp == kWarps;
-	char *stage = smem + L.tile_off + (producer ? 0 : warp) * kWarpStage;
+	constexpr int kStripTiles = kWsWarps * T;
+	const bool producer = warp == kWsWarps;
 	const int IR = L.in_rows;
 	const int NB = IR / kBlockLines;
+	const unsigned line_mask = static_cast<unsigned>(IR - 1);
 	const int P = L.pitch * 2;
-	char *st_addr = stage + (((lane >> 4) << 3) + (lane & 7)) * kStageBytes + ((lane >> 3) & 1) * 16;
-	constexpr int kStoreRows = kTilesPerWarp == 2 ? 8 : 16;
-	constexpr int kStores = 16 / kStoreRows;
-	const int st_row = kTilesPerWarp == 2 ? (lane >> 3) + 4 * ((lane >> 2) & 1)
-	                                      : ((lane >> 3) & 1) + 8 * (lane >> 4) + 2 * ((lane >> 1) & 3);
-	const int st_tile = kTilesPerWarp == 2 ? (lane >> 1) & 1 : 0;
-	const char *ld_addr = stage + st_tile * kTileStage + st_row * kStageBytes + (lane & 1) * 16;
+	const unsigned long long wait_ns = g_chain_wait_ns ? g_chain_wait_ns : kWaitNs;
 
 	if (threadIdx.x == 0) {
 		for (int s = 0; s < NS; ++s) {
 			mbar_init(&full[s], 1);
-			mbar_init(&empty[s], kWarps);
+			mbar_init(&empty[s], kWsWarps);
 		}
 		asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
 		abort_item = 0;
@@ -104,35 +309,46 @@ chain_tma_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_item
 	const int t_end = static_cast<int>(static_cast<long long>(blockIdx.x + 1) * total_items / gridDim.x);
 	for (int t = static_cast<int>(static_cast<long long>(blockIdx.x) * total_items / gridDim.x); t < t_end;) {
 		const FusedJob *Jp = jobs ? &jobs[find_job(jobs, num_jobs, t)] : &single;
-		const Item it = make_item(*Jp, t, t_end, kStripTiles, kThreads);
-		t += it.g_end - it.g_begin;
-		for (int g = it.g_begin + threadIdx.x; g < it.g_end; g += kThreads)
-			vb[g - it.g_begin] = __ldg(Jp->v_base + g);
-		const int ngroups = it.g_end - it.g_begin;
+		const FusedJob &J = *Jp;
+		const int local = t - J.item_begin;
+		const int strip = local / J.groups;
+		const int g_begin = local - strip * J.groups;
+		const int ngroups = min(J.groups - g_begin, t_end - t);
+		t += ngroups;
+		for (int g = threadIdx.x; g < ngroups; g += kThreads)
+			vb[g] = __ldg(J.v_base + g_begin + g);
 
 		if (producer) {
 			__syncthreads();  // group bases visible; every warp is done with the previous item
 			if (lane == 0 && !error) {
-				const void *tmap = jobs ? Jp->tmap : static_cast<const void *>(&single_map);
-				const char *vtab = reinterpret_cast<const char *>(Jp->v_dense);
+				const void *tmap = jobs ? J.tmap : static_cast<const void *>(&single_map);
+				const char *vtab = reinterpret_cast<const char *>(J.v_dense);
+				const int xlo = __ldg(J.win_col + 2 * strip);
+				const int drop = blockIdx.x == 0 ? g_chain_drop_group : -1;
 				// next source block to load; first group of the item whose
 				// window starts at or after the block being replaced
 				int next_blk = vb[0] / kBlockLines;
 				int gneed = 0;
 				// advance `released` to n; false when a wait ran out
+				int rel_s = static_cast<int>(released % NS);
+				unsigned rel_ph = (released / NS) & 1;
 				auto release_to = [&](unsigned n) -> bool {
 					while (released < n) {
-						if (!mbar_wait(&empty[released % NS], (released / NS) & 1))
+						if (!mbar_wait_for(&empty[rel_s], rel_ph, wait_ns))
 							return false;
 						++released;
+						if (++rel_s == NS) {
+							rel_s = 0;
+							rel_ph ^= 1;
+						}
 					}
 					return true;
 				};
-				const int in_blks = (it.src_h + kBlockLines - 1) / kBlockLines;
+				int s = static_cast<int>(base % NS);
+				const int in_blks = (J.src_h + kBlockLines - 1) / kBlockLines;
 				asm volatile("prefetch.tensormap [%0];\n" ::"l"(tmap) : "memory");
-				for (int k = 0; k < ngroups; ++k) {
+				for (int k = 0; k < ngroups; ++k, s = s + 1 == NS ? 0 : s + 1) {
 					const unsigned g = base + k;
-					const int s = static_cast<int>(g % NS);
 					// the stage's fragment slot was last read by group g - NS
 					if (g >= static_cast<unsigned>(NS) && !release_to(g - NS + 1)) {
 						error = 2;
@@ -151,13 +367,18 @@ chain_tma_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_item
 					}
 					if (error)
 						break;
+					if (static_cast<int>(g) == drop) {
+						// test hook: this group's stage is never armed
+						issued = g + 1;
+						continue;
+					}
 					// blocks wholly below the plane (windows are padded to
 					// 16 KV lines; their taps there are zero) become zero
 					// lines, written here, not copied
 					const int copy_end = min(last_blk + 1, in_blks);
 					const int ncopy = max(0, copy_end - next_blk);
 					for (int b = max(next_blk, in_blks); b <= last_blk; ++b) {
-						float4 *z = reinterpret_cast<float4 *>(ring + (b % NB) * kBlockLines * P);
+						float4 *z = reinterpret_cast<float4 *>(ring + (b & (NB - 1)) * kBlockLines * P);
 						for (int i = 0; i < kBlockLines * P / 16; ++i)
 							z[i] = make_float4(0.f, 0.f, 0.f, 0.f);
 						// later tensor copies into this block come after these stores
@@ -165,8 +386,8 @@ chain_tma_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_item
 					}
 					mbar_arrive_expect_tx(&full[s], static_cast<unsigned>(kSlotBytes + ncopy * kBlockLines * P));
 					for (int b = next_blk; b < copy_end; ++b)
-						tma_load_2d(ring + (b % NB) * kBlockLines * P, tmap, it.xlo, b * kBlockLines, &full[s]);
-					bulk_load(vslots + s * kSlotBytes, vtab + static_cast<size_t>(it.g_begin + k) * kSlotBytes,
+						tma_load_2d(ring + (b & (NB - 1)) * kBlockLines * P, tmap, xlo, b * kBlockLines, &full[s]);
+					bulk_load(vslots + s * kSlotBytes, vtab + static_cast<size_t>(g_begin + k) * kSlotBytes,
 					          kSlotBytes, &full[s]);
 					next_blk = max(next_blk, last_blk + 1);
 					issued = g + 1;
@@ -175,82 +396,130 @@ chain_tma_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_item
 					abort_item = 1;  // benign race: every writer stores 1
 			}
 		} else {
-			const int ntiles = (it.dst_w + kTileW - 1) / kTileW;
-			const int tile0 = it.strip * kStripTiles + warp * kTilesPerWarp;
-			uint4 ah[kTilesPerWarp][KH][2];
-			int rel[kTilesPerWarp];
-			Carry carry[kTilesPerWarp];
-			const int st_col = (tile0 + st_tile) * kTileW + (lane & 1) * 8;
-			const bool wide = it.vec_ok && st_col + 8 <= it.dst_w;
-			char *drow = it.dst + static_cast<ptrdiff_t>(it.g_begin * 16 + st_row) * it.dst_stride +
-			             static_cast<ptrdiff_t>(st_col) * 2;
-			const ptrdiff_t group_step = 16 * it.dst_stride;
-			const ptrdiff_t store_step = kStoreRows * it.dst_stride;
+			const int xlo = __ldg(J.win_col + 2 * strip);
+			const int gid = lane >> 2, tig = lane & 3;
+			const int ntiles = (J.dst_w + kTileW - 1) / kTileW;
+			const int tile0 = strip * kStripTiles + warp * T;
+			const bool active = tile0 * kTileW < J.dst_w;
+			uint4 ah[T][KH][2];
+			uint32_t colb[T];
+			uint32_t carry[T][2];
 #pragma unroll
-			for (int j = 0; j < kTilesPerWarp; ++j) {
+			for (int j = 0; j < T; ++j) {
 				const int tile = min(tile0 + j, ntiles - 1);
-				const uint4 *hf = reinterpret_cast<const uint4 *>(Jp->h_taps) + static_cast<size_t>(tile) * KH * 2 * 32 + lane;
+				const uint4 *hf = reinterpret_cast<const uint4 *>(J.h_taps) + static_cast<size_t>(tile) * KH * 2 * 32 + lane;
 #pragma unroll
 				for (int ks = 0; ks < KH; ++ks) {
 					ah[j][ks][0] = __ldg(hf + (ks * 2 + 0) * 32);
 					ah[j][ks][1] = __ldg(hf + (ks * 2 + 1) * 32);
 				}
-				rel[j] = __ldg(Jp->h_left + tile) - it.xlo;
+				const int rel = __ldg(J.h_left + tile) - xlo;
+				colb[j] = H_FIRST ? static_cast<uint32_t>((rel + 2 * tig) * 2)
+				                  : static_cast<uint32_t>((rel + (lane >> 4) * 8) * 2);
+				carry[j][0] = carry[j][1] = 0;
 			}
+			Epi e;
+			e.magic = J.magic;
+			const uint32_t pm = static_cast<uint32_t>(J.pixel_max);
+			e.pmax2 = pm | (pm << 16);
+			{
+				const __half2 b = __floats2half2_rn(1024.0f + J.offset, 1024.0f + J.offset);
+				e.bias_h2 = *reinterpret_cast<const uint32_t *>(&b);
+			}
+			// stores: one 16-byte chunk per lane and store (see chain_kernel.cuh)
+			char *stage = smem + L.tile_off + warp * kWarpStage;
+			char *st_addr = stage + (((lane >> 4) << 3) + (lane & 7)) * kStageBytes + ((lane >> 3) & 1) * 16;
+			constexpr int kStoreRows = store_rows(T);
+			constexpr int kStores = 16 / kStoreRows;
+			const int st_row = store_row(T, lane);
+			const int st_tile = store_tile(T, lane);
+			const char *ld_addr = stage + st_tile * kTileStage + st_row * kStageBytes + (lane & 1) * 16;
+			const int st_col = (tile0 + st_tile) * kTileW + (lane & 1) * 8;
+			const bool wide = J.vec_ok && st_col + 8 <= J.dst_w;
+			char *const dst = static_cast<char *>(J.dst);
+			const ptrdiff_t dst_stride = J.dst_stride;
+			char *drow = dst + static_cast<ptrdiff_t>(g_begin * 16 + st_row) * dst_stride + static_cast<ptrdiff_t>(st_col) * 2;
+			const ptrdiff_t group_step = 16 * dst_stride;
+			const ptrdiff_t store_step = kStoreRows * dst_stride;
+			// groups whose 16 rows all lie in the plane
+			const int full_groups = J.dst_h / 16 - g_begin;
+			// this lane's line in each 16-line window block
+			const int lrow = H_FIRST ? gid : (lane & 7) + ((lane >> 3) & 1) * 8;
 			__syncthreads();  // group bases visible; every warp is done with the previous item
 
-			int cur_vb = vb[0];
-			int cur_slot = wrap(cur_vb % IR, IR);
-			const bool active = tile0 * kTileW < it.dst_w;
+			int prev_vb = vb[0];
+			int s = static_cast<int>(base % NS);
+			unsigned ph = (base / NS) & 1;
 			for (int k = 0; k < ngroups; ++k) {
-				const unsigned g = base + k;
-				const int s = static_cast<int>(g % NS);
 				// every lane polls; the warp goes on only when all saw the copies land
-				if (!__all_sync(0xffffffffu, mbar_wait(&full[s], (g / NS) & 1))) {
+				if (!__all_sync(0xffffffffu, mbar_wait_for(&full[s], ph, wait_ns))) {
 					error = 1;
 					abort_item = 1;  // benign race: every writer stores 1
 					break;
 				}
 				const int vbk = vb[k];
-				const bool reuse = H_FIRST && KV == 1 && k > 0 && vbk - cur_vb == 8;
-				cur_slot = wrap(cur_slot + (vbk - cur_vb), IR);
-				cur_vb = vbk;
 				if (active) {
 					const uint4 *avs = reinterpret_cast<const uint4 *>(vslots + s * kSlotBytes) + lane;
 					uint4 av[KV][2];
+					if (H_FIRST) {
+						uint32_t roff[KV][2];
 #pragma unroll
-					for (int kv = 0; kv < KV; ++kv) {
-						av[kv][0] = avs[(kv * 2 + 0) * 32];
-						av[kv][1] = avs[(kv * 2 + 1) * 32];
-					}
-					uint32_t m[kTilesPerWarp][4];
-#pragma unroll
-					for (int j = 0; j < kTilesPerWarp; ++j)
-						tile_compute<H_FIRST, KV, KH>(it, ring, IR, P, cur_slot, rel[j], ah[j], av, carry[j], reuse, m[j]);
-					// the group's shared data are in registers: release the stage
-					__syncwarp();
-					if (lane == 0)
-						mbar_arrive(&empty[s]);
-#pragma unroll
-					for (int j = 0; j < kTilesPerWarp; ++j) {
-						char *sa = st_addr + j * kTileStage;
-						if (H_FIRST)
-							stsm_x4(sa, m[j][0], m[j][1], m[j][2], m[j][3]);
+						for (int kv = 0; kv < KV; ++kv) {
+							roff[kv][0] = ((static_cast<unsigned>(vbk + 16 * kv + lrow)) & line_mask) * P;
+							roff[kv][1] = ((static_cast<unsigned>(vbk + 16 * kv + lrow + 8)) & line_mask) * P;
+						}
+						uint32_t bv[T][KV][2][2];
+						if (KV == 1 && k > 0 && vbk - prev_vb == 8)
+							hfirst_h<KV, KH, T, true>(ring, roff, colb, ah, carry, bv, e);
 						else
-							stsm_x4_trans(sa, m[j][0], m[j][1], m[j][2], m[j][3]);
+							hfirst_h<KV, KH, T, false>(ring, roff, colb, ah, carry, bv, e);
+#pragma unroll
+						for (int kv = 0; kv < KV; ++kv) {
+							av[kv][0] = avs[(kv * 2 + 0) * 32];
+							av[kv][1] = avs[(kv * 2 + 1) * 32];
+						}
+						// the group's shared data are in registers: release the stage
+						__syncwarp();
+						if (lane == 0)
+							mbar_arrive(&empty[s]);
+						hfirst_v<KV, T>(bv, av, st_addr, e);
+					} else {
+#pragma unroll
+						for (int kv = 0; kv < KV; ++kv) {
+							av[kv][0] = avs[(kv * 2 + 0) * 32];
+							av[kv][1] = avs[(kv * 2 + 1) * 32];
+						}
+						uint32_t roff[KV];
+#pragma unroll
+						for (int kv = 0; kv < KV; ++kv)
+							roff[kv] = ((static_cast<unsigned>(vbk + 16 * kv + lrow)) & line_mask) * P;
+						vfirst_tiles<KV, KH, T>(ring, roff, colb, ah, av, st_addr, e);
+						// the group's shared data are in registers: release the stage
+						__syncwarp();
+						if (lane == 0)
+							mbar_arrive(&empty[s]);
 					}
 					__syncwarp();
-					const bool rows_in = (it.g_begin + k + 1) * 16 <= it.dst_h;
-					if (wide && rows_in) {
+					if (wide && k < full_groups) {
 #pragma unroll
 						for (int i = 0; i < kStores; ++i)
 							*reinterpret_cast<uint4 *>(drow + i * store_step) =
 								*reinterpret_cast<const uint4 *>(ld_addr + i * kStoreRows * kStageBytes);
 					} else {
-#pragma unroll
-						for (int i = 0; i < kStores; ++i)
-							store_chunk(it, ld_addr + i * kStoreRows * kStageBytes,
-							            (it.g_begin + k) * 16 + st_row + i * kStoreRows, st_col);
+						for (int i = 0; i < kStores; ++i) {
+							const int row = (g_begin + k) * 16 + st_row + i * kStoreRows;
+							if (row < J.dst_h && st_col < J.dst_w) {
+								const uint4 v = *reinterpret_cast<const uint4 *>(ld_addr + i * kStoreRows * kStageBytes);
+								uint16_t *d = reinterpret_cast<uint16_t *>(dst + static_cast<ptrdiff_t>(row) * dst_stride) + st_col;
+								if (J.vec_ok && st_col + 8 <= J.dst_w) {
+									*reinterpret_cast<uint4 *>(d) = v;
+								} else {
+									const uint32_t w[4] = { v.x, v.y, v.z, v.w };
+									for (int q = 0; q < 8 && st_col + q < J.dst_w; ++q)
+										d[q] = static_cast<uint16_t>(w[q >> 1] >> (16 * (q & 1)));
+								}
+							}
+						}
 					}
 					__syncwarp();
 				} else {
@@ -258,7 +527,12 @@ chain_tma_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_item
 					if (lane == 0)
 						mbar_arrive(&empty[s]);
 				}
+				prev_vb = vbk;
 				drow += group_step;
+				if (++s == NS) {
+					s = 0;
+					ph ^= 1;
+				}
 			}
 		}
 		base += ngroups;
@@ -268,14 +542,16 @@ chain_tma_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_item
 	}
 
 	if (producer && lane == 0 && (error || abort_item)) {
-		atomicExch(&g_chain_pipeline_error, error ? error : 1);
+		atomicCAS(&g_chain_pipeline_error, 0, error ? error : 1);
 		// copies still in flight land before the CTA leaves: only the last NS
 		// issued groups can have any (an earlier group's stage was reissued
-		// only after every consumer had read it)
+		// only after every consumer had read it); a dropped group has none
+		const int drop = blockIdx.x == 0 ? g_chain_drop_group : -1;
 		for (unsigned g = issued > static_cast<unsigned>(NS) ? issued - NS : 0; g < issued; ++g)
-			mbar_wait(&full[g % NS], (g / NS) & 1);
+			if (static_cast<int>(g) != drop)
+				mbar_wait_for(&full[g % NS], (g / NS) & 1, wait_ns);
 	} else if (!producer && lane == 0 && error) {
-		atomicExch(&g_chain_pipeline_error, error);
+		atomicCAS(&g_chain_pipeline_error, 0, error);
 	}
 }
 

@@ -167,7 +167,7 @@ cudaError_t launch_chain(int variant, const FusedJob *jobs, int num_jobs, int to
 // copies on an mbarrier pipeline (chain_tma_kernel.cuh). Usable when the
 // layout fits (box width <= 256) and the source plane has a tensor map
 // (16-byte aligned base and stride).
-bool chain_tma_enabled();  // true when the environment sets ZG_CHAIN_TMA=1
+bool chain_tma_enabled();  // false when the environment sets ZG_CHAIN_TMA=0
 bool chain_tma_layout(const FusedPlan *const *plans, int n, SmemLayout *out);
 bool chain_tma_source_map(CUtensorMap *map, const FusedJob &j, const SmemLayout &L);
 int chain_tma_grid_size(int variant, size_t smem_bytes);
@@ -175,6 +175,9 @@ cudaError_t launch_chain_tma(int variant, const FusedJob *jobs, int num_jobs, in
                              int grid, const FusedJob &single, const CUtensorMap *single_map, cudaStream_t stream);
 // Nonzero when a pipeline wait of that kernel ran out (optionally reset).
 int chain_tma_pipeline_error(bool reset);
+// Test hook: CTA 0's producer skips group drop_group (-1: none) without
+// arming its stage; waits give up after wait_ns (0: the default 0.25 s).
+int chain_tma_set_fault(int drop_group, unsigned long long wait_ns);
 // A 2-D tensor map (zero fill outside the plane) over a plane of width x
 // height elements, `stride` bytes per line; swizzle128: boxes land in shared
 // memory with the 128-byte swizzle (16-byte chunk c of box line r at chunk

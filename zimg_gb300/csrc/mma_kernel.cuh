@@ -65,21 +65,24 @@ __device__ __forceinline__ void ldsm_x4_trans(uint32_t &r0, uint32_t &r1, uint32
 // D += A * B, m16n8k16, f16 x f16 -> f32
 __device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1)
 {
-	asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
-	             "{%0, %1, %2, %3};\n"
+	asm("mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+	    "{%0, %1, %2, %3};\n"
 	             : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
 	             : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
 // acc (exact 8192 + sum c*v') -> two packed, clamped zimg samples (low/high half).
+// Both values in one paired fp32 multiply-add (round toward minus infinity,
+// so floor((acc - 8192) / 2^14 + 1/2) lands in the low mantissa bits of
+// 1.5*2^23 + offset), the low halves packed, and one s16x2 minimum with
+// relu for the clamp to [0, pixel_max].
 __device__ __forceinline__ uint32_t pack_u16x2(float acc0, float acc1, float magic, uint32_t pmax2)
 {
-	const float y0 = __fmaf_rd(acc0, 6.103515625e-05f, magic);
-	const float y1 = __fmaf_rd(acc1, 6.103515625e-05f, magic);
+	const float2 y = __ffma2_rd(make_float2(acc0, acc1), make_float2(6.103515625e-05f, 6.103515625e-05f),
+	                            make_float2(magic, magic));
 	// low 16 bits of y are the signed sample before clamping
-	uint32_t q = __byte_perm(__float_as_uint(y0), __float_as_uint(y1), 0x5410);
-	asm("max.s16x2 %0, %0, %1;" : "+r"(q) : "r"(0u));
-	asm("min.s16x2 %0, %0, %1;" : "+r"(q) : "r"(pmax2));
+	uint32_t q = __byte_perm(__float_as_uint(y.x), __float_as_uint(y.y), 0x5410);
+	asm("min.relu.s16x2 %0, %0, %1;" : "+r"(q) : "r"(pmax2));
 	return q;
 }
 

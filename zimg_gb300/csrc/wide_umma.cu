@@ -188,8 +188,9 @@ wide_umma_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
 	__shared__ int abort_word, epi_fail_word;
 	volatile int *abort_flag = &abort_word;
 	volatile int *epi_fail = &epi_fail_word;  // set before an epilogue barrier, read after it
-	unsigned char *sm =
-		reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_dyn) + 1023) & ~static_cast<uintptr_t>(1023));
+	// 1024-byte aligned base, as an offset from the shared array so that every
+	// access through it stays a shared-memory access
+	unsigned char *sm = smem_dyn + ((1024u - (smem_addr(smem_dyn) & 1023u)) & 1023u);
 	uint64_t *raw_full = reinterpret_cast<uint64_t *>(sm + kOffBar);
 	uint64_t *raw_empty = raw_full + kStages;
 	uint64_t *x_full = raw_empty + kStages;
