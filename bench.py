@@ -1,10 +1,15 @@
 """Benchmark of the resize path on GB300 (one JSON line on rank 0).
 
-Default workload (the FP32 headline case): FP32 bicubic (b=0, c=0.5)
-downscale of 3 planes 4:4:4 1920x1080 -> 1280x720, a batch of frames per step.
+Default workload (the headline case): one plane 1920x1080 u16 holding 10-bit
+values, Lanczos a=3, to 3840x2160, horizontal pass then vertical, bit-exact
+against zimg's C path; a step is a batch of 64 such frames. The same line
+carries `tc_vs_plain`: the wide-filter FP32 workload (8 planes 7680x4320 ->
+480x270, Lanczos a=4, ~128 taps per output) timed in the same process on
+the tensor-core passes and on the plain FP32 CUDA-core passes, with the
+max-abs error of each against the FP64 oracle beside zimg's C path's.
 Other workloads (--workload):
-  fhd_uhd_u16     1 plane 1920x1080 u16 10-bit Lanczos-3 -> 3840x2160 (bit-exact path)
-  bicubic_f32     the default
+  fhd_uhd_u16     the default
+  bicubic_f32     3 planes 4:4:4 1920x1080 f32 -> 1280x720, bicubic b=0 c=0.5
   wide_f32        8 planes 7680x4320 f32 Lanczos-4 16x down -> 480x270
   yuv420_batch    64 YUV 4:2:0 u16 frames of mixed sizes, Spline36 -> 1920x1080
   extreme_f32     32 images 64x64 -> 6400x6400 and 6400x6400 -> 64x64 f32 Lanczos-3, plus 32 interlaced
@@ -13,6 +18,10 @@ Other workloads (--workload):
                   3840x2160 f32 -> u8 8-bit limited range, ordered dither
   unresize_f32    zimg's UnresizeConversion (inverse bilinear): 8 frames of 3 planes 1920x1080 f32
                   -> 1280x720
+
+Synthetic content follows each configuration: u16 planes are 16x16 blocks of
+uniform 10-bit noise or smooth sinusoids; the bicubic planes uniform [0,1]
+plus 32 step rectangles; the wide and extreme planes band-limited noise.
 
 A step is one pass of the resize path over one batch of synthetic frames that
 are already resident in HBM (inputs larger than L2 across the batch). `value`
@@ -62,7 +71,8 @@ def workload(name: str, frames: int | None, seed: int):
     rng = np.random.default_rng(seed)
     if name == "bicubic_f32":
         n = frames or 128
-        jobs = [_job(1920, 1080, 1280, 720, "float", 32, "bicubic", 0.0, 0.5) for _ in range(3 * n)]
+        jobs = [dict(_job(1920, 1080, 1280, 720, "float", 32, "bicubic", 0.0, 0.5), content="edges")
+                for _ in range(3 * n)]
         cfg = {"workload": "bicubic_f32: 3 planes 4:4:4 1920x1080 f32 -> 1280x720, bicubic b=0 c=0.5",
                "frames_per_step": n, "planes_per_step": 3 * n}
     elif name == "fhd_uhd_u16":
@@ -138,10 +148,46 @@ def job_bytes(j):
     return (j["sw"] * j["sh"] + j["dw"] * j["dh"]) * bpe
 
 
+def u16_blocks(rng, h, w, depth):
+    """16x16 blocks, each (p = 0.5) uniform noise over the depth's range or a
+    smooth sinusoid round(m/2 + m/2 sin(2 pi (x/lx + y/ly) + phase)), lx, ly
+    drawn from [64, 512]."""
+    maxv = (1 << depth) - 1
+    yy, xx = np.mgrid[0:h, 0:w]
+    lx, ly, ph = rng.uniform(64, 512), rng.uniform(64, 512), rng.uniform(0, 2 * np.pi)
+    wave = np.round(maxv / 2 + maxv / 2 * np.sin(2 * np.pi * (xx / lx + yy / ly) + ph)).astype(np.uint16)
+    noise = rng.integers(0, maxv + 1, size=(h, w), dtype=np.uint16)
+    pick = rng.random(((h + 15) // 16, (w + 15) // 16)) < 0.5
+    mask = np.kron(pick, np.ones((16, 16), bool))[:h, :w]
+    return np.where(mask, noise, wave).astype(np.uint16)
+
+
+def step_edges(rng, h, w, n=32):
+    """Uniform [0, 1) plus n axis-aligned rectangles of +-U[0.2, 0.5], not clamped."""
+    x = rng.random((h, w), dtype=np.float32)
+    for _ in range(n):
+        x0, y0 = rng.integers(0, w), rng.integers(0, h)
+        x[y0:y0 + rng.integers(8, 300), x0:x0 + rng.integers(8, 300)] += rng.choice([-1, 1]) * rng.uniform(0.2, 0.5)
+    return x
+
+
+def band_limited(rng, h, w, cutoff=0.25):
+    """White noise low-passed to <= cutoff cycles per sample, rescaled to [0, 1]."""
+    f = np.fft.rfft2(rng.standard_normal((h, w)).astype(np.float32))
+    f[np.abs(np.fft.fftfreq(h)) > cutoff, :] = 0
+    f[:, np.fft.rfftfreq(w) > cutoff] = 0
+    y = np.fft.irfft2(f, s=(h, w))
+    return ((y - y.min()) / (y.max() - y.min())).astype(np.float32)
+
+
 def fill(rng, j):
+    """A synthetic plane with the content the job's configuration names."""
+    h, w = j["sh"], j["sw"]
     if j["ptype"] == "word":
-        return rng.integers(0, 1 << j["depth"], size=(j["sh"], j["sw"]), dtype=np.uint16)
-    return rng.random((j["sh"], j["sw"]), dtype=np.float32)
+        return u16_blocks(rng, h, w, j["depth"])
+    if j.get("content") == "edges":
+        return step_edges(rng, h, w)
+    return band_limited(rng, h, w)
 
 
 # ------------------------------------------------------------------- clocks --
@@ -328,6 +374,9 @@ def run_ours(args):
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(jobs, seconds=args.cpu_seconds)
+    tcp = None
+    if rank == 0 and args.workload == "fhd_uhd_u16" and not args.no_tc_vs_plain:
+        tcp = tc_vs_plain(max(3, args.steps // 2), args.warmup, peak)
 
     if rank == 0:
         line = {"metric": "out Mpixel/s on 1 GB300 + % HBM roofline", "value": round(value, 3), "unit": "Mpixel/s",
@@ -338,9 +387,75 @@ def run_ours(args):
                                parallelism=f"replicas x{world}", graph=bool(args.graph)),
                 "impl": "ours", "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
                 "clocks": sampler.summary(t0, t1), "gpu_launches": launches_per_step * args.steps}
+        if tcp is not None:
+            line["tc_vs_plain"] = tcp
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def tc_vs_plain(steps, warmup, peak):
+    """The wide-filter FP32 workload (8 planes 7680x4320 -> 480x270, Lanczos
+    a=4) on the tensor-core passes and on the plain FP32 CUDA-core passes, on
+    the same resident planes (band-limited noise), each timed with CUDA events
+    over `steps` batches; plus the max-abs error of each against the FP64
+    oracle on one plane, beside zimg's C path's."""
+    import torch
+    import zimg_gb300 as zg
+    from oracle.oracle import Oracle, build
+    jobs, _ = workload("wide_f32", None, seed=0x5EED0003)
+    rng = np.random.default_rng(0x5EED0003)
+    protos = [fill(rng, jobs[0]) for _ in range(2)]
+    srcs = [torch.from_numpy(protos[i % 2]).cuda() for i in range(len(jobs))]
+    out_px = sum(j["dw"] * j["dh"] for j in jobs)
+    alg_bytes = sum(job_bytes(j) for j in jobs)
+    res, first = {}, {}
+    stream = torch.cuda.current_stream()
+    for engine in ("tensor", "cuda"):
+        convs = [zg.ResizeConversion(j["sw"], j["sh"], "float").set_filter(j["kind"], j["a"], j["b"])
+                 .set_dst_width(j["dw"]).set_dst_height(j["dh"]).set_engine(engine) for j in jobs]
+        dsts = [torch.empty((j["dh"], j["dw"]), dtype=torch.float32, device="cuda") for j in jobs]
+        batch = zg.Batch(convs)
+        batch.set_io(srcs, dsts)
+        tmp = torch.empty(max(batch.tmp_size, 1), dtype=torch.uint8, device="cuda")
+        for _ in range(warmup):
+            batch.process(tmp)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            batch.process(tmp)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        res[engine] = {"value": round(out_px / (ms / 1e3) / 1e6, 3), "ms_per_step": round(ms, 5),
+                       "hbm_frac": round(alg_bytes / (ms / 1e3) / 1e9 / peak, 4),
+                       "plan": convs[0].create().info["engine"]}
+        first[engine] = dsts[0].cpu().numpy().astype(np.float64)
+        del batch, dsts, tmp
+    build()
+    o = Oracle()
+    j = jobs[0]
+    f64 = o.resize_plane(protos[0], j["dw"], j["dh"], j["kind"], j["a"], mode="f64", nthreads=os.cpu_count() or 1)
+    c = o.resize_plane(protos[0], j["dw"], j["dh"], j["kind"], j["a"], mode="c", nthreads=os.cpu_count() or 1)
+    err = {k: float(np.max(np.abs(v - f64))) for k, v in first.items()}
+    err["c_path"] = float(np.max(np.abs(c.astype(np.float64) - f64)))
+    return {"workload": "wide_f32: 8 planes 7680x4320 f32 -> 480x270, Lanczos a=4 (~128 taps), band-limited noise",
+            "unit": "Mpixel/s", "tensor": res["tensor"], "plain": res["cuda"],
+            "ratio": round(res["tensor"]["value"] / res["cuda"]["value"], 3),
+            "max_abs_err_vs_fp64": {"tensor": err["tensor"], "plain": err["cuda"], "zimg_c_path": err["c_path"]},
+            "tensor_pipe_active": read_profile_value("wide_f32", "tensor_pipe_active_pct")}
+
+
+def read_profile_value(workload_name, key):
+    """A figure from the committed ncu summary of the workload, if present."""
+    p = os.path.join(ROOT, "profiles", f"traffic_{workload_name}.txt")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith(key + ":"):
+            return float(line.split(":", 1)[1])
+    return None
 
 
 def read_traffic(workload_name):
@@ -356,34 +471,76 @@ def read_traffic(workload_name):
 
 # ---------------------------------------------------------------- CPU side --
 
-def cpu_baseline(jobs, seconds=10.0, impl_label=None):
-    """The oracle's C restatement of zimg's C path on the host cores (all
-    threads, row-parallel per plane), on a bounded sample of the workload."""
-    from oracle.oracle import Oracle, build
-    build()
-    o = Oracle()
-    cores = os.cpu_count() or 1
-    rng = np.random.default_rng(99)
-    sample = []
-    for j in jobs[: min(len(jobs), 6)]:
-        sample.append((j, fill(rng, j)))
-    px = 0
-    t0 = time.perf_counter()
-    n_planes = 0
-    while True:
-        for j, x in sample:
-            o.resize_plane(x, j["dw"], j["dh"], j["kind"], j["a"], j["b"], depth=j["depth"], shift_w=j["shift_w"],
-                           shift_h=j["shift_h"], mode="c", nthreads=cores)
-            px += j["dw"] * j["dh"]
-            n_planes += 1
-            if time.perf_counter() - t0 > seconds:
-                break
-        if time.perf_counter() - t0 > seconds:
-            break
-    dt = time.perf_counter() - t0
-    return {"value": round(px / dt / 1e6, 3), "unit": "Mpixel/s", "cores": cores, "kind": "port",
-            "sample": f"{n_planes} planes of the workload's first {len(sample)} jobs in {dt:.1f} s, zimg C-path "
-                      f"restatement (oracle/zimg_oracle.c), {cores} threads row-parallel"}
+class CpuSample:
+    """zimg's C path (the oracle's restatement of it, resize_impl.cpp:44-114)
+    on every host thread, as zimg runs frames: each conversion planned once
+    (filter contexts built), then frame-parallel workers, one per host
+    thread, each resizing whole planes one after another, as zimg's test
+    application threads frames (graphapp.cpp:355-425). The planes cycle
+    through the workload's first few jobs, with the content the configuration
+    names. The in-line `cpu_baseline` and the reference arm (`--impl
+    reference`) both time this routine, so their rates agree."""
+
+    def __init__(self, jobs, n_jobs=6, seed=99):
+        from oracle.oracle import Oracle, build
+        build()
+        self.o = Oracle()
+        self.cores = os.cpu_count() or 1
+        rng = np.random.default_rng(seed)
+        self.sample = []
+        plans = {}
+        for j in jobs[: min(len(jobs), n_jobs)]:
+            x = fill(rng, j)
+            key = tuple(sorted((k, str(v)) for k, v in j.items()))
+            if key not in plans:
+                plans[key] = self.o.plan(j["sw"], j["sh"], j["dw"], j["dh"], j["kind"], j["a"], j["b"], x.dtype,
+                                         j["depth"], j["shift_w"], j["shift_h"])
+            self.sample.append((j, x, plans[key]))
+
+    def run(self, planes=None, seconds=None):
+        """Every thread resizes planes until `planes` planes are done in all, or
+        for about `seconds`; output Mpixel/s, planes, elapsed seconds."""
+        import threading
+        lock = threading.Lock()
+        state = {"next": 0, "px": 0}
+        t0 = time.perf_counter()
+
+        def worker():
+            outs = {}
+            while True:
+                with lock:
+                    i = state["next"]
+                    if (planes is not None and i >= planes) or (planes is None and time.perf_counter() - t0 >= seconds):
+                        return
+                    state["next"] = i + 1
+                j, x, plan = self.sample[i % len(self.sample)]
+                out = outs.get(id(plan))
+                if out is None:
+                    out = outs[id(plan)] = (np.empty(plan.out_shape, x.dtype), np.empty(max(plan.tmp_size, 1), np.uint8))
+                plan.run(x, out[0], out[1])
+                with lock:
+                    state["px"] += j["dw"] * j["dh"]
+
+        ths = [threading.Thread(target=worker) for _ in range(self.cores)]
+        for th in ths:
+            th.start()
+        for th in ths:
+            th.join()
+        dt = time.perf_counter() - t0
+        return state["px"] / dt / 1e6, state["next"], dt
+
+    def describe(self, n, dt):
+        shapes = sorted({f"{j['sw']}x{j['sh']}->{j['dw']}x{j['dh']}" for j, _, _ in self.sample})
+        return (f"{n} planes ({', '.join(shapes)}) in {dt:.2f} s, zimg C-path restatement (oracle/zimg_oracle.c), "
+                f"conversions planned once, {self.cores} frame-parallel threads")
+
+
+def cpu_baseline(jobs, seconds=10.0):
+    """The in-line CPU baseline: a bounded sample (about `seconds`) of the workload."""
+    cs = CpuSample(jobs)
+    cs.run(planes=cs.cores)  # warm
+    v, n, dt = cs.run(seconds=seconds)
+    return {"value": round(v, 3), "unit": "Mpixel/s", "cores": cs.cores, "kind": "port", "sample": cs.describe(n, dt)}
 
 
 # ------------------------------------------------------- depth conversion --
@@ -726,33 +883,17 @@ def run_reference(args):
         print(json.dumps(line), flush=True)
         return
     jobs, cfg = workload(args.workload, args.frames, seed=0x5EED0000)
-    from oracle.oracle import Oracle, build
-    build()
-    o = Oracle()
-    cores = os.cpu_count() or 1
-    rng = np.random.default_rng(99)
-    j = jobs[0]
-    planes_per_step = 1
-    x = fill(rng, j)
-
-    def step():
-        o.resize_plane(x, j["dw"], j["dh"], j["kind"], j["a"], j["b"], depth=j["depth"], shift_w=j["shift_w"],
-                       shift_h=j["shift_h"], mode="c", nthreads=cores)
-    for _ in range(args.warmup):
-        step()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        step()
-    dt = time.perf_counter() - t0
-    value = j["dw"] * j["dh"] * planes_per_step * args.steps / dt / 1e6
+    cs = CpuSample(jobs)
+    cs.run(planes=args.warmup * cs.cores)
+    # a step: one plane of the workload per host thread, the threads in parallel
+    value, n, dt = cs.run(planes=args.steps * cs.cores)
     line = {"metric": "out Mpixel/s on 1 GB300 + % HBM roofline", "value": round(value, 3), "unit": "Mpixel/s",
             "n_gpus": int(os.environ.get("WORLD_SIZE", "1")), "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": round(dt / args.steps * 1e3, 3), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "u16" if j["ptype"] == "word" else "f32", "data": "synthetic (seeded)",
-            "config": cfg, "impl": "reference",
-            "cpu_baseline": {"value": round(value, 3), "unit": "Mpixel/s", "cores": cores, "kind": "port",
-                             "sample": f"one plane of the workload per step ({j['sw']}x{j['sh']} -> "
-                                       f"{j['dw']}x{j['dh']}), zimg C-path restatement, {cores} threads"},
+            "ms_per_step": round(dt / n * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u16" if jobs[0]["ptype"] == "word" else "f32",
+            "data": "synthetic (seeded)", "config": cfg, "impl": "reference",
+            "cpu_baseline": {"value": round(value, 3), "unit": "Mpixel/s", "cores": cs.cores, "kind": "port",
+                             "sample": "one plane per host thread per step: " + cs.describe(n, dt)},
             "e2e": {"value": round(value, 3), "unit": "Mpixel/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -762,7 +903,7 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
-    ap.add_argument("--workload", default="bicubic_f32")
+    ap.add_argument("--workload", default="fhd_uhd_u16")
     ap.add_argument("--frames", type=int, default=None)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--graph", action="store_true", help="replay the batch from a CUDA graph")
@@ -772,6 +913,8 @@ def main():
     ap.add_argument("--e2e-planes", type=int, default=48)
     ap.add_argument("--e2e-chunks", type=int, default=8, help="sub-batches of the host pipeline")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-tc-vs-plain", action="store_true",
+                    help="skip the wide-filter tensor-core vs plain FP32 comparison of the default line")
     ap.add_argument("--engine", default=None, choices=["auto", "cuda", "tensor"],
                     help="override every job's engine (cuda = the plain CUDA-core kernels)")
     args = ap.parse_args()

@@ -102,6 +102,13 @@ class Oracle:
         L.orc_resize_plane.argtypes = [C.c_int, C.c_uint, C.c_int, C.c_double, C.c_double, C.c_uint, C.c_uint,
                                        C.c_uint, C.c_uint, C.c_double, C.c_double, C.c_double, C.c_double,
                                        C.c_int, C.c_int, C.c_void_p, C.c_ssize_t, C.c_void_p, C.c_ssize_t]
+        L.orc_plan_create.restype = C.c_void_p
+        L.orc_plan_create.argtypes = [C.c_int, C.c_uint, C.c_int, C.c_double, C.c_double, C.c_uint, C.c_uint,
+                                      C.c_uint, C.c_uint, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int]
+        L.orc_plan_tmp_size.restype = C.c_size_t
+        L.orc_plan_tmp_size.argtypes = [C.c_void_p]
+        L.orc_plan_run.argtypes = [C.c_void_p, C.c_void_p, C.c_ssize_t, C.c_void_p, C.c_ssize_t, C.c_void_p]
+        L.orc_plan_free.argtypes = [C.c_void_p]
         L.orc_resize_pass.argtypes = [C.c_int, C.c_uint, C.c_int, C.c_int, C.c_double, C.c_double, C.c_uint,
                                       C.c_uint, C.c_uint, C.c_double, C.c_double, C.c_int, C.c_int, C.c_void_p,
                                       C.c_ssize_t, C.c_void_p, C.c_ssize_t]
@@ -202,6 +209,19 @@ class Oracle:
             raise ValueError(f"resize failed ({rc})")
         return out
 
+    def plan(self, src_w, src_h, dst_w, dst_h, kind, a=math.nan, b=math.nan, dtype=np.uint16, depth=None,
+             shift_w=0.0, shift_h=0.0, subwidth=None, subheight=None, mode="c") -> "Plan":
+        """A conversion planned once (filter contexts built) and run on many
+        planes, each run on the calling thread (zimg_oracle.c orc_plan_*)."""
+        t = T_U16 if np.dtype(dtype) == np.uint16 else T_F32
+        depth = (16 if t == T_U16 else 32) if depth is None else depth
+        h = self.lib.orc_plan_create(t, depth, _f(kind), a, b, src_w, src_h, dst_w, dst_h, shift_w, shift_h,
+                                     float(src_w if subwidth is None else subwidth),
+                                     float(src_h if subheight is None else subheight), 1 if mode == "fma" else 0)
+        if not h:
+            raise ValueError("plan failed")
+        return Plan(self.lib, h, np.dtype(dtype), (dst_h, dst_w))
+
     def resize_pass(self, src: np.ndarray, horizontal: bool, dst_dim: int, kind, a=math.nan, b=math.nan, depth=None,
                     shift=0.0, subwidth=None, mode="c", nthreads=1) -> np.ndarray:
         src = np.ascontiguousarray(src)
@@ -221,6 +241,30 @@ class Oracle:
         if rc:
             raise ValueError(f"resize failed ({rc})")
         return out
+
+
+class Plan:
+    """One planned conversion of the restatement; run() resizes one plane on
+    the calling thread (the foreign call releases the GIL, so Python threads
+    run planes in parallel)."""
+
+    def __init__(self, lib, handle, dtype, out_shape):
+        self.lib, self.h, self.dtype, self.out_shape = lib, handle, dtype, out_shape
+        self.tmp_size = int(lib.orc_plan_tmp_size(handle))
+
+    def run(self, src: np.ndarray, out: np.ndarray, tmp: np.ndarray | None = None):
+        it = self.dtype.itemsize
+        if tmp is None and self.tmp_size:
+            tmp = np.empty(self.tmp_size, np.uint8)
+        rc = self.lib.orc_plan_run(self.h, src.ctypes.data, src.strides[0] // it, out.ctypes.data,
+                                   out.strides[0] // it, None if tmp is None else tmp.ctypes.data)
+        if rc:
+            raise ValueError(f"plan run failed ({rc})")
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.orc_plan_free(self.h)
+            self.h = None
 
 
 class Reference:

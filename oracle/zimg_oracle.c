@@ -605,6 +605,112 @@ int orc_resize_plane(int type, unsigned depth, int kind, double a, double b,
 	return rc;
 }
 
+/*
+ * A conversion planned once and run on many planes, as zimg's graph is built
+ * once and then processes frames (graphapp.cpp:355-425): the filter contexts
+ * of ResizeConversion's passes (resize.cpp:38-104) are computed at creation,
+ * and each run resizes one plane on the calling thread, with the
+ * intermediate plane in caller-provided scratch. This serves the CPU
+ * baseline, which runs frames in parallel on every host thread.
+ */
+typedef struct orc_plan {
+	int type, n, order[2], use_fma;
+	unsigned depth, src_w, src_h, dst_w, dst_h, mid_w, mid_h;
+	orc_ctx ctx[2];
+} orc_plan;
+
+void orc_plan_free(orc_plan *p)
+{
+	if (!p)
+		return;
+	for (int i = 0; i < p->n; ++i)
+		ctx_free(&p->ctx[i]);
+	free(p);
+}
+
+orc_plan *orc_plan_create(int type, unsigned depth, int kind, double a, double b,
+                          unsigned src_w, unsigned src_h, unsigned dst_w, unsigned dst_h,
+                          double shift_w, double shift_h, double subwidth, double subheight, int use_fma)
+{
+	orc_plan *p = calloc(1, sizeof(orc_plan));
+	if (!p)
+		return NULL;
+	p->type = type;
+	p->depth = depth;
+	p->use_fma = use_fma;
+	p->src_w = src_w;
+	p->src_h = src_h;
+	p->dst_w = dst_w;
+	p->dst_h = dst_h;
+	int n = orc_plan_order(src_w, src_h, dst_w, dst_h, shift_w, shift_h, subwidth, subheight, p->order);
+	unsigned cur_w = src_w, cur_h = src_h;
+	for (int i = 0; i < n; ++i) {
+		int h = p->order[i];
+		int rc = h ? ctx_make(&p->ctx[i], kind, a, b, cur_w, dst_w, shift_w, subwidth)
+		           : ctx_make(&p->ctx[i], kind, a, b, cur_h, dst_h, shift_h, subheight);
+		if (rc) {
+			orc_plan_free(p);
+			return NULL;
+		}
+		p->n = i + 1;
+		if (h)
+			cur_w = dst_w;
+		else
+			cur_h = dst_h;
+		if (i == 0) {
+			p->mid_w = cur_w;
+			p->mid_h = cur_h;
+		}
+	}
+	p->n = n;
+	return p;
+}
+
+size_t orc_plan_tmp_size(const orc_plan *p)
+{
+	return p->n == 2 ? (size_t)p->mid_w * p->mid_h * type_size(p->type) : 0;
+}
+
+int orc_plan_run(const orc_plan *p, const void *src, ptrdiff_t src_stride, void *dst, ptrdiff_t dst_stride, void *tmp)
+{
+	size_t ts = type_size(p->type);
+	if (p->n == 0) {
+		for (unsigned i = 0; i < p->dst_h; ++i)
+			memcpy((char *)dst + (size_t)i * dst_stride * ts, (const char *)src + (size_t)i * src_stride * ts,
+			       (size_t)p->dst_w * ts);
+		return 0;
+	}
+	if (p->n == 2 && !tmp)
+		return -1;
+	unsigned cur_w = p->src_w, cur_h = p->src_h;
+	const void *cur = src;
+	ptrdiff_t cur_stride = src_stride;
+	for (int i = 0; i < p->n; ++i) {
+		int h = p->order[i];
+		orc_job job;
+		memset(&job, 0, sizeof(job));
+		job.ctx = &p->ctx[i];
+		job.horizontal = h;
+		job.type = p->type;
+		job.use_fma = p->use_fma;
+		job.pixel_max = (int32_t)((1UL << p->depth) - 1);
+		job.src = cur;
+		job.src_stride = cur_stride;
+		job.out_w = h ? p->dst_w : cur_w;
+		job.out_h = h ? cur_h : p->dst_h;
+		job.dst = i == p->n - 1 ? dst : tmp;
+		job.dst_stride = i == p->n - 1 ? dst_stride : (ptrdiff_t)job.out_w;
+		job.row_begin = 0;
+		job.row_end = job.out_h;
+		run_rows(&job);
+		cur = job.dst;
+		cur_stride = job.dst_stride;
+		cur_w = job.out_w;
+		cur_h = job.out_h;
+	}
+	return 0;
+}
+
 /* One pass (ResizeImplBuilder, resize_impl.cpp:245-267) on a whole plane. */
 int orc_resize_pass(int type, unsigned depth, int horizontal, int kind, double a, double b,
                     unsigned src_w, unsigned src_h, unsigned dst_dim, double shift, double subwidth,
