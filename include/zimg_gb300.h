@@ -298,8 +298,11 @@ ZG_API zg_error_code zg_resize_process(const zg_resize *r, const void *src, ptrd
  * real-time loop that must avoid cudaMalloc/cudaFree and their implicit
  * device-wide synchronisation). It allocates nothing: two-pass conversions
  * keep their intermediate plane in a scratch array compiled into the library,
- * ZG_NO_ALLOC_TMP_BYTES (32 MiB) per GPU, held from the first call on a device
- * until the process exits. A conversion whose zg_resize_get_tmp_size exceeds
+ * ZG_NO_ALLOC_TMP_BYTES (32 MiB) per GPU, held until the process exits from
+ * the time the library's module is loaded on that device (its first kernel
+ * launch or symbol lookup there under CUDA's default lazy loading; context
+ * creation under CUDA_MODULE_LOADING=EAGER, whether or not this entry point
+ * is ever called). A conversion whose zg_resize_get_tmp_size exceeds
  * that is rejected with ZG_ERROR_OUT_OF_MEMORY and nothing is launched.
  * The first call on each device looks up the array's device address
  * (cudaGetSymbolAddress) with that device current; make that first call

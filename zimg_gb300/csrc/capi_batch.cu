@@ -145,6 +145,33 @@ void batch_launch(const zg_batch *b, void *tmp, cudaStream_t st)
 	}
 }
 
+// Jobs whose fused plans have identical tables (the same conversion for many
+// frames, as zimg runs one graph over a stream of frames) read one device copy
+// of them: the first such job's. A launch then touches each distinct table
+// once, and it stays in L2 instead of being fetched again per job.
+void share_tables(zg_batch *b)
+{
+	std::map<std::pair<int, size_t>, std::vector<unsigned>> firsts;  // (variant, blob size) -> jobs owning a copy
+	for (unsigned i = 0; i < b->jobs.size(); ++i) {
+		zg_resize *r = b->jobs[i];
+		if (!r->fused || r->fplan.blob.empty())
+			continue;
+		fused_bind(r->fplan, r->fblob.get());
+		auto &cands = firsts[{ r->fplan.variant, r->fplan.blob.size() }];
+		bool shared = false;
+		for (unsigned f : cands) {
+			const FusedPlan &q = b->jobs[f]->fplan;
+			if (std::memcmp(q.blob.data(), r->fplan.blob.data(), q.blob.size()) == 0) {
+				fused_bind(r->fplan, b->jobs[f]->fblob.get());
+				shared = true;
+				break;
+			}
+		}
+		if (!shared)
+			cands.push_back(i);
+	}
+}
+
 // Tmp offsets, fused work segmentation and the persistent launch groups
 // (fused jobs grouped by kernel variant, in job order within a group).
 void regroup(zg_batch *b)
@@ -160,6 +187,7 @@ void regroup(zg_batch *b)
 	b->groups.clear();
 	b->table_host.clear();
 	b->table_dev.release();
+	share_tables(b);
 	// one wave of work items across the whole batch: split strips into row
 	// segments only as far as needed to fill the GPU
 	std::vector<FusedPlan *> all;
