@@ -271,7 +271,7 @@ bool plan_chain(const FilterTable &first, const FilterTable &second, bool h_firs
 
 SmemLayout chain_layout(const FusedPlan *const *plans, int n)
 {
-	int max_pxa = 0, in = 1, seg_groups = 1, depth = 1, kv = 1;
+	int max_pxa = 0, in = 1, seg_groups = 1, depth = 1, kv = 1, tiles = 1;
 	for (int i = 0; i < n; ++i) {
 		const FusedPlan &p = *plans[i];
 		max_pxa = std::max(max_pxa, p.max_pxa);
@@ -279,6 +279,7 @@ SmemLayout chain_layout(const FusedPlan *const *plans, int n)
 		seg_groups = std::max(seg_groups, p.job.groups);  // an item spans up to a whole strip
 		depth = std::max(depth, p.depth);
 		kv = std::max(kv, p.job.vs);
+		tiles = std::max(tiles, chain_detail::tiles_per_warp(p.job.vs, p.job.hw));
 	}
 	auto a16 = [](size_t x) { return static_cast<int>((x + 15) / 16 * 16); };
 	SmemLayout L{};
@@ -299,7 +300,7 @@ SmemLayout chain_layout(const FusedPlan *const *plans, int n)
 	off += a16(static_cast<size_t>(depth + 2) * kv * 2 * 32 * 16);
 	L.tile_off = off;
 	L.tile_pitch = chain_detail::kStageBytes / 2;
-	off += a16(static_cast<size_t>(chain_detail::kMaxWarps) * chain_detail::kWarpStage);
+	off += a16(static_cast<size_t>(chain_detail::kMaxWarps) * tiles * chain_detail::kTileStage);
 	L.vbase_off = off;
 	off += a16(static_cast<size_t>(seg_groups) * 4);
 	L.ring_off = L.stage_off = L.i_off = L.htaps_off = L.hleft_off = off;

@@ -387,7 +387,7 @@ chain_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 	char *vslots = smem + L.vcoef_off;
 	int *vb = reinterpret_cast<int *>(smem + L.vbase_off);
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-	char *stage = smem + L.tile_off + warp * kWarpStage;
+	char *stage = smem + L.tile_off + warp * tiles_per_warp(KV, KH) * kTileStage;
 	const int IR = L.in_rows;
 	const int P = L.pitch * 2;
 	constexpr int kSlotBytes = KV * 2 * 32 * 16;

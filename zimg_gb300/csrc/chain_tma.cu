@@ -89,7 +89,7 @@ bool chain_tma_enabled()
 
 bool chain_tma_layout(const FusedPlan *const *plans, int n, SmemLayout *out)
 {
-	int max_pxa = 0, in = 1, groups = 1, depth = 1, kv = 1;
+	int max_pxa = 0, in = 1, groups = 1, depth = 1, kv = 1, tiles = 1;
 	for (int i = 0; i < n; ++i) {
 		const FusedPlan &p = *plans[i];
 		if (!p.chain)
@@ -99,8 +99,15 @@ bool chain_tma_layout(const FusedPlan *const *plans, int n, SmemLayout *out)
 		groups = std::max(groups, p.job.groups);
 		depth = std::max(depth, p.depth);
 		kv = std::max(kv, p.job.vs);
+		tiles = std::max(tiles, chain_detail::tiles_per_warp(p.job.vs, p.job.hw));
 	}
 	auto a16 = [](size_t x) { return static_cast<int>((x + 15) / 16 * 16); };
+	auto pow2 = [](int x) {
+		int p = 1;
+		while (p < x)
+			p *= 2;
+		return p;
+	};
 	SmemLayout L{};
 	// box rows of 16 mod 32 bytes (8 mod 16 samples) covering the widest
 	// window: 4-byte fragment loads of 8 lines x 4 pairs hit 32 different
@@ -108,34 +115,41 @@ bool chain_tma_layout(const FusedPlan *const *plans, int n, SmemLayout *out)
 	L.pitch = std::max(8, (max_pxa - 8 + 15) / 16 * 16 + 8);
 	if (L.pitch > kMaxBoxW)
 		return false;
-	// blocks covering any window span of `in` lines, block-rounded at both
-	// ends, rounded up to a power of two (ring lines under a mask)
-	int blocks = (in + 2 * (chain_detail::kBlockLines - 1)) / chain_detail::kBlockLines + 1;
-	int nb = 1;
-	while (nb < blocks)
-		nb *= 2;
-	L.in_rows = nb * chain_detail::kBlockLines;
-	L.depth = depth;
-	L.ring_rows = depth + 2;  // pipeline stages
 	L.stage_rows = 1;
 	L.seg_groups = groups;
 	L.step_groups = 1;
-	int off = 0;
-	L.in_off = off;
-	off += a16(static_cast<size_t>(L.in_rows) * L.pitch * 2);
-	L.vcoef_off = off;
-	off += a16(static_cast<size_t>(L.ring_rows) * kv * 2 * 32 * 16);
-	L.tile_off = off;
-	L.tile_pitch = chain_detail::kStageBytes / 2;
-	off += a16(static_cast<size_t>(chain_detail::kWsWarps) * chain_detail::kWarpStage);
-	L.vbase_off = off;
-	off += a16(static_cast<size_t>(groups) * 4);
-	L.stage_off = off;  // full and empty mbarriers
-	off += a16(static_cast<size_t>(L.ring_rows) * 2 * 8);
-	L.ring_off = L.i_off = L.htaps_off = L.hleft_off = off;
-	L.total_bytes = off + kAlignSlack;
-	*out = L;
-	return static_cast<size_t>(L.total_bytes) <= kTmaSmemMax;
+	L.depth = depth;
+	// ring: 2^n blocks, as many as cover the plan's lines in flight, but no
+	// fewer than a window's blocks plus one (a window of 16 KV lines touches
+	// KV + 1 blocks); stages: the plan's depth + 2, no fewer than 3. The
+	// largest ring, then the most stages, that fit the shared-memory budget.
+	const int nb_want = pow2((in + 2 * (chain_detail::kBlockLines - 1)) / chain_detail::kBlockLines + 1);
+	const int nb_min = pow2(kv + 2);
+	for (int nb = nb_want; nb >= nb_min; nb /= 2) {
+		for (int ns = depth + 2; ns >= 3; --ns) {
+			L.in_rows = nb * chain_detail::kBlockLines;
+			L.ring_rows = ns;  // pipeline stages
+			int off = 0;
+			L.in_off = off;
+			off += a16(static_cast<size_t>(L.in_rows) * L.pitch * 2);
+			L.vcoef_off = off;
+			off += a16(static_cast<size_t>(L.ring_rows) * kv * 2 * 32 * 16);
+			L.tile_off = off;
+			L.tile_pitch = chain_detail::kStageBytes / 2;
+			off += a16(static_cast<size_t>(chain_detail::kWsWarps) * tiles * chain_detail::kTileStage);
+			L.vbase_off = off;
+			off += a16(static_cast<size_t>(groups) * 4);
+			L.stage_off = off;  // full and empty mbarriers
+			off += a16(static_cast<size_t>(L.ring_rows) * 2 * 8);
+			L.ring_off = L.i_off = L.htaps_off = L.hleft_off = off;
+			L.total_bytes = off + kAlignSlack;
+			if (static_cast<size_t>(L.total_bytes) <= kTmaSmemMax) {
+				*out = L;
+				return true;
+			}
+		}
+	}
+	return false;
 }
 
 bool encode_tensor_map_2d(CUtensorMap *map, CUtensorMapDataType type, const void *base, uint64_t width,

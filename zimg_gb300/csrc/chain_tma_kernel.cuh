@@ -427,7 +427,7 @@ chain_tma_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_item
 				e.bias_h2 = *reinterpret_cast<const uint32_t *>(&b);
 			}
 			// stores: one 16-byte chunk per lane and store (see chain_kernel.cuh)
-			char *stage = smem + L.tile_off + warp * kWarpStage;
+			char *stage = smem + L.tile_off + warp * T * kTileStage;
 			char *st_addr = stage + (((lane >> 4) << 3) + (lane & 7)) * kStageBytes + ((lane >> 3) & 1) * 16;
 			constexpr int kStoreRows = store_rows(T);
 			constexpr int kStores = 16 / kStoreRows;
