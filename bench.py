@@ -906,7 +906,9 @@ def main():
     ap.add_argument("--workload", default="fhd_uhd_u16")
     ap.add_argument("--frames", type=int, default=None)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--graph", action="store_true", help="replay the batch from a CUDA graph")
+    ap.add_argument("--graph", action="store_true", default=None,
+                    help="replay the batch from a CUDA graph (the default for yuv420_batch)")
+    ap.add_argument("--no-graph", dest="graph", action="store_false")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
@@ -919,6 +921,8 @@ def main():
                     help="override every job's engine (cuda = the plain CUDA-core kernels)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.graph is None:
+        args.graph = args.workload == "yuv420_batch"
     if args.impl == "reference":
         run_reference(args)
     elif args.workload.startswith("depth_"):

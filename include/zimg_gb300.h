@@ -352,7 +352,11 @@ ZG_API zg_error_code zg_batch_process_graph(zg_batch *b, void *tmp, zg_stream st
  * (optional) receives the number of jobs whose plan changed.
  */
 ZG_API zg_error_code zg_batch_autotune(zg_batch *b, zg_stream stream, unsigned *changed);
-/* Number of kernel launches one zg_batch_process issues. */
+/* Number of kernel launches one zg_batch_process issues. Where every chained
+ * u16 job's source plane admits a tensor map (16-byte aligned base and
+ * stride, set by zg_batch_set_io), the chained jobs of all kernel variants and
+ * the identity planes run as one persistent launch whose CTAs take unit
+ * ranges of equal estimated cost. */
 ZG_API zg_error_code zg_batch_get_launch_count(const zg_batch *b, unsigned *out);
 
 /* ---------------------------------------------------------------- graph --

@@ -340,9 +340,9 @@ def test_batch_matches_single(cuda, oracle):
 
 
 def test_batch_identity_planes_copied(cuda):
-    """Identity conversions in a batch (no pass, resize.cpp:43-47) go through
-    one batched copy launch: exact copies for aligned and unaligned planes,
-    u16 and f32, next to a real conversion."""
+    """Identity conversions in a batch (no pass, resize.cpp:43-47) are copied
+    in the same persistent launch as the chained conversion next to them:
+    exact copies for aligned and unaligned planes, u16 and f32."""
     import torch
     import zimg_gb300 as zg
     rng = np.random.default_rng(6)
@@ -367,7 +367,7 @@ def test_batch_identity_planes_copied(cuda):
     dsts.append(empty(60, 80, np.uint16))
     b = zg.Batch(convs)
     b.set_io(srcs, dsts)
-    assert b.launch_count == 2  # one copy launch for the four identity planes, one fused launch
+    assert b.launch_count == 1  # the chained conversion and the four identity planes in one launch
     for mode in ("plain", "graph"):
         for d in dsts:
             d.zero_()

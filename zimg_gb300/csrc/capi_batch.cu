@@ -46,6 +46,19 @@ struct zg_batch {
 	std::vector<PlaneCopy> copy_host;
 	DeviceBuffer copy_dev;
 	unsigned long long copy_chunks = 0;
+	// one launch for the chained groups and the identity copies together
+	// (chain_mixed_kernel), when every chained job's source plane has a
+	// tensor map: its own job table, tensor maps and per-CTA unit ranges
+	bool mixed_plan = false;
+	bool mixed_now = false;
+	SmemLayout mixed_layout{};
+	int mixed_grid = 0;
+	std::vector<int> mixed_jobs;        // batch job of each mixed table entry
+	std::vector<FusedJob> mixed_host;
+	DeviceBuffer mixed_dev;
+	std::vector<CUtensorMap> mixed_maps_host;
+	DeviceBuffer mixed_maps_dev;
+	DeviceBuffer mixed_ranges_dev;      // grid + 1 unit indices
 	cudaGraphExec_t graph = nullptr;
 	cudaStream_t graph_stream = nullptr;
 	void *graph_tmp = nullptr;
@@ -87,7 +100,18 @@ void batch_launch(const zg_batch *b, void *tmp, cudaStream_t st)
 		throw Error(kErrLogic, "zg_batch_set_io was not called");
 	const FusedJob *table = static_cast<const FusedJob *>(b->table_dev.get());
 	std::vector<std::function<void(cudaStream_t)>> work;
+	if (b->mixed_now) {
+		work.push_back([b](cudaStream_t s) {
+			cuda_check(launch_chain_mixed(static_cast<const FusedJob *>(b->mixed_dev.get()),
+			                              static_cast<int>(b->mixed_host.size()),
+			                              static_cast<const int *>(b->mixed_ranges_dev.get()), b->mixed_layout,
+			                              b->mixed_grid, s),
+			           "mixed batch launch");
+		});
+	}
 	for (const auto &g : b->groups) {
+		if (b->mixed_now && g.tma_plan)
+			continue;  // in the mixed launch
 		work.push_back([&g, table](cudaStream_t s) {
 			FusedJob unused{};
 			if (g.tma_now)
@@ -99,7 +123,7 @@ void batch_launch(const zg_batch *b, void *tmp, cudaStream_t st)
 				           "fused batch launch");
 		});
 	}
-	if (!b->copy_jobs.empty()) {
+	if (!b->copy_jobs.empty() && !b->mixed_now) {
 		work.push_back([b](cudaStream_t s) {
 			cuda_check(launch_plane_copies(static_cast<const PlaneCopy *>(b->copy_dev.get()),
 			                               static_cast<int>(b->copy_jobs.size()), b->copy_chunks, s),
@@ -172,6 +196,116 @@ void share_tables(zg_batch *b)
 	}
 }
 
+// Estimated cost of one work unit of a mixed launch, in bytes at full HBM
+// speed: the unit's share of its plane's algorithmic bytes over the fraction
+// of the HBM roofline its kind of work reaches alone on GB300: H-first groups
+// that reuse the previous group's products (2x upscales) ~70 %, other H-first
+// groups ~38 %, V-first downscales ~47 %, identity copies ~90 %.
+double unit_cost(const zg_resize *r, const FusedJob &j, bool copy)
+{
+	const double bpe = bytes_of(r->sample);
+	const double bytes = (static_cast<double>(r->params.src_width) * r->params.src_height +
+	                      static_cast<double>(r->params.dst_width) * r->params.dst_height) * bpe;
+	const double units = std::max(1, fused_items(j));
+	double eff = 0.9;
+	if (!copy) {
+		const bool hf = j.variant >= 12;
+		const double reuse = r->fplan.reuse_frac;
+		eff = hf ? 1.0 / (reuse / 0.70 + (1.0 - reuse) / 0.38) : 0.47;
+	}
+	return bytes / units / eff;
+}
+
+// The mixed launch (chain_mixed_kernel): every chained group whose layout
+// admits the TMA form and every identity copy in one persistent launch, the
+// units of each CTA balanced by estimated cost. Decided per plan here; used
+// when every source plane also has a tensor map (upload_io).
+void plan_mixed(zg_batch *b)
+{
+	b->mixed_plan = false;
+	b->mixed_now = false;
+	b->mixed_jobs.clear();
+	b->mixed_host.clear();
+	b->mixed_dev.release();
+	b->mixed_maps_dev.release();
+	b->mixed_ranges_dev.release();
+	if (!chain_tma_enabled())
+		return;
+	std::vector<const FusedPlan *> plans;
+	int chained_groups = 0;
+	for (const auto &g : b->groups) {
+		if (!g.tma_plan)
+			continue;
+		++chained_groups;
+		for (int e = g.first; e < g.first + g.count; ++e) {
+			for (size_t i = 0; i < b->jobs.size(); ++i)
+				if (b->table_index[i] == e) {
+					plans.push_back(&b->jobs[i]->fplan);
+					b->mixed_jobs.push_back(static_cast<int>(i));
+				}
+		}
+	}
+	// worth one launch when it replaces more than one
+	if (plans.empty() || chained_groups + (b->copy_jobs.empty() ? 0 : 1) < 2 ||
+	    !chain_tma_layout(plans.data(), static_cast<int>(plans.size()), &b->mixed_layout)) {
+		b->mixed_jobs.clear();
+		return;
+	}
+	for (int c : b->copy_jobs)
+		b->mixed_jobs.push_back(c);
+	std::vector<double> cost;
+	int units = 0;
+	for (size_t e = 0; e < b->mixed_jobs.size(); ++e) {
+		const zg_resize *r = b->jobs[b->mixed_jobs[e]];
+		FusedJob j{};
+		const bool copy = r->num_passes == 0;
+		if (copy) {
+			j.variant = chain_mixed_copy_variant();
+			j.src_w = static_cast<int>(r->params.dst_width * bytes_of(r->sample));
+			j.dst_w = static_cast<int>(r->params.dst_width);
+			j.dst_h = static_cast<int>(r->params.dst_height);
+			j.groups = (j.dst_h + 15) / 16;
+			j.strips = 1;
+			j.segments = j.groups;
+		} else {
+			j = r->fplan.job;
+		}
+		j.item_begin = units;
+		units += fused_items(j);
+		cost.push_back(unit_cost(r, j, copy));
+		b->mixed_host.push_back(j);
+	}
+	b->mixed_grid = std::min(chain_mixed_grid_size(static_cast<size_t>(b->mixed_layout.total_bytes)), units);
+	// per-CTA unit ranges of equal estimated cost
+	double total = 0;
+	for (size_t e = 0; e < b->mixed_host.size(); ++e)
+		total += cost[e] * fused_items(b->mixed_host[e]);
+	std::vector<int> begin(b->mixed_grid + 1, units);
+	begin[0] = 0;
+	double acc = 0;
+	size_t e = 0;
+	for (int c = 1; c < b->mixed_grid; ++c) {
+		const double target = total * c / b->mixed_grid;
+		while (e < b->mixed_host.size() && acc + cost[e] * fused_items(b->mixed_host[e]) <= target) {
+			acc += cost[e] * fused_items(b->mixed_host[e]);
+			++e;
+		}
+		int u = units;
+		if (e < b->mixed_host.size()) {
+			const int n = fused_items(b->mixed_host[e]);
+			u = b->mixed_host[e].item_begin + std::min(n, static_cast<int>((target - acc) / cost[e]));
+		}
+		begin[c] = std::max(begin[c - 1], u);
+	}
+	b->mixed_ranges_dev.reset(begin.size() * sizeof(int));
+	cuda_check(cudaMemcpy(b->mixed_ranges_dev.get(), begin.data(), begin.size() * sizeof(int), cudaMemcpyHostToDevice),
+	           "mixed batch ranges");
+	b->mixed_dev.reset(b->mixed_host.size() * sizeof(FusedJob));
+	b->mixed_maps_host.assign(b->mixed_host.size(), CUtensorMap{});
+	b->mixed_maps_dev.reset(b->mixed_host.size() * sizeof(CUtensorMap));
+	b->mixed_plan = true;
+}
+
 // Tmp offsets, fused work segmentation and the persistent launch groups
 // (fused jobs grouped by kernel variant, in job order within a group).
 void regroup(zg_batch *b)
@@ -237,6 +371,7 @@ void regroup(zg_batch *b)
 	b->copy_dev.release();
 	if (!b->copy_jobs.empty())
 		b->copy_dev.reset(b->copy_jobs.size() * sizeof(PlaneCopy));
+	plan_mixed(b);
 }
 
 // Plane pointers of the fused jobs into the device table (ordered on st; the
@@ -284,6 +419,34 @@ void upload_io(zg_batch *b, cudaStream_t st)
 		cuda_check(cudaMemcpyAsync(b->maps_dev.get(), b->maps_host.data(), b->maps_host.size() * sizeof(CUtensorMap),
 		                           cudaMemcpyHostToDevice, st),
 		           "batch io upload");
+	// the mixed launch: plane pointers, tensor maps of the chained entries
+	b->mixed_now = b->mixed_plan;
+	for (size_t e = 0; b->mixed_now && e < b->mixed_host.size(); ++e) {
+		const int i = b->mixed_jobs[e];
+		const zg_batch_io &x = b->io[i];
+		FusedJob &j = b->mixed_host[e];
+		if (j.variant == chain_mixed_copy_variant()) {
+			j.src = x.src;
+			j.src_stride = x.src_stride;
+			j.dst = x.dst;
+			j.dst_stride = x.dst_stride;
+			auto al = [](const void *q, ptrdiff_t sd) { return reinterpret_cast<uintptr_t>(q) % 16 == 0 && sd % 16 == 0; };
+			j.vec_ok = al(x.src, x.src_stride) && al(x.dst, x.dst_stride) && j.src_w % 16 == 0;
+			j.tmap = nullptr;
+		} else {
+			fused_set_io(j, x.src, x.src_stride, x.dst, x.dst_stride);
+			b->mixed_now = chain_tma_source_map(&b->mixed_maps_host[e], j, b->mixed_layout);
+			j.tmap = static_cast<const CUtensorMap *>(b->mixed_maps_dev.get()) + e;
+		}
+	}
+	if (b->mixed_now) {
+		cuda_check(cudaMemcpyAsync(b->mixed_maps_dev.get(), b->mixed_maps_host.data(),
+		                           b->mixed_maps_host.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice, st),
+		           "batch io upload");
+		cuda_check(cudaMemcpyAsync(b->mixed_dev.get(), b->mixed_host.data(), b->mixed_host.size() * sizeof(FusedJob),
+		                           cudaMemcpyHostToDevice, st),
+		           "batch io upload");
+	}
 	if (!b->copy_host.empty())
 		cuda_check(cudaMemcpyAsync(b->copy_dev.get(), b->copy_host.data(), b->copy_host.size() * sizeof(PlaneCopy),
 		                           cudaMemcpyHostToDevice, st), "batch io upload");
@@ -564,7 +727,15 @@ zg_error_code zg_batch_get_launch_count(const zg_batch *b, unsigned *out)
 	return guarded([&] {
 		if (!b || !out)
 			throw Error(kErrIllegalArgument, "null pointer");
-		unsigned n = static_cast<unsigned>(b->groups.size()) + (b->copy_jobs.empty() ? 0u : 1u);
+		unsigned n = 0;
+		if (b->mixed_now) {
+			// one launch for the chained groups and the copies; other groups apart
+			n = 1;
+			for (const auto &g : b->groups)
+				n += g.tma_plan ? 0u : 1u;
+		} else {
+			n = static_cast<unsigned>(b->groups.size()) + (b->copy_jobs.empty() ? 0u : 1u);
+		}
 		for (size_t i = 0; i < b->jobs.size(); ++i) {
 			if (b->table_index[i] >= 0)
 				continue;

@@ -266,6 +266,13 @@ bool plan_chain(const FilterTable &first, const FilterTable &second, bool h_firs
 	J.magic = 12582912.0f + offset;
 	J.pixel_max = static_cast<float>((1UL << depth) - 1);
 	p.variant = chain_variant(h_first, KV, KH);
+	J.variant = p.variant - 200;
+	// groups whose window starts 8 lines below the previous one reuse its
+	// horizontal products (H first, 16-line windows)
+	int reuse = 0;
+	for (int g = 1; g < groups; ++g)
+		reuse += (h_first && KV == 1 && gbase[g] - gbase[g - 1] == 8) ? 1 : 0;
+	p.reuse_frac = groups > 1 ? static_cast<float>(reuse) / (groups - 1) : 0.0f;
 	return true;
 }
 

@@ -219,6 +219,40 @@ cudaError_t launch_chain_tma(int variant, const FusedJob *jobs, int num_jobs, in
 	                        stream);
 }
 
+int chain_mixed_copy_variant()
+{
+	return chain_detail::kCopyVariant;
+}
+
+int chain_mixed_grid_size(size_t smem_bytes)
+{
+	int dev = 0, sms = 0, per_sm = 0;
+	cudaGetDevice(&dev);
+	cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+	const void *k = reinterpret_cast<const void *>(&chain_detail::chain_mixed_kernel);
+	cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kTmaSmemMax));
+	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, chain_detail::tma_threads(true), smem_bytes) !=
+	        cudaSuccess ||
+	    per_sm < 1)
+		per_sm = 1;
+	return std::max(1, sms) * per_sm;
+}
+
+cudaError_t launch_chain_mixed(const FusedJob *jobs, int num_jobs, const int *cta_begin, const SmemLayout &L, int grid,
+                               cudaStream_t stream)
+{
+	if (static_cast<size_t>(L.total_bytes) > kTmaSmemMax || !jobs || !cta_begin || grid < 1)
+		return cudaErrorInvalidValue;
+	const void *k = reinterpret_cast<const void *>(&chain_detail::chain_mixed_kernel);
+	cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kTmaSmemMax));
+	if (e != cudaSuccess)
+		return e;
+	SmemLayout layout = L;
+	void *args[] = { &jobs, &num_jobs, &cta_begin, &layout };
+	return cudaLaunchKernel(k, dim3(grid), dim3(chain_detail::tma_threads(true)), args,
+	                        static_cast<size_t>(L.total_bytes), stream);
+}
+
 int chain_tma_set_fault(int drop_group, unsigned long long wait_ns)
 {
 	if (cudaMemcpyToSymbol(chain_detail::g_chain_drop_group, &drop_group, sizeof(drop_group)) != cudaSuccess ||

@@ -254,11 +254,351 @@ __device__ __forceinline__ void vfirst_tiles(const char *ring, const uint32_t (&
 		              e.pack(dh1[j], 2));
 }
 
-// Kernel. Shared memory (SmemLayout, from a 128-byte aligned base): ring of
-// NB = in_rows / kBlockLines blocks of source lines, NB a power of two
-// (in_off); NS = ring_rows stages of vertical tap fragments (vcoef_off); one
-// staging tile pair per consumer warp (tile_off); the item's group bases
-// (vbase_off); NS full and NS empty mbarriers (stage_off).
+// Per-CTA pipeline state, shared by the items a CTA processes. Shared memory
+// (SmemLayout, from a 128-byte aligned base): ring of NB = in_rows /
+// kBlockLines blocks of source lines, NB a power of two (in_off); NS =
+// ring_rows stages of vertical tap fragments (vcoef_off); the staged tiles of
+// each consumer warp (tile_off); the item's group bases (vbase_off); NS full
+// and NS empty mbarriers (stage_off).
+struct Pipe {
+	char *smem, *ring, *vslots;
+	int *vb;
+	uint64_t *full, *empty;
+	int *abort_item;
+	int NS, NB, P, warp, lane;
+	unsigned line_mask;
+	bool producer;
+	unsigned long long wait_ns;
+	// groups since the kernel started: `base` is the current item's first
+	// group; the producer also tracks `released` (groups every consumer warp
+	// has finished, as observed on the empty barriers) and `issued`
+	unsigned base, released, issued;
+	int error;
+};
+
+__device__ __forceinline__ void pipe_init(Pipe &p, float4 *smem4, const SmemLayout &L, int *abort_item)
+{
+	// tensor copies land on 128-byte boundaries: align the layout's base (by
+	// an offset from the shared array, so that every access through these
+	// pointers stays a shared-memory access)
+	char *smem = reinterpret_cast<char *>(smem4);
+	smem += (128u - (smem_addr(smem) & 127u)) & 127u;
+	p.smem = smem;
+	p.ring = smem + L.in_off;
+	p.vslots = smem + L.vcoef_off;
+	p.vb = reinterpret_cast<int *>(smem + L.vbase_off);
+	p.full = reinterpret_cast<uint64_t *>(smem + L.stage_off);
+	p.NS = L.ring_rows;
+	p.empty = p.full + p.NS;
+	p.abort_item = abort_item;
+	p.warp = threadIdx.x >> 5;
+	p.lane = threadIdx.x & 31;
+	p.producer = p.warp == kWsWarps;
+	p.NB = L.in_rows / kBlockLines;
+	p.line_mask = static_cast<unsigned>(L.in_rows - 1);
+	p.P = L.pitch * 2;
+	p.wait_ns = g_chain_wait_ns ? g_chain_wait_ns : kWaitNs;
+	p.base = p.released = p.issued = 0;
+	p.error = 0;
+	if (threadIdx.x == 0) {
+		for (int s = 0; s < p.NS; ++s) {
+			mbar_init(&p.full[s], 1);
+			mbar_init(&p.empty[s], kWsWarps);
+		}
+		asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+		*abort_item = 0;
+	}
+	__syncthreads();
+}
+
+// Before the CTA leaves: a wait that ran out is recorded, and the producer
+// first waits (bounded) for its copies still in flight: only the last NS
+// issued groups can have any (an earlier group's stage was reissued only
+// after every consumer had read it); a dropped group has none.
+__device__ __forceinline__ void pipe_finish(Pipe &p)
+{
+	if (p.producer && p.lane == 0 && (p.error || *p.abort_item)) {
+		atomicCAS(&g_chain_pipeline_error, 0, p.error ? p.error : 1);
+		const int drop = blockIdx.x == 0 ? g_chain_drop_group : -1;
+		for (unsigned g = p.issued > static_cast<unsigned>(p.NS) ? p.issued - p.NS : 0; g < p.issued; ++g)
+			if (static_cast<int>(g) != drop)
+				mbar_wait_for(&p.full[g % p.NS], (g / p.NS) & 1, p.wait_ns);
+	} else if (!p.producer && p.lane == 0 && p.error) {
+		atomicCAS(&g_chain_pipeline_error, 0, p.error);
+	}
+}
+
+// One item: groups g_begin .. g_begin + ngroups - 1 of strip `strip` of job
+// J, the group bases already in p.vb. The producer warp brings the data in;
+// the consumer warps compute and store. Both sides pass one CTA barrier
+// (group bases visible, the previous item finished).
+template <bool H_FIRST, int KV, int KH>
+__device__ __forceinline__ void chain_item(Pipe &p, const SmemLayout &L, const FusedJob &J, const void *tmap, int strip,
+                                           int g_begin, int ngroups)
+{
+	constexpr int kSlotBytes = KV * 2 * 32 * 16;
+	constexpr int T = tiles_per_warp(KV, KH);
+	constexpr int kStripTiles = kWsWarps * T;
+	const int NS = p.NS, NB = p.NB, P = p.P, warp = p.warp, lane = p.lane;
+	const unsigned line_mask = p.line_mask;
+	const unsigned long long wait_ns = p.wait_ns;
+	char *const smem = p.smem;
+	char *const ring = p.ring;
+	char *const vslots = p.vslots;
+	const int *const vb = p.vb;
+	uint64_t *const full = p.full;
+	uint64_t *const empty = p.empty;
+	const bool producer = p.producer;
+	if (producer) {
+		__syncthreads();  // group bases visible; every warp is done with the previous item
+		if (lane == 0 && !p.error) {
+						const char *vtab = reinterpret_cast<const char *>(J.v_dense);
+			const int xlo = __ldg(J.win_col + 2 * strip);
+			const int drop = blockIdx.x == 0 ? g_chain_drop_group : -1;
+			// next source block to load; first group of the item whose
+			// window starts at or after the block being replaced
+			int next_blk = vb[0] / kBlockLines;
+			int gneed = 0;
+			// advance `p.released` to n; false when a wait ran out
+			int rel_s = static_cast<int>(p.released % NS);
+			unsigned rel_ph = (p.released / NS) & 1;
+			auto release_to = [&](unsigned n) -> bool {
+				while (p.released < n) {
+					if (!mbar_wait_for(&empty[rel_s], rel_ph, wait_ns))
+						return false;
+					++p.released;
+					if (++rel_s == NS) {
+						rel_s = 0;
+						rel_ph ^= 1;
+					}
+				}
+				return true;
+			};
+			int s = static_cast<int>(p.base % NS);
+			const int in_blks = (J.src_h + kBlockLines - 1) / kBlockLines;
+			asm volatile("prefetch.tensormap [%0];\n" ::"l"(tmap) : "memory");
+			for (int k = 0; k < ngroups; ++k, s = s + 1 == NS ? 0 : s + 1) {
+				const unsigned g = p.base + k;
+				// the stage's fragment slot was last read by group g - NS
+				if (g >= static_cast<unsigned>(NS) && !release_to(g - NS + 1)) {
+					p.error = 2;
+					break;
+				}
+				const int last_blk = (vb[k] + 16 * KV - 1) / kBlockLines;
+				for (int b = next_blk; b <= last_blk && !p.error; ++b) {
+					// ring block b mod NB held block b - NB, which groups
+					// read up to the first one whose window starts past it
+					while (gneed < ngroups && vb[gneed] < (b - NB + 1) * kBlockLines)
+						++gneed;
+					if (gneed > k)
+						p.error = 3;  // the ring cannot hold one window
+					else if (!release_to(p.base + gneed))
+						p.error = 2;
+				}
+				if (p.error)
+					break;
+				if (static_cast<int>(g) == drop) {
+					// test hook: this group's stage is never armed
+					p.issued = g + 1;
+					continue;
+				}
+				// blocks wholly below the plane (windows are padded to
+				// 16 KV lines; their taps there are zero) become zero
+				// lines, written here, not copied
+				const int copy_end = min(last_blk + 1, in_blks);
+				const int ncopy = max(0, copy_end - next_blk);
+				for (int b = max(next_blk, in_blks); b <= last_blk; ++b) {
+					float4 *z = reinterpret_cast<float4 *>(ring + (b & (NB - 1)) * kBlockLines * P);
+					for (int i = 0; i < kBlockLines * P / 16; ++i)
+						z[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+					// later tensor copies into this block come after these stores
+					asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+				}
+				mbar_arrive_expect_tx(&full[s], static_cast<unsigned>(kSlotBytes + ncopy * kBlockLines * P));
+				for (int b = next_blk; b < copy_end; ++b)
+					tma_load_2d(ring + (b & (NB - 1)) * kBlockLines * P, tmap, xlo, b * kBlockLines, &full[s]);
+				bulk_load(vslots + s * kSlotBytes, vtab + static_cast<size_t>(g_begin + k) * kSlotBytes,
+				          kSlotBytes, &full[s]);
+				next_blk = max(next_blk, last_blk + 1);
+				p.issued = g + 1;
+			}
+			if (p.error)
+				*p.abort_item = 1;  // benign race: every writer stores 1
+		}
+	} else {
+		const int xlo = __ldg(J.win_col + 2 * strip);
+		const int gid = lane >> 2, tig = lane & 3;
+		const int ntiles = (J.dst_w + kTileW - 1) / kTileW;
+		const int tile0 = strip * kStripTiles + warp * T;
+		const bool active = tile0 * kTileW < J.dst_w;
+		uint4 ah[T][KH][2];
+		uint32_t colb[T];
+		uint32_t carry[T][2];
+#pragma unroll
+		for (int j = 0; j < T; ++j) {
+			const int tile = min(tile0 + j, ntiles - 1);
+			const uint4 *hf = reinterpret_cast<const uint4 *>(J.h_taps) + static_cast<size_t>(tile) * KH * 2 * 32 + lane;
+#pragma unroll
+			for (int ks = 0; ks < KH; ++ks) {
+				ah[j][ks][0] = __ldg(hf + (ks * 2 + 0) * 32);
+				ah[j][ks][1] = __ldg(hf + (ks * 2 + 1) * 32);
+			}
+			const int rel = __ldg(J.h_left + tile) - xlo;
+			colb[j] = H_FIRST ? static_cast<uint32_t>((rel + 2 * tig) * 2)
+			                  : static_cast<uint32_t>((rel + (lane >> 4) * 8) * 2);
+			carry[j][0] = carry[j][1] = 0;
+		}
+		Epi e;
+		e.magic = J.magic;
+		const uint32_t pm = static_cast<uint32_t>(J.pixel_max);
+		e.pmax2 = pm | (pm << 16);
+		{
+			const __half2 b = __floats2half2_rn(1024.0f + J.offset, 1024.0f + J.offset);
+			e.bias_h2 = *reinterpret_cast<const uint32_t *>(&b);
+		}
+		// stores: one 16-byte chunk per lane and store (see chain_kernel.cuh)
+		char *stage = smem + L.tile_off + warp * T * kTileStage;
+		char *st_addr = stage + (((lane >> 4) << 3) + (lane & 7)) * kStageBytes + ((lane >> 3) & 1) * 16;
+		constexpr int kStoreRows = store_rows(T);
+		constexpr int kStores = 16 / kStoreRows;
+		const int st_row = store_row(T, lane);
+		const int st_tile = store_tile(T, lane);
+		const char *ld_addr = stage + st_tile * kTileStage + st_row * kStageBytes + (lane & 1) * 16;
+		const int st_col = (tile0 + st_tile) * kTileW + (lane & 1) * 8;
+		const bool wide = J.vec_ok && st_col + 8 <= J.dst_w;
+		char *const dst = static_cast<char *>(J.dst);
+		const ptrdiff_t dst_stride = J.dst_stride;
+		char *drow = dst + static_cast<ptrdiff_t>(g_begin * 16 + st_row) * dst_stride + static_cast<ptrdiff_t>(st_col) * 2;
+		const ptrdiff_t group_step = 16 * dst_stride;
+		const ptrdiff_t store_step = kStoreRows * dst_stride;
+		// groups whose 16 rows all lie in the plane
+		const int full_groups = J.dst_h / 16 - g_begin;
+		// this lane's line in each 16-line window block
+		const int lrow = H_FIRST ? gid : (lane & 7) + ((lane >> 3) & 1) * 8;
+		__syncthreads();  // group bases visible; every warp is done with the previous item
+
+		int prev_vb = vb[0];
+		int s = static_cast<int>(p.base % NS);
+		unsigned ph = (p.base / NS) & 1;
+		for (int k = 0; k < ngroups; ++k) {
+			// every lane polls; the warp goes on only when all saw the copies land
+			if (!__all_sync(0xffffffffu, mbar_wait_for(&full[s], ph, wait_ns))) {
+				p.error = 1;
+				*p.abort_item = 1;  // benign race: every writer stores 1
+				break;
+			}
+			const int vbk = vb[k];
+			if (active) {
+				const uint4 *avs = reinterpret_cast<const uint4 *>(vslots + s * kSlotBytes) + lane;
+				uint4 av[KV][2];
+				if (H_FIRST) {
+					uint32_t roff[KV][2];
+#pragma unroll
+					for (int kv = 0; kv < KV; ++kv) {
+						roff[kv][0] = ((static_cast<unsigned>(vbk + 16 * kv + lrow)) & line_mask) * P;
+						roff[kv][1] = ((static_cast<unsigned>(vbk + 16 * kv + lrow + 8)) & line_mask) * P;
+					}
+					uint32_t bv[T][KV][2][2];
+					if (KV == 1 && k > 0 && vbk - prev_vb == 8)
+						hfirst_h<KV, KH, T, true>(ring, roff, colb, ah, carry, bv, e);
+					else
+						hfirst_h<KV, KH, T, false>(ring, roff, colb, ah, carry, bv, e);
+#pragma unroll
+					for (int kv = 0; kv < KV; ++kv) {
+						av[kv][0] = avs[(kv * 2 + 0) * 32];
+						av[kv][1] = avs[(kv * 2 + 1) * 32];
+					}
+					// the group's shared data are in registers: release the stage
+					__syncwarp();
+					if (lane == 0)
+						mbar_arrive(&empty[s]);
+					hfirst_v<KV, T>(bv, av, st_addr, e);
+				} else {
+#pragma unroll
+					for (int kv = 0; kv < KV; ++kv) {
+						av[kv][0] = avs[(kv * 2 + 0) * 32];
+						av[kv][1] = avs[(kv * 2 + 1) * 32];
+					}
+					uint32_t roff[KV];
+#pragma unroll
+					for (int kv = 0; kv < KV; ++kv)
+						roff[kv] = ((static_cast<unsigned>(vbk + 16 * kv + lrow)) & line_mask) * P;
+					vfirst_tiles<KV, KH, T>(ring, roff, colb, ah, av, st_addr, e);
+					// the group's shared data are in registers: release the stage
+					__syncwarp();
+					if (lane == 0)
+						mbar_arrive(&empty[s]);
+				}
+				__syncwarp();
+				if (wide && k < full_groups) {
+#pragma unroll
+					for (int i = 0; i < kStores; ++i)
+						*reinterpret_cast<uint4 *>(drow + i * store_step) =
+							*reinterpret_cast<const uint4 *>(ld_addr + i * kStoreRows * kStageBytes);
+				} else {
+					for (int i = 0; i < kStores; ++i) {
+						const int row = (g_begin + k) * 16 + st_row + i * kStoreRows;
+						if (row < J.dst_h && st_col < J.dst_w) {
+							const uint4 v = *reinterpret_cast<const uint4 *>(ld_addr + i * kStoreRows * kStageBytes);
+							uint16_t *d = reinterpret_cast<uint16_t *>(dst + static_cast<ptrdiff_t>(row) * dst_stride) + st_col;
+							if (J.vec_ok && st_col + 8 <= J.dst_w) {
+								*reinterpret_cast<uint4 *>(d) = v;
+							} else {
+								const uint32_t w[4] = { v.x, v.y, v.z, v.w };
+								for (int q = 0; q < 8 && st_col + q < J.dst_w; ++q)
+									d[q] = static_cast<uint16_t>(w[q >> 1] >> (16 * (q & 1)));
+							}
+						}
+					}
+				}
+				__syncwarp();
+			} else {
+				__syncwarp();
+				if (lane == 0)
+					mbar_arrive(&empty[s]);
+			}
+			prev_vb = vbk;
+			drow += group_step;
+			if (++s == NS) {
+				s = 0;
+				ph ^= 1;
+			}
+		}
+	}
+}
+
+// An identity plane's rows g_begin*16 .. (g_begin + ngroups)*16 - 1, copied
+// by every thread of the CTA, with no pipeline: a batch's identity
+// conversions ride in the same launch. The job's src_w is the row length in
+// bytes; vec_ok says whether planes, strides and rows allow 16-byte chunks.
+__device__ __forceinline__ void copy_item(const FusedJob &J, int g_begin, int ngroups)
+{
+	const int row0 = g_begin * 16, row1 = min(J.dst_h, (g_begin + ngroups) * 16);
+	const int row_bytes = J.src_w;
+	const int warps = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	// one warp per row, its lanes along the row
+	for (int r = row0 + warp; r < row1; r += warps) {
+		const char *s = static_cast<const char *>(J.src) + static_cast<ptrdiff_t>(r) * J.src_stride;
+		char *d = static_cast<char *>(J.dst) + static_cast<ptrdiff_t>(r) * J.dst_stride;
+		if (J.vec_ok) {
+			for (int c = lane * 16; c < row_bytes; c += 32 * 16)
+				*reinterpret_cast<uint4 *>(d + c) = __ldg(reinterpret_cast<const uint4 *>(s + c));
+		} else {
+			for (int c = lane; c < row_bytes; c += 32)
+				d[c] = s[c];
+		}
+	}
+}
+
+// Group bases of an item into shared memory (all threads).
+__device__ __forceinline__ void load_bases(Pipe &p, const FusedJob &J, int g_begin, int ngroups)
+{
+	for (int g = threadIdx.x; g < ngroups; g += blockDim.x)
+		p.vb[g] = __ldg(J.v_base + g_begin + g);
+}
+
+// Kernel for the jobs of one variant: each CTA an equal contiguous range of
+// the launch's (strip, 16-row group) units, job by job and strip by strip.
 template <bool H_FIRST, int KV, int KH>
 __global__ void __launch_bounds__(tma_threads(H_FIRST), 2)
 chain_tma_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, const __grid_constant__ FusedJob single,
@@ -266,293 +606,78 @@ chain_tma_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_item
 {
 	extern __shared__ float4 smem4[];
 	__shared__ int abort_item;
-	// tensor copies land on 128-byte boundaries: align the layout's base (by
-	// an offset from the shared array, so that every access through these
-	// pointers stays a shared-memory access)
-	char *smem = reinterpret_cast<char *>(smem4);
-	smem += (128u - (smem_addr(smem) & 127u)) & 127u;
-	char *ring = smem + L.in_off;
-	char *vslots = smem + L.vcoef_off;
-	int *vb = reinterpret_cast<int *>(smem + L.vbase_off);
-	uint64_t *full = reinterpret_cast<uint64_t *>(smem + L.stage_off);
-	const int NS = L.ring_rows;
-	uint64_t *empty = full + NS;
-	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-	constexpr int kSlotBytes = KV * 2 * 32 * 16;
-	constexpr int T = tiles_per_warp(KV, KH);
-	constexpr int kThreads = tma_threads(H_FIRST);
-	constexpr int kStripTiles = kWsWarps * T;
-	const bool producer = warp == kWsWarps;
-	const int IR = L.in_rows;
-	const int NB = IR / kBlockLines;
-	const unsigned line_mask = static_cast<unsigned>(IR - 1);
-	const int P = L.pitch * 2;
-	const unsigned long long wait_ns = g_chain_wait_ns ? g_chain_wait_ns : kWaitNs;
-
-	if (threadIdx.x == 0) {
-		for (int s = 0; s < NS; ++s) {
-			mbar_init(&full[s], 1);
-			mbar_init(&empty[s], kWsWarps);
-		}
-		asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-		abort_item = 0;
-	}
-	__syncthreads();
-
-	// pipeline counters (groups since the kernel started): `base` is the
-	// current item's first group; the producer also tracks `released` (groups
-	// every consumer warp has finished, as observed on the empty barriers)
-	// and `issued`
-	unsigned base = 0, released = 0, issued = 0;
-	int error = 0;
-
+	Pipe p;
+	pipe_init(p, smem4, L, &abort_item);
 	const int t_end = static_cast<int>(static_cast<long long>(blockIdx.x + 1) * total_items / gridDim.x);
 	for (int t = static_cast<int>(static_cast<long long>(blockIdx.x) * total_items / gridDim.x); t < t_end;) {
-		const FusedJob *Jp = jobs ? &jobs[find_job(jobs, num_jobs, t)] : &single;
-		const FusedJob &J = *Jp;
+		const FusedJob &J = jobs ? jobs[find_job(jobs, num_jobs, t)] : single;
 		const int local = t - J.item_begin;
 		const int strip = local / J.groups;
 		const int g_begin = local - strip * J.groups;
 		const int ngroups = min(J.groups - g_begin, t_end - t);
 		t += ngroups;
-		for (int g = threadIdx.x; g < ngroups; g += kThreads)
-			vb[g] = __ldg(J.v_base + g_begin + g);
-
-		if (producer) {
-			__syncthreads();  // group bases visible; every warp is done with the previous item
-			if (lane == 0 && !error) {
-				const void *tmap = jobs ? J.tmap : static_cast<const void *>(&single_map);
-				const char *vtab = reinterpret_cast<const char *>(J.v_dense);
-				const int xlo = __ldg(J.win_col + 2 * strip);
-				const int drop = blockIdx.x == 0 ? g_chain_drop_group : -1;
-				// next source block to load; first group of the item whose
-				// window starts at or after the block being replaced
-				int next_blk = vb[0] / kBlockLines;
-				int gneed = 0;
-				// advance `released` to n; false when a wait ran out
-				int rel_s = static_cast<int>(released % NS);
-				unsigned rel_ph = (released / NS) & 1;
-				auto release_to = [&](unsigned n) -> bool {
-					while (released < n) {
-						if (!mbar_wait_for(&empty[rel_s], rel_ph, wait_ns))
-							return false;
-						++released;
-						if (++rel_s == NS) {
-							rel_s = 0;
-							rel_ph ^= 1;
-						}
-					}
-					return true;
-				};
-				int s = static_cast<int>(base % NS);
-				const int in_blks = (J.src_h + kBlockLines - 1) / kBlockLines;
-				asm volatile("prefetch.tensormap [%0];\n" ::"l"(tmap) : "memory");
-				for (int k = 0; k < ngroups; ++k, s = s + 1 == NS ? 0 : s + 1) {
-					const unsigned g = base + k;
-					// the stage's fragment slot was last read by group g - NS
-					if (g >= static_cast<unsigned>(NS) && !release_to(g - NS + 1)) {
-						error = 2;
-						break;
-					}
-					const int last_blk = (vb[k] + 16 * KV - 1) / kBlockLines;
-					for (int b = next_blk; b <= last_blk && !error; ++b) {
-						// ring block b mod NB held block b - NB, which groups
-						// read up to the first one whose window starts past it
-						while (gneed < ngroups && vb[gneed] < (b - NB + 1) * kBlockLines)
-							++gneed;
-						if (gneed > k)
-							error = 3;  // the ring cannot hold one window
-						else if (!release_to(base + gneed))
-							error = 2;
-					}
-					if (error)
-						break;
-					if (static_cast<int>(g) == drop) {
-						// test hook: this group's stage is never armed
-						issued = g + 1;
-						continue;
-					}
-					// blocks wholly below the plane (windows are padded to
-					// 16 KV lines; their taps there are zero) become zero
-					// lines, written here, not copied
-					const int copy_end = min(last_blk + 1, in_blks);
-					const int ncopy = max(0, copy_end - next_blk);
-					for (int b = max(next_blk, in_blks); b <= last_blk; ++b) {
-						float4 *z = reinterpret_cast<float4 *>(ring + (b & (NB - 1)) * kBlockLines * P);
-						for (int i = 0; i < kBlockLines * P / 16; ++i)
-							z[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-						// later tensor copies into this block come after these stores
-						asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-					}
-					mbar_arrive_expect_tx(&full[s], static_cast<unsigned>(kSlotBytes + ncopy * kBlockLines * P));
-					for (int b = next_blk; b < copy_end; ++b)
-						tma_load_2d(ring + (b & (NB - 1)) * kBlockLines * P, tmap, xlo, b * kBlockLines, &full[s]);
-					bulk_load(vslots + s * kSlotBytes, vtab + static_cast<size_t>(g_begin + k) * kSlotBytes,
-					          kSlotBytes, &full[s]);
-					next_blk = max(next_blk, last_blk + 1);
-					issued = g + 1;
-				}
-				if (error)
-					abort_item = 1;  // benign race: every writer stores 1
-			}
-		} else {
-			const int xlo = __ldg(J.win_col + 2 * strip);
-			const int gid = lane >> 2, tig = lane & 3;
-			const int ntiles = (J.dst_w + kTileW - 1) / kTileW;
-			const int tile0 = strip * kStripTiles + warp * T;
-			const bool active = tile0 * kTileW < J.dst_w;
-			uint4 ah[T][KH][2];
-			uint32_t colb[T];
-			uint32_t carry[T][2];
-#pragma unroll
-			for (int j = 0; j < T; ++j) {
-				const int tile = min(tile0 + j, ntiles - 1);
-				const uint4 *hf = reinterpret_cast<const uint4 *>(J.h_taps) + static_cast<size_t>(tile) * KH * 2 * 32 + lane;
-#pragma unroll
-				for (int ks = 0; ks < KH; ++ks) {
-					ah[j][ks][0] = __ldg(hf + (ks * 2 + 0) * 32);
-					ah[j][ks][1] = __ldg(hf + (ks * 2 + 1) * 32);
-				}
-				const int rel = __ldg(J.h_left + tile) - xlo;
-				colb[j] = H_FIRST ? static_cast<uint32_t>((rel + 2 * tig) * 2)
-				                  : static_cast<uint32_t>((rel + (lane >> 4) * 8) * 2);
-				carry[j][0] = carry[j][1] = 0;
-			}
-			Epi e;
-			e.magic = J.magic;
-			const uint32_t pm = static_cast<uint32_t>(J.pixel_max);
-			e.pmax2 = pm | (pm << 16);
-			{
-				const __half2 b = __floats2half2_rn(1024.0f + J.offset, 1024.0f + J.offset);
-				e.bias_h2 = *reinterpret_cast<const uint32_t *>(&b);
-			}
-			// stores: one 16-byte chunk per lane and store (see chain_kernel.cuh)
-			char *stage = smem + L.tile_off + warp * T * kTileStage;
-			char *st_addr = stage + (((lane >> 4) << 3) + (lane & 7)) * kStageBytes + ((lane >> 3) & 1) * 16;
-			constexpr int kStoreRows = store_rows(T);
-			constexpr int kStores = 16 / kStoreRows;
-			const int st_row = store_row(T, lane);
-			const int st_tile = store_tile(T, lane);
-			const char *ld_addr = stage + st_tile * kTileStage + st_row * kStageBytes + (lane & 1) * 16;
-			const int st_col = (tile0 + st_tile) * kTileW + (lane & 1) * 8;
-			const bool wide = J.vec_ok && st_col + 8 <= J.dst_w;
-			char *const dst = static_cast<char *>(J.dst);
-			const ptrdiff_t dst_stride = J.dst_stride;
-			char *drow = dst + static_cast<ptrdiff_t>(g_begin * 16 + st_row) * dst_stride + static_cast<ptrdiff_t>(st_col) * 2;
-			const ptrdiff_t group_step = 16 * dst_stride;
-			const ptrdiff_t store_step = kStoreRows * dst_stride;
-			// groups whose 16 rows all lie in the plane
-			const int full_groups = J.dst_h / 16 - g_begin;
-			// this lane's line in each 16-line window block
-			const int lrow = H_FIRST ? gid : (lane & 7) + ((lane >> 3) & 1) * 8;
-			__syncthreads();  // group bases visible; every warp is done with the previous item
-
-			int prev_vb = vb[0];
-			int s = static_cast<int>(base % NS);
-			unsigned ph = (base / NS) & 1;
-			for (int k = 0; k < ngroups; ++k) {
-				// every lane polls; the warp goes on only when all saw the copies land
-				if (!__all_sync(0xffffffffu, mbar_wait_for(&full[s], ph, wait_ns))) {
-					error = 1;
-					abort_item = 1;  // benign race: every writer stores 1
-					break;
-				}
-				const int vbk = vb[k];
-				if (active) {
-					const uint4 *avs = reinterpret_cast<const uint4 *>(vslots + s * kSlotBytes) + lane;
-					uint4 av[KV][2];
-					if (H_FIRST) {
-						uint32_t roff[KV][2];
-#pragma unroll
-						for (int kv = 0; kv < KV; ++kv) {
-							roff[kv][0] = ((static_cast<unsigned>(vbk + 16 * kv + lrow)) & line_mask) * P;
-							roff[kv][1] = ((static_cast<unsigned>(vbk + 16 * kv + lrow + 8)) & line_mask) * P;
-						}
-						uint32_t bv[T][KV][2][2];
-						if (KV == 1 && k > 0 && vbk - prev_vb == 8)
-							hfirst_h<KV, KH, T, true>(ring, roff, colb, ah, carry, bv, e);
-						else
-							hfirst_h<KV, KH, T, false>(ring, roff, colb, ah, carry, bv, e);
-#pragma unroll
-						for (int kv = 0; kv < KV; ++kv) {
-							av[kv][0] = avs[(kv * 2 + 0) * 32];
-							av[kv][1] = avs[(kv * 2 + 1) * 32];
-						}
-						// the group's shared data are in registers: release the stage
-						__syncwarp();
-						if (lane == 0)
-							mbar_arrive(&empty[s]);
-						hfirst_v<KV, T>(bv, av, st_addr, e);
-					} else {
-#pragma unroll
-						for (int kv = 0; kv < KV; ++kv) {
-							av[kv][0] = avs[(kv * 2 + 0) * 32];
-							av[kv][1] = avs[(kv * 2 + 1) * 32];
-						}
-						uint32_t roff[KV];
-#pragma unroll
-						for (int kv = 0; kv < KV; ++kv)
-							roff[kv] = ((static_cast<unsigned>(vbk + 16 * kv + lrow)) & line_mask) * P;
-						vfirst_tiles<KV, KH, T>(ring, roff, colb, ah, av, st_addr, e);
-						// the group's shared data are in registers: release the stage
-						__syncwarp();
-						if (lane == 0)
-							mbar_arrive(&empty[s]);
-					}
-					__syncwarp();
-					if (wide && k < full_groups) {
-#pragma unroll
-						for (int i = 0; i < kStores; ++i)
-							*reinterpret_cast<uint4 *>(drow + i * store_step) =
-								*reinterpret_cast<const uint4 *>(ld_addr + i * kStoreRows * kStageBytes);
-					} else {
-						for (int i = 0; i < kStores; ++i) {
-							const int row = (g_begin + k) * 16 + st_row + i * kStoreRows;
-							if (row < J.dst_h && st_col < J.dst_w) {
-								const uint4 v = *reinterpret_cast<const uint4 *>(ld_addr + i * kStoreRows * kStageBytes);
-								uint16_t *d = reinterpret_cast<uint16_t *>(dst + static_cast<ptrdiff_t>(row) * dst_stride) + st_col;
-								if (J.vec_ok && st_col + 8 <= J.dst_w) {
-									*reinterpret_cast<uint4 *>(d) = v;
-								} else {
-									const uint32_t w[4] = { v.x, v.y, v.z, v.w };
-									for (int q = 0; q < 8 && st_col + q < J.dst_w; ++q)
-										d[q] = static_cast<uint16_t>(w[q >> 1] >> (16 * (q & 1)));
-								}
-							}
-						}
-					}
-					__syncwarp();
-				} else {
-					__syncwarp();
-					if (lane == 0)
-						mbar_arrive(&empty[s]);
-				}
-				prev_vb = vbk;
-				drow += group_step;
-				if (++s == NS) {
-					s = 0;
-					ph ^= 1;
-				}
-			}
-		}
-		base += ngroups;
+		load_bases(p, J, g_begin, ngroups);
+		chain_item<H_FIRST, KV, KH>(p, L, J, jobs ? J.tmap : static_cast<const void *>(&single_map), strip, g_begin,
+		                            ngroups);
+		p.base += ngroups;
 		__syncthreads();  // the next item rewrites the group bases and the ring
 		if (abort_item)
 			break;
 	}
+	pipe_finish(p);
+}
 
-	if (producer && lane == 0 && (error || abort_item)) {
-		atomicCAS(&g_chain_pipeline_error, 0, error ? error : 1);
-		// copies still in flight land before the CTA leaves: only the last NS
-		// issued groups can have any (an earlier group's stage was reissued
-		// only after every consumer had read it); a dropped group has none
-		const int drop = blockIdx.x == 0 ? g_chain_drop_group : -1;
-		for (unsigned g = issued > static_cast<unsigned>(NS) ? issued - NS : 0; g < issued; ++g)
-			if (static_cast<int>(g) != drop)
-				mbar_wait_for(&full[g % NS], (g / NS) & 1, wait_ns);
-	} else if (!producer && lane == 0 && error) {
-		atomicCAS(&g_chain_pipeline_error, 0, error);
+// Variant codes of mixed launches: the chained kernel's variant - 200
+// (H first, KV, KH), or kCopyVariant for an identity plane.
+constexpr int kCopyVariant = 1000;
+
+// One launch over a batch of mixed jobs: every chained variant and identity
+// copies, each CTA the range of units [cta_begin[b], cta_begin[b + 1]) (the
+// host balances the ranges by estimated cost); an item is dispatched on its
+// job's variant.
+__global__ void __launch_bounds__(tma_threads(true), 2)
+chain_mixed_kernel(const FusedJob *__restrict__ jobs, int num_jobs, const int *__restrict__ cta_begin,
+                   const __grid_constant__ SmemLayout L)
+{
+	extern __shared__ float4 smem4[];
+	__shared__ int abort_item;
+	Pipe p;
+	pipe_init(p, smem4, L, &abort_item);
+	const int t_end = __ldg(cta_begin + blockIdx.x + 1);
+	for (int t = __ldg(cta_begin + blockIdx.x); t < t_end;) {
+		const FusedJob &J = jobs[find_job(jobs, num_jobs, t)];
+		const int local = t - J.item_begin;
+		const int strip = local / J.groups;
+		const int g_begin = local - strip * J.groups;
+		const int ngroups = min(J.groups - g_begin, t_end - t);
+		t += ngroups;
+		const int v = J.variant;
+		if (v == kCopyVariant) {
+			copy_item(J, g_begin, ngroups);
+		} else {
+			load_bases(p, J, g_begin, ngroups);
+			switch (v) {
+#define ZG_CHAIN_CASE(HF, KV, KH)                                                                     \
+	case (HF ? 12 : 0) + (KV - 1) * 4 + (KH - 1):                                                      \
+		chain_item<HF, KV, KH>(p, L, J, J.tmap, strip, g_begin, ngroups);                            \
+		break;
+				ZG_CHAIN_CASE(true, 1, 1) ZG_CHAIN_CASE(true, 1, 2) ZG_CHAIN_CASE(true, 1, 3) ZG_CHAIN_CASE(true, 1, 4)
+				ZG_CHAIN_CASE(true, 2, 1) ZG_CHAIN_CASE(true, 2, 2) ZG_CHAIN_CASE(true, 2, 3) ZG_CHAIN_CASE(true, 2, 4)
+				ZG_CHAIN_CASE(true, 3, 1) ZG_CHAIN_CASE(true, 3, 2) ZG_CHAIN_CASE(true, 3, 3) ZG_CHAIN_CASE(true, 3, 4)
+				ZG_CHAIN_CASE(false, 1, 1) ZG_CHAIN_CASE(false, 1, 2) ZG_CHAIN_CASE(false, 1, 3) ZG_CHAIN_CASE(false, 1, 4)
+				ZG_CHAIN_CASE(false, 2, 1) ZG_CHAIN_CASE(false, 2, 2) ZG_CHAIN_CASE(false, 2, 3) ZG_CHAIN_CASE(false, 2, 4)
+				ZG_CHAIN_CASE(false, 3, 1) ZG_CHAIN_CASE(false, 3, 2) ZG_CHAIN_CASE(false, 3, 3) ZG_CHAIN_CASE(false, 3, 4)
+#undef ZG_CHAIN_CASE
+			default:
+				break;
+			}
+		}
+		p.base += J.variant == kCopyVariant ? 0 : ngroups;
+		__syncthreads();  // the next item rewrites the group bases and the ring
+		if (abort_item)
+			break;
 	}
+	pipe_finish(p);
 }
 
 } // namespace chain_detail

@@ -80,6 +80,7 @@ struct FusedJob {
 	float offset;           // 2^(depth-1)
 	int vec_ok;             // planes and strides 16-byte aligned: vector loads and stores
 	const void *tmap;       // TMA-pipelined chained kernel: the source plane's tensor map (device memory)
+	int variant;            // chained kernel's variant - 200 ((H first, KV, KH)); mixed launches dispatch on it
 };
 
 // Shared-memory layout of one launch (the maximum over its jobs).
@@ -107,6 +108,7 @@ struct FusedPlan {
 	int depth = 1;           // prefetch depth in steps
 	bool mma = false;        // tensor-core variant (mma_kernel.cuh or chain_kernel.cuh)
 	bool chain = false;      // tensor-core variant with the passes chained in registers (chain_kernel.cuh)
+	float reuse_frac = 0;    // chained H-first plans: share of groups that reuse the previous group's products
 	std::vector<unsigned char> blob;  // host copy of the tables, uploaded by the owner
 	size_t off_h_taps = 0, off_h_left = 0, off_v_dense = 0, off_v_base = 0, off_win_col = 0;
 };
@@ -175,6 +177,14 @@ cudaError_t launch_chain_tma(int variant, const FusedJob *jobs, int num_jobs, in
                              int grid, const FusedJob &single, const CUtensorMap *single_map, cudaStream_t stream);
 // Nonzero when a pipeline wait of that kernel ran out (optionally reset).
 int chain_tma_pipeline_error(bool reset);
+// One launch over a mixed batch (chained jobs of any variant, each FusedJob's
+// `variant`, and identity copies, variant chain_mixed_copy_variant(), src_w
+// = row bytes, groups = 16-row bands, strips = 1): CTA b processes the units
+// [cta_begin[b], cta_begin[b + 1]). L covers every chained job.
+int chain_mixed_copy_variant();
+int chain_mixed_grid_size(size_t smem_bytes);
+cudaError_t launch_chain_mixed(const FusedJob *jobs, int num_jobs, const int *cta_begin, const SmemLayout &L, int grid,
+                               cudaStream_t stream);
 // Test hook: CTA 0's producer skips group drop_group (-1: none) without
 // arming its stage; waits give up after wait_ns (0: the default 0.25 s).
 int chain_tma_set_fault(int drop_group, unsigned long long wait_ns);
