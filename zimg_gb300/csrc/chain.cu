@@ -123,6 +123,23 @@ bool plan_chain(const FilterTable &first, const FilterTable &second, bool h_firs
 	const int KV = (vspan + 15) / 16;
 	if (KV < 1 || KV > kChainKVMax)
 		return false;
+	// H first: window starts on multiples of 8 lines where that does not widen
+	// the windows past 16 KV lines, so that consecutive groups' windows share
+	// whole 8-line blocks, whose horizontal products the kernel keeps
+	if (h_first) {
+		int vspan8 = 0;
+		for (int g = 0; g < groups; ++g) {
+			int hi = INT_MIN;
+			for (int r = 0; r < 16 && g * 16 + r < static_cast<int>(dst_h); ++r) {
+				const unsigned i = static_cast<unsigned>(g * 16 + r);
+				hi = std::max(hi, static_cast<int>(V.left[i] + V.width));
+			}
+			vspan8 = std::max(vspan8, hi - gbase[g] / 8 * 8);
+		}
+		if ((vspan8 + 15) / 16 == KV)
+			for (int g = 0; g < groups; ++g)
+				gbase[g] = gbase[g] / 8 * 8;
+	}
 
 	// tiles of 16 output columns; window of 16*KH inputs from hstart, which is
 	// even (H first: 4-byte fragment loads) or a multiple of 8 (V first: ldmatrix rows)
@@ -267,12 +284,15 @@ bool plan_chain(const FilterTable &first, const FilterTable &second, bool h_firs
 	J.pixel_max = static_cast<float>((1UL << depth) - 1);
 	p.variant = chain_variant(h_first, KV, KH);
 	J.variant = p.variant - 200;
-	// groups whose window starts 8 lines below the previous one reuse its
-	// horizontal products (H first, 16-line windows)
-	int reuse = 0;
-	for (int g = 1; g < groups; ++g)
-		reuse += (h_first && KV == 1 && gbase[g] - gbase[g - 1] == 8) ? 1 : 0;
-	p.reuse_frac = groups > 1 ? static_cast<float>(reuse) / (groups - 1) : 0.0f;
+	// H first: the share of a window's 8-line blocks that a group can take
+	// over from the previous one (its window moved by a multiple of 8 lines)
+	double kept = 0;
+	for (int g = 1; g < groups; ++g) {
+		const int d = gbase[g] - gbase[g - 1];
+		if (h_first && d % 8 == 0 && d / 8 < 2 * KV)
+			kept += (2.0 * KV - d / 8) / (2.0 * KV);
+	}
+	p.reuse_frac = groups > 1 ? static_cast<float>(kept / (groups - 1)) : 0.0f;
 	return true;
 }
 

@@ -126,62 +126,59 @@ struct Epi {
 	}
 };
 
-// H first, horizontal stage: the warp's T tiles of one group, up to the
-// vertical pass's operands bv. roff[kv][h]: byte offsets in the ring of lines
-// gid + 8h of window block kv; colb[j]: tile j's byte offset of its window's
-// input column 2tig in a line. REUSE (KV == 1 only): lines 0-7 of the window
-// are the previous group's lines 8-15, whose products sit in carry. Each step
-// runs over all tiles before the next, so that the tiles' dependency chains
-// overlap in issue order.
-template <int KV, int KH, int T, bool REUSE>
-__device__ __forceinline__ void hfirst_h(const char *ring, const uint32_t (&roff)[KV][2], const uint32_t (&colb)[T],
-                                         const uint4 (&ah)[T][KH][2], uint32_t (&carry)[T][2],
-                                         uint32_t (&bv)[T][KV][2][2], const Epi &e)
+// H first, horizontal stage: the horizontal products of the 8-line blocks of
+// the group's window (blocks i = 0 .. 2 KV - 1, lines line0 + 8 i ..) for the
+// warp's T tiles, rounded and centred into the vertical pass's operands:
+// blk[j][i][c] holds block i of tile j for its output columns 8c .. 8c + 7
+// (k = lines 2tig, 2tig + 1, n = out col gid, as the mma accumulator leaves
+// them). Blocks i < keep were taken over from the previous group and are not
+// recomputed. colb[j]: tile j's byte offset of its window's input column 2tig
+// in a line. Each step runs over all tiles before the next, so that the
+// tiles' dependency chains overlap in issue order.
+template <int KV, int KH, int T, int KEEP>
+__device__ __forceinline__ void hfirst_h(const char *ring, unsigned line0, unsigned line_mask, int P, int lrow,
+                                         const uint32_t (&colb)[T], const uint4 (&ah)[T][KH][2],
+                                         uint32_t (&blk)[T][2 * KV][2], int keep, const Epi &e)
 {
 #pragma unroll
-	for (int kv = 0; kv < KV; ++kv) {
-		float dh0[T][4], dh1[T][4];  // window lines 0-7, 8-15 of block kv
+	for (int i = 0; i < 2 * KV; ++i) {
+		// KEEP >= 0: the number of kept blocks known at compile time
+		if (KEEP >= 0 ? i < KEEP : i < keep)
+			continue;
+		const char *row = ring + ((line0 + 8 * i + lrow) & line_mask) * P;
+		float dh[T][4];
 #pragma unroll
 		for (int ks = 0; ks < KH; ++ks) {
-			uint32_t b[T][4];
+			uint32_t b[T][2];
 #pragma unroll
 			for (int j = 0; j < T; ++j) {
-				const char *r0 = ring + roff[kv][0] + colb[j] + ks * 32;
-				const char *r1 = ring + roff[kv][1] + colb[j] + ks * 32;
-				if (!REUSE) {
-					b[j][0] = lds32(r0);
-					b[j][1] = lds32(r0 + 16);
-				}
-				b[j][2] = lds32(r1);
-				b[j][3] = lds32(r1 + 16);
+				b[j][0] = lds32(row + colb[j] + ks * 32);
+				b[j][1] = lds32(row + colb[j] + ks * 32 + 16);
 			}
 #pragma unroll
-			for (int j = 0; j < T; ++j) {
-				if (!REUSE)
-					mma2(dh0[j], ah[j][ks][0], ah[j][ks][1], e.centre(b[j][0]), e.centre(b[j][1]), ks == 0);
-				mma2(dh1[j], ah[j][ks][0], ah[j][ks][1], e.centre(b[j][2]), e.centre(b[j][3]), ks == 0);
-			}
+			for (int j = 0; j < T; ++j)
+				mma2(dh[j], ah[j][ks][0], ah[j][ks][1], e.centre(b[j][0]), e.centre(b[j][1]), ks == 0);
 		}
-		// Dh (out col gid / gid+8, lines 2tig..) -> V operands (k = lines, n = out col)
 #pragma unroll
 		for (int j = 0; j < T; ++j) {
-			if (REUSE) {
-				bv[j][kv][0][0] = carry[j][0];
-				bv[j][kv][1][0] = carry[j][1];
-			} else {
-				bv[j][kv][0][0] = e.pack_centre(dh0[j], 0);
-				bv[j][kv][1][0] = e.pack_centre(dh0[j], 2);
-			}
-			bv[j][kv][0][1] = e.pack_centre(dh1[j], 0);
-			bv[j][kv][1][1] = e.pack_centre(dh1[j], 2);
+			blk[j][i][0] = e.pack_centre(dh[j], 0);
+			blk[j][i][1] = e.pack_centre(dh[j], 2);
 		}
 	}
-	if (KV == 1) {
+}
+
+// Window moved by d 8-line blocks: block i becomes block i - d.
+template <int KV, int T>
+__device__ __forceinline__ void shift_blocks(uint32_t (&blk)[T][2 * KV][2], int d)
+{
+	for (int s = 0; s < d; ++s) {
 #pragma unroll
-		for (int j = 0; j < T; ++j) {
-			carry[j][0] = bv[j][0][0][1];
-			carry[j][1] = bv[j][0][1][1];
-		}
+		for (int j = 0; j < T; ++j)
+#pragma unroll
+			for (int i = 0; i + 1 < 2 * KV; ++i) {
+				blk[j][i][0] = blk[j][i + 1][0];
+				blk[j][i][1] = blk[j][i + 1][1];
+			}
 	}
 }
 
@@ -189,7 +186,7 @@ __device__ __forceinline__ void hfirst_h(const char *ring, const uint32_t (&roff
 // tiles at a time, each pair rounded and staged (row-major 8x8 blocks: out
 // row gid / gid+8, out cols 2tig..) before the next.
 template <int KV, int T>
-__device__ __forceinline__ void hfirst_v(const uint32_t (&bv)[T][KV][2][2], const uint4 (&av)[KV][2], char *st_addr,
+__device__ __forceinline__ void hfirst_v(const uint32_t (&blk)[T][2 * KV][2], const uint4 (&av)[KV][2], char *st_addr,
                                          const Epi &e)
 {
 	constexpr int P = T < 2 ? T : 2;
@@ -200,8 +197,8 @@ __device__ __forceinline__ void hfirst_v(const uint32_t (&bv)[T][KV][2][2], cons
 		for (int kv = 0; kv < KV; ++kv) {
 #pragma unroll
 			for (int q = 0; q < P; ++q) {
-				mma2(dv0[q], av[kv][0], av[kv][1], bv[j0 + q][kv][0][0], bv[j0 + q][kv][0][1], kv == 0);
-				mma2(dv1[q], av[kv][0], av[kv][1], bv[j0 + q][kv][1][0], bv[j0 + q][kv][1][1], kv == 0);
+				mma2(dv0[q], av[kv][0], av[kv][1], blk[j0 + q][2 * kv][0], blk[j0 + q][2 * kv + 1][0], kv == 0);
+				mma2(dv1[q], av[kv][0], av[kv][1], blk[j0 + q][2 * kv][1], blk[j0 + q][2 * kv + 1][1], kv == 0);
 			}
 		}
 #pragma unroll
@@ -332,7 +329,9 @@ __device__ __forceinline__ void pipe_finish(Pipe &p)
 // J, the group bases already in p.vb. The producer warp brings the data in;
 // the consumer warps compute and store. Both sides pass one CTA barrier
 // (group bases visible, the previous item finished).
-template <bool H_FIRST, int KV, int KH>
+// SPECIALISE: compile-time bodies for the common reuse cases (the
+// single-variant kernels; the mixed kernel keeps one body per variant).
+template <bool H_FIRST, int KV, int KH, bool SPECIALISE>
 __device__ __forceinline__ void chain_item(Pipe &p, const SmemLayout &L, const FusedJob &J, const void *tmap, int strip,
                                            int g_begin, int ngroups)
 {
@@ -433,7 +432,7 @@ __device__ __forceinline__ void chain_item(Pipe &p, const SmemLayout &L, const F
 		const bool active = tile0 * kTileW < J.dst_w;
 		uint4 ah[T][KH][2];
 		uint32_t colb[T];
-		uint32_t carry[T][2];
+		uint32_t blk[T][2 * KV][2];  // H first: the window's 8-line blocks (hfirst_h)
 #pragma unroll
 		for (int j = 0; j < T; ++j) {
 			const int tile = min(tile0 + j, ntiles - 1);
@@ -446,7 +445,9 @@ __device__ __forceinline__ void chain_item(Pipe &p, const SmemLayout &L, const F
 			const int rel = __ldg(J.h_left + tile) - xlo;
 			colb[j] = H_FIRST ? static_cast<uint32_t>((rel + 2 * tig) * 2)
 			                  : static_cast<uint32_t>((rel + (lane >> 4) * 8) * 2);
-			carry[j][0] = carry[j][1] = 0;
+#pragma unroll
+			for (int i = 0; i < 2 * KV; ++i)
+				blk[j][i][0] = blk[j][i][1] = 0;
 		}
 		Epi e;
 		e.magic = J.magic;
@@ -492,17 +493,23 @@ __device__ __forceinline__ void chain_item(Pipe &p, const SmemLayout &L, const F
 				const uint4 *avs = reinterpret_cast<const uint4 *>(vslots + s * kSlotBytes) + lane;
 				uint4 av[KV][2];
 				if (H_FIRST) {
-					uint32_t roff[KV][2];
-#pragma unroll
-					for (int kv = 0; kv < KV; ++kv) {
-						roff[kv][0] = ((static_cast<unsigned>(vbk + 16 * kv + lrow)) & line_mask) * P;
-						roff[kv][1] = ((static_cast<unsigned>(vbk + 16 * kv + lrow + 8)) & line_mask) * P;
+					// blocks of the previous group's window that this one keeps:
+					// compile-time bodies (SPECIALISE) for a move by one block (2x
+					// upscales) and for none kept
+					const int moved = vbk - prev_vb;
+					const unsigned line0 = static_cast<unsigned>(vbk);
+					const bool slide = k > 0 && (moved & 7) == 0 && moved < 16 * KV;
+					if (SPECIALISE && slide && moved == 8) {
+						shift_blocks<KV, T>(blk, 1);
+						hfirst_h<KV, KH, T, 2 * KV - 1>(ring, line0, line_mask, P, lrow, colb, ah, blk, 0, e);
+					} else if (SPECIALISE && !slide) {
+						hfirst_h<KV, KH, T, 0>(ring, line0, line_mask, P, lrow, colb, ah, blk, 0, e);
+					} else {
+						if (slide)
+							shift_blocks<KV, T>(blk, moved >> 3);
+						hfirst_h<KV, KH, T, -1>(ring, line0, line_mask, P, lrow, colb, ah, blk,
+						                        slide ? 2 * KV - (moved >> 3) : 0, e);
 					}
-					uint32_t bv[T][KV][2][2];
-					if (KV == 1 && k > 0 && vbk - prev_vb == 8)
-						hfirst_h<KV, KH, T, true>(ring, roff, colb, ah, carry, bv, e);
-					else
-						hfirst_h<KV, KH, T, false>(ring, roff, colb, ah, carry, bv, e);
 #pragma unroll
 					for (int kv = 0; kv < KV; ++kv) {
 						av[kv][0] = avs[(kv * 2 + 0) * 32];
@@ -512,7 +519,7 @@ __device__ __forceinline__ void chain_item(Pipe &p, const SmemLayout &L, const F
 					__syncwarp();
 					if (lane == 0)
 						mbar_arrive(&empty[s]);
-					hfirst_v<KV, T>(bv, av, st_addr, e);
+					hfirst_v<KV, T>(blk, av, st_addr, e);
 				} else {
 #pragma unroll
 					for (int kv = 0; kv < KV; ++kv) {
@@ -617,8 +624,8 @@ chain_tma_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_item
 		const int ngroups = min(J.groups - g_begin, t_end - t);
 		t += ngroups;
 		load_bases(p, J, g_begin, ngroups);
-		chain_item<H_FIRST, KV, KH>(p, L, J, jobs ? J.tmap : static_cast<const void *>(&single_map), strip, g_begin,
-		                            ngroups);
+		chain_item<H_FIRST, KV, KH, true>(p, L, J, jobs ? J.tmap : static_cast<const void *>(&single_map), strip,
+		                                  g_begin, ngroups);
 		p.base += ngroups;
 		__syncthreads();  // the next item rewrites the group bases and the ring
 		if (abort_item)
@@ -659,7 +666,7 @@ chain_mixed_kernel(const FusedJob *__restrict__ jobs, int num_jobs, const int *_
 			switch (v) {
 #define ZG_CHAIN_CASE(HF, KV, KH)                                                                     \
 	case (HF ? 12 : 0) + (KV - 1) * 4 + (KH - 1):                                                      \
-		chain_item<HF, KV, KH>(p, L, J, J.tmap, strip, g_begin, ngroups);                            \
+		chain_item<HF, KV, KH, false>(p, L, J, J.tmap, strip, g_begin, ngroups);                     \
 		break;
 				ZG_CHAIN_CASE(true, 1, 1) ZG_CHAIN_CASE(true, 1, 2) ZG_CHAIN_CASE(true, 1, 3) ZG_CHAIN_CASE(true, 1, 4)
 				ZG_CHAIN_CASE(true, 2, 1) ZG_CHAIN_CASE(true, 2, 2) ZG_CHAIN_CASE(true, 2, 3) ZG_CHAIN_CASE(true, 2, 4)
