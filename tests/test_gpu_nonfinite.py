@@ -16,10 +16,12 @@ outputs of its windows. The documented behaviour, pinned here per engine:
     CUDA-core kernels in FMA order; within the FP64 bound on the tensor-core
     passes);
   * the extra non-finite outputs lie within SPREAD[engine] output samples
-    (in rows and columns) of one that zimg gives as non-finite: none for the
-    separate CUDA-core passes, whose windows are each output's own taps (they
-    give exactly zimg's non-finite outputs); 4 for the fused CUDA-core
-    kernel's row groups; 32 for the tensor-core passes' tiles and blocks.
+    (in rows and columns) of one that zimg gives as non-finite: 8 for the
+    separate CUDA-core passes (those of fewer than 32 taps use each output's
+    own taps and give exactly zimg's non-finite outputs; wider ones compute
+    groups of 8 output rows or 4 output columns over a dense window); 4 for
+    the fused CUDA-core kernel's row groups; 32 for the tensor-core passes'
+    tiles and blocks.
 """
 import math
 
@@ -30,7 +32,7 @@ from test_gpu_resize import band_limited, run_conversion
 
 pytestmark = pytest.mark.gpu
 
-SPREAD = {"cuda": 0, "fused": 4, "tensor": 32}
+SPREAD = {"cuda": 8, "fused": 4, "tensor": 32}
 
 
 def _inject(rng, src, n=6):

@@ -50,7 +50,38 @@ void DevicePass::upload()
 	const size_t off_f32 = up(t.rows * sizeof(unsigned));
 	const size_t off_i16 = off_f32 + up(n * sizeof(float));
 	const size_t off_bias = off_i16 + up(n * sizeof(int16_t));
-	const size_t total = off_bias + up(t.rows * sizeof(int32_t));
+	size_t total = off_bias + up(t.rows * sizeof(int32_t));
+	// dense groups of outputs for wide FP32 passes on CUDA cores
+	const bool dense = sample == Sample::F32 && t.width >= kDenseTaps;
+	const unsigned R = dense_rows(horizontal);
+	const unsigned groups = (t.rows + R - 1) / R;
+	std::vector<unsigned> dbase(groups), dspan(groups);
+	unsigned dstride = 0;  // inputs per group in the dense table (the widest group)
+	unsigned dwin = 0;     // widest input window of 32 consecutive groups
+	if (dense) {
+		for (unsigned g = 0; g < groups; ++g) {
+			unsigned lo = ~0u, hi = 0;
+			for (unsigned r = 0; r < R && g * R + r < t.rows; ++r) {
+				lo = std::min(lo, t.left[g * R + r]);
+				hi = std::max(hi, t.left[g * R + r] + t.width);
+			}
+			dbase[g] = lo;
+			dspan[g] = hi - lo;
+			dstride = std::max(dstride, dspan[g]);
+		}
+		for (unsigned g0 = 0; g0 < groups; g0 += 32) {
+			unsigned hi = 0;
+			for (unsigned g = g0; g < std::min(groups, g0 + 32); ++g)
+				hi = std::max(hi, dbase[g] + dspan[g]);
+			dwin = std::max(dwin, hi - dbase[g0]);
+		}
+	}
+	const size_t dense_floats = static_cast<size_t>(groups) * dstride * R;
+	const size_t off_dbase = total;
+	const size_t off_dspan = off_dbase + (dense ? up(groups * sizeof(unsigned)) : 0);
+	const size_t off_dense = off_dspan + (dense ? up(groups * sizeof(unsigned)) : 0);
+	if (dense)
+		total = off_dense + up(dense_floats * sizeof(float));
 
 	std::vector<int32_t> bias(t.rows);
 	for (unsigned i = 0; i < t.rows; ++i) {
@@ -65,6 +96,20 @@ void DevicePass::upload()
 	std::memcpy(host.data() + off_f32, t.f32.data(), n * sizeof(float));
 	std::memcpy(host.data() + off_i16, t.i16.data(), n * sizeof(int16_t));
 	std::memcpy(host.data() + off_bias, bias.data(), t.rows * sizeof(int32_t));
+	if (dense) {
+		std::memcpy(host.data() + off_dbase, dbase.data(), groups * sizeof(unsigned));
+		std::memcpy(host.data() + off_dspan, dspan.data(), groups * sizeof(unsigned));
+		float *d = reinterpret_cast<float *>(host.data() + off_dense);
+		for (unsigned g = 0; g < groups; ++g)
+			for (unsigned r = 0; r < R && g * R + r < t.rows; ++r) {
+				const unsigned i = g * R + r;
+				for (unsigned k = 0; k < t.width; ++k) {
+					const size_t u = t.left[i] - dbase[g] + k;
+					const size_t at = horizontal ? (u * groups + g) * R + r : (static_cast<size_t>(g) * dstride + u) * R + r;
+					d[at] = t.f32[static_cast<size_t>(i) * t.width + k];
+				}
+			}
+	}
 
 	storage.reset(total);
 	cuda_check(cudaMemcpy(storage.get(), host.data(), total, cudaMemcpyHostToDevice), "upload taps");
@@ -77,6 +122,11 @@ void DevicePass::upload()
 	tables.width = t.width;
 	tables.rows = t.rows;
 	tables.input_width = t.input_width;
+	tables.dense = dense ? reinterpret_cast<const float *>(base + off_dense) : nullptr;
+	tables.dbase = dense ? reinterpret_cast<const unsigned *>(base + off_dbase) : nullptr;
+	tables.dspan = dense ? reinterpret_cast<const unsigned *>(base + off_dspan) : nullptr;
+	tables.dstride = dstride;
+	tables.dwin = dwin;
 }
 
 void DevicePass::set_tensor()

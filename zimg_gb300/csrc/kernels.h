@@ -24,7 +24,25 @@ struct PassTables {
 	unsigned width;        // taps per output
 	unsigned rows;         // outputs along the filtered axis
 	unsigned input_width;  // inputs along the filtered axis
+	// FP32 passes of at least kDenseTaps taps, on CUDA cores: outputs in groups
+	// of dense_rows(horizontal) (8 vertically, 4 horizontally); group g's taps
+	// as a dense block over the inputs dbase[g] + u, u < dspan[g] (exact zeros
+	// outside each output's band), so that an input is loaded once per group:
+	// vertical passes dense[(g * dstride + u) * 8 + r], horizontal ones
+	// dense[(u * groups + g) * 4 + r] (a warp's 32 groups side by side);
+	// dwin: the widest input window of 32 consecutive horizontal groups
+	const float *dense;
+	const unsigned *dbase;
+	const unsigned *dspan;
+	unsigned dstride;
+	unsigned dwin;
 };
+
+constexpr unsigned kDenseTaps = 32;
+__host__ __device__ constexpr unsigned dense_rows(bool horizontal)
+{
+	return horizontal ? 4u : 8u;
+}
 
 enum class Sample { U16, F32 };
 
