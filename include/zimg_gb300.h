@@ -410,8 +410,10 @@ typedef struct zg_graph_builder_params {
 	char chromatic_adaptation;
 } zg_graph_builder_params;
 
-/* Buffer descriptors as zimg_image_buffer(_const) (zimg.h:387-433); only whole
- * planes (mask == ZG_BUFFER_MAX) are accepted. */
+/* Buffer descriptors as zimg_image_buffer(_const) (zimg.h:387-433): line i
+ * of plane p at plane[p].data + (i & plane[p].mask) * plane[p].stride, in
+ * device memory; mask = ZG_BUFFER_MAX for a whole plane, else 2^n - 1 for a
+ * ring of 2^n lines (see zg_graph_process_cb). */
 #define ZG_BUFFER_MAX (~0U)
 typedef struct zg_image_buffer_const {
 	unsigned version;
@@ -445,6 +447,28 @@ ZG_API void zg_graph_free(zg_graph *g);
 ZG_API zg_error_code zg_graph_get_tmp_size(const zg_graph *g, size_t *out);
 ZG_API zg_error_code zg_graph_process(const zg_graph *g, const zg_image_buffer_const *src, const zg_image_buffer *dst,
                                void *tmp, zg_stream stream);
+
+/* Replaces zimg_filter_graph_callback and zimg_filter_graph_process with its
+ * callbacks (zimg.h:455-484,550-552), and zimg_filter_graph_get_input/
+ * output_buffering (zimg.h:522,534). Ring-buffer planes (mask != ZG_BUFFER_MAX)
+ * go through whole-plane staging copies in tmp (zg_graph_get_tmp_size covers
+ * them): for each step of input lines (the vertical subsampling unit, e.g. 2
+ * for 4:2:0; i counts luma lines) unpack_cb(unpack_user, i, 0, width) is
+ * called on the calling thread before those lines are read from the input
+ * rings, and pack_cb(pack_user, i, 0, width) after output lines i .. i + step
+ * - 1 have been written to the output rings and the stream has reached them;
+ * a ring line is not overwritten before the callback that consumes or refills
+ * it has returned. The callbacks are called for whole planes too; either may
+ * be NULL. A callback that returns non-zero aborts processing with
+ * ZG_ERROR_USER_CALLBACK_FAILED. The buffering queries return the smallest
+ * ring (in luma lines, a power of 2) the graph accepts: the subsampling step. */
+typedef int (*zg_graph_callback)(void *user, unsigned i, unsigned left, unsigned right);
+ZG_API zg_error_code zg_graph_process_cb(const zg_graph *g, const zg_image_buffer_const *src,
+                                         const zg_image_buffer *dst, void *tmp, zg_graph_callback unpack_cb,
+                                         void *unpack_user, zg_graph_callback pack_cb, void *pack_user,
+                                         zg_stream stream);
+ZG_API zg_error_code zg_graph_get_input_buffering(const zg_graph *g, unsigned *out);
+ZG_API zg_error_code zg_graph_get_output_buffering(const zg_graph *g, unsigned *out);
 /* Per-plane resize parameters the builder chose (as zimg's FilterObserver
  * reports them, graphbuilder.h:45-64); returns 0 passes for a plane copied
  * unchanged. plane in 0..3. */

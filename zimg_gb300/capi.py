@@ -102,6 +102,9 @@ class ImageBuffer(C.Structure):
 
 
 API_VERSION_2_4 = (2 << 8) | 4
+
+# zg_graph_callback: int (*)(void *user, unsigned i, unsigned left, unsigned right)
+GRAPH_CALLBACK = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_uint, C.c_uint, C.c_uint)
 BUFFER_MAX = 0xFFFFFFFF
 
 # (name, restype, argtypes) for every function declared in include/zimg_gb300.h
@@ -149,6 +152,9 @@ SIGNATURES = [
     ("zg_graph_free", None, [_P]),
     ("zg_graph_get_tmp_size", C.c_int, [_P, C.POINTER(C.c_size_t)]),
     ("zg_graph_process", C.c_int, [_P, C.POINTER(ImageBuffer), C.POINTER(ImageBuffer), _P, _P]),
+    ("zg_graph_process_cb", C.c_int, [_P, C.POINTER(ImageBuffer), C.POINTER(ImageBuffer), _P, _P, _P, _P, _P, _P]),
+    ("zg_graph_get_input_buffering", C.c_int, [_P, C.POINTER(C.c_uint)]),
+    ("zg_graph_get_output_buffering", C.c_int, [_P, C.POINTER(C.c_uint)]),
     ("zg_graph_get_plane_params", C.c_int, [_P, C.c_int, C.POINTER(ResizeParams), C.POINTER(C.c_int)]),
 ]
 

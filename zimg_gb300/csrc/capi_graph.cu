@@ -285,8 +285,15 @@ struct zg_graph {
 		zg_depth *pre = nullptr, *post = nullptr, *only = nullptr;
 		size_t pre_pitch = 0, mid_pitch = 0, off_mid = 0, off_tmp = 0;
 		size_t tmp = 0;
+		// ring-buffer (line-masked) planes: the plane's full size, its
+		// vertical subsampling shift, and whole-plane staging copies in tmp
+		unsigned src_w = 0, src_h = 0, src_ssh = 0, dst_ssh = 0;
+		size_t sstage_pitch = 0, dstage_pitch = 0, off_sstage = 0, off_dstage = 0;
 	} planes[4];
 	size_t tmp_size = 0;
+	// lines and widths the callbacks are called with (the luma plane's), and
+	// the vertical subsampling step of the source and destination formats
+	unsigned src_lines = 0, dst_lines = 0, src_width = 0, dst_width = 0, src_step = 1, dst_step = 1;
 
 	~zg_graph()
 	{
@@ -387,6 +394,10 @@ zg_graph *zg_graph_build(const zg_image_format *src_format, const zg_image_forma
 			gpl.h = dp.height;
 			gpl.in_bytes = bytes(s.pixel_type);
 			gpl.out_bytes = bytes(d.pixel_type);
+			gpl.src_w = sp.width;
+			gpl.src_h = sp.height;
+			gpl.src_ssh = chroma && s.color == COLOR_YUV ? s.subsample_h : 0;
+			gpl.dst_ssh = chroma && s.color == COLOR_YUV ? d.subsample_h : 0;
 			// plane formats; full-range BYTE kept at its depth is treated as
 			// limited range for the whole chain (graphbuilder.cpp:912-920)
 			const bool uv = chroma && s.color == COLOR_YUV;
@@ -482,6 +493,25 @@ zg_graph *zg_graph_build(const zg_image_format *src_format, const zg_image_forma
 			gpl.tmp = off + rtmp;
 			g->tmp_size = std::max(g->tmp_size, gpl.tmp);
 		}
+		// staging planes for ring buffers, after the largest per-plane scratch
+		size_t off = (g->tmp_size + 255) & ~static_cast<size_t>(255);
+		for (auto &gpl : g->planes) {
+			if (!gpl.present)
+				continue;
+			gpl.sstage_pitch = pitch_of(gpl.src_w, gpl.in_bytes);
+			gpl.off_sstage = off;
+			off += gpl.sstage_pitch * gpl.src_h;
+			gpl.dstage_pitch = pitch_of(gpl.w, gpl.out_bytes);
+			gpl.off_dstage = off;
+			off += gpl.dstage_pitch * gpl.h;
+		}
+		g->tmp_size = off;
+		g->src_lines = s.height;
+		g->dst_lines = d.height;
+		g->src_width = s.width;
+		g->dst_width = d.width;
+		g->src_step = 1u << s.subsample_h;
+		g->dst_step = 1u << d.subsample_h;
 		result = g.release();
 	});
 	return result;
@@ -514,8 +544,33 @@ zg_error_code zg_graph_get_plane_params(const zg_graph *g, int plane, zg_resize_
 	});
 }
 
+zg_error_code zg_graph_get_input_buffering(const zg_graph *g, unsigned *out)
+{
+	return guarded([&] {
+		if (!g || !out)
+			throw Error(kErrIllegalArgument, "null pointer");
+		*out = g->src_step;
+	});
+}
+
+zg_error_code zg_graph_get_output_buffering(const zg_graph *g, unsigned *out)
+{
+	return guarded([&] {
+		if (!g || !out)
+			throw Error(kErrIllegalArgument, "null pointer");
+		*out = g->dst_step;
+	});
+}
+
 zg_error_code zg_graph_process(const zg_graph *g, const zg_image_buffer_const *src, const zg_image_buffer *dst,
                                void *tmp, zg_stream stream)
+{
+	return zg_graph_process_cb(g, src, dst, tmp, nullptr, nullptr, nullptr, nullptr, stream);
+}
+
+zg_error_code zg_graph_process_cb(const zg_graph *g, const zg_image_buffer_const *src, const zg_image_buffer *dst,
+                                  void *tmp, zg_graph_callback unpack_cb, void *unpack_user, zg_graph_callback pack_cb,
+                                  void *pack_user, zg_stream stream)
 {
 	return guarded([&] {
 		if (!g || !src || !dst)
@@ -523,39 +578,110 @@ zg_error_code zg_graph_process(const zg_graph *g, const zg_image_buffer_const *s
 		if (current_device() != g->device)
 			throw Error(kErrLogic, "graph used on a different device than the one it was created on");
 		cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+		char *t = static_cast<char *>(tmp);
+		auto ring_ok = [](unsigned mask) { return mask == ZG_BUFFER_MAX || ((mask + 1) & mask) == 0; };
+		// planes' effective source and destination (staging for ring planes)
+		const void *from_data[4] = {};
+		ptrdiff_t from_stride[4] = {};
+		void *to_data[4] = {};
+		ptrdiff_t to_stride[4] = {};
+		bool src_ring = false, dst_ring = false;
+		// ring capacity in luma lines (the smallest ring of the format)
+		unsigned src_cap = ~0u, dst_cap = ~0u;
 		for (int p = 0; p < 4; ++p) {
 			const auto &pl = g->planes[p];
 			if (!pl.present)
 				continue;
-			if (src->plane[p].mask != ZG_BUFFER_MAX || dst->plane[p].mask != ZG_BUFFER_MAX)
-				throw Error(kErrUnsupported, "only whole-plane buffers (mask ZG_BUFFER_MAX) are supported");
-			const char *sp = static_cast<const char *>(src->plane[p].data);
-			char *dp = static_cast<char *>(dst->plane[p].data);
-			if (!sp || !dp)
+			const unsigned sm = src->plane[p].mask, dm = dst->plane[p].mask;
+			if (!src->plane[p].data || !dst->plane[p].data)
 				throw Error(kErrIllegalArgument, "null plane pointer");
-			const char *from = sp + static_cast<ptrdiff_t>(pl.off_y) * src->plane[p].stride +
-			                   static_cast<ptrdiff_t>(pl.off_x) * pl.in_bytes;
+			if (!ring_ok(sm) || !ring_ok(dm))
+				throw Error(kErrIllegalArgument, "buffer mask must be 2^n - 1 or ZG_BUFFER_MAX");
+			if (sm != ZG_BUFFER_MAX) {
+				if (((static_cast<unsigned long long>(sm) + 1) << pl.src_ssh) < g->src_step)
+					throw Error(kErrIllegalArgument, "input ring buffer smaller than zg_graph_get_input_buffering");
+				src_ring = true;
+				src_cap = std::min<unsigned long long>(src_cap, (static_cast<unsigned long long>(sm) + 1) << pl.src_ssh);
+				if (!t)
+					throw Error(kErrIllegalArgument, "tmp is null");
+				from_data[p] = t + pl.off_sstage;
+				from_stride[p] = static_cast<ptrdiff_t>(pl.sstage_pitch);
+			} else {
+				from_data[p] = src->plane[p].data;
+				from_stride[p] = src->plane[p].stride;
+			}
+			if (dm != ZG_BUFFER_MAX) {
+				if (((static_cast<unsigned long long>(dm) + 1) << pl.dst_ssh) < g->dst_step)
+					throw Error(kErrIllegalArgument, "output ring buffer smaller than zg_graph_get_output_buffering");
+				dst_ring = true;
+				dst_cap = std::min<unsigned long long>(dst_cap, (static_cast<unsigned long long>(dm) + 1) << pl.dst_ssh);
+				if (!t)
+					throw Error(kErrIllegalArgument, "tmp is null");
+				to_data[p] = t + pl.off_dstage;
+				to_stride[p] = static_cast<ptrdiff_t>(pl.dstage_pitch);
+			} else {
+				to_data[p] = dst->plane[p].data;
+				to_stride[p] = dst->plane[p].stride;
+			}
+		}
+
+		// Input: the unpack callback for each step of lines, as zimg calls it
+		// (zimg.h:455-484), and ring lines gathered into whole staging planes
+		// before anything reads them. A ring slot is rewritten by the callback
+		// only after the copies out of it have completed.
+		if (unpack_cb || src_ring) {
+			unsigned synced = 0;
+			for (unsigned i = 0; i < g->src_lines; i += g->src_step) {
+				if (src_ring && i + g->src_step - synced > src_cap) {
+					cuda_check(cudaStreamSynchronize(st), "ring buffer copies");
+					synced = i;
+				}
+				if (unpack_cb && unpack_cb(unpack_user, i, 0, g->src_width))
+					throw Error(kErrUserCallbackFailed, "user callback failed");
+				for (int p = 0; p < 4 && src_ring; ++p) {
+					const auto &pl = g->planes[p];
+					if (!pl.present || src->plane[p].mask == ZG_BUFFER_MAX)
+						continue;
+					const unsigned l0 = i >> pl.src_ssh;
+					const unsigned l1 = std::min(pl.src_h, (i + g->src_step) >> pl.src_ssh);
+					for (unsigned l = l0; l < l1; ++l)
+						cuda_check(cudaMemcpyAsync(static_cast<char *>(const_cast<void *>(from_data[p])) +
+						                               static_cast<ptrdiff_t>(l) * from_stride[p],
+						                           static_cast<const char *>(src->plane[p].data) +
+						                               static_cast<ptrdiff_t>(l & src->plane[p].mask) * src->plane[p].stride,
+						                           static_cast<size_t>(pl.src_w) * pl.in_bytes, cudaMemcpyDeviceToDevice, st),
+						           "ring buffer copy");
+				}
+			}
+		}
+
+		for (int p = 0; p < 4; ++p) {
+			const auto &pl = g->planes[p];
+			if (!pl.present)
+				continue;
+			const char *sp = static_cast<const char *>(from_data[p]);
+			char *dp = static_cast<char *>(to_data[p]);
+			const ptrdiff_t sst = from_stride[p], dst_st = to_stride[p];
+			const char *from = sp + static_cast<ptrdiff_t>(pl.off_y) * sst + static_cast<ptrdiff_t>(pl.off_x) * pl.in_bytes;
 			if (pl.mode == 0 || pl.mode == 1) {
-				copy_plane(dp, dst->plane[p].stride, from, src->plane[p].stride, static_cast<size_t>(pl.w) * pl.in_bytes,
-				           pl.h, st);
+				copy_plane(dp, dst_st, from, sst, static_cast<size_t>(pl.w) * pl.in_bytes, pl.h, st);
 				continue;
 			}
 			if (pl.mode == 3 || pl.mode == 4) {
-				run_depth(pl.only, from, src->plane[p].stride, dp, dst->plane[p].stride, stream);
+				run_depth(pl.only, from, sst, dp, dst_st, stream);
 				continue;
 			}
 			if (pl.tmp && !tmp)
 				throw Error(kErrIllegalArgument, "tmp is null");
-			char *t = static_cast<char *>(tmp);
 			const void *rs = sp;
-			ptrdiff_t rss = src->plane[p].stride;
+			ptrdiff_t rss = sst;
 			if (pl.pre) {
-				run_depth(pl.pre, sp, src->plane[p].stride, t, static_cast<ptrdiff_t>(pl.pre_pitch), stream);
+				run_depth(pl.pre, sp, sst, t, static_cast<ptrdiff_t>(pl.pre_pitch), stream);
 				rs = t;
 				rss = static_cast<ptrdiff_t>(pl.pre_pitch);
 			}
 			void *rd = pl.post ? static_cast<void *>(t + pl.off_mid) : static_cast<void *>(dp);
-			const ptrdiff_t rds = pl.post ? static_cast<ptrdiff_t>(pl.mid_pitch) : dst->plane[p].stride;
+			const ptrdiff_t rds = pl.post ? static_cast<ptrdiff_t>(pl.mid_pitch) : dst_st;
 			zg_error_code rc = pl.unresize
 			                       ? zg_unresize_process(pl.unresize, rs, rss, rd, rds, t ? t + pl.off_tmp : nullptr, stream)
 			                       : zg_resize_process(pl.resize, rs, rss, rd, rds, t ? t + pl.off_tmp : nullptr, stream);
@@ -565,7 +691,34 @@ zg_error_code zg_graph_process(const zg_graph *g, const zg_image_buffer_const *s
 				throw Error(rc, msg);
 			}
 			if (pl.post)
-				run_depth(pl.post, rd, rds, dp, dst->plane[p].stride, stream);
+				run_depth(pl.post, rd, rds, dp, dst_st, stream);
+		}
+
+		// Output: ring lines scattered from the staging planes a ring's worth
+		// at a time, then the pack callback for each step of lines in it, once
+		// the copies (and everything before them) have completed.
+		if (pack_cb || dst_ring) {
+			const unsigned window = dst_ring ? std::max(g->dst_step, dst_cap / g->dst_step * g->dst_step) : g->dst_lines;
+			for (unsigned w0 = 0; w0 < g->dst_lines; w0 += window) {
+				const unsigned w1 = std::min(g->dst_lines, w0 + window);
+				for (int p = 0; p < 4 && dst_ring; ++p) {
+					const auto &pl = g->planes[p];
+					if (!pl.present || dst->plane[p].mask == ZG_BUFFER_MAX)
+						continue;
+					const unsigned l0 = w0 >> pl.dst_ssh;
+					const unsigned l1 = std::min(pl.h, (w1 + (1u << pl.dst_ssh) - 1) >> pl.dst_ssh);
+					for (unsigned l = l0; l < l1; ++l)
+						cuda_check(cudaMemcpyAsync(static_cast<char *>(dst->plane[p].data) +
+						                               static_cast<ptrdiff_t>(l & dst->plane[p].mask) * dst->plane[p].stride,
+						                           static_cast<const char *>(to_data[p]) + static_cast<ptrdiff_t>(l) * to_stride[p],
+						                           static_cast<size_t>(pl.w) * pl.out_bytes, cudaMemcpyDeviceToDevice, st),
+						           "ring buffer copy");
+				}
+				cuda_check(cudaStreamSynchronize(st), "ring buffer copies");
+				for (unsigned i = w0; i < w1 && pack_cb; i += g->dst_step)
+					if (pack_cb(pack_user, i, 0, g->dst_width))
+						throw Error(kErrUserCallbackFailed, "user callback failed");
+			}
 		}
 	});
 }

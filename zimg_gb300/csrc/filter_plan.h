@@ -21,6 +21,7 @@ struct Error : std::runtime_error {
 enum ErrorCode {
 	kErrUnknown = -1,
 	kErrOutOfMemory = 1,
+	kErrUserCallbackFailed = 2,
 	kErrLogic = 1 << 10,
 	kErrIllegalArgument = 2 << 10,
 	kErrEnumOutOfRange = (2 << 10) + 1,

@@ -521,19 +521,46 @@ class Graph:
         check(load().zg_graph_get_plane_params(self._h, plane, C.byref(p), C.byref(present)))
         return present.value, p
 
-    def process(self, src_planes, dst_planes, tmp=None, stream=None) -> None:
-        def buf(planes):
+    @property
+    def input_buffering(self) -> int:
+        n = C.c_uint()
+        check(load().zg_graph_get_input_buffering(self._h, C.byref(n)))
+        return n.value
+
+    @property
+    def output_buffering(self) -> int:
+        n = C.c_uint()
+        check(load().zg_graph_get_output_buffering(self._h, C.byref(n)))
+        return n.value
+
+    def process(self, src_planes, dst_planes, tmp=None, stream=None, src_masks=None, dst_masks=None,
+                unpack=None, pack=None) -> None:
+        """Planes are 2-D CUDA tensors (or None). A plane given with a mask
+        (2^n - 1) is a ring of 2^n lines: line i at row i & mask. unpack /
+        pack: Python callables f(i, left, right) -> int, called as zimg's
+        zimg_filter_graph_callback (zimg.h:455-484)."""
+        def buf(planes, masks):
             b = capi.ImageBuffer()
             b.version = capi.API_VERSION_2_4
             for i, t in enumerate(planes):
                 if t is None:
                     continue
                 ptr, stride, _, _ = _plane(t)
-                b.plane[i] = capi._PlaneC(ptr, stride, capi.BUFFER_MAX)
+                mask = capi.BUFFER_MAX if not masks or masks[i] is None else masks[i]
+                b.plane[i] = capi._PlaneC(ptr, stride, mask)
             return b
-        s, d = buf(src_planes), buf(dst_planes)
+        s, d = buf(src_planes, src_masks), buf(dst_planes, dst_masks)
         if tmp is None and self.tmp_size:
             import torch
             tmp = torch.empty(self.tmp_size, dtype=torch.uint8, device="cuda")
-        check(load().zg_graph_process(self._h, C.byref(s), C.byref(d), tmp.data_ptr() if tmp is not None else None,
-                                      _stream_handle(stream)))
+        tp = tmp.data_ptr() if tmp is not None else None
+        if unpack is None and pack is None and not src_masks and not dst_masks:
+            check(load().zg_graph_process(self._h, C.byref(s), C.byref(d), tp, _stream_handle(stream)))
+            return
+
+        def wrap(f):
+            return capi.GRAPH_CALLBACK(lambda user, i, left, right: int(f(i, left, right))) if f else None
+        ucb, pcb = wrap(unpack), wrap(pack)
+        check(load().zg_graph_process_cb(self._h, C.byref(s), C.byref(d), tp,
+                                         C.cast(ucb, C.c_void_p) if ucb else None, None,
+                                         C.cast(pcb, C.c_void_p) if pcb else None, None, _stream_handle(stream)))
