@@ -111,9 +111,15 @@ ZG_API void zg_clear_last_error(void);
  *   mode 3: otherwise, to an integer type: x * scale + offset plus the dither
  *           value, clamped, rounded to nearest even (dither.cpp:37-54).
  * scale and offset are zimg's (quantize.h:19-45). Results equal zimg's C path
- * (CPUClass::NONE) bit for bit. Dither NONE and ORDERED (zimg's 16x16
- * matrix, variant chosen by `plane` mod 4, dither.cpp:137-210) are built;
- * RANDOM and ERROR_DIFFUSION return ZG_ERROR_UNSUPPORTED_OPERATION. A limited-range format below 8 bits returns
+ * (CPUClass::NONE) bit for bit. Dither NONE, ORDERED (zimg's 16x16 matrix,
+ * variant chosen by `plane` mod 4, dither.cpp:137-210), RANDOM (zimg's 64x64
+ * blue-noise matrix at the offsets chosen by `plane` mod 4,
+ * dither.cpp:219-234) and ERROR_DIFFUSION (Floyd-Steinberg over the whole
+ * plane, dither.cpp:59-85 and 291-345; one thread block per plane runs the
+ * lines as a wavefront) are built. ERROR_DIFFUSION on a plane of more than
+ * 32 x 32 lines whose width leaves no launch shape within a block's shared
+ * memory (from about 18,000 to 32,000 columns, by height) returns
+ * ZG_ERROR_UNSUPPORTED_OPERATION. A limited-range format below 8 bits returns
  * ZG_ERROR_BIT_DEPTH_OVERFLOW (depth.cpp:52-53), as does a depth beyond its
  * type. */
 typedef enum zg_dither_type {

@@ -121,6 +121,8 @@ class Oracle:
                                              C.POINTER(C.c_float)]
         L.orc_bayer16.argtypes = [C.c_uint, C.c_uint]
         L.orc_bayer16.restype = C.c_uint
+        L.orc_blue_noise.argtypes = [C.c_uint, C.c_uint]
+        L.orc_blue_noise.restype = C.c_uint
         L.orc_dither_value.argtypes = [C.c_int, C.c_uint, C.c_uint, C.c_uint]
         L.orc_dither_value.restype = C.c_float
         L.orc_unresize_plane.argtypes = [C.c_uint, C.c_uint, C.c_uint, C.c_uint, C.c_double, C.c_double,

@@ -24,6 +24,7 @@
 #include "common/except.h"
 #include "common/pixel.h"
 #include "graphengine/filter.h"
+#include "depth/blue.h"
 #include "depth/depth.h"
 #include "unresize/unresize.h"
 #include "resize/filter.h"
@@ -279,6 +280,16 @@ int ref_plan_run(const void *p, const void *src, ptrdiff_t src_stride, void *dst
 	} catch (...) {
 		return catch_all(err, errlen);
 	}
+}
+
+/*
+ * zimg's 64 x 64 blue-noise matrix behind RANDOM dither
+ * (src/zimg/depth/blue.h:10-13), row-major, into out[4096].
+ */
+void ref_blue_noise_table(uint8_t *out)
+{
+	std::memcpy(out, &zimg::depth::blue_noise_table[0][0],
+	            zimg::depth::BLUE_NOISE_LEN * zimg::depth::BLUE_NOISE_LEN);
 }
 
 /*

@@ -815,13 +815,34 @@ unsigned orc_bayer16(unsigned i, unsigned j)
 	return v;
 }
 
-/* Dither offset of row i, column j for plane `seq` (dither.cpp:157-210):
- * value (m + 1) / 257 - 1/2 in float, from the matrix as is (seq 0), mirrored
- * left-right (1), top-bottom (2) or transposed (3). dither 0 = NONE. */
+/* zimg's 64 x 64 blue-noise matrix (blue.h:10-13): data without a generating
+ * rule, read out of zimg's own build into the library's include file, which
+ * packs four row-major entries per little-endian word. */
+static const uint32_t orc_blue_noise_words[1024] = {
+#include "../zimg_gb300/csrc/blue_noise_table.inc"
+};
+
+unsigned orc_blue_noise(unsigned i, unsigned j)
+{
+	const unsigned k = (i & 63) * 64 + (j & 63);
+	return (orc_blue_noise_words[k >> 2] >> (8 * (k & 3))) & 0xFF;
+}
+
+/* Dither offset of row i, column j for plane `seq` (dither.cpp:157-234).
+ * ORDERED (1): (m + 1) / 257 - 1/2 in float, from the Bayer matrix as is
+ * (seq 0), mirrored left-right (1), top-bottom (2) or transposed (3).
+ * RANDOM (2): the same mapping of the blue-noise entry at row (i + voff) mod
+ * 64, column (j + hoff) mod 64, (hoff, voff) = (0, 0), (32, 12), (16, 55),
+ * (48, 26) for seq mod 4 (dither.cpp:226-233). NONE (0): zero. */
 float orc_dither_value(int dither, unsigned seq, unsigned i, unsigned j)
 {
 	if (dither == 0)
 		return 0.0f;
+	if (dither == 2) {
+		static const unsigned hoff[4] = { 0, 32, 16, 48 }, voff[4] = { 0, 12, 55, 26 };
+		const unsigned m = orc_blue_noise(i + voff[seq % 4], j + hoff[seq % 4]);
+		return (float)(m + 1) / 257.0f - 0.5f;
+	}
 	i &= 15;
 	j &= 15;
 	unsigned m;
@@ -925,7 +946,51 @@ int orc_depth_mode(const orc_pixfmt *in, const orc_pixfmt *out, int dither)
 		return 1;
 	if (pix_is_float(out->type))
 		return (pix_is_float(in->type) && in->type == out->type) ? 0 : 2;
-	return (dither == 0 || dither == 1) ? 3 : -2;
+	return (dither >= 0 && dither <= 3) ? 3 : -2;
+}
+
+/* Floyd-Steinberg error diffusion over a whole plane, zimg's C path
+ * (dither.cpp:59-85 per row, rows in order with two error rows that swap,
+ * dither.cpp:328-343). The error rows are padded by one zero on each side and
+ * start at zero. Each sample: x = sample * scale + offset (two roundings),
+ * then the error 0 + left * 7/16 + top-right * 3/16 + top * 5/16 +
+ * top-left * 1/16 summed in that order, x + error, clamped to [0, 2^depth -
+ * 1] (a NaN stays NaN), rounded to nearest even (a NaN gives 0), and the
+ * sample's error x - q. */
+static int orc_error_diffusion(const orc_pixfmt *in, const orc_pixfmt *out, float scale, float offset, unsigned w,
+                               unsigned h, const void *src, ptrdiff_t src_stride, void *dst, ptrdiff_t dst_stride)
+{
+	float *rows = calloc(2 * ((size_t)w + 2), sizeof(float));
+	if (!rows)
+		return -3;
+	float *const err_a = rows, *const err_b = rows + w + 2;
+	const float vmax = (float)((1UL << out->depth) - 1);
+	for (unsigned i = 0; i < h; ++i) {
+		const char *s = (const char *)src + (ptrdiff_t)i * src_stride;
+		char *d = (char *)dst + (ptrdiff_t)i * dst_stride;
+		const float *top = (i % 2) ? err_a : err_b;
+		float *cur = (i % 2) ? err_b : err_a;
+		for (unsigned j = 0; j < w; ++j) {
+			const unsigned je = j + 1;
+			const float p = load_sample(in->type, s, j) * scale;
+			float x = p + offset;
+			float err = 0.0f;
+			err = err + cur[je - 1] * (7.0f / 16.0f);
+			err = err + top[je + 1] * (3.0f / 16.0f);
+			err = err + top[je + 0] * (5.0f / 16.0f);
+			err = err + top[je - 1] * (1.0f / 16.0f);
+			x = x + err;
+			x = x < 0.0f ? 0.0f : (vmax < x ? vmax : x);
+			const unsigned q = isnan(x) ? 0u : (unsigned)lrintf(x);
+			if (out->type == 0)
+				((uint8_t *)d)[j] = (uint8_t)q;
+			else
+				((uint16_t *)d)[j] = (uint16_t)q;
+			cur[je] = x - (float)q;
+		}
+	}
+	free(rows);
+	return 0;
 }
 
 int orc_depth_convert(const orc_pixfmt *in, const orc_pixfmt *out, int dither, unsigned seq, unsigned w, unsigned h,
@@ -936,6 +1001,8 @@ int orc_depth_convert(const orc_pixfmt *in, const orc_pixfmt *out, int dither, u
 		return mode;
 	float scale = 1.0f, offset = 0.0f;
 	orc_depth_scale_offset(in, out, &scale, &offset);
+	if (mode == 3 && dither == 3)
+		return orc_error_diffusion(in, out, scale, offset, w, h, src, src_stride, dst, dst_stride);
 	const unsigned shift = out->depth - in->depth;
 	const float vmax = (float)((1UL << out->depth) - 1);
 	for (unsigned i = 0; i < h; ++i) {

@@ -110,15 +110,16 @@ def test_depth_create_errors(lib):
     import ctypes as C
     from zimg_gb300 import capi
 
-    def create(tin, din, tout, dout, dither=0, fin=0, fout=0):
-        p = capi.DepthParams(64, 32, capi.PixelFormat(tin, din, fin, 0, 0), capi.PixelFormat(tout, dout, fout, 0, 0),
+    def create(tin, din, tout, dout, dither=0, fin=0, fout=0, w=64, h=32):
+        p = capi.DepthParams(w, h, capi.PixelFormat(tin, din, fin, 0, 0), capi.PixelFormat(tout, dout, fout, 0, 0),
                              dither, 0)
-        h = C.c_void_p()
-        return lib.zg_depth_create(C.byref(p), C.byref(h))
+        out = C.c_void_p()
+        return lib.zg_depth_create(C.byref(p), C.byref(out))
 
     assert create(2, 17, 0, 8) == 1028            # HALF deeper than 16 bits: BIT_DEPTH_OVERFLOW
-    assert create(3, 32, 0, 8, dither=2) == 3072  # RANDOM dither: not built
-    assert create(3, 32, 0, 8, dither=3) == 3072  # ERROR_DIFFUSION: not built
+    # ERROR_DIFFUSION on a plane whose wavefront fits no shared-memory budget:
+    # UNSUPPORTED_OPERATION
+    assert create(3, 32, 0, 8, dither=3, w=70000, h=2000) == 3072
     assert create(1, 7, 1, 10) == 1028            # limited range below 8 bits: BIT_DEPTH_OVERFLOW
     assert create(0, 9, 1, 10) == 1028            # depth beyond the type
     assert create(1, 10, 0, 8, dither=9) == 2049  # ENUM_OUT_OF_RANGE

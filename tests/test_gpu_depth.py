@@ -66,6 +66,74 @@ def test_depth_bitexact(cuda, oracle, case):
         assert mode == {0: "copy", 1: "left_shift", 2: "to_float", 3: "dither"}[oracle.depth_mode(fin, fout, dither)]
 
 
+ED_PLANES = [
+    # (pixel in, pixel out, height, width): whole planes of the usual sizes,
+    # a band per warp and several, tall and narrow, wide and short
+    (CASES[28][0], CASES[28][1], 1080, 1920),
+    (CASES[29][0], CASES[29][1], 2160, 3840),
+    (CASES[30][0], CASES[30][1], 540, 960),
+    (CASES[31][0], CASES[31][1], 720, 1280),
+    (CASES[33][0], CASES[33][1], 5000, 100),
+    (CASES[32][0], CASES[32][1], 64, 40000),
+    (CASES[34][0], CASES[34][1], 97, 3),
+    (CASES[28][0], CASES[28][1], 1, 1),
+    (CASES[28][0], CASES[28][1], 4320, 7680),
+]
+
+
+@pytest.mark.parametrize("case", range(len(ED_PLANES)))
+def test_error_diffusion_whole_planes(cuda, oracle, case):
+    """Floyd-Steinberg over whole planes: one serial recurrence per plane, run
+    as a wavefront of bands; equal to the oracle sample for sample."""
+    fin, fout, h, w = ED_PLANES[case]
+    rng = np.random.default_rng(700 + case)
+    src = make_src(rng, fin, h, w, special=False)
+    got, mode = convert(src, fin, fout, "error_diffusion", 0)
+    want = oracle.depth_convert(src, fin, fout, "error_diffusion", 0)
+    assert mode == "dither"
+    np.testing.assert_array_equal(got.view(np.uint8), want.view(np.uint8), err_msg=f"{h}x{w}")
+
+
+def test_error_diffusion_non_finite(cuda, oracle):
+    """zimg's C path keeps a NaN through the clamp, stores 0 for it and
+    carries its NaN error to the samples after and below it; infinities clamp
+    to the range ends with a zero error."""
+    from oracle.oracle import PixelFormat as PF
+    rng = np.random.default_rng(77)
+    src = rng.random((300, 500), dtype=np.float32)
+    src[7, 11] = np.nan
+    src[150, 499] = np.nan
+    src[299, 0] = np.nan
+    src[40, 40:44] = [np.inf, -np.inf, np.inf, -0.0]
+    for fout in (PF("byte", 8), PF("word", 12, True)):
+        got, _ = convert(src, PF("float"), fout, "error_diffusion", 0)
+        want = oracle.depth_convert(src, PF("float"), fout, "error_diffusion", 0)
+        np.testing.assert_array_equal(got, want)
+        assert (got[8:, 12:] == 0).any()
+
+
+def test_random_dither_whole_planes(cuda, oracle):
+    """Blue-noise dither on a 1080p plane, all four plane variants (the
+    table's offsets by plane index)."""
+    from oracle.oracle import PixelFormat as PF
+    rng = np.random.default_rng(78)
+    src = rng.integers(0, 1 << 16, size=(1080, 1920)).astype(np.uint16)
+    for plane in range(4):
+        got, _ = convert(src, PF("word", 16), PF("byte", 8), "random", plane)
+        want = oracle.depth_convert(src, PF("word", 16), PF("byte", 8), "random", plane)
+        np.testing.assert_array_equal(got, want, err_msg=f"plane {plane}")
+
+
+def test_error_diffusion_too_wide(cuda):
+    """A plane whose wavefront shape fits no shared-memory budget is refused
+    at creation (ZG_ERROR_UNSUPPORTED_OPERATION), before any launch."""
+    import zimg_gb300 as zg
+    with pytest.raises(zg.ZimgError) as e:
+        zg.DepthConversion(70000, 2000).set_pixel_in("word", 10).set_pixel_out("byte", 8) \
+            .set_dither_type("error_diffusion").create()
+    assert "error diffusion" in str(e.value)
+
+
 def test_depth_golden(cuda):
     data = np.load(GOLDEN)
     for k in range(int(data["n"])):
@@ -113,6 +181,9 @@ GRAPH_CASES = [
     ("word", 16, 1, "float", 32, 0, (400, 300), (800, 600), 1, "none"),      # RGB, to float after resize
     ("half", 16, 0, "half", 16, 0, (1280, 720), (1920, 1080), 2, "none"),    # HALF: resized in FLOAT
     ("half", 16, 0, "byte", 8, 0, (1920, 1080), (960, 540), 2, "ordered"),
+    ("float", 32, 0, "byte", 8, 0, (640, 360), (1280, 720), 2, "random"),    # blue-noise dither after resize
+    ("word", 16, 1, "byte", 8, 1, (1280, 720), (1920, 1080), 1, "error_diffusion"),  # RGB, diffused after
+    ("word", 10, 0, "byte", 8, 0, (1280, 720), (1280, 720), 2, "error_diffusion"),   # depth only
 ]
 
 
@@ -129,7 +200,7 @@ def test_graph_depth_around_resize(cuda, oracle, case):
                            subsample_h=sub, chroma_location=0)
     dfmt = zg.image_format(dw, dh, dt, depth=dd, pixel_range=dr, color_family=color, subsample_w=sub,
                            subsample_h=sub, chroma_location=0)
-    dmap = {"none": 0, "ordered": 1}
+    dmap = {"none": 0, "ordered": 1, "random": 2, "error_diffusion": 3}
     g = zg.Graph(sfmt, dfmt, zg.graph_params(resample_filter="lanczos", resample_filter_uv="bicubic",
                                              dither_type=dmap[dither]))
     rng = np.random.default_rng(600 + case)

@@ -15,6 +15,9 @@ struct zg_depth {
 	int mode = 0;  // 0 copy, 1 left shift, 2 to float, 3 dither
 	unsigned shift = 0;
 	float scale = 1.0f, offset = 0.0f, vmax = 0.0f;
+	// error diffusion: the plane's wavefront shape (pointers set per call)
+	EdPlane ed{};
+	int ed_warps = 0, ed_ring = 0;
 };
 
 namespace {
@@ -124,8 +127,6 @@ zg_error_code zg_depth_create(const zg_depth_params *params, zg_depth **out)
 		} else if (is_float(co)) {
 			d->mode = (is_float(ci) && ci == co) ? 0 : 2;
 		} else {
-			if (q.dither_type != ZG_DITHER_NONE && q.dither_type != ZG_DITHER_ORDERED)
-				throw Error(kErrUnsupported, "only NONE and ORDERED dithering are supported by this library");
 			d->mode = 3;
 		}
 		// get_scale_offset (quantize.h:34-45): FP64, rounded to float
@@ -133,6 +134,17 @@ zg_error_code zg_depth_create(const zg_depth_params *params, zg_depth **out)
 		d->scale = static_cast<float>(ro / ri);
 		d->offset = static_cast<float>(-oi * ro / ri + oo);
 		d->vmax = static_cast<float>((1UL << fo.depth) - 1);
+		if (d->mode == 3 && q.dither_type == ZG_DITHER_ERROR_DIFFUSION) {
+			d->ed.width = static_cast<int>(q.width);
+			d->ed.height = static_cast<int>(q.height);
+			d->ed.scale = d->scale;
+			d->ed.offset = d->offset;
+			d->ed.vmax = d->vmax;
+			d->ed_warps = ed_choose_warps(d->ed.width, d->ed.height);
+			if (q.width > (1u << 30) || q.height > (1u << 30) || !d->ed_warps ||
+			    !ed_shape(d->ed, d->ed_warps, &d->ed_ring))
+				throw Error(kErrUnsupported, "plane too wide for error diffusion in this library");
+		}
 		d->device = current_device();
 		*out = d.release();
 	});
@@ -178,6 +190,21 @@ zg_error_code zg_depth_process(const zg_depth *d, const void *src, ptrdiff_t src
 			copy_plane(dst, dst_stride, src, src_stride, static_cast<size_t>(q.width) * bo, q.height, st);
 			return;
 		}
+		if (d->mode == 3 && q.dither_type == ZG_DITHER_ERROR_DIFFUSION) {
+			EdLaunch E{};
+			E.planes[0] = d->ed;
+			E.planes[0].src = src;
+			E.planes[0].src_stride = src_stride;
+			E.planes[0].dst = dst;
+			E.planes[0].dst_stride = dst_stride;
+			E.num_planes = 1;
+			E.in_type = ci;
+			E.out_type = co;
+			E.warps = d->ed_warps;
+			E.ring = d->ed_ring;
+			cuda_check(launch_error_diffusion(E, st), "error diffusion launch");
+			return;
+		}
 		DepthLaunch L{};
 		L.src = src;
 		L.src_stride = src_stride;
@@ -190,7 +217,7 @@ zg_error_code zg_depth_process(const zg_depth *d, const void *src, ptrdiff_t src
 		L.vmax = d->vmax;
 		L.shift = d->shift;
 		L.seq = q.plane;
-		L.ordered = q.dither_type == ZG_DITHER_ORDERED;
+		L.dither = q.dither_type == ZG_DITHER_ORDERED ? 1 : (q.dither_type == ZG_DITHER_RANDOM ? 2 : 0);
 		// 8 samples per vector: 8-byte loads of BYTE, 16-byte loads of WORD, HALF and FLOAT
 		L.vec_in = aligned(src, src_stride, bi == 1 ? 8 : 16);
 		L.vec_out = aligned(dst, dst_stride, bo == 1 ? 8 : 16);

@@ -1,7 +1,8 @@
 // Depth conversion of one plane (zimg's DepthConversion, src/zimg/depth/):
 // left shift, integer to FLOAT or HALF, HALF <-> FLOAT, and dither (NONE /
-// ORDERED) to an integer type. One pass over the plane, HBM-bound: each thread converts runs of 8
-// samples of one line with vector loads and stores where the plane allows.
+// ORDERED / RANDOM) to an integer type. One pass over the plane, HBM-bound:
+// each thread converts runs of 8 samples of one line with vector loads and
+// stores where the plane allows. Error diffusion is ed_kernel.cu.
 //
 // Arithmetic is zimg's C path in IEEE single precision, step for step:
 // x * scale rounded, + offset rounded (no fused multiply-add,
@@ -15,6 +16,7 @@
 #include <type_traits>
 
 #include "depth.h"
+#include "depth_device.cuh"
 
 namespace zg {
 
@@ -38,26 +40,11 @@ __device__ __forceinline__ unsigned bayer16(unsigned i, unsigned j)
 	return v;
 }
 
-// HALF samples: IEEE binary16 bits, a type of its own so that templates do
-// not take them for WORD.
-struct Half {
-	uint16_t bits;
+// zimg's 64 x 64 blue-noise matrix (blue.h:10-13), four row-major entries
+// per little-endian word.
+__device__ const uint32_t kBlueNoiseWords[1024] = {
+#include "blue_noise_table.inc"
 };
-
-// binary16 -> binary32, exact; NaNs stay NaN with the quiet bit set.
-__device__ __forceinline__ float half_bits_to_float(uint32_t h)
-{
-	const uint32_t sign = (h & 0x8000u) << 16;
-	const uint32_t e = (h >> 10) & 0x1Fu, m = h & 0x3FFu;
-	if (e == 0x1Fu)
-		return __uint_as_float(sign | 0x7F800000u | (m ? ((m << 13) | 0x00400000u) : 0u));
-	if (e == 0) {
-		// zero or subnormal: m * 2^-24, exact in binary32
-		const float v = __fmul_rn(static_cast<float>(m), 5.9604644775390625e-8f);
-		return __uint_as_float(__float_as_uint(v) | sign);
-	}
-	return __uint_as_float(sign | ((e + 112u) << 23) | (m << 13));
-}
 
 // binary32 -> binary16 bits, rounded to nearest even; overflow to infinity;
 // NaNs keep the payload's top bits with the quiet bit set.
@@ -174,20 +161,33 @@ template <class T, class U, int MODE>
 __global__ void __launch_bounds__(kThreads)
 depth_kernel(DepthLaunch L)
 {
-	__shared__ __align__(16) float table[256];  // this plane's dither values, row-major 16 x 16
+	// this plane's dither values at (line mod 64, column mod 64), row-major;
+	// the 16 x 16 ordered matrix repeats four times across and down
+	__shared__ __align__(16) float table[MODE == 3 ? 64 * 64 : 4];
 	if (MODE == 3) {
-		for (int t = threadIdx.x; t < 256; t += kThreads) {
-			unsigned i = t >> 4, j = t & 15;
+		for (int t = threadIdx.x; t < 64 * 64; t += kThreads) {
+			const unsigned i = t >> 6, j = t & 63;
 			float v = 0.0f;
-			if (L.ordered) {
+			unsigned m = 0;
+			if (L.dither == 1) {
 				// variants by plane (dither.cpp:170-186): as is, mirrored
 				// left-right, top-bottom, transposed
+				const unsigned s = L.seq & 3, i4 = i & 15, j4 = j & 15;
+				const unsigned ii = s == 2 ? 15 - i4 : (s == 3 ? j4 : i4);
+				const unsigned jj = s == 1 ? 15 - j4 : (s == 3 ? i4 : j4);
+				m = bayer16(ii, jj);
+			} else if (L.dither == 2) {
+				// entry (line + voff, column + hoff) mod 64, (hoff, voff)
+				// by plane (dither.cpp:226-233)
 				const unsigned s = L.seq & 3;
-				const unsigned ii = s == 2 ? 15 - i : (s == 3 ? j : i);
-				const unsigned jj = s == 1 ? 15 - j : (s == 3 ? i : j);
-				// (m + 1) / 257 - 1/2 in float (dither.cpp:157-167)
-				v = __fsub_rn(__fdiv_rn(static_cast<float>(bayer16(ii, jj) + 1), 257.0f), 0.5f);
+				const unsigned hoff = s == 1 ? 32 : (s == 2 ? 16 : (s == 3 ? 48 : 0));
+				const unsigned voff = s == 1 ? 12 : (s == 2 ? 55 : (s == 3 ? 26 : 0));
+				const unsigned k = ((i + voff) & 63) * 64 + ((j + hoff) & 63);
+				m = (kBlueNoiseWords[k >> 2] >> (8 * (k & 3))) & 0xFFu;
 			}
+			// (m + 1) / 257 - 1/2 in float (dither.cpp:157-167)
+			if (L.dither)
+				v = __fsub_rn(__fdiv_rn(static_cast<float>(m + 1), 257.0f), 0.5f);
 			table[t] = v;
 		}
 		__syncthreads();
@@ -204,7 +204,7 @@ depth_kernel(DepthLaunch L)
 		{
 			const T *srow = reinterpret_cast<const T *>(static_cast<const char *>(L.src) + static_cast<ptrdiff_t>(i) * L.src_stride);
 			U *drow = reinterpret_cast<U *>(static_cast<char *>(L.dst) + static_cast<ptrdiff_t>(i) * L.dst_stride);
-			const float *trow = table + ((i & 15) << 4);
+			const float *trow = table + ((i & 63) << 6);
 			const int j0 = r * kRun;
 			const int n = min(kRun, L.width - j0);
 			const T *s = srow + j0;
@@ -252,8 +252,8 @@ depth_kernel(DepthLaunch L)
 						q[e] = static_cast<uint32_t>(x[e]) << L.shift;
 				} else {
 					// the run's 8 dither values: j0 is a multiple of 8
-					const float4 t0 = *reinterpret_cast<const float4 *>(trow + (j0 & 15));
-					const float4 t1 = *reinterpret_cast<const float4 *>(trow + (j0 & 15) + 4);
+					const float4 t0 = *reinterpret_cast<const float4 *>(trow + (j0 & 63));
+					const float4 t1 = *reinterpret_cast<const float4 *>(trow + (j0 & 63) + 4);
 					const float dv[kRun] = { t0.x, t0.y, t0.z, t0.w, t1.x, t1.y, t1.z, t1.w };
 #pragma unroll
 					for (int e = 0; e < kRun; ++e) {
