@@ -555,3 +555,72 @@ def graph_plane_chain(o: "Oracle", src: np.ndarray, fs: PixelFormat, fd: PixelFo
                        subwidth=rp["subwidth"], subheight=rp["subheight"],
                        mode="c" if fr.type == "word" else "fma", nthreads=16)
     return y if o.depth_mode(fr, fd, dither) == 0 else o.depth_convert(y, fr, fd, dither, plane)
+
+
+def _same_geometry(a: dict, b: dict) -> bool:
+    return all(a[k] == b[k] for k in ("width", "height", "left", "top", "aw", "ah"))
+
+
+def _float_resize(o: "Oracle", x: np.ndarray, src: dict, dst: dict, kind, a=math.nan, b=math.nan) -> np.ndarray:
+    rp = resize_params(src, dst)
+    return o.resize_plane(x.astype(np.float32), rp["dst_w"], rp["dst_h"], kind, a, b, shift_w=rp["shift_w"],
+                          shift_h=rp["shift_h"], subwidth=rp["subwidth"], subheight=rp["subheight"], mode="fma",
+                          nthreads=16)
+
+
+def graph_straight_alpha(o: "Oracle", srcs: list, fs: list, fd: list, sgeo: list, dgeo: list, color: str,
+                         kind, kind_uv, dither="none", a=math.nan, b=math.nan, a_uv=math.nan, b_uv=math.nan) -> list:
+    """zimg's graph for straight alpha through an interpolating resize
+    (connect_internal, src/zimg/graph/graphbuilder.cpp:1019-1068): srcs / fs /
+    fd hold the colour planes then alpha (PixelFormats with alpha full range,
+    chroma flags on YUV chroma), sgeo / dgeo plane_geometry() of the two
+    formats. Every plane to FLOAT at the source luma geometry (chroma resized
+    up with the chroma filter, make_float_444_state :446-457), colour times
+    alpha as it is (PremultiplyFilter, simple_filters.cpp:76-89), all planes
+    resized to the destination luma geometry (chroma with the chroma filter),
+    colour divided by alpha clamped to [0, 1], 0 where that is 0
+    (UnpremultiplyFilter :98-110), chroma resized to its own geometry, every
+    plane converted to the output format. FP32 resizes in the sequential
+    fused multiply-add order, as graph_plane_chain."""
+    ncolor = len(srcs) - 1
+    gs, gd = sgeo[0], dgeo[0]
+    yuv = color == "yuv"
+
+    def chroma(p):
+        return yuv and p in (1, 2)
+
+    def fl(p):
+        return PixelFormat("float", None, False, chroma(p))
+
+    def to_fmt(x, f_in, f_out, plane):
+        return x if o.depth_mode(f_in, f_out, dither) == 0 else o.depth_convert(x, f_in, f_out, dither, plane)
+
+    planes = []
+    for k in range(ncolor + 1):
+        p = 3 if k == ncolor else k
+        g_src = sgeo[p] if chroma(p) else gs
+        x = to_fmt(srcs[k], fs[k], fl(p), p).astype(np.float32)
+        if chroma(p) and not _same_geometry(g_src, gs):
+            x = _float_resize(o, x, g_src, gs, kind_uv, a_uv, b_uv)
+        planes.append(x)
+    al = planes[ncolor]
+    for k in range(ncolor):
+        planes[k] = (planes[k] * al).astype(np.float32)
+    if not _same_geometry(gs, gd):
+        planes = [_float_resize(o, x, gs, gd, kind_uv if chroma(3 if k == ncolor else k) else kind,
+                                a_uv if chroma(3 if k == ncolor else k) else a,
+                                b_uv if chroma(3 if k == ncolor else k) else b)
+                  for k, x in enumerate(planes)]
+    al = planes[ncolor]
+    c = np.where(al < 0, np.float32(0), np.where(np.float32(1) < al, np.float32(1), al)).astype(np.float32)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        for k in range(ncolor):
+            planes[k] = np.where(c == 0, np.float32(0), planes[k] / c).astype(np.float32)
+    out = []
+    for k in range(ncolor + 1):
+        p = 3 if k == ncolor else k
+        x = planes[k]
+        if chroma(p) and not _same_geometry(gd, dgeo[p]):
+            x = _float_resize(o, x, gd, dgeo[p], kind_uv, a_uv, b_uv)
+        out.append(to_fmt(x, fl(p), fd[k], p))
+    return out

@@ -289,3 +289,86 @@ def test_graph_unresize_refusals(cuda):
         with pytest.raises(zg.ZimgError) as e:
             zg.Graph(s, d, params)
         assert e.value.code == 3076
+
+
+ALPHA_CASES = [
+    # (src type, depth, range, dst type, depth, range, size in, size out, color,
+    #  subsampling in, out, dither, alpha type, premultiplied chain expected)
+    ("word", 10, 0, "byte", 8, 0, (640, 360), (640, 360), 2, 1, 1, "ordered", 1, False),   # depth only
+    ("byte", 8, 1, "word", 16, 1, (640, 360), (960, 540), 1, 0, 0, "none", 2, False),      # premultiplied input
+    ("word", 10, 0, "byte", 8, 0, (1280, 720), (640, 360), 2, 1, 1, "ordered", 1, True),   # straight, resized
+    ("float", 32, 0, "float", 32, 0, (400, 300), (600, 450), 1, 0, 0, "none", 1, True),
+    ("byte", 8, 0, "byte", 8, 0, (320, 240), (480, 360), 0, 0, 0, "error_diffusion", 1, True),
+    ("half", 16, 0, "word", 12, 0, (640, 480), (320, 240), 2, 1, 1, "random", 1, True),
+    ("word", 10, 0, "word", 10, 0, (640, 360), (640, 360), 2, 1, 0, "none", 1, True),     # 4:2:0 -> 4:4:4 only
+    ("word", 16, 1, "byte", 8, 1, (512, 512), (512, 512), 1, 0, 0, "random", 1, False),    # full-range alpha depth change
+]
+
+
+def _alpha_plane(rng, f, h, w):
+    if f.type in ("float", "half"):
+        x = (rng.random((h, w), dtype=np.float32) * 1.2 - 0.1).astype(np.float32)  # a little outside [0, 1]
+        x[:, : w // 8] = 0.0                                                          # transparent columns
+        return x.astype(np.float16).view(np.uint16) if f.type == "half" else x
+    x = rng.integers(0, 1 << f.bits, size=(h, w)).astype(f.dtype)
+    x[:, : w // 8] = 0
+    return x
+
+
+@pytest.mark.parametrize("case", range(len(ALPHA_CASES)))
+def test_graph_alpha(cuda, oracle, case):
+    """Graphs with an alpha plane: alpha depth changes (alpha is full range in
+    the integer types, graphbuilder.cpp:404-408), premultiplied alpha resized
+    plane by plane, and straight alpha through an interpolating resize, which
+    zimg premultiplies in FLOAT 4:4:4 (graphbuilder.cpp:594-600,1019-1068);
+    every plane equal to the oracle's restatement."""
+    import torch
+    import zimg_gb300 as zg
+    from oracle import oracle as O
+    st, sd, sr, dt, dd, dr, (sw, sh), (dw, dh), color, subi, subo, dither, alpha, premul = ALPHA_CASES[case]
+    cname = ["grey", "rgb", "yuv"][color]
+    sfmt = zg.image_format(sw, sh, st, depth=sd, pixel_range=sr, color_family=color, subsample_w=subi,
+                           subsample_h=subi, chroma_location=0, alpha=alpha)
+    dfmt = zg.image_format(dw, dh, dt, depth=dd, pixel_range=dr, color_family=color, subsample_w=subo,
+                           subsample_h=subo, chroma_location=0, alpha=alpha)
+    dmap = {"none": 0, "ordered": 1, "random": 2, "error_diffusion": 3}
+    g = zg.Graph(sfmt, dfmt, zg.graph_params(resample_filter="lanczos", resample_filter_uv="bicubic",
+                                             dither_type=dmap[dither]))
+    rng = np.random.default_rng(800 + case)
+    ncolor = 1 if color == 0 else 3
+    sgeo = O.plane_geometry(dict(width=sw, height=sh, subsample_w=subi, subsample_h=subi, color=cname,
+                                 chroma_location=0))
+    dgeo = O.plane_geometry(dict(width=dw, height=dh, subsample_w=subo, subsample_h=subo, color=cname,
+                                 chroma_location=0))
+    srcs, fss, fds, dsts = [], [], [], []
+    for p in range(ncolor):
+        uv = color == 2 and p > 0
+        fs, fd = O.PixelFormat(st, sd, bool(sr), uv), O.PixelFormat(dt, dd, bool(dr), uv)
+        srcs.append(make_src(rng, fs, sgeo[p]["height"], sgeo[p]["width"], special=False))
+        fss.append(fs)
+        fds.append(fd)
+        dsts.append(empty(dgeo[p]["height"], dgeo[p]["width"], dt))
+    is_int = lambda t: t in ("byte", "word")  # noqa: E731
+    fa_s, fa_d = O.PixelFormat(st, sd, is_int(st), False), O.PixelFormat(dt, dd, is_int(dt), False)
+    srcs.append(_alpha_plane(rng, fa_s, sh, sw))
+    fss.append(fa_s)
+    fds.append(fa_d)
+    dsts.append(empty(dh, dw, dt))
+    if premul:
+        wants = O.graph_straight_alpha(oracle, srcs, fss, fds, sgeo, dgeo, cname, "lanczos", "bicubic", dither)
+    else:
+        wants = []
+        for k in range(ncolor + 1):
+            p = 3 if k == ncolor else k
+            gs, gd = (sgeo[0], dgeo[0]) if p == 3 or color != 2 else (sgeo[p], dgeo[p])
+            rp = None if (sw, sh) == (dw, dh) and subi == subo else O.resize_params(gs, gd)
+            kind = "bicubic" if color == 2 and p in (1, 2) else "lanczos"
+            wants.append(O.graph_plane_chain(oracle, srcs[k], fss[k], fds[k], rp, kind, dither=dither, plane=p))
+    planes_in = [to_dev(s) for s in srcs[:ncolor]] + [None] * (3 - ncolor) + [to_dev(srcs[ncolor])]
+    planes_out = dsts[:ncolor] + [None] * (3 - ncolor) + [dsts[ncolor]]
+    g.process(planes_in, planes_out)
+    torch.cuda.synchronize()
+    for k in range(ncolor + 1):
+        got = to_host(dsts[k], O.PixelFormat(dt, dd).dtype)
+        np.testing.assert_array_equal(got.view(np.uint8), wants[k].view(np.uint8),
+                                      err_msg=f"{ALPHA_CASES[case]} plane {k}")

@@ -23,7 +23,7 @@ LIB = os.path.join(OUT_DIR, "libzimg_gb300.so")
 SOURCES = ["filter_plan.cpp", "capi.cu", "capi_graph.cu", "capi_batch.cu", "capi_static_tmp.cu",
            "pass_kernels.cu", "fused.cu", "fused_inst_v_f32.cu", "fused_inst_v_u16.cu", "fused_inst_h_f32.cu",
            "fused_inst_h_u16.cu", "mma.cu", "chain.cu", "chain_tma.cu", "wide_kernel.cu", "wide_umma.cu", "copy_kernel.cu",
-           "depth_kernel.cu", "ed_kernel.cu", "capi_depth.cu", "unresize_plan.cpp", "unresize_kernel.cu", "capi_unresize.cu"]
+           "depth_kernel.cu", "ed_kernel.cu", "alpha_kernel.cu", "capi_depth.cu", "unresize_plan.cpp", "unresize_kernel.cu", "capi_unresize.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

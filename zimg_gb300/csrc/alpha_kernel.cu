@@ -1,0 +1,74 @@
+// Straight-alpha premultiply and unpremultiply of FLOAT planes (zimg's
+// PremultiplyFilter / UnpremultiplyFilter, src/zimg/graph/simple_filters.cpp:
+// 69-110), one launch for up to three colour planes against one alpha plane.
+// HBM-bound: each thread handles four samples of one line per step.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+
+#include "alpha.h"
+
+namespace zg {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+template <bool INVERSE>
+__global__ void __launch_bounds__(kThreads) alpha_kernel(AlphaLaunch L)
+{
+	const int quads = (L.width + 3) / 4;
+	const long long per_plane = static_cast<long long>(quads) * L.height;
+	const long long total = per_plane * L.num_planes;
+	for (long long u = static_cast<long long>(blockIdx.x) * kThreads + threadIdx.x; u < total;
+	     u += static_cast<long long>(gridDim.x) * kThreads) {
+		const int p = static_cast<int>(u / per_plane);
+		const long long r = u - p * per_plane;
+		const int i = static_cast<int>(r / quads);
+		const int j0 = static_cast<int>(r - static_cast<long long>(i) * quads) * 4;
+		float *x = reinterpret_cast<float *>(static_cast<char *>(L.planes[p]) + static_cast<ptrdiff_t>(i) * L.stride);
+		const float *a = reinterpret_cast<const float *>(static_cast<const char *>(L.alpha) +
+		                                                 static_cast<ptrdiff_t>(i) * L.alpha_stride);
+		const int n = min(4, L.width - j0);
+		for (int e = 0; e < n; ++e) {
+			const float v = x[j0 + e], al = a[j0 + e];
+			if (INVERSE) {
+				// alpha clamped to [0, 1] (a NaN passes), 0 where it is 0
+				const float c = al < 0.0f ? 0.0f : (1.0f < al ? 1.0f : al);
+				x[j0 + e] = c == 0.0f ? 0.0f : __fdiv_rn(v, c);
+			} else {
+				// zimg multiplies by the alpha sample as it is (its clamped
+				// copy goes unused, simple_filters.cpp:83-85)
+				x[j0 + e] = __fmul_rn(v, al);
+			}
+		}
+	}
+}
+
+} // namespace
+
+cudaError_t launch_alpha(const AlphaLaunch &L, bool inverse, cudaStream_t stream)
+{
+	if (L.width <= 0 || L.height <= 0 || L.num_planes <= 0)
+		return cudaSuccess;
+	if (L.num_planes > 3)
+		return cudaErrorInvalidValue;
+	static int sms = 0;
+	if (!sms) {
+		int dev = 0;
+		cudaGetDevice(&dev);
+		cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+		if (sms < 1)
+			sms = 1;
+	}
+	const long long units = static_cast<long long>((L.width + 3) / 4) * L.height * L.num_planes;
+	const int grid = static_cast<int>(std::min<long long>((units + kThreads - 1) / kThreads, static_cast<long long>(sms) * 8));
+	if (inverse)
+		alpha_kernel<true><<<grid, kThreads, 0, stream>>>(L);
+	else
+		alpha_kernel<false><<<grid, kThreads, 0, stream>>>(L);
+	return cudaGetLastError();
+}
+
+} // namespace zg

@@ -7,6 +7,7 @@
 // subrectangle copies (graphbuilder.cpp:540-573) and the shift / subwidth
 // mapping of resize_plane (graphbuilder.cpp:769-776).
 #include "capi_common.h"
+#include "alpha.h"
 
 #include <cfloat>
 #include <cmath>
@@ -256,6 +257,67 @@ zg_depth *make_depth(unsigned w, unsigned h, const PixFmt &in, const PixFmt &out
 	return d;
 }
 
+// The resize of one plane between two geometries (resize_plane,
+// graphbuilder.cpp:769-776).
+zg_resize_params geom_resize_params(const PlaneGeom &sp, const PlaneGeom &dp)
+{
+	zg_resize_params rp;
+	zg_resize_params_default(&rp);
+	const double scale_w = dp.aw / sp.aw;
+	const double scale_h = dp.ah / sp.ah;
+	rp.src_width = sp.width;
+	rp.src_height = sp.height;
+	rp.dst_width = dp.width;
+	rp.dst_height = dp.height;
+	rp.shift_w = sp.left - dp.left / scale_w;
+	rp.shift_h = sp.top - dp.top / scale_h;
+	rp.subwidth = sp.aw * (dp.width / dp.aw);
+	rp.subheight = sp.ah * (dp.height / dp.ah);
+	return rp;
+}
+
+zg_resize *make_float_resize(const PlaneGeom &sp, const PlaneGeom &dp, int filter, double a, double b, size_t *tmp)
+{
+	zg_resize_params rp = geom_resize_params(sp, dp);
+	rp.pixel_type = ZG_PIXEL_FLOAT;
+	rp.depth = 32;
+	rp.filter = static_cast<zg_resample_filter>(filter);
+	rp.filter_param_a = a;
+	rp.filter_param_b = b;
+	zg_resize *r = nullptr;
+	zg_error_code rc = zg_resize_create(&rp, &r);
+	if (rc != ZG_ERROR_SUCCESS) {
+		char msg[256];
+		zg_get_last_error(msg, sizeof(msg));
+		throw Error(rc, msg);
+	}
+	size_t t = 0;
+	zg_resize_get_tmp_size(r, &t);
+	*tmp = std::max(*tmp, t);
+	return r;
+}
+
+void run_resize(const zg_resize *r, const void *src, ptrdiff_t ss, void *dst, ptrdiff_t ds, void *tmp, zg_stream st)
+{
+	zg_error_code rc = zg_resize_process(r, src, ss, dst, ds, tmp, st);
+	if (rc != ZG_ERROR_SUCCESS) {
+		char msg[256];
+		zg_get_last_error(msg, sizeof(msg));
+		throw Error(rc, msg);
+	}
+}
+
+// needs_interpolation_plane (graphbuilder.cpp:509-525): another active size
+// or another fractional phase of the active region's corner
+bool needs_interpolation_plane(const PlaneGeom &a, const PlaneGeom &b)
+{
+	auto phase = [](double x) {
+		double ip;
+		return std::modf(x, &ip);
+	};
+	return a.aw != b.aw || a.ah != b.ah || phase(a.left) != phase(b.left) || phase(a.top) != phase(b.top);
+}
+
 void run_depth(const zg_depth *d, const void *src, ptrdiff_t ss, void *dst, ptrdiff_t ds, zg_stream st)
 {
 	zg_error_code rc = zg_depth_process(d, src, ss, dst, ds, st);
@@ -290,6 +352,28 @@ struct zg_graph {
 		unsigned src_w = 0, src_h = 0, src_ssh = 0, dst_ssh = 0;
 		size_t sstage_pitch = 0, dstage_pitch = 0, off_sstage = 0, off_dstage = 0;
 	} planes[4];
+	// Straight alpha through an interpolating resize (connect_internal,
+	// graphbuilder.cpp:1019-1068): every plane to FLOAT 4:4:4 at the source
+	// luma geometry (chroma resized up), colour planes multiplied by alpha,
+	// all four resized to the destination luma geometry, colour divided by
+	// alpha, chroma resized to its own geometry, every plane converted to the
+	// output format. Float planes in tmp: four at the source luma size (slot
+	// 3 alpha), four at the destination luma size when that differs, one
+	// chroma plane at each end, then the resizes' scratch.
+	struct Premul {
+		bool on = false;
+		int ncolor = 0;
+		bool across_needed = false;  // source and destination luma geometry differ
+		unsigned sw = 0, sh = 0, dw = 0, dh = 0;
+		size_t s_pitch = 0, d_pitch = 0, off_s = 0, off_d = 0;
+		zg_depth *in[4] = {}, *out[4] = {};
+		zg_resize *up = nullptr;         // YUV chroma: source chroma -> source luma geometry
+		zg_resize *across = nullptr;     // source -> destination luma geometry, luma filter
+		zg_resize *across_uv = nullptr;  // the same with the chroma filter (YUV)
+		zg_resize *down = nullptr;       // YUV chroma: destination luma -> destination chroma geometry
+		unsigned cs_w = 0, cs_h = 0, cd_w = 0, cd_h = 0;
+		size_t cs_pitch = 0, cd_pitch = 0, off_cs = 0, off_cd = 0, off_rtmp = 0;
+	} premul;
 	size_t tmp_size = 0;
 	// lines and widths the callbacks are called with (the luma plane's), and
 	// the vertical subsampling step of the source and destination formats
@@ -304,6 +388,14 @@ struct zg_graph {
 			zg_depth_free(p.post);
 			zg_depth_free(p.only);
 		}
+		for (int p = 0; p < 4; ++p) {
+			zg_depth_free(premul.in[p]);
+			zg_depth_free(premul.out[p]);
+		}
+		zg_resize_free(premul.up);
+		zg_resize_free(premul.across);
+		zg_resize_free(premul.across_uv);
+		zg_resize_free(premul.down);
 	}
 };
 
@@ -371,14 +463,112 @@ zg_graph *zg_graph_build(const zg_image_format *src_format, const zg_image_forma
 			throw Error(kErrNoColorspaceConversion, "colorspace conversion is outside the resize path");
 		if (s.alpha != d.alpha)
 			throw Error(kErrUnsupported, "alpha conversion is outside the resize path");
-		if (s.alpha && format_change)
-			throw Error(kErrUnsupported, "depth conversion of alpha planes is not supported by this library");
+		(void)format_change;
 
 		auto g = std::make_unique<zg_graph>();
 		g->device = current_device();
 		auto bytes = [](int t) { return t == ZG_PIXEL_BYTE ? 1u : (t == ZG_PIXEL_FLOAT ? 4u : 2u); };
+		const int dither = static_cast<int>(gp.dither_type);
+		// A plane's pixel format: chroma of YUV centred; alpha full range in
+		// the integer types, never chroma (alpha_from_luma,
+		// graphbuilder.cpp:404-408)
+		auto plane_fmt = [](const FormatState &f, int p) {
+			if (p == PLANE_A) {
+				const bool is_int = f.pixel_type == ZG_PIXEL_BYTE || f.pixel_type == ZG_PIXEL_WORD;
+				return PixFmt{ f.pixel_type, f.depth, is_int, false };
+			}
+			const bool uv = (p == PLANE_U || p == PLANE_V) && f.color == COLOR_YUV;
+			return PixFmt{ f.pixel_type, f.depth, f.range == 1, uv };
+		};
+		// needs_interpolation over the planes both formats have
+		// (graphbuilder.cpp:527-538)
+		bool interpolate = needs_interpolation_plane(s.planes[PLANE_Y], d.planes[PLANE_Y]);
+		if (s.color != COLOR_GREY)
+			interpolate = interpolate || needs_interpolation_plane(s.planes[PLANE_U], d.planes[PLANE_U]) ||
+			              needs_interpolation_plane(s.planes[PLANE_V], d.planes[PLANE_V]);
+		if (s.alpha)
+			interpolate = interpolate || needs_interpolation_plane(s.planes[PLANE_A], d.planes[PLANE_A]);
+		// straight alpha is premultiplied around an interpolating resize
+		// (needs_premul, graphbuilder.cpp:594-600)
+		const bool premul = s.alpha == 1 && interpolate;
+		if (premul && gp.resample_filter == ZG_RESIZE_UNRESIZE)
+			throw Error(kErrUnsupported, "unresize of images with straight alpha is not supported by this library");
 
-		for (int p = 0; p < 4; ++p) {
+		for (int p = 0; p < 4 && premul; ++p) {
+			const bool chroma = p == PLANE_U || p == PLANE_V;
+			if (chroma && s.color == COLOR_GREY)
+				continue;
+			auto &pm = g->premul;
+			const PlaneGeom &gs = s.planes[PLANE_Y], &gd = d.planes[PLANE_Y];
+			if (!pm.on) {
+				pm.on = true;
+				pm.ncolor = s.color == COLOR_GREY ? 1 : 3;
+				pm.sw = gs.width;
+				pm.sh = gs.height;
+				pm.dw = gd.width;
+				pm.dh = gd.height;
+				pm.s_pitch = pitch_of(gs.width, 4);
+				pm.d_pitch = pitch_of(gd.width, 4);
+				pm.across_needed = !(gs == gd);
+			}
+			auto &gpl = g->planes[p];
+			gpl.present = true;
+			gpl.mode = 5;
+			const int q = (s.color == COLOR_RGB && chroma) ? PLANE_Y : p;
+			const PlaneGeom &sp = s.planes[q], &dp = d.planes[q];
+			gpl.w = dp.width;
+			gpl.h = dp.height;
+			gpl.in_bytes = bytes(s.pixel_type);
+			gpl.out_bytes = bytes(d.pixel_type);
+			gpl.src_w = sp.width;
+			gpl.src_h = sp.height;
+			gpl.src_ssh = chroma && s.color == COLOR_YUV ? s.subsample_h : 0;
+			gpl.dst_ssh = chroma && s.color == COLOR_YUV ? d.subsample_h : 0;
+			const bool uv = chroma && s.color == COLOR_YUV;
+			// make_float_444_state (graphbuilder.cpp:446-457)
+			const PixFmt fl{ ZG_PIXEL_FLOAT, 32, false, uv };
+			pm.in[p] = make_depth(sp.width, sp.height, plane_fmt(s, p), fl, dither, p);
+			pm.out[p] = make_depth(dp.width, dp.height, fl, plane_fmt(d, p), dither, p);
+			if (uv && !(sp == gs) && !pm.up) {
+				pm.up = make_float_resize(sp, gs, gp.resample_filter_uv, gp.filter_param_a_uv, gp.filter_param_b_uv,
+				                          &pm.off_rtmp);
+				pm.cs_w = sp.width;
+				pm.cs_h = sp.height;
+			}
+			if (uv && !(dp == gd) && !pm.down) {
+				pm.down = make_float_resize(gd, dp, gp.resample_filter_uv, gp.filter_param_a_uv, gp.filter_param_b_uv,
+				                            &pm.off_rtmp);
+				pm.cd_w = dp.width;
+				pm.cd_h = dp.height;
+			}
+			if (pm.across_needed && !pm.across)
+				pm.across = make_float_resize(gs, gd, gp.resample_filter, gp.filter_param_a, gp.filter_param_b,
+				                              &pm.off_rtmp);
+			if (pm.across_needed && uv && !pm.across_uv)
+				pm.across_uv = make_float_resize(gs, gd, gp.resample_filter_uv, gp.filter_param_a_uv,
+				                                 gp.filter_param_b_uv, &pm.off_rtmp);
+		}
+		if (premul) {
+			// tmp layout; off_rtmp held the largest resize scratch until now
+			auto &pm = g->premul;
+			const size_t rscratch = pm.off_rtmp;
+			size_t off = 0;
+			pm.off_s = off;
+			off += 4 * pm.s_pitch * pm.sh;
+			pm.off_d = off;
+			if (pm.across_needed)
+				off += 4 * pm.d_pitch * pm.dh;
+			pm.cs_pitch = pitch_of(pm.cs_w, 4);
+			pm.off_cs = off;
+			off += pm.cs_pitch * pm.cs_h;
+			pm.cd_pitch = pitch_of(pm.cd_w, 4);
+			pm.off_cd = off;
+			off += pm.cd_pitch * pm.cd_h;
+			pm.off_rtmp = off;
+			g->tmp_size = off + rscratch;
+		}
+
+		for (int p = 0; p < 4 && !premul; ++p) {
 			const bool chroma = p == PLANE_U || p == PLANE_V;
 			if (chroma && s.color == COLOR_GREY)
 				continue;
@@ -400,11 +590,9 @@ zg_graph *zg_graph_build(const zg_image_format *src_format, const zg_image_forma
 			gpl.dst_ssh = chroma && s.color == COLOR_YUV ? d.subsample_h : 0;
 			// plane formats; full-range BYTE kept at its depth is treated as
 			// limited range for the whole chain (graphbuilder.cpp:912-920)
-			const bool uv = chroma && s.color == COLOR_YUV;
-			PixFmt fs{ s.pixel_type, s.depth, s.range == 1, uv }, fd{ d.pixel_type, d.depth, d.range == 1, uv };
+			PixFmt fs = plane_fmt(s, p), fd = plane_fmt(d, p);
 			if (fs.type == ZG_PIXEL_BYTE && fs.full && fd.full && fs.depth == fd.depth)
 				fs.full = fd.full = false;
-			const int dither = static_cast<int>(gp.dither_type);
 
 			if (sp == dp) {
 				if (fmt_equal(fs, fd)) {
@@ -435,8 +623,6 @@ zg_graph *zg_graph_build(const zg_image_format *src_format, const zg_image_forma
 				}
 			}
 			gpl.mode = 2;
-			const double scale_w = dp.aw / sp.aw;
-			const double scale_h = dp.ah / sp.ah;
 			const bool unresize = gp.resample_filter == ZG_RESIZE_UNRESIZE;
 			if (unresize && (sp.aw != sp.width || sp.ah != sp.height || dp.aw != dp.width || dp.ah != dp.height))
 				throw Error(kErrResamplingNotAvailable, "unresize not supported for given subregion");
@@ -444,21 +630,12 @@ zg_graph *zg_graph_build(const zg_image_format *src_format, const zg_image_forma
 			const PixFmt fr = unresize ? PixFmt{ ZG_PIXEL_FLOAT, 32, false, false }
 			                           : choose_resize_format(fs, fd, static_cast<double>(sp.width) * sp.height,
 			                                                  static_cast<double>(dp.width) * dp.height);
-			zg_resize_params rp;
-			zg_resize_params_default(&rp);
-			rp.src_width = sp.width;
-			rp.src_height = sp.height;
+			zg_resize_params rp = geom_resize_params(sp, dp);
 			rp.pixel_type = static_cast<zg_pixel_type>(fr.type);
 			rp.depth = fr.type == ZG_PIXEL_FLOAT ? 32 : fr.depth;
-			rp.dst_width = dp.width;
-			rp.dst_height = dp.height;
 			rp.filter = static_cast<zg_resample_filter>(chroma && s.color == COLOR_YUV ? gp.resample_filter_uv : gp.resample_filter);
 			rp.filter_param_a = chroma && s.color == COLOR_YUV ? gp.filter_param_a_uv : gp.filter_param_a;
 			rp.filter_param_b = chroma && s.color == COLOR_YUV ? gp.filter_param_b_uv : gp.filter_param_b;
-			rp.shift_w = sp.left - dp.left / scale_w;
-			rp.shift_h = sp.top - dp.top / scale_h;
-			rp.subwidth = sp.aw * (dp.width / dp.aw);
-			rp.subheight = sp.ah * (dp.height / dp.ah);
 			gpl.params = rp;
 			size_t rtmp = 0;
 			zg_error_code rc;
@@ -671,6 +848,8 @@ zg_error_code zg_graph_process_cb(const zg_graph *g, const zg_image_buffer_const
 				run_depth(pl.only, from, sst, dp, dst_st, stream);
 				continue;
 			}
+			if (pl.mode == 5)
+				continue;
 			if (pl.tmp && !tmp)
 				throw Error(kErrIllegalArgument, "tmp is null");
 			const void *rs = sp;
@@ -692,6 +871,70 @@ zg_error_code zg_graph_process_cb(const zg_graph *g, const zg_image_buffer_const
 			}
 			if (pl.post)
 				run_depth(pl.post, rd, rds, dp, dst_st, stream);
+		}
+
+		if (g->premul.on) {
+			const auto &pm = g->premul;
+			if (!t)
+				throw Error(kErrIllegalArgument, "tmp is null");
+			const ptrdiff_t sps = static_cast<ptrdiff_t>(pm.s_pitch), dps = static_cast<ptrdiff_t>(pm.d_pitch);
+			auto s_plane = [&](int p) { return t + pm.off_s + static_cast<size_t>(p) * pm.s_pitch * pm.sh; };
+			auto d_plane = [&](int p) {
+				return pm.across_needed ? t + pm.off_d + static_cast<size_t>(p) * pm.d_pitch * pm.dh : s_plane(p);
+			};
+			char *rtmp = t + pm.off_rtmp;
+			// to FLOAT 4:4:4 at the source luma geometry
+			for (int p = 0; p < 4; ++p) {
+				if (!g->planes[p].present)
+					continue;
+				const bool up = (p == PLANE_U || p == PLANE_V) && pm.up;
+				if (up) {
+					run_depth(pm.in[p], from_data[p], from_stride[p], t + pm.off_cs, static_cast<ptrdiff_t>(pm.cs_pitch),
+					          stream);
+					run_resize(pm.up, t + pm.off_cs, static_cast<ptrdiff_t>(pm.cs_pitch), s_plane(p), sps, rtmp, stream);
+				} else {
+					run_depth(pm.in[p], from_data[p], from_stride[p], s_plane(p), sps, stream);
+				}
+			}
+			AlphaLaunch A{};
+			A.num_planes = pm.ncolor;
+			for (int p = 0; p < pm.ncolor; ++p)
+				A.planes[p] = s_plane(p);
+			A.stride = sps;
+			A.alpha = s_plane(PLANE_A);
+			A.alpha_stride = sps;
+			A.width = static_cast<int>(pm.sw);
+			A.height = static_cast<int>(pm.sh);
+			cuda_check(launch_alpha(A, false, st), "premultiply launch");
+			if (pm.across_needed) {
+				for (int p = 0; p < 4; ++p) {
+					if (!g->planes[p].present)
+						continue;
+					const zg_resize *r = (p == PLANE_U || p == PLANE_V) && pm.across_uv ? pm.across_uv : pm.across;
+					run_resize(r, s_plane(p), sps, d_plane(p), dps, rtmp, stream);
+				}
+			}
+			for (int p = 0; p < pm.ncolor; ++p)
+				A.planes[p] = d_plane(p);
+			A.stride = dps;
+			A.alpha = d_plane(PLANE_A);
+			A.alpha_stride = dps;
+			A.width = static_cast<int>(pm.dw);
+			A.height = static_cast<int>(pm.dh);
+			cuda_check(launch_alpha(A, true, st), "unpremultiply launch");
+			// chroma to its own geometry, then every plane to the output format
+			for (int p = 0; p < 4; ++p) {
+				if (!g->planes[p].present)
+					continue;
+				const bool down = (p == PLANE_U || p == PLANE_V) && pm.down;
+				if (down) {
+					run_resize(pm.down, d_plane(p), dps, t + pm.off_cd, static_cast<ptrdiff_t>(pm.cd_pitch), rtmp, stream);
+					run_depth(pm.out[p], t + pm.off_cd, static_cast<ptrdiff_t>(pm.cd_pitch), to_data[p], to_stride[p],
+					          stream);
+				} else {
+					run_depth(pm.out[p], d_plane(p), dps, to_data[p], to_stride[p], stream);
+				}
+			}
 		}
 
 		// Output: ring lines scattered from the staging planes a ring's worth
