@@ -370,11 +370,17 @@ ZG_API zg_error_code zg_batch_get_launch_count(const zg_batch *b, unsigned *out)
  * (zimg.h:507,550-552,679; zimg.cpp:662-690). The format structs have the same
  * layout and meaning as zimg_image_format and zimg_graph_builder_params
  * (zimg.h:558-647), so a zimg caller's structs can be passed through after a
- * pointer cast. Supported: GREY/YUV/RGB with alpha, WORD or FLOAT, equal pixel
- * type, depth and colorspace on both sides; chroma siting, field parity and
- * active regions are honoured as zimg's graph builder does
- * (graphbuilder.cpp:65-188,331-366,753-824). Anything needing a colorspace,
- * depth or field-parity conversion returns ZG_ERROR_UNSUPPORTED_OPERATION.
+ * pointer cast. Supported: GREY/YUV/RGB with or without alpha, every pixel
+ * type, changes of size, subsampling, pixel type, depth and range (the depth
+ * conversions with the graph's dither type, placed as zimg places them,
+ * graphbuilder.cpp:720-751,864-953); chroma siting, field parity and active
+ * regions as zimg's graph builder maps them (graphbuilder.cpp:65-188,331-366,
+ * 753-824). Alpha planes are full range in the integer types; straight alpha
+ * through an interpolating resize is premultiplied in FLOAT 4:4:4 and divided
+ * out afterwards, as zimg does (graphbuilder.cpp:594-600,1019-1068). A change
+ * of colour family, matrix, transfer or primaries returns
+ * ZG_ERROR_NO_COLORSPACE_CONVERSION; a change of alpha type, and unresize of
+ * an image with straight alpha, ZG_ERROR_UNSUPPORTED_OPERATION.
  */
 typedef struct zg_image_format {
 	unsigned version;
