@@ -624,3 +624,89 @@ def graph_straight_alpha(o: "Oracle", srcs: list, fs: list, fd: list, sgeo: list
             x = _float_resize(o, x, gd, dgeo[p], kind_uv, a_uv, b_uv)
         out.append(to_fmt(x, fl(p), fd[k], p))
     return out
+
+
+# ---------------------------------------------------------------- colorspace --
+# zimg API codes (zimg.h:283-352) -> zimg's internal enum values
+# (colorspace.h:19-60), as translate_matrix / _transfer / _primaries map them
+# (zimg.cpp:238-305). Codes absent from the maps raise (NO_COLORSPACE_CONVERSION).
+CSP_MATRIX = {0: 1, 1: 3, 2: 0, 4: 4, 5: 2, 6: 2, 7: 5, 8: 6, 9: 7, 10: 8, 12: 9, 13: 10, 14: 12}
+CSP_TRANSFER = {1: 4, 2: 0, 7: 7, 6: 4, 4: 5, 5: 6, 11: 8, 12: 9, 13: 10, 14: 4, 15: 4, 8: 1, 9: 2, 10: 3,
+                16: 11, 17: 12, 18: 13}
+CSP_PRIMARIES = {4: 1, 5: 2, 1: 4, 2: 0, 6: 3, 7: 3, 8: 5, 9: 6, 10: 7, 11: 8, 12: 9, 22: 10}
+CSP_OPS = ("matrix", "gamma", "hlg", "hlg_inverse", "cl_to_rgb", "cl_to_yuv")
+
+
+def csp_internal(matrix: int, transfer: int, primaries: int) -> tuple:
+    """API codes -> internal enum values; KeyError when zimg has no mapping."""
+    return CSP_MATRIX[matrix], CSP_TRANSFER[transfer], CSP_PRIMARIES[primaries]
+
+
+def _bind_colorspace(L):
+    L.orc_colorspace_create.argtypes = [C.c_int] * 6 + [C.c_double, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int)]
+    L.orc_colorspace_create.restype = C.c_void_p
+    L.orc_colorspace_free.argtypes = [C.c_void_p]
+    L.orc_colorspace_num_ops.argtypes = [C.c_void_p]
+    L.orc_colorspace_op.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_float)]
+    L.orc_colorspace_run.argtypes = [C.c_void_p, C.c_uint, C.c_uint, C.POINTER(C.c_void_p), C.POINTER(C.c_ssize_t),
+                                     C.POINTER(C.c_void_p), C.POINTER(C.c_ssize_t)]
+
+
+def _planes_args(planes):
+    ptrs = (C.c_void_p * 3)(*[p.ctypes.data for p in planes])
+    strides = (C.c_ssize_t * 3)(*[p.strides[0] for p in planes])
+    return ptrs, strides
+
+
+def _orc_colorspace(self, planes, csp_in, csp_out, peak=100.0, approximate=False, scene=False, adapt=False):
+    """zimg's ColorspaceConversion (C path) on three FLOAT planes. csp_in /
+    csp_out: (matrix, transfer, primaries) API codes. Returns (planes, ops):
+    the converted planes and the names of the operations applied."""
+    L = self.lib
+    if not getattr(L, "_csp_bound", False):
+        _bind_colorspace(L)
+        L._csp_bound = True
+    err = C.c_int()
+    h = L.orc_colorspace_create(*csp_internal(*csp_in), *csp_internal(*csp_out), float(peak), int(approximate),
+                                int(scene), int(adapt), C.byref(err))
+    if not h:
+        raise ValueError(f"no colorspace conversion ({err.value})")
+    try:
+        ops = [CSP_OPS[L.orc_colorspace_op(h, k, None)] for k in range(L.orc_colorspace_num_ops(h))]
+        src = [np.ascontiguousarray(p, dtype=np.float32) for p in planes]
+        out = [np.empty_like(src[0]) for _ in range(3)]
+        hh, ww = src[0].shape
+        si, ss = _planes_args(src)
+        di, ds = _planes_args(out)
+        L.orc_colorspace_run(h, ww, hh, si, ss, di, ds)
+        return (out if ops else src), ops
+    finally:
+        L.orc_colorspace_free(h)
+
+
+def _ref_colorspace(self, planes, csp_in, csp_out, peak=100.0, approximate=False, scene=False, adapt=False, cpu=0):
+    """zimg's own ColorspaceConversion (oracle/_ref) on three FLOAT planes."""
+    L = self.lib
+    if not getattr(L, "_csp_bound", False):
+        L.ref_colorspace.argtypes = [C.c_int] * 6 + [C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint, C.c_uint,
+                                                     C.POINTER(C.c_void_p), C.POINTER(C.c_ssize_t),
+                                                     C.POINTER(C.c_void_p), C.POINTER(C.c_ssize_t), C.c_char_p,
+                                                     C.c_size_t]
+        L._csp_bound = True
+    src = [np.ascontiguousarray(p, dtype=np.float32) for p in planes]
+    out = [np.empty_like(src[0]) for _ in range(3)]
+    hh, ww = src[0].shape
+    si, ss = _planes_args(src)
+    di, ds = _planes_args(out)
+    err = C.create_string_buffer(256)
+    rc = L.ref_colorspace(*csp_internal(*csp_in), *csp_internal(*csp_out), float(peak), int(approximate), int(scene),
+                          int(adapt), cpu, ww, hh, si, ss, di, ds, err, 256)
+    if rc == 3:
+        return src
+    if rc:
+        raise ValueError(err.value.decode())
+    return out
+
+
+Oracle.colorspace = _orc_colorspace
+Reference.colorspace = _ref_colorspace

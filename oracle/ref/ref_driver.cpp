@@ -24,6 +24,7 @@
 #include "common/except.h"
 #include "common/pixel.h"
 #include "graphengine/filter.h"
+#include "colorspace/colorspace.h"
 #include "depth/blue.h"
 #include "depth/depth.h"
 #include "unresize/unresize.h"
@@ -120,6 +121,24 @@ void run_filter(const graphengine::Filter &f, const void *src, ptrdiff_t src_str
 		f.process(&in, &out, i, 0, desc.format.width, ctx, tmp);
 
 	std::free(ctx);
+	std::free(tmp);
+}
+
+// Whole planes through a filter of three planes (a colorspace conversion).
+void run_filter3(const graphengine::Filter &f, const void *const src[3], const ptrdiff_t src_stride[3],
+                 void *const dst[3], const ptrdiff_t dst_stride[3])
+{
+	const graphengine::FilterDescriptor &desc = f.descriptor();
+	graphengine::BufferDescriptor in[3], out[3];
+	for (int p = 0; p < 3; ++p) {
+		in[p] = graphengine::BufferDescriptor{ const_cast<void *>(src[p]), src_stride[p], ~0U };
+		out[p] = graphengine::BufferDescriptor{ dst[p], dst_stride[p], ~0U };
+	}
+	void *tmp = desc.scratchpad_size ? aligned_buf(desc.scratchpad_size) : nullptr;
+	if (desc.scratchpad_size && !tmp)
+		throw std::bad_alloc{};
+	for (unsigned i = 0; i < desc.format.height; ++i)
+		f.process(in, out, i, 0, desc.format.width, nullptr, tmp);
 	std::free(tmp);
 }
 
@@ -276,6 +295,38 @@ int ref_plan_run(const void *p, const void *src, ptrdiff_t src_stride, void *dst
 		run_filter(*plan->first, src, src_stride, tmp, tmp_stride);
 		run_filter(*plan->second, tmp, tmp_stride, dst, dst_stride);
 		std::free(tmp);
+		return 0;
+	} catch (...) {
+		return catch_all(err, errlen);
+	}
+}
+
+/*
+ * zimg's ColorspaceConversion (src/zimg/colorspace/colorspace.h:117-132) on
+ * three FLOAT planes. Colorspaces as zimg's internal enum values
+ * (colorspace.h:19-60); cpu as ref_plan_create. Returns 3 when the
+ * conversion is the identity (no filter; dst untouched).
+ */
+int ref_colorspace(int m_in, int t_in, int p_in, int m_out, int t_out, int p_out, double peak, int approx, int scene,
+                   int adapt, int cpu, unsigned w, unsigned h, const void *const src[3], const ptrdiff_t src_stride[3],
+                   void *const dst[3], const ptrdiff_t dst_stride[3], char *err, size_t errlen)
+{
+	try {
+		namespace cs = zimg::colorspace;
+		cs::ColorspaceConversion conv{ w, h };
+		conv.set_csp_in({ static_cast<cs::MatrixCoefficients>(m_in), static_cast<cs::TransferCharacteristics>(t_in),
+		                  static_cast<cs::ColorPrimaries>(p_in) })
+			.set_csp_out({ static_cast<cs::MatrixCoefficients>(m_out), static_cast<cs::TransferCharacteristics>(t_out),
+			               static_cast<cs::ColorPrimaries>(p_out) })
+			.set_peak_luminance(peak)
+			.set_approximate_gamma(approx != 0)
+			.set_scene_referred(scene != 0)
+			.set_chromatic_adaptation(adapt != 0)
+			.set_cpu(make_cpu(cpu));
+		std::unique_ptr<graphengine::Filter> f = conv.create();
+		if (!f)
+			return 3;
+		run_filter3(*f, src, src_stride, dst, dst_stride);
 		return 0;
 	} catch (...) {
 		return catch_all(err, errlen);

@@ -1317,3 +1317,718 @@ int orc_unresize_plane(unsigned up_w, unsigned up_h, unsigned orig_w, unsigned o
 	orc_unresize_ctx_free(&ch);
 	return 0;
 }
+
+/* ======================================================================
+ * Colorspace conversion (src/zimg/colorspace/): zimg's ColorspaceConversion
+ * on three FLOAT planes, C path (CPUClass::NONE). Enum values follow zimg's
+ * internal order (colorspace.h:19-60), which fixes the order its path search
+ * visits neighbours in.
+ * ====================================================================== */
+
+enum { CM_UNSPEC, CM_RGB, CM_601, CM_709, CM_FCC, CM_240M, CM_YCGCO, CM_2020_NCL, CM_2020_CL, CM_CHROM_NCL,
+       CM_CHROM_CL, CM_LMS, CM_ICTCP, CM_COUNT };
+enum { TC_UNSPEC, TC_LINEAR, TC_LOG100, TC_LOG316, TC_709, TC_470M, TC_470BG, TC_240M, TC_XVYCC, TC_1361, TC_SRGB,
+       TC_2084, TC_428, TC_B67, TC_COUNT };
+enum { CP_UNSPEC, CP_470M, CP_470BG, CP_SMPTE_C, CP_709, CP_FILM, CP_2020, CP_XYZ, CP_DCI_P3, CP_DCI_P3_D65,
+       CP_EBU_3213_E, CP_COUNT };
+
+typedef struct { int m, t, p; } orc_csp;
+typedef struct { double v[3][3]; } orc_m3;
+typedef struct { double v[3]; } orc_v3;
+
+/* ---- transfer functions (gamma.cpp:12-343), float, libm ---- */
+#define O_709_A 1.09929682680944f
+#define O_709_B 0.018053968510807f
+#define O_240_A 1.111572195921731f
+#define O_240_B 0.022821585529445f
+#define O_SRGB_A 1.055010718947587f
+#define O_SRGB_B 0.003041282560128f
+#define O_PQ_M1 0.1593017578125f
+#define O_PQ_M2 78.84375f
+#define O_PQ_C1 0.8359375f
+#define O_PQ_C2 18.8515625f
+#define O_PQ_C3 18.6875f
+#define O_HLG_A 0.17883277f
+#define O_HLG_B 0.28466892f
+#define O_HLG_C 0.55991073f
+#define O_PQ_OOTF 59.49080238715383f
+
+static float fmaxz(float x) { return x < 0.0f ? 0.0f : x; }  /* std::max(x, 0.0f): a NaN stays */
+
+static float t709_oetf(float x) { x = fmaxz(x); return x < O_709_B ? x * 4.5f : O_709_A * powf(x, 0.45f) - (O_709_A - 1.0f); }
+static float t709_ioetf(float x) { x = fmaxz(x); return x < 4.5f * O_709_B ? x / 4.5f : powf((x + (O_709_A - 1.0f)) / O_709_A, 1.0f / 0.45f); }
+static float tlog100(float x) { return x <= 0.01f ? 0.0f : 1.0f + log10f(x) / 2.0f; }
+static float tlog100_i(float x) { return x <= 0.0f ? 0.01f : powf(10.0f, 2 * (x - 1.0f)); }
+static float tlog316(float x) { return x <= 0.00316227766f ? 0.0f : 1.0f + log10f(x) / 2.5f; }
+static float tlog316_i(float x) { return x <= 0.0f ? 0.00316227766f : powf(10.0f, 2.5f * (x - 1.0f)); }
+static float t470m(float x) { return x < 0.0f ? 0.0f : powf(x, 2.2f); }
+static float t470m_i(float x) { return x < 0.0f ? 0.0f : powf(x, 1.0f / 2.2f); }
+static float t470bg(float x) { return x < 0.0f ? 0.0f : powf(x, 2.8f); }
+static float t470bg_i(float x) { return x < 0.0f ? 0.0f : powf(x, 1.0f / 2.8f); }
+static float t240_oetf(float x) { x = fmaxz(x); return x < 4.0f * O_240_B ? x / 4.0f : powf((x + (O_240_A - 1.0f)) / O_240_A, 1.0f / 0.45f); }
+static float t240_ioetf(float x) { x = fmaxz(x); return x < O_240_B ? x * 4.0f : O_240_A * powf(x, 0.45f) - (O_240_A - 1.0f); }
+/* fabs / copysign on the bits: gcc 13's floating-point range propagation
+ * drops the fabsf inside copysignf(f(fabsf(x)), x) at -O2 when the call is
+ * reached under x < 0 */
+static float abs_bits(float x)
+{
+	uint32_t u;
+	memcpy(&u, &x, 4);
+	u &= 0x7FFFFFFFu;
+	memcpy(&x, &u, 4);
+	return x;
+}
+static float copysign_bits(float mag, float sgn)
+{
+	uint32_t a, b;
+	memcpy(&a, &mag, 4);
+	memcpy(&b, &sgn, 4);
+	a = (a & 0x7FFFFFFFu) | (b & 0x80000000u);
+	memcpy(&mag, &a, 4);
+	return mag;
+}
+static float txvycc_oetf(float x) { return copysign_bits(t709_oetf(abs_bits(x)), x); }
+static float txvycc_ioetf(float x) { return copysign_bits(t709_ioetf(abs_bits(x)), x); }
+static float t1361_oetf(float x) { return x >= 0.0f ? t709_oetf(x) : -t709_oetf(-x * 4.0f) / 4.0f; }
+static float t1361_ioetf(float x) { return x >= 0.0f ? t709_ioetf(x) : -t709_ioetf(-x * 4.0f) / 4.0f; }
+static float thlg_oetf(float x) { x = fmaxz(x); return x <= (1.0f / 12.0f) ? sqrtf(3.0f * x) : O_HLG_A * logf(12.0f * x - O_HLG_B) + O_HLG_C; }
+static float thlg_ioetf(float x) { x = fmaxz(x); return x <= 0.5f ? (x * x) * (1.0f / 3.0f) : (expf((x - O_HLG_C) / O_HLG_A) + O_HLG_B) / 12.0f; }
+static float t1886(float x) { return x < 0.0f ? 0.0f : powf(x, 2.4f); }
+static float t1886_i(float x) { return x < 0.0f ? 0.0f : powf(x, 1.0f / 2.4f); }
+static float tsrgb(float x) { x = fmaxz(x); return x < 12.92f * O_SRGB_B ? x / 12.92f : powf((x + (O_SRGB_A - 1.0f)) / O_SRGB_A, 2.4f); }
+static float tsrgb_i(float x) { x = fmaxz(x); return x < O_SRGB_B ? x * 12.92f : O_SRGB_A * powf(x, 1.0f / 2.4f) - (O_SRGB_A - 1.0f); }
+static float t1361_eotf(float x) { return (x < 0.0f || x > 1.0f) ? t1361_ioetf(x) : t1886(x); }
+static float t1361_ieotf(float x) { return (x < 0.0f || x > 1.0f) ? t1361_oetf(x) : t1886_i(x); }
+static float txvycc_eotf(float x) { return (x < 0.0f || x > 1.0f) ? txvycc_ioetf(x) : t1886(x); }
+static float txvycc_ieotf(float x) { return (x < 0.0f || x > 1.0f) ? txvycc_oetf(x) : t1886_i(x); }
+static float tpq_eotf(float x)
+{
+	if (!(x > 0.0f))
+		return 0.0f;
+	const float xp = powf(x, 1.0f / O_PQ_M2);
+	float num = xp - O_PQ_C1, den = O_PQ_C2 - O_PQ_C3 * xp;
+	num = num < 0.0f ? 0.0f : num;
+	den = den < FLT_MIN ? FLT_MIN : den;
+	return powf(num / den, 1.0f / O_PQ_M1);
+}
+static float tpq_ieotf(float x)
+{
+	if (!(x > 0.0f))
+		return 0.0f;
+	const float xp = powf(x, O_PQ_M1);
+	const float num = (O_PQ_C1 - 1.0f) + (O_PQ_C2 - O_PQ_C3) * xp;
+	const float den = 1.0f + O_PQ_C3 * xp;
+	return powf(1.0f + num / den, O_PQ_M2);
+}
+static float t428(float x) { return x < 0.0f ? 0.0f : 52.37f / 48.0f * powf(x, 2.6f); }
+static float t428_i(float x) { return x < 0.0f ? 0.0f : powf(x * (48.0f / 52.37f), 1.0f / 2.6f); }
+static float ootf12(float x) { return x < 0.0f ? x : powf(x, 1.2f); }
+static float ootf12_i(float x) { return x < 0.0f ? x : powf(x, 1.0f / 1.2f); }
+static float thlg_eotf(float x) { return ootf12(thlg_ioetf(x)); }
+static float thlg_ieotf(float x) { return thlg_oetf(ootf12_i(x)); }
+static float tpq_oetf(float x) { return tpq_ieotf(t1886(t709_oetf(x * O_PQ_OOTF)) / 100.0f); }
+static float tpq_ioetf(float x) { return t709_ioetf(t1886_i(tpq_eotf(x) * 100.0f)) / O_PQ_OOTF; }
+
+typedef float (*orc_tf)(float);
+typedef struct { orc_tf to_linear, to_gamma; float to_linear_scale, to_gamma_scale; } orc_transfer;
+
+/* select_transfer_function (gamma.cpp:346-411) */
+static orc_transfer orc_select_transfer(int t, double peak, int scene)
+{
+	orc_transfer f = { 0, 0, 1.0f, 1.0f };
+	switch (t) {
+	case TC_LOG100: f.to_linear = tlog100_i; f.to_gamma = tlog100; break;
+	case TC_LOG316: f.to_linear = tlog316_i; f.to_gamma = tlog316; break;
+	case TC_709: f.to_linear = scene ? t709_ioetf : t1886; f.to_gamma = scene ? t709_oetf : t1886_i; break;
+	case TC_470M: f.to_linear = t470m; f.to_gamma = t470m_i; break;
+	case TC_470BG: f.to_linear = t470bg; f.to_gamma = t470bg_i; break;
+	case TC_240M: f.to_linear = scene ? t240_ioetf : t1886; f.to_gamma = scene ? t240_oetf : t1886_i; break;
+	case TC_1361: f.to_linear = scene ? t1361_ioetf : t1361_eotf; f.to_gamma = scene ? t1361_oetf : t1361_ieotf; break;
+	case TC_XVYCC: f.to_linear = scene ? txvycc_ioetf : txvycc_eotf; f.to_gamma = scene ? txvycc_oetf : txvycc_ieotf; break;
+	case TC_SRGB: f.to_linear = tsrgb; f.to_gamma = tsrgb_i; break;
+	case TC_2084:
+		f.to_linear = scene ? tpq_ioetf : tpq_eotf;
+		f.to_gamma = scene ? tpq_oetf : tpq_ieotf;
+		f.to_linear_scale = (float)(10000.0f / peak);
+		f.to_gamma_scale = (float)(peak / 10000.0f);
+		break;
+	case TC_428: f.to_linear = t428; f.to_gamma = t428_i; break;
+	case TC_B67:
+		f.to_linear = scene ? thlg_ioetf : thlg_eotf;
+		f.to_gamma = scene ? thlg_oetf : thlg_ieotf;
+		f.to_linear_scale = scene ? 12.0f : (float)(1000.0 / peak);
+		f.to_gamma_scale = scene ? 1.0f / 12.0f : (float)(peak / 1000.0);
+		break;
+	default: break;
+	}
+	return f;
+}
+
+/* ---- 3x3 algebra in double (matrix3.cpp) ---- */
+static orc_m3 m3_mul(orc_m3 a, orc_m3 b)
+{
+	orc_m3 r;
+	for (int i = 0; i < 3; ++i)
+		for (int j = 0; j < 3; ++j) {
+			double acc = 0;
+			for (int k = 0; k < 3; ++k)
+				acc += a.v[i][k] * b.v[k][j];
+			r.v[i][j] = acc;
+		}
+	return r;
+}
+static orc_v3 m3_apply(orc_m3 m, orc_v3 x)
+{
+	orc_v3 r;
+	for (int i = 0; i < 3; ++i) {
+		double acc = 0;
+		for (int k = 0; k < 3; ++k)
+			acc += m.v[i][k] * x.v[k];
+		r.v[i] = acc;
+	}
+	return r;
+}
+static double det2(double a, double b, double c, double d) { return a * d - b * c; }
+static orc_m3 m3_inverse(orc_m3 m)
+{
+	const double (*a)[3] = m.v;
+	double det = 0;
+	det += a[0][0] * det2(a[1][1], a[1][2], a[2][1], a[2][2]);
+	det -= a[0][1] * det2(a[1][0], a[1][2], a[2][0], a[2][2]);
+	det += a[0][2] * det2(a[1][0], a[1][1], a[2][0], a[2][1]);
+	orc_m3 r;
+	r.v[0][0] = det2(a[1][1], a[1][2], a[2][1], a[2][2]) / det;
+	r.v[0][1] = det2(a[0][2], a[0][1], a[2][2], a[2][1]) / det;
+	r.v[0][2] = det2(a[0][1], a[0][2], a[1][1], a[1][2]) / det;
+	r.v[1][0] = det2(a[1][2], a[1][0], a[2][2], a[2][0]) / det;
+	r.v[1][1] = det2(a[0][0], a[0][2], a[2][0], a[2][2]) / det;
+	r.v[1][2] = det2(a[0][2], a[0][0], a[1][2], a[1][0]) / det;
+	r.v[2][0] = det2(a[1][0], a[1][1], a[2][0], a[2][1]) / det;
+	r.v[2][1] = det2(a[0][1], a[0][0], a[2][1], a[2][0]) / det;
+	r.v[2][2] = det2(a[0][0], a[0][1], a[1][0], a[1][1]) / det;
+	return r;
+}
+static orc_m3 m3_identity(void)
+{
+	orc_m3 r = { { { 1, 0, 0 }, { 0, 1, 0 }, { 0, 0, 1 } } };
+	return r;
+}
+static orc_v3 xy_to_xyz(double x, double y)
+{
+	orc_v3 r = { { x / y, 1.0, (1.0 - x - y) / y } };
+	return r;
+}
+static orc_v3 v3_cross(orc_v3 a, orc_v3 b)
+{
+	orc_v3 r = { { a.v[1] * b.v[2] - a.v[2] * b.v[1], a.v[2] * b.v[0] - a.v[0] * b.v[2], a.v[0] * b.v[1] - a.v[1] * b.v[0] } };
+	return r;
+}
+static double v3_dot(orc_v3 a, orc_v3 b) { return a.v[0] * b.v[0] + a.v[1] * b.v[1] + a.v[2] * b.v[2]; }
+
+/* ---- colorimetry (colorspace_param.cpp/.h): published constants ---- */
+static void yuv_kr_kb(int m, double *kr, double *kb)
+{
+	switch (m) {
+	case CM_FCC: *kr = 0.3; *kb = 0.11; break;
+	case CM_240M: *kr = 0.212; *kb = 0.087; break;
+	case CM_601: *kr = 0.299; *kb = 0.114; break;
+	case CM_709: *kr = 0.2126; *kb = 0.0722; break;
+	case CM_2020_NCL: case CM_2020_CL: *kr = 0.2627; *kb = 0.0593; break;
+	default: *kr = 0; *kb = 0; break;
+	}
+}
+static orc_v3 white_point(int p)
+{
+	switch (p) {
+	case CP_470M: case CP_FILM: return xy_to_xyz(0.31, 0.316);                 /* illuminant C */
+	case CP_XYZ: return xy_to_xyz(1.0 / 3.0, 1.0 / 3.0);                        /* illuminant E */
+	case CP_DCI_P3: return xy_to_xyz(0.314, 0.351);                             /* DCI white */
+	default: return xy_to_xyz(0.3127, 0.3290);                                  /* D65 */
+	}
+}
+static void primaries_xy(int p, double o[3][2])
+{
+	static const double t470m[3][2] = { { 0.670, 0.330 }, { 0.210, 0.710 }, { 0.140, 0.080 } };
+	static const double t470bg[3][2] = { { 0.640, 0.330 }, { 0.290, 0.600 }, { 0.150, 0.060 } };
+	static const double smptec[3][2] = { { 0.630, 0.340 }, { 0.310, 0.595 }, { 0.155, 0.070 } };
+	static const double r709[3][2] = { { 0.640, 0.330 }, { 0.300, 0.600 }, { 0.150, 0.060 } };
+	static const double film[3][2] = { { 0.681, 0.319 }, { 0.243, 0.692 }, { 0.145, 0.049 } };
+	static const double r2020[3][2] = { { 0.708, 0.292 }, { 0.170, 0.797 }, { 0.131, 0.046 } };
+	static const double p3[3][2] = { { 0.680, 0.320 }, { 0.265, 0.690 }, { 0.150, 0.060 } };
+	static const double ebu[3][2] = { { 0.630, 0.340 }, { 0.295, 0.605 }, { 0.155, 0.077 } };
+	const double (*s)[2] = r709;
+	switch (p) {
+	case CP_470M: s = t470m; break;
+	case CP_470BG: s = t470bg; break;
+	case CP_SMPTE_C: s = smptec; break;
+	case CP_FILM: s = film; break;
+	case CP_2020: s = r2020; break;
+	case CP_DCI_P3: case CP_DCI_P3_D65: s = p3; break;
+	case CP_EBU_3213_E: s = ebu; break;
+	default: break;
+	}
+	memcpy(o, s, sizeof(r709));
+}
+static orc_m3 rgb_to_yuv_kr_kb(double kr, double kb)
+{
+	const double kg = 1.0 - kr - kb, us = 1.0 / (2.0 - 2.0 * kb), vs = 1.0 / (2.0 - 2.0 * kr);
+	orc_m3 r = { { { kr, kg, kb }, { -kr * us, -kg * us, (1.0 - kb) * us }, { (1.0 - kr) * vs, -kg * vs, -kb * vs } } };
+	return r;
+}
+static orc_m3 ncl_rgb_to_yuv(int m)
+{
+	if (m == CM_YCGCO) {
+		orc_m3 r = { { { 0.25, 0.5, 0.25 }, { -0.25, 0.5, -0.25 }, { 0.5, 0, -0.5 } } };
+		return r;
+	}
+	if (m == CM_LMS) {
+		orc_m3 r = { { { 1688.0 / 4096.0, 2146.0 / 4096.0, 262.0 / 4096.0 },
+		               { 683.0 / 4096.0, 2951.0 / 4096.0, 462.0 / 4096.0 },
+		               { 99.0 / 4096.0, 309.0 / 4096.0, 3688.0 / 4096.0 } } };
+		return r;
+	}
+	double kr, kb;
+	yuv_kr_kb(m, &kr, &kb);
+	return rgb_to_yuv_kr_kb(kr, kb);
+}
+/* ITU-T H.273 E-22..E-27 */
+static void kr_kb_from_primaries(int p, double *kr, double *kb)
+{
+	double xy[3][2];
+	primaries_xy(p, xy);
+	const orc_v3 r = xy_to_xyz(xy[0][0], xy[0][1]), g = xy_to_xyz(xy[1][0], xy[1][1]), b = xy_to_xyz(xy[2][0], xy[2][1]);
+	const orc_v3 w = white_point(p);
+	const orc_v3 xr = { { r.v[0], g.v[0], b.v[0] } }, yr = { { r.v[1], g.v[1], b.v[1] } }, zr = { { r.v[2], g.v[2], b.v[2] } };
+	const double den = v3_dot(xr, v3_cross(yr, zr));
+	*kr = v3_dot(w, v3_cross(g, b)) / den;
+	*kb = v3_dot(w, v3_cross(r, g)) / den;
+}
+static orc_m3 ncl_rgb_to_yuv_from_primaries(int p)
+{
+	if (p == CP_709)
+		return ncl_rgb_to_yuv(CM_709);
+	if (p == CP_2020)
+		return ncl_rgb_to_yuv(CM_2020_NCL);
+	double kr, kb;
+	kr_kb_from_primaries(p, &kr, &kb);
+	return rgb_to_yuv_kr_kb(kr, kb);
+}
+static orc_m3 lms_to_ictcp(int t)
+{
+	if (t == TC_B67) {
+		orc_m3 r = { { { 0.5, 0.5, 0.0 }, { 3625.0 / 4096.0, -7465.0 / 4096.0, 3840.0 / 4096.0 },
+		               { 9500.0 / 4096.0, -9212.0 / 4096.0, -288.0 / 4096.0 } } };
+		return r;
+	}
+	orc_m3 r = { { { 0.5, 0.5, 0.0 }, { 6610.0 / 4096.0, -13613.0 / 4096.0, 7003.0 / 4096.0 },
+	               { 17933.0 / 4096.0, -17390.0 / 4096.0, -543.0 / 4096.0 } } };
+	return r;
+}
+static orc_m3 rgb_to_xyz(int p)
+{
+	if (p == CP_XYZ)
+		return m3_identity();
+	double xy[3][2];
+	primaries_xy(p, xy);
+	orc_m3 cols;  /* rows X, Y, Z; columns R, G, B */
+	for (int c = 0; c < 3; ++c) {
+		const orc_v3 v = xy_to_xyz(xy[c][0], xy[c][1]);
+		for (int r = 0; r < 3; ++r)
+			cols.v[r][c] = v.v[r];
+	}
+	const orc_v3 s = m3_apply(m3_inverse(cols), white_point(p));
+	orc_m3 m;
+	for (int r = 0; r < 3; ++r)
+		for (int c = 0; c < 3; ++c)
+			m.v[r][c] = cols.v[r][c] * s.v[c];
+	return m;
+}
+static orc_m3 xyz_to_rgb(int p)
+{
+	if (p == CP_XYZ)
+		return m3_identity();
+	return m3_inverse(rgb_to_xyz(p));
+}
+/* Bradford adaptation (http://www.brucelindbloom.com, Eqn_ChromAdapt) */
+static orc_m3 white_adapt(int in, int out)
+{
+	const orc_m3 br = { { { 0.8951, 0.2664, -0.1614 }, { -0.7502, 1.7135, 0.0367 }, { 0.0389, -0.0685, 1.0296 } } };
+	const orc_v3 wi = white_point(in), wo = white_point(out);
+	if (wi.v[0] == wo.v[0] && wi.v[1] == wo.v[1] && wi.v[2] == wo.v[2])
+		return m3_identity();
+	const orc_v3 ri = m3_apply(br, wi), ro = m3_apply(br, wo);
+	orc_m3 d = { { { 0 } } };
+	for (int k = 0; k < 3; ++k)
+		d.v[k][k] = ro.v[k] / ri.v[k];
+	return m3_mul(m3_mul(m3_inverse(br), d), br);
+}
+
+/* ---- the path between two colorspaces (colorspace_graph.cpp) ---- */
+enum { E_NCL_YUV2RGB, E_NCL_RGB2YUV, E_ICTCP2LMS, E_LMS2ICTCP, E_G2L, E_L2G, E_CL_YUV2RGB, E_CL_RGB2YUV, E_GAMUT };
+
+static int csp_key(orc_csp c) { return (c.m * TC_COUNT + c.t) * CP_COUNT + c.p; }
+static int csp_eq(orc_csp a, orc_csp b) { return a.m == b.m && a.t == b.t && a.p == b.p; }
+
+static int csp_valid(orc_csp c)
+{
+	if (c.m == CM_2020_CL && c.t != TC_709)
+		return 0;
+	if ((c.m == CM_CHROM_NCL || c.m == CM_CHROM_CL) && c.p == CP_UNSPEC)
+		return 0;
+	if (c.m == CM_ICTCP && !((c.t == TC_2084 || c.t == TC_B67) && c.p == CP_2020))
+		return 0;
+	if (c.m == CM_LMS && !((c.t == TC_LINEAR || c.t == TC_2084 || c.t == TC_B67) && c.p == CP_2020))
+		return 0;
+	return 1;
+}
+
+typedef struct { orc_csp to; int edge; } orc_edge;
+
+static int neighbours(orc_csp c, orc_edge *e)
+{
+	int n = 0;
+#define ADD(M, T, P, E) do { e[n].to.m = (M); e[n].to.t = (T); e[n].to.p = (P); e[n].edge = (E); ++n; } while (0)
+	if (c.m == CM_RGB) {
+		for (int m = 0; m < CM_COUNT; ++m) {
+			if (m == CM_UNSPEC || m == CM_RGB || m == CM_2020_CL || m == CM_CHROM_NCL || m == CM_CHROM_CL || m == CM_LMS ||
+			    m == CM_ICTCP)
+				continue;
+			ADD(m, c.t, c.p, E_NCL_RGB2YUV);
+		}
+		if (c.p != CP_UNSPEC)
+			ADD(CM_CHROM_NCL, c.t, c.p, E_NCL_RGB2YUV);
+		if (c.t == TC_LINEAR) {
+			for (int t = 0; t < TC_COUNT; ++t) {
+				if (t == c.t || t == TC_UNSPEC)
+					continue;
+				ADD(c.m, t, c.p, E_L2G);
+				if (c.p != CP_UNSPEC)
+					ADD(CM_CHROM_CL, t, c.p, E_CL_RGB2YUV);
+			}
+			if (c.p != CP_UNSPEC)
+				for (int p = 0; p < CP_COUNT; ++p)
+					if (p != c.p && p != CP_UNSPEC)
+						ADD(c.m, c.t, p, E_GAMUT);
+			ADD(CM_2020_CL, TC_709, c.p, E_CL_RGB2YUV);
+			if (c.p == CP_2020)
+				ADD(CM_LMS, c.t, c.p, E_NCL_RGB2YUV);
+		} else if (c.t != TC_UNSPEC) {
+			ADD(c.m, TC_LINEAR, c.p, E_G2L);
+		}
+	} else if (c.m == CM_2020_CL || c.m == CM_CHROM_CL) {
+		ADD(CM_RGB, TC_LINEAR, c.p, E_CL_YUV2RGB);
+	} else if (c.m == CM_LMS) {
+		if (c.t == TC_2084 || c.t == TC_B67) {
+			ADD(CM_ICTCP, c.t, c.p, E_LMS2ICTCP);
+			ADD(c.m, TC_LINEAR, c.p, E_G2L);
+		}
+		if (c.t == TC_LINEAR) {
+			ADD(CM_RGB, c.t, c.p, E_NCL_YUV2RGB);
+			ADD(c.m, TC_2084, c.p, E_L2G);
+			ADD(c.m, TC_B67, c.p, E_L2G);
+		}
+	} else if (c.m == CM_ICTCP) {
+		if (c.t == TC_2084 || c.t == TC_B67)
+			ADD(CM_LMS, c.t, c.p, E_ICTCP2LMS);
+	} else if (c.m != CM_UNSPEC) {
+		ADD(CM_RGB, c.t, c.p, E_NCL_YUV2RGB);
+	}
+#undef ADD
+	return n;
+}
+
+/* Breadth-first search from in to out; returns the number of edges (at most
+ * 6 used by zimg) written to steps[]/froms[], or -1 if there is no path. */
+static int csp_path(orc_csp in, orc_csp out, int *edges, orc_csp *froms, int max)
+{
+	enum { NKEY = CM_COUNT * TC_COUNT * CP_COUNT };
+	char *visited = calloc(NKEY, 1);
+	int *parent = malloc(sizeof(int) * NKEY), *pedge = malloc(sizeof(int) * NKEY);
+	orc_csp *queue = malloc(sizeof(orc_csp) * NKEY);
+	int head = 0, tail = 0, found = 0;
+	orc_csp v = in;
+	visited[csp_key(in)] = 1;
+	queue[tail++] = in;
+	while (head < tail) {
+		v = queue[head++];
+		if (csp_eq(v, out)) {
+			found = 1;
+			break;
+		}
+		orc_edge e[64];
+		const int n = neighbours(v, e);
+		for (int k = 0; k < n; ++k) {
+			const int key = csp_key(e[k].to);
+			if (visited[key])
+				continue;
+			visited[key] = 1;
+			queue[tail++] = e[k].to;
+			parent[key] = csp_key(v);
+			pedge[key] = e[k].edge;
+		}
+	}
+	int len = -1;
+	if (found) {
+		int rev_e[64], rev_k[64], cnt = 0, key = csp_key(out);
+		while (key != csp_key(in) && cnt < 64) {
+			rev_e[cnt] = pedge[key];
+			rev_k[cnt] = parent[key];
+			key = parent[key];
+			++cnt;
+		}
+		if (cnt <= max) {
+			for (int k = 0; k < cnt; ++k) {
+				edges[k] = rev_e[cnt - 1 - k];
+				const int fk = rev_k[cnt - 1 - k];
+				froms[k].p = fk % CP_COUNT;
+				froms[k].t = (fk / CP_COUNT) % TC_COUNT;
+				froms[k].m = fk / (CP_COUNT * TC_COUNT);
+			}
+			len = cnt;
+		}
+	}
+	free(visited);
+	free(parent);
+	free(pedge);
+	free(queue);
+	return len;
+}
+
+/* ---- operations (operation.cpp, operation_impl.cpp C classes) ---- */
+enum { OP_MATRIX, OP_GAMMA, OP_HLG, OP_HLG_INV, OP_CL2RGB, OP_CL2YUV };
+typedef struct {
+	int kind;
+	float m[3][3];
+	orc_tf f, g;       /* GAMMA: f; CL2RGB: f to linear; CL2YUV: f to gamma */
+	float pre, post;   /* GAMMA */
+	float kr, kg, kb, scale, nb, pb, nr, pr;
+} orc_op;
+
+struct orc_colorspace {
+	int nops;
+	orc_op ops[6];
+};
+
+static orc_op op_matrix(orc_m3 m)
+{
+	orc_op o;
+	memset(&o, 0, sizeof(o));
+	o.kind = OP_MATRIX;
+	for (int i = 0; i < 3; ++i)
+		for (int j = 0; j < 3; ++j)
+			o.m[i][j] = (float)m.v[i][j];
+	return o;
+}
+
+static orc_op make_op(int edge, orc_csp in, orc_csp out, double peak, int approx, int scene, int adapt)
+{
+	orc_op o;
+	memset(&o, 0, sizeof(o));
+	const int b67_display_in = in.p != CP_UNSPEC && !approx && !scene;
+	const int b67_display_out = out.p != CP_UNSPEC && !approx && !scene;
+	switch (edge) {
+	case E_NCL_YUV2RGB:
+		return op_matrix(m3_inverse(in.m == CM_CHROM_NCL ? ncl_rgb_to_yuv_from_primaries(in.p) : ncl_rgb_to_yuv(in.m)));
+	case E_NCL_RGB2YUV:
+		return op_matrix(out.m == CM_CHROM_NCL ? ncl_rgb_to_yuv_from_primaries(out.p) : ncl_rgb_to_yuv(out.m));
+	case E_ICTCP2LMS: return op_matrix(m3_inverse(lms_to_ictcp(in.t)));
+	case E_LMS2ICTCP: return op_matrix(lms_to_ictcp(in.t));
+	case E_G2L:
+		if (in.t == TC_B67 && b67_display_in) {
+			const orc_m3 m = ncl_rgb_to_yuv_from_primaries(in.p);
+			o.kind = OP_HLG_INV;
+			o.kr = (float)m.v[0][0]; o.kg = (float)m.v[0][1]; o.kb = (float)m.v[0][2];
+			o.scale = orc_select_transfer(TC_B67, peak, 0).to_linear_scale;
+		} else {
+			const orc_transfer f = orc_select_transfer(in.t, peak, scene);
+			o.kind = OP_GAMMA; o.f = f.to_linear; o.pre = 1.0f; o.post = f.to_linear_scale;
+		}
+		return o;
+	case E_L2G:
+		if (out.t == TC_B67 && b67_display_out) {
+			const orc_m3 m = ncl_rgb_to_yuv_from_primaries(out.p);
+			o.kind = OP_HLG;
+			o.kr = (float)m.v[0][0]; o.kg = (float)m.v[0][1]; o.kb = (float)m.v[0][2];
+			o.scale = orc_select_transfer(TC_B67, peak, 0).to_gamma_scale;
+		} else {
+			const orc_transfer f = orc_select_transfer(out.t, peak, scene);
+			o.kind = OP_GAMMA; o.f = f.to_gamma; o.pre = f.to_gamma_scale; o.post = 1.0f;
+		}
+		return o;
+	case E_GAMUT: {
+		orc_m3 m = adapt ? m3_mul(m3_mul(xyz_to_rgb(out.p), white_adapt(in.p, out.p)), rgb_to_xyz(in.p))
+		                 : m3_mul(xyz_to_rgb(out.p), rgb_to_xyz(in.p));
+		return op_matrix(m);
+	}
+	case E_CL_YUV2RGB: {
+		const orc_transfer f = orc_select_transfer(in.t, peak, 1);
+		const orc_m3 m = in.m == CM_CHROM_CL ? ncl_rgb_to_yuv_from_primaries(in.p) : ncl_rgb_to_yuv(in.m);
+		o.kind = OP_CL2RGB; o.f = f.to_linear; o.g = f.to_gamma;
+		o.kr = (float)m.v[0][0]; o.kg = (float)m.v[0][1]; o.kb = (float)m.v[0][2];
+		o.scale = f.to_linear_scale;
+		o.nb = f.to_gamma(1.0f - (float)m.v[0][2]);
+		o.pb = 1.0f - f.to_gamma((float)m.v[0][2]);
+		o.nr = f.to_gamma(1.0f - (float)m.v[0][0]);
+		o.pr = 1.0f - f.to_gamma((float)m.v[0][0]);
+		return o;
+	}
+	case E_CL_RGB2YUV: {
+		const orc_transfer f = orc_select_transfer(out.t, peak, 1);
+		const orc_m3 m = out.m == CM_CHROM_CL ? ncl_rgb_to_yuv_from_primaries(out.p) : ncl_rgb_to_yuv(out.m);
+		o.kind = OP_CL2YUV; o.f = f.to_gamma;
+		o.kr = (float)m.v[0][0]; o.kg = (float)m.v[0][1]; o.kb = (float)m.v[0][2];
+		o.scale = f.to_gamma_scale;
+		o.nb = f.to_gamma(1.0f - (float)m.v[0][2]);
+		o.pb = 1.0f - f.to_gamma((float)m.v[0][2]);
+		o.nr = f.to_gamma(1.0f - (float)m.v[0][0]);
+		o.pr = 1.0f - f.to_gamma((float)m.v[0][0]);
+		return o;
+	}
+	default: return o;
+	}
+}
+
+/* ColorspaceConversion::create (colorspace.cpp:94-121): SMPTE 240M transfer
+ * read as BT.709 unless scene-referred; no operations when the effective
+ * colorspaces are equal. Arguments are zimg's internal enum values. Returns
+ * NULL with *err set (-1 invalid colorspace or no path, -2 no memory). */
+struct orc_colorspace *orc_colorspace_create(int m_in, int t_in, int p_in, int m_out, int t_out, int p_out,
+                                             double peak, int approx, int scene, int adapt, int *err)
+{
+	*err = 0;
+	orc_csp in = { m_in, t_in, p_in }, out = { m_out, t_out, p_out };
+	if (!scene) {
+		if (in.t == TC_240M)
+			in.t = TC_709;
+		if (out.t == TC_240M)
+			out.t = TC_709;
+	}
+	struct orc_colorspace *c = calloc(1, sizeof(*c));
+	if (!c) {
+		*err = -2;
+		return NULL;
+	}
+	if (csp_eq(in, out))
+		return c;
+	if (!csp_valid(in) || !csp_valid(out)) {
+		free(c);
+		*err = -1;
+		return NULL;
+	}
+	int edges[6];
+	orc_csp froms[6];
+	const int n = csp_path(in, out, edges, froms, 6);
+	if (n < 0) {
+		free(c);
+		*err = -1;
+		return NULL;
+	}
+	for (int k = 0; k < n; ++k) {
+		const orc_csp to = k + 1 < n ? froms[k + 1] : out;
+		c->ops[k] = make_op(edges[k], froms[k], to, peak, approx, scene, adapt);
+	}
+	c->nops = n;
+	return c;
+}
+
+void orc_colorspace_free(struct orc_colorspace *c)
+{
+	free(c);
+}
+
+int orc_colorspace_num_ops(const struct orc_colorspace *c)
+{
+	return c->nops;
+}
+
+/* Kind of operation k (OP_* order: matrix, gamma, HLG, inverse HLG, CL to
+ * RGB, CL to YUV), and its float matrix when it has one. */
+int orc_colorspace_op(const struct orc_colorspace *c, int k, float *m9)
+{
+	if (k < 0 || k >= c->nops)
+		return -1;
+	if (m9)
+		memcpy(m9, c->ops[k].m, sizeof(c->ops[k].m));
+	return c->ops[k].kind;
+}
+
+static void apply_op(const orc_op *o, float *a, float *b, float *c)
+{
+	switch (o->kind) {
+	case OP_MATRIX: {
+		const float x = o->m[0][0] * *a + o->m[0][1] * *b + o->m[0][2] * *c;
+		const float y = o->m[1][0] * *a + o->m[1][1] * *b + o->m[1][2] * *c;
+		const float z = o->m[2][0] * *a + o->m[2][1] * *b + o->m[2][2] * *c;
+		*a = x; *b = y; *c = z;
+		break;
+	}
+	case OP_GAMMA:
+		*a = o->post * o->f(*a * o->pre);
+		*b = o->post * o->f(*b * o->pre);
+		*c = o->post * o->f(*c * o->pre);
+		break;
+	case OP_HLG: {
+		const float gamma = 1.2f;
+		float r = *a * o->scale, g = *b * o->scale, bb = *c * o->scale;
+		float yd = o->kr * r + o->kg * g + o->kb * bb;
+		yd = yd < FLT_MIN ? FLT_MIN : yd;
+		const float ys_inv = powf(yd, (1.0f - gamma) / gamma);
+		*a = thlg_oetf(r * ys_inv);
+		*b = thlg_oetf(g * ys_inv);
+		*c = thlg_oetf(bb * ys_inv);
+		break;
+	}
+	case OP_HLG_INV: {
+		const float gamma = 1.2f;
+		float r = thlg_ioetf(*a), g = thlg_ioetf(*b), bb = thlg_ioetf(*c);
+		float ys = o->kr * r + o->kg * g + o->kb * bb;
+		ys = ys < FLT_MIN ? FLT_MIN : ys;
+		ys = powf(ys, gamma - 1.0f);
+		r = r * ys; g = g * ys; bb = bb * ys;
+		*a = r * o->scale; *b = g * o->scale; *c = bb * o->scale;
+		break;
+	}
+	case OP_CL2RGB: {
+		const float y = *a, u = *b, v = *c;
+		const float bmy = u < 0 ? u * 2.0f * o->nb : u * 2.0f * o->pb;
+		const float rmy = v < 0 ? v * 2.0f * o->nr : v * 2.0f * o->pr;
+		const float bb = o->f(bmy + y), r = o->f(rmy + y), yl = o->f(y);
+		const float g = (yl - o->kr * r - o->kb * bb) / o->kg;
+		*a = r * o->scale; *b = g * o->scale; *c = bb * o->scale;
+		break;
+	}
+	case OP_CL2YUV: {
+		float r = *a * o->scale, g = *b * o->scale, bb = *c * o->scale;
+		const float y = o->f(o->kr * r + o->kg * g + o->kb * bb);
+		bb = o->f(bb);
+		r = o->f(r);
+		const float u = (bb - y < 0.0f) ? (bb - y) / (2.0f * o->nb) : (bb - y) / (2.0f * o->pb);
+		const float v = (r - y < 0.0f) ? (r - y) / (2.0f * o->nr) : (r - y) / (2.0f * o->pr);
+		*a = y; *b = u; *c = v;
+		break;
+	}
+	default: break;
+	}
+}
+
+/* Three FLOAT planes (strides in bytes) through the conversion. */
+void orc_colorspace_run(const struct orc_colorspace *c, unsigned w, unsigned h, const void *const src[3],
+                        const ptrdiff_t src_stride[3], void *const dst[3], const ptrdiff_t dst_stride[3])
+{
+	for (unsigned i = 0; i < h; ++i) {
+		const float *s0 = (const float *)((const char *)src[0] + (ptrdiff_t)i * src_stride[0]);
+		const float *s1 = (const float *)((const char *)src[1] + (ptrdiff_t)i * src_stride[1]);
+		const float *s2 = (const float *)((const char *)src[2] + (ptrdiff_t)i * src_stride[2]);
+		float *d0 = (float *)((char *)dst[0] + (ptrdiff_t)i * dst_stride[0]);
+		float *d1 = (float *)((char *)dst[1] + (ptrdiff_t)i * dst_stride[1]);
+		float *d2 = (float *)((char *)dst[2] + (ptrdiff_t)i * dst_stride[2]);
+		for (unsigned j = 0; j < w; ++j) {
+			float a = s0[j], b = s1[j], cc = s2[j];
+			for (int k = 0; k < c->nops; ++k)
+				apply_op(&c->ops[k], &a, &b, &cc);
+			d0[j] = a;
+			d1[j] = b;
+			d2[j] = cc;
+		}
+	}
+}
