@@ -157,6 +157,48 @@ ZG_API zg_error_code zg_depth_get_info(const zg_depth *d, int *mode);
 ZG_API zg_error_code zg_depth_process(const zg_depth *d, const void *src, ptrdiff_t src_stride, void *dst,
                                       ptrdiff_t dst_stride, zg_stream stream);
 
+/* --------------------------------------------------------------- colorspace --
+ * Replaces zimg's ColorspaceConversion (src/zimg/colorspace/colorspace.h:
+ * 117-132, colorspace.cpp:94-121) and its filter's process: three FLOAT
+ * planes (Y'CbCr with centred chroma, R'G'B', linear RGB, ICtCp, ... as the
+ * colorspaces say) converted per pixel. Colorspaces are zimg's API codes
+ * (zimg_matrix_coefficients_e, zimg_transfer_characteristics_e,
+ * zimg_color_primaries_e, zimg.h:283-352), mapped as zimg.cpp:238-305 maps
+ * them: a code outside 0..255 returns ZG_ERROR_ENUM_OUT_OF_RANGE, a code
+ * zimg does not map, an invalid colorspace or a pair without a path
+ * ZG_ERROR_NO_COLORSPACE_CONVERSION. The operations are zimg's (path search
+ * colorspace_graph.cpp:197-245; matrices computed in double and rounded to
+ * float; transfer functions gamma.cpp). Matrix steps round like zimg's C
+ * path; transfer functions use CUDA's powf / logf / log10f / expf, whose
+ * results may differ from the C library's by a few units in the last place,
+ * so outputs agree with zimg's C path to within the error bound the tests
+ * state, not bit for bit. */
+typedef struct zg_colorspace_params {
+	unsigned width, height;
+	int matrix_in, transfer_in, primaries_in;
+	int matrix_out, transfer_out, primaries_out;
+	double peak_luminance;      /* cd/m^2 of SDR white for PQ / HLG; NaN: 100 */
+	int approximate_gamma;      /* as zimg: display-referred HLG then uses the per-channel curve */
+	int scene_referred;
+	int chromatic_adaptation;   /* Bradford white-point adaptation between primaries */
+} zg_colorspace_params;
+
+typedef struct zg_colorspace zg_colorspace;
+
+ZG_API zg_error_code zg_colorspace_create(const zg_colorspace_params *params, zg_colorspace **out);
+ZG_API void zg_colorspace_free(zg_colorspace *c);
+/* Number of per-pixel operations (0: the identity) and, when kinds is not
+ * NULL, their kinds in order into kinds[6]: 0 3x3 matrix, 1 transfer
+ * function, 2 HLG OOTF + OETF, 3 inverse HLG, 4 constant luminance to RGB,
+ * 5 RGB to constant luminance. */
+ZG_API zg_error_code zg_colorspace_get_info(const zg_colorspace *c, unsigned *num_ops, int *kinds);
+/* Convert the three planes src[0..2] into dst[0..2] (device pointers, strides
+ * in bytes; dst may equal src plane by plane). The identity copies when dst
+ * differs from src. Never allocates and never synchronises. */
+ZG_API zg_error_code zg_colorspace_process(const zg_colorspace *c, const void *const src[3],
+                                           const ptrdiff_t src_stride[3], void *const dst[3],
+                                           const ptrdiff_t dst_stride[3], zg_stream stream);
+
 /* ----------------------------------------------------------------- unresize --
  * Replaces zimg's UnresizeConversion (src/zimg/unresize/unresize.h:96-114,
  * unresize.cpp:34-91): the least-squares inverse of a bilinear upsampling of

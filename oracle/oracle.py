@@ -650,6 +650,7 @@ def _bind_colorspace(L):
     L.orc_colorspace_op.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_float)]
     L.orc_colorspace_run.argtypes = [C.c_void_p, C.c_uint, C.c_uint, C.POINTER(C.c_void_p), C.POINTER(C.c_ssize_t),
                                      C.POINTER(C.c_void_p), C.POINTER(C.c_ssize_t)]
+    L.orc_colorspace_run_f64.argtypes = L.orc_colorspace_run.argtypes
 
 
 def _planes_args(planes):
@@ -658,10 +659,13 @@ def _planes_args(planes):
     return ptrs, strides
 
 
-def _orc_colorspace(self, planes, csp_in, csp_out, peak=100.0, approximate=False, scene=False, adapt=False):
+def _orc_colorspace(self, planes, csp_in, csp_out, peak=100.0, approximate=False, scene=False, adapt=False,
+                    fp64=False):
     """zimg's ColorspaceConversion (C path) on three FLOAT planes. csp_in /
     csp_out: (matrix, transfer, primaries) API codes. Returns (planes, ops):
-    the converted planes and the names of the operations applied."""
+    the converted planes and the names of the operations applied. fp64: the
+    same operations with the same float parameters evaluated in double, into
+    float64 planes (the reference float evaluations are measured against)."""
     L = self.lib
     if not getattr(L, "_csp_bound", False):
         _bind_colorspace(L)
@@ -674,12 +678,14 @@ def _orc_colorspace(self, planes, csp_in, csp_out, peak=100.0, approximate=False
     try:
         ops = [CSP_OPS[L.orc_colorspace_op(h, k, None)] for k in range(L.orc_colorspace_num_ops(h))]
         src = [np.ascontiguousarray(p, dtype=np.float32) for p in planes]
-        out = [np.empty_like(src[0]) for _ in range(3)]
+        out = [np.empty(src[0].shape, np.float64 if fp64 else np.float32) for _ in range(3)]
         hh, ww = src[0].shape
         si, ss = _planes_args(src)
         di, ds = _planes_args(out)
-        L.orc_colorspace_run(h, ww, hh, si, ss, di, ds)
-        return (out if ops else src), ops
+        (L.orc_colorspace_run_f64 if fp64 else L.orc_colorspace_run)(h, ww, hh, si, ss, di, ds)
+        if not ops:
+            return ([p.astype(np.float64) for p in src] if fp64 else src), ops
+        return out, ops
     finally:
         L.orc_colorspace_free(h)
 

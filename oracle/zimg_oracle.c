@@ -1353,20 +1353,6 @@ typedef struct { double v[3]; } orc_v3;
 #define O_HLG_C 0.55991073f
 #define O_PQ_OOTF 59.49080238715383f
 
-static float fmaxz(float x) { return x < 0.0f ? 0.0f : x; }  /* std::max(x, 0.0f): a NaN stays */
-
-static float t709_oetf(float x) { x = fmaxz(x); return x < O_709_B ? x * 4.5f : O_709_A * powf(x, 0.45f) - (O_709_A - 1.0f); }
-static float t709_ioetf(float x) { x = fmaxz(x); return x < 4.5f * O_709_B ? x / 4.5f : powf((x + (O_709_A - 1.0f)) / O_709_A, 1.0f / 0.45f); }
-static float tlog100(float x) { return x <= 0.01f ? 0.0f : 1.0f + log10f(x) / 2.0f; }
-static float tlog100_i(float x) { return x <= 0.0f ? 0.01f : powf(10.0f, 2 * (x - 1.0f)); }
-static float tlog316(float x) { return x <= 0.00316227766f ? 0.0f : 1.0f + log10f(x) / 2.5f; }
-static float tlog316_i(float x) { return x <= 0.0f ? 0.00316227766f : powf(10.0f, 2.5f * (x - 1.0f)); }
-static float t470m(float x) { return x < 0.0f ? 0.0f : powf(x, 2.2f); }
-static float t470m_i(float x) { return x < 0.0f ? 0.0f : powf(x, 1.0f / 2.2f); }
-static float t470bg(float x) { return x < 0.0f ? 0.0f : powf(x, 2.8f); }
-static float t470bg_i(float x) { return x < 0.0f ? 0.0f : powf(x, 1.0f / 2.8f); }
-static float t240_oetf(float x) { x = fmaxz(x); return x < 4.0f * O_240_B ? x / 4.0f : powf((x + (O_240_A - 1.0f)) / O_240_A, 1.0f / 0.45f); }
-static float t240_ioetf(float x) { x = fmaxz(x); return x < O_240_B ? x * 4.0f : O_240_A * powf(x, 0.45f) - (O_240_A - 1.0f); }
 /* fabs / copysign on the bits: gcc 13's floating-point range propagation
  * drops the fabsf inside copysignf(f(fabsf(x)), x) at -O2 when the call is
  * reached under x < 0 */
@@ -1387,75 +1373,77 @@ static float copysign_bits(float mag, float sgn)
 	memcpy(&mag, &a, 4);
 	return mag;
 }
-static float txvycc_oetf(float x) { return copysign_bits(t709_oetf(abs_bits(x)), x); }
-static float txvycc_ioetf(float x) { return copysign_bits(t709_ioetf(abs_bits(x)), x); }
-static float t1361_oetf(float x) { return x >= 0.0f ? t709_oetf(x) : -t709_oetf(-x * 4.0f) / 4.0f; }
-static float t1361_ioetf(float x) { return x >= 0.0f ? t709_ioetf(x) : -t709_ioetf(-x * 4.0f) / 4.0f; }
-static float thlg_oetf(float x) { x = fmaxz(x); return x <= (1.0f / 12.0f) ? sqrtf(3.0f * x) : O_HLG_A * logf(12.0f * x - O_HLG_B) + O_HLG_C; }
-static float thlg_ioetf(float x) { x = fmaxz(x); return x <= 0.5f ? (x * x) * (1.0f / 3.0f) : (expf((x - O_HLG_C) / O_HLG_A) + O_HLG_B) / 12.0f; }
-static float t1886(float x) { return x < 0.0f ? 0.0f : powf(x, 2.4f); }
-static float t1886_i(float x) { return x < 0.0f ? 0.0f : powf(x, 1.0f / 2.4f); }
-static float tsrgb(float x) { x = fmaxz(x); return x < 12.92f * O_SRGB_B ? x / 12.92f : powf((x + (O_SRGB_A - 1.0f)) / O_SRGB_A, 2.4f); }
-static float tsrgb_i(float x) { x = fmaxz(x); return x < O_SRGB_B ? x * 12.92f : O_SRGB_A * powf(x, 1.0f / 2.4f) - (O_SRGB_A - 1.0f); }
-static float t1361_eotf(float x) { return (x < 0.0f || x > 1.0f) ? t1361_ioetf(x) : t1886(x); }
-static float t1361_ieotf(float x) { return (x < 0.0f || x > 1.0f) ? t1361_oetf(x) : t1886_i(x); }
-static float txvycc_eotf(float x) { return (x < 0.0f || x > 1.0f) ? txvycc_ioetf(x) : t1886(x); }
-static float txvycc_ieotf(float x) { return (x < 0.0f || x > 1.0f) ? txvycc_oetf(x) : t1886_i(x); }
-static float tpq_eotf(float x)
-{
-	if (!(x > 0.0f))
-		return 0.0f;
-	const float xp = powf(x, 1.0f / O_PQ_M2);
-	float num = xp - O_PQ_C1, den = O_PQ_C2 - O_PQ_C3 * xp;
-	num = num < 0.0f ? 0.0f : num;
-	den = den < FLT_MIN ? FLT_MIN : den;
-	return powf(num / den, 1.0f / O_PQ_M1);
-}
-static float tpq_ieotf(float x)
-{
-	if (!(x > 0.0f))
-		return 0.0f;
-	const float xp = powf(x, O_PQ_M1);
-	const float num = (O_PQ_C1 - 1.0f) + (O_PQ_C2 - O_PQ_C3) * xp;
-	const float den = 1.0f + O_PQ_C3 * xp;
-	return powf(1.0f + num / den, O_PQ_M2);
-}
-static float t428(float x) { return x < 0.0f ? 0.0f : 52.37f / 48.0f * powf(x, 2.6f); }
-static float t428_i(float x) { return x < 0.0f ? 0.0f : powf(x * (48.0f / 52.37f), 1.0f / 2.6f); }
-static float ootf12(float x) { return x < 0.0f ? x : powf(x, 1.2f); }
-static float ootf12_i(float x) { return x < 0.0f ? x : powf(x, 1.0f / 1.2f); }
-static float thlg_eotf(float x) { return ootf12(thlg_ioetf(x)); }
-static float thlg_ieotf(float x) { return thlg_oetf(ootf12_i(x)); }
-static float tpq_oetf(float x) { return tpq_ieotf(t1886(t709_oetf(x * O_PQ_OOTF)) / 100.0f); }
-static float tpq_ioetf(float x) { return t709_ioetf(t1886_i(tpq_eotf(x) * 100.0f)) / O_PQ_OOTF; }
+#define CSR float
+#define CSN(n) n
+#define CSPOW powf
+#define CSLOG logf
+#define CSLOG10 log10f
+#define CSEXP expf
+#define CSSQRT sqrtf
+#define CSABS abs_bits
+#define CSCOPYSIGN copysign_bits
+#include "colorspace_tf.inc"
+#undef CSR
+#undef CSN
+#undef CSPOW
+#undef CSLOG
+#undef CSLOG10
+#undef CSEXP
+#undef CSSQRT
+#undef CSABS
+#undef CSCOPYSIGN
+#define CSR double
+#define CSN(n) n##_d
+#define CSPOW pow
+#define CSLOG log
+#define CSLOG10 log10
+#define CSEXP exp
+#define CSSQRT sqrt
+#define CSABS fabs
+#define CSCOPYSIGN copysign
+#include "colorspace_tf.inc"
+#undef CSR
+#undef CSN
+#undef CSPOW
+#undef CSLOG
+#undef CSLOG10
+#undef CSEXP
+#undef CSSQRT
+#undef CSABS
+#undef CSCOPYSIGN
 
 typedef float (*orc_tf)(float);
-typedef struct { orc_tf to_linear, to_gamma; float to_linear_scale, to_gamma_scale; } orc_transfer;
+typedef double (*orc_tfd)(double);
+typedef struct {
+	orc_tf to_linear, to_gamma;
+	orc_tfd to_linear_d, to_gamma_d;  /* the same functions in FP64 */
+	float to_linear_scale, to_gamma_scale;
+} orc_transfer;
 
 /* select_transfer_function (gamma.cpp:346-411) */
 static orc_transfer orc_select_transfer(int t, double peak, int scene)
 {
-	orc_transfer f = { 0, 0, 1.0f, 1.0f };
+	orc_transfer f = { 0, 0, 0, 0, 1.0f, 1.0f };
 	switch (t) {
-	case TC_LOG100: f.to_linear = tlog100_i; f.to_gamma = tlog100; break;
-	case TC_LOG316: f.to_linear = tlog316_i; f.to_gamma = tlog316; break;
-	case TC_709: f.to_linear = scene ? t709_ioetf : t1886; f.to_gamma = scene ? t709_oetf : t1886_i; break;
-	case TC_470M: f.to_linear = t470m; f.to_gamma = t470m_i; break;
-	case TC_470BG: f.to_linear = t470bg; f.to_gamma = t470bg_i; break;
-	case TC_240M: f.to_linear = scene ? t240_ioetf : t1886; f.to_gamma = scene ? t240_oetf : t1886_i; break;
-	case TC_1361: f.to_linear = scene ? t1361_ioetf : t1361_eotf; f.to_gamma = scene ? t1361_oetf : t1361_ieotf; break;
-	case TC_XVYCC: f.to_linear = scene ? txvycc_ioetf : txvycc_eotf; f.to_gamma = scene ? txvycc_oetf : txvycc_ieotf; break;
-	case TC_SRGB: f.to_linear = tsrgb; f.to_gamma = tsrgb_i; break;
+	case TC_LOG100: f.to_linear = tlog100_i; f.to_linear_d = tlog100_i_d; f.to_gamma = tlog100; f.to_gamma_d = tlog100_d; break;
+	case TC_LOG316: f.to_linear = tlog316_i; f.to_linear_d = tlog316_i_d; f.to_gamma = tlog316; f.to_gamma_d = tlog316_d; break;
+	case TC_709: f.to_linear = scene ? t709_ioetf : t1886; f.to_linear_d = scene ? t709_ioetf_d : t1886_d; f.to_gamma = scene ? t709_oetf : t1886_i; f.to_gamma_d = scene ? t709_oetf_d : t1886_i_d; break;
+	case TC_470M: f.to_linear = t470m; f.to_linear_d = t470m_d; f.to_gamma = t470m_i; f.to_gamma_d = t470m_i_d; break;
+	case TC_470BG: f.to_linear = t470bg; f.to_linear_d = t470bg_d; f.to_gamma = t470bg_i; f.to_gamma_d = t470bg_i_d; break;
+	case TC_240M: f.to_linear = scene ? t240_ioetf : t1886; f.to_linear_d = scene ? t240_ioetf_d : t1886_d; f.to_gamma = scene ? t240_oetf : t1886_i; f.to_gamma_d = scene ? t240_oetf_d : t1886_i_d; break;
+	case TC_1361: f.to_linear = scene ? t1361_ioetf : t1361_eotf; f.to_linear_d = scene ? t1361_ioetf_d : t1361_eotf_d; f.to_gamma = scene ? t1361_oetf : t1361_ieotf; f.to_gamma_d = scene ? t1361_oetf_d : t1361_ieotf_d; break;
+	case TC_XVYCC: f.to_linear = scene ? txvycc_ioetf : txvycc_eotf; f.to_linear_d = scene ? txvycc_ioetf_d : txvycc_eotf_d; f.to_gamma = scene ? txvycc_oetf : txvycc_ieotf; f.to_gamma_d = scene ? txvycc_oetf_d : txvycc_ieotf_d; break;
+	case TC_SRGB: f.to_linear = tsrgb; f.to_linear_d = tsrgb_d; f.to_gamma = tsrgb_i; f.to_gamma_d = tsrgb_i_d; break;
 	case TC_2084:
-		f.to_linear = scene ? tpq_ioetf : tpq_eotf;
-		f.to_gamma = scene ? tpq_oetf : tpq_ieotf;
+		f.to_linear = scene ? tpq_ioetf : tpq_eotf; f.to_linear_d = scene ? tpq_ioetf_d : tpq_eotf_d;
+		f.to_gamma = scene ? tpq_oetf : tpq_ieotf; f.to_gamma_d = scene ? tpq_oetf_d : tpq_ieotf_d;
 		f.to_linear_scale = (float)(10000.0f / peak);
 		f.to_gamma_scale = (float)(peak / 10000.0f);
 		break;
-	case TC_428: f.to_linear = t428; f.to_gamma = t428_i; break;
+	case TC_428: f.to_linear = t428; f.to_linear_d = t428_d; f.to_gamma = t428_i; f.to_gamma_d = t428_i_d; break;
 	case TC_B67:
-		f.to_linear = scene ? thlg_ioetf : thlg_eotf;
-		f.to_gamma = scene ? thlg_oetf : thlg_ieotf;
+		f.to_linear = scene ? thlg_ioetf : thlg_eotf; f.to_linear_d = scene ? thlg_ioetf_d : thlg_eotf_d;
+		f.to_gamma = scene ? thlg_oetf : thlg_ieotf; f.to_gamma_d = scene ? thlg_oetf_d : thlg_ieotf_d;
 		f.to_linear_scale = scene ? 12.0f : (float)(1000.0 / peak);
 		f.to_gamma_scale = scene ? 1.0f / 12.0f : (float)(peak / 1000.0);
 		break;
@@ -1800,6 +1788,7 @@ typedef struct {
 	int kind;
 	float m[3][3];
 	orc_tf f, g;       /* GAMMA: f; CL2RGB: f to linear; CL2YUV: f to gamma */
+	orc_tfd fd;        /* f in FP64 */
 	float pre, post;   /* GAMMA */
 	float kr, kg, kb, scale, nb, pb, nr, pr;
 } orc_op;
@@ -1841,7 +1830,7 @@ static orc_op make_op(int edge, orc_csp in, orc_csp out, double peak, int approx
 			o.scale = orc_select_transfer(TC_B67, peak, 0).to_linear_scale;
 		} else {
 			const orc_transfer f = orc_select_transfer(in.t, peak, scene);
-			o.kind = OP_GAMMA; o.f = f.to_linear; o.pre = 1.0f; o.post = f.to_linear_scale;
+			o.kind = OP_GAMMA; o.f = f.to_linear; o.fd = f.to_linear_d; o.pre = 1.0f; o.post = f.to_linear_scale;
 		}
 		return o;
 	case E_L2G:
@@ -1852,7 +1841,7 @@ static orc_op make_op(int edge, orc_csp in, orc_csp out, double peak, int approx
 			o.scale = orc_select_transfer(TC_B67, peak, 0).to_gamma_scale;
 		} else {
 			const orc_transfer f = orc_select_transfer(out.t, peak, scene);
-			o.kind = OP_GAMMA; o.f = f.to_gamma; o.pre = f.to_gamma_scale; o.post = 1.0f;
+			o.kind = OP_GAMMA; o.f = f.to_gamma; o.fd = f.to_gamma_d; o.pre = f.to_gamma_scale; o.post = 1.0f;
 		}
 		return o;
 	case E_GAMUT: {
@@ -1863,7 +1852,7 @@ static orc_op make_op(int edge, orc_csp in, orc_csp out, double peak, int approx
 	case E_CL_YUV2RGB: {
 		const orc_transfer f = orc_select_transfer(in.t, peak, 1);
 		const orc_m3 m = in.m == CM_CHROM_CL ? ncl_rgb_to_yuv_from_primaries(in.p) : ncl_rgb_to_yuv(in.m);
-		o.kind = OP_CL2RGB; o.f = f.to_linear; o.g = f.to_gamma;
+		o.kind = OP_CL2RGB; o.f = f.to_linear; o.fd = f.to_linear_d; o.g = f.to_gamma;
 		o.kr = (float)m.v[0][0]; o.kg = (float)m.v[0][1]; o.kb = (float)m.v[0][2];
 		o.scale = f.to_linear_scale;
 		o.nb = f.to_gamma(1.0f - (float)m.v[0][2]);
@@ -1875,7 +1864,7 @@ static orc_op make_op(int edge, orc_csp in, orc_csp out, double peak, int approx
 	case E_CL_RGB2YUV: {
 		const orc_transfer f = orc_select_transfer(out.t, peak, 1);
 		const orc_m3 m = out.m == CM_CHROM_CL ? ncl_rgb_to_yuv_from_primaries(out.p) : ncl_rgb_to_yuv(out.m);
-		o.kind = OP_CL2YUV; o.f = f.to_gamma;
+		o.kind = OP_CL2YUV; o.f = f.to_gamma; o.fd = f.to_gamma_d;
 		o.kr = (float)m.v[0][0]; o.kg = (float)m.v[0][1]; o.kb = (float)m.v[0][2];
 		o.scale = f.to_gamma_scale;
 		o.nb = f.to_gamma(1.0f - (float)m.v[0][2]);
@@ -2008,6 +1997,84 @@ static void apply_op(const orc_op *o, float *a, float *b, float *c)
 		break;
 	}
 	default: break;
+	}
+}
+
+/* The same operation in FP64 with the same float parameters: the error of
+ * a float evaluation is measured against this. */
+static void apply_op_d(const orc_op *o, double *a, double *b, double *c)
+{
+	switch (o->kind) {
+	case OP_MATRIX: {
+		const double x = (double)o->m[0][0] * *a + (double)o->m[0][1] * *b + (double)o->m[0][2] * *c;
+		const double y = (double)o->m[1][0] * *a + (double)o->m[1][1] * *b + (double)o->m[1][2] * *c;
+		const double z = (double)o->m[2][0] * *a + (double)o->m[2][1] * *b + (double)o->m[2][2] * *c;
+		*a = x; *b = y; *c = z;
+		break;
+	}
+	case OP_GAMMA:
+		*a = o->post * o->fd(*a * o->pre);
+		*b = o->post * o->fd(*b * o->pre);
+		*c = o->post * o->fd(*c * o->pre);
+		break;
+	case OP_HLG: {
+		const double gamma = 1.2f;
+		double r = *a * o->scale, g = *b * o->scale, bb = *c * o->scale;
+		double yd = o->kr * r + o->kg * g + o->kb * bb;
+		yd = yd < FLT_MIN ? FLT_MIN : yd;
+		const double ys_inv = pow(yd, (double)((1.0f - 1.2f) / 1.2f));
+		(void)gamma;
+		*a = thlg_oetf_d(r * ys_inv);
+		*b = thlg_oetf_d(g * ys_inv);
+		*c = thlg_oetf_d(bb * ys_inv);
+		break;
+	}
+	case OP_HLG_INV: {
+		double r = thlg_ioetf_d(*a), g = thlg_ioetf_d(*b), bb = thlg_ioetf_d(*c);
+		double ys = o->kr * r + o->kg * g + o->kb * bb;
+		ys = ys < FLT_MIN ? FLT_MIN : ys;
+		ys = pow(ys, (double)(1.2f - 1.0f));
+		*a = r * ys * o->scale; *b = g * ys * o->scale; *c = bb * ys * o->scale;
+		break;
+	}
+	case OP_CL2RGB: {
+		const double y = *a, u = *b, v = *c;
+		const double bmy = u < 0 ? u * 2.0 * o->nb : u * 2.0 * o->pb;
+		const double rmy = v < 0 ? v * 2.0 * o->nr : v * 2.0 * o->pr;
+		const double bb = o->fd(bmy + y), r = o->fd(rmy + y), yl = o->fd(y);
+		const double g = (yl - o->kr * r - o->kb * bb) / o->kg;
+		*a = r * o->scale; *b = g * o->scale; *c = bb * o->scale;
+		break;
+	}
+	case OP_CL2YUV: {
+		double r = *a * o->scale, g = *b * o->scale, bb = *c * o->scale;
+		const double y = o->fd(o->kr * r + o->kg * g + o->kb * bb);
+		bb = o->fd(bb);
+		r = o->fd(r);
+		*a = y;
+		*b = (bb - y < 0.0) ? (bb - y) / (2.0 * o->nb) : (bb - y) / (2.0 * o->pb);
+		*c = (r - y < 0.0) ? (r - y) / (2.0 * o->nr) : (r - y) / (2.0 * o->pr);
+		break;
+	}
+	default: break;
+	}
+}
+
+/* Three FLOAT planes through the conversion evaluated in FP64, into three
+ * double planes (strides in bytes). */
+void orc_colorspace_run_f64(const struct orc_colorspace *c, unsigned w, unsigned h, const void *const src[3],
+                            const ptrdiff_t src_stride[3], void *const dst[3], const ptrdiff_t dst_stride[3])
+{
+	for (unsigned i = 0; i < h; ++i) {
+		for (unsigned j = 0; j < w; ++j) {
+			double v[3];
+			for (int p = 0; p < 3; ++p)
+				v[p] = ((const float *)((const char *)src[p] + (ptrdiff_t)i * src_stride[p]))[j];
+			for (int k = 0; k < c->nops; ++k)
+				apply_op_d(&c->ops[k], &v[0], &v[1], &v[2]);
+			for (int p = 0; p < 3; ++p)
+				((double *)((char *)dst[p] + (ptrdiff_t)i * dst_stride[p]))[j] = v[p];
+		}
 	}
 }
 

@@ -47,9 +47,9 @@ def test_struct_layouts_match_header(lib):
 #include <stddef.h>
 #include "zimg_gb300.h"
 int main(void) {
-  printf("%zu %zu %zu %zu %zu %zu %zu\n", sizeof(zg_pass_params), sizeof(zg_resize_params), sizeof(zg_batch_io),
+  printf("%zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(zg_pass_params), sizeof(zg_resize_params), sizeof(zg_batch_io),
          sizeof(zg_image_format), sizeof(zg_graph_builder_params), sizeof(zg_image_buffer),
-         offsetof(zg_image_format, active_region));
+         offsetof(zg_image_format, active_region), sizeof(zg_colorspace_params));
   return 0;
 }
 '''
@@ -61,7 +61,7 @@ int main(void) {
         got = [int(x) for x in subprocess.check_output([exe]).split()]
     want = [C.sizeof(capi.PassParams), C.sizeof(capi.ResizeParams), C.sizeof(capi.BatchIO),
             C.sizeof(capi.ImageFormat), C.sizeof(capi.GraphBuilderParams), C.sizeof(capi.ImageBuffer),
-            capi.ImageFormat.active_region.offset]
+            capi.ImageFormat.active_region.offset, C.sizeof(capi.ColorspaceParams)]
     assert got == want
 
 
@@ -127,6 +127,25 @@ def test_depth_create_errors(lib):
     p = capi.DepthParams(0, 32, capi.PixelFormat(1, 10, 0, 0, 0), capi.PixelFormat(0, 8, 0, 0, 0), 0, 0)
     h = C.c_void_p()
     assert lib.zg_depth_create(C.byref(p), C.byref(h)) == 2050  # INVALID_IMAGE_SIZE
+
+
+def test_colorspace_create_errors(lib):
+    """zg_colorspace_create maps zimg's API codes as zimg.cpp:114-123,238-305
+    does and finds zimg's paths, failing with zimg's codes before touching a
+    device."""
+    import ctypes as C
+    from zimg_gb300 import capi
+
+    def create(cin, cout):
+        p = capi.ColorspaceParams(16, 16, *cin, *cout, math.nan, 0, 0, 0)
+        h = C.c_void_p()
+        return lib.zg_colorspace_create(C.byref(p), C.byref(h))
+
+    assert create((1, 1, 1), (0, 300, 1)) == 2049   # outside 0..255: ENUM_OUT_OF_RANGE
+    assert create((11, 1, 1), (0, 1, 1)) == 3074    # ST 2085 YDZDX: not mapped, NO_COLORSPACE_CONVERSION
+    assert create((1, 1, 1), (2, 2, 2)) == 3074     # no path to an unspecified colorspace
+    assert create((10, 16, 9), (0, 1, 1)) == 3074   # BT.2020 CL needs BT.709 transfer (invalid)
+    assert create((14, 1, 9), (0, 1, 1)) == 3074    # ICtCp needs PQ or HLG
 
 
 def test_unresize_create_errors(lib):

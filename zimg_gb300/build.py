@@ -23,8 +23,14 @@ LIB = os.path.join(OUT_DIR, "libzimg_gb300.so")
 SOURCES = ["filter_plan.cpp", "capi.cu", "capi_graph.cu", "capi_batch.cu", "capi_static_tmp.cu",
            "pass_kernels.cu", "fused.cu", "fused_inst_v_f32.cu", "fused_inst_v_u16.cu", "fused_inst_h_f32.cu",
            "fused_inst_h_u16.cu", "mma.cu", "chain.cu", "chain_tma.cu", "wide_kernel.cu", "wide_umma.cu", "copy_kernel.cu",
-           "depth_kernel.cu", "ed_kernel.cu", "alpha_kernel.cu", "capi_depth.cu", "unresize_plan.cpp", "unresize_kernel.cu", "capi_unresize.cu"]
+           "depth_kernel.cu", "ed_kernel.cu", "alpha_kernel.cu", "capi_depth.cu", "colorspace_plan.cpp",
+           "colorspace_kernel.cu", "capi_colorspace.cu", "unresize_plan.cpp", "unresize_kernel.cu", "capi_unresize.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+# Per-file flags: the colorspace kernel rounds every product and sum on its
+# own, as zimg's C code does (no multiply-add contraction on the device).
+FILE_FLAGS = {"colorspace_kernel.cu": ["-fmad=false"]}
 
 
 def _nvcc() -> str:
@@ -54,10 +60,10 @@ def _compile(src: str, digest: str, verbose: bool) -> str:
     obj = os.path.join(OBJ_DIR, src + ".o")
     stamp = obj + ".stamp"
     with open(path, "rb") as fh:
-        key = hashlib.sha1(fh.read() + digest.encode() + " ".join(_flags()).encode()).hexdigest()
+        key = hashlib.sha1(fh.read() + digest.encode() + " ".join(_flags() + FILE_FLAGS.get(src, [])).encode()).hexdigest()
     if os.path.exists(obj) and os.path.exists(stamp) and open(stamp).read() == key:
         return obj
-    cmd = [_nvcc(), *_flags(), "-c", path, "-o", obj]
+    cmd = [_nvcc(), *_flags(), *FILE_FLAGS.get(src, []), "-c", path, "-o", obj]
     if src.endswith(".cu"):
         cmd.insert(1, "-Xptxas=-v" if verbose else "-Xptxas=-O3")
     res = subprocess.run(cmd, capture_output=True, text=True)

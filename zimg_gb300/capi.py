@@ -63,6 +63,13 @@ class DepthParams(C.Structure):
 DITHER = {"none": 0, "ordered": 1, "random": 2, "error_diffusion": 3}
 
 
+class ColorspaceParams(C.Structure):
+    _fields_ = [("width", C.c_uint), ("height", C.c_uint), ("matrix_in", C.c_int), ("transfer_in", C.c_int),
+                ("primaries_in", C.c_int), ("matrix_out", C.c_int), ("transfer_out", C.c_int),
+                ("primaries_out", C.c_int), ("peak_luminance", C.c_double), ("approximate_gamma", C.c_int),
+                ("scene_referred", C.c_int), ("chromatic_adaptation", C.c_int)]
+
+
 class UnresizeParams(C.Structure):
     _fields_ = [("up_width", C.c_uint), ("up_height", C.c_uint), ("orig_width", C.c_uint),
                 ("orig_height", C.c_uint), ("shift_w", C.c_double), ("shift_h", C.c_double)]
@@ -123,6 +130,11 @@ SIGNATURES = [
     ("zg_depth_free", None, [C.c_void_p]),
     ("zg_depth_get_info", C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     ("zg_depth_process", C.c_int, [C.c_void_p, C.c_void_p, C.c_ssize_t, C.c_void_p, C.c_ssize_t, C.c_void_p]),
+    ("zg_colorspace_create", C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    ("zg_colorspace_free", None, [C.c_void_p]),
+    ("zg_colorspace_get_info", C.c_int, [C.c_void_p, C.POINTER(C.c_uint), C.POINTER(C.c_int)]),
+    ("zg_colorspace_process", C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_ssize_t),
+                                        C.POINTER(C.c_void_p), C.POINTER(C.c_ssize_t), C.c_void_p]),
     ("zg_clear_last_error", None, []),
     ("zg_get_version_info", None, [C.POINTER(C.c_uint)] * 3),
     ("zg_compute_filter", C.c_int, [C.c_int, C.c_double, C.c_double, C.c_uint, C.c_uint, C.c_double, C.c_double,

@@ -304,6 +304,64 @@ class DepthConversion(_Builder):
         return Depth(h.value, p)
 
 
+class Colorspace:
+    """The created colorspace conversion (zimg's ColorspaceConversion::create
+    result): three FLOAT planes in, three out."""
+
+    OPS = ("matrix", "gamma", "hlg", "hlg_inverse", "cl_to_rgb", "cl_to_yuv")
+
+    def __init__(self, handle, params: capi.ColorspaceParams):
+        self._h = handle
+        self.params = params
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            load().zg_colorspace_free(self._h)
+            self._h = None
+
+    @property
+    def ops(self) -> list:
+        n = C.c_uint()
+        kinds = (C.c_int * 6)()
+        check(load().zg_colorspace_get_info(self._h, C.byref(n), kinds))
+        return [self.OPS[kinds[k]] for k in range(n.value)]
+
+    def process(self, src, dst, stream=None) -> None:
+        """src, dst: three 2-D float32 CUDA tensors each (dst may be src)."""
+        sp = (C.c_void_p * 3)(*[_plane(t)[0] for t in src])
+        ss = (C.c_ssize_t * 3)(*[_plane(t)[1] for t in src])
+        dp = (C.c_void_p * 3)(*[_plane(t)[0] for t in dst])
+        ds = (C.c_ssize_t * 3)(*[_plane(t)[1] for t in dst])
+        check(load().zg_colorspace_process(self._h, sp, ss, dp, ds, _stream_handle(stream)))
+
+
+class ColorspaceConversion(_Builder):
+    """ColorspaceConversion{width, height} (src/zimg/colorspace/colorspace.h:
+    117-132): colorspaces as (matrix, transfer, primaries) zimg API codes."""
+
+    def __init__(self, width: int, height: int):
+        self.width, self.height = width, height
+        self.csp_in = (2, 2, 2)
+        self.csp_out = (2, 2, 2)
+        self.peak_luminance = 100.0
+        self.approximate_gamma = self.scene_referred = self.chromatic_adaptation = False
+
+    def set_csp_in(self, matrix, transfer, primaries): return self._set("csp_in", (matrix, transfer, primaries))
+    def set_csp_out(self, matrix, transfer, primaries): return self._set("csp_out", (matrix, transfer, primaries))
+    def set_peak_luminance(self, v: float): return self._set("peak_luminance", float(v))
+    def set_approximate_gamma(self, v: bool): return self._set("approximate_gamma", bool(v))
+    def set_scene_referred(self, v: bool): return self._set("scene_referred", bool(v))
+    def set_chromatic_adaptation(self, v: bool): return self._set("chromatic_adaptation", bool(v))
+
+    def create(self) -> Colorspace:
+        p = capi.ColorspaceParams(self.width, self.height, *self.csp_in, *self.csp_out, self.peak_luminance,
+                                  int(self.approximate_gamma), int(self.scene_referred),
+                                  int(self.chromatic_adaptation))
+        h = C.c_void_p()
+        check(load().zg_colorspace_create(C.byref(p), C.byref(h)))
+        return Colorspace(h.value, p)
+
+
 class Unresize:
     """The created unresize (zimg's UnresizeConversion::create result)."""
 
