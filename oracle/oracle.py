@@ -716,3 +716,42 @@ def _ref_colorspace(self, planes, csp_in, csp_out, peak=100.0, approximate=False
 
 Oracle.colorspace = _orc_colorspace
 Reference.colorspace = _ref_colorspace
+
+
+def graph_colorspace(o: "Oracle", srcs: list, fs: list, fd: list, sgeo: list, dgeo: list, scolor: str, dcolor: str,
+                     csp_in: tuple, csp_out: tuple, kind, kind_uv, dither="none", **kw) -> list:
+    """zimg's graph for a colorspace change (connect_color_channels,
+    src/zimg/graph/graphbuilder.cpp:975-1014): every colour plane to FLOAT
+    4:4:4 at the work geometry (each dimension from the smaller side's luma
+    plane, :982-991; chroma with the chroma filter), a GREY source read as
+    RGB with equal planes, the colorspace conversion (csp_in / csp_out API
+    codes, the GREY source's matrix taken as RGB), then each output plane
+    from the work planes to its geometry and format. srcs / fs: the source's
+    colour planes and formats; fd: the output planes' formats (one for GREY)."""
+    sy, dy = sgeo[0], dgeo[0]
+    w_src, h_src = (sy if sy["width"] < dy["width"] else dy), (sy if sy["height"] < dy["height"] else dy)
+    gw = dict(width=w_src["width"], left=w_src["left"], aw=w_src["aw"],
+              height=h_src["height"], top=h_src["top"], ah=h_src["ah"])
+
+    def chain(x, g_from, g_to, f_from, f_to, k, plane):
+        rp = None if _same_geometry(g_from, g_to) else resize_params(g_from, g_to)
+        return graph_plane_chain(o, x, f_from, f_to, rp, k, dither=dither, plane=plane)
+
+    work = []
+    for p, (x, f) in enumerate(zip(srcs, fs)):
+        uv = scolor == "yuv" and p > 0
+        g_from = sgeo[p] if scolor == "yuv" else sy
+        work.append(chain(x, g_from, gw, f, PixelFormat("float", None, False, uv), kind_uv if uv else kind, p)
+                    .astype(np.float32))
+    while len(work) < 3:
+        work.append(work[0].copy())
+    cin = ((csp_out[0] if dcolor == "rgb" else 0),) + tuple(csp_in[1:]) if scolor == "grey" else csp_in
+    conv, _ = o.colorspace(work, cin, csp_out, **kw)
+    yuv_work = csp_out[0] != 0
+    out = []
+    for p, f in enumerate(fd):
+        uv = dcolor == "yuv" and p > 0
+        g_to = dgeo[p] if dcolor == "yuv" else dy
+        out.append(chain(conv[p], gw, g_to, PixelFormat("float", None, False, p > 0 and yuv_work), f,
+                         kind_uv if uv else kind, p))
+    return out

@@ -146,3 +146,97 @@ def test_colorspace_errors(cuda):
     with pytest.raises(zg.ZimgError) as e:
         zg.ColorspaceConversion(8, 8).set_csp_in(1, 1, 1).set_csp_out(0, 300, 1).create()  # out of range
     assert e.value.code == 2049
+
+
+GRAPH_CASES = [
+    # (src type, depth, range, dst type, depth, range, size in, size out, colour in, out, subsampling in, out,
+    #  colorspace in, out (matrix, transfer, primaries), dither, exact)
+    ("byte", 8, 0, "byte", 8, 1, (640, 360), (640, 360), "yuv", "rgb", 1, 0, (1, 1, 1), (0, 1, 1), "none", True),
+    ("word", 10, 0, "word", 10, 0, (1920, 1080), (1280, 720), "yuv", "yuv", 1, 1, (9, 14, 9), (1, 1, 1), "ordered",
+     False),
+    ("float", 32, 0, "float", 32, 0, (400, 300), (600, 450), "rgb", "yuv", 0, 1, (0, 13, 1), (1, 1, 1), "none", False),
+    ("word", 16, 1, "byte", 8, 0, (640, 480), (640, 480), "rgb", "grey", 0, 0, (0, 1, 1), (1, 1, 1), "none", True),
+    ("byte", 8, 1, "byte", 8, 1, (320, 240), (320, 240), "grey", "rgb", 0, 0, (1, 1, 1), (0, 13, 1), "none", False),
+    ("word", 10, 0, "word", 10, 0, (640, 360), (640, 360), "grey", "yuv", 0, 1, (1, 1, 1), (1, 1, 1), "none", True),
+    ("byte", 8, 0, "byte", 8, 0, (640, 360), (320, 180), "yuv", "grey", 1, 0, (1, 1, 1), (1, 1, 1), "none", True),
+    ("half", 16, 0, "float", 32, 0, (640, 360), (640, 360), "yuv", "rgb", 1, 0, (9, 16, 9), (0, 16, 9), "none", True),
+    ("word", 10, 0, "byte", 8, 0, (1280, 720), (1920, 1080), "yuv", "yuv", 1, 1, (9, 16, 9), (1, 1, 1),
+     "error_diffusion", False),
+]
+
+
+@pytest.mark.parametrize("case", range(len(GRAPH_CASES)))
+def test_graph_colorspace(cuda, oracle, case):
+    """zg_graph with a colorspace or colour-family change, against the
+    oracle's restatement of zimg's graph (connect_color_channels,
+    graphbuilder.cpp:975-1014; grey_to_yuv / grey_to_rgb / yuv_to_grey
+    :604-659). Conversions made of matrices only (and the family changes
+    without a conversion) are bit-exact; with transfer functions, integer
+    outputs may differ by one code value where the small float difference
+    crosses a rounding boundary, and float outputs stay within 1e-3 of
+    max(1, |value|) (the kernel's own bound against FP64 is tested above)."""
+    import torch
+    import zimg_gb300 as zg
+    from oracle import oracle as O
+    from test_gpu_depth import empty, to_host
+    from test_gpu_depth import to_dev as to_dev_any
+    from test_oracle_depth import make_src
+    (st, sd, sr, dt, dd, dr, (sw, sh), (dw, dh), ci, co, subi, subo, csi, cso, dither, exact) = GRAPH_CASES[case]
+    fam = {"grey": 0, "rgb": 1, "yuv": 2}
+    sfmt = zg.image_format(sw, sh, st, depth=sd, pixel_range=sr, color_family=fam[ci], subsample_w=subi,
+                           subsample_h=subi, chroma_location=0, matrix_coefficients=csi[0],
+                           transfer_characteristics=csi[1], color_primaries=csi[2])
+    dfmt = zg.image_format(dw, dh, dt, depth=dd, pixel_range=dr, color_family=fam[co], subsample_w=subo,
+                           subsample_h=subo, chroma_location=0, matrix_coefficients=cso[0],
+                           transfer_characteristics=cso[1], color_primaries=cso[2])
+    dmap = {"none": 0, "ordered": 1, "random": 2, "error_diffusion": 3}
+    g = zg.Graph(sfmt, dfmt, zg.graph_params(resample_filter="bicubic", resample_filter_uv="bilinear",
+                                             dither_type=dmap[dither]))
+    rng = np.random.default_rng(1300 + case)
+    sgeo = O.plane_geometry(dict(width=sw, height=sh, subsample_w=subi, subsample_h=subi, color=ci, chroma_location=0))
+    dgeo = O.plane_geometry(dict(width=dw, height=dh, subsample_w=subo, subsample_h=subo, color=co, chroma_location=0))
+    n_in, n_out = (1 if ci == "grey" else 3), (1 if co == "grey" else 3)
+    srcs, fs = [], []
+    for p in range(n_in):
+        f = O.PixelFormat(st, sd, bool(sr), ci == "yuv" and p > 0)
+        x = make_src(rng, f, sgeo[p]["height"], sgeo[p]["width"], special=False)
+        if not exact and st in ("byte", "word") and not sr:
+            # legal video levels: beyond them PQ's curve overflows to inf and
+            # a gamut matrix makes NaN, which error diffusion then carries
+            # through the rest of the plane (zimg's C path does the same)
+            lo, hi = 16 << (f.bits - 8), (240 if f.chroma else 235) << (f.bits - 8)
+            x = np.clip(x, lo, hi).astype(x.dtype)
+        srcs.append(x)
+        fs.append(f)
+    fd = [O.PixelFormat(dt, dd, bool(dr), co == "yuv" and p > 0) for p in range(n_out)]
+    dsts = [empty(dgeo[p]["height"], dgeo[p]["width"], dt) for p in range(3 if co != "grey" else 1)]
+    needs = not (csi == cso or (csi[1:] == cso[1:] and (ci == "grey" or (ci != "rgb" and co == "grey"))))
+    if needs:
+        wants = O.graph_colorspace(oracle, srcs, fs, fd, sgeo, dgeo, ci, co, csi, cso, "bicubic", "bilinear", dither)
+    else:
+        # family change alone: luma through its chain; chroma neutral, duplicated or dropped
+        rp = None if (sw, sh) == (dw, dh) else O.resize_params(sgeo[0], dgeo[0])
+        y = O.graph_plane_chain(oracle, srcs[0], fs[0], fd[0], rp, "bicubic", dither=dither, plane=0)
+        wants = [y]
+        if ci == "grey" and co == "yuv":
+            neutral = (1 << (fd[0].bits - 1)) if dt in ("byte", "word") else 0
+            wants += [np.full((dgeo[p]["height"], dgeo[p]["width"]), neutral, fd[0].dtype) for p in (1, 2)]
+        elif ci == "grey" and co == "rgb":
+            wants += [y.copy(), y.copy()]
+    planes_in = [to_dev_any(x) for x in srcs] + [None] * (4 - n_in)
+    planes_out = dsts + [None] * (4 - len(dsts))
+    g.process(planes_in, planes_out)
+    torch.cuda.synchronize()
+    for p in range(len(wants)):
+        got = to_host(dsts[p], fd[min(p, len(fd) - 1)].dtype)
+        want = wants[p]
+        what = f"{GRAPH_CASES[case]} plane {p}"
+        if exact:
+            np.testing.assert_array_equal(got.view(np.uint8), want.view(np.uint8), err_msg=what)
+        elif dt in ("byte", "word"):
+            diff = np.abs(got.astype(np.int64) - want.astype(np.int64))
+            assert diff.max() <= 1, f"{what}: max difference {diff.max()}"
+            assert (diff > 0).mean() < 0.01, f"{what}: {(diff > 0).mean():.4f} of samples differ"
+        else:
+            err = np.abs(got.astype(np.float64) - want.astype(np.float64)) / np.maximum(1.0, np.abs(want))
+            assert np.nanmax(err) <= 1e-3, f"{what}: max relative error {np.nanmax(err):.3g}"

@@ -1,9 +1,10 @@
-// Straight-alpha premultiply / unpremultiply of FLOAT planes (alpha_kernel.cu).
+// zimg's simple graph filters on device planes (alpha_kernel.cu).
 #pragma once
 
 #include <cuda_runtime.h>
 
 #include <cstddef>
+#include <cstdint>
 
 namespace zg {
 
@@ -18,5 +19,10 @@ struct AlphaLaunch {
 
 // inverse false: x * alpha; true: x / clamp(alpha, 0, 1), 0 where that is 0.
 cudaError_t launch_alpha(const AlphaLaunch &L, bool inverse, cudaStream_t stream);
+
+// Every sample of a plane set to `value` (its low `bytes` bytes; bytes 1, 2
+// or 4).
+cudaError_t launch_fill(void *dst, ptrdiff_t stride, int width, int height, int bytes, uint32_t value,
+                        cudaStream_t stream);
 
 } // namespace zg

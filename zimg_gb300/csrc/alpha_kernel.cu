@@ -1,7 +1,9 @@
-// Straight-alpha premultiply and unpremultiply of FLOAT planes (zimg's
-// PremultiplyFilter / UnpremultiplyFilter, src/zimg/graph/simple_filters.cpp:
-// 69-110), one launch for up to three colour planes against one alpha plane.
-// HBM-bound: each thread handles four samples of one line per step.
+// zimg's simple graph filters (src/zimg/graph/simple_filters.cpp): straight-
+// alpha premultiply and unpremultiply of FLOAT planes (PremultiplyFilter /
+// UnpremultiplyFilter, :69-110), one launch for up to three colour planes
+// against one alpha plane, and a plane filled with one value
+// (ValueInitializeFilter, :20-66). HBM-bound: each thread handles four
+// samples of one line per step.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -46,14 +48,25 @@ __global__ void __launch_bounds__(kThreads) alpha_kernel(AlphaLaunch L)
 	}
 }
 
-} // namespace
-
-cudaError_t launch_alpha(const AlphaLaunch &L, bool inverse, cudaStream_t stream)
+__global__ void __launch_bounds__(kThreads) fill_kernel(void *dst, ptrdiff_t stride, int width, int height, int bytes,
+                                                      uint32_t value)
 {
-	if (L.width <= 0 || L.height <= 0 || L.num_planes <= 0)
-		return cudaSuccess;
-	if (L.num_planes > 3)
-		return cudaErrorInvalidValue;
+	const long long total = static_cast<long long>(width) * height;
+	for (long long u = static_cast<long long>(blockIdx.x) * kThreads + threadIdx.x; u < total;
+	     u += static_cast<long long>(gridDim.x) * kThreads) {
+		const int i = static_cast<int>(u / width), j = static_cast<int>(u - static_cast<long long>(i) * width);
+		char *row = static_cast<char *>(dst) + static_cast<ptrdiff_t>(i) * stride;
+		if (bytes == 1)
+			reinterpret_cast<uint8_t *>(row)[j] = static_cast<uint8_t>(value);
+		else if (bytes == 2)
+			reinterpret_cast<uint16_t *>(row)[j] = static_cast<uint16_t>(value);
+		else
+			reinterpret_cast<uint32_t *>(row)[j] = value;
+	}
+}
+
+int grid_for(long long units)
+{
 	static int sms = 0;
 	if (!sms) {
 		int dev = 0;
@@ -62,8 +75,30 @@ cudaError_t launch_alpha(const AlphaLaunch &L, bool inverse, cudaStream_t stream
 		if (sms < 1)
 			sms = 1;
 	}
-	const long long units = static_cast<long long>((L.width + 3) / 4) * L.height * L.num_planes;
-	const int grid = static_cast<int>(std::min<long long>((units + kThreads - 1) / kThreads, static_cast<long long>(sms) * 8));
+	return static_cast<int>(std::min<long long>((units + kThreads - 1) / kThreads, static_cast<long long>(sms) * 8));
+}
+
+} // namespace
+
+cudaError_t launch_fill(void *dst, ptrdiff_t stride, int width, int height, int bytes, uint32_t value,
+                        cudaStream_t stream)
+{
+	if (width <= 0 || height <= 0)
+		return cudaSuccess;
+	if (bytes != 1 && bytes != 2 && bytes != 4)
+		return cudaErrorInvalidValue;
+	fill_kernel<<<grid_for(static_cast<long long>(width) * height), kThreads, 0, stream>>>(dst, stride, width, height,
+	                                                                                      bytes, value);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_alpha(const AlphaLaunch &L, bool inverse, cudaStream_t stream)
+{
+	if (L.width <= 0 || L.height <= 0 || L.num_planes <= 0)
+		return cudaSuccess;
+	if (L.num_planes > 3)
+		return cudaErrorInvalidValue;
+	const int grid = grid_for(static_cast<long long>((L.width + 3) / 4) * L.height * L.num_planes);
 	if (inverse)
 		alpha_kernel<true><<<grid, kThreads, 0, stream>>>(L);
 	else

@@ -8,6 +8,7 @@
 // mapping of resize_plane (graphbuilder.cpp:769-776).
 #include "capi_common.h"
 #include "alpha.h"
+#include "colorspace_plan.h"
 
 #include <cfloat>
 #include <cmath>
@@ -41,6 +42,7 @@ struct FormatState {
 	int parity;
 	int chroma_location;
 	int alpha;
+	csp::Space cs;  // matrix, transfer, primaries as zimg's internal values
 	PlaneGeom planes[4];
 };
 
@@ -133,6 +135,15 @@ FormatState import_format(const zg_image_format &f)
 	s.alpha = f.version >= kApi24 ? f.alpha : 0;
 	if (s.alpha < 0 || s.alpha > 2)
 		throw Error(kErrEnumOutOfRange, "unrecognized alpha type");
+	// translate_matrix / _transfer / _primaries (zimg.cpp:238-305,425-431)
+	s.cs = csp::from_api(s.matrix, s.transfer, s.primaries);
+	// colour family against matrix (validate_state, graphbuilder.cpp:199-216)
+	if (s.color == COLOR_GREY && s.cs.m == csp::M_RGB)
+		throw Error(kErrColorFamilyMismatch, "GREY color family cannot have RGB matrix coefficients");
+	if (s.color == COLOR_RGB && s.cs.m != csp::M_UNSPEC && s.cs.m != csp::M_RGB)
+		throw Error(kErrColorFamilyMismatch, "RGB color family cannot have YUV matrix coefficients");
+	if (s.color == COLOR_YUV && s.cs.m == csp::M_RGB)
+		throw Error(kErrColorFamilyMismatch, "YUV color family cannot have RGB matrix coefficients");
 
 	double al = 0.0, at = 0.0, aw = s.width, ah = s.height;
 	if (f.version >= kApi21) {
@@ -328,13 +339,133 @@ void run_depth(const zg_depth *d, const void *src, ptrdiff_t ss, void *dst, ptrd
 	}
 }
 
+// One plane from one geometry and pixel format to another, as zimg's
+// connect_plane does it (graphbuilder.cpp:892-953): a depth conversion into
+// the format resize works in (choose_resize_format), the resize, a depth
+// conversion to the output format; a copy or a depth conversion alone when
+// the geometry is kept. Its scratch (the intermediate planes and the
+// resize's tmp) is `scratch` bytes.
+struct Chain {
+	int kind = 0;  // 0 copy, 1 depth only, 2 resize
+	unsigned sw = 0, sh = 0, dw = 0, dh = 0, in_bytes = 0, out_bytes = 0;
+	zg_depth *pre = nullptr, *post = nullptr, *only = nullptr;
+	zg_resize *resize = nullptr;
+	size_t pre_pitch = 0, mid_pitch = 0, off_mid = 0, off_rtmp = 0, scratch = 0;
+
+	void release()
+	{
+		zg_depth_free(pre);
+		zg_depth_free(post);
+		zg_depth_free(only);
+		zg_resize_free(resize);
+		pre = post = only = nullptr;
+		resize = nullptr;
+	}
+};
+
+unsigned sample_bytes(int t)
+{
+	return t == ZG_PIXEL_BYTE ? 1u : (t == ZG_PIXEL_FLOAT ? 4u : 2u);
+}
+
+Chain make_chain(const PlaneGeom &sp, const PlaneGeom &dp, const PixFmt &fs, const PixFmt &fd, int filter, double a,
+                 double b, int dither, int plane)
+{
+	Chain c;
+	c.sw = sp.width;
+	c.sh = sp.height;
+	c.dw = dp.width;
+	c.dh = dp.height;
+	c.in_bytes = sample_bytes(fs.type);
+	c.out_bytes = sample_bytes(fd.type);
+	if (sp == dp) {
+		if (!fmt_equal(fs, fd)) {
+			c.kind = 1;
+			c.only = make_depth(dp.width, dp.height, fs, fd, dither, plane);
+		}
+		return c;
+	}
+	c.kind = 2;
+	const PixFmt fr = choose_resize_format(fs, fd, static_cast<double>(sp.width) * sp.height,
+	                                       static_cast<double>(dp.width) * dp.height);
+	zg_resize_params rp = geom_resize_params(sp, dp);
+	rp.pixel_type = static_cast<zg_pixel_type>(fr.type);
+	rp.depth = fr.type == ZG_PIXEL_FLOAT ? 32 : fr.depth;
+	rp.filter = static_cast<zg_resample_filter>(filter);
+	rp.filter_param_a = a;
+	rp.filter_param_b = b;
+	zg_error_code rc = zg_resize_create(&rp, &c.resize);
+	if (rc != ZG_ERROR_SUCCESS) {
+		char msg[256];
+		zg_get_last_error(msg, sizeof(msg));
+		throw Error(rc, msg);
+	}
+	size_t rtmp = 0;
+	zg_resize_get_tmp_size(c.resize, &rtmp);
+	size_t off = 0;
+	if (!fmt_equal(fs, fr)) {
+		c.pre = make_depth(sp.width, sp.height, fs, fr, dither, plane);
+		c.pre_pitch = pitch_of(sp.width, sample_bytes(fr.type));
+		off += c.pre_pitch * sp.height;
+	}
+	if (!fmt_equal(fr, fd)) {
+		c.post = make_depth(dp.width, dp.height, fr, fd, dither, plane);
+		c.mid_pitch = pitch_of(dp.width, sample_bytes(fr.type));
+		c.off_mid = off;
+		off += c.mid_pitch * dp.height;
+	}
+	c.off_rtmp = off;
+	c.scratch = off + rtmp;
+	return c;
+}
+
+void run_chain(const Chain &c, const void *src, ptrdiff_t ss, void *dst, ptrdiff_t ds, char *scratch, zg_stream st)
+{
+	if (c.kind == 0) {
+		copy_plane(dst, ds, src, ss, static_cast<size_t>(c.dw) * c.out_bytes, c.dh, reinterpret_cast<cudaStream_t>(st));
+		return;
+	}
+	if (c.kind == 1) {
+		run_depth(c.only, src, ss, dst, ds, st);
+		return;
+	}
+	const void *rs = src;
+	ptrdiff_t rss = ss;
+	if (c.pre) {
+		run_depth(c.pre, src, ss, scratch, static_cast<ptrdiff_t>(c.pre_pitch), st);
+		rs = scratch;
+		rss = static_cast<ptrdiff_t>(c.pre_pitch);
+	}
+	void *rd = c.post ? static_cast<void *>(scratch + c.off_mid) : dst;
+	const ptrdiff_t rds = c.post ? static_cast<ptrdiff_t>(c.mid_pitch) : ds;
+	run_resize(c.resize, rs, rss, rd, rds, scratch + c.off_rtmp, st);
+	if (c.post)
+		run_depth(c.post, rd, rds, dst, ds, st);
+}
+
+// needs_colorspace (graphbuilder.cpp:484-506)
+bool needs_colorspace(const FormatState &s, const FormatState &d)
+{
+	if (s.cs == d.cs)
+		return false;
+	if (s.cs.t == d.cs.t && s.cs.p == d.cs.p) {
+		if (s.color == COLOR_GREY)
+			return false;  // GREY to YUV / RGB: value-initialised or duplicated planes
+		if (s.color != COLOR_RGB && d.color == COLOR_GREY)
+			return false;  // YUV / GREY to GREY: chroma dropped
+	}
+	return true;
+}
+
 } // namespace
 
 struct zg_graph {
 	int device;
 	struct Plane {
-		bool present = false;
-		int mode = 0;  // 0 copy, 1 copy subrectangle, 2 resize, 3 depth only, 4 depth of a subrectangle
+		bool present = false;      // read, written or both
+		bool has_src = false, has_dst = false;
+		int mode = 0;  // 0 copy, 1 copy subrectangle, 2 resize, 3 depth only, 4 depth of a subrectangle,
+		               // 5 straight-alpha chain, 6 colorspace chain, 7 made from other planes
 		unsigned w = 0, h = 0;      // output size
 		unsigned off_x = 0, off_y = 0;
 		unsigned in_bytes = 0, out_bytes = 0;
@@ -374,6 +505,25 @@ struct zg_graph {
 		unsigned cs_w = 0, cs_h = 0, cd_w = 0, cd_h = 0;
 		size_t cs_pitch = 0, cd_pitch = 0, off_cs = 0, off_cd = 0, off_rtmp = 0;
 	} premul;
+	// A colorspace change (connect_color_channels, graphbuilder.cpp:975-1014):
+	// the colour planes to FLOAT 4:4:4 at the work geometry (each dimension
+	// the smaller side's), GREY duplicated into three planes, the colorspace
+	// operations in place, then each output plane from the work planes to
+	// its geometry and format. Work planes and the chains' shared scratch in
+	// tmp from off_work.
+	struct Color {
+		bool on = false;
+		int n_in = 0, n_out = 0;  // colour planes read / written
+		unsigned ww = 0, wh = 0;
+		size_t w_pitch = 0, off_work = 0, off_scratch = 0;
+		Chain in[3], out[3];
+		csp::Plan plan;
+	} color;
+	// output planes made without a source plane of their own (grey_to_yuv /
+	// grey_to_rgb, graphbuilder.cpp:615-659): 1 filled with fill_value, 2 a
+	// copy of the luma output
+	int out_fill[4] = {};
+	uint32_t fill_value = 0;
 	size_t tmp_size = 0;
 	// lines and widths the callbacks are called with (the luma plane's), and
 	// the vertical subsampling step of the source and destination formats
@@ -396,6 +546,10 @@ struct zg_graph {
 		zg_resize_free(premul.across);
 		zg_resize_free(premul.across_uv);
 		zg_resize_free(premul.down);
+		for (int p = 0; p < 3; ++p) {
+			color.in[p].release();
+			color.out[p].release();
+		}
 	}
 };
 
@@ -459,8 +613,13 @@ zg_graph *zg_graph_build(const zg_image_format *src_format, const zg_image_forma
 
 		const bool format_change =
 			s.pixel_type != d.pixel_type || s.depth != d.depth || (s.pixel_type != ZG_PIXEL_FLOAT && s.range != d.range);
-		if (s.color != d.color || s.matrix != d.matrix || s.transfer != d.transfer || s.primaries != d.primaries)
-			throw Error(kErrNoColorspaceConversion, "colorspace conversion is outside the resize path");
+		const bool colorspace = needs_colorspace(s, d);
+		if (!colorspace && s.color != d.color && !(s.color == COLOR_GREY || d.color == COLOR_GREY))
+			throw Error(kErrNoColorspaceConversion, "colour family change without a colorspace conversion");
+		if (colorspace && s.alpha == 1)
+			throw Error(kErrUnsupported, "colorspace conversion of images with straight alpha is not supported by this library");
+		if (colorspace && gp.resample_filter == ZG_RESIZE_UNRESIZE)
+			throw Error(kErrUnsupported, "colorspace conversion with unresize is not supported by this library");
 		if (s.alpha != d.alpha)
 			throw Error(kErrUnsupported, "alpha conversion is outside the resize path");
 		(void)format_change;
@@ -483,7 +642,7 @@ zg_graph *zg_graph_build(const zg_image_format *src_format, const zg_image_forma
 		// needs_interpolation over the planes both formats have
 		// (graphbuilder.cpp:527-538)
 		bool interpolate = needs_interpolation_plane(s.planes[PLANE_Y], d.planes[PLANE_Y]);
-		if (s.color != COLOR_GREY)
+		if (s.color != COLOR_GREY && d.color != COLOR_GREY)
 			interpolate = interpolate || needs_interpolation_plane(s.planes[PLANE_U], d.planes[PLANE_U]) ||
 			              needs_interpolation_plane(s.planes[PLANE_V], d.planes[PLANE_V]);
 		if (s.alpha)
@@ -512,7 +671,7 @@ zg_graph *zg_graph_build(const zg_image_format *src_format, const zg_image_forma
 				pm.across_needed = !(gs == gd);
 			}
 			auto &gpl = g->planes[p];
-			gpl.present = true;
+			gpl.present = gpl.has_src = gpl.has_dst = true;
 			gpl.mode = 5;
 			const int q = (s.color == COLOR_RGB && chroma) ? PLANE_Y : p;
 			const PlaneGeom &sp = s.planes[q], &dp = d.planes[q];
@@ -570,12 +729,14 @@ zg_graph *zg_graph_build(const zg_image_format *src_format, const zg_image_forma
 
 		for (int p = 0; p < 4 && !premul; ++p) {
 			const bool chroma = p == PLANE_U || p == PLANE_V;
-			if (chroma && s.color == COLOR_GREY)
+			if (chroma && (s.color == COLOR_GREY || d.color == COLOR_GREY))
 				continue;
 			if (p == PLANE_A && !s.alpha)
 				continue;
+			if (colorspace && p != PLANE_A)
+				continue;
 			auto &gpl = g->planes[p];
-			gpl.present = true;
+			gpl.present = gpl.has_src = gpl.has_dst = true;
 			// RGB planes share the luma plane's conversion (graphbuilder.cpp:892-905).
 			const int q = (s.color == COLOR_RGB && chroma) ? PLANE_Y : p;
 			const PlaneGeom &sp = s.planes[q];
@@ -669,6 +830,95 @@ zg_graph *zg_graph_build(const zg_image_format *src_format, const zg_image_forma
 			gpl.off_tmp = off;
 			gpl.tmp = off + rtmp;
 			g->tmp_size = std::max(g->tmp_size, gpl.tmp);
+		}
+		// GREY to YUV / RGB without a colorspace change: the chroma outputs
+		// are the neutral value in the output format, or copies of the luma
+		// output (grey_to_yuv / grey_to_rgb, graphbuilder.cpp:615-659)
+		if (!colorspace && s.color == COLOR_GREY && d.color != COLOR_GREY) {
+			const PixFmt fy = plane_fmt(d, PLANE_Y);
+			if (fy.type == ZG_PIXEL_BYTE || fy.type == ZG_PIXEL_WORD)
+				g->fill_value = 1u << (fy.depth - 1);
+			for (int p : { PLANE_U, PLANE_V }) {
+				auto &gpl = g->planes[p];
+				gpl.present = gpl.has_dst = true;
+				gpl.mode = 7;
+				gpl.w = d.planes[p].width;
+				gpl.h = d.planes[p].height;
+				gpl.out_bytes = bytes(d.pixel_type);
+				gpl.dst_ssh = d.color == COLOR_YUV ? d.subsample_h : 0;
+				g->out_fill[p] = d.color == COLOR_YUV ? 1 : 2;
+			}
+		}
+		if (colorspace) {
+			auto &cm = g->color;
+			cm.on = true;
+			cm.n_in = s.color == COLOR_GREY ? 1 : 3;
+			cm.n_out = d.color == COLOR_GREY ? 1 : 3;
+			// work geometry: each dimension from the smaller side
+			// (graphbuilder.cpp:982-991)
+			const PlaneGeom &sy = s.planes[PLANE_Y], &dy = d.planes[PLANE_Y];
+			const PlaneGeom &wsrc = sy.width < dy.width ? sy : dy, &hsrc = sy.height < dy.height ? sy : dy;
+			PlaneGeom gw;
+			gw.width = wsrc.width;
+			gw.left = wsrc.left;
+			gw.aw = wsrc.aw;
+			gw.height = hsrc.height;
+			gw.top = hsrc.top;
+			gw.ah = hsrc.ah;
+			cm.ww = gw.width;
+			cm.wh = gw.height;
+			cm.w_pitch = pitch_of(gw.width, 4);
+			const bool yuv_in = s.color == COLOR_YUV;
+			// after the conversion the planes are YUV unless the output
+			// matrix is RGB (convert_colorspace, graphbuilder.cpp:853-861)
+			const bool yuv_work = d.cs.m != csp::M_RGB;
+			size_t scratch = 0;
+			for (int p = 0; p < cm.n_in; ++p) {
+				const bool chroma = p != PLANE_Y;
+				const int q = (s.color == COLOR_RGB && chroma) ? PLANE_Y : p;
+				const bool uv = chroma && yuv_in;
+				cm.in[p] = make_chain(s.planes[q], gw, plane_fmt(s, p), PixFmt{ ZG_PIXEL_FLOAT, 32, false, uv },
+				                      uv ? gp.resample_filter_uv : gp.resample_filter,
+				                      uv ? gp.filter_param_a_uv : gp.filter_param_a,
+				                      uv ? gp.filter_param_b_uv : gp.filter_param_b, dither, p);
+				scratch = std::max(scratch, cm.in[p].scratch);
+				auto &gpl = g->planes[p];
+				gpl.present = gpl.has_src = true;
+				gpl.mode = 6;
+				gpl.in_bytes = bytes(s.pixel_type);
+				gpl.src_w = s.planes[q].width;
+				gpl.src_h = s.planes[q].height;
+				gpl.src_ssh = uv ? s.subsample_h : 0;
+			}
+			for (int p = 0; p < cm.n_out; ++p) {
+				const bool chroma = p != PLANE_Y;
+				const int q = (d.color == COLOR_RGB && chroma) ? PLANE_Y : p;
+				const bool uv_work = chroma && yuv_work, uv = chroma && d.color == COLOR_YUV;
+				cm.out[p] = make_chain(gw, d.planes[q], PixFmt{ ZG_PIXEL_FLOAT, 32, false, uv_work }, plane_fmt(d, p),
+				                       uv ? gp.resample_filter_uv : gp.resample_filter,
+				                       uv ? gp.filter_param_a_uv : gp.filter_param_a,
+				                       uv ? gp.filter_param_b_uv : gp.filter_param_b, dither, p);
+				scratch = std::max(scratch, cm.out[p].scratch);
+				auto &gpl = g->planes[p];
+				gpl.present = gpl.has_dst = true;
+				gpl.mode = 6;
+				gpl.w = d.planes[q].width;
+				gpl.h = d.planes[q].height;
+				gpl.out_bytes = bytes(d.pixel_type);
+				gpl.dst_ssh = uv ? d.subsample_h : 0;
+			}
+			// GREY is read as RGB with equal planes (grey_to_rgb before the
+			// conversion, graphbuilder.cpp:998-1002)
+			csp::Space from = s.cs;
+			if (s.color == COLOR_GREY)
+				from.m = d.color == COLOR_RGB ? d.cs.m : csp::M_RGB;
+			const double peak = std::isnan(gp.nominal_peak_luminance) ? 100.0 : gp.nominal_peak_luminance;
+			const bool v25 = gp.version >= ZG_MAKE_API_VERSION(2, 5);
+			cm.plan = csp::make_plan(from, d.cs, peak, gp.allow_approximate_gamma != 0,
+			                         v25 && gp.scene_referred != 0, v25 && gp.chromatic_adaptation != 0);
+			cm.off_work = (g->tmp_size + 255) & ~static_cast<size_t>(255);
+			cm.off_scratch = cm.off_work + 3 * cm.w_pitch * cm.wh;
+			g->tmp_size = cm.off_scratch + scratch;
 		}
 		// staging planes for ring buffers, after the largest per-plane scratch
 		size_t off = (g->tmp_size + 255) & ~static_cast<size_t>(255);
@@ -769,8 +1019,9 @@ zg_error_code zg_graph_process_cb(const zg_graph *g, const zg_image_buffer_const
 			const auto &pl = g->planes[p];
 			if (!pl.present)
 				continue;
-			const unsigned sm = src->plane[p].mask, dm = dst->plane[p].mask;
-			if (!src->plane[p].data || !dst->plane[p].data)
+			const unsigned sm = pl.has_src ? src->plane[p].mask : ZG_BUFFER_MAX;
+			const unsigned dm = pl.has_dst ? dst->plane[p].mask : ZG_BUFFER_MAX;
+			if ((pl.has_src && !src->plane[p].data) || (pl.has_dst && !dst->plane[p].data))
 				throw Error(kErrIllegalArgument, "null plane pointer");
 			if (!ring_ok(sm) || !ring_ok(dm))
 				throw Error(kErrIllegalArgument, "buffer mask must be 2^n - 1 or ZG_BUFFER_MAX");
@@ -783,7 +1034,7 @@ zg_error_code zg_graph_process_cb(const zg_graph *g, const zg_image_buffer_const
 					throw Error(kErrIllegalArgument, "tmp is null");
 				from_data[p] = t + pl.off_sstage;
 				from_stride[p] = static_cast<ptrdiff_t>(pl.sstage_pitch);
-			} else {
+			} else if (pl.has_src) {
 				from_data[p] = src->plane[p].data;
 				from_stride[p] = src->plane[p].stride;
 			}
@@ -796,7 +1047,7 @@ zg_error_code zg_graph_process_cb(const zg_graph *g, const zg_image_buffer_const
 					throw Error(kErrIllegalArgument, "tmp is null");
 				to_data[p] = t + pl.off_dstage;
 				to_stride[p] = static_cast<ptrdiff_t>(pl.dstage_pitch);
-			} else {
+			} else if (pl.has_dst) {
 				to_data[p] = dst->plane[p].data;
 				to_stride[p] = dst->plane[p].stride;
 			}
@@ -817,7 +1068,7 @@ zg_error_code zg_graph_process_cb(const zg_graph *g, const zg_image_buffer_const
 					throw Error(kErrUserCallbackFailed, "user callback failed");
 				for (int p = 0; p < 4 && src_ring; ++p) {
 					const auto &pl = g->planes[p];
-					if (!pl.present || src->plane[p].mask == ZG_BUFFER_MAX)
+					if (!pl.has_src || src->plane[p].mask == ZG_BUFFER_MAX)
 						continue;
 					const unsigned l0 = i >> pl.src_ssh;
 					const unsigned l1 = std::min(pl.src_h, (i + g->src_step) >> pl.src_ssh);
@@ -848,7 +1099,7 @@ zg_error_code zg_graph_process_cb(const zg_graph *g, const zg_image_buffer_const
 				run_depth(pl.only, from, sst, dp, dst_st, stream);
 				continue;
 			}
-			if (pl.mode == 5)
+			if (pl.mode >= 5)
 				continue;
 			if (pl.tmp && !tmp)
 				throw Error(kErrIllegalArgument, "tmp is null");
@@ -937,6 +1188,46 @@ zg_error_code zg_graph_process_cb(const zg_graph *g, const zg_image_buffer_const
 			}
 		}
 
+		if (g->color.on) {
+			const auto &cm = g->color;
+			if (!t)
+				throw Error(kErrIllegalArgument, "tmp is null");
+			const ptrdiff_t wp = static_cast<ptrdiff_t>(cm.w_pitch);
+			auto work = [&](int p) { return t + cm.off_work + static_cast<size_t>(p) * cm.w_pitch * cm.wh; };
+			char *scratch = t + cm.off_scratch;
+			for (int p = 0; p < cm.n_in; ++p)
+				run_chain(cm.in[p], from_data[p], from_stride[p], work(p), wp, scratch, stream);
+			for (int p = cm.n_in; p < 3; ++p)
+				copy_plane(work(p), wp, work(0), wp, static_cast<size_t>(cm.ww) * 4, cm.wh, st);
+			if (cm.plan.num_ops) {
+				csp::Launch L{};
+				for (int p = 0; p < 3; ++p) {
+					L.src[p] = work(p);
+					L.dst[p] = work(p);
+					L.src_stride[p] = L.dst_stride[p] = wp;
+				}
+				L.width = static_cast<int>(cm.ww);
+				L.height = static_cast<int>(cm.wh);
+				L.vec = reinterpret_cast<uintptr_t>(work(0)) % 16 == 0;  // pitches are multiples of 256 bytes
+				L.plan = cm.plan;
+				cuda_check(csp::launch_colorspace(L, st), "colorspace launch");
+			}
+			for (int p = 0; p < cm.n_out; ++p)
+				run_chain(cm.out[p], work(p), wp, to_data[p], to_stride[p], scratch, stream);
+		}
+		for (int p = 0; p < 4; ++p) {
+			if (g->out_fill[p] == 1) {
+				const auto &pl = g->planes[p];
+				cuda_check(launch_fill(to_data[p], to_stride[p], static_cast<int>(pl.w), static_cast<int>(pl.h),
+				                       static_cast<int>(pl.out_bytes), g->fill_value, st),
+				           "plane fill");
+			} else if (g->out_fill[p] == 2) {
+				const auto &pl = g->planes[p];
+				copy_plane(to_data[p], to_stride[p], to_data[PLANE_Y], to_stride[PLANE_Y],
+				           static_cast<size_t>(pl.w) * pl.out_bytes, pl.h, st);
+			}
+		}
+
 		// Output: ring lines scattered from the staging planes a ring's worth
 		// at a time, then the pack callback for each step of lines in it, once
 		// the copies (and everything before them) have completed.
@@ -946,7 +1237,7 @@ zg_error_code zg_graph_process_cb(const zg_graph *g, const zg_image_buffer_const
 				const unsigned w1 = std::min(g->dst_lines, w0 + window);
 				for (int p = 0; p < 4 && dst_ring; ++p) {
 					const auto &pl = g->planes[p];
-					if (!pl.present || dst->plane[p].mask == ZG_BUFFER_MAX)
+					if (!pl.has_dst || dst->plane[p].mask == ZG_BUFFER_MAX)
 						continue;
 					const unsigned l0 = w0 >> pl.dst_ssh;
 					const unsigned l1 = std::min(pl.h, (w1 + (1u << pl.dst_ssh) - 1) >> pl.dst_ssh);
