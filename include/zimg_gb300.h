@@ -420,9 +420,16 @@ ZG_API zg_error_code zg_batch_get_launch_count(const zg_batch *b, unsigned *out)
  * 753-824). Alpha planes are full range in the integer types; straight alpha
  * through an interpolating resize is premultiplied in FLOAT 4:4:4 and divided
  * out afterwards, as zimg does (graphbuilder.cpp:594-600,1019-1068). A change
- * of colour family, matrix, transfer or primaries returns
- * ZG_ERROR_NO_COLORSPACE_CONVERSION; a change of alpha type, and unresize of
- * an image with straight alpha, ZG_ERROR_UNSUPPORTED_OPERATION.
+ * of matrix, transfer or primaries runs zimg's colorspace chain
+ * (graphbuilder.cpp:975-1014): the colour planes to FLOAT 4:4:4 at the
+ * smaller of the two geometries, the colorspace conversion (see
+ * zg_colorspace_*), then each output plane to its geometry and format; GREY
+ * to YUV / RGB without a conversion fills / duplicates the chroma planes and
+ * YUV to GREY drops them. Colorspace codes zimg does not map, and pairs
+ * without a path, return ZG_ERROR_NO_COLORSPACE_CONVERSION. A change of
+ * alpha type, a colorspace change of an image with straight alpha, and
+ * unresize of an image with straight alpha or with a colorspace change
+ * return ZG_ERROR_UNSUPPORTED_OPERATION.
  */
 typedef struct zg_image_format {
 	unsigned version;
