@@ -499,7 +499,7 @@ zg_error_code zg_resize_process(const zg_resize *r, const void *src, ptrdiff_t s
 			j.item_begin = 0;
 			CUtensorMap map;
 			if (r->tma && chain_tma_source_map(&map, j, r->tlayout)) {
-				cuda_check(launch_chain_tma(r->fplan.variant, nullptr, 1, fused_items(j), r->tlayout, r->tgrid, j, &map,
+				cuda_check(launch_chain_tma(r->fplan.variant, nullptr, 1, fused_items(j), nullptr, r->tlayout, r->tgrid, j, &map,
 				                            st),
 				           "fused resize launch");
 				return;

@@ -8,9 +8,11 @@
 #include "capi_common.h"
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <functional>
 #include <map>
+#include <string>
 
 using namespace zg;
 
@@ -28,6 +30,7 @@ struct zg_batch {
 		bool tma_now = false;
 		SmemLayout tlayout{};
 		int tgrid = 0;
+		int ranges_off = -1;  // CTA unit ranges in ranges_dev (ints), or -1
 	};
 
 	int device;
@@ -37,6 +40,8 @@ struct zg_batch {
 	size_t tmp_size = 0;
 	std::vector<zg_batch_io> io;
 	std::vector<Group> groups;
+	std::vector<int> ranges_host;
+	DeviceBuffer ranges_dev;
 	std::vector<FusedJob> table_host;
 	DeviceBuffer table_dev;
 	std::vector<CUtensorMap> maps_host;  // per table entry (chained TMA groups)
@@ -112,11 +117,12 @@ void batch_launch(const zg_batch *b, void *tmp, cudaStream_t st)
 	for (const auto &g : b->groups) {
 		if (b->mixed_now && g.tma_plan)
 			continue;  // in the mixed launch
-		work.push_back([&g, table](cudaStream_t s) {
+		const int *ranges = g.ranges_off < 0 ? nullptr : static_cast<const int *>(b->ranges_dev.get()) + g.ranges_off;
+		work.push_back([&g, table, ranges](cudaStream_t s) {
 			FusedJob unused{};
 			if (g.tma_now)
-				cuda_check(launch_chain_tma(g.variant, table + g.first, g.count, g.tiles, g.tlayout, g.tgrid, unused,
-				                            nullptr, s),
+				cuda_check(launch_chain_tma(g.variant, table + g.first, g.count, g.tiles, ranges, g.tlayout, g.tgrid,
+				                            unused, nullptr, s),
 				           "fused batch launch");
 			else
 				cuda_check(launch_fused(g.variant, table + g.first, g.count, g.tiles, g.layout, g.grid, unused, s),
@@ -319,6 +325,7 @@ void regroup(zg_batch *b)
 			b->tmp_size += (b->jobs[i]->tmp_size + 255) & ~static_cast<size_t>(255);
 	}
 	b->groups.clear();
+	b->ranges_host.clear();
 	b->table_host.clear();
 	b->table_dev.release();
 	share_tables(b);
@@ -353,10 +360,32 @@ void regroup(zg_batch *b)
 		g.grid = fused_grid_size(g.variant, static_cast<size_t>(g.layout.total_bytes));
 		if (plans[0]->chain && chain_tma_enabled()) {
 			g.tma_plan = chain_tma_layout(plans.data(), static_cast<int>(plans.size()), &g.tlayout);
-			if (g.tma_plan)
+			if (g.tma_plan) {
 				g.tgrid = chain_tma_grid_size(g.variant, static_cast<size_t>(g.tlayout.total_bytes));
+				// jobs of one shape with at least a strip per CTA: strips in
+				// step across neighbouring CTAs
+				bool same = true;
+				for (unsigned i : kv.second)
+					same = same && b->jobs[i]->fplan.job.groups == b->jobs[kv.second[0]]->fplan.job.groups;
+				const char *order = std::getenv("ZG_CHAIN_ORDER");
+				const bool lockstep = !(order && std::string(order) == "equal");
+				const std::vector<int> r = same && lockstep ? chain_tma_lockstep_ranges(
+				                                                  g.tiles, b->jobs[kv.second[0]]->fplan.job.groups, g.tgrid)
+				                                            : std::vector<int>();
+				if (!r.empty()) {
+					g.ranges_off = static_cast<int>(b->ranges_host.size());
+					b->ranges_host.insert(b->ranges_host.end(), r.begin(), r.end());
+				}
+			}
 		}
 		b->groups.push_back(g);
+	}
+	b->ranges_dev.release();
+	if (!b->ranges_host.empty()) {
+		b->ranges_dev.reset(b->ranges_host.size() * sizeof(int));
+		cuda_check(cudaMemcpy(b->ranges_dev.get(), b->ranges_host.data(), b->ranges_host.size() * sizeof(int),
+		                      cudaMemcpyHostToDevice),
+		           "strip ranges");
 	}
 	if (!b->table_host.empty()) {
 		b->table_dev.reset(b->table_host.size() * sizeof(FusedJob));

@@ -199,8 +199,9 @@ int chain_tma_grid_size(int variant, size_t smem_bytes)
 	return std::max(1, sms) * per_sm;
 }
 
-cudaError_t launch_chain_tma(int variant, const FusedJob *jobs, int num_jobs, int total_items, const SmemLayout &L,
-                             int grid, const FusedJob &single, const CUtensorMap *single_map, cudaStream_t stream)
+cudaError_t launch_chain_tma(int variant, const FusedJob *jobs, int num_jobs, int total_items, const int *ranges,
+                             const SmemLayout &L, int grid, const FusedJob &single, const CUtensorMap *single_map,
+                             cudaStream_t stream)
 {
 	if (static_cast<size_t>(L.total_bytes) > kTmaSmemMax || (!jobs && !single_map))
 		return cudaErrorInvalidValue;
@@ -213,10 +214,28 @@ cudaError_t launch_chain_tma(int variant, const FusedJob *jobs, int num_jobs, in
 	CUtensorMap map{};
 	if (single_map)
 		map = *single_map;
-	void *args[] = { &jobs, &num_jobs, &total_items, &one, &layout, &map };
-	grid = std::max(1, std::min(grid, total_items));
+	void *args[] = { &jobs, &num_jobs, &total_items, &ranges, &one, &layout, &map };
+	if (!ranges)
+		grid = std::max(1, std::min(grid, total_items));
 	return cudaLaunchKernel(k, dim3(grid), dim3(tma_threads(variant)), args, static_cast<size_t>(L.total_bytes),
 	                        stream);
+}
+
+std::vector<int> chain_tma_lockstep_ranges(int total_items, int groups, int grid)
+{
+	std::vector<int> r;
+	if (groups <= 0 || grid <= 0 || total_items % groups || total_items / groups < grid)
+		return r;
+	const long long lead = static_cast<long long>(grid) * groups;
+	const long long rest = total_items - lead;
+	r.resize(4 * static_cast<size_t>(grid));
+	for (int b = 0; b < grid; ++b) {
+		r[4 * b] = b * groups;
+		r[4 * b + 1] = (b + 1) * groups;
+		r[4 * b + 2] = static_cast<int>(lead + rest * b / grid);
+		r[4 * b + 3] = static_cast<int>(lead + rest * (b + 1) / grid);
+	}
+	return r;
 }
 
 int chain_mixed_copy_variant()

@@ -604,32 +604,51 @@ __device__ __forceinline__ void load_bases(Pipe &p, const FusedJob &J, int g_beg
 		p.vb[g] = __ldg(J.v_base + g_begin + g);
 }
 
-// Kernel for the jobs of one variant: each CTA an equal contiguous range of
-// the launch's (strip, 16-row group) units, job by job and strip by strip.
+// Kernel for the jobs of one variant. The launch's (strip, 16-row group)
+// units are numbered job by job and strip by strip. Without `ranges` each
+// CTA takes an equal contiguous range of them; with it, CTA b takes the two
+// ranges [ranges[4b], ranges[4b+1]) and [ranges[4b+2], ranges[4b+3]) in
+// order (a whole strip, so that neighbouring CTAs run neighbouring strips in
+// step and read their shared columns once through L2, then an equal share of
+// the strips left over).
 template <bool H_FIRST, int KV, int KH>
 __global__ void __launch_bounds__(tma_threads(H_FIRST), 2)
-chain_tma_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, const __grid_constant__ FusedJob single,
-                 const __grid_constant__ SmemLayout L, const __grid_constant__ CUtensorMap single_map)
+chain_tma_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, const int *__restrict__ ranges,
+                 const __grid_constant__ FusedJob single, const __grid_constant__ SmemLayout L,
+                 const __grid_constant__ CUtensorMap single_map)
 {
 	extern __shared__ float4 smem4[];
 	__shared__ int abort_item;
 	Pipe p;
 	pipe_init(p, smem4, L, &abort_item);
-	const int t_end = static_cast<int>(static_cast<long long>(blockIdx.x + 1) * total_items / gridDim.x);
-	for (int t = static_cast<int>(static_cast<long long>(blockIdx.x) * total_items / gridDim.x); t < t_end;) {
-		const FusedJob &J = jobs ? jobs[find_job(jobs, num_jobs, t)] : single;
-		const int local = t - J.item_begin;
-		const int strip = local / J.groups;
-		const int g_begin = local - strip * J.groups;
-		const int ngroups = min(J.groups - g_begin, t_end - t);
-		t += ngroups;
-		load_bases(p, J, g_begin, ngroups);
-		chain_item<H_FIRST, KV, KH, true>(p, L, J, jobs ? J.tmap : static_cast<const void *>(&single_map), strip,
-		                                  g_begin, ngroups);
-		p.base += ngroups;
-		__syncthreads();  // the next item rewrites the group bases and the ring
-		if (abort_item)
-			break;
+	int r_begin[2], r_end[2];
+	if (ranges) {
+		r_begin[0] = __ldg(ranges + 4 * blockIdx.x);
+		r_end[0] = __ldg(ranges + 4 * blockIdx.x + 1);
+		r_begin[1] = __ldg(ranges + 4 * blockIdx.x + 2);
+		r_end[1] = __ldg(ranges + 4 * blockIdx.x + 3);
+	} else {
+		r_begin[0] = static_cast<int>(static_cast<long long>(blockIdx.x) * total_items / gridDim.x);
+		r_end[0] = static_cast<int>(static_cast<long long>(blockIdx.x + 1) * total_items / gridDim.x);
+		r_begin[1] = r_end[1] = 0;
+	}
+	for (int r = 0; r < 2 && !abort_item; ++r) {
+		const int t_end = r_end[r];
+		for (int t = r_begin[r]; t < t_end;) {
+			const FusedJob &J = jobs ? jobs[find_job(jobs, num_jobs, t)] : single;
+			const int local = t - J.item_begin;
+			const int strip = local / J.groups;
+			const int g_begin = local - strip * J.groups;
+			const int ngroups = min(J.groups - g_begin, t_end - t);
+			t += ngroups;
+			load_bases(p, J, g_begin, ngroups);
+			chain_item<H_FIRST, KV, KH, true>(p, L, J, jobs ? J.tmap : static_cast<const void *>(&single_map), strip,
+			                                  g_begin, ngroups);
+			p.base += ngroups;
+			__syncthreads();  // the next item rewrites the group bases and the ring
+			if (abort_item)
+				break;
+		}
 	}
 	pipe_finish(p);
 }

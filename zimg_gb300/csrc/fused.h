@@ -173,8 +173,17 @@ bool chain_tma_enabled();  // false when the environment sets ZG_CHAIN_TMA=0
 bool chain_tma_layout(const FusedPlan *const *plans, int n, SmemLayout *out);
 bool chain_tma_source_map(CUtensorMap *map, const FusedJob &j, const SmemLayout &L);
 int chain_tma_grid_size(int variant, size_t smem_bytes);
-cudaError_t launch_chain_tma(int variant, const FusedJob *jobs, int num_jobs, int total_items, const SmemLayout &L,
-                             int grid, const FusedJob &single, const CUtensorMap *single_map, cudaStream_t stream);
+// ranges: null (each CTA an equal contiguous range of the units), or 4 ints
+// per CTA of `grid`, two unit ranges each CTA runs in order
+// (chain_tma_lockstep_ranges).
+cudaError_t launch_chain_tma(int variant, const FusedJob *jobs, int num_jobs, int total_items, const int *ranges,
+                             const SmemLayout &L, int grid, const FusedJob &single, const CUtensorMap *single_map,
+                             cudaStream_t stream);
+// Per-CTA unit ranges for `grid` CTAs over jobs of `groups` units per strip
+// and `total_items` units: CTA b first the whole strip b, then an equal share
+// of the strips beyond the first `grid`. Empty when there are fewer strips
+// than CTAs (equal ranges then).
+std::vector<int> chain_tma_lockstep_ranges(int total_items, int groups, int grid);
 // Nonzero when a pipeline wait of that kernel ran out (optionally reset).
 int chain_tma_pipeline_error(bool reset);
 // One launch over a mixed batch (chained jobs of any variant, each FusedJob's
