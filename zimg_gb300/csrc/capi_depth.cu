@@ -2,6 +2,7 @@
 // device planes. The choice of conversion and its constants follow
 // src/zimg/depth/depth.cpp:43-66 and quantize.h:19-45.
 #include <cstdint>
+#include <cstdlib>
 #include <string>
 
 #include "capi_common.h"
@@ -141,6 +142,9 @@ zg_error_code zg_depth_create(const zg_depth_params *params, zg_depth **out)
 			d->ed.offset = d->offset;
 			d->ed.vmax = d->vmax;
 			d->ed_warps = ed_choose_warps(d->ed.width, d->ed.height);
+			// tuning override: warps per block (a bad value fails below)
+			if (const char *env = std::getenv("ZG_ED_WARPS"))
+				d->ed_warps = std::atoi(env);
 			if (q.width > (1u << 30) || q.height > (1u << 30) || !d->ed_warps ||
 			    !ed_shape(d->ed, d->ed_warps, &d->ed_ring))
 				throw Error(kErrUnsupported, "plane too wide for error diffusion in this library");

@@ -40,36 +40,34 @@ constexpr int kMinSpacing = ((kTail + 3 + kEdChunk + kEdChunk - 1) / kEdChunk) *
 constexpr int kMaxWarps = 32;
 constexpr size_t kMaxSmem = 227 * 1024;
 
-// Where warp w of nw is on global step S0 (a multiple of kEdChunk): the band
-// it owns and the band's step; live while that band has work left.
+// Where a warp is on the current chunk: the band it owns and the band's
+// step; live while that band has work left. Warp w starts at global step
+// w * spacing and moves to band + warps every `cycle` steps.
 struct Where {
 	int band, step;
 	bool live;
 };
 
-__device__ __forceinline__ Where where_at(const EdPlane &p, int w, int nw, int s0)
+__device__ __forceinline__ bool where_live(const Where &x, int rel, const EdPlane &p)
 {
-	Where r{ 0, 0, false };
-	const int rel = s0 - w * p.spacing;
-	if (rel < 0)
-		return r;
-	const int k = rel / p.cycle;
-	r.band = w + k * nw;
-	r.step = rel - k * p.cycle;
-	r.live = r.band < p.bands && r.step < kTail + p.width;
-	return r;
+	return rel >= 0 && x.band < p.bands && x.step < kTail + p.width;
 }
 
-template <class T>
-__device__ __forceinline__ const T *line_ptr(const EdPlane &p, int row)
+// The next chunk's position (rel: global step - w * spacing, advanced here).
+__device__ __forceinline__ void where_next(Where &x, int &rel, int w, int nw, const EdPlane &p)
 {
-	return reinterpret_cast<const T *>(static_cast<const char *>(p.src) + static_cast<ptrdiff_t>(row) * p.src_stride);
-}
-
-template <class U>
-__device__ __forceinline__ U *out_ptr(const EdPlane &p, int row)
-{
-	return reinterpret_cast<U *>(static_cast<char *>(p.dst) + static_cast<ptrdiff_t>(row) * p.dst_stride);
+	rel += kEdChunk;
+	if (rel == 0) {
+		x.band = w;
+		x.step = 0;
+	} else if (rel > 0) {
+		x.step += kEdChunk;
+		if (x.step >= p.cycle) {
+			x.step -= p.cycle;
+			x.band += nw;
+		}
+	}
+	x.live = where_live(x, rel, p);
 }
 
 template <class T, class U>
@@ -91,22 +89,36 @@ __global__ void __launch_bounds__(kMaxWarps * 32) ed_kernel(const __grid_constan
 
 	T pre[kEdChunk];
 	auto fetch = [&](const Where &wh) {
+		if (!wh.live) {
+#pragma unroll
+			for (int j = 0; j < kEdChunk; ++j)
+				pre[j] = T{};
+			return;
+		}
+		const int rows_left = H - wh.band * kBandLines - half;  // line 2j + half exists iff 2j < rows_left
+		const char *base = static_cast<const char *>(p.src) +
+		                   static_cast<ptrdiff_t>(wh.band * kBandLines + half) * p.src_stride;
+		const ptrdiff_t step2 = 2 * p.src_stride;
+		const int cb = wh.step + t16 - kEdLag * half;
 #pragma unroll
 		for (int j = 0; j < kEdChunk; ++j) {
-			const int l = 2 * j + half, row = wh.band * kBandLines + l;
-			const int c = wh.step + t16 - kEdLag * l;
-			const bool ok = wh.live && row < H && static_cast<unsigned>(c) < static_cast<unsigned>(W);
-			pre[j] = ok ? line_ptr<T>(p, row)[c] : T{};
+			const int c = cb - 2 * kEdLag * j;
+			const bool ok = 2 * j < rows_left && static_cast<unsigned>(c) < static_cast<unsigned>(W);
+			pre[j] = ok ? reinterpret_cast<const T *>(base + j * step2)[c] : T{};
 		}
 	};
 
 	// errors: left neighbour; h2 / h3 / h4 the line above at columns c + 1,
 	// c, c - 1 for this step, h1 the one for the next step
 	float left = 0.0f, h1 = 0.0f, h2 = 0.0f, h3 = 0.0f, h4 = 0.0f;
-	Where cur = where_at(p, w, nw, 0);
+	int rel = -w * p.spacing;
+	Where cur{ w, 0, false };
+	cur.live = where_live(cur, rel, p);
 	fetch(cur);
 	for (int s0 = 0; s0 < p.steps; s0 += kEdChunk) {
-		const Where nxt = where_at(p, w, nw, s0 + kEdChunk);
+		Where nxt = cur;
+		int rel_next = rel;
+		where_next(nxt, rel_next, w, nw, p);
 		if (cur.live) {
 			// x = sample * scale + offset, two roundings (dither.cpp:76)
 #pragma unroll
@@ -128,37 +140,44 @@ __global__ void __launch_bounds__(kMaxWarps * 32) ed_kernel(const __grid_constan
 				}
 			}
 			const bool row_ok = cur.band * kBandLines + lane < H;
+			const bool above = cur.band > 0;
+			const int c0 = cur.step - kEdLag * lane;
+			// Branch-free steps: every lane computes, inactive lanes (before
+			// or after their line, or below the plane) keep a zero error.
 #pragma unroll
 			for (int t = 0; t < kEdChunk; ++t) {
-				const int c = cur.step + t - kEdLag * lane;
-				float e = 0.0f;
-				if (row_ok && static_cast<unsigned>(c) < static_cast<unsigned>(W)) {
-					// 0 + left * 7/16 + top-right * 3/16 + top * 5/16 +
-					// top-left * 1/16, in that order (dither.cpp:78-83)
-					float err = __fadd_rn(0.0f, __fmul_rn(left, 0.4375f));
-					err = __fadd_rn(err, __fmul_rn(h2, 0.1875f));
-					err = __fadd_rn(err, __fmul_rn(h3, 0.3125f));
-					err = __fadd_rn(err, __fmul_rn(h4, 0.0625f));
-					float x = __fadd_rn(tile_in[lane * kEdPitch + t], err);
-					// std::clamp: a NaN passes through
-					x = x < 0.0f ? 0.0f : (vmax < x ? vmax : x);
-					// nearest even: x + 1.5 * 2^23 has an ulp of 1 for
-					// 0 <= x < 2^22; lrint of a NaN stores 0
-					const float r = __fadd_rn(x, 12582912.0f);
-					const bool nan = x != x;
-					const float y = nan ? 0.0f : __fsub_rn(r, 12582912.0f);
-					tile_out[lane * kEdPitch + t] = nan ? 0u : (__float_as_uint(r) & 0xFFFFu);
-					e = __fsub_rn(x, y);
-					if (lane == kBandLines - 1)
-						ring[c & rmask] = e;
-				}
+				const int c = c0 + t;
+				const bool act = row_ok && static_cast<unsigned>(c) < static_cast<unsigned>(W);
+				// left * 7/16 + top-right * 3/16 + top * 5/16 + top-left *
+				// 1/16, in that order (dither.cpp:78-83). zimg's sum starts
+				// from 0, which only turns a -0 into +0: the sample's base is
+				// never -0 (x * scale + offset with offset never -0), so a
+				// zero's sign cannot reach x and the start is left out.
+				float err = __fmul_rn(left, 0.4375f);
+				err = __fadd_rn(err, __fmul_rn(h2, 0.1875f));
+				err = __fadd_rn(err, __fmul_rn(h3, 0.3125f));
+				err = __fadd_rn(err, __fmul_rn(h4, 0.0625f));
+				const float x = __fadd_rn(tile_in[lane * kEdPitch + t], err);
+				// std::clamp to [0, vmax] (x is never -0); a NaN clamps to 0
+				// here, stores 0 as zimg's lrint does, and keeps its NaN as
+				// the error below
+				const float xc = fminf(fmaxf(x, 0.0f), vmax);
+				// nearest even: xc + 1.5 * 2^23 has an ulp of 1 for
+				// 0 <= xc < 2^22
+				const float r = __fadd_rn(xc, 12582912.0f);
+				const float y = __fsub_rn(r, 12582912.0f);
+				tile_out[lane * kEdPitch + t] = __float_as_uint(r) & 0xFFFFu;
+				const float e = act ? (x != x ? x : __fsub_rn(xc, y)) : 0.0f;
+				if (lane == kBandLines - 1 && act)
+					ring[c & rmask] = e;
 				left = e;
-				float u = __shfl_up_sync(0xffffffffu, e, 1);
-				if (lane == 0) {
-					const int c3 = c + kEdLag;
-					u = (cur.band > 0 && static_cast<unsigned>(c3) < static_cast<unsigned>(W)) ? ring_above[c3 & rmask]
-					                                                                            : 0.0f;
-				}
+				const float down = __shfl_up_sync(0xffffffffu, e, 1);
+				// line 0 reads the previous band's last line instead; every
+				// lane loads its slot (lanes are 3 columns apart: distinct
+				// banks) and line 0 keeps it
+				const int c3 = c + kEdLag;
+				const float ra = ring_above[c3 & rmask];
+				const float u = lane != 0 ? down : ((above && static_cast<unsigned>(c3) < static_cast<unsigned>(W)) ? ra : 0.0f);
 				h4 = h3;
 				h3 = h2;
 				h2 = h1;
@@ -167,17 +186,21 @@ __global__ void __launch_bounds__(kMaxWarps * 32) ed_kernel(const __grid_constan
 		}
 		__syncwarp();
 		if (cur.live) {
+			const int rows_left = H - cur.band * kBandLines - half;
+			char *base = static_cast<char *>(p.dst) + static_cast<ptrdiff_t>(cur.band * kBandLines + half) * p.dst_stride;
+			const ptrdiff_t step2 = 2 * p.dst_stride;
+			const int cb = cur.step + t16 - kEdLag * half;
 #pragma unroll
 			for (int j = 0; j < kEdChunk; ++j) {
-				const int l = 2 * j + half, row = cur.band * kBandLines + l;
-				const int c = cur.step + t16 - kEdLag * l;
-				if (row < H && static_cast<unsigned>(c) < static_cast<unsigned>(W))
-					out_ptr<U>(p, row)[c] = static_cast<U>(tile_out[l * kEdPitch + t16]);
+				const int c = cb - 2 * kEdLag * j;
+				if (2 * j < rows_left && static_cast<unsigned>(c) < static_cast<unsigned>(W))
+					reinterpret_cast<U *>(base + j * step2)[c] = static_cast<U>(tile_out[(2 * j + half) * kEdPitch + t16]);
 			}
 		}
 		// ring writes of this chunk become visible to the next band's warp
 		__syncthreads();
 		cur = nxt;
+		rel = rel_next;
 	}
 }
 
@@ -257,9 +280,10 @@ int ed_choose_warps(int width, int height)
 	const int bands = (height + kBandLines - 1) / kBandLines;
 	if (bands <= 1)
 		return 1;
-	// one step of a warp: a chain of ~12 dependent operations (~48 cycles),
-	// ~26 issued instructions; four schedulers share the warps in flight
-	constexpr double kChain = 48.0, kIssue = 26.0;
+	// one step of a warp: ~190 cycles of latency, plus ~54 issued
+	// instructions per warp in flight over four schedulers (fitted to
+	// measured 540p, 1080p and 2160p planes at 4 to 32 warps)
+	constexpr double kChain = 190.0, kIssue = 54.0;
 	int best = 0;
 	double best_cost = 0.0;
 	for (int nw = 2; nw <= kMaxWarps; ++nw) {
@@ -270,7 +294,7 @@ int ed_choose_warps(int width, int height)
 		if (!ed_shape(p, nw, &ring))
 			continue;
 		const int in_flight = std::min({ nw, bands, (kTail + width + p.spacing - 1) / p.spacing });
-		const double cost = static_cast<double>(p.steps) * std::max(kChain, in_flight * kIssue / 4.0);
+		const double cost = static_cast<double>(p.steps) * (kChain + in_flight * kIssue / 4.0);
 		if (!best || cost < best_cost) {
 			best = nw;
 			best_cost = cost;
