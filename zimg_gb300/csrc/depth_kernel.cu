@@ -156,39 +156,42 @@ __device__ __forceinline__ void store_run(U *p, const uint32_t (&r)[kRun], int n
 	}
 }
 
-// MODE 1: left shift; 2: to float; 3: dither to integer.
-template <class T, class U, int MODE>
+// MODE 1: left shift; 2: to float; 3: dither to integer. DITHER (MODE 3):
+// 0 none, 1 ordered, 2 random.
+template <class T, class U, int MODE, int DITHER>
 __global__ void __launch_bounds__(kThreads)
 depth_kernel(DepthLaunch L)
 {
-	// this plane's dither values at (line mod 64, column mod 64), row-major;
-	// the 16 x 16 ordered matrix repeats four times across and down
-	__shared__ __align__(16) float table[MODE == 3 ? 64 * 64 : 4];
-	if (MODE == 3) {
-		for (int t = threadIdx.x; t < 64 * 64; t += kThreads) {
-			const unsigned i = t >> 6, j = t & 63;
-			float v = 0.0f;
-			unsigned m = 0;
-			if (L.dither == 1) {
-				// variants by plane (dither.cpp:170-186): as is, mirrored
-				// left-right, top-bottom, transposed
-				const unsigned s = L.seq & 3, i4 = i & 15, j4 = j & 15;
-				const unsigned ii = s == 2 ? 15 - i4 : (s == 3 ? j4 : i4);
-				const unsigned jj = s == 1 ? 15 - j4 : (s == 3 ? i4 : j4);
-				m = bayer16(ii, jj);
-			} else if (L.dither == 2) {
-				// entry (line + voff, column + hoff) mod 64, (hoff, voff)
-				// by plane (dither.cpp:226-233)
-				const unsigned s = L.seq & 3;
-				const unsigned hoff = s == 1 ? 32 : (s == 2 ? 16 : (s == 3 ? 48 : 0));
-				const unsigned voff = s == 1 ? 12 : (s == 2 ? 55 : (s == 3 ? 26 : 0));
-				const unsigned k = ((i + voff) & 63) * 64 + ((j + hoff) & 63);
-				m = (kBlueNoiseWords[k >> 2] >> (8 * (k & 3))) & 0xFFu;
-			}
+	// ORDERED: this plane's 16 x 16 dither values, row-major. RANDOM: the
+	// values (m + 1) / 257 - 1/2 of the 256 matrix entries m, and the
+	// plane's 64 x 64 entries already moved by its offsets, four per word.
+	__shared__ __align__(16) float table[DITHER == 1 ? 256 : (DITHER == 2 ? 256 : 4)];
+	__shared__ __align__(16) uint32_t noise[DITHER == 2 ? 1024 : 1];
+	if (MODE == 3 && DITHER == 1) {
+		for (int t = threadIdx.x; t < 256; t += kThreads) {
+			const unsigned i = t >> 4, j = t & 15;
+			// variants by plane (dither.cpp:170-186): as is, mirrored
+			// left-right, top-bottom, transposed
+			const unsigned s = L.seq & 3;
+			const unsigned ii = s == 2 ? 15 - i : (s == 3 ? j : i);
+			const unsigned jj = s == 1 ? 15 - j : (s == 3 ? i : j);
 			// (m + 1) / 257 - 1/2 in float (dither.cpp:157-167)
-			if (L.dither)
-				v = __fsub_rn(__fdiv_rn(static_cast<float>(m + 1), 257.0f), 0.5f);
-			table[t] = v;
+			table[t] = __fsub_rn(__fdiv_rn(static_cast<float>(bayer16(ii, jj) + 1), 257.0f), 0.5f);
+		}
+		__syncthreads();
+	}
+	if (MODE == 3 && DITHER == 2) {
+		for (int t = threadIdx.x; t < 256; t += kThreads)
+			table[t] = __fsub_rn(__fdiv_rn(static_cast<float>(t + 1), 257.0f), 0.5f);
+		// entry (line + voff, column + hoff) mod 64, (hoff, voff) by plane
+		// (dither.cpp:226-233); hoff is a multiple of 4, so rows rotate by
+		// whole words
+		const unsigned s = L.seq & 3;
+		const unsigned hoff = s == 1 ? 32 : (s == 2 ? 16 : (s == 3 ? 48 : 0));
+		const unsigned voff = s == 1 ? 12 : (s == 2 ? 55 : (s == 3 ? 26 : 0));
+		for (int t = threadIdx.x; t < 1024; t += kThreads) {
+			const unsigned i = t >> 4, wj = t & 15;
+			noise[t] = kBlueNoiseWords[((i + voff) & 63) * 16 + ((wj + hoff / 4) & 15)];
 		}
 		__syncthreads();
 	}
@@ -204,7 +207,7 @@ depth_kernel(DepthLaunch L)
 		{
 			const T *srow = reinterpret_cast<const T *>(static_cast<const char *>(L.src) + static_cast<ptrdiff_t>(i) * L.src_stride);
 			U *drow = reinterpret_cast<U *>(static_cast<char *>(L.dst) + static_cast<ptrdiff_t>(i) * L.dst_stride);
-			const float *trow = table + ((i & 63) << 6);
+			const float *trow = table + ((i & 15) << 4);
 			const int j0 = r * kRun;
 			const int n = min(kRun, L.width - j0);
 			const T *s = srow + j0;
@@ -252,9 +255,22 @@ depth_kernel(DepthLaunch L)
 						q[e] = static_cast<uint32_t>(x[e]) << L.shift;
 				} else {
 					// the run's 8 dither values: j0 is a multiple of 8
-					const float4 t0 = *reinterpret_cast<const float4 *>(trow + (j0 & 63));
-					const float4 t1 = *reinterpret_cast<const float4 *>(trow + (j0 & 63) + 4);
-					const float dv[kRun] = { t0.x, t0.y, t0.z, t0.w, t1.x, t1.y, t1.z, t1.w };
+					float dv[kRun];
+					if constexpr (DITHER == 1) {
+						const float4 t0 = *reinterpret_cast<const float4 *>(trow + (j0 & 15));
+						const float4 t1 = *reinterpret_cast<const float4 *>(trow + (j0 & 15) + 4);
+						dv[0] = t0.x; dv[1] = t0.y; dv[2] = t0.z; dv[3] = t0.w;
+						dv[4] = t1.x; dv[5] = t1.y; dv[6] = t1.z; dv[7] = t1.w;
+					} else if constexpr (DITHER == 2) {
+						const uint2 m8 = *reinterpret_cast<const uint2 *>(noise + (i & 63) * 16 + ((j0 & 63) >> 2));
+#pragma unroll
+						for (int e = 0; e < kRun; ++e)
+							dv[e] = table[((e < 4 ? m8.x : m8.y) >> (8 * (e & 3))) & 0xFFu];
+					} else {
+#pragma unroll
+						for (int e = 0; e < kRun; ++e)
+							dv[e] = 0.0f;
+					}
 #pragma unroll
 					for (int e = 0; e < kRun; ++e) {
 						float v = __fadd_rn(__fmul_rn(x[e], L.scale), L.offset);
@@ -286,19 +302,24 @@ cudaError_t launch_tu(int mode, const DepthLaunch &L, int grid, cudaStream_t st)
 	switch (mode) {
 	case 1:
 		if constexpr (is_int<T> && is_int<U>) {
-			depth_kernel<T, U, 1><<<grid, kThreads, 0, st>>>(L);
+			depth_kernel<T, U, 1, 0><<<grid, kThreads, 0, st>>>(L);
 			return cudaGetLastError();
 		}
 		return cudaErrorInvalidValue;
 	case 2:
 		if constexpr (is_fp<U>) {
-			depth_kernel<T, U, 2><<<grid, kThreads, 0, st>>>(L);
+			depth_kernel<T, U, 2, 0><<<grid, kThreads, 0, st>>>(L);
 			return cudaGetLastError();
 		}
 		return cudaErrorInvalidValue;
 	case 3:
 		if constexpr (is_int<U>) {
-			depth_kernel<T, U, 3><<<grid, kThreads, 0, st>>>(L);
+			if (L.dither == 1)
+				depth_kernel<T, U, 3, 1><<<grid, kThreads, 0, st>>>(L);
+			else if (L.dither == 2)
+				depth_kernel<T, U, 3, 2><<<grid, kThreads, 0, st>>>(L);
+			else
+				depth_kernel<T, U, 3, 0><<<grid, kThreads, 0, st>>>(L);
 			return cudaGetLastError();
 		}
 		return cudaErrorInvalidValue;
