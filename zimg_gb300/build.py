@@ -28,9 +28,8 @@ SOURCES = ["filter_plan.cpp", "capi.cu", "capi_graph.cu", "capi_batch.cu", "capi
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
-# Per-file flags: the colorspace kernel rounds every product and sum on its
-# own, as zimg's C code does (no multiply-add contraction on the device).
-FILE_FLAGS = {"colorspace_kernel.cu": ["-fmad=false"]}
+# Per-file nvcc flags (none at present).
+FILE_FLAGS: dict[str, list[str]] = {}
 
 
 def _nvcc() -> str:

@@ -4,8 +4,9 @@
 // in registers, one pass over the planes. HBM-bound for matrix-only plans
 // (12 bytes read and 12 written per pixel); transfer functions add a few
 // dozen instructions per channel. Each thread converts runs of 4 pixels of a
-// line (16-byte vectors where all planes allow). Compiled without
-// multiply-add contraction: every product and sum rounds as in zimg's C code.
+// line (16-byte vectors where all planes allow). Every product, sum and
+// quotient is written with the separately rounding CS_* forms, as zimg's C
+// code rounds them.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -25,65 +26,66 @@ __device__ __forceinline__ void apply_op(const Op &o, float &a, float &b, float 
 {
 	switch (o.kind) {
 	case OP_MATRIX: {
-		const float x = o.m[0][0] * a + o.m[0][1] * b + o.m[0][2] * c;
-		const float y = o.m[1][0] * a + o.m[1][1] * b + o.m[1][2] * c;
-		const float z = o.m[2][0] * a + o.m[2][1] * b + o.m[2][2] * c;
+		const float x = CS_ADD(CS_ADD(CS_MUL(o.m[0][0], a), CS_MUL(o.m[0][1], b)), CS_MUL(o.m[0][2], c));
+		const float y = CS_ADD(CS_ADD(CS_MUL(o.m[1][0], a), CS_MUL(o.m[1][1], b)), CS_MUL(o.m[1][2], c));
+		const float z = CS_ADD(CS_ADD(CS_MUL(o.m[2][0], a), CS_MUL(o.m[2][1], b)), CS_MUL(o.m[2][2], c));
 		a = x;
 		b = y;
 		c = z;
 		break;
 	}
 	case OP_GAMMA:
-		a = o.post * apply_tf(o.f, a * o.pre);
-		b = o.post * apply_tf(o.f, b * o.pre);
-		c = o.post * apply_tf(o.f, c * o.pre);
+		a = CS_MUL(o.post, apply_tf(o.f, CS_MUL(a, o.pre)));
+		b = CS_MUL(o.post, apply_tf(o.f, CS_MUL(b, o.pre)));
+		c = CS_MUL(o.post, apply_tf(o.f, CS_MUL(c, o.pre)));
 		break;
 	case OP_HLG: {
 		// display-referred HLG: system gamma 1.2 on the luma (operation_impl.cpp:76-114)
 		const float gamma = 1.2f;
-		const float r = a * o.scale, g = b * o.scale, bb = c * o.scale;
-		float yd = o.kr * r + o.kg * g + o.kb * bb;
+		const float r = CS_MUL(a, o.scale), g = CS_MUL(b, o.scale), bb = CS_MUL(c, o.scale);
+		float yd = CS_ADD(CS_ADD(CS_MUL(o.kr, r), CS_MUL(o.kg, g)), CS_MUL(o.kb, bb));
 		yd = yd < FLT_MIN ? FLT_MIN : yd;
 		const float ys_inv = powf(yd, (1.0f - gamma) / gamma);
-		a = hlg_oetf(r * ys_inv);
-		b = hlg_oetf(g * ys_inv);
-		c = hlg_oetf(bb * ys_inv);
+		a = hlg_oetf(CS_MUL(r, ys_inv));
+		b = hlg_oetf(CS_MUL(g, ys_inv));
+		c = hlg_oetf(CS_MUL(bb, ys_inv));
 		break;
 	}
 	case OP_HLG_INV: {
 		const float gamma = 1.2f;
 		float r = hlg_inv_oetf(a), g = hlg_inv_oetf(b), bb = hlg_inv_oetf(c);
-		float ys = o.kr * r + o.kg * g + o.kb * bb;
+		float ys = CS_ADD(CS_ADD(CS_MUL(o.kr, r), CS_MUL(o.kg, g)), CS_MUL(o.kb, bb));
 		ys = ys < FLT_MIN ? FLT_MIN : ys;
 		ys = powf(ys, gamma - 1.0f);
-		r = r * ys;
-		g = g * ys;
-		bb = bb * ys;
-		a = r * o.scale;
-		b = g * o.scale;
-		c = bb * o.scale;
+		r = CS_MUL(r, ys);
+		g = CS_MUL(g, ys);
+		bb = CS_MUL(bb, ys);
+		a = CS_MUL(r, o.scale);
+		b = CS_MUL(g, o.scale);
+		c = CS_MUL(bb, o.scale);
 		break;
 	}
 	case OP_CL_TO_RGB: {
 		// BT.2020 constant luminance to linear RGB (operation_impl.cpp:156-206)
 		const float y = a, u = b, v = c;
-		const float bmy = u < 0 ? u * 2.0f * o.nb : u * 2.0f * o.pb;
-		const float rmy = v < 0 ? v * 2.0f * o.nr : v * 2.0f * o.pr;
-		const float bl = apply_tf(o.f, bmy + y), rl = apply_tf(o.f, rmy + y), yl = apply_tf(o.f, y);
-		const float g = (yl - o.kr * rl - o.kb * bl) / o.kg;
-		a = rl * o.scale;
-		b = g * o.scale;
-		c = bl * o.scale;
+		const float bmy = u < 0 ? CS_MUL(CS_MUL(u, 2.0f), o.nb) : CS_MUL(CS_MUL(u, 2.0f), o.pb);
+		const float rmy = v < 0 ? CS_MUL(CS_MUL(v, 2.0f), o.nr) : CS_MUL(CS_MUL(v, 2.0f), o.pr);
+		const float bl = apply_tf(o.f, CS_ADD(bmy, y)), rl = apply_tf(o.f, CS_ADD(rmy, y)), yl = apply_tf(o.f, y);
+		const float g = CS_DIV(CS_SUB(CS_SUB(yl, CS_MUL(o.kr, rl)), CS_MUL(o.kb, bl)), o.kg);
+		a = CS_MUL(rl, o.scale);
+		b = CS_MUL(g, o.scale);
+		c = CS_MUL(bl, o.scale);
 		break;
 	}
 	case OP_CL_TO_YUV: {
 		// linear RGB to BT.2020 constant luminance (operation_impl.cpp:209-258)
-		float r = a * o.scale, g = b * o.scale, bb = c * o.scale;
-		const float y = apply_tf(o.f, o.kr * r + o.kg * g + o.kb * bb);
+		float r = CS_MUL(a, o.scale), g = CS_MUL(b, o.scale), bb = CS_MUL(c, o.scale);
+		const float y = apply_tf(o.f, CS_ADD(CS_ADD(CS_MUL(o.kr, r), CS_MUL(o.kg, g)), CS_MUL(o.kb, bb)));
 		bb = apply_tf(o.f, bb);
 		r = apply_tf(o.f, r);
-		const float u = (bb - y < 0.0f) ? (bb - y) / (2.0f * o.nb) : (bb - y) / (2.0f * o.pb);
-		const float v = (r - y < 0.0f) ? (r - y) / (2.0f * o.nr) : (r - y) / (2.0f * o.pr);
+		const float bmy = CS_SUB(bb, y), rmy = CS_SUB(r, y);
+		const float u = bmy < 0.0f ? CS_DIV(bmy, CS_MUL(2.0f, o.nb)) : CS_DIV(bmy, CS_MUL(2.0f, o.pb));
+		const float v = rmy < 0.0f ? CS_DIV(rmy, CS_MUL(2.0f, o.nr)) : CS_DIV(rmy, CS_MUL(2.0f, o.pr));
 		a = y;
 		b = u;
 		c = v;
