@@ -261,12 +261,13 @@ __device__ __forceinline__ void h_pass(const Item &it, const char *smem, const S
 		const bool two = y + 1 < b;
 		const float *r0p = in + (y & imask) * pitch + l;
 		const float *r1p = in + ((y + 1) & imask) * pitch + l;
-		float acc0 = init, acc1 = init;
+		// the two lines in one paired FMA per tap (two independent
+		// round-to-nearest FMAs, as the scalar form)
+		float2 acc = make_float2(init, init);
 #pragma unroll
-		for (int k = 0; k < HW; ++k) {
-			acc0 = __fmaf_rn(taps[k], r0p[k], acc0);
-			acc1 = __fmaf_rn(taps[k], r1p[k], acc1);
-		}
+		for (int k = 0; k < HW; ++k)
+			acc = __ffma2_rn(make_float2(taps[k], taps[k]), make_float2(r0p[k], r1p[k]), acc);
+		const float acc0 = acc.x, acc1 = acc.y;
 		if (!FINAL) {
 			float v0 = acc0, v1 = acc1;
 			if (U16) {
@@ -318,15 +319,17 @@ __device__ __forceinline__ void v_pass(const Item &it, const char *smem, const S
 		for (int s = 0; s < VS; ++s)
 			off[s] = ((base + s) & imask) * in_pitch;
 		for (int q = (warp % wpg) * 32 + lane; q < quads; q += wpg * 32) {
-			float acc[kGroup][4];
+			// columns (0, 1) and (2, 3) of each row in paired FMAs: two
+			// independent round-to-nearest FMAs per instruction, the same
+			// results as four scalar ones
+			float2 acc2[kGroup][2];
 #pragma unroll
 			for (int j = 0; j < kGroup; ++j)
-#pragma unroll
-				for (int e = 0; e < 4; ++e)
-					acc[j][e] = init;
+				acc2[j][0] = acc2[j][1] = make_float2(init, init);
 #pragma unroll
 			for (int s = 0; s < VS; ++s) {
 				const float4 x = *reinterpret_cast<const float4 *>(in + off[s] + 4 * q);
+				const float2 x01 = make_float2(x.x, x.y), x23 = make_float2(x.z, x.w);
 				float cj[kGroup];
 				if constexpr (kGroup == 4) {
 					const float4 c4 = reinterpret_cast<const float4 *>(cf)[s];
@@ -341,11 +344,18 @@ __device__ __forceinline__ void v_pass(const Item &it, const char *smem, const S
 				}
 #pragma unroll
 				for (int j = 0; j < kGroup; ++j) {
-					acc[j][0] = __fmaf_rn(cj[j], x.x, acc[j][0]);
-					acc[j][1] = __fmaf_rn(cj[j], x.y, acc[j][1]);
-					acc[j][2] = __fmaf_rn(cj[j], x.z, acc[j][2]);
-					acc[j][3] = __fmaf_rn(cj[j], x.w, acc[j][3]);
+					const float2 cc = make_float2(cj[j], cj[j]);
+					acc2[j][0] = __ffma2_rn(cc, x01, acc2[j][0]);
+					acc2[j][1] = __ffma2_rn(cc, x23, acc2[j][1]);
 				}
+			}
+			float acc[kGroup][4];
+#pragma unroll
+			for (int j = 0; j < kGroup; ++j) {
+				acc[j][0] = acc2[j][0].x;
+				acc[j][1] = acc2[j][0].y;
+				acc[j][2] = acc2[j][1].x;
+				acc[j][3] = acc2[j][1].y;
 			}
 #pragma unroll
 			for (int j = 0; j < kGroup; ++j) {
