@@ -97,6 +97,20 @@ bool aligned(const void *p, ptrdiff_t stride, unsigned a)
 
 } // namespace
 
+namespace zg {
+
+bool depth_ed_plane(const ::zg_depth *d, EdPlane *plane, int *in_type, int *out_type)
+{
+	if (!d || d->mode != 3 || d->params.dither_type != ZG_DITHER_ERROR_DIFFUSION)
+		return false;
+	*plane = d->ed;
+	*in_type = type_code(d->params.pixel_in.type);
+	*out_type = type_code(d->params.pixel_out.type);
+	return true;
+}
+
+} // namespace zg
+
 extern "C" {
 
 zg_error_code zg_depth_create(const zg_depth_params *params, zg_depth **out)

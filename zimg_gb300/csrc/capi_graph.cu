@@ -8,10 +8,12 @@
 // mapping of resize_plane (graphbuilder.cpp:769-776).
 #include "capi_common.h"
 #include "alpha.h"
+#include "depth.h"
 #include "colorspace_plan.h"
 
 #include <cfloat>
 #include <cmath>
+#include <vector>
 
 using namespace zg;
 
@@ -443,6 +445,66 @@ void run_chain(const Chain &c, const void *src, ptrdiff_t ss, void *dst, ptrdiff
 		run_depth(c.post, rd, rds, dst, ds, st);
 }
 
+// Error-diffusion conversions of a frame's planes, side by side: one launch
+// per run of up to kEdMaxPlanes planes of the same pixel types, every block
+// with the most warps any of them wants; a plane whose shape does not fit
+// that launch runs on its own.
+template <class D>
+void run_ed_planes(const D *items, int n, zg_stream stream)
+{
+	cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+	std::vector<bool> done(n, false);
+	for (int a = 0; a < n; ++a) {
+		if (done[a])
+			continue;
+		EdPlane pa;
+		int it = 0, ot = 0;
+		depth_ed_plane(items[a].d, &pa, &it, &ot);
+		std::vector<int> group{ a };
+		for (int b = a + 1; b < n && static_cast<int>(group.size()) < kEdMaxPlanes; ++b) {
+			EdPlane pb;
+			int it2 = 0, ot2 = 0;
+			if (!done[b] && depth_ed_plane(items[b].d, &pb, &it2, &ot2) && it2 == it && ot2 == ot)
+				group.push_back(b);
+		}
+		int warps = 1;
+		for (int k : group) {
+			EdPlane q;
+			int i2 = 0, o2 = 0;
+			depth_ed_plane(items[k].d, &q, &i2, &o2);
+			warps = std::max(warps, ed_choose_warps(q.width, q.height));
+		}
+		EdLaunch E{};
+		E.in_type = it;
+		E.out_type = ot;
+		E.warps = warps;
+		E.ring = 1;
+		bool ok = true;
+		for (int k : group) {
+			EdPlane q;
+			int i2 = 0, o2 = 0;
+			depth_ed_plane(items[k].d, &q, &i2, &o2);
+			int ring = 0;
+			ok = ok && ed_shape(q, warps, &ring);
+			q.src = items[k].src;
+			q.src_stride = items[k].ss;
+			q.dst = items[k].dst;
+			q.dst_stride = items[k].ds;
+			E.planes[E.num_planes++] = q;
+			E.ring = std::max(E.ring, ring);
+		}
+		ok = ok && ed_smem_bytes(warps, E.ring) <= 227 * 1024;
+		if (ok) {
+			cuda_check(launch_error_diffusion(E, st), "error diffusion launch");
+		} else {
+			for (int k : group)
+				run_depth(items[k].d, items[k].src, items[k].ss, items[k].dst, items[k].ds, stream);
+		}
+		for (int k : group)
+			done[k] = true;
+	}
+}
+
 // needs_colorspace (graphbuilder.cpp:484-506)
 bool needs_colorspace(const FormatState &s, const FormatState &d)
 {
@@ -477,6 +539,11 @@ struct zg_graph {
 		// planes live in tmp (pre at 0, mid next, resize scratch last)
 		zg_depth *pre = nullptr, *post = nullptr, *only = nullptr;
 		size_t pre_pitch = 0, mid_pitch = 0, off_mid = 0, off_tmp = 0;
+		// the last step diffuses errors: it runs after every plane's other
+		// steps, in one launch with the frame's other such planes (a resize
+		// before it writes into a region of tmp of the plane's own)
+		bool ed_last = false;
+		size_t off_mid_own = 0;
 		size_t tmp = 0;
 		// ring-buffer (line-masked) planes: the plane's full size, its
 		// vertical subsampling shift, and whole-plane staging copies in tmp
@@ -831,6 +898,21 @@ zg_graph *zg_graph_build(const zg_image_format *src_format, const zg_image_forma
 			gpl.tmp = off + rtmp;
 			g->tmp_size = std::max(g->tmp_size, gpl.tmp);
 		}
+		{
+			size_t off = (g->tmp_size + 255) & ~static_cast<size_t>(255);
+			for (auto &gpl : g->planes) {
+				EdPlane ep;
+				int it = 0, ot = 0;
+				if ((gpl.mode == 3 || gpl.mode == 4) && depth_ed_plane(gpl.only, &ep, &it, &ot)) {
+					gpl.ed_last = true;
+				} else if (gpl.mode == 2 && gpl.post && depth_ed_plane(gpl.post, &ep, &it, &ot)) {
+					gpl.ed_last = true;
+					gpl.off_mid_own = off;
+					off += gpl.mid_pitch * gpl.h;
+				}
+			}
+			g->tmp_size = off;
+		}
 		// GREY to YUV / RGB without a colorspace change: the chroma outputs
 		// are the neutral value in the output format, or copies of the luma
 		// output (grey_to_yuv / grey_to_rgb, graphbuilder.cpp:615-659)
@@ -1083,6 +1165,14 @@ zg_error_code zg_graph_process_cb(const zg_graph *g, const zg_image_buffer_const
 			}
 		}
 
+		struct Deferred {
+			const zg_depth *d;
+			const void *src;
+			ptrdiff_t ss;
+			void *dst;
+			ptrdiff_t ds;
+		};
+		std::vector<Deferred> deferred;
 		for (int p = 0; p < 4; ++p) {
 			const auto &pl = g->planes[p];
 			if (!pl.present)
@@ -1096,7 +1186,10 @@ zg_error_code zg_graph_process_cb(const zg_graph *g, const zg_image_buffer_const
 				continue;
 			}
 			if (pl.mode == 3 || pl.mode == 4) {
-				run_depth(pl.only, from, sst, dp, dst_st, stream);
+				if (pl.ed_last)
+					deferred.push_back({ pl.only, from, sst, dp, dst_st });
+				else
+					run_depth(pl.only, from, sst, dp, dst_st, stream);
 				continue;
 			}
 			if (pl.mode >= 5)
@@ -1110,7 +1203,7 @@ zg_error_code zg_graph_process_cb(const zg_graph *g, const zg_image_buffer_const
 				rs = t;
 				rss = static_cast<ptrdiff_t>(pl.pre_pitch);
 			}
-			void *rd = pl.post ? static_cast<void *>(t + pl.off_mid) : static_cast<void *>(dp);
+			void *rd = pl.post ? static_cast<void *>(t + (pl.ed_last ? pl.off_mid_own : pl.off_mid)) : static_cast<void *>(dp);
 			const ptrdiff_t rds = pl.post ? static_cast<ptrdiff_t>(pl.mid_pitch) : dst_st;
 			zg_error_code rc = pl.unresize
 			                       ? zg_unresize_process(pl.unresize, rs, rss, rd, rds, t ? t + pl.off_tmp : nullptr, stream)
@@ -1120,9 +1213,12 @@ zg_error_code zg_graph_process_cb(const zg_graph *g, const zg_image_buffer_const
 				zg_get_last_error(msg, sizeof(msg));
 				throw Error(rc, msg);
 			}
-			if (pl.post)
+			if (pl.post && pl.ed_last)
+				deferred.push_back({ pl.post, rd, rds, dp, dst_st });
+			else if (pl.post)
 				run_depth(pl.post, rd, rds, dp, dst_st, stream);
 		}
+		run_ed_planes(deferred.data(), static_cast<int>(deferred.size()), stream);
 
 		if (g->premul.on) {
 			const auto &pm = g->premul;

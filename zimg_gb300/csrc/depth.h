@@ -68,3 +68,14 @@ size_t ed_smem_bytes(int warps, int ring);
 cudaError_t launch_error_diffusion(const EdLaunch &L, cudaStream_t stream);
 
 } // namespace zg
+
+struct zg_depth;
+
+namespace zg {
+
+// The error-diffusion plane of a depth conversion object (its size, scale,
+// offset and range; pointers unset) and its pixel types; false when the
+// conversion does not diffuse errors.
+bool depth_ed_plane(const ::zg_depth *d, EdPlane *plane, int *in_type, int *out_type);
+
+} // namespace zg
