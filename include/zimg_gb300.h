@@ -385,6 +385,9 @@ ZG_API void zg_batch_free(zg_batch *b);
 ZG_API zg_error_code zg_batch_get_tmp_size(const zg_batch *b, size_t *out);
 /* Copy a host table of num_jobs entries into the batch's device table (async on stream). */
 ZG_API zg_error_code zg_batch_set_io(zg_batch *b, const zg_batch_io *io, zg_stream stream);
+/* One batch runs on one stream at a time: its launches share the batch's
+ * device tables and work counter, so two zg_batch_process calls on the same
+ * batch must not overlap (order them on one stream, or use two batches). */
 ZG_API zg_error_code zg_batch_process(const zg_batch *b, void *tmp, zg_stream stream);
 ZG_API zg_error_code zg_batch_process_graph(zg_batch *b, void *tmp, zg_stream stream);
 /*
@@ -403,8 +406,9 @@ ZG_API zg_error_code zg_batch_autotune(zg_batch *b, zg_stream stream, unsigned *
 /* Number of kernel launches one zg_batch_process issues. Where every chained
  * u16 job's source plane admits a tensor map (16-byte aligned base and
  * stride, set by zg_batch_set_io), the chained jobs of all kernel variants and
- * the identity planes run as one persistent launch whose CTAs take unit
- * ranges of equal estimated cost. */
+ * the identity planes run as one persistent launch whose CTAs take chunks of
+ * work units from a counter (large chunks first, by estimated cost, small
+ * ones last). */
 ZG_API zg_error_code zg_batch_get_launch_count(const zg_batch *b, unsigned *out);
 
 /* ---------------------------------------------------------------- graph --

@@ -63,7 +63,9 @@ struct zg_batch {
 	DeviceBuffer mixed_dev;
 	std::vector<CUtensorMap> mixed_maps_host;
 	DeviceBuffer mixed_maps_dev;
-	DeviceBuffer mixed_ranges_dev;      // grid + 1 unit indices
+	DeviceBuffer mixed_ranges_dev;      // chunk bounds (mixed_chunks + 1 unit indices)
+	int mixed_chunks = 0;
+	DeviceBuffer mixed_sched_dev;       // the launch's chunk counter and CTA exit count (zero between launches)
 	cudaGraphExec_t graph = nullptr;
 	cudaStream_t graph_stream = nullptr;
 	void *graph_tmp = nullptr;
@@ -109,7 +111,8 @@ void batch_launch(const zg_batch *b, void *tmp, cudaStream_t st)
 		work.push_back([b](cudaStream_t s) {
 			cuda_check(launch_chain_mixed(static_cast<const FusedJob *>(b->mixed_dev.get()),
 			                              static_cast<int>(b->mixed_host.size()),
-			                              static_cast<const int *>(b->mixed_ranges_dev.get()), b->mixed_layout,
+			                              static_cast<const int *>(b->mixed_ranges_dev.get()), b->mixed_chunks,
+			                              static_cast<unsigned *>(b->mixed_sched_dev.get()), b->mixed_layout,
 			                              b->mixed_grid, s),
 			           "mixed batch launch");
 		});
@@ -235,6 +238,8 @@ void plan_mixed(zg_batch *b)
 	b->mixed_dev.release();
 	b->mixed_maps_dev.release();
 	b->mixed_ranges_dev.release();
+	b->mixed_sched_dev.release();
+	b->mixed_chunks = 0;
 	if (!chain_tma_enabled())
 		return;
 	std::vector<const FusedPlan *> plans;
@@ -282,30 +287,27 @@ void plan_mixed(zg_batch *b)
 		b->mixed_host.push_back(j);
 	}
 	b->mixed_grid = std::min(chain_mixed_grid_size(static_cast<size_t>(b->mixed_layout.total_bytes)), units);
-	// per-CTA unit ranges of equal estimated cost
-	double total = 0;
-	for (size_t e = 0; e < b->mixed_host.size(); ++e)
-		total += cost[e] * fused_items(b->mixed_host[e]);
-	std::vector<int> begin(b->mixed_grid + 1, units);
-	begin[0] = 0;
-	double acc = 0;
-	size_t e = 0;
-	for (int c = 1; c < b->mixed_grid; ++c) {
-		const double target = total * c / b->mixed_grid;
-		while (e < b->mixed_host.size() && acc + cost[e] * fused_items(b->mixed_host[e]) <= target) {
-			acc += cost[e] * fused_items(b->mixed_host[e]);
-			++e;
-		}
-		int u = units;
-		if (e < b->mixed_host.size()) {
-			const int n = fused_items(b->mixed_host[e]);
-			u = b->mixed_host[e].item_begin + std::min(n, static_cast<int>((target - acc) / cost[e]));
-		}
-		begin[c] = std::max(begin[c - 1], u);
+	// guided chunks of the units by estimated cost, at least 12 units each;
+	// chained jobs' chunks end on strip boundaries (an item's start costs
+	// about 3 groups), identity copies (last in the table) anywhere
+	std::vector<int> item_begin, items, strip_units;
+	for (const FusedJob &j : b->mixed_host) {
+		item_begin.push_back(j.item_begin);
+		items.push_back(fused_items(j));
+		strip_units.push_back(j.variant == chain_mixed_copy_variant() ? 0 : j.groups);
 	}
-	b->mixed_ranges_dev.reset(begin.size() * sizeof(int));
-	cuda_check(cudaMemcpy(b->mixed_ranges_dev.get(), begin.data(), begin.size() * sizeof(int), cudaMemcpyHostToDevice),
-	           "mixed batch ranges");
+	const std::vector<int> bounds = chain_mixed_chunks(item_begin, items, cost, strip_units, b->mixed_grid, 12);
+	if (bounds.size() < 2) {
+		b->mixed_jobs.clear();
+		b->mixed_host.clear();
+		return;
+	}
+	b->mixed_chunks = static_cast<int>(bounds.size()) - 1;
+	b->mixed_ranges_dev.reset(bounds.size() * sizeof(int));
+	cuda_check(cudaMemcpy(b->mixed_ranges_dev.get(), bounds.data(), bounds.size() * sizeof(int), cudaMemcpyHostToDevice),
+	           "mixed batch chunks");
+	b->mixed_sched_dev.reset(2 * sizeof(unsigned));
+	cuda_check(cudaMemset(b->mixed_sched_dev.get(), 0, 2 * sizeof(unsigned)), "mixed batch chunks");
 	b->mixed_dev.reset(b->mixed_host.size() * sizeof(FusedJob));
 	b->mixed_maps_host.assign(b->mixed_host.size(), CUtensorMap{});
 	b->mixed_maps_dev.reset(b->mixed_host.size() * sizeof(CUtensorMap));

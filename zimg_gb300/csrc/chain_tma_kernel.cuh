@@ -658,52 +658,71 @@ chain_tma_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_item
 constexpr int kCopyVariant = 1000;
 
 // One launch over a batch of mixed jobs: every chained variant and identity
-// copies, each CTA the range of units [cta_begin[b], cta_begin[b + 1]) (the
-// host balances the ranges by estimated cost); an item is dispatched on its
-// job's variant.
+// copies. CTAs take chunks of units from a counter (guided sizes, cut by the
+// host from estimated costs: large chunks first, small ones last, so that
+// the CTAs end together); an item is dispatched on its job's variant.
 __global__ void __launch_bounds__(tma_threads(true), 2)
-chain_mixed_kernel(const FusedJob *__restrict__ jobs, int num_jobs, const int *__restrict__ cta_begin,
-                   const __grid_constant__ SmemLayout L)
+chain_mixed_kernel(const FusedJob *__restrict__ jobs, int num_jobs, const int *__restrict__ bounds, int num_chunks,
+                   unsigned *sched, const __grid_constant__ SmemLayout L)
 {
 	extern __shared__ float4 smem4[];
 	__shared__ int abort_item;
+	__shared__ int chunk;
 	Pipe p;
 	pipe_init(p, smem4, L, &abort_item);
-	const int t_end = __ldg(cta_begin + blockIdx.x + 1);
-	for (int t = __ldg(cta_begin + blockIdx.x); t < t_end;) {
-		const FusedJob &J = jobs[find_job(jobs, num_jobs, t)];
-		const int local = t - J.item_begin;
-		const int strip = local / J.groups;
-		const int g_begin = local - strip * J.groups;
-		const int ngroups = min(J.groups - g_begin, t_end - t);
-		t += ngroups;
-		const int v = J.variant;
-		if (v == kCopyVariant) {
-			copy_item(J, g_begin, ngroups);
-		} else {
-			load_bases(p, J, g_begin, ngroups);
-			switch (v) {
+	// chunks in the order CTAs ask for them (guided sizes: large first)
+	for (;;) {
+		if (threadIdx.x == 0)
+			chunk = static_cast<int>(atomicAdd(&sched[0], 1u));
+		__syncthreads();
+		const int m = chunk;
+		__syncthreads();  // every thread has read it before thread 0 asks again
+		if (m >= num_chunks || abort_item)
+			break;
+		const int t_end = __ldg(bounds + m + 1);
+		for (int t = __ldg(bounds + m); t < t_end;) {
+			const FusedJob &J = jobs[find_job(jobs, num_jobs, t)];
+			const int local = t - J.item_begin;
+			const int strip = local / J.groups;
+			const int g_begin = local - strip * J.groups;
+			const int ngroups = min(J.groups - g_begin, t_end - t);
+			t += ngroups;
+			const int v = J.variant;
+			if (v == kCopyVariant) {
+				copy_item(J, g_begin, ngroups);
+			} else {
+				load_bases(p, J, g_begin, ngroups);
+				switch (v) {
 #define ZG_CHAIN_CASE(HF, KV, KH)                                                                     \
 	case (HF ? 12 : 0) + (KV - 1) * 4 + (KH - 1):                                                      \
 		chain_item<HF, KV, KH, false>(p, L, J, J.tmap, strip, g_begin, ngroups);                     \
 		break;
-				ZG_CHAIN_CASE(true, 1, 1) ZG_CHAIN_CASE(true, 1, 2) ZG_CHAIN_CASE(true, 1, 3) ZG_CHAIN_CASE(true, 1, 4)
-				ZG_CHAIN_CASE(true, 2, 1) ZG_CHAIN_CASE(true, 2, 2) ZG_CHAIN_CASE(true, 2, 3) ZG_CHAIN_CASE(true, 2, 4)
-				ZG_CHAIN_CASE(true, 3, 1) ZG_CHAIN_CASE(true, 3, 2) ZG_CHAIN_CASE(true, 3, 3) ZG_CHAIN_CASE(true, 3, 4)
-				ZG_CHAIN_CASE(false, 1, 1) ZG_CHAIN_CASE(false, 1, 2) ZG_CHAIN_CASE(false, 1, 3) ZG_CHAIN_CASE(false, 1, 4)
-				ZG_CHAIN_CASE(false, 2, 1) ZG_CHAIN_CASE(false, 2, 2) ZG_CHAIN_CASE(false, 2, 3) ZG_CHAIN_CASE(false, 2, 4)
-				ZG_CHAIN_CASE(false, 3, 1) ZG_CHAIN_CASE(false, 3, 2) ZG_CHAIN_CASE(false, 3, 3) ZG_CHAIN_CASE(false, 3, 4)
+					ZG_CHAIN_CASE(true, 1, 1) ZG_CHAIN_CASE(true, 1, 2) ZG_CHAIN_CASE(true, 1, 3) ZG_CHAIN_CASE(true, 1, 4)
+					ZG_CHAIN_CASE(true, 2, 1) ZG_CHAIN_CASE(true, 2, 2) ZG_CHAIN_CASE(true, 2, 3) ZG_CHAIN_CASE(true, 2, 4)
+					ZG_CHAIN_CASE(true, 3, 1) ZG_CHAIN_CASE(true, 3, 2) ZG_CHAIN_CASE(true, 3, 3) ZG_CHAIN_CASE(true, 3, 4)
+					ZG_CHAIN_CASE(false, 1, 1) ZG_CHAIN_CASE(false, 1, 2) ZG_CHAIN_CASE(false, 1, 3) ZG_CHAIN_CASE(false, 1, 4)
+					ZG_CHAIN_CASE(false, 2, 1) ZG_CHAIN_CASE(false, 2, 2) ZG_CHAIN_CASE(false, 2, 3) ZG_CHAIN_CASE(false, 2, 4)
+					ZG_CHAIN_CASE(false, 3, 1) ZG_CHAIN_CASE(false, 3, 2) ZG_CHAIN_CASE(false, 3, 3) ZG_CHAIN_CASE(false, 3, 4)
 #undef ZG_CHAIN_CASE
-			default:
-				break;
+				default:
+					break;
+				}
 			}
+			p.base += J.variant == kCopyVariant ? 0 : ngroups;
+			__syncthreads();  // the next item rewrites the group bases and the ring
+			if (abort_item)
+				break;
 		}
-		p.base += J.variant == kCopyVariant ? 0 : ngroups;
-		__syncthreads();  // the next item rewrites the group bases and the ring
-		if (abort_item)
-			break;
 	}
 	pipe_finish(p);
+	// the last CTA out leaves the counters zero for the next launch
+	if (threadIdx.x == 0) {
+		__threadfence();
+		if (atomicAdd(&sched[1], 1u) == gridDim.x - 1) {
+			atomicExch(&sched[0], 0u);
+			atomicExch(&sched[1], 0u);
+		}
+	}
 }
 
 } // namespace chain_detail

@@ -188,12 +188,26 @@ std::vector<int> chain_tma_lockstep_ranges(int total_items, int groups, int grid
 int chain_tma_pipeline_error(bool reset);
 // One launch over a mixed batch (chained jobs of any variant, each FusedJob's
 // `variant`, and identity copies, variant chain_mixed_copy_variant(), src_w
-// = row bytes, groups = 16-row bands, strips = 1): CTA b processes the units
-// [cta_begin[b], cta_begin[b + 1]). L covers every chained job.
+// = row bytes, groups = 16-row bands, strips = 1). The units are cut into
+// num_chunks chunks, chunk m the units [bounds[m], bounds[m + 1]) (device
+// memory, strictly increasing); each CTA takes the next chunk from the
+// counter sched[0] until none is left. sched (two words in device memory,
+// zero before the first launch) is left zero when the launch ends: the last
+// CTA out resets it, so launches on one stream (and graph replays) reuse it;
+// launches that may overlap need their own. L covers every chained job.
 int chain_mixed_copy_variant();
 int chain_mixed_grid_size(size_t smem_bytes);
-cudaError_t launch_chain_mixed(const FusedJob *jobs, int num_jobs, const int *cta_begin, const SmemLayout &L, int grid,
-                               cudaStream_t stream);
+cudaError_t launch_chain_mixed(const FusedJob *jobs, int num_jobs, const int *bounds, int num_chunks, unsigned *sched,
+                               const SmemLayout &L, int grid, cudaStream_t stream);
+// Guided chunk bounds for launch_chain_mixed: units [0, units) of jobs with
+// item_begin[e] .. item_begin[e] + items[e] - 1 (in order, contiguous) at an
+// estimated cost per unit cost[e]; each chunk takes 1 / (2 grid) of the cost
+// still left, but at least min_units units (or the rest), and a chunk that
+// ends inside a job with strip_units[e] > 0 units per strip ends on the
+// nearest strip boundary instead.
+std::vector<int> chain_mixed_chunks(const std::vector<int> &item_begin, const std::vector<int> &items,
+                                    const std::vector<double> &cost, const std::vector<int> &strip_units, int grid,
+                                    int min_units);
 // Test hook: CTA 0's producer skips group drop_group (-1: none) without
 // arming its stage; waits give up after wait_ns (0: the default 0.25 s).
 int chain_tma_set_fault(int drop_group, unsigned long long wait_ns);
