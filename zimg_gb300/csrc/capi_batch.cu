@@ -31,6 +31,11 @@ struct zg_batch {
 		SmemLayout tlayout{};
 		int tgrid = 0;
 		int ranges_off = -1;  // CTA unit ranges in ranges_dev (ints), or -1
+		// guided chunks (CUDA-core streaming groups): bounds at chunks_off in
+		// chunks_dev, num_chunks chunks, the counter pair at `sched` in
+		// sched_dev; num_chunks 0: a static split (the chained groups keep
+		// strips in step, measured faster for them)
+		int chunks_off = 0, num_chunks = 0, sched = 0;
 	};
 
 	int device;
@@ -42,6 +47,9 @@ struct zg_batch {
 	std::vector<Group> groups;
 	std::vector<int> ranges_host;
 	DeviceBuffer ranges_dev;
+	std::vector<int> chunks_host;
+	DeviceBuffer chunks_dev;
+	DeviceBuffer sched_dev;  // two words per group (zero between launches)
 	std::vector<FusedJob> table_host;
 	DeviceBuffer table_dev;
 	std::vector<CUtensorMap> maps_host;  // per table entry (chained TMA groups)
@@ -101,6 +109,17 @@ void rethrow_last(zg_error_code rc)
 
 constexpr size_t kSideStreams = 4;
 
+// CUDA-core streaming launches take guided chunks of their units (false
+// when the environment sets ZG_BATCH_CHUNKS=0: equal static shares).
+bool batch_chunks_enabled()
+{
+	static const bool on = [] {
+		const char *e = std::getenv("ZG_BATCH_CHUNKS");
+		return !(e && e[0] == '0');
+	}();
+	return on;
+}
+
 void batch_launch(const zg_batch *b, void *tmp, cudaStream_t st)
 {
 	if (b->io.size() != b->jobs.size())
@@ -109,11 +128,12 @@ void batch_launch(const zg_batch *b, void *tmp, cudaStream_t st)
 	std::vector<std::function<void(cudaStream_t)>> work;
 	if (b->mixed_now) {
 		work.push_back([b](cudaStream_t s) {
+			WorkChunks c;
+			c.bounds = static_cast<const int *>(b->mixed_ranges_dev.get());
+			c.num = b->mixed_chunks;
+			c.sched = static_cast<unsigned *>(b->mixed_sched_dev.get());
 			cuda_check(launch_chain_mixed(static_cast<const FusedJob *>(b->mixed_dev.get()),
-			                              static_cast<int>(b->mixed_host.size()),
-			                              static_cast<const int *>(b->mixed_ranges_dev.get()), b->mixed_chunks,
-			                              static_cast<unsigned *>(b->mixed_sched_dev.get()), b->mixed_layout,
-			                              b->mixed_grid, s),
+			                              static_cast<int>(b->mixed_host.size()), c, b->mixed_layout, b->mixed_grid, s),
 			           "mixed batch launch");
 		});
 	}
@@ -121,14 +141,20 @@ void batch_launch(const zg_batch *b, void *tmp, cudaStream_t st)
 		if (b->mixed_now && g.tma_plan)
 			continue;  // in the mixed launch
 		const int *ranges = g.ranges_off < 0 ? nullptr : static_cast<const int *>(b->ranges_dev.get()) + g.ranges_off;
-		work.push_back([&g, table, ranges](cudaStream_t s) {
+		WorkChunks c;
+		if (!g.tma_now && g.num_chunks > 0) {
+			c.bounds = static_cast<const int *>(b->chunks_dev.get()) + g.chunks_off;
+			c.num = g.num_chunks;
+			c.sched = static_cast<unsigned *>(b->sched_dev.get()) + g.sched;
+		}
+		work.push_back([&g, table, ranges, c](cudaStream_t s) {
 			FusedJob unused{};
 			if (g.tma_now)
 				cuda_check(launch_chain_tma(g.variant, table + g.first, g.count, g.tiles, ranges, g.tlayout, g.tgrid,
 				                            unused, nullptr, s),
 				           "fused batch launch");
 			else
-				cuda_check(launch_fused(g.variant, table + g.first, g.count, g.tiles, g.layout, g.grid, unused, s),
+				cuda_check(launch_fused(g.variant, table + g.first, g.count, g.tiles, g.layout, g.grid, unused, s, c),
 				           "fused batch launch");
 		});
 	}
@@ -328,6 +354,7 @@ void regroup(zg_batch *b)
 	}
 	b->groups.clear();
 	b->ranges_host.clear();
+	b->chunks_host.clear();
 	b->table_host.clear();
 	b->table_dev.release();
 	share_tables(b);
@@ -380,7 +407,41 @@ void regroup(zg_batch *b)
 				}
 			}
 		}
+		// CUDA-core streaming groups: guided chunks of the group's units (cost
+		// per unit: the job's samples over its units), ending on strip
+		// boundaries (measured: bicubic 1.293 -> 1.214 ms per step)
+		if (batch_chunks_enabled() && fused_takes_chunks(g.variant)) {
+			std::vector<int> item_begin, items, strips_of;
+			std::vector<double> cost;
+			for (unsigned i : kv.second) {
+				const FusedJob &j = b->table_host[b->table_index[i]];
+				const zg_resize *r = b->jobs[i];
+				item_begin.push_back(j.item_begin);
+				items.push_back(fused_items(j));
+				cost.push_back((static_cast<double>(r->params.src_width) * r->params.src_height +
+				                static_cast<double>(r->params.dst_width) * r->params.dst_height) /
+				               std::max(1, fused_items(j)));
+				strips_of.push_back(j.segments);
+			}
+			const std::vector<int> bo = chain_mixed_chunks(item_begin, items, cost, strips_of, g.grid, 8);
+			if (bo.size() >= 2) {
+				g.chunks_off = static_cast<int>(b->chunks_host.size());
+				g.num_chunks = static_cast<int>(bo.size()) - 1;
+				g.sched = 2 * static_cast<int>(b->groups.size());
+				b->chunks_host.insert(b->chunks_host.end(), bo.begin(), bo.end());
+			}
+		}
 		b->groups.push_back(g);
+	}
+	b->chunks_dev.release();
+	b->sched_dev.release();
+	if (!b->chunks_host.empty()) {
+		b->chunks_dev.reset(b->chunks_host.size() * sizeof(int));
+		cuda_check(cudaMemcpy(b->chunks_dev.get(), b->chunks_host.data(), b->chunks_host.size() * sizeof(int),
+		                      cudaMemcpyHostToDevice),
+		           "work chunks");
+		b->sched_dev.reset(2 * b->groups.size() * sizeof(unsigned));
+		cuda_check(cudaMemset(b->sched_dev.get(), 0, 2 * b->groups.size() * sizeof(unsigned)), "work chunks");
 	}
 	b->ranges_dev.release();
 	if (!b->ranges_host.empty()) {

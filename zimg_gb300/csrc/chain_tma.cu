@@ -258,17 +258,20 @@ int chain_mixed_grid_size(size_t smem_bytes)
 	return std::max(1, sms) * per_sm;
 }
 
-cudaError_t launch_chain_mixed(const FusedJob *jobs, int num_jobs, const int *bounds, int num_chunks, unsigned *sched,
-                               const SmemLayout &L, int grid, cudaStream_t stream)
+cudaError_t launch_chain_mixed(const FusedJob *jobs, int num_jobs, const WorkChunks &chunks, const SmemLayout &L,
+                               int grid, cudaStream_t stream)
 {
-	if (static_cast<size_t>(L.total_bytes) > kTmaSmemMax || !jobs || !bounds || !sched || num_chunks < 1 || grid < 1)
+	if (static_cast<size_t>(L.total_bytes) > kTmaSmemMax || !jobs || !chunks.bounds || !chunks.sched ||
+	    chunks.num < 1 || grid < 1)
 		return cudaErrorInvalidValue;
 	const void *k = reinterpret_cast<const void *>(&chain_detail::chain_mixed_kernel);
 	cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kTmaSmemMax));
 	if (e != cudaSuccess)
 		return e;
 	SmemLayout layout = L;
-	void *args[] = { &jobs, &num_jobs, &bounds, &num_chunks, &sched, &layout };
+	WorkChunks C = chunks;
+	grid = std::min(grid, C.num);
+	void *args[] = { &jobs, &num_jobs, &C, &layout };
 	return cudaLaunchKernel(k, dim3(grid), dim3(chain_detail::tma_threads(true)), args,
 	                        static_cast<size_t>(L.total_bytes), stream);
 }
@@ -304,15 +307,17 @@ std::vector<int> chain_mixed_chunks(const std::vector<int> &item_begin, const st
 			got += k * cost[f];
 		}
 		// inside a job with strips: end on the nearest strip boundary past u
-		// (a chunk that splits a strip makes its tail a second item)
+		// where that changes the chunk by at most a quarter
 		if (v < units && strip_units[f] > 0 && v > item_begin[f]) {
 			const int su = strip_units[f], off = v - item_begin[f];
 			int w = item_begin[f] + (off + su / 2) / su * su;
 			if (w <= u)
 				w = item_begin[f] + (off / su + 1) * su;
 			w = std::min(w, item_begin[f] + items[f]);
-			got += (w - v) * cost[f];  // units moved in (or out)
-			v = w;
+			if (4 * std::abs(w - v) <= v - u) {
+				got += (w - v) * cost[f];  // units moved in (or out)
+				v = w;
+			}
 		}
 		bounds.push_back(v);
 		left -= got;

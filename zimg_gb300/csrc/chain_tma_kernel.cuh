@@ -36,6 +36,7 @@
 
 #include "chain_kernel.cuh"
 #include "pipeline.cuh"
+#include "work_chunks.cuh"
 
 namespace zg {
 namespace chain_detail {
@@ -662,8 +663,8 @@ constexpr int kCopyVariant = 1000;
 // host from estimated costs: large chunks first, small ones last, so that
 // the CTAs end together); an item is dispatched on its job's variant.
 __global__ void __launch_bounds__(tma_threads(true), 2)
-chain_mixed_kernel(const FusedJob *__restrict__ jobs, int num_jobs, const int *__restrict__ bounds, int num_chunks,
-                   unsigned *sched, const __grid_constant__ SmemLayout L)
+chain_mixed_kernel(const FusedJob *__restrict__ jobs, int num_jobs, const __grid_constant__ WorkChunks C,
+                   const __grid_constant__ SmemLayout L)
 {
 	extern __shared__ float4 smem4[];
 	__shared__ int abort_item;
@@ -672,15 +673,11 @@ chain_mixed_kernel(const FusedJob *__restrict__ jobs, int num_jobs, const int *_
 	pipe_init(p, smem4, L, &abort_item);
 	// chunks in the order CTAs ask for them (guided sizes: large first)
 	for (;;) {
-		if (threadIdx.x == 0)
-			chunk = static_cast<int>(atomicAdd(&sched[0], 1u));
-		__syncthreads();
-		const int m = chunk;
-		__syncthreads();  // every thread has read it before thread 0 asks again
-		if (m >= num_chunks || abort_item)
+		const int m = next_chunk(C, &chunk);
+		if (m < 0 || abort_item)
 			break;
-		const int t_end = __ldg(bounds + m + 1);
-		for (int t = __ldg(bounds + m); t < t_end;) {
+		const int t_end = __ldg(C.bounds + m + 1);
+		for (int t = __ldg(C.bounds + m); t < t_end;) {
 			const FusedJob &J = jobs[find_job(jobs, num_jobs, t)];
 			const int local = t - J.item_begin;
 			const int strip = local / J.groups;
@@ -715,14 +712,7 @@ chain_mixed_kernel(const FusedJob *__restrict__ jobs, int num_jobs, const int *_
 		}
 	}
 	pipe_finish(p);
-	// the last CTA out leaves the counters zero for the next launch
-	if (threadIdx.x == 0) {
-		__threadfence();
-		if (atomicAdd(&sched[1], 1u) == gridDim.x - 1) {
-			atomicExch(&sched[0], 0u);
-			atomicExch(&sched[1], 0u);
-		}
-	}
+	chunks_finish(C);  // the last CTA out leaves the counter zero for the next launch
 }
 
 } // namespace chain_detail

@@ -9,10 +9,14 @@
 namespace zg {
 
 // per-(H_FIRST, U16) instantiation units (fused_inst_*.cu)
-cudaError_t launch_fused_v_f32(int, int, const FusedJob *, int, int, const SmemLayout &, int, const FusedJob &, cudaStream_t);
-cudaError_t launch_fused_v_u16(int, int, const FusedJob *, int, int, const SmemLayout &, int, const FusedJob &, cudaStream_t);
-cudaError_t launch_fused_h_f32(int, int, const FusedJob *, int, int, const SmemLayout &, int, const FusedJob &, cudaStream_t);
-cudaError_t launch_fused_h_u16(int, int, const FusedJob *, int, int, const SmemLayout &, int, const FusedJob &, cudaStream_t);
+cudaError_t launch_fused_v_f32(int, int, const FusedJob *, int, int, const SmemLayout &, int, const FusedJob &,
+                               const WorkChunks &, cudaStream_t);
+cudaError_t launch_fused_v_u16(int, int, const FusedJob *, int, int, const SmemLayout &, int, const FusedJob &,
+                               const WorkChunks &, cudaStream_t);
+cudaError_t launch_fused_h_f32(int, int, const FusedJob *, int, int, const SmemLayout &, int, const FusedJob &,
+                               const WorkChunks &, cudaStream_t);
+cudaError_t launch_fused_h_u16(int, int, const FusedJob *, int, int, const SmemLayout &, int, const FusedJob &,
+                               const WorkChunks &, cudaStream_t);
 const void *fused_kernel_ptr_v_f32(int hw, int vs);
 const void *fused_kernel_ptr_v_u16(int hw, int vs);
 const void *fused_kernel_ptr_h_f32(int hw, int vs);
@@ -360,8 +364,13 @@ int fused_grid_size(int variant, size_t smem_bytes)
 	return std::max(1, sms) * per_sm;
 }
 
+bool fused_takes_chunks(int variant)
+{
+	return variant >= 0 && variant < 100;
+}
+
 cudaError_t launch_fused(int variant, const FusedJob *jobs, int num_jobs, int total_tiles, const SmemLayout &smem_bytes,
-                         int grid, const FusedJob &single, cudaStream_t stream)
+                         int grid, const FusedJob &single, cudaStream_t stream, const WorkChunks &chunks)
 {
 	if (variant >= 200)
 		return launch_chain(variant, jobs, num_jobs, total_tiles, smem_bytes, grid, single, stream);
@@ -372,11 +381,12 @@ cudaError_t launch_fused(int variant, const FusedJob *jobs, int num_jobs, int to
 	grid = std::max(1, std::min(grid, total_tiles));
 	if (smem_bytes.total_bytes > static_cast<int>(kSmemMax))
 		return cudaErrorInvalidValue;
+	const WorkChunks &c = chunks;
 	if (hf)
-		return u16 ? launch_fused_h_u16(hw, vs, jobs, num_jobs, total_tiles, smem_bytes, grid, single, stream)
-		           : launch_fused_h_f32(hw, vs, jobs, num_jobs, total_tiles, smem_bytes, grid, single, stream);
-	return u16 ? launch_fused_v_u16(hw, vs, jobs, num_jobs, total_tiles, smem_bytes, grid, single, stream)
-	           : launch_fused_v_f32(hw, vs, jobs, num_jobs, total_tiles, smem_bytes, grid, single, stream);
+		return u16 ? launch_fused_h_u16(hw, vs, jobs, num_jobs, total_tiles, smem_bytes, grid, single, c, stream)
+		           : launch_fused_h_f32(hw, vs, jobs, num_jobs, total_tiles, smem_bytes, grid, single, c, stream);
+	return u16 ? launch_fused_v_u16(hw, vs, jobs, num_jobs, total_tiles, smem_bytes, grid, single, c, stream)
+	           : launch_fused_v_f32(hw, vs, jobs, num_jobs, total_tiles, smem_bytes, grid, single, c, stream);
 }
 
 void fused_set_io(FusedJob &j, const void *src, ptrdiff_t src_stride, void *dst, ptrdiff_t dst_stride)

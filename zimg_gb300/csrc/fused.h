@@ -83,6 +83,18 @@ struct FusedJob {
 	int variant;            // chained kernel's variant - 200 ((H first, KV, KH)); mixed launches dispatch on it
 };
 
+// Guided work chunks of a persistent launch (work_chunks.cuh): chunk m is
+// the work units [bounds[m], bounds[m + 1]) (device memory, strictly
+// increasing, num chunks); CTAs take chunks from the counter sched[0] in the
+// order they ask. sched (two words in device memory) is zero before a launch
+// and left zero after it; launches that may overlap need their own. With
+// sched == nullptr a launch splits its units statically.
+struct WorkChunks {
+	const int *bounds = nullptr;
+	int num = 0;
+	unsigned *sched = nullptr;
+};
+
 // Shared-memory layout of one launch (the maximum over its jobs).
 struct SmemLayout {
 	int pitch;              // elements per ring line (largest strip patch + pad)
@@ -138,7 +150,11 @@ SmemLayout fused_layout(const FusedPlan *const *plans, int n);
 // same variant) as one persistent grid; with jobs == nullptr, run `single`
 // (passed by value as a kernel parameter).
 cudaError_t launch_fused(int variant, const FusedJob *jobs, int num_jobs, int total_items, const SmemLayout &L,
-                         int grid, const FusedJob &single, cudaStream_t stream);
+                         int grid, const FusedJob &single, cudaStream_t stream, const WorkChunks &chunks = {});
+// Whether launch_fused takes guided chunks for this variant (the CUDA-core
+// streaming kernel does; the tensor-core forms launched through it split
+// their units statically).
+bool fused_takes_chunks(int variant);
 
 size_t fused_max_smem();
 int fused_grid_size(int variant, size_t smem_bytes);
@@ -188,23 +204,19 @@ std::vector<int> chain_tma_lockstep_ranges(int total_items, int groups, int grid
 int chain_tma_pipeline_error(bool reset);
 // One launch over a mixed batch (chained jobs of any variant, each FusedJob's
 // `variant`, and identity copies, variant chain_mixed_copy_variant(), src_w
-// = row bytes, groups = 16-row bands, strips = 1). The units are cut into
-// num_chunks chunks, chunk m the units [bounds[m], bounds[m + 1]) (device
-// memory, strictly increasing); each CTA takes the next chunk from the
-// counter sched[0] until none is left. sched (two words in device memory,
-// zero before the first launch) is left zero when the launch ends: the last
-// CTA out resets it, so launches on one stream (and graph replays) reuse it;
-// launches that may overlap need their own. L covers every chained job.
+// = row bytes, groups = 16-row bands, strips = 1), its units in guided
+// chunks (required). L covers every chained job.
 int chain_mixed_copy_variant();
 int chain_mixed_grid_size(size_t smem_bytes);
-cudaError_t launch_chain_mixed(const FusedJob *jobs, int num_jobs, const int *bounds, int num_chunks, unsigned *sched,
-                               const SmemLayout &L, int grid, cudaStream_t stream);
-// Guided chunk bounds for launch_chain_mixed: units [0, units) of jobs with
-// item_begin[e] .. item_begin[e] + items[e] - 1 (in order, contiguous) at an
-// estimated cost per unit cost[e]; each chunk takes 1 / (2 grid) of the cost
-// still left, but at least min_units units (or the rest), and a chunk that
-// ends inside a job with strip_units[e] > 0 units per strip ends on the
-// nearest strip boundary instead.
+cudaError_t launch_chain_mixed(const FusedJob *jobs, int num_jobs, const WorkChunks &chunks, const SmemLayout &L,
+                               int grid, cudaStream_t stream);
+// Guided chunk bounds: units [0, units) of jobs with item_begin[e] ..
+// item_begin[e] + items[e] - 1 (in order, contiguous) at an estimated cost
+// per unit cost[e]; each chunk takes 1 / (2 grid) of the cost still left, but
+// at least min_units units (or the rest), and a chunk that ends inside a job
+// with strip_units[e] > 0 units per strip ends on the nearest strip boundary
+// instead where that changes it by at most a quarter (a chunk that splits a
+// strip makes its tail a second item, which starts its pipeline again).
 std::vector<int> chain_mixed_chunks(const std::vector<int> &item_begin, const std::vector<int> &items,
                                     const std::vector<double> &cost, const std::vector<int> &strip_units, int grid,
                                     int min_units);

@@ -6,6 +6,8 @@
 
 #include "fused_kernel.cuh"
 
+#include <algorithm>
+
 #define ZG_FUSED_INSTANCE(NAME, HF, U16)                                                                           \
 	namespace zg {                                                                                                 \
 	namespace {                                                                                                    \
@@ -30,7 +32,8 @@
 		return hw == 0 ? ptr_vs_##NAME<6>(vs) : (hw == 1 ? ptr_vs_##NAME<8>(vs) : ptr_vs_##NAME<16>(vs));          \
 	}                                                                                                              \
 	cudaError_t launch_fused_##NAME(int hw, int vs, const FusedJob *jobs, int num_jobs, int total_tiles,          \
-	                                const SmemLayout &L, int grid, const FusedJob &single, cudaStream_t stream)    \
+	                                const SmemLayout &L, int grid, const FusedJob &single, const WorkChunks &C,    \
+	                                cudaStream_t stream)                                                           \
 	{                                                                                                              \
 		const void *k = fused_kernel_ptr_##NAME(hw, vs);                                                           \
 		cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,                      \
@@ -39,7 +42,10 @@
 			return e;                                                                                              \
 		FusedJob one = single;                                                                                     \
 		SmemLayout layout = L;                                                                                     \
-		void *args[] = { &jobs, &num_jobs, &total_tiles, &one, &layout };                                          \
+		WorkChunks chunks = C;                                                                                     \
+		if (chunks.sched)                                                                                          \
+			grid = std::max(1, std::min(grid, chunks.num));                                                        \
+		void *args[] = { &jobs, &num_jobs, &total_tiles, &one, &layout, &chunks };                                 \
 		return cudaLaunchKernel(k, dim3(grid), dim3(kStreamThreads), args, static_cast<size_t>(L.total_bytes),    \
 		                        stream);                                                                           \
 	}                                                                                                              \

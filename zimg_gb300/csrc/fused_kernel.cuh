@@ -17,6 +17,7 @@
 #pragma once
 
 #include "fused.h"
+#include "work_chunks.cuh"
 
 namespace zg {
 namespace fused_detail {
@@ -427,7 +428,7 @@ __device__ __forceinline__ void load_coef(const Item &it, int g0, int g1, char *
 template <bool H_FIRST, bool U16, int HW, int VS>
 __global__ void __launch_bounds__(kThreads, H_FIRST ? 4 : 5)
 fused_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, const __grid_constant__ FusedJob single,
-             const __grid_constant__ SmemLayout L)
+             const __grid_constant__ SmemLayout L, const __grid_constant__ WorkChunks C)
 {
 	constexpr int kGroup = group_rows(H_FIRST);
 	extern __shared__ float4 smem4[];
@@ -445,77 +446,94 @@ fused_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 		smem4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
 	__syncthreads();
 
-	// this CTA's equal share of the launch's units, in job / strip / step order
-	const int t_end = static_cast<int>(static_cast<long long>(blockIdx.x + 1) * total_items / gridDim.x);
-	for (int t = static_cast<int>(static_cast<long long>(blockIdx.x) * total_items / gridDim.x); t < t_end;) {
-		const FusedJob *Jp = jobs ? &jobs[find_job(jobs, num_jobs, t)] : &single;
-		const Item it = make_item<HW>(*Jp, t, t_end, smem, L);
-		t += it.units;
-		__syncthreads();  // group bases visible
-
-		const int nsteps = (it.g_end - it.g_begin + it.step_groups - 1) / it.step_groups;
-		// step k covers groups [gk, gk1); its new source lines are [lo_k, hi_k)
-		int hi_prev = reinterpret_cast<const int *>(smem + L.vbase_off)[0];
-		auto step_groups_of = [&](int k, int *g0, int *g1) {
-			*g0 = it.g_begin + k * it.step_groups;
-			*g1 = min(it.g_end, *g0 + it.step_groups);
-		};
-		// prologue: step 0's lines and taps
-		{
-			int g0, g1;
-			step_groups_of(0, &g0, &g1);
-			const int hi = step_end<VS>(it, smem, L, g1);
-			if (U16)
-				load_lines<true>(it, hi_prev, hi, stage, smask, L.pitch);
-			else
-				load_lines<false>(it, hi_prev, hi, reinterpret_cast<char *>(H_FIRST ? in : ring),
-				                  H_FIRST ? imask : rmask, L.pitch);
-			load_coef<VS, kGroup>(it, g0, g1, smem + L.vcoef_off);
-			cp_async_commit();
+	// the launch's units in job / strip / step order: guided chunks
+	// (C.sched), or this CTA's equal share
+	__shared__ int chunk;
+	int c_begin = static_cast<int>(static_cast<long long>(blockIdx.x) * total_items / gridDim.x);
+	int c_end = static_cast<int>(static_cast<long long>(blockIdx.x + 1) * total_items / gridDim.x);
+	for (bool first = true;; first = false) {
+		if (C.sched) {
+			const int m = next_chunk(C, &chunk);
+			if (m < 0)
+				break;
+			c_begin = __ldg(C.bounds + m);
+			c_end = __ldg(C.bounds + m + 1);
+		} else if (!first) {
+			break;
 		}
-		__syncthreads();  // lines stored by plain loads (unaligned u16) are visible to every converter
-		int lo_cur = hi_prev;
-		int hi_cur = step_end<VS>(it, smem, L, min(it.g_end, it.g_begin + it.step_groups));
+		const int t_end = c_end;
+		for (int t = c_begin; t < t_end;) {
+			const FusedJob *Jp = jobs ? &jobs[find_job(jobs, num_jobs, t)] : &single;
+			const Item it = make_item<HW>(*Jp, t, t_end, smem, L);
+			t += it.units;
+			__syncthreads();  // group bases visible
 
-		for (int k = 0; k < nsteps; ++k) {
-			int g0, g1;
-			step_groups_of(k, &g0, &g1);
-			// prefetch step k+1
-			int hi_next = hi_cur;
-			if (k + 1 < nsteps) {
-				int n0, n1;
-				step_groups_of(k + 1, &n0, &n1);
-				hi_next = step_end<VS>(it, smem, L, n1);
+			const int nsteps = (it.g_end - it.g_begin + it.step_groups - 1) / it.step_groups;
+			// step k covers groups [gk, gk1); its new source lines are [lo_k, hi_k)
+			int hi_prev = reinterpret_cast<const int *>(smem + L.vbase_off)[0];
+			auto step_groups_of = [&](int k, int *g0, int *g1) {
+				*g0 = it.g_begin + k * it.step_groups;
+				*g1 = min(it.g_end, *g0 + it.step_groups);
+			};
+			// prologue: step 0's lines and taps
+			{
+				int g0, g1;
+				step_groups_of(0, &g0, &g1);
+				const int hi = step_end<VS>(it, smem, L, g1);
 				if (U16)
-					load_lines<true>(it, hi_cur, hi_next, stage, smask, L.pitch);
+					load_lines<true>(it, hi_prev, hi, stage, smask, L.pitch);
 				else
-					load_lines<false>(it, hi_cur, hi_next, reinterpret_cast<char *>(H_FIRST ? in : ring),
+					load_lines<false>(it, hi_prev, hi, reinterpret_cast<char *>(H_FIRST ? in : ring),
 					                  H_FIRST ? imask : rmask, L.pitch);
-				load_coef<VS, kGroup>(it, n0, n1, smem + L.vcoef_off + ((k + 1) & 1) * (L.vbase_off - L.vcoef_off) / 2);
+				load_coef<VS, kGroup>(it, g0, g1, smem + L.vcoef_off);
+				cp_async_commit();
 			}
-			cp_async_commit();
-			cp_async_wait<1>();
-			if (U16)
-				convert_lines(it, lo_cur, hi_cur, stage, smask, H_FIRST ? in : ring, H_FIRST ? imask : rmask, L.pitch);
-			__syncthreads();
+			__syncthreads();  // lines stored by plain loads (unaligned u16) are visible to every converter
+			int lo_cur = hi_prev;
+			int hi_cur = step_end<VS>(it, smem, L, min(it.g_end, it.g_begin + it.step_groups));
 
-			const float *coef = reinterpret_cast<const float *>(smem + L.vcoef_off + (k & 1) * (L.vbase_off - L.vcoef_off) / 2);
-			if (H_FIRST) {
-				// new source lines -> intermediate ring
-				h_pass<U16, false, HW>(it, smem, L, in, imask, lo_cur, hi_cur, ring, rmask, 0);
+			for (int k = 0; k < nsteps; ++k) {
+				int g0, g1;
+				step_groups_of(k, &g0, &g1);
+				// prefetch step k+1
+				int hi_next = hi_cur;
+				if (k + 1 < nsteps) {
+					int n0, n1;
+					step_groups_of(k + 1, &n0, &n1);
+					hi_next = step_end<VS>(it, smem, L, n1);
+					if (U16)
+						load_lines<true>(it, hi_cur, hi_next, stage, smask, L.pitch);
+					else
+						load_lines<false>(it, hi_cur, hi_next, reinterpret_cast<char *>(H_FIRST ? in : ring),
+						                  H_FIRST ? imask : rmask, L.pitch);
+					load_coef<VS, kGroup>(it, n0, n1, smem + L.vcoef_off + ((k + 1) & 1) * (L.vbase_off - L.vcoef_off) / 2);
+				}
+				cp_async_commit();
+				cp_async_wait<1>();
+				if (U16)
+					convert_lines(it, lo_cur, hi_cur, stage, smask, H_FIRST ? in : ring, H_FIRST ? imask : rmask, L.pitch);
 				__syncthreads();
-				v_pass<U16, true, VS, kGroup>(it, smem, L, ring, rmask, kStripW, g0, g1, coef, kStripW / 4, nullptr, 0);
-			} else {
-				v_pass<U16, false, VS, kGroup>(it, smem, L, ring, rmask, L.pitch, g0, g1, coef, it.pxa / 4, I, L.pitch);
-				__syncthreads();
-				h_pass<U16, true, HW>(it, smem, L, I, 0x7fffffff, 0, (g1 - g0) * kGroup, nullptr, 0, g0 * kGroup);
+
+				const float *coef = reinterpret_cast<const float *>(smem + L.vcoef_off + (k & 1) * (L.vbase_off - L.vcoef_off) / 2);
+				if (H_FIRST) {
+					// new source lines -> intermediate ring
+					h_pass<U16, false, HW>(it, smem, L, in, imask, lo_cur, hi_cur, ring, rmask, 0);
+					__syncthreads();
+					v_pass<U16, true, VS, kGroup>(it, smem, L, ring, rmask, kStripW, g0, g1, coef, kStripW / 4, nullptr, 0);
+				} else {
+					v_pass<U16, false, VS, kGroup>(it, smem, L, ring, rmask, L.pitch, g0, g1, coef, it.pxa / 4, I, L.pitch);
+					__syncthreads();
+					h_pass<U16, true, HW>(it, smem, L, I, 0x7fffffff, 0, (g1 - g0) * kGroup, nullptr, 0, g0 * kGroup);
+				}
+				lo_cur = hi_cur;
+				hi_cur = hi_next;
 			}
-			lo_cur = hi_cur;
-			hi_cur = hi_next;
+			cp_async_wait<0>();
+			__syncthreads();  // the next item reuses every buffer
 		}
-		cp_async_wait<0>();
-		__syncthreads();  // the next item reuses every buffer
 	}
+	if (C.sched)
+		chunks_finish(C);
 }
 
 } // namespace fused_detail
