@@ -339,6 +339,53 @@ def test_batch_matches_single(cuda, oracle):
             np.testing.assert_array_equal(to_host(d, np.uint16), w, err_msg=mode)
 
 
+def test_batch_work_chunks_repeat(cuda, oracle):
+    """Launches whose CTAs take guided chunks of work from a counter (the
+    one-launch mixed batch, the CUDA-core streaming batch) leave the counter
+    zero for the next launch: every repetition, plain or replayed from a
+    graph, writes every output in full and bit-exact."""
+    import torch
+    import zimg_gb300 as zg
+    rng = np.random.default_rng(11)
+    # mixed u16 batch in one launch: 2.25x and 1.5x upscales, a 2x downscale
+    # and identity planes of one output size (a YUV batch's luma planes)
+    u16_shapes = [(240, 320), (360, 640), (1080, 1920), (540, 960), (360, 640), (240, 320), (1080, 1920)]
+    convs, srcs, dsts, wants = [], [], [], []
+    for sh, sw in u16_shapes:
+        src = make_u16(rng, sh, sw, 10)
+        convs.append(zg.ResizeConversion(sw, sh, "word").set_depth(10).set_filter("spline36")
+                     .set_dst_width(960).set_dst_height(540))
+        srcs.append(to_dev(src))
+        dsts.append(empty(540, 960, np.uint16))
+        wants.append(oracle.resize_plane(src, 960, 540, "spline36", depth=10))
+    mixed = zg.Batch(convs)
+    mixed.set_io(srcs, dsts)
+    assert mixed.launch_count == 1
+    # f32 batch on the CUDA-core streaming kernel
+    f_convs, f_srcs, f_dsts, f_wants = [], [], [], []
+    for k in range(6):
+        src = rng.random((270 + 6 * k, 480), dtype=np.float32)
+        f_convs.append(zg.ResizeConversion(480, 270 + 6 * k, "float").set_filter("bicubic", 0.0, 0.5)
+                       .set_dst_width(320).set_dst_height(180).set_engine("cuda"))
+        f_srcs.append(to_dev(src))
+        f_dsts.append(empty(180, 320, np.float32))
+        f_wants.append(oracle.resize_plane(src, 320, 180, "bicubic", 0.0, 0.5, mode="fma"))
+    stream_batch = zg.Batch(f_convs)
+    stream_batch.set_io(f_srcs, f_dsts)
+    for rep in range(3):
+        for mode in ("plain", "graph"):
+            for d in dsts + f_dsts:
+                d.fill_(-1)
+            for b in (mixed, stream_batch):
+                (b.process if mode == "plain" else b.process_graph)()
+            torch.cuda.synchronize()
+            for i, (d, w) in enumerate(zip(dsts, wants)):
+                np.testing.assert_array_equal(to_host(d, np.uint16), w, err_msg=(rep, mode, "u16", i))
+            for i, (d, w) in enumerate(zip(f_dsts, f_wants)):
+                np.testing.assert_array_equal(to_host(d, np.float32).view(np.uint32), w.view(np.uint32),
+                                              err_msg=(rep, mode, "f32", i))
+
+
 def test_batch_identity_planes_copied(cuda):
     """Identity conversions in a batch (no pass, resize.cpp:43-47) are copied
     in the same persistent launch as the chained conversion next to them:
