@@ -143,6 +143,22 @@ def test_tensor_core_u16_bitexact(cuda, oracle, depth, shape):
         np.testing.assert_array_equal(got, want, err_msg=str((shape, kind, depth)))
 
 
+@pytest.mark.parametrize("depth,shape", [(12, (1080, 1920, 2160, 3840)), (16, (1080, 1920, 2160, 3840)),
+                                         (12, (2160, 3840, 1080, 1920))])
+def test_deep_u16_fused_int32_bitexact(cuda, oracle, depth, shape):
+    """u16 planes deeper than the float-exactness proof allows (12-bit HDR,
+    16-bit) run the fused CUDA-core kernel in zimg's int32 arithmetic
+    (resize_impl.cpp:31-59), bit-exact against zimg's C path at full size,
+    H first (upscale) and V first (downscale)."""
+    sh, sw, dh, dw = shape
+    rng = np.random.default_rng(depth * 7 + sw)
+    src = make_u16(rng, sh, sw, depth)
+    got, r = run_conversion(src, dw, dh, "lanczos", 3, depth=depth)
+    assert r.info["engine"] == "cuda", r.info
+    want = oracle.resize_plane(src, dw, dh, "lanczos", 3, depth=depth, mode="c", nthreads=16)
+    np.testing.assert_array_equal(got, want, err_msg=str((depth, shape)))
+
+
 def _f32_check(oracle, src, got, dst_w, dst_h, kind, a=math.nan, b=math.nan, exact=True, **kw):
     fma = oracle.resize_plane(src, dst_w, dst_h, kind, a, b, mode="fma", nthreads=16, **kw)
     if exact:

@@ -8,7 +8,7 @@
 
 namespace zg {
 
-// per-(H_FIRST, U16) instantiation units (fused_inst_*.cu)
+// per-(H_FIRST, kind) instantiation units (fused_inst_*.cu)
 cudaError_t launch_fused_v_f32(int, int, const FusedJob *, int, int, const SmemLayout &, int, const FusedJob &,
                                const WorkChunks &, cudaStream_t);
 cudaError_t launch_fused_v_u16(int, int, const FusedJob *, int, int, const SmemLayout &, int, const FusedJob &,
@@ -21,6 +21,12 @@ const void *fused_kernel_ptr_v_f32(int hw, int vs);
 const void *fused_kernel_ptr_v_u16(int hw, int vs);
 const void *fused_kernel_ptr_h_f32(int hw, int vs);
 const void *fused_kernel_ptr_h_u16(int hw, int vs);
+cudaError_t launch_fused_v_i16(int, int, const FusedJob *, int, int, const SmemLayout &, int, const FusedJob &,
+                               const WorkChunks &, cudaStream_t);
+cudaError_t launch_fused_h_i16(int, int, const FusedJob *, int, int, const SmemLayout &, int, const FusedJob &,
+                               const WorkChunks &, cudaStream_t);
+const void *fused_kernel_ptr_v_i16(int hw, int vs);
+const void *fused_kernel_ptr_h_i16(int hw, int vs);
 
 namespace {
 
@@ -63,9 +69,30 @@ bool u16_exact_in_float(const FilterTable &t, unsigned depth)
 	return true;
 }
 
-float tap_value(const FilterTable &t, bool u16, unsigned i, unsigned k)
+// zimg's int32 sums cannot overflow: sum |tap| * 2^15 + 8192 < 2^31 per row.
+bool u16_fits_int32(const FilterTable &t)
+{
+	for (unsigned i = 0; i < t.rows; ++i) {
+		long long mag = 8192;
+		for (unsigned k = 0; k < t.width; ++k)
+			mag += static_cast<long long>(std::abs(static_cast<int>(t.i16[static_cast<size_t>(i) * t.width + k]))) << 15;
+		if (mag >= (1LL << 31))
+			return false;
+	}
+	return true;
+}
+
+// A tap as the kernel reads it: the f32 tap, the int16 tap as a float, or
+// (integer arithmetic) the int16 tap as int32 bits.
+float tap_value(const FilterTable &t, bool u16, bool integer, unsigned i, unsigned k)
 {
 	const size_t at = static_cast<size_t>(i) * t.width + k;
+	if (integer) {
+		const int32_t v = t.i16[at];
+		float f;
+		std::memcpy(&f, &v, sizeof(f));
+		return f;
+	}
 	return u16 ? static_cast<float>(t.i16[at]) : t.f32[at];
 }
 
@@ -79,7 +106,9 @@ bool plan_fused(const FilterTable &first, const FilterTable &second, bool h_firs
 	const FilterTable &V = h_first ? second : first;
 	if (H.rows != dst_w || V.rows != dst_h || H.input_width != src_w || V.input_width != src_h)
 		return false;
-	if (u16 && (!u16_exact_in_float(H, depth) || !u16_exact_in_float(V, depth)))
+	// u16: exact float arithmetic where the planner can prove it, else zimg's int32
+	const bool integer = u16 && (!u16_exact_in_float(H, depth) || !u16_exact_in_float(V, depth));
+	if (integer && (!u16_fits_int32(H) || !u16_fits_int32(V)))
 		return false;
 
 	const int hw_i = bucket_index(kHwBuckets, 3, static_cast<int>(H.width));
@@ -160,7 +189,7 @@ bool plan_fused(const FilterTable &first, const FilterTable &second, bool h_firs
 		auto pow2 = [](int x) { int r = 1; while (r < x) r <<= 1; return r; };
 		FusedJob &J = p.job;
 		J.h_first = h_first ? 1 : 0;
-		J.kind = static_cast<int>(u16 ? FusedKind::U16_EXACT : FusedKind::F32);
+		J.kind = static_cast<int>(integer ? FusedKind::U16_INT : (u16 ? FusedKind::U16_EXACT : FusedKind::F32));
 		J.hw = HW;
 		J.vs = VS;
 		J.step_groups = step_groups;
@@ -192,7 +221,7 @@ bool plan_fused(const FilterTable &first, const FilterTable &second, bool h_firs
 	int *h_left = reinterpret_cast<int *>(p.blob.data() + p.off_h_left);
 	for (unsigned c = 0; c < dst_w; ++c) {
 		for (unsigned k = 0; k < H.width; ++k)
-			h_taps[static_cast<size_t>(c) * HW + k] = tap_value(H, u16, c, k);
+			h_taps[static_cast<size_t>(c) * HW + k] = tap_value(H, u16, integer, c, k);
 		h_left[c] = static_cast<int>(H.left[c]);
 	}
 	float *v_dense = reinterpret_cast<float *>(p.blob.data() + p.off_v_dense);
@@ -205,7 +234,7 @@ bool plan_fused(const FilterTable &first, const FilterTable &second, bool h_firs
 				break;
 			const int d = static_cast<int>(V.left[i]) - gbase[g];
 			for (unsigned k = 0; k < V.width; ++k)
-				v_dense[(static_cast<size_t>(g) * VS + d + k) * kGroup + j] = tap_value(V, u16, i, k);
+				v_dense[(static_cast<size_t>(g) * VS + d + k) * kGroup + j] = tap_value(V, u16, integer, i, k);
 		}
 	}
 	std::memcpy(p.blob.data() + p.off_win_col, win_col.data(), win_col.size() * sizeof(int));
@@ -217,11 +246,12 @@ bool plan_fused(const FilterTable &first, const FilterTable &second, bool h_firs
 	J.dst_h = static_cast<int>(dst_h);
 	J.strips = strips;
 	J.strip_w = kStripW;
-	const float offset = u16 ? static_cast<float>(std::ldexp(1.0, static_cast<int>(depth) - 1)) : 0.0f;
+	// centring offset: 2^(depth-1) for exact float sums, zimg's 32768 for int32 ones
+	const float offset = integer ? 32768.0f : (u16 ? static_cast<float>(std::ldexp(1.0, static_cast<int>(depth) - 1)) : 0.0f);
 	J.offset = offset;
 	J.magic = 12582912.0f + offset;
 	J.pixel_max = u16 ? static_cast<float>((1UL << depth) - 1) : 0.0f;
-	p.variant = ((J.h_first * 2 + (u16 ? 1 : 0)) * 3 + hw_i) * 4 + vs_i;
+	p.variant = ((J.h_first * 3 + (integer ? 2 : (u16 ? 1 : 0))) * 3 + hw_i) * 4 + vs_i;
 	return true;
 }
 
@@ -273,12 +303,13 @@ void fused_bind(FusedPlan &p, const void *device_blob)
 
 namespace {
 
-void split_variant(int variant, int *hf, int *u16, int *hw_i, int *vs_i)
+// kind: 0 f32, 1 u16 in exact float sums, 2 u16 in int32 sums
+void split_variant(int variant, int *hf, int *kind, int *hw_i, int *vs_i)
 {
 	*vs_i = variant % 4;
 	*hw_i = (variant / 4) % 3;
-	*u16 = (variant / 12) % 2;
-	*hf = (variant / 24) % 2;
+	*kind = (variant / 12) % 3;
+	*hf = (variant / 36) % 2;
 }
 
 const void *kernel_ptr(int variant)
@@ -287,11 +318,13 @@ const void *kernel_ptr(int variant)
 		return chain_kernel_ptr(variant);
 	if (variant >= 100)
 		return mma_kernel_ptr(variant);
-	int hf, u16, hw, vs;
-	split_variant(variant, &hf, &u16, &hw, &vs);
+	int hf, kind, hw, vs;
+	split_variant(variant, &hf, &kind, &hw, &vs);
 	if (hf)
-		return u16 ? fused_kernel_ptr_h_u16(hw, vs) : fused_kernel_ptr_h_f32(hw, vs);
-	return u16 ? fused_kernel_ptr_v_u16(hw, vs) : fused_kernel_ptr_v_f32(hw, vs);
+		return kind == 2 ? fused_kernel_ptr_h_i16(hw, vs)
+		                 : (kind == 1 ? fused_kernel_ptr_h_u16(hw, vs) : fused_kernel_ptr_h_f32(hw, vs));
+	return kind == 2 ? fused_kernel_ptr_v_i16(hw, vs)
+	                 : (kind == 1 ? fused_kernel_ptr_v_u16(hw, vs) : fused_kernel_ptr_v_f32(hw, vs));
 }
 
 } // namespace
@@ -314,7 +347,7 @@ SmemLayout fused_layout(const FusedPlan *const *plans, int n)
 		stage = std::max(stage, p.stage_rows);
 		seg_groups = std::max(seg_groups, std::min(p.job.groups, kItemGroupsMax));
 		step_groups = std::max(step_groups, p.job.step_groups);
-		u16 = p.job.kind == static_cast<int>(FusedKind::U16_EXACT);
+		u16 = p.job.kind != static_cast<int>(FusedKind::F32);
 		h_first = p.job.h_first != 0;
 	}
 	auto a16 = [](size_t x) { return static_cast<int>((x + 15) / 16 * 16); };
@@ -376,17 +409,19 @@ cudaError_t launch_fused(int variant, const FusedJob *jobs, int num_jobs, int to
 		return launch_chain(variant, jobs, num_jobs, total_tiles, smem_bytes, grid, single, stream);
 	if (variant >= 100)
 		return launch_mma(variant, jobs, num_jobs, total_tiles, smem_bytes, grid, single, stream);
-	int hf, u16, hw, vs;
-	split_variant(variant, &hf, &u16, &hw, &vs);
+	int hf, kind, hw, vs;
+	split_variant(variant, &hf, &kind, &hw, &vs);
 	grid = std::max(1, std::min(grid, total_tiles));
 	if (smem_bytes.total_bytes > static_cast<int>(kSmemMax))
 		return cudaErrorInvalidValue;
 	const WorkChunks &c = chunks;
 	if (hf)
-		return u16 ? launch_fused_h_u16(hw, vs, jobs, num_jobs, total_tiles, smem_bytes, grid, single, c, stream)
-		           : launch_fused_h_f32(hw, vs, jobs, num_jobs, total_tiles, smem_bytes, grid, single, c, stream);
-	return u16 ? launch_fused_v_u16(hw, vs, jobs, num_jobs, total_tiles, smem_bytes, grid, single, c, stream)
-	           : launch_fused_v_f32(hw, vs, jobs, num_jobs, total_tiles, smem_bytes, grid, single, c, stream);
+		return kind == 2 ? launch_fused_h_i16(hw, vs, jobs, num_jobs, total_tiles, smem_bytes, grid, single, c, stream)
+		     : kind == 1 ? launch_fused_h_u16(hw, vs, jobs, num_jobs, total_tiles, smem_bytes, grid, single, c, stream)
+		                 : launch_fused_h_f32(hw, vs, jobs, num_jobs, total_tiles, smem_bytes, grid, single, c, stream);
+	return kind == 2 ? launch_fused_v_i16(hw, vs, jobs, num_jobs, total_tiles, smem_bytes, grid, single, c, stream)
+	     : kind == 1 ? launch_fused_v_u16(hw, vs, jobs, num_jobs, total_tiles, smem_bytes, grid, single, c, stream)
+	                 : launch_fused_v_f32(hw, vs, jobs, num_jobs, total_tiles, smem_bytes, grid, single, c, stream);
 }
 
 void fused_set_io(FusedJob &j, const void *src, ptrdiff_t src_stride, void *dst, ptrdiff_t dst_stride)

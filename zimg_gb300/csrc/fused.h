@@ -23,7 +23,12 @@ namespace zg {
 //              planner has proved that every partial sum stays below 2^24, so
 //              each multiply-add is exact and the result equals zimg's int32
 //              arithmetic bit for bit (resize_impl.cpp:31-59,78-95).
-enum class FusedKind : int { F32 = 0, U16_EXACT = 1 };
+//   U16_INT:   u16 samples where that proof fails (deeper samples: 12-bit,
+//              16-bit): zimg's own int32 arithmetic, samples centred by 32768
+//              (unpack_pixel_u16), 8192 + sum(tap * sample) in int32, then
+//              (sum >> 14) + 32768 clamped to the depth (pack_pixel_u16);
+//              planned where |taps| * 2^15 + 8192 stays below 2^31.
+enum class FusedKind : int { F32 = 0, U16_EXACT = 1, U16_INT = 2 };
 
 // Vertical taps come in groups of group_rows() output rows laid out densely over a
 // window of VS input lines (VS = 8, 12, 16 or 24); horizontal taps per output

@@ -1,4 +1,4 @@
-// One (H_FIRST, U16) instantiation unit of the fused streaming kernel:
+// One (H_FIRST, U16, INT) instantiation unit of the fused streaming kernel:
 // kernel pointers per (HW, VS) bucket and the launcher. Each fused_inst_*.cu
 // expands ZG_FUSED_INSTANCE once; the units are separate to compile in
 // parallel.
@@ -8,13 +8,13 @@
 
 #include <algorithm>
 
-#define ZG_FUSED_INSTANCE(NAME, HF, U16)                                                                           \
+#define ZG_FUSED_INSTANCE(NAME, HF, U16, INT)                                                                      \
 	namespace zg {                                                                                                 \
 	namespace {                                                                                                    \
 	template <int HW, int VS>                                                                                      \
 	const void *ptr_##NAME()                                                                                       \
 	{                                                                                                              \
-		return reinterpret_cast<const void *>(&fused_detail::fused_kernel<HF, U16, HW, VS>);                       \
+		return reinterpret_cast<const void *>(&fused_detail::fused_kernel<HF, U16, HW, VS, INT>);                  \
 	}                                                                                                              \
 	template <int HW>                                                                                              \
 	const void *ptr_vs_##NAME(int vs)                                                                              \

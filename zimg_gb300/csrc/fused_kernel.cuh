@@ -58,6 +58,13 @@ __device__ __forceinline__ float u16_round(float acc, float magic, float pixel_m
 	return fminf(fmaxf(y, 12582912.0f), 12582912.0f + pixel_max);
 }
 
+// zimg's int32 rounding (pack_pixel_u16, resize_impl.cpp:36-42): acc holds
+// 8192 + sum(tap * (v - 32768)); (acc >> 14) + 32768 clamped to [0, pixel_max].
+__device__ __forceinline__ int u16_round_int(int acc, int pixel_max)
+{
+	return min(max((acc >> 14) + 32768, 0), pixel_max);
+}
+
 __device__ __forceinline__ int find_job(const FusedJob *__restrict__ jobs, int num_jobs, int t)
 {
 	int lo = 0, hi = num_jobs - 1;
@@ -197,15 +204,18 @@ __device__ __forceinline__ void load_lines(const Item &it, int a, int b, char *r
 }
 
 // Convert the u16 lines this thread loaded with load_lines(a, b) from the
-// raw staging ring to centred floats in `ring`.
+// raw staging ring to centred floats in `ring` (INT: v - 32768 as int32 bits).
+template <bool INT>
 __device__ __forceinline__ void convert_chunk(const char *srow, float *drow, int q, float bias)
 {
 	const uint4 u = *reinterpret_cast<const uint4 *>(srow + q * 16);
 	const uint32_t w[4] = { u.x, u.y, u.z, u.w };
 	float f[8];
 #pragma unroll
-	for (int k = 0; k < 8; ++k)
-		f[k] = __int_as_float(0x4B000000 | ((w[k >> 1] >> (16 * (k & 1))) & 0xFFFFu)) - bias;
+	for (int k = 0; k < 8; ++k) {
+		const uint32_t v = (w[k >> 1] >> (16 * (k & 1))) & 0xFFFFu;
+		f[k] = INT ? __int_as_float(static_cast<int>(v) - 32768) : __int_as_float(0x4B000000 | v) - bias;
+	}
 	*reinterpret_cast<float4 *>(drow + q * 8) = make_float4(f[0], f[1], f[2], f[3]);
 	*reinterpret_cast<float4 *>(drow + q * 8 + 4) = make_float4(f[4], f[5], f[6], f[7]);
 }
@@ -214,6 +224,7 @@ __device__ __forceinline__ void convert_chunk(const char *srow, float *drow, int
 // in `ring`. With cp.async copies each thread converts exactly the chunks it
 // copied (the mapping of load_lines); plain loads were made visible by a
 // CTA barrier, so any mapping serves.
+template <bool INT>
 __device__ __forceinline__ void convert_lines(const Item &it, int a, int b, const char *stage, int smask,
                                               float *ring, int rmask, int pitch)
 {
@@ -226,14 +237,14 @@ __device__ __forceinline__ void convert_lines(const Item &it, int a, int b, cons
 		if (l0 >= lpp)
 			return;
 		for (int y = a + l0; y < b; y += lpp)
-			convert_chunk(stage + (y & smask) * pitch * 2, ring + (y & rmask) * pitch, q, bias);
+			convert_chunk<INT>(stage + (y & smask) * pitch * 2, ring + (y & rmask) * pitch, q, bias);
 		return;
 	}
 	for (int y = a + warp; y < b; y += kWarps) {
 		const char *srow = stage + (y & smask) * pitch * 2;
 		float *drow = ring + (y & rmask) * pitch;
 		for (int q = lane; q < chunks; q += 32)
-			convert_chunk(srow, drow, q, bias);
+			convert_chunk<INT>(srow, drow, q, bias);
 	}
 }
 
@@ -241,7 +252,7 @@ __device__ __forceinline__ void convert_lines(const Item &it, int a, int b, cons
 // Thread = output column; two lines per iteration for independent chains.
 // FINAL: write destination rows (row index = r0 + (y - a)); else write ring
 // slots (y & omask) of `out`.
-template <bool U16, bool FINAL, int HW>
+template <bool U16, bool FINAL, int HW, bool INT = false>
 __device__ __forceinline__ void h_pass(const Item &it, const char *smem, const SmemLayout &L, const float *in,
                                        int imask, int a, int b, float *out, int omask, int r0)
 {
@@ -258,6 +269,36 @@ __device__ __forceinline__ void h_pass(const Item &it, const char *smem, const S
 	const int l = col_ok ? reinterpret_cast<const int *>(smem + L.hleft_off)[c] - it.xlo : 0;
 	const float init = U16 ? 8192.0f : 0.0f;
 	const int pitch = L.pitch;
+	if constexpr (INT) {
+		// zimg's int32 sums (taps and centred samples as int32 bits)
+		const int pmax = static_cast<int>(it.pixel_max);
+		for (int y = a; y < b; y += 2) {
+			const bool two = y + 1 < b;
+			const float *r0p = in + (y & imask) * pitch + l;
+			const float *r1p = in + ((y + 1) & imask) * pitch + l;
+			int acc0 = 8192, acc1 = 8192;
+#pragma unroll
+			for (int k = 0; k < HW; ++k) {
+				const int t = __float_as_int(taps[k]);
+				acc0 += t * __float_as_int(r0p[k]);
+				acc1 += t * __float_as_int(r1p[k]);
+			}
+			const int q0 = u16_round_int(acc0, pmax), q1 = u16_round_int(acc1, pmax);
+			if (!FINAL) {
+				out[(y & omask) * kStripW + c] = __int_as_float(q0 - 32768);
+				if (two)
+					out[((y + 1) & omask) * kStripW + c] = __int_as_float(q1 - 32768);
+			} else if (col_ok) {
+				const int oy = r0 + (y - a);
+				char *d0 = it.dst + static_cast<ptrdiff_t>(oy) * it.dst_stride;
+				if (oy < it.dst_h)
+					reinterpret_cast<uint16_t *>(d0)[it.c0 + c] = static_cast<uint16_t>(q0);
+				if (two && oy + 1 < it.dst_h)
+					reinterpret_cast<uint16_t *>(d0 + it.dst_stride)[it.c0 + c] = static_cast<uint16_t>(q1);
+			}
+		}
+		return;
+	}
 	for (int y = a; y < b; y += 2) {
 		const bool two = y + 1 < b;
 		const float *r0p = in + (y & imask) * pitch + l;
@@ -301,7 +342,7 @@ __device__ __forceinline__ void h_pass(const Item &it, const char *smem, const S
 // Vertical pass for groups [g0, g1): out line (g - g0)*4 + j, columns 4q..4q+3:
 //   sum_s dense[g][s][j] * in[(base[g] + s) & imask][4q + e]
 // FINAL: destination rows g*4 + j (columns c0 + 4q ...); else lines of I.
-template <bool U16, bool FINAL, int VS, int kGroup>
+template <bool U16, bool FINAL, int VS, int kGroup, bool INT = false>
 __device__ __forceinline__ void v_pass(const Item &it, const char *smem, const SmemLayout &L, const float *in,
                                        int imask, int in_pitch, int g0, int g1, const float *coef, int quads,
                                        float *I, int i_pitch)
@@ -320,6 +361,54 @@ __device__ __forceinline__ void v_pass(const Item &it, const char *smem, const S
 		for (int s = 0; s < VS; ++s)
 			off[s] = ((base + s) & imask) * in_pitch;
 		for (int q = (warp % wpg) * 32 + lane; q < quads; q += wpg * 32) {
+			if constexpr (INT) {
+				// zimg's int32 sums (taps and centred samples as int32 bits)
+				int acc[kGroup][4];
+#pragma unroll
+				for (int j = 0; j < kGroup; ++j)
+					acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 8192;
+#pragma unroll
+				for (int s = 0; s < VS; ++s) {
+					const int4 x = *reinterpret_cast<const int4 *>(in + off[s] + 4 * q);
+#pragma unroll
+					for (int j = 0; j < kGroup; ++j) {
+						const int cj = __float_as_int(cf[s * kGroup + j]);
+						acc[j][0] += cj * x.x;
+						acc[j][1] += cj * x.y;
+						acc[j][2] += cj * x.z;
+						acc[j][3] += cj * x.w;
+					}
+				}
+				const int pmax = static_cast<int>(it.pixel_max);
+#pragma unroll
+				for (int j = 0; j < kGroup; ++j) {
+					int u[4];
+#pragma unroll
+					for (int e = 0; e < 4; ++e)
+						u[e] = u16_round_int(acc[j][e], pmax);
+					if (!FINAL) {
+						*reinterpret_cast<int4 *>(I + (gi * kGroup + j) * i_pitch + 4 * q) =
+							make_int4(u[0] - 32768, u[1] - 32768, u[2] - 32768, u[3] - 32768);
+					} else {
+						const int r = g * kGroup + j;
+						if (r >= it.dst_h)
+							continue;
+						const int x0 = 4 * q;
+						uint16_t *d = reinterpret_cast<uint16_t *>(it.dst + static_cast<ptrdiff_t>(r) * it.dst_stride) +
+						              it.c0 + x0;
+						if (it.vec_ok && x0 + 3 < it.cols_valid) {
+							*reinterpret_cast<uint2 *>(d) = make_uint2(static_cast<uint32_t>(u[0]) | (static_cast<uint32_t>(u[1]) << 16),
+							                                           static_cast<uint32_t>(u[2]) | (static_cast<uint32_t>(u[3]) << 16));
+						} else {
+#pragma unroll
+							for (int e = 0; e < 4; ++e)
+								if (x0 + e < it.cols_valid)
+									d[e] = static_cast<uint16_t>(u[e]);
+						}
+					}
+				}
+				continue;
+			}
 			// columns (0, 1) and (2, 3) of each row in paired FMAs: two
 			// independent round-to-nearest FMAs per instruction, the same
 			// results as four scalar ones
@@ -425,7 +514,7 @@ __device__ __forceinline__ void load_coef(const Item &it, int g0, int g1, char *
 		cp_async16(dst + i * 16, src + i * 16, 16);
 }
 
-template <bool H_FIRST, bool U16, int HW, int VS>
+template <bool H_FIRST, bool U16, int HW, int VS, bool INT = false>
 __global__ void __launch_bounds__(kThreads, H_FIRST ? 4 : 5)
 fused_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, const __grid_constant__ FusedJob single,
              const __grid_constant__ SmemLayout L, const __grid_constant__ WorkChunks C)
@@ -511,19 +600,19 @@ fused_kernel(const FusedJob *__restrict__ jobs, int num_jobs, int total_items, c
 				cp_async_commit();
 				cp_async_wait<1>();
 				if (U16)
-					convert_lines(it, lo_cur, hi_cur, stage, smask, H_FIRST ? in : ring, H_FIRST ? imask : rmask, L.pitch);
+					convert_lines<INT>(it, lo_cur, hi_cur, stage, smask, H_FIRST ? in : ring, H_FIRST ? imask : rmask, L.pitch);
 				__syncthreads();
 
 				const float *coef = reinterpret_cast<const float *>(smem + L.vcoef_off + (k & 1) * (L.vbase_off - L.vcoef_off) / 2);
 				if (H_FIRST) {
 					// new source lines -> intermediate ring
-					h_pass<U16, false, HW>(it, smem, L, in, imask, lo_cur, hi_cur, ring, rmask, 0);
+					h_pass<U16, false, HW, INT>(it, smem, L, in, imask, lo_cur, hi_cur, ring, rmask, 0);
 					__syncthreads();
-					v_pass<U16, true, VS, kGroup>(it, smem, L, ring, rmask, kStripW, g0, g1, coef, kStripW / 4, nullptr, 0);
+					v_pass<U16, true, VS, kGroup, INT>(it, smem, L, ring, rmask, kStripW, g0, g1, coef, kStripW / 4, nullptr, 0);
 				} else {
-					v_pass<U16, false, VS, kGroup>(it, smem, L, ring, rmask, L.pitch, g0, g1, coef, it.pxa / 4, I, L.pitch);
+					v_pass<U16, false, VS, kGroup, INT>(it, smem, L, ring, rmask, L.pitch, g0, g1, coef, it.pxa / 4, I, L.pitch);
 					__syncthreads();
-					h_pass<U16, true, HW>(it, smem, L, I, 0x7fffffff, 0, (g1 - g0) * kGroup, nullptr, 0, g0 * kGroup);
+					h_pass<U16, true, HW, INT>(it, smem, L, I, 0x7fffffff, 0, (g1 - g0) * kGroup, nullptr, 0, g0 * kGroup);
 				}
 				lo_cur = hi_cur;
 				hi_cur = hi_next;
