@@ -24,7 +24,7 @@ SOURCES = ["filter_plan.cpp", "capi.cu", "capi_graph.cu", "capi_batch.cu", "capi
            "pass_kernels.cu", "fused.cu", "fused_inst_v_f32.cu", "fused_inst_v_u16.cu", "fused_inst_h_f32.cu",
            "fused_inst_h_u16.cu", "fused_inst_v_i16.cu", "fused_inst_h_i16.cu", "mma.cu", "chain.cu", "chain_tma.cu", "wide_kernel.cu", "wide_umma.cu", "copy_kernel.cu",
            "depth_kernel.cu", "ed_kernel.cu", "alpha_kernel.cu", "capi_depth.cu", "colorspace_plan.cpp",
-           "colorspace_kernel.cu", "capi_colorspace.cu", "unresize_plan.cpp", "unresize_kernel.cu", "capi_unresize.cu"]
+           "colorspace_kernel.cu", "capi_colorspace.cu", "work_chunks.cpp", "unresize_plan.cpp", "unresize_kernel.cu", "capi_unresize.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include "filter_plan.h"
+#include "work_chunks.h"
 
 namespace zg {
 
@@ -215,16 +216,6 @@ int chain_mixed_copy_variant();
 int chain_mixed_grid_size(size_t smem_bytes);
 cudaError_t launch_chain_mixed(const FusedJob *jobs, int num_jobs, const WorkChunks &chunks, const SmemLayout &L,
                                int grid, cudaStream_t stream);
-// Guided chunk bounds: units [0, units) of jobs with item_begin[e] ..
-// item_begin[e] + items[e] - 1 (in order, contiguous) at an estimated cost
-// per unit cost[e]; each chunk takes 1 / (2 grid) of the cost still left, but
-// at least min_units units (or the rest), and a chunk that ends inside a job
-// with strip_units[e] > 0 units per strip ends on the nearest strip boundary
-// instead where that changes it by at most a quarter (a chunk that splits a
-// strip makes its tail a second item, which starts its pipeline again).
-std::vector<int> chain_mixed_chunks(const std::vector<int> &item_begin, const std::vector<int> &items,
-                                    const std::vector<double> &cost, const std::vector<int> &strip_units, int grid,
-                                    int min_units);
 // Test hook: CTA 0's producer skips group drop_group (-1: none) without
 // arming its stage; waits give up after wait_ns (0: the default 0.25 s).
 int chain_tma_set_fault(int drop_group, unsigned long long wait_ns);
