@@ -12,8 +12,11 @@
 //   H-first step:  new source lines --H--> ring (intermediate lines)
 //                  ring --V--> destination rows
 //
-// u16 samples are staged raw and converted once to exact centred floats. The
-// grid is persistent: CTA b takes items b, b + gridDim.x, ...
+// u16 samples are staged raw and converted once to exact centred floats, or
+// (INT, depths the float proof cannot cover) to centred int32 values held as
+// float bits, summed in zimg's int32 arithmetic. The grid is persistent: in a
+// batch CTAs take guided chunks of the units (work_chunks.cuh), otherwise an
+// equal contiguous share each.
 #pragma once
 
 #include "fused.h"
